@@ -1,0 +1,137 @@
+/* Finite-difference stencils of the sledgehamr plugin surface:
+ * sledgehamr::utils::Laplacian<order> and sledgehamr::utils::Gradient<order>
+ * for order 0..3, plus the constexpr_for helper that project code uses.
+ *
+ * Reference: source/utils/sledgehamr_utils.h:11-17 (constexpr_for),
+ *            :50-94 (Laplacian<0..3>), :106-188 (Gradient<0..3>).
+ *
+ * The coefficients are those of the standard central difference formulas:
+ *   order 1 (2nd-order accurate, 7 points):  (S1 - 6 c) / dx^2
+ *   order 2 (4th-order, 13 points):  (-S2 + 16 S1 - 90 c) / (12 dx^2)
+ *   order 3 (6th-order, 19 points):  (2 S3 - 27 S2 + 270 S1 - 1470 c) / (180 dx^2)
+ * where Sr is the sum of the six neighbours at distance r along the axes,
+ * accumulated in the order +x, -x, +y, -y, +z, -z.  The division by the
+ * denominator is done as a multiplication by its reciprocal: that
+ * reciprocal is loop invariant and is hoisted out of cell loops, which
+ * matters on GB300 where an FP64 division costs about as much as ten FP64
+ * fused multiply-adds.  The result differs from a true division by at most
+ * one rounding.
+ */
+#ifndef SLEDGEHAMR_SLEDGEHAMR_UTILS_H_
+#define SLEDGEHAMR_SLEDGEHAMR_UTILS_H_
+
+#include <type_traits>
+#include <utility>
+
+#include "sh_amrex.h"
+
+namespace sledgehamr {
+namespace utils {
+
+/* Compile-time loop: calls f(std::integral_constant<..., i>) for
+ * i = Start, Start+Inc, ... < End. */
+template <auto Start, auto End, auto Inc, class F>
+AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE constexpr void constexpr_for(F &&f) {
+    if constexpr (Start < End) {
+        f(std::integral_constant<decltype(Start), Start>());
+        constexpr_for<Start + Inc, End, Inc>(f);
+    }
+}
+
+namespace detail {
+
+/* Sum of the six axis neighbours of (i,j,k) at distance r. */
+template <class A4>
+AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE double
+axis_ring_sum(const A4 &s, int i, int j, int k, int c, int r) {
+    double acc = s(i + r, j, k, c);
+    acc += s(i - r, j, k, c);
+    acc += s(i, j + r, k, c);
+    acc += s(i, j - r, k, c);
+    acc += s(i, j, k + r, c);
+    acc += s(i, j, k - r, c);
+    return acc;
+}
+
+/* Weights of the Laplacian rings: r = 0 is the centre cell. */
+template <int Order>
+AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE constexpr double lap_ring(int r) {
+    if constexpr (Order == 1) {
+        return r == 0 ? -6. : 1.;
+    } else if constexpr (Order == 2) {
+        return r == 0 ? -90. : (r == 1 ? 16. : -1.);
+    } else {
+        return r == 0 ? -1470. : (r == 1 ? 270. : (r == 2 ? -27. : 2.));
+    }
+}
+template <int Order>
+AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE constexpr double lap_denom() {
+    return Order == 1 ? 1. : (Order == 2 ? 12. : 180.);
+}
+
+/* Offset of cell (i,j,k) by d along axis 'x', 'y' or 'z'. */
+template <class A4>
+AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE double
+along(const A4 &s, int i, int j, int k, int c, char axis, int d) {
+    return axis == 'x' ? s(i + d, j, k, c)
+                       : (axis == 'y' ? s(i, j + d, k, c) : s(i, j, k + d, c));
+}
+
+} // namespace detail
+
+template <int Order>
+AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE double
+Laplacian(amrex::Array4<amrex::Real const> const &state, const int i,
+          const int j, const int k, const int c, const double dx2) {
+    if constexpr (Order == 0) {
+        return 0.;
+    } else {
+        /* outermost ring first, centre last */
+        double acc = detail::lap_ring<Order>(Order) *
+                     detail::axis_ring_sum(state, i, j, k, c, Order);
+        constexpr_for<1, Order, 1>([&](auto q) {
+            constexpr int r = Order - q;
+            acc += detail::lap_ring<Order>(r) *
+                   detail::axis_ring_sum(state, i, j, k, c, r);
+        });
+        acc += detail::lap_ring<Order>(0) * state(i, j, k, c);
+        return acc * (1. / (detail::lap_denom<Order>() * dx2));
+    }
+}
+
+template <int Order>
+AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE double
+Gradient(amrex::Array4<amrex::Real const> const &state, const int i,
+         const int j, const int k, const int c, const double dx,
+         const char axis) {
+    using detail::along;
+    if constexpr (Order == 0) {
+        return 0.;
+    } else if constexpr (Order == 1) {
+        /* (f(+1) - f(-1)) / (2 dx) */
+        return (along(state, i, j, k, c, axis, 1) -
+                along(state, i, j, k, c, axis, -1)) *
+               (1. / (2. * dx));
+    } else if constexpr (Order == 2) {
+        /* (-f(+2) + 8 f(+1) + f(-2) - 8 f(-1)) / (12 dx) */
+        double acc = -along(state, i, j, k, c, axis, 2);
+        acc += 8. * along(state, i, j, k, c, axis, 1);
+        acc += along(state, i, j, k, c, axis, -2);
+        acc -= 8. * along(state, i, j, k, c, axis, -1);
+        return acc * (1. / (12. * dx));
+    } else {
+        /* (f(+3) - f(-3) - 9 f(+2) + 9 f(-2) + 45 f(+1) - 45 f(-1)) / (60 dx) */
+        double acc = along(state, i, j, k, c, axis, 3);
+        acc -= along(state, i, j, k, c, axis, -3);
+        acc -= 9. * along(state, i, j, k, c, axis, 2);
+        acc += 9. * along(state, i, j, k, c, axis, -2);
+        acc += 45. * along(state, i, j, k, c, axis, 1);
+        acc -= 45. * along(state, i, j, k, c, axis, -1);
+        return acc * (1. / (60. * dx));
+    }
+}
+
+} // namespace utils
+} // namespace sledgehamr
+
+#endif // SLEDGEHAMR_SLEDGEHAMR_UTILS_H_

@@ -1,0 +1,232 @@
+/* C ABI of libsledgehamr_gb300.so: sledgehamr's time-stepping hot path on one
+ * GB300 GPU.
+ *
+ * The library replaces, for a host driver written in C, C++ or Python
+ * (ctypes), the AMReX-backed operations that sledgehamr's TimeStepper calls on
+ * every step:
+ *   sh_level_advance ........ Integrator::Advance + IntegratorRkn/Lsssprk3/
+ *                             Leapfrog::Integrate
+ *                             (source/integrators/integrator.cpp:11-31,
+ *                              rkn.cpp:25-120, lsssprk3.cpp:14-31,
+ *                              leapfrog.cpp:13-57), including the project's
+ *                             FillRhs/FillAddRhs (source/macros.h:301-485)
+ *   sh_level_fill_patch ..... LevelSynchronizer::FillPatch for lev <= 0
+ *                             (source/level_synchronizer.cpp:94-144)
+ *   sh_level_rhs ............ Sledgehamr::FillRhs (macros.h:301-379)
+ *   sh_average_down ......... LevelSynchronizer::AverageDownTo and the
+ *                             average-down of CreateShadowLevel
+ *                             (level_synchronizer.cpp:219-233,
+ *                              sledgehamr.cpp:247-248)
+ *   sh_average_down_te ...... LevelSynchronizer::ComputeTruncationErrors
+ *                             (level_synchronizer.cpp:240-357, kernels.h:18-42)
+ *   sh_tag .................. Sledgehamr::ErrorEst / DoErrorEstCpu
+ *                             (sledgehamr.cpp:207-348, macros.h:489-686)
+ *   sh_gw_spectrum .......... GravitationalWaves::ComputeSpectrum
+ *                             (gravitational_waves.cpp:52-322)
+ *   sh_spectrum_bins,
+ *   sh_index_to_k ........... Sledgehamr::ReadSpectrumKs / ReadProj data
+ *                             (sledgehamr.cpp:554-615, generated as
+ *                              pySledgehamr/Sledgehamr.py:7-27)
+ *   sh_evolve_periodic ...... host-to-host convenience: upload, nsteps x
+ *                             Advance(0), download, for a periodic cubic level
+ *
+ * Projects (per-cell hooks) are compiled into the library; see
+ * sh_project_find.  Component order of a level: the project's fields, then
+ * its momenta (SLEDGEHAMR_ADD_SCALARS / ADD_CONJUGATE_MOMENTA), then, when
+ * gravitational waves are on, u_xx u_yy u_zz u_xy u_xz u_yz du_xx ... du_yz.
+ *
+ * Host array layouts:
+ *   canonical  - one array for a level covering its whole cubic periodic
+ *                domain of N^3 cells: a[((n*N + k)*N + j)*N + i]
+ *   boxes      - the valid cells of every box one after the other, each box
+ *                component-major, x fastest.
+ *
+ * Every function returns SH_OK (0) or a negative status; the message of the
+ * last failure is available from sh_ctx_last_error.  No function aborts the
+ * process.  Calls on one context are not thread-safe; different contexts
+ * are independent.  All work is issued on the context's stream; functions
+ * that take or return host arrays synchronise that stream before returning.
+ */
+#ifndef SLEDGEHAMR_GB300_H_
+#define SLEDGEHAMR_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define SH_API __attribute__((visibility("default")))
+#else
+#define SH_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SH_OK 0
+#define SH_ERR_ARG (-1)
+#define SH_ERR_PROJECT (-2)
+#define SH_ERR_CUDA (-3)
+#define SH_ERR_NOMEM (-4)
+#define SH_ERR_UNSUPPORTED (-5)
+#define SH_ERR_TIMEOUT (-6)
+#define SH_ERR_NONFINITE (-7)
+
+/* integrator.type (source/integrators/integrator.h:12-23).  The AMReX
+ * integrators 0-4 abort in the reference (amrex_integrators.cpp:19-20) and
+ * are rejected here with SH_ERR_UNSUPPORTED. */
+#define SH_INTEGRATOR_LSSSPRK3 10
+#define SH_INTEGRATOR_LEAPFROG 11
+#define SH_INTEGRATOR_RKN_TABLEAU 20
+#define SH_INTEGRATOR_RKN4 21
+#define SH_INTEGRATOR_RKN5 22
+
+/* sh_level_advance flags */
+#define SH_ADVANCE_NO_SWAP 1 /* shadow level: integrate old -> new in place
+                                of swapping first (integrator.cpp:12-15) */
+
+/* which time level of a sh_level */
+#define SH_NEW 0
+#define SH_OLD 1
+
+typedef struct sh_ctx sh_ctx;
+typedef struct sh_level sh_level;
+
+/* An index box, bounds inclusive, as amrex::Box. */
+typedef struct sh_box {
+    int lo[3];
+    int hi[3];
+} sh_box;
+
+/* ---- context -------------------------------------------------------------- */
+SH_API int sh_ctx_create(int device, sh_ctx **out);
+SH_API int sh_ctx_destroy(sh_ctx *ctx);
+SH_API const char *sh_ctx_last_error(const sh_ctx *ctx);
+/* Use an existing cudaStream_t (NULL: the context's own stream). */
+SH_API int sh_ctx_set_stream(sh_ctx *ctx, void *cuda_stream);
+SH_API void *sh_ctx_stream(sh_ctx *ctx);
+SH_API int sh_ctx_synchronize(sh_ctx *ctx);
+/* Number of kernels this context has launched so far. */
+SH_API long long sh_ctx_kernel_launches(const sh_ctx *ctx);
+/* Per-kernel timing with CUDA events recorded on the context stream around
+ * every launch while enabled (the categories of sledgehamr's
+ * PerformanceMonitor: "rhs" (stage kernels), "fill_patch", "average_down",
+ * "tagging", "gw_spectrum", "data_move").  sh_ctx_profile(ctx, 1) clears
+ * and starts, (ctx, 0) stops; sh_ctx_profile_read synchronises the stream
+ * and returns the summed device time and the launch count of a category. */
+SH_API int sh_ctx_profile(sh_ctx *ctx, int enable);
+SH_API int sh_ctx_profile_read(sh_ctx *ctx, const char *category, double *total_ms,
+                               long long *launches);
+
+/* ---- projects ------------------------------------------------------------- */
+SH_API int sh_project_count(void);
+SH_API const char *sh_project_name(int id);
+SH_API int sh_project_find(const char *name, int *id);
+/* Components of a level of the project (with_gw adds the 12 tensor
+ * components) and the number of field/momentum pairs. */
+SH_API int sh_project_ncomp(int id, int with_gw, int *ncomp, int *npairs);
+
+/* ---- levels ---------------------------------------------------------------- */
+/* A level of one project: boxes inside the periodic domain [dlo, dhi], with
+ * nghost ghost cells, holding two time levels (SH_NEW, SH_OLD) as
+ * sledgehamr's grid_new/grid_old, plus the scratch the integrators need. */
+SH_API int sh_level_create(sh_ctx *ctx, int project, int with_gw, const int domain_lo[3],
+                    const int domain_hi[3], const sh_box *boxes, int nbox, int nghost,
+                    sh_level **out);
+SH_API int sh_level_destroy(sh_ctx *ctx, sh_level *level);
+SH_API int sh_level_info(const sh_level *level, int *ncomp, int *nbox, long long *nvalid_cells);
+SH_API int sh_level_time(const sh_level *level, int which, double *t, int *istep);
+SH_API int sh_level_set_time(sh_level *level, int which, double t, int istep);
+
+/* Copy valid cells between host and a time level (layout 0: canonical,
+ * which requires one cubic domain covered by the level's boxes; layout 1:
+ * boxes).  Ghost cells are not touched. */
+SH_API int sh_level_write(sh_ctx *ctx, sh_level *level, int which, int layout, const double *host);
+SH_API int sh_level_read(sh_ctx *ctx, const sh_level *level, int which, int layout, double *host);
+/* Same with device arrays, asynchronous on the context stream. */
+SH_API int sh_level_write_device(sh_ctx *ctx, sh_level *level, int which, int layout,
+                          const double *dev);
+SH_API int sh_level_read_device(sh_ctx *ctx, const sh_level *level, int which, int layout,
+                         double *dev);
+
+/* Ghost cells of one time level from the valid cells of the same level,
+ * periodic in every direction (FillPatch / FillIntermediatePatch for
+ * lev <= 0). */
+SH_API int sh_level_fill_patch(sh_ctx *ctx, sh_level *level, int which);
+
+/* One step of integrator `integrator` (SH_INTEGRATOR_*) of a periodic
+ * level: swap(new, old) unless SH_ADVANCE_NO_SWAP, FillPatch(old), integrate
+ * old -> new, t_new = t_old + dt, istep_new = istep_old + 1.
+ * tableau (type 20 only): nodes[s], bbar[s], b[s], then the lower triangle
+ * of a including the diagonal, row by row.  params/gw_params: the vectors
+ * that SetParamsRhs / SetParamsGravitationalWaveRhs produce (at most 32 and
+ * 16 doubles).  ko_order 0 (off), 2 or 3 with ko_strength[ncomp]. */
+SH_API int sh_level_advance(sh_ctx *ctx, sh_level *level, int integrator, const double *tableau,
+                     int nstages, double dt, double dx, const double *params, int nparams,
+                     const double *gw_params, int ngw, int ko_order, const double *ko_strength,
+                     int flags);
+
+/* rhs = f(state) (FillRhs) for the valid cells of time level `which`
+ * (ghosts must be filled); result in boxes layout on the host. */
+SH_API int sh_level_rhs(sh_ctx *ctx, sh_level *level, int which, double time, int lev, double dt,
+                 double dx, const double *params, int nparams, const double *gw_params,
+                 int ngw, int ko_order, const double *ko_strength, double *host_rhs);
+
+/* ---- level synchronisation ------------------------------------------------- */
+/* crse(which_c) = 2x2x2 average of fine(which_f) on every coarse cell
+ * covered by a fine box. */
+SH_API int sh_average_down(sh_ctx *ctx, const sh_level *fine, int which_f, sh_level *crse,
+                    int which_c);
+/* Truncation errors: for every coarse cell covered by fine(NEW),
+ * te = |crse(NEW) - avg(fine)| is stored in fine(OLD) at the even fine cell
+ * (2i, 2j, 2k), and crse(NEW) = avg(fine). */
+SH_API int sh_average_down_te(sh_ctx *ctx, sh_level *fine, sh_level *crse);
+
+/* ---- tagging ---------------------------------------------------------------- */
+/* Tags of time level NEW (ghosts must be filled) with the project's
+ * TagCellForRefinement<true>; if use_te, also the truncation errors stored
+ * in time level OLD, modified by TruncationModifier<n> and compared with
+ * te_crit[n].  mask_out (host, boxes layout, one byte per valid cell) gets 1
+ * for tagged cells; counts_out (may be NULL) gets total, user and ncomp
+ * per-component counts as sledgehamr's CPU tagger reports them;
+ * list_out (may be NULL, room for list_capacity entries) gets the indices of
+ * tagged cells in boxes layout, ascending, and *ntagged their number. */
+SH_API int sh_tag(sh_ctx *ctx, sh_level *level, int use_te, double time, int lev, double dt,
+           double dx, const double *te_crit, const double *params_tag, int nparams_tag,
+           const double *params_mod, int nparams_mod, uint8_t *mask_out,
+           long long *counts_out, int32_t *list_out, long long list_capacity,
+           long long *ntagged);
+
+/* ---- gravitational-wave spectrum -------------------------------------------- */
+/* Bins of unique k^2 (unbinned) for a dim^3 grid: sorted i^2+j^2+k^2 over the
+ * integer FFT frequencies. */
+SH_API int sh_spectrum_bins(int dim, long long *out, int capacity, int *nbins);
+/* Effective momentum per index (projection_type 1: sin, 2: 4th-order, 3:
+ * 6th-order central difference eigenvalue). */
+SH_API int sh_index_to_k(int dim, int projection_type, double *out);
+/* TT-projected GW spectrum of time level NEW of a level covering its cubic
+ * domain with one box.  comps: the six tensor components (absolute component
+ * indices, order xx xy xz yy yz zz); default (NULL): du_xx du_xy du_xz du_yy
+ * du_yz du_zz.  Results in bins_out (capacity max_bins), number of bins in
+ * *nbins and their k^2 in ks_out (may be NULL). */
+SH_API int sh_gw_spectrum(sh_ctx *ctx, const sh_level *level, const int *comps, int zero_padding,
+                   int projection_type, int unbinned, double *bins_out, long long *ks_out,
+                   int max_bins, int *nbins);
+
+/* ---- convenience --------------------------------------------------------------- */
+/* Evolve a periodic cubic level of N^3 cells (boxes of max_grid cells per
+ * side, max_grid <= 0: one box) by nsteps steps; host arrays in canonical
+ * layout.  init_new (may be NULL): content of the second time level before
+ * the first step. */
+SH_API int sh_evolve_periodic(sh_ctx *ctx, int project, int integrator, const double *tableau,
+                       int nstages, int N, int max_grid, int nghost, int ncomp, int with_gw,
+                       const double *state_in, const double *init_new, double *state_out,
+                       double t0, double dt, double dx, int nsteps, const double *params,
+                       int nparams, const double *gw_params, int ngw, int ko_order,
+                       const double *ko_strength);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SLEDGEHAMR_GB300_H_ */

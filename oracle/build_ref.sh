@@ -1,0 +1,20 @@
+#!/bin/sh
+# ORACLE (test infrastructure only).
+# Compiles oracle/_ref/libshref.so from the reference's own per-cell headers
+# where they lie under /root/reference (source/utils/sledgehamr_utils.h,
+# source/kernels.h, projects/*/kernels_*.h, MinimalExample.h) together with
+# the oracle drivers.  Nothing is copied out of the reference tree.
+# Usage: sh oracle/build_ref.sh [REFERENCE_ROOT]
+set -e
+REF=${1:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+if [ ! -d "$REF/source" ]; then
+    echo "build_ref: no reference tree at $REF; skipping" >&2
+    exit 0
+fi
+mkdir -p "$HERE/_ref"
+${CXX:-g++} -std=c++17 -O2 -ffp-contract=off -fPIC -shared -fopenmp \
+    -include "$HERE/ref_shim/ref_prelude.h" \
+    -I"$HERE/ref_shim" -I"$REF/source/utils" -I"$REF/source" -I"$REF/projects" -I"$HERE" \
+    "$HERE/ref_harness.cpp" -o "$HERE/_ref/libshref.so"
+echo "built $HERE/_ref/libshref.so"

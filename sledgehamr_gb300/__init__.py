@@ -1,0 +1,335 @@
+"""sledgehamr_gb300: sledgehamr's time-stepping hot path on a GB300 GPU.
+
+Python host mirror of the library's C ABI (include/sledgehamr_gb300.h).  The
+names follow the reference's operations: a :class:`Level` holds a level's two
+time levels (grid_new / grid_old), :meth:`Level.advance` is
+Integrator::Advance, :meth:`Level.fill_patch` is LevelSynchronizer::FillPatch,
+:func:`average_down` / :func:`average_down_te` are AverageDownTo /
+ComputeTruncationErrors, :meth:`Level.tag` is ErrorEst and
+:meth:`Level.gw_spectrum` is GravitationalWaves::ComputeSpectrum.
+
+All compute runs in libsledgehamr_gb300.so on the GPU; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import SH_NEW, SH_OLD, SH_ADVANCE_NO_SWAP, ShBox
+
+# integrator.type (source/integrators/integrator.h:12-23)
+LSSSPRK3 = 10
+LEAPFROG = 11
+RKN_TABLEAU = 20
+RKN4 = 21
+RKN5 = 22
+
+# project ids compiled into the library
+PROJECTS = ("AxionStrings", "MinimalExample", "NextToMinimalExample",
+            "FirstOrderPhaseTransition", "AxionStringsLap1", "AxionStringsLap2",
+            "AxionStringsLap3")
+
+
+class ShError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"sledgehamr_gb300 error {code}: {msg}")
+        self.code = code
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    return C.c_void_p(a.ctypes.data)
+
+
+def _f64(a, n=None):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+    if n is not None and a.size < n:
+        raise ValueError("array too short")
+    return a
+
+
+def project_id(name: str) -> int:
+    lib = _lib.load()
+    pid = C.c_int(-1)
+    rc = lib.sh_project_find(name.encode(), C.byref(pid))
+    if rc != 0:
+        raise ShError(rc, f"unknown project {name!r}")
+    return pid.value
+
+
+def project_ncomp(name: str, with_gw: bool = False) -> tuple[int, int]:
+    lib = _lib.load()
+    nc, npair = C.c_int(), C.c_int()
+    rc = lib.sh_project_ncomp(project_id(name), int(with_gw), C.byref(nc), C.byref(npair))
+    if rc != 0:
+        raise ShError(rc, f"project {name} with_gw={with_gw}")
+    return nc.value, npair.value
+
+
+def spectrum_bins(dim: int) -> np.ndarray:
+    """Sorted unique k^2 of a dim^3 grid (pySledgehamr CreateUniqueVals)."""
+    lib = _lib.load()
+    n = C.c_int()
+    lib.sh_spectrum_bins(dim, None, 0, C.byref(n))
+    out = np.empty(n.value, dtype=np.int64)
+    rc = lib.sh_spectrum_bins(dim, _ptr(out), n.value, C.byref(n))
+    if rc != 0:
+        raise ShError(rc, "sh_spectrum_bins")
+    return out
+
+
+def index_to_k(dim: int, projection_type: int) -> np.ndarray:
+    lib = _lib.load()
+    out = np.empty(dim, dtype=np.float64)
+    rc = lib.sh_index_to_k(dim, projection_type, _ptr(out))
+    if rc != 0:
+        raise ShError(rc, "sh_index_to_k")
+    return out
+
+
+class Context:
+    """A CUDA device and stream (sh_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _lib.load()
+        h = C.c_void_p()
+        rc = self.lib.sh_ctx_create(device, C.byref(h))
+        if rc != 0:
+            raise ShError(rc, f"could not create a context on device {device}")
+        self.h = h
+
+    def check(self, rc: int, what: str = ""):
+        if rc != 0:
+            msg = self.lib.sh_ctx_last_error(self.h)
+            raise ShError(rc, f"{what}: {msg.decode() if msg else ''}")
+
+    @property
+    def stream(self) -> int:
+        return self.lib.sh_ctx_stream(self.h) or 0
+
+    def set_stream(self, stream_ptr: int | None):
+        self.check(self.lib.sh_ctx_set_stream(self.h, C.c_void_p(stream_ptr or 0)), "set_stream")
+
+    def synchronize(self):
+        self.check(self.lib.sh_ctx_synchronize(self.h), "synchronize")
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self.lib.sh_ctx_kernel_launches(self.h))
+
+    def profile(self, enable: bool = True):
+        """Start (clearing) or stop per-kernel CUDA-event timing."""
+        self.check(self.lib.sh_ctx_profile(self.h, int(enable)), "profile")
+
+    def profile_read(self, category: str) -> tuple[float, int]:
+        """(summed device ms, launches) of a kernel category since profile()."""
+        ms, n = C.c_double(), C.c_longlong()
+        self.check(self.lib.sh_ctx_profile_read(self.h, category.encode(), C.byref(ms),
+                                                C.byref(n)), "profile_read")
+        return ms.value, n.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sh_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- convenience -----------------------------------------------------------
+    def evolve_periodic(self, project: str, integrator: int, state: np.ndarray, t0: float,
+                        dt: float, dx: float, nsteps: int, params: Sequence[float] = (),
+                        gw_params: Sequence[float] = (), with_gw: bool = False,
+                        nghost: int = 2, max_grid: int = 0, tableau=None, init_new=None,
+                        ko_order: int = 0, ko_strength=None) -> np.ndarray:
+        """nsteps steps of a periodic cubic level; state in canonical layout
+        (ncomp, N, N, N) with x fastest."""
+        st = _f64(state)
+        ncomp, N = st.shape[0], st.shape[-1]
+        out = np.empty_like(st)
+        tab = _f64(tableau)
+        nst = 0 if tableau is None else self._nstages(tab)
+        p = _f64(list(params) or [0.0])
+        g = _f64(list(gw_params) or [0.0])
+        ko = _f64(ko_strength)
+        rc = self.lib.sh_evolve_periodic(
+            self.h, project_id(project), integrator, _ptr(tab), nst, N, max_grid, nghost,
+            ncomp, int(with_gw), _ptr(st), _ptr(_f64(init_new)), _ptr(out), t0, dt, dx, nsteps,
+            _ptr(p), len(params), _ptr(g), len(gw_params), ko_order, _ptr(ko))
+        self.check(rc, "sh_evolve_periodic")
+        return out
+
+    @staticmethod
+    def _nstages(tab: np.ndarray) -> int:
+        for s in range(1, 9):
+            if tab.size == 3 * s + s * (s + 1) // 2:
+                return s
+        raise ValueError("tableau length does not match any stage count")
+
+
+def chop_boxes(N: int, max_grid: int) -> list[tuple[tuple[int, int, int], tuple[int, int, int]]]:
+    mg = N if max_grid <= 0 or max_grid >= N else max_grid
+    out = []
+    for z in range(0, N, mg):
+        for y in range(0, N, mg):
+            for x in range(0, N, mg):
+                out.append(((x, y, z), (min(x + mg, N) - 1, min(y + mg, N) - 1,
+                                        min(z + mg, N) - 1)))
+    return out
+
+
+class Level:
+    """A level of boxes with two time levels (sh_level)."""
+
+    def __init__(self, ctx: Context, project: str, boxes, domain_lo, domain_hi, nghost: int,
+                 with_gw: bool = False):
+        self.ctx = ctx
+        self.project = project
+        arr = (ShBox * len(boxes))()
+        for q, (lo, hi) in enumerate(boxes):
+            arr[q].lo[:] = list(lo)
+            arr[q].hi[:] = list(hi)
+        dlo = (C.c_int * 3)(*domain_lo)
+        dhi = (C.c_int * 3)(*domain_hi)
+        h = C.c_void_p()
+        ctx.check(ctx.lib.sh_level_create(ctx.h, project_id(project), int(with_gw), dlo, dhi,
+                                          arr, len(boxes), nghost, C.byref(h)),
+                  "sh_level_create")
+        self.h = h
+        self.boxes = [(tuple(lo), tuple(hi)) for lo, hi in boxes]
+        nc, nb, nv = C.c_int(), C.c_int(), C.c_longlong()
+        ctx.lib.sh_level_info(h, C.byref(nc), C.byref(nb), C.byref(nv))
+        self.ncomp, self.nbox, self.nvalid = nc.value, nb.value, nv.value
+        self.domain = (tuple(domain_lo), tuple(domain_hi))
+
+    @classmethod
+    def periodic(cls, ctx: Context, project: str, N: int, nghost: int, max_grid: int = 0,
+                 with_gw: bool = False) -> "Level":
+        return cls(ctx, project, chop_boxes(N, max_grid), (0, 0, 0), (N - 1, N - 1, N - 1),
+                   nghost, with_gw)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.sh_level_destroy(self.ctx.h, self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def time(self, which: int = SH_NEW) -> tuple[float, int]:
+        t, s = C.c_double(), C.c_int()
+        self.ctx.lib.sh_level_time(self.h, which, C.byref(t), C.byref(s))
+        return t.value, s.value
+
+    def set_time(self, t: float, which: int = SH_NEW, istep: int = 0):
+        self.ctx.lib.sh_level_set_time(self.h, which, t, istep)
+
+    def write(self, data: np.ndarray, which: int = SH_NEW, layout: int = 0):
+        a = _f64(data)
+        if a.size != self.nvalid * self.ncomp:
+            raise ValueError("data size does not match the level")
+        self.ctx.check(self.ctx.lib.sh_level_write(self.ctx.h, self.h, which, layout, _ptr(a)),
+                       "sh_level_write")
+
+    def read(self, which: int = SH_NEW, layout: int = 0) -> np.ndarray:
+        out = np.empty(self.nvalid * self.ncomp, dtype=np.float64)
+        self.ctx.check(self.ctx.lib.sh_level_read(self.ctx.h, self.h, which, layout, _ptr(out)),
+                       "sh_level_read")
+        if layout == 0:
+            N = self.domain[1][0] - self.domain[0][0] + 1
+            return out.reshape(self.ncomp, N, N, N)
+        return out
+
+    def write_device(self, dev_ptr: int, which: int = SH_NEW, layout: int = 0):
+        self.ctx.check(self.ctx.lib.sh_level_write_device(self.ctx.h, self.h, which, layout,
+                                                          C.c_void_p(dev_ptr)),
+                       "sh_level_write_device")
+
+    def read_device(self, dev_ptr: int, which: int = SH_NEW, layout: int = 0):
+        self.ctx.check(self.ctx.lib.sh_level_read_device(self.ctx.h, self.h, which, layout,
+                                                         C.c_void_p(dev_ptr)),
+                       "sh_level_read_device")
+
+    def fill_patch(self, which: int = SH_NEW):
+        self.ctx.check(self.ctx.lib.sh_level_fill_patch(self.ctx.h, self.h, which),
+                       "sh_level_fill_patch")
+
+    def advance(self, integrator: int, dt: float, dx: float, params: Sequence[float] = (),
+                gw_params: Sequence[float] = (), tableau=None, ko_order: int = 0,
+                ko_strength=None, flags: int = 0):
+        tab = _f64(tableau)
+        nst = 0 if tableau is None else Context._nstages(tab)
+        p = _f64(list(params) or [0.0])
+        g = _f64(list(gw_params) or [0.0])
+        self.ctx.check(self.ctx.lib.sh_level_advance(
+            self.ctx.h, self.h, integrator, _ptr(tab), nst, dt, dx, _ptr(p), len(params),
+            _ptr(g), len(gw_params), ko_order, _ptr(_f64(ko_strength)), flags),
+            "sh_level_advance")
+
+    def rhs(self, time: float, lev: int, dt: float, dx: float, params=(), gw_params=(),
+            which: int = SH_NEW, ko_order: int = 0, ko_strength=None) -> np.ndarray:
+        out = np.empty(self.nvalid * self.ncomp, dtype=np.float64)
+        p = _f64(list(params) or [0.0])
+        g = _f64(list(gw_params) or [0.0])
+        self.ctx.check(self.ctx.lib.sh_level_rhs(
+            self.ctx.h, self.h, which, time, lev, dt, dx, _ptr(p), len(params), _ptr(g),
+            len(gw_params), ko_order, _ptr(_f64(ko_strength)), _ptr(out)), "sh_level_rhs")
+        return out
+
+    def tag(self, time: float, lev: int, dt: float, dx: float, use_te: bool = False,
+            te_crit=None, params_tag=(), params_mod=(), want_list: bool = False):
+        """Returns (mask in boxes layout, counts, tag list or None)."""
+        mask = np.empty(self.nvalid, dtype=np.uint8)
+        counts = np.zeros(2 + self.ncomp, dtype=np.int64)
+        tc = _f64(te_crit) if te_crit is not None else None
+        pt = _f64(list(params_tag) or [0.0])
+        pm = _f64(list(params_mod) or [0.0])
+        lst = np.empty(self.nvalid if want_list else 1, dtype=np.int32)
+        nt = C.c_longlong()
+        self.ctx.check(self.ctx.lib.sh_tag(
+            self.ctx.h, self.h, int(use_te), time, lev, dt, dx, _ptr(tc), _ptr(pt),
+            len(params_tag), _ptr(pm), len(params_mod), _ptr(mask), _ptr(counts),
+            _ptr(lst) if want_list else None, self.nvalid if want_list else 0, C.byref(nt)),
+            "sh_tag")
+        return mask, counts, (lst[: nt.value].copy() if want_list else None)
+
+    def gw_spectrum(self, zero_padding: int = 1, projection_type: int = 2, unbinned: bool = True,
+                    comps: Sequence[int] | None = None):
+        N = self.domain[1][0] - self.domain[0][0] + 1
+        P = N * zero_padding
+        cap = 3 * (P // 2 + 1) ** 2 + 16
+        bins = np.empty(cap, dtype=np.float64)
+        ks = np.empty(cap, dtype=np.int64)
+        nb = C.c_int()
+        c6 = None if comps is None else np.ascontiguousarray(np.asarray(comps, dtype=np.int32))
+        self.ctx.check(self.ctx.lib.sh_gw_spectrum(
+            self.ctx.h, self.h, _ptr(c6), zero_padding, projection_type, int(unbinned),
+            _ptr(bins), _ptr(ks), cap, C.byref(nb)), "sh_gw_spectrum")
+        return bins[: nb.value].copy(), ks[: nb.value].copy()
+
+
+def average_down(ctx: Context, fine: Level, crse: Level, which_f: int = SH_NEW,
+                 which_c: int = SH_NEW):
+    ctx.check(ctx.lib.sh_average_down(ctx.h, fine.h, which_f, crse.h, which_c), "sh_average_down")
+
+
+def average_down_te(ctx: Context, fine: Level, crse: Level):
+    ctx.check(ctx.lib.sh_average_down_te(ctx.h, fine.h, crse.h), "sh_average_down_te")

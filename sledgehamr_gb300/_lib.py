@@ -1,0 +1,99 @@
+"""ctypes binding of libsledgehamr_gb300.so (include/sledgehamr_gb300.h).
+
+The library is the only compute path of this package: loading fails loudly
+when it has not been built (run ``python -c "import __graft_entry__ as g;
+g.build()"`` or ``python sledgehamr_gb300/build.py``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libsledgehamr_gb300.so")
+
+SH_OK = 0
+SH_ERR_ARG = -1
+SH_ERR_PROJECT = -2
+SH_ERR_CUDA = -3
+SH_ERR_NOMEM = -4
+SH_ERR_UNSUPPORTED = -5
+SH_ERR_TIMEOUT = -6
+SH_ERR_NONFINITE = -7
+
+SH_NEW = 0
+SH_OLD = 1
+SH_ADVANCE_NO_SWAP = 1
+
+dp = C.POINTER(C.c_double)
+ip = C.POINTER(C.c_int)
+llp = C.POINTER(C.c_longlong)
+vp = C.c_void_p
+
+
+class ShBox(C.Structure):
+    _fields_ = [("lo", C.c_int * 3), ("hi", C.c_int * 3)]
+
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "sh_ctx_create": (C.c_int, [C.c_int, C.POINTER(vp)]),
+    "sh_ctx_destroy": (C.c_int, [vp]),
+    "sh_ctx_last_error": (C.c_char_p, [vp]),
+    "sh_ctx_set_stream": (C.c_int, [vp, vp]),
+    "sh_ctx_stream": (vp, [vp]),
+    "sh_ctx_synchronize": (C.c_int, [vp]),
+    "sh_ctx_kernel_launches": (C.c_longlong, [vp]),
+    "sh_ctx_profile": (C.c_int, [vp, C.c_int]),
+    "sh_ctx_profile_read": (C.c_int, [vp, C.c_char_p, dp, llp]),
+    "sh_project_count": (C.c_int, []),
+    "sh_project_name": (C.c_char_p, [C.c_int]),
+    "sh_project_find": (C.c_int, [C.c_char_p, ip]),
+    "sh_project_ncomp": (C.c_int, [C.c_int, C.c_int, ip, ip]),
+    "sh_level_create": (C.c_int, [vp, C.c_int, C.c_int, ip, ip, C.POINTER(ShBox), C.c_int,
+                                  C.c_int, C.POINTER(vp)]),
+    "sh_level_destroy": (C.c_int, [vp, vp]),
+    "sh_level_info": (C.c_int, [vp, ip, ip, llp]),
+    "sh_level_time": (C.c_int, [vp, C.c_int, dp, ip]),
+    "sh_level_set_time": (C.c_int, [vp, C.c_int, C.c_double, C.c_int]),
+    "sh_level_write": (C.c_int, [vp, vp, C.c_int, C.c_int, vp]),
+    "sh_level_read": (C.c_int, [vp, vp, C.c_int, C.c_int, vp]),
+    "sh_level_write_device": (C.c_int, [vp, vp, C.c_int, C.c_int, vp]),
+    "sh_level_read_device": (C.c_int, [vp, vp, C.c_int, C.c_int, vp]),
+    "sh_level_fill_patch": (C.c_int, [vp, vp, C.c_int]),
+    "sh_level_advance": (C.c_int, [vp, vp, C.c_int, vp, C.c_int, C.c_double, C.c_double, vp,
+                                   C.c_int, vp, C.c_int, C.c_int, vp, C.c_int]),
+    "sh_level_rhs": (C.c_int, [vp, vp, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double,
+                               vp, C.c_int, vp, C.c_int, C.c_int, vp, vp]),
+    "sh_average_down": (C.c_int, [vp, vp, C.c_int, vp, C.c_int]),
+    "sh_average_down_te": (C.c_int, [vp, vp, vp]),
+    "sh_tag": (C.c_int, [vp, vp, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double, vp, vp,
+                         C.c_int, vp, C.c_int, vp, vp, vp, C.c_longlong, llp]),
+    "sh_spectrum_bins": (C.c_int, [C.c_int, vp, C.c_int, ip]),
+    "sh_index_to_k": (C.c_int, [C.c_int, C.c_int, vp]),
+    "sh_gw_spectrum": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, C.c_int, ip]),
+    "sh_evolve_periodic": (C.c_int, [vp, C.c_int, C.c_int, vp, C.c_int, C.c_int, C.c_int,
+                                     C.c_int, C.c_int, C.c_int, vp, vp, vp, C.c_double,
+                                     C.c_double, C.c_double, C.c_int, vp, C.c_int, vp, C.c_int,
+                                     C.c_int, vp]),
+}
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Loads the library once; raises if it is missing (no CPU fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            f"{LIB_PATH} is missing: build the CUDA library first "
+            "(python sledgehamr_gb300/build.py)")
+    lib = C.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib

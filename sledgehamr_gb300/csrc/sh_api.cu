@@ -1,0 +1,1286 @@
+/* C ABI of libsledgehamr_gb300.so (declared in include/sledgehamr_gb300.h):
+ * contexts, levels, host/device data movement, periodic ghost fill, the
+ * integrator drivers that sequence the fused stage kernels of
+ * sh_stage.cuh, average-down (with and without truncation errors) and
+ * tagging with deterministic tag-list compaction.
+ */
+#include "sledgehamr_gb300.h"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "sh_gw.h"
+#include "sh_internal.h"
+
+/* ---- project registry --------------------------------------------------- */
+namespace sh {
+extern const ProjectOps project_AxionStrings;
+extern const ProjectOps project_MinimalExample;
+extern const ProjectOps project_NextToMinimalExample;
+extern const ProjectOps project_FirstOrderPhaseTransition;
+extern const ProjectOps project_AxionStringsLap1;
+extern const ProjectOps project_AxionStringsLap2;
+extern const ProjectOps project_AxionStringsLap3;
+
+/* Ids match the oracle's project numbering. */
+static const ProjectOps *const kProjects[] = {
+    &project_AxionStrings,   &project_MinimalExample,   &project_NextToMinimalExample,
+    &project_FirstOrderPhaseTransition, &project_AxionStringsLap1, &project_AxionStringsLap2,
+    &project_AxionStringsLap3};
+
+int project_count() { return (int)(sizeof(kProjects) / sizeof(kProjects[0])); }
+const ProjectOps *project_by_id(int id) {
+    return (id >= 0 && id < project_count()) ? kProjects[id] : nullptr;
+}
+} // namespace sh
+
+using namespace sh;
+
+/* ---- context / level structures ------------------------------------------- */
+struct ProfRecord {
+    int category;
+    cudaEvent_t start, stop;
+};
+static const char *const kProfCategories[] = {"rhs",     "fill_patch",  "average_down",
+                                              "tagging", "gw_spectrum", "data_move"};
+enum ProfCat { kProfRhs = 0, kProfFill, kProfAvg, kProfTag, kProfGw, kProfMove, kProfCount };
+
+struct sh_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    std::string err;
+    long long launches = 0;
+    /* growing device scratch for host transfers and reductions */
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+    GwCache gw;
+    bool profiling = false;
+    std::vector<ProfRecord> prof;
+    std::vector<cudaEvent_t> event_pool;
+    double prof_ms[kProfCount] = {0, 0, 0, 0, 0, 0};
+    long long prof_n[kProfCount] = {0, 0, 0, 0, 0, 0};
+};
+
+struct sh_level {
+    int project = -1;
+    const ProjectOps *ops = nullptr;
+    bool with_gw = false;
+    int ncomp = 0, npairs = 0, nghost = 0;
+    int dlo[3] = {0, 0, 0}, dhi[3] = {0, 0, 0};
+    std::vector<sh_box> boxes;
+    std::vector<BoxDev> hboxes;
+    std::vector<long long> vbase; /* prefix sums of valid cells per box */
+    long long total_gvol = 0, nvalid = 0;
+    BoxDev *d_boxes = nullptr;
+    TileDev *d_tiles = nullptr;
+    int ntiles = 0;
+    GhostCopyDev *d_ghost = nullptr;
+    int nghost_rects = 0;
+    long long nghost_cells = 0;
+    long long *d_vbase = nullptr; /* nbox + 1 */
+    double *buf[3] = {nullptr, nullptr, nullptr}; /* SH_NEW, SH_OLD, alt */
+    double *kbuf = nullptr;  /* K buffers, kbuf_elems each */
+    size_t kbuf_elems = 0;
+    int kbuf_count = 0;
+    double t[2] = {-1.7976931348623157e308, -1.7976931348623157e308};
+    int istep[2] = {0, 0};
+};
+
+namespace {
+
+struct ShError : std::runtime_error {
+    int code;
+    ShError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+inline void ck(cudaError_t e, const char *what) {
+    if (e != cudaSuccess)
+        throw ShError(SH_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <class F>
+int guarded(sh_ctx *ctx, F &&f) {
+    try {
+        f();
+        return SH_OK;
+    } catch (const ShError &e) {
+        if (ctx) ctx->err = e.what();
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        if (ctx) ctx->err = "host allocation failed";
+        return SH_ERR_NOMEM;
+    } catch (const std::exception &e) {
+        if (ctx) ctx->err = e.what();
+        return SH_ERR_ARG;
+    }
+}
+
+inline void require(bool c, const std::string &msg) {
+    if (!c) throw ShError(SH_ERR_ARG, msg);
+}
+
+void *dmalloc(size_t bytes, const char *what) {
+    void *p = nullptr;
+    if (bytes == 0) return nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        throw ShError(SH_ERR_NOMEM, std::string("device allocation failed: ") + what);
+    }
+    ck(e, what);
+    return p;
+}
+
+void *ctx_scratch(sh_ctx *ctx, size_t bytes) {
+    if (bytes > ctx->scratch_bytes) {
+        if (ctx->scratch) {
+            ck(cudaStreamSynchronize(ctx->stream), "sync before scratch resize");
+            cudaFree(ctx->scratch);
+        }
+        ctx->scratch = dmalloc(bytes, "context scratch");
+        ctx->scratch_bytes = bytes;
+    }
+    return ctx->scratch;
+}
+
+inline void set_device(sh_ctx *ctx) { ck(cudaSetDevice(ctx->device), "cudaSetDevice"); }
+
+cudaEvent_t pooled_event(sh_ctx *ctx) {
+    if (!ctx->event_pool.empty()) {
+        cudaEvent_t e = ctx->event_pool.back();
+        ctx->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    ck(cudaEventCreate(&e), "event create");
+    return e;
+}
+
+/* Records CUDA events around the launches of one category while profiling. */
+struct ProfScope {
+    sh_ctx *ctx;
+    int cat;
+    cudaEvent_t a = nullptr;
+    ProfScope(sh_ctx *c, int category) : ctx(c), cat(category) {
+        if (ctx->profiling) {
+            a = pooled_event(ctx);
+            cudaEventRecord(a, ctx->stream);
+        }
+    }
+    ~ProfScope() {
+        if (a) {
+            cudaEvent_t b = pooled_event(ctx);
+            cudaEventRecord(b, ctx->stream);
+            ctx->prof.push_back(ProfRecord{cat, a, b});
+        }
+    }
+};
+
+void profile_resolve(sh_ctx *ctx) {
+    if (ctx->prof.empty()) return;
+    ck(cudaStreamSynchronize(ctx->stream), "profile sync");
+    for (const ProfRecord &r : ctx->prof) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, r.start, r.stop) == cudaSuccess) {
+            ctx->prof_ms[r.category] += ms;
+            ctx->prof_n[r.category] += 1;
+        }
+        ctx->event_pool.push_back(r.start);
+        ctx->event_pool.push_back(r.stop);
+    }
+    ctx->prof.clear();
+}
+
+/* ---- data movement kernels ------------------------------------------------ */
+
+/* Locate the box of valid cell number v (prefix sums vbase[0..nbox]). */
+__device__ __forceinline__ int find_box(const long long *vbase, int nbox, long long v) {
+    int lo = 0, hi = nbox - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (vbase[mid] <= v) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+/* layout 0: canonical domain array; layout 1: boxes (packed valid cells).
+ * dir 0: host-side array -> level buffer; dir 1: level buffer -> array. */
+__global__ void move_kernel(const BoxDev *boxes, const long long *vbase, int nbox, int ncomp,
+                            long long nvalid, double *buf, double *arr, int layout, int dir,
+                            int N0, int N1, int N2, int dlo0, int dlo1, int dlo2) {
+    const long long total = nvalid * ncomp;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const long long v = e % nvalid;
+        const int n = (int)(e / nvalid);
+        const int bx = find_box(vbase, nbox, v);
+        const BoxDev &b = boxes[bx];
+        const long long lv = v - vbase[bx];
+        const int vx = b.hi[0] - b.lo[0] + 1, vy = b.hi[1] - b.lo[1] + 1;
+        const int i = b.lo[0] + (int)(lv % vx);
+        const int j = b.lo[1] + (int)((lv / vx) % vy);
+        const int k = b.lo[2] + (int)(lv / ((long long)vx * vy));
+        const long long bi = b.off * ncomp + (long long)n * b.gvol + (i - b.glo[0]) +
+                             (long long)(j - b.glo[1]) * b.gdim[0] +
+                             (long long)(k - b.glo[2]) * b.gdim[0] * b.gdim[1];
+        long long ai;
+        if (layout == 0)
+            ai = (((long long)n * N2 + (k - dlo2)) * N1 + (j - dlo1)) * N0 + (i - dlo0);
+        else
+            ai = vbase[bx] * ncomp + (long long)n * (vbase[bx + 1] - vbase[bx]) + lv;
+        if (dir == 0) buf[bi] = arr[ai];
+        else arr[ai] = buf[bi];
+    }
+}
+
+/* Periodic ghost fill: one thread per ghost cell of the copy plan. */
+__global__ void ghost_copy_kernel(const BoxDev *boxes, const GhostCopyDev *rects, int nrects,
+                                  long long ncells, int ncomp, double *buf) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncells;
+         c += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = nrects - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (rects[mid].first <= c) lo = mid;
+            else hi = mid - 1;
+        }
+        const GhostCopyDev &r = rects[lo];
+        const long long lc = c - r.first;
+        const int nx = r.hi[0] - r.lo[0] + 1, ny = r.hi[1] - r.lo[1] + 1;
+        const int i = r.lo[0] + (int)(lc % nx);
+        const int j = r.lo[1] + (int)((lc / nx) % ny);
+        const int k = r.lo[2] + (int)(lc / ((long long)nx * ny));
+        const BoxDev &db = boxes[r.dbox];
+        const BoxDev &sb = boxes[r.sbox];
+        const int si = i - r.shift[0], sj = j - r.shift[1], sk = k - r.shift[2];
+        const long long di = db.off * ncomp + (i - db.glo[0]) +
+                             (long long)(j - db.glo[1]) * db.gdim[0] +
+                             (long long)(k - db.glo[2]) * db.gdim[0] * db.gdim[1];
+        const long long sidx = sb.off * ncomp + (si - sb.glo[0]) +
+                               (long long)(sj - sb.glo[1]) * sb.gdim[0] +
+                               (long long)(sk - sb.glo[2]) * sb.gdim[0] * sb.gdim[1];
+        for (int n = 0; n < ncomp; ++n) buf[di + n * db.gvol] = buf[sidx + n * sb.gvol];
+    }
+}
+
+/* One rectangle of coarse cells [lo, hi] lying in coarse box cbox and under
+ * fine box fbox. */
+struct AvgRect {
+    int fbox, cbox;
+    int lo[3], hi[3];
+    long long first;
+};
+
+/* Plain average-down (k, j, i summation order) or, with te != nullptr, the
+ * average-down with truncation error of kernels::AverageDownWithTruncationError
+ * (summation order (0,0,0) (1,0,0) (0,1,0) (0,0,1) (1,1,0) (1,0,1) (0,1,1)
+ * (1,1,1)). */
+__global__ void avgdown_kernel(const AvgRect *rects, int nrects, long long ncells,
+                               const BoxDev *fboxes, const BoxDev *cboxes, int ncomp,
+                               const double *fine, double *crse, double *te) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncells;
+         c += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = nrects - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (rects[mid].first <= c) lo = mid;
+            else hi = mid - 1;
+        }
+        const AvgRect &r = rects[lo];
+        const long long lc = c - r.first;
+        const int nx = r.hi[0] - r.lo[0] + 1, ny = r.hi[1] - r.lo[1] + 1;
+        const int i = r.lo[0] + (int)(lc % nx);
+        const int j = r.lo[1] + (int)((lc / nx) % ny);
+        const int k = r.lo[2] + (int)(lc / ((long long)nx * ny));
+        const BoxDev &fb = fboxes[r.fbox];
+        const BoxDev &cb = cboxes[r.cbox];
+        const long long fx = fb.gdim[0], fxy = fx * fb.gdim[1];
+        const long long f0 = fb.off * ncomp + (2 * i - fb.glo[0]) + (2 * j - fb.glo[1]) * fx +
+                             (2 * k - fb.glo[2]) * fxy;
+        const long long c0 = cb.off * ncomp + (i - cb.glo[0]) +
+                             (long long)(j - cb.glo[1]) * cb.gdim[0] +
+                             (long long)(k - cb.glo[2]) * cb.gdim[0] * cb.gdim[1];
+        for (int n = 0; n < ncomp; ++n) {
+            const double *f = fine + f0 + n * fb.gvol;
+            if (te) {
+                double s = f[0];
+                s += f[1];
+                s += f[fx];
+                s += f[fxy];
+                s += f[1 + fx];
+                s += f[1 + fxy];
+                s += f[fx + fxy];
+                s += f[1 + fx + fxy];
+                const double avg = 0.125 * s;
+                double *cc = crse + c0 + n * cb.gvol;
+                te[f0 + n * fb.gvol] = fabs(*cc - avg);
+                *cc = avg;
+            } else {
+                double s = 0.0;
+                for (int dk = 0; dk < 2; ++dk)
+                    for (int dj = 0; dj < 2; ++dj)
+                        for (int di = 0; di < 2; ++di) s += f[di + dj * fx + dk * fxy];
+                crse[c0 + n * cb.gvol] = s * 0.125;
+            }
+        }
+    }
+}
+
+/* Tag-list compaction, pass 1: tagged cells per chunk of kChunk mask bytes. */
+constexpr int kChunk = 4096;
+__global__ void tag_count_kernel(const unsigned char *mask, long long n, int *chunk_counts) {
+    const long long base = (long long)blockIdx.x * kChunk;
+    int cnt = 0;
+    for (int q = threadIdx.x; q < kChunk; q += blockDim.x) {
+        long long e = base + q;
+        if (e < n) cnt += mask[e] != 0;
+    }
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    __shared__ int ws[32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int s = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += ws[w];
+        chunk_counts[blockIdx.x] = s;
+    }
+}
+/* pass 2: exclusive scan of the chunk counts (one block). */
+__global__ void tag_scan_kernel(int *chunk_counts, int nchunks, long long *chunk_base,
+                                long long *total) {
+    __shared__ long long carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int start = 0; start < nchunks; start += blockDim.x) {
+        const int idx = start + threadIdx.x;
+        long long v = idx < nchunks ? chunk_counts[idx] : 0;
+        /* inclusive block scan via warp shuffles */
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        long long x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            long long y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        __shared__ long long wsum[32];
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            long long w = lane < (int)(blockDim.x >> 5) ? wsum[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                long long y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            wsum[lane] = w;
+        }
+        __syncthreads();
+        const long long incl = x + (warp > 0 ? wsum[warp - 1] : 0);
+        if (idx < nchunks) chunk_base[idx] = carry + incl - v;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry += incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+/* pass 3: write the indices of tagged cells in ascending order; within a
+ * chunk, warps take 32-byte slices in order and use ballots for their
+ * offsets. */
+__global__ void tag_write_kernel(const unsigned char *mask, long long n,
+                                 const long long *chunk_base, int *list, long long capacity) {
+    const long long base = (long long)blockIdx.x * kChunk;
+    __shared__ int warp_tot[32];
+    __shared__ long long running;
+    if (threadIdx.x == 0) running = chunk_base[blockIdx.x];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int slab = 0; slab < kChunk; slab += blockDim.x) {
+        const long long e = base + slab + threadIdx.x;
+        const bool t = (slab + threadIdx.x < kChunk) && e < n && mask[e] != 0;
+        const unsigned bal = __ballot_sync(0xffffffffu, t);
+        if (lane == 0) warp_tot[warp] = __popc(bal);
+        __syncthreads();
+        long long off = running;
+        for (int w = 0; w < warp; ++w) off += warp_tot[w];
+        if (t) {
+            const long long pos = off + __popc(bal & ((1u << lane) - 1u));
+            if (pos < capacity) list[pos] = (int)e;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            long long s = 0;
+            for (int w = 0; w < nw; ++w) s += warp_tot[w];
+            running += s;
+        }
+        __syncthreads();
+    }
+}
+
+int grid_for(long long work, int block = 256) {
+    long long g = (work + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > 152LL * 32) g = 152LL * 32;
+    return (int)g;
+}
+
+/* ---- level construction ------------------------------------------------- */
+
+bool box_intersect(const int alo[3], const int ahi[3], const int blo[3], const int bhi[3],
+                   int lo[3], int hi[3]) {
+    for (int d = 0; d < 3; ++d) {
+        lo[d] = std::max(alo[d], blo[d]);
+        hi[d] = std::min(ahi[d], bhi[d]);
+        if (lo[d] > hi[d]) return false;
+    }
+    return true;
+}
+
+void build_ghost_plan(sh_level *L) {
+    std::vector<GhostCopyDev> rects;
+    long long run = 0;
+    const int ext[3] = {L->dhi[0] - L->dlo[0] + 1, L->dhi[1] - L->dlo[1] + 1,
+                        L->dhi[2] - L->dlo[2] + 1};
+    const int g = L->nghost;
+    for (size_t b = 0; b < L->boxes.size(); ++b) {
+        int glo[3], ghi[3];
+        for (int d = 0; d < 3; ++d) {
+            glo[d] = L->boxes[b].lo[d] - g;
+            ghi[d] = L->boxes[b].hi[d] + g;
+        }
+        for (size_t s = 0; s < L->boxes.size(); ++s)
+            for (int sz = -1; sz <= 1; ++sz)
+                for (int sy = -1; sy <= 1; ++sy)
+                    for (int sx = -1; sx <= 1; ++sx) {
+                        if (s == b && sx == 0 && sy == 0 && sz == 0) continue;
+                        const int sh[3] = {sx * ext[0], sy * ext[1], sz * ext[2]};
+                        int slo[3], shi[3];
+                        for (int d = 0; d < 3; ++d) {
+                            slo[d] = L->boxes[s].lo[d] + sh[d];
+                            shi[d] = L->boxes[s].hi[d] + sh[d];
+                        }
+                        int lo[3], hi[3];
+                        if (!box_intersect(glo, ghi, slo, shi, lo, hi)) continue;
+                        GhostCopyDev r;
+                        r.dbox = (int)b;
+                        r.sbox = (int)s;
+                        for (int d = 0; d < 3; ++d) {
+                            r.lo[d] = lo[d];
+                            r.hi[d] = hi[d];
+                            r.shift[d] = sh[d];
+                        }
+                        r.first = run;
+                        run += (long long)(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) *
+                               (hi[2] - lo[2] + 1);
+                        rects.push_back(r);
+                    }
+    }
+    L->nghost_rects = (int)rects.size();
+    L->nghost_cells = run;
+    if (!rects.empty()) {
+        L->d_ghost = (GhostCopyDev *)dmalloc(rects.size() * sizeof(GhostCopyDev), "ghost plan");
+        ck(cudaMemcpy(L->d_ghost, rects.data(), rects.size() * sizeof(GhostCopyDev),
+                      cudaMemcpyHostToDevice),
+           "ghost plan upload");
+    }
+}
+
+void level_free(sh_level *L) {
+    cudaFree(L->d_boxes);
+    cudaFree(L->d_tiles);
+    cudaFree(L->d_ghost);
+    cudaFree(L->d_vbase);
+    for (int q = 0; q < 3; ++q) cudaFree(L->buf[q]);
+    cudaFree(L->kbuf);
+}
+
+void ensure_kbuf(sh_level *L, size_t elems, int count) {
+    if (elems * count <= L->kbuf_elems * L->kbuf_count && elems <= L->kbuf_elems) return;
+    cudaFree(L->kbuf);
+    L->kbuf = nullptr;
+    L->kbuf = (double *)dmalloc(elems * count * sizeof(double), "integrator K buffers");
+    L->kbuf_elems = elems;
+    L->kbuf_count = count;
+}
+
+void fill_patch(sh_ctx *ctx, sh_level *L, double *buf) {
+    if (L->nghost_cells == 0) return;
+    ProfScope ps(ctx, kProfFill);
+    ghost_copy_kernel<<<grid_for(L->nghost_cells), 256, 0, ctx->stream>>>(
+        L->d_boxes, L->d_ghost, L->nghost_rects, L->nghost_cells, L->ncomp, buf);
+    ctx->launches++;
+    ck(cudaGetLastError(), "ghost fill launch");
+}
+
+void launch_stage(sh_ctx *ctx, sh_level *L, StageArgs &a, int ko_order) {
+    a.tiles = L->d_tiles;
+    a.boxes = L->d_boxes;
+    a.ncomp = L->ncomp;
+    ProfScope ps(ctx, kProfRhs);
+    StageLaunch sl;
+    sl.args = a;
+    sl.ntiles = L->ntiles;
+    sl.with_gw = L->with_gw;
+    sl.ko_order = ko_order;
+    cudaError_t e = L->ops->launch_stage(sl, ctx->stream);
+    if (e == cudaErrorNotSupported)
+        throw ShError(SH_ERR_UNSUPPORTED, "project has no gravitational-wave hooks");
+    ck(e, "stage kernel launch");
+    ctx->launches++;
+}
+
+void fill_common(StageArgs &a, const sh_level *L, double dt, double dx, const double *params,
+                 int nparams, const double *gw_params, int ngw, int ko_order,
+                 const double *ko_strength) {
+    require(nparams >= 0 && nparams <= kMaxParams, "at most 32 Rhs parameters");
+    require(ngw >= 0 && ngw <= kMaxGwParams, "at most 16 GW parameters");
+    require(ko_order == 0 || ko_order == 2 || ko_order == 3, "ko_order must be 0, 2 or 3");
+    require(ko_order == 0 || ko_strength != nullptr, "ko_strength required");
+    require(L->nghost >= ko_order, "nghost smaller than the dissipation stencil");
+    std::memset(&a, 0, sizeof(a));
+    a.dt = dt;
+    a.dx = dx;
+    for (int q = 0; q < nparams; ++q) a.params[q] = params[q];
+    for (int q = 0; q < ngw; ++q) a.gw_params[q] = gw_params[q];
+    if (ko_order)
+        for (int n = 0; n < L->ncomp; ++n) a.ko_strength[n] = ko_strength[n];
+}
+
+struct Tableau {
+    std::vector<double> nodes, bbar, b;
+    std::vector<std::vector<double>> a;
+};
+
+/* source/integrators/rkn.cpp:130-152 */
+Tableau rkn_tableau(int type, const double *flat, int s) {
+    Tableau t;
+    if (type == SH_INTEGRATOR_RKN4) {
+        t.nodes = {0.0, 0.5, 1.0};
+        t.a = {{0.0}, {1. / 8., 0.0}, {0.0, 0.5, 0.0}};
+        t.bbar = {1. / 6., 1. / 3., 0.0};
+        t.b = {1. / 6., 4. / 6., 1. / 6.};
+    } else if (type == SH_INTEGRATOR_RKN5) {
+        t.nodes = {0.0, 1. / 5., 2. / 3., 1.0};
+        t.a = {{0.0}, {1. / 50., 0.0}, {-1. / 27., 7. / 27., 0.0},
+               {3. / 10., -2. / 35., 9. / 35., 0.0}};
+        t.bbar = {14. / 336., 100. / 336., 54. / 336., 0.0};
+        t.b = {14. / 336., 125. / 336., 162. / 336., 35. / 336.};
+    } else {
+        require(flat != nullptr && s >= 1 && s <= kMaxStages, "user tableau: 1..8 stages");
+        t.nodes.assign(flat, flat + s);
+        t.bbar.assign(flat + s, flat + 2 * s);
+        t.b.assign(flat + 2 * s, flat + 3 * s);
+        const double *tri = flat + 3 * s;
+        for (int i = 0; i < s; ++i) {
+            t.a.emplace_back(tri, tri + i + 1);
+            tri += i + 1;
+            require(t.a.back().back() == 0.0, "RKN tableau must be explicit");
+        }
+    }
+    return t;
+}
+
+/* Integrate old -> new with the fused stage kernels.  Buffers: 0 = new,
+ * 1 = old, 2 = alt; stage states alternate between new and alt. */
+void integrate(sh_ctx *ctx, sh_level *L, int type, const double *tableau, int nstages,
+               double dt, double dx, const double *params, int nparams, const double *gw_params,
+               int ngw, int ko_order, const double *ko_strength) {
+    const double t0 = L->t[SH_OLD];
+    const size_t kelems = (size_t)L->total_gvol * L->ncomp;
+    StageArgs a;
+    fill_common(a, L, dt, dx, params, nparams, gw_params, ngw, ko_order, ko_strength);
+    a.y0 = L->buf[SH_OLD];
+    a.nk = L->npairs;
+
+    if (type == SH_INTEGRATOR_RKN4 || type == SH_INTEGRATOR_RKN5 ||
+        type == SH_INTEGRATOR_RKN_TABLEAU) {
+        Tableau tb = rkn_tableau(type, tableau, nstages);
+        const int S = (int)tb.b.size();
+        ensure_kbuf(L, (size_t)L->total_gvol * L->npairs, S);
+        double *kb[kMaxStages];
+        for (int s = 0; s < S; ++s) kb[s] = L->kbuf + (size_t)s * L->total_gvol * L->npairs;
+        int cur = SH_OLD; /* buffer holding Y_i */
+        for (int i = 0; i < S; ++i) {
+            StageArgs s = a;
+            s.state = L->buf[cur];
+            s.time = t0 + dt * tb.nodes[i];
+            s.nkin = i;
+            for (int j = 0; j < i; ++j) s.kin[j] = kb[j];
+            const int next = (cur == SH_NEW) ? 2 : SH_NEW;
+            s.out = L->buf[next];
+            if (i < S - 1) {
+                s.epi = kEpiRknStage;
+                s.kout = kb[i];
+                s.c_mom = dt * tb.nodes[i + 1];
+                for (int j = 0; j <= i; ++j) s.c_k[j] = dt * dt * tb.a[i + 1][j];
+            } else {
+                s.epi = kEpiRknFinal;
+                s.kout = nullptr;
+                s.c_mom = dt;
+                for (int j = 0; j < S; ++j) {
+                    s.c_k[j] = dt * dt * tb.bbar[j];
+                    s.c_k2[j] = dt * tb.b[j];
+                }
+            }
+            launch_stage(ctx, L, s, ko_order);
+            fill_patch(ctx, L, L->buf[next]);
+            cur = next;
+        }
+        if (cur != SH_NEW) std::swap(L->buf[SH_NEW], L->buf[2]);
+    } else if (type == SH_INTEGRATOR_LSSSPRK3) {
+        ensure_kbuf(L, kelems, 1);
+        StageArgs s = a;
+        /* k1 = f(y0); u1 = y0 + dt k1 */
+        s.state = L->buf[SH_OLD];
+        s.time = t0;
+        s.epi = kEpiSsp0;
+        s.kout = L->kbuf;
+        s.c_out = dt;
+        s.out = L->buf[SH_NEW];
+        launch_stage(ctx, L, s, ko_order);
+        fill_patch(ctx, L, L->buf[SH_NEW]);
+        /* k1 = f(u1) + k1; u2 = y0 + dt/4 k1 */
+        s.state = L->buf[SH_NEW];
+        s.time = t0 + dt;
+        s.epi = kEpiSspAdd;
+        s.weight = 1.;
+        s.kin[0] = L->kbuf;
+        s.nkin = 1;
+        s.kout = L->kbuf;
+        s.c_out = dt / 4.;
+        s.out = L->buf[2];
+        launch_stage(ctx, L, s, ko_order);
+        fill_patch(ctx, L, L->buf[2]);
+        /* k1 = f(u2) + k1/4; y1 = y0 + 2dt/3 k1 */
+        s.state = L->buf[2];
+        s.time = t0 + dt / 2.;
+        s.weight = 0.25;
+        s.kout = nullptr;
+        s.c_out = dt * 2. / 3.;
+        s.out = L->buf[SH_NEW];
+        launch_stage(ctx, L, s, ko_order);
+        fill_patch(ctx, L, L->buf[SH_NEW]);
+    } else if (type == SH_INTEGRATOR_LEAPFROG) {
+        ensure_kbuf(L, (size_t)L->total_gvol * L->npairs, 1);
+        StageArgs s = a;
+        s.state = L->buf[SH_OLD];
+        s.time = t0;
+        s.epi = kEpiLf0;
+        s.kout = L->kbuf;
+        s.out = L->buf[SH_NEW];
+        launch_stage(ctx, L, s, ko_order);
+        fill_patch(ctx, L, L->buf[SH_NEW]);
+        s.state = L->buf[SH_NEW];
+        s.time = t0 + dt;
+        s.epi = kEpiLf1;
+        s.kin[0] = L->kbuf;
+        s.nkin = 1;
+        s.kout = nullptr;
+        s.out = L->buf[2];
+        launch_stage(ctx, L, s, ko_order);
+        fill_patch(ctx, L, L->buf[2]);
+        std::swap(L->buf[SH_NEW], L->buf[2]);
+    } else if (type >= 0 && type <= 4) {
+        throw ShError(SH_ERR_UNSUPPORTED, "AMReX integrators (types 0-4) are not supported");
+    } else {
+        throw ShError(SH_ERR_ARG, "unknown integrator type " + std::to_string(type));
+    }
+}
+
+void move(sh_ctx *ctx, const sh_level *L, double *buf, double *arr, int layout, int dir) {
+    require(layout == 0 || layout == 1, "layout must be 0 (canonical) or 1 (boxes)");
+    if (layout == 0) {
+        long long dv = 1;
+        for (int d = 0; d < 3; ++d) dv *= (L->dhi[d] - L->dlo[d] + 1);
+        require(dv == L->nvalid, "canonical layout needs boxes covering the whole domain");
+    }
+    const long long work = L->nvalid * L->ncomp;
+    ProfScope ps(ctx, kProfMove);
+    move_kernel<<<grid_for(work), 256, 0, ctx->stream>>>(
+        L->d_boxes, L->d_vbase, (int)L->boxes.size(), L->ncomp, L->nvalid, buf, arr, layout,
+        dir, L->dhi[0] - L->dlo[0] + 1, L->dhi[1] - L->dlo[1] + 1, L->dhi[2] - L->dlo[2] + 1,
+        L->dlo[0], L->dlo[1], L->dlo[2]);
+    ctx->launches++;
+    ck(cudaGetLastError(), "data movement launch");
+}
+
+std::vector<AvgRect> avg_plan(const sh_level *F, const sh_level *C, long long &ncells) {
+    std::vector<AvgRect> r;
+    ncells = 0;
+    for (size_t fb = 0; fb < F->boxes.size(); ++fb) {
+        int clo[3], chi[3];
+        for (int d = 0; d < 3; ++d) {
+            auto cdiv = [](int a) { return a >= 0 ? a / 2 : -((-a + 1) / 2); };
+            clo[d] = cdiv(F->boxes[fb].lo[d]);
+            chi[d] = cdiv(F->boxes[fb].hi[d]);
+        }
+        for (size_t cb = 0; cb < C->boxes.size(); ++cb) {
+            int lo[3], hi[3];
+            if (!box_intersect(clo, chi, C->boxes[cb].lo, C->boxes[cb].hi, lo, hi)) continue;
+            AvgRect a;
+            a.fbox = (int)fb;
+            a.cbox = (int)cb;
+            for (int d = 0; d < 3; ++d) {
+                a.lo[d] = lo[d];
+                a.hi[d] = hi[d];
+            }
+            a.first = ncells;
+            ncells += (long long)(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+            r.push_back(a);
+        }
+    }
+    return r;
+}
+
+void average_down_impl(sh_ctx *ctx, const sh_level *F, const double *fine, const sh_level *C,
+                       double *crse, double *te) {
+    require(F->ncomp == C->ncomp, "fine and coarse levels differ in components");
+    for (const sh_box &b : F->boxes)
+        for (int d = 0; d < 3; ++d)
+            require(b.lo[d] % 2 == 0 && b.hi[d] % 2 != 0 && b.lo[d] >= 0,
+                    "fine boxes must be aligned to the refinement ratio 2");
+    long long ncells = 0;
+    std::vector<AvgRect> plan = avg_plan(F, C, ncells);
+    if (ncells == 0) return;
+    AvgRect *d = (AvgRect *)ctx_scratch(ctx, plan.size() * sizeof(AvgRect));
+    ck(cudaMemcpyAsync(d, plan.data(), plan.size() * sizeof(AvgRect), cudaMemcpyHostToDevice,
+                       ctx->stream),
+       "average-down plan upload");
+    ProfScope ps(ctx, kProfAvg);
+    avgdown_kernel<<<grid_for(ncells), 256, 0, ctx->stream>>>(
+        d, (int)plan.size(), ncells, F->d_boxes, C->d_boxes, F->ncomp, fine, crse, te);
+    ctx->launches++;
+    ck(cudaGetLastError(), "average-down launch");
+    ck(cudaStreamSynchronize(ctx->stream), "average-down");
+}
+
+} // namespace
+
+/* ====================================================================== */
+extern "C" {
+
+int sh_ctx_create(int device, sh_ctx **out) {
+    if (!out) return SH_ERR_ARG;
+    *out = nullptr;
+    sh_ctx *ctx = new (std::nothrow) sh_ctx();
+    if (!ctx) return SH_ERR_NOMEM;
+    ctx->device = device;
+    int rc = guarded(ctx, [&] {
+        int n = 0;
+        ck(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+        require(device >= 0 && device < n, "no such CUDA device");
+        set_device(ctx);
+        ck(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking), "stream create");
+        ctx->stream = ctx->own_stream;
+    });
+    if (rc != SH_OK) {
+        std::fprintf(stderr, "sh_ctx_create: %s\n", ctx->err.c_str());
+        delete ctx;
+        return rc;
+    }
+    *out = ctx;
+    return SH_OK;
+}
+
+int sh_ctx_destroy(sh_ctx *ctx) {
+    if (!ctx) return SH_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    cudaFree(ctx->scratch);
+    ctx->gw.release();
+    for (const ProfRecord &r : ctx->prof) {
+        cudaEventDestroy(r.start);
+        cudaEventDestroy(r.stop);
+    }
+    for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+    return SH_OK;
+}
+
+const char *sh_ctx_last_error(const sh_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int sh_ctx_set_stream(sh_ctx *ctx, void *s) {
+    if (!ctx) return SH_ERR_ARG;
+    ctx->stream = s ? (cudaStream_t)s : ctx->own_stream;
+    return SH_OK;
+}
+
+void *sh_ctx_stream(sh_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+int sh_ctx_synchronize(sh_ctx *ctx) {
+    if (!ctx) return SH_ERR_ARG;
+    return guarded(ctx, [&] { ck(cudaStreamSynchronize(ctx->stream), "synchronize"); });
+}
+
+long long sh_ctx_kernel_launches(const sh_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+int sh_ctx_profile(sh_ctx *ctx, int enable) {
+    if (!ctx) return SH_ERR_ARG;
+    return guarded(ctx, [&] {
+        set_device(ctx);
+        profile_resolve(ctx);
+        if (enable) {
+            for (int c = 0; c < kProfCount; ++c) {
+                ctx->prof_ms[c] = 0;
+                ctx->prof_n[c] = 0;
+            }
+        }
+        ctx->profiling = enable != 0;
+    });
+}
+
+int sh_ctx_profile_read(sh_ctx *ctx, const char *category, double *total_ms,
+                        long long *launches) {
+    if (!ctx || !category) return SH_ERR_ARG;
+    return guarded(ctx, [&] {
+        set_device(ctx);
+        profile_resolve(ctx);
+        for (int c = 0; c < kProfCount; ++c)
+            if (std::strcmp(kProfCategories[c], category) == 0) {
+                if (total_ms) *total_ms = ctx->prof_ms[c];
+                if (launches) *launches = ctx->prof_n[c];
+                return;
+            }
+        throw ShError(SH_ERR_ARG, std::string("unknown profile category ") + category);
+    });
+}
+
+int sh_project_count(void) { return project_count(); }
+
+const char *sh_project_name(int id) {
+    const ProjectOps *p = project_by_id(id);
+    return p ? p->name : nullptr;
+}
+
+int sh_project_find(const char *name, int *id) {
+    if (!name || !id) return SH_ERR_ARG;
+    for (int q = 0; q < project_count(); ++q)
+        if (std::strcmp(project_by_id(q)->name, name) == 0) {
+            *id = q;
+            return SH_OK;
+        }
+    return SH_ERR_PROJECT;
+}
+
+int sh_project_ncomp(int id, int with_gw, int *ncomp, int *npairs) {
+    const ProjectOps *p = project_by_id(id);
+    if (!p) return SH_ERR_PROJECT;
+    if (with_gw && !p->has_gw) return SH_ERR_UNSUPPORTED;
+    if (ncomp) *ncomp = p->nscalars + (with_gw ? 12 : 0);
+    if (npairs) *npairs = p->nscalars / 2 + (with_gw ? 6 : 0);
+    return SH_OK;
+}
+
+int sh_level_create(sh_ctx *ctx, int project, int with_gw, const int domain_lo[3],
+                    const int domain_hi[3], const sh_box *boxes, int nbox, int nghost,
+                    sh_level **out) {
+    if (!ctx || !out) return SH_ERR_ARG;
+    *out = nullptr;
+    sh_level *L = new (std::nothrow) sh_level();
+    if (!L) return SH_ERR_NOMEM;
+    int rc = guarded(ctx, [&] {
+        set_device(ctx);
+        L->ops = project_by_id(project);
+        if (!L->ops) throw ShError(SH_ERR_PROJECT, "unknown project id");
+        if (with_gw && !L->ops->has_gw)
+            throw ShError(SH_ERR_UNSUPPORTED, "project has no gravitational-wave hooks");
+        require(boxes && nbox > 0 && domain_lo && domain_hi, "boxes and domain required");
+        require(nghost >= L->ops->reach && nghost <= 8,
+                "nghost must cover the project's stencil reach and be at most 8");
+        L->project = project;
+        L->with_gw = with_gw != 0;
+        L->ncomp = L->ops->nscalars + (L->with_gw ? 12 : 0);
+        L->npairs = L->ops->nscalars / 2 + (L->with_gw ? 6 : 0);
+        require(L->ncomp <= kMaxComp, "too many components");
+        L->nghost = nghost;
+        for (int d = 0; d < 3; ++d) {
+            L->dlo[d] = domain_lo[d];
+            L->dhi[d] = domain_hi[d];
+            require(domain_hi[d] >= domain_lo[d], "empty domain");
+        }
+        L->boxes.assign(boxes, boxes + nbox);
+        long long base = 0, vb = 0;
+        std::vector<TileDev> tiles;
+        L->vbase.push_back(0);
+        for (int b = 0; b < nbox; ++b) {
+            BoxDev bd;
+            std::memset(&bd, 0, sizeof(bd));
+            bd.off = base;
+            long long gv = 1;
+            for (int d = 0; d < 3; ++d) {
+                require(boxes[b].hi[d] >= boxes[b].lo[d], "empty box");
+                require(boxes[b].lo[d] >= domain_lo[d] && boxes[b].hi[d] <= domain_hi[d],
+                        "box outside the domain");
+                bd.lo[d] = boxes[b].lo[d];
+                bd.hi[d] = boxes[b].hi[d];
+                bd.glo[d] = boxes[b].lo[d] - nghost;
+                bd.gdim[d] = boxes[b].hi[d] - boxes[b].lo[d] + 1 + 2 * nghost;
+                gv *= bd.gdim[d];
+            }
+            bd.gvol = gv;
+            base += gv;
+            const long long nv = (long long)(bd.hi[0] - bd.lo[0] + 1) *
+                                 (bd.hi[1] - bd.lo[1] + 1) * (bd.hi[2] - bd.lo[2] + 1);
+            vb += nv;
+            L->vbase.push_back(vb);
+            L->hboxes.push_back(bd);
+            for (int z = bd.lo[2]; z <= bd.hi[2]; z += kTileZ)
+                for (int y = bd.lo[1]; y <= bd.hi[1]; y += kTileY)
+                    for (int x = bd.lo[0]; x <= bd.hi[0]; x += kTileX)
+                        tiles.push_back(TileDev{b, x, y, z});
+        }
+        L->total_gvol = base;
+        L->nvalid = vb;
+        L->ntiles = (int)tiles.size();
+        L->d_boxes = (BoxDev *)dmalloc(L->hboxes.size() * sizeof(BoxDev), "box table");
+        ck(cudaMemcpy(L->d_boxes, L->hboxes.data(), L->hboxes.size() * sizeof(BoxDev),
+                      cudaMemcpyHostToDevice),
+           "box table upload");
+        L->d_tiles = (TileDev *)dmalloc(tiles.size() * sizeof(TileDev), "tile table");
+        ck(cudaMemcpy(L->d_tiles, tiles.data(), tiles.size() * sizeof(TileDev),
+                      cudaMemcpyHostToDevice),
+           "tile table upload");
+        L->d_vbase = (long long *)dmalloc(L->vbase.size() * sizeof(long long), "box prefix");
+        ck(cudaMemcpy(L->d_vbase, L->vbase.data(), L->vbase.size() * sizeof(long long),
+                      cudaMemcpyHostToDevice),
+           "box prefix upload");
+        build_ghost_plan(L);
+        const size_t bytes = (size_t)L->total_gvol * L->ncomp * sizeof(double);
+        for (int q = 0; q < 3; ++q) {
+            L->buf[q] = (double *)dmalloc(bytes, "level buffer");
+            ck(cudaMemsetAsync(L->buf[q], 0, bytes, ctx->stream), "level buffer clear");
+        }
+        ck(cudaStreamSynchronize(ctx->stream), "level create");
+    });
+    if (rc != SH_OK) {
+        level_free(L);
+        delete L;
+        return rc;
+    }
+    *out = L;
+    return SH_OK;
+}
+
+int sh_level_destroy(sh_ctx *ctx, sh_level *L) {
+    if (!ctx || !L) return SH_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    level_free(L);
+    delete L;
+    return SH_OK;
+}
+
+int sh_level_info(const sh_level *L, int *ncomp, int *nbox, long long *nvalid) {
+    if (!L) return SH_ERR_ARG;
+    if (ncomp) *ncomp = L->ncomp;
+    if (nbox) *nbox = (int)L->boxes.size();
+    if (nvalid) *nvalid = L->nvalid;
+    return SH_OK;
+}
+
+int sh_level_time(const sh_level *L, int which, double *t, int *istep) {
+    if (!L || (which != SH_NEW && which != SH_OLD)) return SH_ERR_ARG;
+    if (t) *t = L->t[which];
+    if (istep) *istep = L->istep[which];
+    return SH_OK;
+}
+
+int sh_level_set_time(sh_level *L, int which, double t, int istep) {
+    if (!L || (which != SH_NEW && which != SH_OLD)) return SH_ERR_ARG;
+    L->t[which] = t;
+    L->istep[which] = istep;
+    return SH_OK;
+}
+
+int sh_level_write(sh_ctx *ctx, sh_level *L, int which, int layout, const double *host) {
+    if (!ctx || !L || !host || (which != SH_NEW && which != SH_OLD)) return SH_ERR_ARG;
+    return guarded(ctx, [&] {
+        set_device(ctx);
+        const size_t bytes = (size_t)L->nvalid * L->ncomp * sizeof(double);
+        double *stage = (double *)ctx_scratch(ctx, bytes);
+        ck(cudaMemcpyAsync(stage, host, bytes, cudaMemcpyHostToDevice, ctx->stream), "upload");
+        move(ctx, L, L->buf[which], stage, layout, 0);
+        ck(cudaStreamSynchronize(ctx->stream), "upload");
+    });
+}
+
+int sh_level_read(sh_ctx *ctx, const sh_level *L, int which, int layout, double *host) {
+    if (!ctx || !L || !host || (which != SH_NEW && which != SH_OLD)) return SH_ERR_ARG;
+    return guarded(ctx, [&] {
+        set_device(ctx);
+        const size_t bytes = (size_t)L->nvalid * L->ncomp * sizeof(double);
+        double *stage = (double *)ctx_scratch(ctx, bytes);
+        move(ctx, L, L->buf[which], stage, layout, 1);
+        ck(cudaMemcpyAsync(host, stage, bytes, cudaMemcpyDeviceToHost, ctx->stream), "download");
+        ck(cudaStreamSynchronize(ctx->stream), "download");
+    });
+}
+
+int sh_level_write_device(sh_ctx *ctx, sh_level *L, int which, int layout, const double *dev) {
+    if (!ctx || !L || !dev || (which != SH_NEW && which != SH_OLD)) return SH_ERR_ARG;
+    return guarded(ctx, [&] {
+        set_device(ctx);
+        move(ctx, L, L->buf[which], const_cast<double *>(dev), layout, 0);
+    });
+}
+
+int sh_level_read_device(sh_ctx *ctx, const sh_level *L, int which, int layout, double *dev) {
+    if (!ctx || !L || !dev || (which != SH_NEW && which != SH_OLD)) return SH_ERR_ARG;
+    return guarded(ctx, [&] {
+        set_device(ctx);
+        move(ctx, L, L->buf[which], dev, layout, 1);
+    });
+}
+
+int sh_level_fill_patch(sh_ctx *ctx, sh_level *L, int which) {
+    if (!ctx || !L || (which != SH_NEW && which != SH_OLD)) return SH_ERR_ARG;
+    return guarded(ctx, [&] {
+        set_device(ctx);
+        fill_patch(ctx, L, L->buf[which]);
+    });
+}
+
+int sh_level_advance(sh_ctx *ctx, sh_level *L, int integrator, const double *tableau,
+                     int nstages, double dt, double dx, const double *params, int nparams,
+                     const double *gw_params, int ngw, int ko_order, const double *ko_strength,
+                     int flags) {
+    if (!ctx || !L) return SH_ERR_ARG;
+    return guarded(ctx, [&] {
+        set_device(ctx);
+        require(dt > 0 && dx > 0, "dt and dx must be positive");
+        if (!(flags & SH_ADVANCE_NO_SWAP)) {
+            std::swap(L->buf[SH_NEW], L->buf[SH_OLD]);
+            std::swap(L->t[SH_NEW], L->t[SH_OLD]);
+            std::swap(L->istep[SH_NEW], L->istep[SH_OLD]);
+        }
+        fill_patch(ctx, L, L->buf[SH_OLD]);
+        integrate(ctx, L, integrator, tableau, nstages, dt, dx, params, nparams, gw_params, ngw,
+                  ko_order, ko_strength);
+        L->t[SH_NEW] = L->t[SH_OLD] + dt;
+        L->istep[SH_NEW] = L->istep[SH_OLD] + 1;
+        ck(cudaGetLastError(), "advance");
+    });
+}
+
+int sh_level_rhs(sh_ctx *ctx, sh_level *L, int which, double time, int lev, double dt,
+                 double dx, const double *params, int nparams, const double *gw_params, int ngw,
+                 int ko_order, const double *ko_strength, double *host_rhs) {
+    if (!ctx || !L || !host_rhs || (which != SH_NEW && which != SH_OLD)) return SH_ERR_ARG;
+    return guarded(ctx, [&] {
+        set_device(ctx);
+        StageArgs a;
+        fill_common(a, L, dt, dx, params, nparams, gw_params, ngw, ko_order, ko_strength);
+        a.state = L->buf[which];
+        a.out = L->buf[2];
+        a.epi = kEpiPlainRhs;
+        a.time = time;
+        a.lev = lev;
+        launch_stage(ctx, L, a, ko_order);
+        const size_t bytes = (size_t)L->nvalid * L->ncomp * sizeof(double);
+        double *stage = (double *)ctx_scratch(ctx, bytes);
+        move(ctx, L, L->buf[2], stage, 1, 1);
+        ck(cudaMemcpyAsync(host_rhs, stage, bytes, cudaMemcpyDeviceToHost, ctx->stream),
+           "download");
+        ck(cudaStreamSynchronize(ctx->stream), "rhs");
+    });
+}
+
+int sh_average_down(sh_ctx *ctx, const sh_level *F, int which_f, sh_level *C, int which_c) {
+    if (!ctx || !F || !C) return SH_ERR_ARG;
+    if ((which_f != SH_NEW && which_f != SH_OLD) || (which_c != SH_NEW && which_c != SH_OLD))
+        return SH_ERR_ARG;
+    return guarded(ctx, [&] {
+        set_device(ctx);
+        average_down_impl(ctx, F, F->buf[which_f], C, C->buf[which_c], nullptr);
+    });
+}
+
+int sh_average_down_te(sh_ctx *ctx, sh_level *F, sh_level *C) {
+    if (!ctx || !F || !C) return SH_ERR_ARG;
+    return guarded(ctx, [&] {
+        set_device(ctx);
+        average_down_impl(ctx, F, F->buf[SH_NEW], C, C->buf[SH_NEW], F->buf[SH_OLD]);
+    });
+}
+
+int sh_tag(sh_ctx *ctx, sh_level *L, int use_te, double time, int lev, double dt, double dx,
+           const double *te_crit, const double *params_tag, int nparams_tag,
+           const double *params_mod, int nparams_mod, uint8_t *mask_out, long long *counts_out,
+           int32_t *list_out, long long list_capacity, long long *ntagged) {
+    if (!ctx || !L || !mask_out) return SH_ERR_ARG;
+    return guarded(ctx, [&] {
+        set_device(ctx);
+        require(L->nghost >= 1, "tagging reads the +1 neighbours: nghost >= 1");
+        require(nparams_tag >= 0 && nparams_tag <= kMaxParams, "at most 32 tag parameters");
+        require(nparams_mod >= 0 && nparams_mod <= kMaxComp, "at most 32 modifier parameters");
+        require(!use_te || te_crit, "te_crit required with truncation errors");
+        require(L->nvalid < (1LL << 31), "tag list indices are 32-bit");
+        TagArgs a;
+        std::memset(&a, 0, sizeof(a));
+        a.boxes = L->d_boxes;
+        a.tiles = L->d_tiles;
+        a.state = L->buf[SH_NEW];
+        a.te = use_te ? L->buf[SH_OLD] : nullptr;
+        a.ncomp = L->ncomp;
+        a.lev = lev;
+        a.time = time;
+        a.dt = dt;
+        a.dx = dx;
+        for (int n = 0; n < L->ncomp; ++n) a.te_crit[n] = use_te ? te_crit[n] : 0.0;
+        for (int q = 0; q < nparams_tag; ++q) a.params_tag[q] = params_tag[q];
+        for (int q = 0; q < nparams_mod; ++q) a.params_mod[q] = params_mod[q];
+        const int nbox = (int)L->boxes.size();
+        const long long nchunks = (L->nvalid + kChunk - 1) / kChunk;
+        /* scratch: mask | mask offsets | counts | chunk counts | chunk bases | total | list */
+        size_t off = 0;
+        auto carve = [&](size_t bytes) {
+            size_t o = off;
+            off += (bytes + 255) & ~size_t(255);
+            return o;
+        };
+        const size_t o_mask = carve(L->nvalid);
+        const size_t o_moff = carve(nbox * sizeof(long long));
+        const size_t o_cnt = carve((2 + kMaxComp) * sizeof(unsigned long long));
+        const size_t o_cc = carve(nchunks * sizeof(int));
+        const size_t o_cb = carve(nchunks * sizeof(long long));
+        const size_t o_tot = carve(sizeof(long long));
+        const size_t o_list = carve((list_out ? std::max<long long>(list_capacity, 1) : 1) *
+                                    sizeof(int));
+        char *base = (char *)ctx_scratch(ctx, off);
+        a.mask = (unsigned char *)(base + o_mask);
+        a.mask_off = (const long long *)(base + o_moff);
+        a.counts = (unsigned long long *)(base + o_cnt);
+        ck(cudaMemcpyAsync(base + o_moff, L->vbase.data(), nbox * sizeof(long long),
+                           cudaMemcpyHostToDevice, ctx->stream),
+           "mask offsets");
+        ck(cudaMemsetAsync(a.counts, 0, (2 + kMaxComp) * sizeof(unsigned long long), ctx->stream),
+           "count clear");
+        ProfScope ps(ctx, kProfTag);
+        ck(L->ops->launch_tag(a, L->ntiles, ctx->stream), "tag launch");
+        ctx->launches++;
+        int *cc = (int *)(base + o_cc);
+        long long *cb = (long long *)(base + o_cb);
+        long long *tot = (long long *)(base + o_tot);
+        int *list = (int *)(base + o_list);
+        tag_count_kernel<<<(unsigned)nchunks, 256, 0, ctx->stream>>>(a.mask, L->nvalid, cc);
+        tag_scan_kernel<<<1, 1024, 0, ctx->stream>>>(cc, (int)nchunks, cb, tot);
+        ctx->launches += 2;
+        if (list_out && list_capacity > 0) {
+            tag_write_kernel<<<(unsigned)nchunks, 256, 0, ctx->stream>>>(a.mask, L->nvalid, cb,
+                                                                         list, list_capacity);
+            ctx->launches++;
+        }
+        ck(cudaGetLastError(), "tag compaction launch");
+        ck(cudaMemcpyAsync(mask_out, a.mask, L->nvalid, cudaMemcpyDeviceToHost, ctx->stream),
+           "mask download");
+        unsigned long long counts[2 + kMaxComp];
+        ck(cudaMemcpyAsync(counts, a.counts, sizeof(counts), cudaMemcpyDeviceToHost, ctx->stream),
+           "count download");
+        long long total = 0;
+        ck(cudaMemcpyAsync(&total, tot, sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream),
+           "tag total download");
+        ck(cudaStreamSynchronize(ctx->stream), "tag");
+        if (list_out && list_capacity > 0) {
+            const long long nl = std::min(total, list_capacity);
+            ck(cudaMemcpy(list_out, list, nl * sizeof(int), cudaMemcpyDeviceToHost),
+               "tag list download");
+        }
+        if (ntagged) *ntagged = total;
+        if (counts_out)
+            for (int n = 0; n < 2 + L->ncomp; ++n) counts_out[n] = (long long)counts[n];
+    });
+}
+
+int sh_gw_spectrum(sh_ctx *ctx, const sh_level *L, const int *comps, int zero_padding,
+                   int projection_type, int unbinned, double *bins_out, long long *ks_out,
+                   int max_bins, int *nbins) {
+    if (!ctx || !L || !bins_out || !nbins) return SH_ERR_ARG;
+    return guarded(ctx, [&] {
+        set_device(ctx);
+        require(L->with_gw || comps, "level has no GW components; pass comps");
+        require(zero_padding >= 1, "zero_padding must be >= 1");
+        require(projection_type >= 1 && projection_type <= 3, "projection_type must be 1..3");
+        const int N = L->dhi[0] - L->dlo[0] + 1;
+        long long dv = 1;
+        for (int d = 0; d < 3; ++d) {
+            require(L->dhi[d] - L->dlo[d] + 1 == N, "spectrum needs a cubic domain");
+            dv *= N;
+        }
+        require(dv == L->nvalid, "spectrum needs a level covering its whole domain");
+        require((N * zero_padding) % 2 == 0, "spectrum grid size must be even");
+        int c6[6];
+        const int ns = L->ops->nscalars;
+        const int dflt[6] = {ns + 6, ns + 9, ns + 10, ns + 7, ns + 11, ns + 8};
+        for (int q = 0; q < 6; ++q) {
+            c6[q] = comps ? comps[q] : dflt[q];
+            require(c6[q] >= 0 && c6[q] < L->ncomp, "component index out of range");
+        }
+        const size_t sbytes = gw_scratch_bytes(N, zero_padding);
+        const int P = N * zero_padding;
+        const size_t maxbins = (size_t)3 * (P / 2 + 1) * (P / 2 + 1) + 16;
+        char *base = (char *)ctx_scratch(ctx, sbytes + maxbins * sizeof(double) + 256);
+        double *bins_dev = (double *)(base + ((sbytes + 255) & ~size_t(255)));
+        int nb = 0;
+        std::string err;
+        ProfScope ps(ctx, kProfGw);
+        cudaError_t e = gw_spectrum_device(ctx->gw, ctx->stream, L->d_boxes, L->d_vbase,
+                                           (int)L->boxes.size(), L->nvalid, L->ncomp,
+                                           L->buf[SH_NEW], c6, N, L->dlo, zero_padding,
+                                           projection_type, unbinned, (double *)base, bins_dev,
+                                           &nb, &ctx->launches, err);
+        if (!err.empty()) throw ShError(SH_ERR_CUDA, err);
+        ck(e, "gw spectrum");
+        *nbins = nb;
+        require(nb <= max_bins, "bins_out too small");
+        ck(cudaMemcpyAsync(bins_out, bins_dev, nb * sizeof(double), cudaMemcpyDeviceToHost,
+                           ctx->stream),
+           "spectrum download");
+        ck(cudaStreamSynchronize(ctx->stream), "gw spectrum");
+        if (ks_out) std::copy(ctx->gw.ks.begin(), ctx->gw.ks.end(), ks_out);
+    });
+}
+
+int sh_evolve_periodic(sh_ctx *ctx, int project, int integrator, const double *tableau,
+                       int nstages, int N, int max_grid, int nghost, int ncomp, int with_gw,
+                       const double *state_in, const double *init_new, double *state_out,
+                       double t0, double dt, double dx, int nsteps, const double *params,
+                       int nparams, const double *gw_params, int ngw, int ko_order,
+                       const double *ko_strength) {
+    if (!ctx || !state_in || !state_out || N <= 0 || nsteps < 0) return SH_ERR_ARG;
+    int nc = 0;
+    int rc = sh_project_ncomp(project, with_gw, &nc, nullptr);
+    if (rc != SH_OK) return rc;
+    if (nc != ncomp) {
+        ctx->err = "ncomp does not match the project";
+        return SH_ERR_ARG;
+    }
+    std::vector<sh_box> boxes;
+    const int mg = (max_grid <= 0 || max_grid >= N) ? N : max_grid;
+    for (int z = 0; z < N; z += mg)
+        for (int y = 0; y < N; y += mg)
+            for (int x = 0; x < N; x += mg)
+                boxes.push_back(sh_box{{x, y, z},
+                                       {std::min(x + mg, N) - 1, std::min(y + mg, N) - 1,
+                                        std::min(z + mg, N) - 1}});
+    const int dlo[3] = {0, 0, 0}, dhi[3] = {N - 1, N - 1, N - 1};
+    sh_level *L = nullptr;
+    rc = sh_level_create(ctx, project, with_gw, dlo, dhi, boxes.data(), (int)boxes.size(), nghost,
+                         &L);
+    if (rc != SH_OK) return rc;
+    rc = sh_level_write(ctx, L, SH_NEW, 0, state_in);
+    if (rc == SH_OK && init_new) rc = sh_level_write(ctx, L, SH_OLD, 0, init_new);
+    if (rc == SH_OK) sh_level_set_time(L, SH_NEW, t0, 0);
+    for (int s = 0; s < nsteps && rc == SH_OK; ++s)
+        rc = sh_level_advance(ctx, L, integrator, tableau, nstages, dt, dx, params, nparams,
+                              gw_params, ngw, ko_order, ko_strength, 0);
+    if (rc == SH_OK) rc = sh_level_read(ctx, L, SH_NEW, 0, state_out);
+    sh_level_destroy(ctx, L);
+    return rc;
+}
+
+} /* extern "C" */

@@ -1,0 +1,163 @@
+"""ctypes access to the ORACLE libraries (test infrastructure only).
+
+Oracle()            -> oracle/_build/liboracle.so, the CPU restatement
+Oracle(ref=True)    -> oracle/_ref/libshref.so, the same drivers around the
+                       reference's own per-cell headers (only where the
+                       sledgehamr sources were present to build it)
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_SO = os.path.join(ROOT, "oracle", "_build", "liboracle.so")
+REF_SO = os.path.join(ROOT, "oracle", "_ref", "libshref.so")
+
+PROJECT_IDS = {"AxionStrings": 0, "MinimalExample": 1, "NextToMinimalExample": 2,
+               "FirstOrderPhaseTransition": 3, "AxionStringsLap1": 4, "AxionStringsLap2": 5,
+               "AxionStringsLap3": 6}
+
+vp = C.c_void_p
+
+
+def _p(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def _f(a):
+    return None if a is None else np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+
+
+def build_oracle():
+    if not os.path.exists(ORACLE_SO):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+class Oracle:
+    def __init__(self, ref: bool = False):
+        if ref:
+            if not ref_available():
+                raise FileNotFoundError(REF_SO)
+            self.lib = C.CDLL(REF_SO)
+            self.pre = "ref_"
+        else:
+            build_oracle()
+            self.lib = C.CDLL(ORACLE_SO)
+            self.pre = "orc_"
+
+    def _fn(self, name):
+        f = getattr(self.lib, self.pre + name)
+        f.restype = C.c_int
+        return f
+
+    def evolve_periodic(self, project, integrator, state, t0, dt, dx, nsteps, params=(),
+                        gw_params=(), with_gw=False, nghost=2, max_grid=0, tableau=None,
+                        init_new=None, ko_order=0, ko_strength=None):
+        st = _f(state)
+        out = np.empty_like(st)
+        tab = _f(tableau)
+        nst = 0
+        if tableau is not None:
+            for s in range(1, 9):
+                if tab.size == 3 * s + s * (s + 1) // 2:
+                    nst = s
+        p = _f(list(params) or [0.0])
+        g = _f(list(gw_params) or [0.0])
+        rc = self._fn("evolve_periodic")(
+            PROJECT_IDS[project], integrator, _p(tab), nst, st.shape[-1], max_grid, nghost,
+            st.shape[0], int(with_gw), _p(st), _p(_f(init_new)), _p(out), C.c_double(t0),
+            C.c_double(dt), C.c_double(dx), nsteps, _p(p), len(params), _p(g), len(gw_params),
+            ko_order, _p(_f(ko_strength)))
+        if rc != 0:
+            raise RuntimeError(f"{self.pre}evolve_periodic rc={rc}")
+        return out
+
+    def fill_rhs(self, project, state, time, lev, dt, dx, params=(), gw_params=(),
+                 with_gw=False, nghost=3, ko_order=0, ko_strength=None, rhs_init=None):
+        st = _f(state)
+        out = np.zeros_like(st) if rhs_init is None else _f(rhs_init).copy()
+        p = _f(list(params) or [0.0])
+        g = _f(list(gw_params) or [0.0])
+        rc = self._fn("fill_rhs")(PROJECT_IDS[project], st.shape[-1], nghost, st.shape[0],
+                                  int(with_gw), _p(st), _p(out), C.c_double(time), lev,
+                                  C.c_double(dt), C.c_double(dx), _p(p), _p(g), ko_order,
+                                  _p(_f(ko_strength)))
+        if rc != 0:
+            raise RuntimeError(f"fill_rhs rc={rc}")
+        return out
+
+    def avgdown_te(self, fine, crse, te):
+        f, c, t = _f(fine), _f(crse).copy(), _f(te).copy()
+        rc = self._fn("avgdown_te")(f.shape[0], c.shape[-1], _p(f), _p(c), _p(t))
+        if rc != 0:
+            raise RuntimeError("avgdown_te")
+        return c, t
+
+    def average_down(self, fine):
+        f = _f(fine)
+        Nc = f.shape[-1] // 2
+        c = np.zeros((f.shape[0], Nc, Nc, Nc))
+        rc = self._fn("average_down")(f.shape[0], Nc, _p(f), _p(c))
+        if rc != 0:
+            raise RuntimeError("average_down")
+        return c
+
+    def tag(self, project, state, te, time, lev, dt, dx, te_crit=None, params_tag=(),
+            params_mod=(), max_grid=0):
+        st = _f(state)
+        ncomp, N = st.shape[0], st.shape[-1]
+        mask = np.zeros((N, N, N), dtype=np.uint8)
+        counts = np.zeros(2 + ncomp, dtype=np.int64)
+        pt = _f(list(params_tag) or [0.0])
+        pm = _f(list(params_mod) or [0.0])
+        tc = _f(te_crit) if te_crit is not None else _f(np.full(ncomp, np.finfo(float).max))
+        rc = self._fn("tag")(PROJECT_IDS[project], N, max_grid, ncomp, _p(st), _p(_f(te)),
+                             C.c_double(time), lev, C.c_double(dt), C.c_double(dx), _p(tc),
+                             _p(pt), _p(pm), _p(mask), C.c_void_p(counts.ctypes.data))
+        if rc != 0:
+            raise RuntimeError(f"tag rc={rc}")
+        return mask, counts
+
+    def gw_spectrum(self, comps6, zero_padding=1, projection_type=2, unbinned=True):
+        c = _f(comps6)
+        N = c.shape[-1]
+        P = N * zero_padding
+        cap = 3 * (P // 2 + 1) ** 2 + 16
+        bins = np.empty(cap)
+        ks = np.empty(cap, dtype=np.int64)
+        nb = C.c_int()
+        rc = self._fn("gw_spectrum")(_p(c), N, zero_padding, projection_type, int(unbinned),
+                                     _p(bins), _p(ks), cap, C.byref(nb))
+        if rc != 0:
+            raise RuntimeError("gw_spectrum")
+        return bins[: nb.value].copy(), ks[: nb.value].copy()
+
+    def unique_k2(self, dim):
+        cap = 3 * (dim // 2 + 1) ** 2 + 16
+        out = np.empty(cap, dtype=np.int64)
+        n = C.c_int()
+        rc = self._fn("unique_k2")(dim, _p(out), cap, C.byref(n))
+        if rc != 0:
+            raise RuntimeError("unique_k2")
+        return out[: n.value].copy()
+
+    def index_to_k(self, dim, projection_type):
+        out = np.empty(dim)
+        self._fn("index_to_k")(dim, projection_type, _p(out))
+        return out
+
+    def stencil(self, kind, order, field, dx):
+        f = _f(field)
+        out = np.empty_like(f)
+        rc = self._fn("stencil")(kind, order, f.shape[-1], _p(f), C.c_double(dx), _p(out))
+        if rc != 0:
+            raise RuntimeError("stencil")
+        return out
