@@ -1,0 +1,106 @@
+"""The reference's unmodified project kernel headers compile against this
+library's plugin shim (include/sledgehamr) with g++ and with nvcc for
+sm_103a, and their hooks, called through the shim's Array4, agree with this
+library's restated projects.  Skipped where the sledgehamr sources are
+absent."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from tests.conftest import ROOT
+
+REF = "/root/reference"
+pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "projects")),
+                                reason="sledgehamr sources not present")
+
+TU = r'''
+#include <sledgehamr.h>
+#include "AxionStrings/setup.h"
+#include "AxionStrings/kernels_rhs.h"
+#include "AxionStrings/kernels_tagging.h"
+namespace AxionStrings { SLEDGEHAMR_FINISH_SETUP }
+#include "FirstOrderPhaseTransition/setup.h"
+#include "FirstOrderPhaseTransition/kernels_rhs.h"
+#include "FirstOrderPhaseTransition/kernels_tagging.h"
+namespace FirstOrderPhaseTransition { SLEDGEHAMR_FINISH_SETUP }
+#include "MinimalExample/MinimalExample.h"
+#include <cstdio>
+#ifndef __CUDACC__
+int main() {
+    const int N = 8, g = 2, M = N + 2 * g;
+    static double st[4 * M * M * M];
+    unsigned long long x = 12345;
+    for (double &v : st) { x = x * 6364136223846793005ULL + 1442695040888963407ULL;
+                           v = (double)(x >> 11) / 9007199254740992.0 - 0.5; }
+    amrex::Array4<const double> s(st, amrex::Dim3{-g, -g, -g}, amrex::Dim3{N + g, N + g, N + g}, 4);
+    for (int k = 0; k < N; ++k) for (int j = 0; j < N; ++j) for (int i = 0; i < N; ++i) {
+        double r[4];
+        amrex::Array4<double> rhs(r, 0, 0, 1, amrex::Dim3{i, j, k}, amrex::Dim3{i + 1, j + 1, k + 1}, 4);
+        AxionStrings::ShHooks::rhs(rhs, s, i, j, k, 0, 1.3, 0.1, 0.25, nullptr);
+        int tag = AxionStrings::ShHooks::tag(s, i, j, k, 0, 1.3, 0.1, 0.25, nullptr);
+        std::printf("%.17g %.17g %.17g %.17g %d\n", r[0], r[1], r[2], r[3], tag);
+    }
+    MinimalExample::MinimalExample m;
+    return m.scalar_fields.size() == 4 ? 0 : 1;
+}
+#endif
+'''
+
+
+def _build(tmp, compiler, ext, extra):
+    src = tmp / ("dropin" + ext)
+    src.write_text(TU)
+    inc = ["-I" + os.path.join(ROOT, "include", "sledgehamr"), "-I" + os.path.join(REF, "projects")]
+    out = tmp / ("dropin_" + compiler)
+    cmd = [compiler] + extra + inc + [str(src), "-o", str(out)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    return out
+
+
+def test_reference_project_headers_compile_with_gxx_and_run(tmp_path, oracle):
+    exe = _build(tmp_path, "g++", ".cpp", ["-std=c++17", "-O2", "-ffp-contract=off"])
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0
+    vals = np.array([[float(v) for v in line.split()] for line in r.stdout.strip().splitlines()])
+    assert vals.shape == (512, 5)
+    # the same cells through the oracle's restatement of AxionStrings
+    N, g = 8, 2
+    M = N + 2 * g
+    x = 12345
+    st = np.empty(4 * M ** 3)
+    for q in range(st.size):
+        x = (x * 6364136223846793005 + 1442695040888963407) % (1 << 64)
+        st[q] = (x >> 11) / 9007199254740992.0 - 0.5
+    st = st.reshape(4, M, M, M)[:, g:-g, g:-g, g:-g]
+    # periodicity is not assumed: compare the interior cells only, where the
+    # 13-point stencil stays inside the 8^3 block
+    rhs = oracle.fill_rhs("AxionStrings", st, 1.3, 0, 0.1, 0.25, nghost=3)
+    got = vals[:, :4].T.reshape(4, N, N, N)
+    inner = (slice(None), slice(2, -2), slice(2, -2), slice(2, -2))
+    assert np.allclose(got[inner], rhs[inner], rtol=1e-13, atol=1e-13)
+
+
+@pytest.mark.skipif(shutil.which("nvcc") is None and not os.path.exists("/usr/local/cuda/bin/nvcc"),
+                    reason="nvcc absent")
+def test_reference_project_headers_compile_with_nvcc(tmp_path):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    src = tmp_path / "dropin.cu"
+    src.write_text(TU + r'''
+template <class H>
+__global__ void k(const amrex::Array4<const double> s, double *out) {
+    double r[H::kNScalars];
+    amrex::Array4<double> rhs(r, 0, 0, 1, amrex::Dim3{2, 2, 2}, amrex::Dim3{3, 3, 3}, H::kNScalars);
+    H::rhs(rhs, s, 2, 2, 2, 0, 1.0, 0.1, 0.25, nullptr);
+    out[0] = r[H::kNScalars - 1] + H::tag(s, 2, 2, 2, 0, 1.0, 0.1, 0.25, nullptr);
+}
+template __global__ void k<AxionStrings::ShHooks>(const amrex::Array4<const double>, double *);
+''')
+    inc = ["-I" + os.path.join(ROOT, "include", "sledgehamr"), "-I" + os.path.join(REF, "projects")]
+    r = subprocess.run([nvcc, "-std=c++17", "--expt-relaxed-constexpr", "-gencode",
+                        "arch=compute_103a,code=sm_103a", "-c", str(src), "-o",
+                        str(tmp_path / "dropin.o")] + inc, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
