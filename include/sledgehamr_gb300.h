@@ -197,6 +197,25 @@ SH_API int sh_tag(sh_ctx *ctx, sh_level *level, int use_te, double time, int lev
            long long *counts_out, int32_t *list_out, long long list_capacity,
            long long *ntagged);
 
+/* Same tagging as sh_tag, for callers that must not allocate GPU memory:
+ * hosts that hand out all device memory through their own pool or
+ * allocator, or that cannot afford the device-wide synchronisation a
+ * cudaMalloc/cudaFree implies in the middle of a step.  This entry point has
+ * no counterpart in sledgehamr.  Its working memory (mask, tag list,
+ * counters) is one fixed array inside the library, reserved on every GPU
+ * that loads the library until the process exits; a level may hold at most
+ * SH_TAG_STATIC_MAX_CELLS valid cells (larger levels get SH_ERR_ARG).  The
+ * first call on a device looks up that array's device address, so make that
+ * first call before capturing the stream into a CUDA graph.  All calls share
+ * the array: calls whose GPU work overlaps (different streams or contexts on
+ * one device) race and must be serialised by the caller. */
+#define SH_TAG_STATIC_MAX_CELLS (1 << 22)
+SH_API int sh_tag_static(sh_ctx *ctx, sh_level *level, int use_te, double time, int lev,
+                         double dt, double dx, const double *te_crit,
+                         const double *params_tag, int nparams_tag, const double *params_mod,
+                         int nparams_mod, uint8_t *mask_out, long long *counts_out,
+                         int32_t *list_out, long long list_capacity, long long *ntagged);
+
 /* ---- gravitational-wave spectrum -------------------------------------------- */
 /* Bins of unique k^2 (unbinned) for a dim^3 grid: sorted i^2+j^2+k^2 over the
  * integer FFT frequencies. */

@@ -21,6 +21,8 @@ SH_ERR_UNSUPPORTED = -5
 SH_ERR_TIMEOUT = -6
 SH_ERR_NONFINITE = -7
 
+SH_TAG_STATIC_MAX_CELLS = 1 << 22
+
 SH_NEW = 0
 SH_OLD = 1
 SH_ADVANCE_NO_SWAP = 1
@@ -69,6 +71,8 @@ SIGNATURES = {
     "sh_average_down_te": (C.c_int, [vp, vp, vp]),
     "sh_tag": (C.c_int, [vp, vp, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double, vp, vp,
                          C.c_int, vp, C.c_int, vp, vp, vp, C.c_longlong, llp]),
+    "sh_tag_static": (C.c_int, [vp, vp, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double,
+                                vp, vp, C.c_int, vp, C.c_int, vp, vp, vp, C.c_longlong, llp]),
     "sh_spectrum_bins": (C.c_int, [C.c_int, vp, C.c_int, ip]),
     "sh_index_to_k": (C.c_int, [C.c_int, C.c_int, vp]),
     "sh_gw_spectrum": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, C.c_int, ip]),

@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 #include <cstring>
 #include <new>
 #include <stdexcept>
@@ -1284,3 +1285,126 @@ int sh_evolve_periodic(sh_ctx *ctx, int project, int integrator, const double *t
 }
 
 } /* extern "C" */
+
+/* ---- allocation-free tagging ------------------------------------------------
+ * Working memory of sh_tag_static: one fixed array per GPU, laid out as
+ *   [0, 512)                counters (total, user, per component)
+ *   [512, 768)              number of tagged cells
+ *   [768, 5120)             per-chunk tag counts (up to 1024 chunks)
+ *   [5120, 16384)           per-chunk list offsets
+ *   [16384, +4 MiB)         tag mask, one byte per valid cell
+ *   [16384 + 4 MiB, +16 MiB) tag list, one int per cell
+ */
+namespace {
+constexpr size_t kStaticCountsOff = 0;
+constexpr size_t kStaticTotalOff = 512;
+constexpr size_t kStaticChunkCntOff = 768;
+constexpr size_t kStaticChunkBaseOff = 5120;
+constexpr size_t kStaticMaskOff = 16384;
+constexpr size_t kStaticListOff = kStaticMaskOff + (size_t)SH_TAG_STATIC_MAX_CELLS;
+constexpr size_t kStaticBytes = kStaticListOff + (size_t)SH_TAG_STATIC_MAX_CELLS * sizeof(int);
+static_assert((SH_TAG_STATIC_MAX_CELLS + kChunk - 1) / kChunk * sizeof(int) <=
+                  kStaticChunkBaseOff - kStaticChunkCntOff,
+              "chunk counts do not fit");
+static_assert((SH_TAG_STATIC_MAX_CELLS + kChunk - 1) / kChunk * sizeof(long long) <=
+                  kStaticMaskOff - kStaticChunkBaseOff,
+              "chunk offsets do not fit");
+
+static __device__ __align__(256) unsigned char g_tag_static[kStaticBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_tag_static_mutex;
+void *g_tag_static_ptr[kMaxDevices] = {nullptr};
+
+/* Device address of g_tag_static on the context's device (looked up once per
+ * device, with that device current). */
+unsigned char *tag_static_base(sh_ctx *ctx) {
+    require(ctx->device >= 0 && ctx->device < kMaxDevices, "device index out of range");
+    std::lock_guard<std::mutex> lock(g_tag_static_mutex);
+    if (!g_tag_static_ptr[ctx->device]) {
+        void *p = nullptr;
+        ck(cudaGetSymbolAddress(&p, g_tag_static), "cudaGetSymbolAddress(g_tag_static)");
+        g_tag_static_ptr[ctx->device] = p;
+    }
+    return (unsigned char *)g_tag_static_ptr[ctx->device];
+}
+} // namespace
+
+extern "C" int sh_tag_static(sh_ctx *ctx, sh_level *L, int use_te, double time, int lev,
+                             double dt, double dx, const double *te_crit,
+                             const double *params_tag, int nparams_tag,
+                             const double *params_mod, int nparams_mod, uint8_t *mask_out,
+                             long long *counts_out, int32_t *list_out, long long list_capacity,
+                             long long *ntagged) {
+    if (!ctx || !L || !mask_out) return SH_ERR_ARG;
+    return guarded(ctx, [&] {
+        set_device(ctx);
+        require(L->nvalid <= SH_TAG_STATIC_MAX_CELLS,
+                "sh_tag_static: level has " + std::to_string(L->nvalid) +
+                    " valid cells, more than SH_TAG_STATIC_MAX_CELLS (" +
+                    std::to_string(SH_TAG_STATIC_MAX_CELLS) + ")");
+        require(L->nghost >= 1, "tagging reads the +1 neighbours: nghost >= 1");
+        require(nparams_tag >= 0 && nparams_tag <= kMaxParams, "at most 32 tag parameters");
+        require(nparams_mod >= 0 && nparams_mod <= kMaxComp, "at most 32 modifier parameters");
+        require(!use_te || te_crit, "te_crit required with truncation errors");
+        unsigned char *base = tag_static_base(ctx);
+        TagArgs a;
+        std::memset(&a, 0, sizeof(a));
+        a.boxes = L->d_boxes;
+        a.tiles = L->d_tiles;
+        a.state = L->buf[SH_NEW];
+        a.te = use_te ? L->buf[SH_OLD] : nullptr;
+        a.ncomp = L->ncomp;
+        a.lev = lev;
+        a.time = time;
+        a.dt = dt;
+        a.dx = dx;
+        for (int n = 0; n < L->ncomp; ++n) a.te_crit[n] = use_te ? te_crit[n] : 0.0;
+        for (int q = 0; q < nparams_tag; ++q) a.params_tag[q] = params_tag[q];
+        for (int q = 0; q < nparams_mod; ++q) a.params_mod[q] = params_mod[q];
+        a.mask = base + kStaticMaskOff;
+        a.mask_off = L->d_vbase; /* prefix sums of valid cells = mask offsets */
+        a.counts = (unsigned long long *)(base + kStaticCountsOff);
+        const long long nchunks = (L->nvalid + kChunk - 1) / kChunk;
+        int *cc = (int *)(base + kStaticChunkCntOff);
+        long long *cb = (long long *)(base + kStaticChunkBaseOff);
+        long long *tot = (long long *)(base + kStaticTotalOff);
+        int *list = (int *)(base + kStaticListOff);
+        const long long dev_cap =
+            std::min<long long>(list_out ? list_capacity : 0, SH_TAG_STATIC_MAX_CELLS);
+        /* the array keeps the previous call's contents: the counters must
+         * start at zero (mask, chunk counts and offsets are fully rewritten) */
+        ck(cudaMemsetAsync(base + kStaticCountsOff, 0, kStaticChunkCntOff, ctx->stream),
+           "static counters clear");
+        ck(L->ops->launch_tag(a, L->ntiles, ctx->stream), "tag launch");
+        ctx->launches++;
+        tag_count_kernel<<<(unsigned)nchunks, 256, 0, ctx->stream>>>(a.mask, L->nvalid, cc);
+        tag_scan_kernel<<<1, 1024, 0, ctx->stream>>>(cc, (int)nchunks, cb, tot);
+        ctx->launches += 2;
+        if (dev_cap > 0) {
+            tag_write_kernel<<<(unsigned)nchunks, 256, 0, ctx->stream>>>(a.mask, L->nvalid, cb,
+                                                                         list, dev_cap);
+            ctx->launches++;
+        }
+        ck(cudaGetLastError(), "tag compaction launch");
+        ck(cudaMemcpyAsync(mask_out, a.mask, L->nvalid, cudaMemcpyDeviceToHost, ctx->stream),
+           "mask download");
+        unsigned long long counts[2 + kMaxComp];
+        ck(cudaMemcpyAsync(counts, a.counts, sizeof(counts), cudaMemcpyDeviceToHost, ctx->stream),
+           "count download");
+        long long total = 0;
+        ck(cudaMemcpyAsync(&total, tot, sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream),
+           "tag total download");
+        ck(cudaStreamSynchronize(ctx->stream), "tag");
+        if (dev_cap > 0) {
+            const long long nl = std::min(total, dev_cap);
+            ck(cudaMemcpyAsync(list_out, list, nl * sizeof(int), cudaMemcpyDeviceToHost,
+                               ctx->stream),
+               "tag list download");
+            ck(cudaStreamSynchronize(ctx->stream), "tag list");
+        }
+        if (ntagged) *ntagged = total;
+        if (counts_out)
+            for (int n = 0; n < 2 + L->ncomp; ++n) counts_out[n] = (long long)counts[n];
+    });
+}
