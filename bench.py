@@ -1,26 +1,35 @@
-"""Benchmark of the time-stepping hot path: cell-updates/s of one GPU.
+"""Benchmark of the time-stepping hot path: cell-updates/s on one GPU.
 
-Workload (one "step" = one RKN4 step, Integrator::Advance, of the level):
-  AxionStrings equations, 128^3 periodic single level, L = 32 (dx = 0.25),
-  2nd-order (7-point) Laplacian, lambda = 1, eta0 = 0.1, dt = 0.0625, FP64,
-  seeded band-limited Gaussian initial state (|k| <= 1, unit variance).
-  One cell-update = one valid cell advanced by one full step, all components.
+Workloads (--workload):
+  amr (default): axion strings with AMR - 256^3 coarse grid (L = 64,
+      dx = 0.25) plus up to 2 refinement levels (ratio 2, blocking factor 8,
+      max grid size 32), 4th-order Laplacian, lambda = 1, RKN4 with
+      subcycling, eta from 0.1; tags = plaquette winding OR truncation error
+      (te_crit = 1e-3, shadow level), string-width threshold 1.5, regrid
+      interval 0.25; one step = one coarse step (Advance(0) with every finer
+      sub-step, level synchronisation and regrid).  The default
+      --steps 91 --warmup 3 runs eta 0.1 -> 6.0.
+  single: 128^3 periodic single level, L = 32, 2nd-order Laplacian,
+      lambda = 1, eta0 = 0.1, dt = 0.0625, one RKN4 step per step.
+One cell-update = one valid cell of one level advanced by one full step of
+that level, all components.  FP64, seeded band-limited Gaussian initial
+state (|k| <= 1, unit variance, Pi = 0).
 
-value   : device-resident state; K timed steps, each bracketed by CUDA events
-          on the library's stream; L2 flushed (a 512 MB write) between timed
-          steps, outside the events.
-e2e     : the same step through the public C ABI with host buffers: every
-          step uploads the state from pinned host memory, advances, and
-          downloads the result (both copies inside the timed region).
-roofline: the fused stage kernel, algorithmic bytes per launch divided by its
-          average duration, against the measured HBM copy bandwidth.
-cpu_baseline: the CPU oracle (FP64 restatement of the reference, OpenMP) on
-          the host cores, a bounded sample of the same workload.
+value   : device-resident state; each timed step bracketed by CUDA events on
+          the library's stream, L2 flushed (512 MB write) between timed steps
+          outside the events.
+e2e     : the whole job through the public C ABI with host buffers: the
+          initial state uploaded from pinned host memory, the steps, every
+          level read back to pinned host memory (per-step bytes = totals / K).
+roofline: the fused stage kernels (Rhs + RKN4 stage update): algorithmic bytes
+          of all their launches over their summed duration (CUDA events the
+          library records around each launch on its stream), against the
+          measured HBM copy bandwidth.
+cpu_baseline: the CPU oracle (FP64 restatement, OpenMP, all host cores) on a
+          bounded sample of the same workload.
 
 --impl reference: the reference's CPU path on the host cores (the oracle
-port on this machine; oracle/_ref where the reference could be compiled).
-
-Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+port; the reference itself cannot be built without AMReX).
 """
 from __future__ import annotations
 
@@ -37,21 +46,18 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-N = 128
-L = 32.0
-DX = L / N
-DT = 0.25 * DX
-ETA0 = 0.1
-PROJECT = "AxionStringsLap1"
-PARAMS = [1.0, 0.0]
-NGHOST = 1
 METRIC = "cell-updates/s"
-# Algorithmic HBM words per cell-update of the fused RKN4 schedule this
-# library runs for 2 position + 2 momentum components (stage i reads the
-# stage state, y0 and K_0..K_{i-1} and writes K_i and the next stage state;
-# the last stage writes y1): 10 + 16 + 16 = 42 FP64 words.
+# Algorithmic HBM words per cell-update of the fused RKN4 schedule for 2
+# position + 2 momentum components: stage i reads the stage state, y0 and
+# K_0..K_{i-1} and writes K_i and the next stage state; the last stage writes
+# y1: 10 + 16 + 16 = 42 FP64 words.
 WORDS_PER_CELL_UPDATE = 42
-STAGE_KERNELS_PER_STEP = 3
+
+SINGLE = dict(N=128, L=32.0, project="AxionStringsLap1", params=[1.0, 0.0], nghost=1,
+              eta0=0.1)
+AMR = dict(N0=256, L=64.0, project="AxionStringsLap2", params=[1.0, 0.0], nghost=2,
+           t_start=0.1, cfl=0.25, max_level=2, blocking_factor=8, max_grid_size=32,
+           n_error_buf=2, regrid_dt=0.25, te_crit=1e-3, string_width_threshold=1.5)
 
 
 def peaks():
@@ -109,67 +115,132 @@ class ClockSampler:
                 "samples": len(self.samples)}
 
 
-def initial_state():
+def amr_config(sh):
+    a = AMR
+    return sh.amr_config(a["project"], N0=a["N0"], L=a["L"], cfl=a["cfl"], t_start=a["t_start"],
+                         nghost=a["nghost"], max_level=a["max_level"],
+                         blocking_factor=a["blocking_factor"], max_grid_size=a["max_grid_size"],
+                         n_error_buf=a["n_error_buf"], regrid_dt=a["regrid_dt"],
+                         te_crit=[a["te_crit"]] * 4, params=a["params"],
+                         string_width_threshold=a["string_width_threshold"])
+
+
+def amr_state():
     from sledgehamr_gb300 import ic
-    return ic.axion_string_ic(N, L, kmax=1.0, seed=0)
+    return ic.axion_string_ic(AMR["N0"], AMR["L"], kmax=1.0, seed=0)
 
 
-def cpu_baseline(state, budget_s=12.0, max_steps=400):
-    """The oracle on the host cores: RKN4 steps of the full 128^3 level,
-    repeated in batches until about budget_s seconds of CPU work."""
-    from tests.oracle_lib import Oracle
+def single_state():
+    from sledgehamr_gb300 import ic
+    return ic.axion_string_ic(SINGLE["N"], SINGLE["L"], kmax=1.0, seed=0)
+
+
+def workload_config(name):
+    if name == "amr":
+        a = AMR
+        return {"workload": "axion strings AMR: 256^3 coarse + 2 refinement levels (ratio 2, "
+                            "blocking factor 8, max grid 32), 4th-order Laplacian, lambda=1, "
+                            "RKN4 with subcycling, winding + truncation-error tags "
+                            "(te_crit 1e-3), FP64",
+                "N0": a["N0"], "L": a["L"], "dx0": a["L"] / a["N0"], "cfl": a["cfl"],
+                "eta0": a["t_start"], "string_width_threshold": a["string_width_threshold"],
+                "regrid_dt": a["regrid_dt"], "n_error_buf": a["n_error_buf"],
+                "project": a["project"], "integrator": "RKN4 (type 21)",
+                "l2": "flushed between timed steps (512 MB write, outside events)"}
+    s = SINGLE
+    return {"workload": "axion strings 128^3 periodic single level, RKN4, 7-point Laplacian, "
+                        "lambda=1, FP64", "N": s["N"], "L": s["L"], "dx": s["L"] / s["N"],
+            "dt": 0.25 * s["L"] / s["N"], "project": s["project"],
+            "integrator": "RKN4 (type 21)",
+            "l2": "flushed between timed steps (512 MB write, outside events)"}
+
+
+def cpu_baseline(workload, budget_s=12.0, max_steps=400):
+    """The oracle on the host cores, steps until about budget_s seconds."""
+    from tests.oracle_lib import Oracle, OracleAmr
+    import sledgehamr_gb300 as sh
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    if workload == "amr":
+        o = OracleAmr(amr_config(sh), amr_state())
+        steps, el = 0, 0.0
+        while el < budget_s and steps < max_steps:
+            t0 = time.perf_counter()
+            o.step(1)
+            el += time.perf_counter() - t0
+            steps += 1
+        cu = o.info()["cell_updates"]
+        o.close()
+        return {"value": cu / el, "unit": METRIC, "cores": cores, "kind": "port",
+                "sample": f"first {steps} coarse steps of the AMR run (oracle, FP64, OpenMP), "
+                          f"{cu} cell-updates in {el:.1f} s"}
+    s = SINGLE
+    dx = s["L"] / s["N"]
     orc = Oracle()
-    orc.evolve_periodic(PROJECT, 21, state, t0=ETA0, dt=DT, dx=DX, nsteps=1, params=PARAMS,
-                        nghost=NGHOST)  # warm-up
-    steps, el = 0, 0.0
-    batch = 2
-    st = state
+    st = single_state()
+    steps, el, batch = 0, 0.0, 2
     while el < budget_s and steps < max_steps:
         t0 = time.perf_counter()
-        st = orc.evolve_periodic(PROJECT, 21, st, t0=ETA0 + steps * DT, dt=DT, dx=DX,
-                                 nsteps=batch, params=PARAMS, nghost=NGHOST)
+        st = orc.evolve_periodic(s["project"], 21, st, t0=s["eta0"] + steps * 0.25 * dx,
+                                 dt=0.25 * dx, dx=dx, nsteps=batch, params=s["params"],
+                                 nghost=s["nghost"])
         el += time.perf_counter() - t0
         steps += batch
         batch = min(2 * batch, 64)
-    return {"value": N ** 3 * steps / el, "unit": METRIC,
-            "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)),
-            "kind": "port",
-            "sample": f"{steps} RKN4 steps of the 128^3 level (FP64 oracle, OpenMP), {el:.1f} s"}
+    return {"value": s["N"] ** 3 * steps / el, "unit": METRIC, "cores": cores, "kind": "port",
+            "sample": f"{steps} RKN4 steps of the 128^3 level (oracle, FP64, OpenMP), {el:.1f} s"}
 
 
 def run_reference(args):
-    """The reference's CPU implementation of the path on the host cores."""
+    """The reference's CPU implementation of the path (oracle port) on the
+    host cores: each step one step of the same workload, within a time
+    budget."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    # The reference's compiled per-cell code (oracle/_ref) has no 7-point
-    # Laplacian project, so the workload runs on the oracle port, the FP64
-    # restatement of the reference's loop drivers and integrator.
-    from tests.oracle_lib import Oracle
-    kind = "port"
-    orc = Oracle()
-    st = initial_state()
-    project = PROJECT
-    for _ in range(args.warmup):
-        orc.evolve_periodic(project, 21, st, t0=ETA0, dt=DT, dx=DX, nsteps=1, params=PARAMS,
-                            nghost=NGHOST)
-    times = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        st = orc.evolve_periodic(project, 21, st, t0=ETA0, dt=DT, dx=DX, nsteps=1,
-                                 params=PARAMS, nghost=NGHOST)
-        times.append(time.perf_counter() - t0)
-    ms = 1e3 * float(np.mean(times))
-    value = N ** 3 / (ms / 1e3)
+    import sledgehamr_gb300 as sh
+    from tests.oracle_lib import Oracle, OracleAmr
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    times, cus = [], []
+    budget = 150.0
+    if args.workload == "amr":
+        o = OracleAmr(amr_config(sh), amr_state())
+        for _ in range(args.warmup):
+            o.step(1)
+        spent = 0.0
+        for _ in range(args.steps):
+            c0 = o.info()["cell_updates"]
+            t0 = time.perf_counter()
+            o.step(1)
+            dt = time.perf_counter() - t0
+            times.append(dt)
+            cus.append(o.info()["cell_updates"] - c0)
+            spent += dt
+            if spent > budget:
+                break
+        o.close()
+    else:
+        s = SINGLE
+        dx = s["L"] / s["N"]
+        orc = Oracle()
+        st = single_state()
+        for _ in range(args.warmup):
+            st = orc.evolve_periodic(s["project"], 21, st, t0=s["eta0"], dt=0.25 * dx, dx=dx,
+                                     nsteps=1, params=s["params"], nghost=s["nghost"])
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            st = orc.evolve_periodic(s["project"], 21, st, t0=s["eta0"], dt=0.25 * dx, dx=dx,
+                                     nsteps=1, params=s["params"], nghost=s["nghost"])
+            times.append(time.perf_counter() - t0)
+            cus.append(s["N"] ** 3)
+    value = float(sum(cus) / sum(times))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 0,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "axion strings 128^3 periodic, RKN4, 7-point Laplacian, FP64",
-                   "N": N, "L": L, "dt": DT},
-        "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": kind,
-                         "sample": f"{args.steps} full RKN4 steps of the 128^3 level"},
+        "steps": len(times), "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(times)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": workload_config(args.workload),
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
+                         "sample": f"{len(times)} steps of the workload on the oracle port "
+                                   f"(reference build unavailable: AMReX absent)"},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -179,13 +250,15 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="amr", choices=["amr", "single"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
-    if args.warmup < 3:
-        args.warmup = 3
+    if args.steps is None:
+        args.steps = 91 if args.workload == "amr" else 20
+    args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         run_reference(args)
         return
@@ -202,20 +275,37 @@ def main():
     torch.cuda.set_device(local)
     ctx = sh.Context(local)
     # one explicit stream for the library's kernels, the CUDA events and the
-    # L2 flush (the legacy default stream would not order with the
-    # library's own non-blocking stream)
+    # L2 flush (the legacy default stream does not order with the library's
+    # own non-blocking stream)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
-
-    state = initial_state()
-    lv = sh.Level.periodic(ctx, PROJECT, N, NGHOST)
-    lv.write(state)
-    lv.set_time(ETA0)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
-    def step():
-        lv.advance(sh.RKN4, DT, DX, params=PARAMS)
+    if args.workload == "amr":
+        state = amr_state()
+        sim = sh.Amr(ctx, amr_config(sh), state)
+
+        def step():
+            sim.step(1)
+
+        def cell_updates():
+            return sim.info()["cell_updates"]
+    else:
+        s = SINGLE
+        state = single_state()
+        dx = s["L"] / s["N"]
+        lv = sh.Level.periodic(ctx, s["project"], s["N"], s["nghost"])
+        lv.write(state)
+        lv.set_time(s["eta0"])
+        count = [0]
+
+        def step():
+            lv.advance(sh.RKN4, 0.25 * dx, dx, params=s["params"])
+            count[0] += s["N"] ** 3
+
+        def cell_updates():
+            return count[0]
 
     for _ in range(args.warmup):
         step()
@@ -226,83 +316,105 @@ def main():
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     l0 = ctx.kernel_launches
+    cu0 = cell_updates()
     ctx.profile(True)
     with ClockSampler(local) as clk:
-        for s in range(args.steps):
+        for q in range(args.steps):
             flush.zero_()
-            starts[s].record(stream)
+            starts[q].record(stream)
             step()
-            ends[s].record(stream)
+            ends[q].record(stream)
         torch.cuda.synchronize()
     launches = ctx.kernel_launches - l0
-    stage_total_ms, stage_launches = ctx.profile_read("rhs")
-    fill_total_ms, fill_launches = ctx.profile_read("fill_patch")
+    cus = cell_updates() - cu0
+    stage_ms, stage_launches = ctx.profile_read("rhs")
+    fill_ms, fill_launches = ctx.profile_read("fill_patch")
+    other = {c: ctx.profile_read(c)[0] for c in ("average_down", "tagging", "data_move")}
     ctx.profile(False)
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    ms = float(sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / args.steps)
+    total_ms = float(sum(a.elapsed_time(b) for a, b in zip(starts, ends)))
     if world > 1:
-        t = torch.tensor([ms], device="cuda")
+        t = torch.tensor([total_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    cells = N ** 3
-    value = world * cells / (ms / 1e3)
-
-    # roofline of the fused stage kernel: CUDA events recorded by the library
-    # around every stage-kernel launch on its stream during the timed steps
-    stage_ms = stage_total_ms / max(stage_launches, 1)
-    bytes_per_stage = WORDS_PER_CELL_UPDATE * 8 * cells / STAGE_KERNELS_PER_STEP
-    achieved = bytes_per_stage / (stage_ms / 1e3) / 1e9
+        total_ms = float(t.item())
+    value = world * cus / (total_ms / 1e3)
+    achieved = WORDS_PER_CELL_UPDATE * 8 * cus / (stage_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
+    amr_info = None
+    if args.workload == "amr":
+        amr_info = sim.info()
+        levels = [{"level": l, "boxes": sim.level(l).nbox, "cells": sim.level(l).nvalid}
+                  for l in range(amr_info["finest"] + 1)]
+        sim.close()
 
-    # e2e through the public API with pinned host buffers
-    host_in = torch.from_numpy(state.astype(np.float64)).pin_memory()
-    host_out = torch.empty_like(host_in).pin_memory()
-    e2e_steps = max(3, min(args.steps, 10))
-    lv.set_time(ETA0)
+    # e2e: the whole job through the public API with pinned host buffers
+    host_in = torch.from_numpy(np.ascontiguousarray(state)).pin_memory()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        ctx.check(ctx.lib.sh_level_write(ctx.h, lv.h, sh.SH_NEW, 0, host_in.data_ptr()), "write")
-        step()
-        ctx.check(ctx.lib.sh_level_read(ctx.h, lv.h, sh.SH_NEW, 0, host_out.data_ptr()), "read")
-    torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
-    nbytes = state.size * 8
+    if args.workload == "amr":
+        sim2 = sh.Amr(ctx, amr_config(sh), host_in.numpy())
+        for _ in range(args.warmup + args.steps):
+            sim2.step(1)
+        e2e_cus = sim2.info()["cell_updates"]
+        d2h = 0
+        for l in range(sim2.info()["finest"] + 1):
+            v = sim2.level(l)
+            out = torch.empty(v.nvalid * v.ncomp, dtype=torch.float64).pin_memory()
+            ctx.check(ctx.lib.sh_level_read(ctx.h, v.h, sh.SH_NEW, 1, out.data_ptr()), "read")
+            d2h += out.numel() * 8
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        e2e_steps = args.warmup + args.steps
+        sim2.close()
+        h2d = state.size * 8
+    else:
+        host_out = torch.empty_like(host_in).pin_memory()
+        e2e_steps = max(3, min(args.steps, 10))
+        s = SINGLE
+        dx = s["L"] / s["N"]
+        for _ in range(e2e_steps):
+            ctx.check(ctx.lib.sh_level_write(ctx.h, lv.h, sh.SH_NEW, 0, host_in.data_ptr()),
+                      "write")
+            lv.advance(sh.RKN4, 0.25 * dx, dx, params=s["params"])
+            ctx.check(ctx.lib.sh_level_read(ctx.h, lv.h, sh.SH_NEW, 0, host_out.data_ptr()),
+                      "read")
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        e2e_cus = s["N"] ** 3 * e2e_steps
+        h2d = d2h = state.size * 8 * e2e_steps
+        lv.close()
 
-    out = np.asarray(host_out.numpy())
-    finite = bool(np.isfinite(out).all())
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(state)
+        cpu = cpu_baseline(args.workload)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded Gaussian random field, |k|<=1)",
-            "config": {"workload": "axion strings 128^3 periodic single level, RKN4, 7-point "
-                                   "Laplacian, lambda=1, FP64", "N": N, "L": L, "dx": DX,
-                       "dt": DT, "project": PROJECT, "integrator": "RKN4 (type 21)",
-                       "l2": "flushed between timed steps (512 MB write, outside events)",
-                       "parallelism": f"replicas x{world}"},
-            "e2e": {"value": world * cells / e2e_s, "unit": METRIC, "h2d_bytes_per_step": nbytes,
-                    "d2h_bytes_per_step": nbytes},
+            "config": dict(workload_config(args.workload), parallelism=f"replicas x{world}"),
+            "e2e": {"value": world * e2e_cus / e2e_s, "unit": METRIC,
+                    "h2d_bytes_per_step": h2d / e2e_steps, "d2h_bytes_per_step": d2h / e2e_steps},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
-                         "peak_kind": peak_kind, "kernel": "stage_kernel (fused Rhs + RKN4 "
-                         "stage update)", "bytes_per_launch": bytes_per_stage,
-                         "stage_ms": stage_ms, "stage_launches": stage_launches,
-                         "ghost_fill_ms": fill_total_ms / max(fill_launches, 1)},
+                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                         "kernel": "stage_kernel (fused Rhs + RKN4 stage update)",
+                         "bytes_per_cell_update": WORDS_PER_CELL_UPDATE * 8,
+                         "stage_ms_total": stage_ms, "stage_launches": stage_launches,
+                         "fill_ms_total": fill_ms, "fill_launches": fill_launches,
+                         "other_ms": other},
             "clocks": clk.summary(),
-            "result_finite": finite,
+            "cell_updates_timed": cus,
         }
+        if amr_info:
+            line["amr"] = {"finest": amr_info["finest"], "nregrids": amr_info["nregrids"],
+                           "levels_at_end": levels}
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
-    lv.close()
     ctx.close()
     if world > 1:
         dist.destroy_process_group()

@@ -136,6 +136,11 @@ SH_API int sh_level_create(sh_ctx *ctx, int project, int with_gw, const int doma
 SH_API int sh_level_destroy(sh_ctx *ctx, sh_level *level);
 SH_API int sh_level_info(const sh_level *level, int *ncomp, int *nbox, long long *nvalid_cells);
 SH_API int sh_level_time(const sh_level *level, int which, double *t, int *istep);
+/* Box list of a level (capacity boxes; *nbox receives the count). */
+SH_API int sh_level_boxes(const sh_level *level, sh_box *out, int capacity, int *nbox);
+/* AMR level index handed to the project hooks as `lev` (default 0; the
+ * shadow level is -1). */
+SH_API int sh_level_set_index(sh_level *level, int lev);
 SH_API int sh_level_set_time(sh_level *level, int which, double t, int istep);
 
 /* Copy valid cells between host and a time level (layout 0: canonical,
@@ -153,6 +158,26 @@ SH_API int sh_level_read_device(sh_ctx *ctx, const sh_level *level, int which, i
  * periodic in every direction (FillPatch / FillIntermediatePatch for
  * lev <= 0). */
 SH_API int sh_level_fill_patch(sh_ctx *ctx, sh_level *level, int which);
+
+/* Link a fine level to its coarse level (NULL unlinks).  From then on the
+ * fine level's FillPatch (sh_level_fill_patch, and the fills inside
+ * sh_level_advance) fills the ghost cells not covered by the fine level's own
+ * boxes by quadratic interpolation (amr.interpolation_type CellQuadratic)
+ * from the coarse data at the fill time, linearly interpolated in time
+ * between the coarse level's OLD and NEW time levels (LevelSynchronizer::
+ * FillPatch / FillIntermediatePatch for lev > 0,
+ * source/level_synchronizer.cpp:94-214, :613-632).  The coarse level must
+ * cover the parents of those cells and have nghost >= 1 with filled ghosts;
+ * the link must be renewed when either level's boxes change. */
+SH_API int sh_level_set_coarse(sh_ctx *ctx, sh_level *fine, sh_level *coarse);
+/* Fill time level which_dst of dst (valid and ghost cells) from the valid
+ * cells of src (time level which_src; any box layout of the same domain,
+ * may be NULL) and interpolate the cells src does not cover from `coarse` at
+ * `time` (LevelSynchronizer::FillCoarsePatch when src is NULL,
+ * level_synchronizer.cpp:56-82; RemakeLevel's FillPatch otherwise,
+ * sledgehamr.cpp:173-189). */
+SH_API int sh_level_fill_from(sh_ctx *ctx, sh_level *dst, int which_dst, const sh_level *src,
+                              int which_src, sh_level *coarse, double time);
 
 /* One step of integrator `integrator` (SH_INTEGRATOR_*) of a periodic
  * level: swap(new, old) unless SH_ADVANCE_NO_SWAP, FillPatch(old), integrate
@@ -231,6 +256,60 @@ SH_API int sh_index_to_k(int dim, int projection_type, double *out);
 SH_API int sh_gw_spectrum(sh_ctx *ctx, const sh_level *level, const int *comps, int zero_padding,
                    int projection_type, int unbinned, double *bins_out, long long *ks_out,
                    int max_bins, int *nbins);
+
+/* ---- AMR time stepping ---------------------------------------------------- */
+/* A hierarchy of levels advanced with sledgehamr's recursive subcycling
+ * (TimeStepper::Advance, source/time_stepper.cpp:90-171): each level takes
+ * two steps per step of the level below, levels are averaged down after
+ * their finer levels, and, when any te_crit is finite, regrids are scheduled
+ * ahead of time with a shadow level (half resolution, twice the time step)
+ * so that truncation errors are available at regrid time
+ * (time_stepper.cpp:221-295, sledgehamr.cpp:234-251).  Tags combine the
+ * project's TagCellForRefinement<true> with truncation errors (sh_tag);
+ * new grids are blocking-factor blocks of the buffered tags merged into
+ * boxes of at most max_grid_size cells. */
+typedef struct sh_amr sh_amr;
+typedef struct sh_amr_config {
+    int project;                 /* sh_project_find id */
+    int with_gw;
+    int integrator;              /* integrator.type */
+    int nghost;                  /* amr.nghost */
+    int N0;                      /* amr.coarse_level_grid_size */
+    int max_level;               /* amr.max_refinement_levels */
+    int blocking_factor;         /* amr.blocking_factor */
+    int max_grid_size;           /* grid size of every level */
+    int n_error_buf;             /* amr.n_error_buf */
+    int record_regrids;          /* keep tags and boxes of every regrid */
+    double L;                    /* sim.L */
+    double cfl;                  /* sim.cfl */
+    double t_start;              /* sim.t_start */
+    double regrid_dt;            /* amr.regrid_dt */
+    double string_width_threshold; /* AxionStrings CreateLevelIf (<= 0: off) */
+    double string_lambda;        /* lambda of the string width */
+    double te_crit[32];          /* amr.te_crit per component (>= DBL_MAX: off) */
+    double params[32];           /* SetParamsRhs */
+    int nparams;
+    double gw_params[16];        /* SetParamsGravitationalWaveRhs */
+    int ngw;
+} sh_amr_config;
+
+SH_API int sh_amr_config_defaults(sh_amr_config *cfg);
+/* Hierarchy with level 0 = level0 (canonical layout, N0^3 cells, boxes of
+ * max_grid_size) at t_start. */
+SH_API int sh_amr_create(sh_ctx *ctx, const sh_amr_config *cfg, const double *level0,
+                         sh_amr **out);
+SH_API int sh_amr_destroy(sh_ctx *ctx, sh_amr *amr);
+/* n coarse steps (Sledgehamr::Evolve loop bodies). */
+SH_API int sh_amr_step(sh_ctx *ctx, sh_amr *amr, int n);
+SH_API int sh_amr_info(const sh_amr *amr, int *finest, long long *cell_updates, int *nregrids);
+/* Level lev of the hierarchy (owned by it; valid until the next step). */
+SH_API int sh_amr_level(const sh_amr *amr, int lev, sh_level **level);
+/* Regrid record q (with record_regrids): the tagged level and time, its
+ * boxes, its tag mask (boxes layout) and the new boxes of the level above. */
+SH_API int sh_amr_regrid_record(const sh_amr *amr, int q, int *lev, double *time,
+                                sh_box *tagged_boxes, int cap_tagged, int *n_tagged,
+                                uint8_t *mask, long long cap_mask, long long *n_mask,
+                                sh_box *new_boxes, int cap_new, int *n_new);
 
 /* ---- convenience --------------------------------------------------------------- */
 /* Evolve a periodic cubic level of N^3 cells (boxes of max_grid cells per

@@ -119,6 +119,9 @@ struct MF {
     double t = -DBL_MAX;
     int istep = 0;
     bool contains_truncation_errors = false;
+    /* owner box of every block of `res` cells of the domain (-1: uncovered) */
+    std::vector<int> owner;
+    int res = 0, nbx = 0, nby = 0, nbz = 0;
 
     void define(const Box &dom, const std::vector<Box> &boxes, int ncomp,
                 int nghost, double time = -DBL_MAX) {
@@ -126,6 +129,28 @@ struct MF {
         contains_truncation_errors = false;
         fabs.assign(boxes.size(), Fab());
         for (size_t b = 0; b < boxes.size(); ++b) fabs[b].define(boxes[b], ncomp, nghost);
+        auto gcd = [](int a, int b) {
+            a = a < 0 ? -a : a;
+            b = b < 0 ? -b : b;
+            while (b) { int r = a % b; a = b; b = r; }
+            return a;
+        };
+        res = gcd(gcd(dom.len(0), dom.len(1)), dom.len(2));
+        for (const Box &b : boxes) {
+            res = gcd(res, b.lo.x - dom.lo.x); res = gcd(res, b.hi.x + 1 - dom.lo.x);
+            res = gcd(res, b.lo.y - dom.lo.y); res = gcd(res, b.hi.y + 1 - dom.lo.y);
+            res = gcd(res, b.lo.z - dom.lo.z); res = gcd(res, b.hi.z + 1 - dom.lo.z);
+        }
+        if (res <= 0) res = 1;
+        nbx = dom.len(0) / res; nby = dom.len(1) / res; nbz = dom.len(2) / res;
+        owner.assign((size_t)nbx * nby * nbz, -1);
+        for (size_t q = 0; q < boxes.size(); ++q) {
+            const Box &b = boxes[q];
+            for (int z = (b.lo.z - dom.lo.z) / res; z <= (b.hi.z - dom.lo.z) / res; ++z)
+                for (int y = (b.lo.y - dom.lo.y) / res; y <= (b.hi.y - dom.lo.y) / res; ++y)
+                    for (int x = (b.lo.x - dom.lo.x) / res; x <= (b.hi.x - dom.lo.x) / res; ++x)
+                        owner[((size_t)z * nby + y) * nbx + x] = (int)q;
+        }
     }
     bool defined() const { return !fabs.empty(); }
     std::vector<Box> boxes() const {
@@ -135,6 +160,14 @@ struct MF {
     }
     void clear() { fabs.clear(); }
 };
+
+/* Find the fab of `mf` whose valid box contains cell (i,j,k), or -1. */
+inline int find_fab(const MF &mf, int i, int j, int k) {
+    if (!mf.domain.contains(i, j, k) || mf.res <= 0) return -1;
+    const int x = (i - mf.domain.lo.x) / mf.res, y = (j - mf.domain.lo.y) / mf.res,
+              z = (k - mf.domain.lo.z) / mf.res;
+    return mf.owner[((size_t)z * mf.nby + y) * mf.nbx + x];
+}
 
 template <class F>
 inline void for_cells(const Box &b, F &&f) {
@@ -211,12 +244,10 @@ inline void fill_boundary_periodic(MF &mf) {
             int si = dlo.x + pmod(i - dlo.x, NX);
             int sj = dlo.y + pmod(j - dlo.y, NY);
             int sk = dlo.z + pmod(k - dlo.z, NZ);
-            for (size_t s = 0; s < mf.fabs.size(); ++s) {
-                if (!mf.fabs[s].vbox.contains(si, sj, sk)) continue;
-                auto sa = mf.fabs[s].ca();
-                for (int n = 0; n < mf.nc; ++n) d(i, j, k, n) = sa(si, sj, sk, n);
-                return;
-            }
+            const int s = find_fab(mf, si, sj, sk);
+            if (s < 0) return;
+            auto sa = mf.fabs[s].ca();
+            for (int n = 0; n < mf.nc; ++n) d(i, j, k, n) = sa(si, sj, sk, n);
         });
     }
 }
@@ -467,12 +498,6 @@ inline void avgdown_te_cell(int i, int j, int k, int ncomp, const A4<double> &cr
     }
 }
 
-/* Find the fab of `mf` whose valid box contains cell (i,j,k), or -1. */
-inline int find_fab(const MF &mf, int i, int j, int k) {
-    for (size_t b = 0; b < mf.fabs.size(); ++b)
-        if (mf.fabs[b].vbox.contains(i, j, k)) return (int)b;
-    return -1;
-}
 
 /* Plain 2x2x2 average of fine onto every coarse cell covered by fine
  * (amrex::average_down with ratio 2); sum in k, j, i loop order. */

@@ -18,7 +18,7 @@ from typing import Sequence
 import numpy as np
 
 from . import _lib
-from ._lib import SH_NEW, SH_OLD, SH_ADVANCE_NO_SWAP, ShBox
+from ._lib import SH_NEW, SH_OLD, SH_ADVANCE_NO_SWAP, ShAmrConfig, ShBox
 
 # integrator.type (source/integrators/integrator.h:12-23)
 LSSSPRK3 = 10
@@ -333,3 +333,111 @@ def average_down(ctx: Context, fine: Level, crse: Level, which_f: int = SH_NEW,
 
 def average_down_te(ctx: Context, fine: Level, crse: Level):
     ctx.check(ctx.lib.sh_average_down_te(ctx.h, fine.h, crse.h), "sh_average_down_te")
+
+
+def amr_config(project: str, **kw) -> ShAmrConfig:
+    """sh_amr_config with the library defaults, then the given fields
+    (te_crit, params, gw_params as sequences)."""
+    lib = _lib.load()
+    cfg = ShAmrConfig()
+    lib.sh_amr_config_defaults(C.byref(cfg))
+    cfg.project = project_id(project)
+    for k, v in kw.items():
+        if k in ("te_crit",):
+            for n, x in enumerate(v):
+                cfg.te_crit[n] = x
+        elif k == "params":
+            for n, x in enumerate(v):
+                cfg.params[n] = x
+            cfg.nparams = len(v)
+        elif k == "gw_params":
+            for n, x in enumerate(v):
+                cfg.gw_params[n] = x
+            cfg.ngw = len(v)
+        else:
+            setattr(cfg, k, v)
+    return cfg
+
+
+def _boxes_of(arr, n):
+    return [((arr[q].lo[0], arr[q].lo[1], arr[q].lo[2]), (arr[q].hi[0], arr[q].hi[1], arr[q].hi[2]))
+            for q in range(n)]
+
+
+class LevelView:
+    """Read access to a level owned by an Amr hierarchy."""
+
+    def __init__(self, ctx: Context, handle):
+        self.ctx, self.h = ctx, handle
+        nc, nb, nv = C.c_int(), C.c_int(), C.c_longlong()
+        ctx.lib.sh_level_info(handle, C.byref(nc), C.byref(nb), C.byref(nv))
+        self.ncomp, self.nbox, self.nvalid = nc.value, nb.value, nv.value
+        arr = (ShBox * max(self.nbox, 1))()
+        n = C.c_int()
+        ctx.lib.sh_level_boxes(handle, arr, self.nbox, C.byref(n))
+        self.boxes = _boxes_of(arr, n.value)
+
+    def read(self, which: int = SH_NEW) -> np.ndarray:
+        out = np.empty(self.nvalid * self.ncomp, dtype=np.float64)
+        self.ctx.check(self.ctx.lib.sh_level_read(self.ctx.h, self.h, which, 1, _ptr(out)),
+                       "sh_level_read")
+        return out
+
+    def time(self, which: int = SH_NEW):
+        t, s = C.c_double(), C.c_int()
+        self.ctx.lib.sh_level_time(self.h, which, C.byref(t), C.byref(s))
+        return t.value, s.value
+
+
+class Amr:
+    """AMR hierarchy advanced by the library's time stepper (sh_amr)."""
+
+    def __init__(self, ctx: Context, cfg: ShAmrConfig, level0: np.ndarray):
+        self.ctx = ctx
+        self.cfg = cfg
+        a = _f64(level0)
+        h = C.c_void_p()
+        ctx.check(ctx.lib.sh_amr_create(ctx.h, C.byref(cfg), _ptr(a), C.byref(h)),
+                  "sh_amr_create")
+        self.h = h
+
+    def step(self, n: int = 1):
+        self.ctx.check(self.ctx.lib.sh_amr_step(self.ctx.h, self.h, n), "sh_amr_step")
+
+    def info(self):
+        f, cu, nr = C.c_int(), C.c_longlong(), C.c_int()
+        self.ctx.lib.sh_amr_info(self.h, C.byref(f), C.byref(cu), C.byref(nr))
+        return {"finest": f.value, "cell_updates": cu.value, "nregrids": nr.value}
+
+    def level(self, lev: int) -> LevelView:
+        h = C.c_void_p()
+        self.ctx.check(self.ctx.lib.sh_amr_level(self.h, lev, C.byref(h)), "sh_amr_level")
+        return LevelView(self.ctx, h)
+
+    def regrid_record(self, q: int):
+        lev, t = C.c_int(), C.c_double()
+        nt, nn, nm = C.c_int(), C.c_int(), C.c_longlong()
+        lib = self.ctx.lib
+        self.ctx.check(lib.sh_amr_regrid_record(self.h, q, C.byref(lev), C.byref(t), None, 0,
+                                                C.byref(nt), None, 0, C.byref(nm), None, 0,
+                                                C.byref(nn)), "regrid_record")
+        tb = (ShBox * max(nt.value, 1))()
+        nb = (ShBox * max(nn.value, 1))()
+        mask = np.empty(max(nm.value, 1), dtype=np.uint8)
+        self.ctx.check(lib.sh_amr_regrid_record(self.h, q, C.byref(lev), C.byref(t), tb,
+                                                nt.value, C.byref(nt), _ptr(mask), nm.value,
+                                                C.byref(nm), nb, nn.value, C.byref(nn)),
+                       "regrid_record")
+        return {"lev": lev.value, "time": t.value, "tagged_boxes": _boxes_of(tb, nt.value),
+                "mask": mask[: nm.value].copy(), "new_boxes": _boxes_of(nb, nn.value)}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.sh_amr_destroy(self.ctx.h, self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

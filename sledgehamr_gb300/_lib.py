@@ -37,6 +37,18 @@ class ShBox(C.Structure):
     _fields_ = [("lo", C.c_int * 3), ("hi", C.c_int * 3)]
 
 
+class ShAmrConfig(C.Structure):
+    _fields_ = [("project", C.c_int), ("with_gw", C.c_int), ("integrator", C.c_int),
+                ("nghost", C.c_int), ("N0", C.c_int), ("max_level", C.c_int),
+                ("blocking_factor", C.c_int), ("max_grid_size", C.c_int),
+                ("n_error_buf", C.c_int), ("record_regrids", C.c_int),
+                ("L", C.c_double), ("cfl", C.c_double), ("t_start", C.c_double),
+                ("regrid_dt", C.c_double), ("string_width_threshold", C.c_double),
+                ("string_lambda", C.c_double), ("te_crit", C.c_double * 32),
+                ("params", C.c_double * 32), ("nparams", C.c_int),
+                ("gw_params", C.c_double * 16), ("ngw", C.c_int)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "sh_ctx_create": (C.c_int, [C.c_int, C.POINTER(vp)]),
@@ -58,11 +70,23 @@ SIGNATURES = {
     "sh_level_info": (C.c_int, [vp, ip, ip, llp]),
     "sh_level_time": (C.c_int, [vp, C.c_int, dp, ip]),
     "sh_level_set_time": (C.c_int, [vp, C.c_int, C.c_double, C.c_int]),
+    "sh_level_boxes": (C.c_int, [vp, C.POINTER(ShBox), C.c_int, ip]),
+    "sh_level_set_index": (C.c_int, [vp, C.c_int]),
+    "sh_amr_config_defaults": (C.c_int, [C.POINTER(ShAmrConfig)]),
+    "sh_amr_create": (C.c_int, [vp, C.POINTER(ShAmrConfig), vp, C.POINTER(vp)]),
+    "sh_amr_destroy": (C.c_int, [vp, vp]),
+    "sh_amr_step": (C.c_int, [vp, vp, C.c_int]),
+    "sh_amr_info": (C.c_int, [vp, ip, llp, ip]),
+    "sh_amr_level": (C.c_int, [vp, C.c_int, C.POINTER(vp)]),
+    "sh_amr_regrid_record": (C.c_int, [vp, C.c_int, ip, dp, C.POINTER(ShBox), C.c_int, ip, vp,
+                                       C.c_longlong, llp, C.POINTER(ShBox), C.c_int, ip]),
     "sh_level_write": (C.c_int, [vp, vp, C.c_int, C.c_int, vp]),
     "sh_level_read": (C.c_int, [vp, vp, C.c_int, C.c_int, vp]),
     "sh_level_write_device": (C.c_int, [vp, vp, C.c_int, C.c_int, vp]),
     "sh_level_read_device": (C.c_int, [vp, vp, C.c_int, C.c_int, vp]),
     "sh_level_fill_patch": (C.c_int, [vp, vp, C.c_int]),
+    "sh_level_set_coarse": (C.c_int, [vp, vp, vp]),
+    "sh_level_fill_from": (C.c_int, [vp, vp, C.c_int, vp, C.c_int, vp, C.c_double]),
     "sh_level_advance": (C.c_int, [vp, vp, C.c_int, vp, C.c_int, C.c_double, C.c_double, vp,
                                    C.c_int, vp, C.c_int, C.c_int, vp, C.c_int]),
     "sh_level_rhs": (C.c_int, [vp, vp, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double,

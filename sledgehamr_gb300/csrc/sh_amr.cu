@@ -1,0 +1,269 @@
+/* AMR hierarchy on the GPU (sh_amr_* of include/sledgehamr_gb300.h): the
+ * host time stepper of sh_amr_driver.h over levels held by this library. */
+#include <cfloat>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "sh_amr_driver.h"
+#include "sledgehamr_gb300.h"
+
+namespace {
+
+/* Level handle of the driver: the library level plus link bookkeeping, so
+ * that a fine level's coarse-fine plan is rebuilt whenever either level was
+ * re-created. */
+struct GpuLevel {
+    sh_level *L = nullptr;
+    long long gen = 0;
+    const GpuLevel *linked = nullptr;
+    long long linked_gen = -1;
+};
+
+struct ShFail : std::runtime_error {
+    int code;
+    ShFail(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+struct GpuBackend {
+    using Level = GpuLevel *;
+    sh_ctx *ctx;
+    sh_amr_config cfg;
+    int ncomp = 0;
+    long long next_gen = 1;
+
+    void ok(int rc, const char *what) {
+        if (rc != SH_OK)
+            throw ShFail(rc, std::string(what) + ": " + sh_ctx_last_error(ctx));
+    }
+
+    Level create(int lev, const std::vector<shamr::IBox> &boxes, int N) {
+        std::vector<sh_box> bx(boxes.size());
+        for (size_t q = 0; q < boxes.size(); ++q)
+            for (int d = 0; d < 3; ++d) {
+                bx[q].lo[d] = boxes[q].lo[d];
+                bx[q].hi[d] = boxes[q].hi[d];
+            }
+        const int lo[3] = {0, 0, 0}, hi[3] = {N - 1, N - 1, N - 1};
+        GpuLevel *g = new GpuLevel();
+        ok(sh_level_create(ctx, cfg.project, cfg.with_gw, lo, hi, bx.data(), (int)bx.size(),
+                           cfg.nghost, &g->L),
+           "sh_level_create");
+        sh_level_set_index(g->L, lev);
+        g->gen = next_gen++;
+        return g;
+    }
+    void destroy(Level &l) {
+        if (l) {
+            sh_level_destroy(ctx, l->L);
+            delete l;
+        }
+        l = nullptr;
+    }
+    double time(const Level &l, int which) {
+        double t;
+        sh_level_time(l->L, which, &t, nullptr);
+        return t;
+    }
+    int istep(const Level &l, int which) {
+        int s;
+        sh_level_time(l->L, which, nullptr, &s);
+        return s;
+    }
+    void set_time(Level &l, int which, double t, int s) { sh_level_set_time(l->L, which, t, s); }
+    void link(Level f, const Level c) {
+        if (!c) {
+            if (f->linked) ok(sh_level_set_coarse(ctx, f->L, nullptr), "unlink");
+            f->linked = nullptr;
+            f->linked_gen = -1;
+            return;
+        }
+        if (f->linked == c && f->linked_gen == c->gen) return;
+        ok(sh_level_set_coarse(ctx, f->L, c->L), "sh_level_set_coarse");
+        f->linked = c;
+        f->linked_gen = c->gen;
+    }
+    void advance(int lev, Level &l, Level *coarse, double dt, double dx, bool no_swap) {
+        link(l, coarse ? *coarse : nullptr);
+        ok(sh_level_advance(ctx, l->L, cfg.integrator, nullptr, 0, dt, dx, cfg.params,
+                            cfg.nparams, cfg.gw_params, cfg.ngw, 0, nullptr,
+                            no_swap ? SH_ADVANCE_NO_SWAP : 0),
+           "sh_level_advance");
+    }
+    void average_down(Level &f, int wf, Level &c, int wc) {
+        ok(sh_average_down(ctx, f->L, wf, c->L, wc), "sh_average_down");
+    }
+    void average_down_te(Level &f, Level &c) {
+        ok(sh_average_down_te(ctx, f->L, c->L), "sh_average_down_te");
+    }
+    std::vector<uint8_t> tag(Level &l, bool use_te, double time, int lev, double dt, double dx) {
+        int nc = 0, nb = 0;
+        long long nv = 0;
+        sh_level_info(l->L, &nc, &nb, &nv);
+        std::vector<uint8_t> mask((size_t)nv);
+        ok(sh_tag(ctx, l->L, use_te ? 1 : 0, time, lev, dt, dx, cfg.te_crit, nullptr, 0,
+                  nullptr, 0, mask.data(), nullptr, nullptr, 0, nullptr),
+           "sh_tag");
+        return mask;
+    }
+    void fill_from_coarse(Level &f, Level &c, double time) {
+        ok(sh_level_fill_from(ctx, f->L, SH_NEW, nullptr, SH_NEW, c->L, time), "fill from coarse");
+    }
+    void remake(Level &fresh, Level &old, Level &c, double time) {
+        ok(sh_level_fill_from(ctx, fresh->L, SH_NEW, old->L, SH_NEW, c->L, time), "remake");
+    }
+    void refresh_ghosts(Level &l, int which, Level *coarse) {
+        link(l, coarse ? *coarse : nullptr);
+        ok(sh_level_fill_patch(ctx, l->L, which), "sh_level_fill_patch");
+    }
+};
+
+} // namespace
+
+struct sh_amr {
+    GpuBackend backend;
+    std::unique_ptr<shamr::Driver<GpuBackend>> driver;
+    std::string err;
+};
+
+namespace {
+shamr::Config driver_config(const sh_amr_config &c, int ncomp) {
+    shamr::Config d;
+    d.N0 = c.N0;
+    d.L = c.L;
+    d.cfl = c.cfl;
+    d.t_start = c.t_start;
+    d.nghost = c.nghost;
+    d.max_level = c.max_level;
+    d.blocking_factor = c.blocking_factor;
+    d.max_grid_size = c.max_grid_size;
+    d.n_error_buf = c.n_error_buf;
+    d.regrid_dt = c.regrid_dt;
+    d.string_width_threshold = c.string_width_threshold;
+    d.string_lambda = c.string_lambda;
+    d.te_crit.assign(c.te_crit, c.te_crit + ncomp);
+    return d;
+}
+
+template <class F>
+int amr_guard(sh_ctx *ctx, F &&f) {
+    try {
+        f();
+        return SH_OK;
+    } catch (const ShFail &e) {
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        return SH_ERR_NOMEM;
+    } catch (const std::exception &e) {
+        (void)e;
+        return SH_ERR_ARG;
+    }
+}
+} // namespace
+
+extern "C" {
+
+int sh_amr_config_defaults(sh_amr_config *c) {
+    if (!c) return SH_ERR_ARG;
+    std::memset(c, 0, sizeof(*c));
+    c->integrator = SH_INTEGRATOR_RKN4;
+    c->nghost = 2;
+    c->N0 = 64;
+    c->max_level = 2;
+    c->blocking_factor = 8;
+    c->max_grid_size = 32;
+    c->n_error_buf = 1;
+    c->L = 16.;
+    c->cfl = 0.25;
+    c->t_start = 0.1;
+    c->string_lambda = 1.;
+    for (int n = 0; n < 32; ++n) c->te_crit[n] = DBL_MAX;
+    return SH_OK;
+}
+
+int sh_amr_create(sh_ctx *ctx, const sh_amr_config *cfg, const double *level0, sh_amr **out) {
+    if (!ctx || !cfg || !level0 || !out) return SH_ERR_ARG;
+    *out = nullptr;
+    int ncomp = 0;
+    int rc = sh_project_ncomp(cfg->project, cfg->with_gw, &ncomp, nullptr);
+    if (rc != SH_OK) return rc;
+    if (cfg->nparams < 0 || cfg->nparams > 32 || cfg->ngw < 0 || cfg->ngw > 16)
+        return SH_ERR_ARG;
+    sh_amr *a = new (std::nothrow) sh_amr();
+    if (!a) return SH_ERR_NOMEM;
+    a->backend.ctx = ctx;
+    a->backend.cfg = *cfg;
+    a->backend.ncomp = ncomp;
+    rc = amr_guard(ctx, [&] {
+        a->driver.reset(new shamr::Driver<GpuBackend>(a->backend, driver_config(*cfg, ncomp)));
+        a->driver->record_regrids = cfg->record_regrids != 0;
+        a->driver->init_coarse([&](GpuLevel *&l) {
+            a->backend.ok(sh_level_write(ctx, l->L, SH_NEW, 0, level0), "sh_level_write");
+        });
+    });
+    if (rc != SH_OK) {
+        delete a;
+        return rc;
+    }
+    *out = a;
+    return SH_OK;
+}
+
+int sh_amr_destroy(sh_ctx *ctx, sh_amr *a) {
+    if (!ctx || !a) return SH_ERR_ARG;
+    delete a;
+    return SH_OK;
+}
+
+int sh_amr_step(sh_ctx *ctx, sh_amr *a, int n) {
+    if (!ctx || !a || n < 0) return SH_ERR_ARG;
+    return amr_guard(ctx, [&] {
+        for (int q = 0; q < n; ++q) a->driver->step();
+    });
+}
+
+int sh_amr_info(const sh_amr *a, int *finest, long long *cell_updates, int *nregrids) {
+    if (!a) return SH_ERR_ARG;
+    if (finest) *finest = a->driver->finest;
+    if (cell_updates) *cell_updates = a->driver->cell_updates;
+    if (nregrids) *nregrids = (int)a->driver->regrids.size();
+    return SH_OK;
+}
+
+int sh_amr_level(const sh_amr *a, int lev, sh_level **level) {
+    if (!a || !level || lev < 0 || lev > a->driver->finest) return SH_ERR_ARG;
+    *level = a->driver->levels[lev]->L;
+    return SH_OK;
+}
+
+int sh_amr_regrid_record(const sh_amr *a, int q, int *lev, double *time, sh_box *tagged_boxes,
+                         int cap_tagged, int *n_tagged, uint8_t *mask, long long cap_mask,
+                         long long *n_mask, sh_box *new_boxes, int cap_new, int *n_new) {
+    if (!a || q < 0 || q >= (int)a->driver->regrids.size()) return SH_ERR_ARG;
+    const shamr::RegridRecord &r = a->driver->regrids[q];
+    if (lev) *lev = r.lev;
+    if (time) *time = r.time;
+    auto put = [](const std::vector<shamr::IBox> &src, sh_box *dst, int cap, int *n) {
+        if (n) *n = (int)src.size();
+        if (!dst) return true;
+        if (cap < (int)src.size()) return false;
+        for (size_t k = 0; k < src.size(); ++k)
+            for (int d = 0; d < 3; ++d) {
+                dst[k].lo[d] = src[k].lo[d];
+                dst[k].hi[d] = src[k].hi[d];
+            }
+        return true;
+    };
+    if (!put(r.boxes_tagged_level, tagged_boxes, cap_tagged, n_tagged)) return SH_ERR_ARG;
+    if (!put(r.new_boxes, new_boxes, cap_new, n_new)) return SH_ERR_ARG;
+    if (n_mask) *n_mask = (long long)r.mask.size();
+    if (mask) {
+        if (cap_mask < (long long)r.mask.size()) return SH_ERR_ARG;
+        std::memcpy(mask, r.mask.data(), r.mask.size());
+    }
+    return SH_OK;
+}
+
+} /* extern "C" */

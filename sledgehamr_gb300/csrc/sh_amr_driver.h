@@ -1,0 +1,519 @@
+/* Host-side AMR time stepper: sledgehamr's recursive subcycling with shadow
+ * level, truncation-error scheduling and regrids, over a backend that owns
+ * the level data and runs the numerical operations.
+ *
+ * Reference (order of operations restated here):
+ *   TimeStepper::Advance ........... source/time_stepper.cpp:90-133
+ *   TimeStepper::SynchronizeLevels . time_stepper.cpp:140-162
+ *   TimeStepper::SynchronizeTimes .. time_stepper.cpp:168-171
+ *   TimeStepper::ScheduleRegrid .... time_stepper.cpp:221-295
+ *   TimeStepper::DoRegridIfScheduled / NoShadowRegrid / DoRegrid
+ *                                    time_stepper.cpp:301-397
+ *   RegridScheduler ................ source/regrid_scheduler.{h,cpp}
+ *   Integrator::Advance ............ source/integrators/integrator.cpp:11-31
+ *   Sledgehamr::CreateShadowLevel .. source/sledgehamr.cpp:234-251
+ *   Sledgehamr::ErrorEst ........... sledgehamr.cpp:207-229
+ *   MakeNewLevelFromCoarse / RemakeLevel / ClearLevel
+ *                                    sledgehamr.cpp:149-198
+ *   AxionStrings CreateLevelIf ..... projects/AxionStrings/cosmology.h:25-27,
+ *                                    :46-48 (string width <= threshold)
+ *
+ * New grids (the part sledgehamr delegates to AMReX's clustering or its
+ * local regrid): the tags of level l are buffered by n_error_buf cells,
+ * coarsened to blocks of blocking_factor cells of level l+1, restricted to
+ * blocks whose surroundings (ceil(nghost/2)+1 cells of level l) lie inside
+ * level l, and the tagged blocks are merged, inside aligned windows of
+ * max_grid_size cells, into boxes by x-runs, then equal runs along y, then
+ * along z.  At most one new level is added per regrid, as in AMReX.
+ *
+ * The backend B provides (Level is a handle it owns):
+ *   Level create(int lev, const std::vector<IBox>&, int N);   // lev -1: shadow
+ *   void destroy(Level&);
+ *   void set_time(Level&, int which, double t, int istep);
+ *   double time(const Level&, int which); int istep(const Level&, int which);
+ *   void advance(int lev, Level&, Level *coarse, double dt, double dx, bool no_swap);
+ *   void average_down(Level &fine, int which_f, Level &crse, int which_c);
+ *   void average_down_te(Level &fine, Level &crse);
+ *   std::vector<uint8_t> tag(Level&, bool use_te, double time, int lev,
+ *                            double dt, double dx);          // boxes layout
+ *   void fill_from_coarse(Level &fine, Level &crse, double time);
+ *   void remake(Level &fresh, Level &old, Level &crse, double time);
+ *   void refresh_ghosts(Level&, int which, Level *coarse);
+ */
+#ifndef SH_AMR_DRIVER_H_
+#define SH_AMR_DRIVER_H_
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+#include <functional>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace shamr {
+
+constexpr int kNew = 0, kOld = 1;
+
+struct IBox {
+    int lo[3];
+    int hi[3];
+    long long volume() const {
+        return (long long)(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+    }
+};
+
+struct Config {
+    int N0 = 64;                /* coarse cells per side */
+    double L = 16.;             /* box length */
+    double cfl = 0.25;          /* dt = cfl dx */
+    double t_start = 0.1;
+    int nghost = 2;
+    int max_level = 2;
+    int blocking_factor = 8;    /* cells of the created level */
+    int max_grid_size = 32;     /* cells of the created level */
+    int n_error_buf = 1;        /* cells of the tagged level */
+    double regrid_dt = 0.;      /* coarse-level regrid interval */
+    std::vector<double> te_crit; /* per component; DBL_MAX: off */
+    double string_width_threshold = 0.; /* > 0: AxionStrings CreateLevelIf */
+    double string_lambda = 1.;  /* lambda of cosmology.h */
+};
+
+struct RegridRecord {
+    int lev;          /* level whose tags made level lev+1 */
+    double time;
+    std::vector<IBox> boxes_tagged_level;
+    std::vector<uint8_t> mask; /* boxes layout of the tagged level */
+    std::vector<IBox> new_boxes;
+};
+
+template <class B>
+class Driver {
+  public:
+    using Level = typename B::Level;
+
+    Driver(B &backend, const Config &cfg) : b(backend), c(cfg) {
+        if (c.max_level < 0 || c.N0 <= 0 || c.blocking_factor < 2 ||
+            c.max_grid_size % c.blocking_factor != 0 || c.blocking_factor % 2 != 0)
+            throw std::invalid_argument("invalid AMR configuration");
+        shadow_hierarchy = false;
+        for (double x : c.te_crit)
+            if (x != DBL_MAX) shadow_hierarchy = true;
+        for (int l = 0; l <= c.max_level; ++l) {
+            dimN.push_back(c.N0 << l);
+            dx.push_back(c.L / (double)dimN[l]);
+            dt.push_back(dx[l] * c.cfl);
+            regrid_dt.push_back(c.regrid_dt / std::pow(2., l));
+            last_regrid_time.push_back(c.t_start);
+        }
+        levels.resize(c.max_level + 1);
+        boxes.resize(c.max_level + 1);
+        te_valid.assign(c.max_level + 1, false);
+    }
+
+    ~Driver() {
+        for (int l = 0; l <= finest; ++l) b.destroy(levels[l]);
+        if (shadow_defined) b.destroy(shadow);
+    }
+
+    /* Level 0 from the caller's data: boxes of max_grid_size cells. */
+    void init_coarse(const std::function<void(Level &)> &fill) {
+        boxes[0] = chop(0, c.N0, c.max_grid_size);
+        levels[0] = b.create(0, boxes[0], dimN[0]);
+        fill(levels[0]);
+        b.set_time(levels[0], kNew, c.t_start, 0);
+        b.set_time(levels[0], kOld, -DBL_MAX, 0);
+        finest = 0;
+    }
+
+    /* One coarse step (Evolve's loop body). */
+    void step() { advance(0); }
+
+    /* ---- queries ---- */
+    int finest = 0;
+    bool shadow_hierarchy = false;
+    std::vector<std::vector<IBox>> boxes;
+    std::vector<Level> levels;
+    std::vector<double> dt, dx;
+    std::vector<int> dimN;
+    std::vector<RegridRecord> regrids;
+    bool record_regrids = false;
+    long long cell_updates = 0;
+    std::vector<std::string> trace; /* advance/sync/regrid events */
+    bool record_trace = false;
+
+  private:
+    B &b;
+    Config c;
+    Level shadow{};
+    bool shadow_defined = false;
+    std::vector<bool> te_valid;
+    struct Sched {
+        int lowest;
+        double t;
+        bool matches(double time) const {
+            double teps = t * 1e-12;
+            return t > time - teps && t < time + teps;
+        }
+    };
+    std::vector<Sched> schedule;
+    std::vector<double> regrid_dt, last_regrid_time;
+
+    void note(const std::string &s) {
+        if (record_trace) trace.push_back(s);
+    }
+
+    /* ---- RegridScheduler ---- */
+    int find_schedule(double t) const {
+        for (size_t q = 0; q < schedule.size(); ++q)
+            if (schedule[q].matches(t)) return (int)q;
+        return -1;
+    }
+    void schedule_regrid(int lev, double t) {
+        int id = find_schedule(t);
+        if (id < 0) schedule.push_back(Sched{lev, t});
+        else schedule[id].lowest = std::min(lev, schedule[id].lowest);
+    }
+    bool do_regrid_at(int lev, double t) const {
+        int id = find_schedule(t);
+        return id >= 0 && schedule[id].lowest == lev;
+    }
+    bool need_te(int lev, double t) const {
+        int id = find_schedule(t);
+        return id >= 0 && lev >= schedule[id].lowest;
+    }
+    void did_regrid(double t) {
+        int id = find_schedule(t);
+        if (id >= 0) schedule.erase(schedule.begin() + id);
+    }
+
+    /* ---- project hook: Sledgehamr::DoCreateLevelIf ---- */
+    bool create_level_if(int lev, double time) const {
+        if (lev <= 0) return true;
+        if (c.string_width_threshold <= 0) return true;
+        /* StringWidth(lev-1, eta) = 1 / (sqrt(2 lambda) eta dx[lev-1]) */
+        const double mr = std::sqrt(2. * c.string_lambda) * time;
+        const double width = 1. / (mr * dx[lev - 1]);
+        return width <= c.string_width_threshold;
+    }
+
+    double tnew(int lev) { return b.time(levels[lev], kNew); }
+    int istep_new(int lev) { return b.istep(levels[lev], kNew); }
+
+    /* ---- TimeStepper::Advance ---- */
+    void advance(int lev) {
+        if (shadow_hierarchy) schedule_regrid_if_needed(lev);
+        else no_shadow_regrid(lev);
+        note("advance " + std::to_string(lev) + " t=" + std::to_string(tnew(lev)));
+        b.advance(lev, levels[lev], lev > 0 ? &levels[lev - 1] : nullptr, dt[lev], dx[lev],
+                  false);
+        te_valid[lev] = false;
+        for (const IBox &bx : boxes[lev]) cell_updates += bx.volume();
+        if (lev != finest) {
+            advance(lev + 1);
+            advance(lev + 1);
+        }
+        synchronize_levels(lev);
+        do_regrid_if_scheduled(lev);
+        if (lev == 0)
+            for (int l = 1; l <= finest; ++l)
+                b.set_time(levels[l], kNew, tnew(0), istep_new(l));
+    }
+
+    void synchronize_levels(int lev) {
+        const bool te = need_te(lev, tnew(lev));
+        if (lev < finest) {
+            if (!(shadow_hierarchy && te)) {
+                note("average_down " + std::to_string(lev + 1) + "->" + std::to_string(lev));
+                b.average_down(levels[lev + 1], kNew, levels[lev], kNew);
+                te_valid[lev + 1] = false;
+            }
+        }
+        if (lev >= 1 - (shadow_hierarchy ? 1 : 0) && te) {
+            note("truncation_errors " + std::to_string(lev));
+            if (lev == 0) {
+                const double ts = b.time(shadow, kNew);
+                if (!(std::fabs(ts - tnew(0)) < tnew(0) * 1e-8))
+                    throw std::runtime_error("shadow level not in sync with the coarse level");
+                b.average_down_te(levels[0], shadow);
+                b.destroy(shadow);
+                shadow_defined = false;
+            } else {
+                b.average_down_te(levels[lev], levels[lev - 1]);
+            }
+            te_valid[lev] = true;
+        }
+    }
+
+    /* TimeStepper::ScheduleRegrid */
+    void schedule_regrid_if_needed(int lev) {
+        const double time = tnew(lev);
+        const int istep = istep_new(lev);
+        if (do_regrid_at(lev, time + dt[lev])) return;
+        if (b.time(levels[lev], kOld) == time) return;
+        if (lev >= c.max_level) return;
+        if (istep % 2 == 0 && lev > 0) return;
+        const double next = lev > 0 ? time + 3. * dt[lev] : time + 2. * dt[lev];
+        if (!create_level_if(lev + 1, next)) return;
+        if (next <= last_regrid_time[lev] + regrid_dt[lev]) return;
+        if (lev == 0 && b.time(levels[0], kOld) == -DBL_MAX) return;
+        schedule_regrid(lev, time + dt[lev]);
+        note("schedule " + std::to_string(lev) + " at " + std::to_string(time + dt[lev]));
+        if (lev == 0) create_shadow_level();
+    }
+
+    /* Sledgehamr::CreateShadowLevel + Integrator::Advance(-1) */
+    void create_shadow_level() {
+        std::vector<IBox> sb;
+        for (const IBox &bx : boxes[0]) {
+            IBox s;
+            for (int d = 0; d < 3; ++d) {
+                s.lo[d] = bx.lo[d] / 2;
+                s.hi[d] = bx.hi[d] / 2;
+            }
+            sb.push_back(s);
+        }
+        if (shadow_defined) b.destroy(shadow);
+        shadow = b.create(-1, sb, dimN[0] / 2);
+        shadow_defined = true;
+        const double t_old = b.time(levels[0], kOld);
+        b.average_down(levels[0], kOld, shadow, kOld);
+        b.set_time(shadow, kOld, t_old, 0);
+        b.advance(-1, shadow, nullptr, 2. * dt[0], 2. * dx[0], true);
+        note("shadow advanced to " + std::to_string(b.time(shadow, kNew)));
+    }
+
+    void do_regrid_if_scheduled(int lev) {
+        const double time = tnew(lev);
+        if (!do_regrid_at(lev, time)) return;
+        do_regrid(lev, time);
+        did_regrid(time);
+    }
+
+    /* TimeStepper::NoShadowRegrid */
+    void no_shadow_regrid(int lev) {
+        const double time = tnew(lev);
+        if (lev >= c.max_level) return;
+        if (time + dt[lev] <= last_regrid_time[lev] + regrid_dt[lev]) return;
+        if (!create_level_if(lev + 1, time + dt[lev])) return;
+        do_regrid(lev, time);
+    }
+
+    /* TimeStepper::DoRegrid with the global regrid path. */
+    void do_regrid(int lev, double time) {
+        note("regrid " + std::to_string(lev) + " at " + std::to_string(time));
+        regrid(lev, time);
+        for (int l = lev; l <= finest; ++l) last_regrid_time[l] = time;
+    }
+
+    /* ---- new grids ---- */
+    static std::vector<IBox> chop(int lo_unused, int N, int mg) {
+        std::vector<IBox> r;
+        for (int z = 0; z < N; z += mg)
+            for (int y = 0; y < N; y += mg)
+                for (int x = 0; x < N; x += mg)
+                    r.push_back(IBox{{x, y, z},
+                                     {std::min(x + mg, N) - 1, std::min(y + mg, N) - 1,
+                                      std::min(z + mg, N) - 1}});
+        return r;
+    }
+
+    static int pmod(int a, int n) {
+        int r = a % n;
+        return r < 0 ? r + n : r;
+    }
+    static int fdiv(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
+
+    /* Sledgehamr::ErrorEst: tags of level l at `time` (empty if skipped). */
+    std::vector<uint8_t> error_est(int l, double time) {
+        if (time == c.t_start && shadow_hierarchy) return {};
+        if (!create_level_if(l + 1, time)) return {};
+        if (shadow_hierarchy && !te_valid[l])
+            throw std::runtime_error("tagging with truncation errors but none computed on level " +
+                                     std::to_string(l));
+        return b.tag(levels[l], shadow_hierarchy, time, l, dt[l], dx[l]);
+    }
+
+    /* New boxes of level l+1 from the tags of level l (mask in the boxes
+     * layout of mask_boxes), nested in the (new) boxes of level l. */
+    std::vector<IBox> new_grids(int l, const std::vector<uint8_t> &mask,
+                                const std::vector<IBox> &mask_boxes,
+                                const std::vector<IBox> &nest_boxes) {
+        const int bf = c.blocking_factor;
+        const int cb = bf / 2;              /* block size in level-l cells */
+        const int Nl = dimN[l];
+        if (Nl % cb != 0) throw std::runtime_error("level size not a multiple of the block");
+        const int nb = Nl / cb;             /* blocks per side */
+        std::vector<uint8_t> blk((size_t)nb * nb * nb, 0);
+        const int buf = c.n_error_buf;
+        size_t q = 0;
+        for (const IBox &bx : mask_boxes)
+            for (int k = bx.lo[2]; k <= bx.hi[2]; ++k)
+                for (int j = bx.lo[1]; j <= bx.hi[1]; ++j)
+                    for (int i = bx.lo[0]; i <= bx.hi[0]; ++i, ++q) {
+                        if (!mask[q]) continue;
+                        /* blocks touched by the buffered cell [i-buf, i+buf]^3 */
+                        const int b0[3] = {fdiv(i - buf, cb), fdiv(j - buf, cb),
+                                           fdiv(k - buf, cb)};
+                        const int b1[3] = {fdiv(i + buf, cb), fdiv(j + buf, cb),
+                                           fdiv(k + buf, cb)};
+                        for (int bk = b0[2]; bk <= b1[2]; ++bk)
+                            for (int bj = b0[1]; bj <= b1[1]; ++bj)
+                                for (int bi = b0[0]; bi <= b1[0]; ++bi)
+                                    blk[((size_t)pmod(bk, nb) * nb + pmod(bj, nb)) * nb +
+                                        pmod(bi, nb)] = 1;
+                    }
+        if (l >= 1) {
+            /* nesting: the block grown by m level-l cells must lie in level l */
+            const int m = (c.nghost + 1) / 2 + 1;
+            const int lb = c.blocking_factor; /* level-l boxes are unions of these */
+            const int nlb = Nl / lb;
+            std::vector<uint8_t> cov((size_t)nlb * nlb * nlb, 0);
+            for (const IBox &bx : nest_boxes)
+                for (int k = bx.lo[2] / lb; k <= bx.hi[2] / lb; ++k)
+                    for (int j = bx.lo[1] / lb; j <= bx.hi[1] / lb; ++j)
+                        for (int i = bx.lo[0] / lb; i <= bx.hi[0] / lb; ++i)
+                            cov[((size_t)k * nlb + j) * nlb + i] = 1;
+            for (int bk = 0; bk < nb; ++bk)
+                for (int bj = 0; bj < nb; ++bj)
+                    for (int bi = 0; bi < nb; ++bi) {
+                        uint8_t &v = blk[((size_t)bk * nb + bj) * nb + bi];
+                        if (!v) continue;
+                        const int lo[3] = {bi * cb - m, bj * cb - m, bk * cb - m};
+                        const int hi[3] = {(bi + 1) * cb + m - 1, (bj + 1) * cb + m - 1,
+                                           (bk + 1) * cb + m - 1};
+                        bool ok = true;
+                        for (int z = (int)std::floor((double)lo[2] / lb);
+                             ok && z <= (int)std::floor((double)hi[2] / lb); ++z)
+                            for (int y = (int)std::floor((double)lo[1] / lb);
+                                 ok && y <= (int)std::floor((double)hi[1] / lb); ++y)
+                                for (int x = (int)std::floor((double)lo[0] / lb);
+                                     ok && x <= (int)std::floor((double)hi[0] / lb); ++x)
+                                    ok = cov[((size_t)pmod(z, nlb) * nlb + pmod(y, nlb)) * nlb +
+                                             pmod(x, nlb)] != 0;
+                        if (!ok) v = 0;
+                    }
+        }
+        /* merge tagged blocks within aligned windows of max_grid_size */
+        const int w = c.max_grid_size / bf; /* blocks per window side */
+        std::vector<IBox> out;
+        for (int wz = 0; wz < nb; wz += w)
+            for (int wy = 0; wy < nb; wy += w)
+                for (int wx = 0; wx < nb; wx += w) {
+                    struct Run {
+                        int x0, x1, y0, y1, z0, z1;
+                    };
+                    std::vector<Run> runs;
+                    for (int z = wz; z < std::min(wz + w, nb); ++z)
+                        for (int y = wy; y < std::min(wy + w, nb); ++y) {
+                            int x = wx;
+                            while (x < std::min(wx + w, nb)) {
+                                if (!blk[((size_t)z * nb + y) * nb + x]) {
+                                    ++x;
+                                    continue;
+                                }
+                                int x1 = x;
+                                while (x1 + 1 < std::min(wx + w, nb) &&
+                                       blk[((size_t)z * nb + y) * nb + x1 + 1])
+                                    ++x1;
+                                runs.push_back(Run{x, x1, y, y, z, z});
+                                x = x1 + 1;
+                            }
+                        }
+                    /* merge runs with equal x extent along y, then along z */
+                    auto merge = [&](bool along_y) {
+                        std::vector<Run> res;
+                        for (const Run &r : runs) {
+                            bool merged = false;
+                            for (Run &p : res) {
+                                if (along_y) {
+                                    if (p.x0 == r.x0 && p.x1 == r.x1 && p.z0 == r.z0 &&
+                                        p.z1 == r.z1 && p.y1 + 1 == r.y0) {
+                                        p.y1 = r.y1;
+                                        merged = true;
+                                        break;
+                                    }
+                                } else {
+                                    if (p.x0 == r.x0 && p.x1 == r.x1 && p.y0 == r.y0 &&
+                                        p.y1 == r.y1 && p.z1 + 1 == r.z0) {
+                                        p.z1 = r.z1;
+                                        merged = true;
+                                        break;
+                                    }
+                                }
+                            }
+                            if (!merged) res.push_back(r);
+                        }
+                        runs = res;
+                    };
+                    merge(true);
+                    merge(false);
+                    for (const Run &r : runs)
+                        out.push_back(IBox{{r.x0 * bf, r.y0 * bf, r.z0 * bf},
+                                           {(r.x1 + 1) * bf - 1, (r.y1 + 1) * bf - 1,
+                                            (r.z1 + 1) * bf - 1}});
+                }
+        return out;
+    }
+
+    /* AmrCore::regrid(lbase, time) with the grids above. */
+    void regrid(int lbase, double time) {
+        const int top = std::min(finest, c.max_level - 1);
+        /* tags of every level on its current grids first (ErrorEst) */
+        std::vector<std::vector<uint8_t>> tags(top + 1);
+        std::vector<std::vector<IBox>> old_boxes = boxes;
+        for (int l = lbase; l <= top; ++l) tags[l] = error_est(l, time);
+        int new_finest = lbase;
+        for (int l = lbase; l <= top; ++l) {
+            std::vector<IBox> nb;
+            if (!tags[l].empty()) nb = new_grids(l, tags[l], old_boxes[l], boxes[l]);
+            if (record_regrids) {
+                RegridRecord rr;
+                rr.lev = l;
+                rr.time = time;
+                rr.boxes_tagged_level = old_boxes[l];
+                rr.mask = tags[l];
+                rr.new_boxes = nb;
+                regrids.push_back(rr);
+            }
+            if (nb.empty()) break;
+            const int f = l + 1;
+            b.refresh_ghosts(levels[l], kNew, l > 0 ? &levels[l - 1] : nullptr);
+            if (f <= finest) {
+                /* RemakeLevel: fill the new layout from the old one and the
+                 * coarse level; the old time level is redefined, times kept */
+                const double tn = b.time(levels[f], kNew), to = b.time(levels[f], kOld);
+                const int sn = b.istep(levels[f], kNew), so = b.istep(levels[f], kOld);
+                Level fresh = b.create(f, nb, dimN[f]);
+                b.remake(fresh, levels[f], levels[l], time);
+                b.destroy(levels[f]);
+                levels[f] = fresh;
+                b.set_time(levels[f], kNew, tn, sn);
+                b.set_time(levels[f], kOld, to, so);
+            } else {
+                /* MakeNewLevelFromCoarse */
+                Level fresh = b.create(f, nb, dimN[f]);
+                b.fill_from_coarse(fresh, levels[l], time);
+                levels[f] = fresh;
+                b.set_time(levels[f], kNew, time, 0);
+                b.set_time(levels[f], kOld, -DBL_MAX, 0);
+            }
+            boxes[f] = nb;
+            te_valid[f] = false;
+            new_finest = f;
+            if (f > finest) break; /* at most one new level per regrid */
+        }
+        /* ClearLevel for the levels above the new finest */
+        for (int l = finest; l > new_finest; --l) {
+            b.destroy(levels[l]);
+            levels[l] = Level{};
+            boxes[l].clear();
+        }
+        finest = new_finest;
+    }
+};
+
+} // namespace shamr
+
+#endif

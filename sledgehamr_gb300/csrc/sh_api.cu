@@ -91,6 +91,16 @@ struct sh_level {
     int kbuf_count = 0;
     double t[2] = {-1.7976931348623157e308, -1.7976931348623157e308};
     int istep[2] = {0, 0};
+    /* coarse level for two-level ghost fills (nullptr: periodic single level) */
+    sh_level *coarse = nullptr;
+    void *d_cf = nullptr; /* CfRect list of ghost cells interpolated from coarse */
+    int ncf_rects = 0;
+    long long ncf = 0;    /* cells in those rectangles */
+    std::vector<int> owner; /* owner box of each block of owner_res cells */
+    int owner_res = 1;
+    int owner_nb[3] = {1, 1, 1};
+    int *d_owner = nullptr;
+    int lev_index = 0;    /* `lev` handed to the project hooks */
 };
 
 namespace {
@@ -271,6 +281,137 @@ __global__ void ghost_copy_kernel(const BoxDev *boxes, const GhostCopyDev *rects
     }
 }
 
+/* A rectangle [lo, hi] of cells of box dbox (ghost-grown) filled by
+ * quadratic interpolation from the coarse level. */
+struct CfRect {
+    int dbox;
+    int lo[3], hi[3];
+    long long first; /* running cell count */
+};
+
+/* Block map of a level: owner box of every aligned block of `res` cells
+ * (-1 where no box). */
+struct OwnerMapDev {
+    const int *owner;
+    int res;
+    int nb[3];
+    int dlo[3];
+    int ext[3];
+};
+
+/* Copy rectangles between two levels (dst ghost-grown cells from src valid
+ * cells shifted by a periodic image). */
+__global__ void copy_rects_kernel(const BoxDev *dboxes, double *dbuf, const BoxDev *sboxes,
+                                  const double *sbuf, const GhostCopyDev *rects, int nrects,
+                                  long long ncells, int ncomp) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncells;
+         c += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = nrects - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (rects[mid].first <= c) lo = mid;
+            else hi = mid - 1;
+        }
+        const GhostCopyDev &r = rects[lo];
+        const long long lc = c - r.first;
+        const int nx = r.hi[0] - r.lo[0] + 1, ny = r.hi[1] - r.lo[1] + 1;
+        const int i = r.lo[0] + (int)(lc % nx);
+        const int j = r.lo[1] + (int)((lc / nx) % ny);
+        const int k = r.lo[2] + (int)(lc / ((long long)nx * ny));
+        const BoxDev &db = dboxes[r.dbox];
+        const BoxDev &sb = sboxes[r.sbox];
+        const int si = i - r.shift[0], sj = j - r.shift[1], sk = k - r.shift[2];
+        const long long di = db.off * ncomp + (i - db.glo[0]) +
+                             (long long)(j - db.glo[1]) * db.gdim[0] +
+                             (long long)(k - db.glo[2]) * db.gdim[0] * db.gdim[1];
+        const long long sidx = sb.off * ncomp + (si - sb.glo[0]) +
+                               (long long)(sj - sb.glo[1]) * sb.gdim[0] +
+                               (long long)(sk - sb.glo[2]) * sb.gdim[0] * sb.gdim[1];
+        for (int n = 0; n < ncomp; ++n) dbuf[di + n * db.gvol] = sbuf[sidx + n * sb.gvol];
+    }
+}
+
+/* Quadratic (CellQuadratic) interpolation of fine cells from the 3x3x3
+ * coarse cells around their parent, after linear interpolation in time
+ * between the coarse old and new data (mode 0: old only, 1: new only,
+ * 2: alpha old + beta new).  With u_abc the coarse values at offsets
+ * a, b, c in {-1, 0, 1} and xi = -1/4 or +1/4 the fine-cell centre offset
+ * in coarse units per axis:
+ *   u = u000 + sum_d xi_d D_d + 1/2 sum_d xi_d^2 D_dd + sum_{d<e} xi_d xi_e D_de
+ * with D_d = (u_+ - u_-)/2, D_dd = u_+ - 2 u_0 + u_-, and
+ * D_de = (u_++ - u_+- - u_-+ + u_--)/4 in the plane of d and e.
+ * The parent (periodically wrapped) is found through the coarse level's
+ * block map; its neighbours are read from the parent box's ghost cells. */
+__global__ void cf_interp_kernel(const CfRect *rects, int nrects, long long ncells,
+                                 const BoxDev *fboxes, double *fbuf, const BoxDev *cboxes,
+                                 OwnerMapDev cmap, const double *c_old, const double *c_new,
+                                 int mode, double alpha, double beta, int ncomp) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < ncells;
+         q += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = nrects - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (rects[mid].first <= q) lo = mid;
+            else hi = mid - 1;
+        }
+        const CfRect &r = rects[lo];
+        const long long lc = q - r.first;
+        const int nx = r.hi[0] - r.lo[0] + 1, ny = r.hi[1] - r.lo[1] + 1;
+        const int fi = r.lo[0] + (int)(lc % nx);
+        const int fj = r.lo[1] + (int)((lc / nx) % ny);
+        const int fk = r.lo[2] + (int)(lc / ((long long)nx * ny));
+        const int f3[3] = {fi, fj, fk};
+        int P[3], W[3], o = 0;
+        for (int d = 0; d < 3; ++d) {
+            P[d] = f3[d] >= 0 ? f3[d] / 2 : -((-f3[d] + 1) / 2);
+            o |= (f3[d] - 2 * P[d]) << d;
+            int w = (P[d] - cmap.dlo[d]) % cmap.ext[d];
+            if (w < 0) w += cmap.ext[d];
+            W[d] = cmap.dlo[d] + w;
+        }
+        const int cbox = cmap.owner[((long long)((W[2] - cmap.dlo[2]) / cmap.res) * cmap.nb[1] +
+                                     (W[1] - cmap.dlo[1]) / cmap.res) *
+                                        cmap.nb[0] +
+                                    (W[0] - cmap.dlo[0]) / cmap.res];
+        if (cbox < 0) continue; /* excluded by the host's coverage check */
+        const BoxDev &fb = fboxes[r.dbox];
+        const BoxDev &cb = cboxes[cbox];
+        const long long cx = cb.gdim[0], cxy = cx * cb.gdim[1];
+        const long long c0 = cb.off * ncomp + (W[0] - cb.glo[0]) + (W[1] - cb.glo[1]) * cx +
+                             (W[2] - cb.glo[2]) * cxy;
+        const long long f0 = fb.off * ncomp + (fi - fb.glo[0]) +
+                             (long long)(fj - fb.glo[1]) * fb.gdim[0] +
+                             (long long)(fk - fb.glo[2]) * fb.gdim[0] * fb.gdim[1];
+        const double xi = (o & 1) ? 0.25 : -0.25;
+        const double yi = (o & 2) ? 0.25 : -0.25;
+        const double zi = (o & 4) ? 0.25 : -0.25;
+        for (int nn = 0; nn < ncomp; ++nn) {
+            const long long base = c0 + nn * cb.gvol;
+            auto u = [&](int a, int b2, int d) {
+                const long long e = base + a + b2 * cx + d * cxy;
+                if (mode == 0) return c_old[e];
+                if (mode == 1) return c_new[e];
+                return alpha * c_old[e] + beta * c_new[e];
+            };
+            const double u0 = u(0, 0, 0);
+            const double dxp = u(1, 0, 0), dxm = u(-1, 0, 0);
+            const double dyp = u(0, 1, 0), dym = u(0, -1, 0);
+            const double dzp = u(0, 0, 1), dzm = u(0, 0, -1);
+            const double Dx = (dxp - dxm) * 0.5, Dy = (dyp - dym) * 0.5, Dz = (dzp - dzm) * 0.5;
+            const double Dxx = dxp - 2. * u0 + dxm;
+            const double Dyy = dyp - 2. * u0 + dym;
+            const double Dzz = dzp - 2. * u0 + dzm;
+            const double Dxy = (u(1, 1, 0) - u(1, -1, 0) - u(-1, 1, 0) + u(-1, -1, 0)) * 0.25;
+            const double Dxz = (u(1, 0, 1) - u(1, 0, -1) - u(-1, 0, 1) + u(-1, 0, -1)) * 0.25;
+            const double Dyz = (u(0, 1, 1) - u(0, 1, -1) - u(0, -1, 1) + u(0, -1, -1)) * 0.25;
+            const double v = u0 + xi * Dx + yi * Dy + zi * Dz +
+                             0.5 * (xi * xi * Dxx + yi * yi * Dyy + zi * zi * Dzz) +
+                             xi * yi * Dxy + xi * zi * Dxz + yi * zi * Dyz;
+            fbuf[f0 + nn * fb.gvol] = v;
+        }
+    }
+}
+
 /* One rectangle of coarse cells [lo, hi] lying in coarse box cbox and under
  * fine box fbox. */
 struct AvgRect {
@@ -441,52 +582,200 @@ bool box_intersect(const int alo[3], const int ahi[3], const int blo[3], const i
     return true;
 }
 
-void build_ghost_plan(sh_level *L) {
-    std::vector<GhostCopyDev> rects;
-    long long run = 0;
-    const int ext[3] = {L->dhi[0] - L->dlo[0] + 1, L->dhi[1] - L->dlo[1] + 1,
-                        L->dhi[2] - L->dlo[2] + 1};
-    const int g = L->nghost;
-    for (size_t b = 0; b < L->boxes.size(); ++b) {
-        int glo[3], ghi[3];
-        for (int d = 0; d < 3; ++d) {
-            glo[d] = L->boxes[b].lo[d] - g;
-            ghi[d] = L->boxes[b].hi[d] + g;
+/* Owner map of a level: blocks of `res` cells, res = the largest size that
+ * divides the domain and every box bound (boxes are unions of blocks). */
+void build_owner_map(sh_level *L) {
+    auto gcd = [](int a, int b) {
+        a = a < 0 ? -a : a;
+        b = b < 0 ? -b : b;
+        while (b) {
+            int r = a % b;
+            a = b;
+            b = r;
         }
-        for (size_t s = 0; s < L->boxes.size(); ++s)
-            for (int sz = -1; sz <= 1; ++sz)
-                for (int sy = -1; sy <= 1; ++sy)
-                    for (int sx = -1; sx <= 1; ++sx) {
-                        if (s == b && sx == 0 && sy == 0 && sz == 0) continue;
-                        const int sh[3] = {sx * ext[0], sy * ext[1], sz * ext[2]};
-                        int slo[3], shi[3];
-                        for (int d = 0; d < 3; ++d) {
-                            slo[d] = L->boxes[s].lo[d] + sh[d];
-                            shi[d] = L->boxes[s].hi[d] + sh[d];
-                        }
-                        int lo[3], hi[3];
-                        if (!box_intersect(glo, ghi, slo, shi, lo, hi)) continue;
+        return a;
+    };
+    int res = 0;
+    for (int d = 0; d < 3; ++d) res = gcd(res, L->dhi[d] - L->dlo[d] + 1);
+    for (const sh_box &b : L->boxes)
+        for (int d = 0; d < 3; ++d) {
+            res = gcd(res, b.lo[d] - L->dlo[d]);
+            res = gcd(res, b.hi[d] + 1 - L->dlo[d]);
+        }
+    if (res <= 0) res = 1;
+    L->owner_res = res;
+    for (int d = 0; d < 3; ++d) L->owner_nb[d] = (L->dhi[d] - L->dlo[d] + 1) / res;
+    L->owner.assign((size_t)L->owner_nb[0] * L->owner_nb[1] * L->owner_nb[2], -1);
+    for (size_t q = 0; q < L->boxes.size(); ++q) {
+        const sh_box &b = L->boxes[q];
+        for (int z = (b.lo[2] - L->dlo[2]) / res; z <= (b.hi[2] - L->dlo[2]) / res; ++z)
+            for (int y = (b.lo[1] - L->dlo[1]) / res; y <= (b.hi[1] - L->dlo[1]) / res; ++y)
+                for (int x = (b.lo[0] - L->dlo[0]) / res; x <= (b.hi[0] - L->dlo[0]) / res; ++x) {
+                    int &o = L->owner[((size_t)z * L->owner_nb[1] + y) * L->owner_nb[0] + x];
+                    if (o >= 0) throw ShError(SH_ERR_ARG, "boxes of a level overlap");
+                    o = (int)q;
+                }
+    }
+    L->d_owner = (int *)dmalloc(L->owner.size() * sizeof(int), "owner map");
+    ck(cudaMemcpy(L->d_owner, L->owner.data(), L->owner.size() * sizeof(int),
+                  cudaMemcpyHostToDevice),
+       "owner map upload");
+}
+
+OwnerMapDev owner_map_dev(const sh_level *L) {
+    OwnerMapDev m;
+    m.owner = L->d_owner;
+    m.res = L->owner_res;
+    for (int d = 0; d < 3; ++d) {
+        m.nb[d] = L->owner_nb[d];
+        m.dlo[d] = L->dlo[d];
+        m.ext[d] = L->dhi[d] - L->dlo[d] + 1;
+    }
+    return m;
+}
+
+inline int floordiv(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
+
+/* Fill plan of dst's ghost-grown boxes, built on the block grid of src:
+ * every block region of a dst box takes the valid cells of its owner box in
+ * src (periodic images included) and regions no src box owns are
+ * interpolated from the coarse level (FillPatchTwoLevels /
+ * InterpFromCoarseLevel).  With ghosts_only (src == dst: ghost fill) the
+ * valid region of every dst box is skipped. */
+struct FillPlan {
+    std::vector<GhostCopyDev> rects;
+    long long rect_cells = 0;
+    std::vector<CfRect> cf;
+    long long cf_cells = 0;
+};
+
+FillPlan build_fill_plan(const sh_level *D, const sh_level *S, const sh_level *C,
+                         bool ghosts_only) {
+    FillPlan P;
+    const int ext[3] = {D->dhi[0] - D->dlo[0] + 1, D->dhi[1] - D->dlo[1] + 1,
+                        D->dhi[2] - D->dlo[2] + 1};
+    if (S)
+        for (int d = 0; d < 3; ++d)
+            require(S->dlo[d] == D->dlo[d] && S->dhi[d] == D->dhi[d],
+                    "fill source has a different domain");
+    if (C) {
+        require(C->ncomp == D->ncomp, "coarse level differs in components");
+        require(C->nghost >= 1, "coarse level needs at least one ghost cell");
+        for (int d = 0; d < 3; ++d)
+            require(2 * (C->dhi[d] - C->dlo[d] + 1) == ext[d] && 2 * C->dlo[d] == D->dlo[d],
+                    "coarse domain is not the fine domain coarsened by 2");
+    }
+    /* blocks: those of src, or (no src) those of dst */
+    const sh_level *G = S ? S : D;
+    const int R = G->owner_res;
+    const int g = D->nghost;
+    for (size_t b = 0; b < D->boxes.size(); ++b) {
+        int glo[3], ghi[3], blo[3], bhi[3];
+        for (int d = 0; d < 3; ++d) {
+            glo[d] = D->boxes[b].lo[d] - g;
+            ghi[d] = D->boxes[b].hi[d] + g;
+            blo[d] = floordiv(glo[d] - D->dlo[d], R);
+            bhi[d] = floordiv(ghi[d] - D->dlo[d], R);
+        }
+        for (int bz = blo[2]; bz <= bhi[2]; ++bz)
+            for (int by = blo[1]; by <= bhi[1]; ++by)
+                for (int bx = blo[0]; bx <= bhi[0]; ++bx) {
+                    const int bb[3] = {bx, by, bz};
+                    int lo[3], hi[3], sh[3], wb[3];
+                    bool inside_valid = true;
+                    for (int d = 0; d < 3; ++d) {
+                        lo[d] = std::max(glo[d], D->dlo[d] + bb[d] * R);
+                        hi[d] = std::min(ghi[d], D->dlo[d] + (bb[d] + 1) * R - 1);
+                        const int nbd = G->owner_nb[d];
+                        wb[d] = ((bb[d] % nbd) + nbd) % nbd;
+                        sh[d] = (bb[d] - wb[d]) * R; /* periodic image offset */
+                        if (lo[d] < D->boxes[b].lo[d] || hi[d] > D->boxes[b].hi[d])
+                            inside_valid = false;
+                    }
+                    if (ghosts_only && inside_valid) continue;
+                    const int own = S ? S->owner[((size_t)wb[2] * G->owner_nb[1] + wb[1]) *
+                                                     G->owner_nb[0] +
+                                                 wb[0]]
+                                      : -1;
+                    const long long ncell = (long long)(hi[0] - lo[0] + 1) *
+                                            (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+                    if (own >= 0) {
+                        if (S == D && own == (int)b && sh[0] == 0 && sh[1] == 0 && sh[2] == 0)
+                            continue;
                         GhostCopyDev r;
                         r.dbox = (int)b;
-                        r.sbox = (int)s;
+                        r.sbox = own;
                         for (int d = 0; d < 3; ++d) {
                             r.lo[d] = lo[d];
                             r.hi[d] = hi[d];
                             r.shift[d] = sh[d];
                         }
-                        r.first = run;
-                        run += (long long)(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) *
-                               (hi[2] - lo[2] + 1);
-                        rects.push_back(r);
+                        r.first = P.rect_cells;
+                        P.rect_cells += ncell;
+                        P.rects.push_back(r);
+                        continue;
                     }
+                    if (!C) continue; /* nothing to fill from: left as is */
+                    /* parents of the region must lie on the coarse level */
+                    for (int pz = floordiv(lo[2], 2); pz <= floordiv(hi[2], 2); ++pz)
+                        for (int py = floordiv(lo[1], 2); py <= floordiv(hi[1], 2); ++py)
+                            for (int px = floordiv(lo[0], 2); px <= floordiv(hi[0], 2); ++px) {
+                                const int p3[3] = {px, py, pz};
+                                int cb[3];
+                                for (int d = 0; d < 3; ++d) {
+                                    const int cext = C->dhi[d] - C->dlo[d] + 1;
+                                    int w = (p3[d] - C->dlo[d]) % cext;
+                                    if (w < 0) w += cext;
+                                    cb[d] = w / C->owner_res;
+                                }
+                                if (C->owner[((size_t)cb[2] * C->owner_nb[1] + cb[1]) *
+                                                 C->owner_nb[0] +
+                                             cb[0]] < 0)
+                                    throw ShError(SH_ERR_ARG,
+                                                  "coarse level does not cover the cells to "
+                                                  "interpolate (levels are not properly nested)");
+                            }
+                    CfRect cr;
+                    cr.dbox = (int)b;
+                    for (int d = 0; d < 3; ++d) {
+                        cr.lo[d] = lo[d];
+                        cr.hi[d] = hi[d];
+                    }
+                    cr.first = P.cf_cells;
+                    P.cf_cells += ncell;
+                    P.cf.push_back(cr);
+                }
     }
-    L->nghost_rects = (int)rects.size();
-    L->nghost_cells = run;
-    if (!rects.empty()) {
-        L->d_ghost = (GhostCopyDev *)dmalloc(rects.size() * sizeof(GhostCopyDev), "ghost plan");
-        ck(cudaMemcpy(L->d_ghost, rects.data(), rects.size() * sizeof(GhostCopyDev),
+    return P;
+}
+
+void build_ghost_plan(sh_level *L) {
+    FillPlan P = build_fill_plan(L, L, nullptr, true);
+    L->nghost_rects = (int)P.rects.size();
+    L->nghost_cells = P.rect_cells;
+    if (!P.rects.empty()) {
+        L->d_ghost = (GhostCopyDev *)dmalloc(P.rects.size() * sizeof(GhostCopyDev), "ghost plan");
+        ck(cudaMemcpy(L->d_ghost, P.rects.data(), P.rects.size() * sizeof(GhostCopyDev),
                       cudaMemcpyHostToDevice),
            "ghost plan upload");
+    }
+}
+
+/* GetLevelData time selection (level_synchronizer.cpp:613-632) for data of
+ * level C at time t; mode 0 old, 1 new, 2 both with weights. */
+void coarse_time_weights(const sh_level *C, double t, int &mode, double &alpha, double &beta) {
+    const double tn = C->t[SH_NEW], to = C->t[SH_OLD];
+    const double teps = std::fabs(tn - to) * 1.e-3;
+    alpha = 0.;
+    beta = 0.;
+    if (t > tn - teps && t < tn + teps) {
+        mode = 1;
+    } else if (t > to - teps && t < to + teps) {
+        mode = 0;
+    } else {
+        mode = 2;
+        alpha = (tn - t) / (tn - to);
+        beta = (t - to) / (tn - to);
     }
 }
 
@@ -495,6 +784,8 @@ void level_free(sh_level *L) {
     cudaFree(L->d_tiles);
     cudaFree(L->d_ghost);
     cudaFree(L->d_vbase);
+    cudaFree(L->d_cf);
+    cudaFree(L->d_owner);
     for (int q = 0; q < 3; ++q) cudaFree(L->buf[q]);
     cudaFree(L->kbuf);
 }
@@ -508,13 +799,29 @@ void ensure_kbuf(sh_level *L, size_t elems, int count) {
     L->kbuf_count = count;
 }
 
-void fill_patch(sh_ctx *ctx, sh_level *L, double *buf) {
-    if (L->nghost_cells == 0) return;
+/* FillPatch / FillIntermediatePatch of one buffer of L at time t: ghost
+ * cells from the valid cells of the same level (periodic images), then, on a
+ * fine level linked to its coarse level, the remaining ghost cells from the
+ * coarse data at time t. */
+void fill_patch(sh_ctx *ctx, sh_level *L, double *buf, double t) {
     ProfScope ps(ctx, kProfFill);
-    ghost_copy_kernel<<<grid_for(L->nghost_cells), 256, 0, ctx->stream>>>(
-        L->d_boxes, L->d_ghost, L->nghost_rects, L->nghost_cells, L->ncomp, buf);
-    ctx->launches++;
-    ck(cudaGetLastError(), "ghost fill launch");
+    if (L->nghost_cells > 0) {
+        ghost_copy_kernel<<<grid_for(L->nghost_cells), 256, 0, ctx->stream>>>(
+            L->d_boxes, L->d_ghost, L->nghost_rects, L->nghost_cells, L->ncomp, buf);
+        ctx->launches++;
+        ck(cudaGetLastError(), "ghost fill launch");
+    }
+    if (L->coarse && L->ncf > 0) {
+        int mode;
+        double alpha, beta;
+        coarse_time_weights(L->coarse, t, mode, alpha, beta);
+        cf_interp_kernel<<<grid_for(L->ncf), 256, 0, ctx->stream>>>(
+            (const CfRect *)L->d_cf, L->ncf_rects, L->ncf, L->d_boxes, buf, L->coarse->d_boxes,
+            owner_map_dev(L->coarse), L->coarse->buf[SH_OLD], L->coarse->buf[SH_NEW], mode,
+            alpha, beta, L->ncomp);
+        ctx->launches++;
+        ck(cudaGetLastError(), "coarse-fine fill launch");
+    }
 }
 
 void launch_stage(sh_ctx *ctx, sh_level *L, StageArgs &a, int ko_order) {
@@ -596,6 +903,7 @@ void integrate(sh_ctx *ctx, sh_level *L, int type, const double *tableau, int ns
     fill_common(a, L, dt, dx, params, nparams, gw_params, ngw, ko_order, ko_strength);
     a.y0 = L->buf[SH_OLD];
     a.nk = L->npairs;
+    a.lev = L->lev_index;
 
     if (type == SH_INTEGRATOR_RKN4 || type == SH_INTEGRATOR_RKN5 ||
         type == SH_INTEGRATOR_RKN_TABLEAU) {
@@ -628,7 +936,7 @@ void integrate(sh_ctx *ctx, sh_level *L, int type, const double *tableau, int ns
                 }
             }
             launch_stage(ctx, L, s, ko_order);
-            fill_patch(ctx, L, L->buf[next]);
+            fill_patch(ctx, L, L->buf[next], i < S - 1 ? t0 + dt * tb.nodes[i + 1] : t0 + dt);
             cur = next;
         }
         if (cur != SH_NEW) std::swap(L->buf[SH_NEW], L->buf[2]);
@@ -643,7 +951,7 @@ void integrate(sh_ctx *ctx, sh_level *L, int type, const double *tableau, int ns
         s.c_out = dt;
         s.out = L->buf[SH_NEW];
         launch_stage(ctx, L, s, ko_order);
-        fill_patch(ctx, L, L->buf[SH_NEW]);
+        fill_patch(ctx, L, L->buf[SH_NEW], t0 + dt);
         /* k1 = f(u1) + k1; u2 = y0 + dt/4 k1 */
         s.state = L->buf[SH_NEW];
         s.time = t0 + dt;
@@ -655,7 +963,7 @@ void integrate(sh_ctx *ctx, sh_level *L, int type, const double *tableau, int ns
         s.c_out = dt / 4.;
         s.out = L->buf[2];
         launch_stage(ctx, L, s, ko_order);
-        fill_patch(ctx, L, L->buf[2]);
+        fill_patch(ctx, L, L->buf[2], t0 + dt / 2.);
         /* k1 = f(u2) + k1/4; y1 = y0 + 2dt/3 k1 */
         s.state = L->buf[2];
         s.time = t0 + dt / 2.;
@@ -664,7 +972,7 @@ void integrate(sh_ctx *ctx, sh_level *L, int type, const double *tableau, int ns
         s.c_out = dt * 2. / 3.;
         s.out = L->buf[SH_NEW];
         launch_stage(ctx, L, s, ko_order);
-        fill_patch(ctx, L, L->buf[SH_NEW]);
+        fill_patch(ctx, L, L->buf[SH_NEW], t0 + dt);
     } else if (type == SH_INTEGRATOR_LEAPFROG) {
         ensure_kbuf(L, (size_t)L->total_gvol * L->npairs, 1);
         StageArgs s = a;
@@ -674,7 +982,7 @@ void integrate(sh_ctx *ctx, sh_level *L, int type, const double *tableau, int ns
         s.kout = L->kbuf;
         s.out = L->buf[SH_NEW];
         launch_stage(ctx, L, s, ko_order);
-        fill_patch(ctx, L, L->buf[SH_NEW]);
+        fill_patch(ctx, L, L->buf[SH_NEW], t0 + dt);
         s.state = L->buf[SH_NEW];
         s.time = t0 + dt;
         s.epi = kEpiLf1;
@@ -683,7 +991,7 @@ void integrate(sh_ctx *ctx, sh_level *L, int type, const double *tableau, int ns
         s.kout = nullptr;
         s.out = L->buf[2];
         launch_stage(ctx, L, s, ko_order);
-        fill_patch(ctx, L, L->buf[2]);
+        fill_patch(ctx, L, L->buf[2], t0 + dt);
         std::swap(L->buf[SH_NEW], L->buf[2]);
     } else if (type >= 0 && type <= 4) {
         throw ShError(SH_ERR_UNSUPPORTED, "AMReX integrators (types 0-4) are not supported");
@@ -950,6 +1258,7 @@ int sh_level_create(sh_ctx *ctx, int project, int with_gw, const int domain_lo[3
         ck(cudaMemcpy(L->d_vbase, L->vbase.data(), L->vbase.size() * sizeof(long long),
                       cudaMemcpyHostToDevice),
            "box prefix upload");
+        build_owner_map(L);
         build_ghost_plan(L);
         const size_t bytes = (size_t)L->total_gvol * L->ncomp * sizeof(double);
         for (int q = 0; q < 3; ++q) {
@@ -988,6 +1297,21 @@ int sh_level_time(const sh_level *L, int which, double *t, int *istep) {
     if (!L || (which != SH_NEW && which != SH_OLD)) return SH_ERR_ARG;
     if (t) *t = L->t[which];
     if (istep) *istep = L->istep[which];
+    return SH_OK;
+}
+
+int sh_level_boxes(const sh_level *L, sh_box *out, int capacity, int *nbox) {
+    if (!L || !nbox) return SH_ERR_ARG;
+    *nbox = (int)L->boxes.size();
+    if (!out) return SH_OK;
+    if (capacity < (int)L->boxes.size()) return SH_ERR_ARG;
+    std::copy(L->boxes.begin(), L->boxes.end(), out);
+    return SH_OK;
+}
+
+int sh_level_set_index(sh_level *L, int lev) {
+    if (!L) return SH_ERR_ARG;
+    L->lev_index = lev;
     return SH_OK;
 }
 
@@ -1042,7 +1366,75 @@ int sh_level_fill_patch(sh_ctx *ctx, sh_level *L, int which) {
     if (!ctx || !L || (which != SH_NEW && which != SH_OLD)) return SH_ERR_ARG;
     return guarded(ctx, [&] {
         set_device(ctx);
-        fill_patch(ctx, L, L->buf[which]);
+        fill_patch(ctx, L, L->buf[which], L->t[which]);
+    });
+}
+
+int sh_level_set_coarse(sh_ctx *ctx, sh_level *fine, sh_level *coarse) {
+    if (!ctx || !fine) return SH_ERR_ARG;
+    return guarded(ctx, [&] {
+        set_device(ctx);
+        cudaFree(fine->d_cf);
+        fine->d_cf = nullptr;
+        fine->ncf = 0;
+        fine->ncf_rects = 0;
+        fine->coarse = nullptr;
+        if (!coarse) return;
+        require(coarse != fine, "a level cannot be its own coarse level");
+        FillPlan P = build_fill_plan(fine, fine, coarse, true);
+        if (!P.cf.empty()) {
+            fine->d_cf = dmalloc(P.cf.size() * sizeof(CfRect), "coarse-fine plan");
+            ck(cudaMemcpy(fine->d_cf, P.cf.data(), P.cf.size() * sizeof(CfRect),
+                          cudaMemcpyHostToDevice),
+               "coarse-fine plan upload");
+        }
+        fine->ncf_rects = (int)P.cf.size();
+        fine->ncf = P.cf_cells;
+        fine->coarse = coarse;
+    });
+}
+
+int sh_level_fill_from(sh_ctx *ctx, sh_level *dst, int which_dst, const sh_level *src,
+                       int which_src, sh_level *coarse, double time) {
+    if (!ctx || !dst || (which_dst != SH_NEW && which_dst != SH_OLD)) return SH_ERR_ARG;
+    if (src && which_src != SH_NEW && which_src != SH_OLD) return SH_ERR_ARG;
+    return guarded(ctx, [&] {
+        set_device(ctx);
+        require(src != dst, "source and destination must differ");
+        if (src) require(src->ncomp == dst->ncomp, "source differs in components");
+        FillPlan P = build_fill_plan(dst, src, coarse, false);
+        void *d_rects = nullptr, *d_cf = nullptr;
+        if (!P.rects.empty()) {
+            d_rects = dmalloc(P.rects.size() * sizeof(GhostCopyDev), "fill plan");
+            ck(cudaMemcpy(d_rects, P.rects.data(), P.rects.size() * sizeof(GhostCopyDev),
+                          cudaMemcpyHostToDevice),
+               "fill plan upload");
+            ProfScope ps(ctx, kProfFill);
+            copy_rects_kernel<<<grid_for(P.rect_cells), 256, 0, ctx->stream>>>(
+                dst->d_boxes, dst->buf[which_dst], src->d_boxes, src->buf[which_src],
+                (const GhostCopyDev *)d_rects, (int)P.rects.size(), P.rect_cells, dst->ncomp);
+            ctx->launches++;
+            ck(cudaGetLastError(), "fill copy launch");
+        }
+        if (!P.cf.empty()) {
+            require(coarse != nullptr, "cells not covered by the source need a coarse level");
+            d_cf = dmalloc(P.cf.size() * sizeof(CfRect), "coarse fill plan");
+            ck(cudaMemcpy(d_cf, P.cf.data(), P.cf.size() * sizeof(CfRect), cudaMemcpyHostToDevice),
+               "coarse fill plan upload");
+            int mode;
+            double alpha, beta;
+            coarse_time_weights(coarse, time, mode, alpha, beta);
+            ProfScope ps(ctx, kProfFill);
+            cf_interp_kernel<<<grid_for(P.cf_cells), 256, 0, ctx->stream>>>(
+                (const CfRect *)d_cf, (int)P.cf.size(), P.cf_cells, dst->d_boxes,
+                dst->buf[which_dst], coarse->d_boxes, owner_map_dev(coarse), coarse->buf[SH_OLD],
+                coarse->buf[SH_NEW], mode, alpha, beta, dst->ncomp);
+            ctx->launches++;
+            ck(cudaGetLastError(), "coarse fill launch");
+        }
+        ck(cudaStreamSynchronize(ctx->stream), "fill_from");
+        cudaFree(d_rects);
+        cudaFree(d_cf);
     });
 }
 
@@ -1059,7 +1451,7 @@ int sh_level_advance(sh_ctx *ctx, sh_level *L, int integrator, const double *tab
             std::swap(L->t[SH_NEW], L->t[SH_OLD]);
             std::swap(L->istep[SH_NEW], L->istep[SH_OLD]);
         }
-        fill_patch(ctx, L, L->buf[SH_OLD]);
+        fill_patch(ctx, L, L->buf[SH_OLD], L->t[SH_OLD]);
         integrate(ctx, L, integrator, tableau, nstages, dt, dx, params, nparams, gw_params, ngw,
                   ko_order, ko_strength);
         L->t[SH_NEW] = L->t[SH_OLD] + dt;

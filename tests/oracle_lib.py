@@ -161,3 +161,70 @@ class Oracle:
         if rc != 0:
             raise RuntimeError("stencil")
         return out
+
+
+class OracleAmr:
+    """The oracle's AMR hierarchy (same time stepper, CPU numerics)."""
+
+    def __init__(self, cfg, level0):
+        build_oracle()
+        self.lib = C.CDLL(ORACLE_SO)
+        self.lib.orc_amr_create.restype = C.c_void_p
+        self.lib.orc_amr_create.argtypes = [C.c_void_p, C.c_void_p]
+        for n in ("orc_amr_step", "orc_amr_info", "orc_amr_boxes", "orc_amr_read",
+                  "orc_amr_regrid_record"):
+            getattr(self.lib, n).restype = C.c_int
+        self.lib.orc_amr_destroy.argtypes = [C.c_void_p]
+        a = _f(level0)
+        self.h = self.lib.orc_amr_create(C.byref(cfg), _p(a))
+        if not self.h:
+            raise RuntimeError("orc_amr_create failed")
+        self.h = C.c_void_p(self.h)
+        self.ncomp = a.shape[0]
+
+    def step(self, n=1):
+        if self.lib.orc_amr_step(self.h, n) != 0:
+            raise RuntimeError("orc_amr_step failed")
+
+    def info(self):
+        f, cu, nr = C.c_int(), C.c_longlong(), C.c_int()
+        self.lib.orc_amr_info(self.h, C.byref(f), C.byref(cu), C.byref(nr))
+        return {"finest": f.value, "cell_updates": cu.value, "nregrids": nr.value}
+
+    def boxes(self, lev):
+        out = np.empty(6 * 100000, dtype=np.int32)
+        n = self.lib.orc_amr_boxes(self.h, lev, _p(out), 100000)
+        if n < 0:
+            raise RuntimeError("orc_amr_boxes")
+        b = out[: 6 * n].reshape(n, 6)
+        return [(tuple(int(x) for x in r[:3]), tuple(int(x) for x in r[3:])) for r in b]
+
+    def read(self, lev, which=0):
+        bx = self.boxes(lev)
+        nv = sum((h[0] - l[0] + 1) * (h[1] - l[1] + 1) * (h[2] - l[2] + 1) for l, h in bx)
+        out = np.empty(nv * self.ncomp)
+        t = C.c_double()
+        self.lib.orc_amr_read(self.h, lev, which, _p(out), C.byref(t))
+        return out, t.value
+
+    def regrid_record(self, q):
+        lev, t = C.c_int(), C.c_double()
+        nt, nn, nm = C.c_int(), C.c_int(), C.c_longlong()
+        self.lib.orc_amr_regrid_record(self.h, q, C.byref(lev), C.byref(t), None, 0,
+                                       C.byref(nt), None, C.c_longlong(0), C.byref(nm), None, 0,
+                                       C.byref(nn))
+        tb = np.empty(6 * max(nt.value, 1), dtype=np.int32)
+        nb = np.empty(6 * max(nn.value, 1), dtype=np.int32)
+        mask = np.empty(max(nm.value, 1), dtype=np.uint8)
+        self.lib.orc_amr_regrid_record(self.h, q, C.byref(lev), C.byref(t), _p(tb), nt.value,
+                                       C.byref(nt), _p(mask), C.c_longlong(nm.value),
+                                       C.byref(nm), _p(nb), nn.value, C.byref(nn))
+        conv = lambda a, n: [(tuple(int(x) for x in r[:3]), tuple(int(x) for x in r[3:]))
+                             for r in a[: 6 * n].reshape(n, 6)]
+        return {"lev": lev.value, "time": t.value, "tagged_boxes": conv(tb, nt.value),
+                "mask": mask[: nm.value].copy(), "new_boxes": conv(nb, nn.value)}
+
+    def close(self):
+        if self.h:
+            self.lib.orc_amr_destroy(self.h)
+            self.h = None
