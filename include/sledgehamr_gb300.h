@@ -323,6 +323,64 @@ SH_API int sh_evolve_periodic(sh_ctx *ctx, int project, int integrator, const do
                        int nparams, const double *gw_params, int ngw, int ko_order,
                        const double *ko_strength);
 
+/* ------------------------------------------------------------------------ */
+/* Ensembles: many periodic cubes (realisations) of one physics family,
+ * stepped together by one set of fused stage-kernel launches per step, in
+ * FP64 or in FP32 with Kahan-compensated state updates.  No counterpart in
+ * the reference, which evolves one simulation per process; the equations
+ * and integrators are those of the projects named below.
+ *
+ *   SH_FAMILY_AXION_LAP1/2  Psi1 Psi2 Pi1 Pi2 (ncomp 4), RKN4
+ *       Pi' = -2 Pi/t + lap Psi - lambda Psi [t^2 (|Psi|^2 - 1) + c]
+ *       (AxionStringsLap1/2 of this library; 7- / 13-point Laplacian);
+ *       params per realisation: {lambda, c, 0, 0}.
+ *   SH_FAMILY_FOPT_GW       Phi dPhi u_xx u_yy u_zz u_xy u_xz u_yz du_xx ..
+ *       du_yz (ncomp 14, the level order), leapfrog (kick-drift-kick),
+ *       4th-order stencils (FirstOrderPhaseTransition with GW, pure potential);
+ *       params per realisation: {q2, q3, q4, 0}.
+ *
+ * Host arrays of one realisation are canonical (component-major, N^3 cells,
+ * x fastest).  Realisation r has N[r]^3 cells and spacing dx[r]. */
+#define SH_FAMILY_AXION_LAP1 1
+#define SH_FAMILY_AXION_LAP2 2
+#define SH_FAMILY_FOPT_GW 3
+#define SH_PREC_FP64 0
+#define SH_PREC_FP32_KAHAN 1
+#define SH_PREC_FP32 2
+
+typedef struct sh_ensemble sh_ensemble;
+
+SH_API int sh_ensemble_create(sh_ctx *ctx, int family, int precision, int nreal, const int *N,
+                              const double *dx, const double *params, sh_ensemble **out);
+SH_API int sh_ensemble_destroy(sh_ensemble *e);
+SH_API const char *sh_ensemble_last_error(const sh_ensemble *e);
+SH_API int sh_ensemble_info(const sh_ensemble *e, int *family, int *precision, int *nreal,
+                            int *ncomp, long long *cells, long long *device_bytes, int *tile_nz);
+SH_API long long sh_ensemble_kernel_launches(const sh_ensemble *e);
+/* Time of the state (all realisations share it). */
+SH_API int sh_ensemble_set_time(sh_ensemble *e, double t);
+SH_API int sh_ensemble_time(sh_ensemble *e, double *t);
+/* Upload / download realisation r (FP64 host values; an upload clears the
+ * compensation, a download returns value minus compensation). */
+SH_API int sh_ensemble_write(sh_ensemble *e, int r, const double *host);
+SH_API int sh_ensemble_read(sh_ensemble *e, int r, double *host);
+/* nsteps steps of size dt; asynchronous on the context's stream.  With
+ * graphs on, every step replays a CUDA graph of its kernels. */
+SH_API int sh_ensemble_set_graph(sh_ensemble *e, int on);
+SH_API int sh_ensemble_step(sh_ensemble *e, double dt, int nsteps);
+/* Tile depth along z; 0 times {4, 8, 16, 32, 64} on the current state
+ * (leaving state, compensation and time unchanged) and keeps the fastest. */
+SH_API int sh_ensemble_tune(sh_ensemble *e, int tile_nz, double dt, int *chosen);
+/* Diagnostics per realisation: total energy (FP64 sums of the densities
+ * listed at energy_kernel), number of string-pierced cells (axion
+ * families; plaquette winding as in AxionStrings tagging), GW spectrum of
+ * realisation r (FOPT_GW; arguments as sh_gw_spectrum). */
+SH_API int sh_ensemble_energy(sh_ensemble *e, double *energy);
+SH_API int sh_ensemble_string_count(sh_ensemble *e, long long *counts);
+SH_API int sh_ensemble_gw_spectrum(sh_ensemble *e, int r, int zero_padding, int projection_type,
+                                   int unbinned, double *bins_out, long long *ks_out,
+                                   int max_bins, int *nbins);
+
 #ifdef __cplusplus
 }
 #endif

@@ -441,3 +441,121 @@ class Amr:
             self.close()
         except Exception:
             pass
+
+
+# ensemble families and precisions (sh_ensemble_create)
+FAMILY_AXION_LAP1 = _lib.SH_FAMILY_AXION_LAP1
+FAMILY_AXION_LAP2 = _lib.SH_FAMILY_AXION_LAP2
+FAMILY_FOPT_GW = _lib.SH_FAMILY_FOPT_GW
+PREC_FP64 = _lib.SH_PREC_FP64
+PREC_FP32_KAHAN = _lib.SH_PREC_FP32_KAHAN
+PREC_FP32 = _lib.SH_PREC_FP32
+_FAMILY_NCOMP = {FAMILY_AXION_LAP1: 4, FAMILY_AXION_LAP2: 4, FAMILY_FOPT_GW: 14}
+
+
+class Ensemble:
+    """Many periodic realisations of one physics family stepped together
+    (sh_ensemble).  ``params`` holds four numbers per realisation:
+    (lambda, c, 0, 0) for the axion families, (q2, q3, q4, 0) for FOPT_GW."""
+
+    def __init__(self, ctx: Context, family: int, precision: int, N: Sequence[int],
+                 dx: Sequence[float], params=None):
+        self.ctx = ctx
+        self.family = family
+        self.N = [int(n) for n in N]
+        self.ncomp = _FAMILY_NCOMP[family]
+        n = np.ascontiguousarray(np.asarray(self.N, dtype=np.int32))
+        d = _f64(dx, len(self.N))
+        p = None if params is None else _f64(params, 4 * len(self.N))
+        h = C.c_void_p()
+        rc = ctx.lib.sh_ensemble_create(ctx.h, family, precision, len(self.N), _ptr(n), _ptr(d),
+                                        _ptr(p), C.byref(h))
+        if rc != 0:
+            raise ShError(rc, "sh_ensemble_create failed")
+        self.h = h
+
+    def check(self, rc: int, what: str):
+        if rc != 0:
+            msg = self.ctx.lib.sh_ensemble_last_error(self.h) or b""
+            raise ShError(rc, f"{what}: {msg.decode(errors='replace')}")
+
+    def info(self) -> dict:
+        f, p, nr, nc, tz = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        cells, nbytes = C.c_longlong(), C.c_longlong()
+        self.check(self.ctx.lib.sh_ensemble_info(self.h, C.byref(f), C.byref(p), C.byref(nr),
+                                                 C.byref(nc), C.byref(cells), C.byref(nbytes),
+                                                 C.byref(tz)), "sh_ensemble_info")
+        return {"family": f.value, "precision": p.value, "nreal": nr.value, "ncomp": nc.value,
+                "cells": cells.value, "device_bytes": nbytes.value, "tile_nz": tz.value}
+
+    def kernel_launches(self) -> int:
+        return int(self.ctx.lib.sh_ensemble_kernel_launches(self.h))
+
+    def set_time(self, t: float):
+        self.check(self.ctx.lib.sh_ensemble_set_time(self.h, float(t)), "set_time")
+
+    def time(self) -> float:
+        t = C.c_double()
+        self.check(self.ctx.lib.sh_ensemble_time(self.h, C.byref(t)), "time")
+        return t.value
+
+    def write(self, r: int, state: np.ndarray):
+        a = _f64(state, self.ncomp * self.N[r] ** 3)
+        self.check(self.ctx.lib.sh_ensemble_write(self.h, r, _ptr(a)), "write")
+
+    def read(self, r: int) -> np.ndarray:
+        N = self.N[r]
+        out = np.empty((self.ncomp, N, N, N), dtype=np.float64)
+        self.check(self.ctx.lib.sh_ensemble_read(self.h, r, _ptr(out)), "read")
+        return out
+
+    def set_graph(self, on: bool = True):
+        self.check(self.ctx.lib.sh_ensemble_set_graph(self.h, int(on)), "set_graph")
+
+    def step(self, dt: float, nsteps: int = 1):
+        self.check(self.ctx.lib.sh_ensemble_step(self.h, float(dt), int(nsteps)), "step")
+
+    def tune(self, dt: float, tile_nz: int = 0) -> int:
+        ch = C.c_int()
+        self.check(self.ctx.lib.sh_ensemble_tune(self.h, int(tile_nz), float(dt), C.byref(ch)),
+                   "tune")
+        return ch.value
+
+    def energy(self) -> np.ndarray:
+        e = np.empty(len(self.N), dtype=np.float64)
+        self.check(self.ctx.lib.sh_ensemble_energy(self.h, _ptr(e)), "energy")
+        return e
+
+    def string_count(self) -> np.ndarray:
+        c = np.empty(len(self.N), dtype=np.int64)
+        self.check(self.ctx.lib.sh_ensemble_string_count(self.h, _ptr(c)), "string_count")
+        return c
+
+    def gw_spectrum(self, r: int, zero_padding: int = 1, projection_type: int = 2,
+                    unbinned: bool = True):
+        P = self.N[r] * zero_padding
+        cap = 3 * (P // 2 + 1) ** 2 + 16
+        bins = np.empty(cap, dtype=np.float64)
+        ks = np.empty(cap, dtype=np.int64)
+        nb = C.c_int()
+        self.check(self.ctx.lib.sh_ensemble_gw_spectrum(
+            self.h, r, zero_padding, projection_type, int(unbinned), _ptr(bins), _ptr(ks), cap,
+            C.byref(nb)), "gw_spectrum")
+        return bins[: nb.value].copy(), ks[: nb.value].copy()
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.sh_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -23,6 +23,13 @@ SH_ERR_NONFINITE = -7
 
 SH_TAG_STATIC_MAX_CELLS = 1 << 22
 
+SH_FAMILY_AXION_LAP1 = 1
+SH_FAMILY_AXION_LAP2 = 2
+SH_FAMILY_FOPT_GW = 3
+SH_PREC_FP64 = 0
+SH_PREC_FP32_KAHAN = 1
+SH_PREC_FP32 = 2
+
 SH_NEW = 0
 SH_OLD = 1
 SH_ADVANCE_NO_SWAP = 1
@@ -72,6 +79,22 @@ SIGNATURES = {
     "sh_level_set_time": (C.c_int, [vp, C.c_int, C.c_double, C.c_int]),
     "sh_level_boxes": (C.c_int, [vp, C.POINTER(ShBox), C.c_int, ip]),
     "sh_level_set_index": (C.c_int, [vp, C.c_int]),
+    "sh_ensemble_create": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, ip, dp, dp, C.POINTER(vp)]),
+    "sh_ensemble_destroy": (C.c_int, [vp]),
+    "sh_ensemble_last_error": (C.c_char_p, [vp]),
+    "sh_ensemble_info": (C.c_int, [vp, ip, ip, ip, ip, llp, llp, ip]),
+    "sh_ensemble_kernel_launches": (C.c_longlong, [vp]),
+    "sh_ensemble_set_time": (C.c_int, [vp, C.c_double]),
+    "sh_ensemble_time": (C.c_int, [vp, dp]),
+    "sh_ensemble_write": (C.c_int, [vp, C.c_int, dp]),
+    "sh_ensemble_read": (C.c_int, [vp, C.c_int, dp]),
+    "sh_ensemble_set_graph": (C.c_int, [vp, C.c_int]),
+    "sh_ensemble_step": (C.c_int, [vp, C.c_double, C.c_int]),
+    "sh_ensemble_tune": (C.c_int, [vp, C.c_int, C.c_double, ip]),
+    "sh_ensemble_energy": (C.c_int, [vp, dp]),
+    "sh_ensemble_string_count": (C.c_int, [vp, llp]),
+    "sh_ensemble_gw_spectrum": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, dp, llp,
+                                          C.c_int, ip]),
     "sh_amr_config_defaults": (C.c_int, [C.POINTER(ShAmrConfig)]),
     "sh_amr_create": (C.c_int, [vp, C.POINTER(ShAmrConfig), vp, C.POINTER(vp)]),
     "sh_amr_destroy": (C.c_int, [vp, vp]),

@@ -1,0 +1,1094 @@
+/* Batched periodic levels ("ensembles") with fused, shared-memory-tiled
+ * stage kernels in FP32 with Kahan-compensated updates, or in FP64.
+ *
+ * These are the chosen precision and batching forms of the hot path for the
+ * two physics families of the configured workloads, written against the
+ * equations directly rather than through the double-typed plugin hooks:
+ *
+ *   axion strings (AxionStringsLap1/2, NextToMinimalExample form):
+ *     Psi' = Pi,  Pi' = -2 Pi/eta + lap_N(Psi) - lambda Psi [eta^2 (|Psi|^2-1) + c]
+ *     integrated with RKN4 (source/integrators/rkn.cpp:25-120, tableau
+ *     :130-139; every stage uses the step's initial momenta).
+ *   first-order phase transition + GW tensor (FirstOrderPhaseTransition):
+ *     Phi'' = lap Phi + q2 Phi + q3 Phi^2 + q4 Phi^3,
+ *     u_ij'' = lap u_ij + d_i Phi d_j Phi  (4th-order Laplacian and gradient)
+ *     integrated with the kick-drift-kick leapfrog (leapfrog.cpp:13-57).
+ *
+ * Layout: every realisation r of an ensemble is one periodic cube of N_r^3
+ * cells with no ghost cells (neighbours are wrapped in the kernel); each
+ * component is one array with all realisations concatenated.  A thread
+ * block owns a 32 x 8 column tile of one realisation and marches in z,
+ * keeping the (2R+1) planes the stencil needs in a shared-memory ring; the
+ * stage positions Y_i = y0 + c h y0' + h^2 sum a K_j are rebuilt while a
+ * plane is loaded (so each stage reads y0, y0' and the earlier K once,
+ * halos coming from L2), and the last stage writes the new state with
+ * compensated summation: t = y + (d - c); c = (t - y) - (d - c); y = t.
+ * Algorithmic HBM traffic per cell-update (4 components, RKN4): 26 words
+ * plus 8 compensation words; (14 components, leapfrog): 49 words plus 42.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "sh_internal.h"
+#include "sledgehamr_gb300.h"
+
+namespace sh {
+namespace fast {
+
+constexpr int TX = 32, TY = 8;
+
+struct RealDesc {
+    long long off; /* first cell of the realisation in every array */
+    int N;
+    double dx;     /* grid spacing */
+    double p[4];   /* physics parameters (lambda, c) or (q2, q3, q4, -) */
+};
+
+struct FastTile {
+    int r;
+    int x0, y0, z0, nz;
+};
+
+template <class R>
+struct AxionArgs {
+    const RealDesc *desc;
+    const FastTile *tiles;
+    const R *y0[2], *m0[2]; /* state in */
+    R *y1[2], *m1[2];       /* state out */
+    R *cy[2], *cm[2];       /* compensations (in place) */
+    R *K[2][2];             /* K_0, K_1 (two components each) */
+    double *time;           /* two slots; the step reads slot `slot` and the */
+    int slot;               /* last stage writes slot 1 - slot = t + h */
+    double h;
+};
+
+__device__ __forceinline__ int wrap(int a, int N) { return a < 0 ? a + N : (a >= N ? a - N : a); }
+
+template <class R>
+__device__ __forceinline__ void kahan_add(R &y, R d, R &c) {
+    const R v = d - c;
+    const R t = y + v;
+    c = (t - y) - v;
+    y = t;
+}
+
+/* RKN4 stage kernel for the axion family.  ORDER: Laplacian order (1: 7
+ * points, 2: 13 points).  STAGE 0 and 1 write K_STAGE; STAGE 2 writes the
+ * new state. */
+template <class R, int ORDER, int STAGE, bool KAHAN>
+__global__ void __launch_bounds__(TX *TY) axion_rkn4_kernel(const __grid_constant__ AxionArgs<R> a) {
+    constexpr int H = ORDER;             /* halo */
+    constexpr int RING = 2 * H + 1;
+    constexpr int W = TX + 2 * H, HH = TY + 2 * H;
+    __shared__ R ring[RING][2][HH][W];
+
+    const FastTile tl = a.tiles[blockIdx.x];
+    const RealDesc d = a.desc[tl.r];
+    const int N = d.N;
+    const long long off = d.off;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+    const int x = tl.x0 + tx, y = tl.y0 + ty;
+    const bool active = x < N && y < N;
+
+    /* RKN4 tableau (rkn.cpp:130-139): c = {0, 1/2, 1}; a21 = 1/8; a32 = 1/2;
+     * bbar = {1/6, 1/3, 0}; b = {1/6, 2/3, 1/6}. */
+    const double hh = a.h * a.h;
+    const R cm = (R)(STAGE == 0 ? 0. : (STAGE == 1 ? 0.5 * a.h : a.h));
+    const R ck = (R)(STAGE == 1 ? hh / 8. : (STAGE == 2 ? hh / 2. : 0.));
+    const double t0 = a.time[a.slot];
+    const double ts = t0 + a.h * (STAGE == 0 ? 0. : (STAGE == 1 ? 0.5 : 1.));
+    if (STAGE == 2 && blockIdx.x == 0 && tid == 0) a.time[1 - a.slot] = t0 + a.h;
+    const R friction = (R)(-2. / ts);
+    const R lam = (R)d.p[0];
+    const R cst = (R)d.p[1];
+    const R eta2 = (R)(ts * ts);
+    const R inv_dx2 = (R)(1. / (d.dx * d.dx));
+    const R* Kin = STAGE == 1 ? a.K[0][0] : (STAGE == 2 ? a.K[1][0] : nullptr);
+    const R* Kin2 = STAGE == 1 ? a.K[0][1] : (STAGE == 2 ? a.K[1][1] : nullptr);
+
+    auto load_plane = [&](int z, int slot) {
+        const int zw = wrap(z, N);
+        for (int p = tid; p < W * HH; p += TX * TY) {
+            const int px = p % W, py = p / W;
+            const int gx = wrap(tl.x0 - H + px, N), gy = wrap(tl.y0 - H + py, N);
+            const long long e = off + ((long long)zw * N + gy) * N + gx;
+            R v0 = a.y0[0][e], v1 = a.y0[1][e];
+            if (STAGE > 0) {
+                v0 += cm * a.m0[0][e] + ck * Kin[e];
+                v1 += cm * a.m0[1][e] + ck * Kin2[e];
+            }
+            ring[slot][0][py][px] = v0;
+            ring[slot][1][py][px] = v1;
+        }
+    };
+
+    const int zb = tl.z0 - H, ze = tl.z0 + tl.nz + H; /* planes [zb, ze) */
+    for (int z = zb; z < ze; ++z) {
+        load_plane(z, (z - zb) % RING);
+        __syncthreads();
+        const int zc = z - H;
+        if (zc >= tl.z0 && active) {
+            const int sc = (zc - zb) % RING;
+            R lap[2];
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                const R u0 = ring[sc][c][ty + H][tx + H];
+                if (ORDER == 1) {
+                    R s = ring[sc][c][ty + H][tx + H + 1] + ring[sc][c][ty + H][tx + H - 1];
+                    s += ring[sc][c][ty + H + 1][tx + H] + ring[sc][c][ty + H - 1][tx + H];
+                    s += ring[(sc + 1) % RING][c][ty + H][tx + H] +
+                         ring[(sc + RING - 1) % RING][c][ty + H][tx + H];
+                    lap[c] = (s - (R)6 * u0) * inv_dx2;
+                } else {
+                    R s1 = ring[sc][c][ty + H][tx + H + 1] + ring[sc][c][ty + H][tx + H - 1];
+                    s1 += ring[sc][c][ty + H + 1][tx + H] + ring[sc][c][ty + H - 1][tx + H];
+                    s1 += ring[(sc + 1) % RING][c][ty + H][tx + H] +
+                          ring[(sc + RING - 1) % RING][c][ty + H][tx + H];
+                    R s2 = ring[sc][c][ty + H][tx + H + 2] + ring[sc][c][ty + H][tx + H - 2];
+                    s2 += ring[sc][c][ty + H + 2][tx + H] + ring[sc][c][ty + H - 2][tx + H];
+                    s2 += ring[(sc + 2) % RING][c][ty + H][tx + H] +
+                          ring[(sc + RING - 2) % RING][c][ty + H][tx + H];
+                    lap[c] = ((R)16 * s1 - s2 - (R)90 * u0) * (inv_dx2 / (R)12);
+                }
+            }
+            const long long e = off + ((long long)zc * N + y) * N + x;
+            const R p0 = ring[sc][0][ty + H][tx + H], p1 = ring[sc][1][ty + H][tx + H];
+            const R q0 = a.m0[0][e], q1 = a.m0[1][e];
+            const R v = lam * (eta2 * (p0 * p0 + p1 * p1 - (R)1) + cst);
+            const R k0 = friction * q0 + lap[0] - p0 * v;
+            const R k1 = friction * q1 + lap[1] - p1 * v;
+            if (STAGE < 2) {
+                a.K[STAGE][0][e] = k0;
+                a.K[STAGE][1][e] = k1;
+            } else {
+                const R h = (R)a.h, h2 = (R)hh;
+                const R ka0 = a.K[0][0][e], ka1 = a.K[0][1][e];
+                const R kb0 = a.K[1][0][e], kb1 = a.K[1][1][e];
+                /* y1 = y0 + h y0' + h^2 (K0/6 + K1/3); y1' = y0' + h (K0/6 + 2K1/3 + K2/6) */
+                const R dy0 = h * q0 + h2 * (ka0 * (R)(1. / 6.) + kb0 * (R)(1. / 3.));
+                const R dy1 = h * q1 + h2 * (ka1 * (R)(1. / 6.) + kb1 * (R)(1. / 3.));
+                const R dm0 = h * ((ka0 + k0) * (R)(1. / 6.) + kb0 * (R)(2. / 3.));
+                const R dm1 = h * ((ka1 + k1) * (R)(1. / 6.) + kb1 * (R)(2. / 3.));
+                R y0v = a.y0[0][e], y1v = a.y0[1][e], m0v = q0, m1v = q1;
+                if (KAHAN) {
+                    R c0 = a.cy[0][e], c1 = a.cy[1][e], c2 = a.cm[0][e], c3 = a.cm[1][e];
+                    kahan_add(y0v, dy0, c0);
+                    kahan_add(y1v, dy1, c1);
+                    kahan_add(m0v, dm0, c2);
+                    kahan_add(m1v, dm1, c3);
+                    a.cy[0][e] = c0;
+                    a.cy[1][e] = c1;
+                    a.cm[0][e] = c2;
+                    a.cm[1][e] = c3;
+                } else {
+                    y0v += dy0;
+                    y1v += dy1;
+                    m0v += dm0;
+                    m1v += dm1;
+                }
+                a.y1[0][e] = y0v;
+                a.y1[1][e] = y1v;
+                a.m1[0][e] = m0v;
+                a.m1[1][e] = m1v;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <class R>
+struct FoptArgs {
+    const RealDesc *desc;
+    const FastTile *tiles;
+    const R *x[7];   /* positions read by the stencil (Phi, u_xx..u_yz) */
+    const R *v[7];   /* momenta in (S0: v0, S1: vh) */
+    R *xo[7];        /* S0: x1 */
+    R *vo[7];        /* S0: vh, S1: v1 */
+    R *cx[7], *cv[7];
+    double *time; /* two slots, as for AxionArgs; STAGE 1 writes slot 1 - slot */
+    int slot;
+    double dt;
+};
+
+/* Leapfrog kick-drift-kick stage kernel for Phi + GW tensor (7 position and
+ * 7 momentum components; 4th-order Laplacian and gradient, halo 2).
+ * STAGE 0: a = f(x0); vh = v0 + dt/2 a; x1 = x0 + dt vh.
+ * STAGE 1: a = f(x1); v1 = vh + dt/2 a.
+ * Potential: dPhi' = lap Phi + q2 Phi + q3 Phi^2 + q4 Phi^3 (p[0..2]). */
+template <class R, int STAGE, bool KAHAN>
+__global__ void __launch_bounds__(TX *TY) fopt_leapfrog_kernel(const __grid_constant__ FoptArgs<R> a) {
+    constexpr int H = 2, RING = 5, W = TX + 2 * H, HH = TY + 2 * H, NC = 7;
+    extern __shared__ unsigned char smem_raw[];
+    R(*ring)[NC][HH][W] = reinterpret_cast<R(*)[NC][HH][W]>(smem_raw);
+
+    const FastTile tl = a.tiles[blockIdx.x];
+    const RealDesc d = a.desc[tl.r];
+    const int N = d.N;
+    const long long off = d.off;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+    const int x = tl.x0 + tx, y = tl.y0 + ty;
+    const bool active = x < N && y < N;
+    const R q2 = (R)d.p[0], q3 = (R)d.p[1], q4 = (R)d.p[2];
+    const R inv12dx2 = (R)(1. / (12. * d.dx * d.dx));
+    const R inv12dx = (R)(1. / (12. * d.dx));
+    const R hdt = (R)(0.5 * a.dt), dt = (R)a.dt;
+    if (STAGE == 1 && blockIdx.x == 0 && tid == 0) a.time[1 - a.slot] = a.time[a.slot] + a.dt;
+
+    auto load_plane = [&](int z, int slot) {
+        const int zw = wrap(z, N);
+        for (int p = tid; p < W * HH; p += TX * TY) {
+            const int px = p % W, py = p / W;
+            const int gx = wrap(tl.x0 - H + px, N), gy = wrap(tl.y0 - H + py, N);
+            const long long e = off + ((long long)zw * N + gy) * N + gx;
+#pragma unroll
+            for (int c = 0; c < NC; ++c) ring[slot][c][py][px] = a.x[c][e];
+        }
+    };
+    const int zb = tl.z0 - H, ze = tl.z0 + tl.nz + H;
+    for (int z = zb; z < ze; ++z) {
+        load_plane(z, (z - zb) % RING);
+        __syncthreads();
+        const int zc = z - H;
+        if (zc >= tl.z0 && active) {
+            const int s0 = (zc - zb) % RING;
+            const int sp1 = (s0 + 1) % RING, sp2 = (s0 + 2) % RING;
+            const int sm1 = (s0 + RING - 1) % RING, sm2 = (s0 + RING - 2) % RING;
+            const int cx_ = tx + H, cy_ = ty + H;
+            R acc[NC];
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                const R u0 = ring[s0][c][cy_][cx_];
+                R s1 = ring[s0][c][cy_][cx_ + 1] + ring[s0][c][cy_][cx_ - 1];
+                s1 += ring[s0][c][cy_ + 1][cx_] + ring[s0][c][cy_ - 1][cx_];
+                s1 += ring[sp1][c][cy_][cx_] + ring[sm1][c][cy_][cx_];
+                R s2 = ring[s0][c][cy_][cx_ + 2] + ring[s0][c][cy_][cx_ - 2];
+                s2 += ring[s0][c][cy_ + 2][cx_] + ring[s0][c][cy_ - 2][cx_];
+                s2 += ring[sp2][c][cy_][cx_] + ring[sm2][c][cy_][cx_];
+                acc[c] = ((R)16 * s1 - s2 - (R)90 * u0) * inv12dx2;
+            }
+            /* 4th-order gradient of Phi */
+            R g[3];
+            g[0] = ((R)8 * (ring[s0][0][cy_][cx_ + 1] - ring[s0][0][cy_][cx_ - 1]) -
+                    (ring[s0][0][cy_][cx_ + 2] - ring[s0][0][cy_][cx_ - 2])) * inv12dx;
+            g[1] = ((R)8 * (ring[s0][0][cy_ + 1][cx_] - ring[s0][0][cy_ - 1][cx_]) -
+                    (ring[s0][0][cy_ + 2][cx_] - ring[s0][0][cy_ - 2][cx_])) * inv12dx;
+            g[2] = ((R)8 * (ring[sp1][0][cy_][cx_] - ring[sm1][0][cy_][cx_]) -
+                    (ring[sp2][0][cy_][cx_] - ring[sm2][0][cy_][cx_])) * inv12dx;
+            const R phi = ring[s0][0][cy_][cx_];
+            acc[0] += phi * (q2 + phi * (q3 + phi * q4));
+            acc[1] += g[0] * g[0];
+            acc[2] += g[1] * g[1];
+            acc[3] += g[2] * g[2];
+            acc[4] += g[0] * g[1];
+            acc[5] += g[0] * g[2];
+            acc[6] += g[1] * g[2];
+            const long long e = off + ((long long)zc * N + y) * N + x;
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                R vv = a.v[c][e];
+                if (KAHAN) {
+                    R cvv = a.cv[c][e];
+                    kahan_add(vv, hdt * acc[c], cvv);
+                    a.cv[c][e] = cvv;
+                } else {
+                    vv += hdt * acc[c];
+                }
+                a.vo[c][e] = vv;
+                if (STAGE == 0) {
+                    R xx = ring[s0][c][cy_][cx_];
+                    if (KAHAN) {
+                        R cxx = a.cx[c][e];
+                        kahan_add(xx, dt * vv, cxx);
+                        a.cx[c][e] = cxx;
+                    } else {
+                        xx += dt * vv;
+                    }
+                    a.xo[c][e] = xx;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+} // namespace fast
+} // namespace sh
+
+/* ======================================================================= */
+/* Diagnostics: FP64 energy per realisation and string (winding) counts.   */
+namespace sh {
+namespace fast {
+
+/* Energy density summed per block in FP64; one partial per block, reduced
+ * per realisation on the host in block order (deterministic).
+ * axion: 1/2 (Pi1^2 + Pi2^2) + 1/2 |grad Psi|^2 + lambda/4 eta^2 (|Psi|^2-1)^2
+ *        + lambda c/2 |Psi|^2
+ * FOPT : 1/2 dPhi^2 + 1/2 |grad Phi|^2 + V(Phi),
+ *        V = -(q2/2 Phi^2 + q3/3 Phi^3 + q4/4 Phi^4);
+ * gradients are 2nd-order central differences. */
+template <class R>
+__global__ void energy_kernel(const RealDesc *desc, const FastTile *tiles, const R *f0,
+                              const R *f1, const R *m0, const R *m1, const R *cf0, const R *cf1,
+                              const R *cm0, const R *cm1, int family, double eta,
+                              double *partial) {
+    const FastTile tl = tiles[blockIdx.x];
+    const RealDesc d = desc[tl.r];
+    const int N = d.N;
+    const double dx = d.dx;
+    const int x = tl.x0 + threadIdx.x, y = tl.y0 + threadIdx.y;
+    double acc = 0.;
+    /* the compensation holds minus the lost low part */
+    auto val = [&](const R *f, const R *c, long long e) {
+        return (double)f[e] - (c ? (double)c[e] : 0.);
+    };
+    if (x < N && y < N) {
+        for (int z = tl.z0; z < tl.z0 + tl.nz; ++z) {
+            const long long e = d.off + ((long long)z * N + y) * N + x;
+            auto at = [&](const R *f, const R *c, int dx_, int dy_, int dz_) {
+                return val(f, c, d.off + ((long long)wrap(z + dz_, N) * N + wrap(y + dy_, N)) * N +
+                                     wrap(x + dx_, N));
+            };
+            double gsum = 0.;
+            const int ncf = family == 3 ? 1 : 2;
+            for (int q = 0; q < ncf; ++q) {
+                const R *f = q == 0 ? f0 : f1;
+                const R *c = q == 0 ? cf0 : cf1;
+                const double gx = (at(f, c, 1, 0, 0) - at(f, c, -1, 0, 0)) / (2. * dx);
+                const double gy = (at(f, c, 0, 1, 0) - at(f, c, 0, -1, 0)) / (2. * dx);
+                const double gz = (at(f, c, 0, 0, 1) - at(f, c, 0, 0, -1)) / (2. * dx);
+                gsum += gx * gx + gy * gy + gz * gz;
+            }
+            if (family == 3) {
+                const double phi = val(f0, cf0, e), dp = val(m0, cm0, e);
+                const double V =
+                    -(d.p[0] / 2. * phi * phi + d.p[1] / 3. * phi * phi * phi +
+                      d.p[2] / 4. * phi * phi * phi * phi);
+                acc += 0.5 * dp * dp + 0.5 * gsum + V;
+            } else {
+                const double p0 = val(f0, cf0, e), p1 = val(f1, cf1, e);
+                const double q0 = val(m0, cm0, e), q1 = val(m1, cm1, e);
+                const double r2m1 = p0 * p0 + p1 * p1 - 1.;
+                acc += 0.5 * (q0 * q0 + q1 * q1) + 0.5 * gsum +
+                       d.p[0] / 4. * eta * eta * r2m1 * r2m1 +
+                       d.p[0] * d.p[1] / 2. * (p0 * p0 + p1 * p1);
+            }
+        }
+    }
+    acc *= dx * dx * dx;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    __shared__ double ws[TX * TY / 32];
+    if ((threadIdx.x & 31) == 0) ws[(threadIdx.y * TX + threadIdx.x) >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        double s = 0.;
+        for (int w = 0; w < TX * TY / 32; ++w) s += ws[w];
+        partial[blockIdx.x] = s;
+    }
+}
+
+/* Cells pierced by a string (AxionStrings TagCellForRefinement, the count of
+ * Cosmology::GetStringTags, projects/AxionStrings/cosmology.cpp:114-142). */
+__device__ __forceinline__ int edge_xing(double a1, double a2, double b1, double b2) {
+    if (__dmul_rn(a2, b2) >= 0) return 0;
+    return (__dmul_rn(a2, b1) - __dmul_rn(a1, b2)) > 0 ? 1 : -1;
+}
+
+template <class R>
+__global__ void string_count_kernel(const RealDesc *desc, const FastTile *tiles, const R *f0,
+                                    const R *f1, const R *c0, const R *c1,
+                                    unsigned long long *counts) {
+    const FastTile tl = tiles[blockIdx.x];
+    const RealDesc d = desc[tl.r];
+    const int N = d.N;
+    const int x = tl.x0 + threadIdx.x, y = tl.y0 + threadIdx.y;
+    unsigned long long n = 0;
+    if (x < N && y < N) {
+        for (int z = tl.z0; z < tl.z0 + tl.nz; ++z) {
+            auto v = [&](const R *f, int dx_, int dy_, int dz_) {
+                const long long e =
+                    d.off + ((long long)wrap(z + dz_, N) * N + wrap(y + dy_, N)) * N + wrap(x + dx_, N);
+                const R *c = f == f0 ? c0 : c1;
+                return (double)f[e] - (c ? (double)c[e] : 0.);
+            };
+            const int P[3][2][3] = {{{1, 0, 0}, {0, 1, 0}}, {{1, 0, 0}, {0, 0, 1}},
+                                    {{0, 1, 0}, {0, 0, 1}}};
+            bool hit = false;
+            for (int pl = 0; pl < 3 && !hit; ++pl) {
+                const int *p = P[pl][0], *q = P[pl][1];
+                const int cx[4] = {0, p[0], p[0] + q[0], q[0]};
+                const int cy[4] = {0, p[1], p[1] + q[1], q[1]};
+                const int cz[4] = {0, p[2], p[2] + q[2], q[2]};
+                int w = 0;
+                for (int e = 0; e < 4; ++e) {
+                    const int f = (e + 1) & 3;
+                    w += edge_xing(v(f0, cx[e], cy[e], cz[e]), v(f1, cx[e], cy[e], cz[e]),
+                                   v(f0, cx[f], cy[f], cz[f]), v(f1, cx[f], cy[f], cz[f]));
+                }
+                hit = w != 0;
+            }
+            n += hit;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) n += __shfl_down_sync(0xffffffffu, n, o);
+    if ((threadIdx.x & 31) == 0 && n) atomicAdd(&counts[tl.r], n);
+}
+
+/* Conversion between host FP64 and device storage (value + compensation). */
+template <class R>
+__global__ void store_kernel(const double *src, R *dst, R *comp, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double v = src[i];
+        const R r = (R)v;
+        dst[i] = r;
+        if (comp) comp[i] = (R)0;
+    }
+}
+template <class R>
+__global__ void load_kernel(const R *src, const R *comp, double *dst, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        /* the compensation holds minus the lost low part */
+        dst[i] = (double)src[i] - (comp ? (double)comp[i] : 0.);
+    }
+}
+
+/* Pack one GW component of realisation r into a zero-padded (pN)^3 FP64
+ * array for the spectrum (compensation included). */
+template <class R>
+__global__ void gw_pack_fast_kernel(const R *src, const R *comp, long long off, int N, int P,
+                                    double *dst) {
+    const long long n = (long long)N * N * N;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / ((long long)N * N));
+        dst[((long long)z * P + y) * P + x] =
+            (double)src[off + i] - (comp ? (double)comp[off + i] : 0.);
+    }
+}
+
+} // namespace fast
+} // namespace sh
+
+/* ======================================================================= */
+/* Host side: ensembles (sh_ensemble_* of include/sledgehamr_gb300.h).      */
+#include <functional>
+#include <memory>
+#include <stdexcept>
+
+#include "sh_gw.h"
+
+namespace {
+using namespace sh::fast;
+
+struct FastErr : std::runtime_error {
+    int code;
+    FastErr(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+inline void fck(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw FastErr(e == cudaErrorMemoryAllocation ? SH_ERR_NOMEM : SH_ERR_CUDA,
+                      std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+inline void freq(bool c, const std::string &m) {
+    if (!c) throw FastErr(SH_ERR_ARG, m);
+}
+int fgrid(long long n) {
+    return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 152LL * 32));
+}
+constexpr int kTuneCandidates[5] = {4, 8, 16, 32, 64};
+} // namespace
+
+struct sh_ensemble {
+    sh_ctx *ctx = nullptr;
+    int family = 0, precision = 0, nreal = 0, ncomp = 0;
+    size_t esize = 4;
+    std::vector<RealDesc> desc;
+    long long total = 0; /* cells of all realisations */
+    RealDesc *d_desc = nullptr;
+    std::vector<FastTile> tiles;
+    FastTile *d_tiles = nullptr;
+    int tile_nz = 16;
+    /* component arrays of `total` elements: state A (current) and B, the
+     * Kahan compensations C (FP32_KAHAN only) and stage scratch K */
+    std::vector<void *> A, B, C, K;
+    void *A0 = nullptr; /* A[0] at creation: parity of the A/B buffers */
+    double *d_time = nullptr; /* two slots */
+    int slot = 0;
+    double *d_partial = nullptr;
+    size_t partial_cap = 0;
+    unsigned long long *d_counts = nullptr;
+    sh::GwCache gw;
+    void *gw_scratch = nullptr;
+    size_t gw_scratch_cap = 0;
+    std::string err;
+    long long launches = 0;
+    /* one CUDA graph of a whole step per buffer parity, for step size graph_dt */
+    bool use_graph = false;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    double graph_dt[2] = {0., 0.};
+};
+
+namespace {
+
+cudaStream_t est(const sh_ensemble *E) { return (cudaStream_t)sh_ctx_stream(E->ctx); }
+
+void drop_graphs(sh_ensemble *E) {
+    for (int p = 0; p < 2; ++p)
+        if (E->graph[p]) {
+            cudaGraphExecDestroy(E->graph[p]);
+            E->graph[p] = nullptr;
+        }
+}
+
+void build_tiles(sh_ensemble *E, int nz) {
+    std::vector<FastTile> t;
+    for (int r = 0; r < E->nreal; ++r) {
+        const int N = E->desc[r].N;
+        const int tz = std::min(nz, N);
+        for (int z = 0; z < N; z += tz)
+            for (int y = 0; y < N; y += TY)
+                for (int x = 0; x < N; x += TX) t.push_back(FastTile{r, x, y, z, std::min(tz, N - z)});
+    }
+    FastTile *d = nullptr;
+    fck(cudaMalloc(&d, t.size() * sizeof(FastTile)), "tile table");
+    fck(cudaMemcpy(d, t.data(), t.size() * sizeof(FastTile), cudaMemcpyHostToDevice),
+        "tile table upload");
+    cudaFree(E->d_tiles);
+    E->d_tiles = d;
+    E->tiles.swap(t);
+    E->tile_nz = nz;
+    drop_graphs(E);
+}
+
+template <class R>
+R *arr(const std::vector<void *> &v, int i) {
+    return (R *)v[i];
+}
+
+int launches_per_step(const sh_ensemble *E) { return E->family == 3 ? 2 : 3; }
+
+/* One step from state `in` (time slot `slot`) to state `out`. */
+template <class R, bool KAHAN>
+void step_impl(sh_ensemble *E, const std::vector<void *> &in, const std::vector<void *> &out,
+               int slot, double dt, cudaStream_t s) {
+    const dim3 block(TX, TY);
+    const int nt = (int)E->tiles.size();
+    if (E->family != 3) {
+        AxionArgs<R> a;
+        std::memset(&a, 0, sizeof(a));
+        a.desc = E->d_desc;
+        a.tiles = E->d_tiles;
+        for (int c = 0; c < 2; ++c) {
+            a.y0[c] = arr<R>(in, c);
+            a.m0[c] = arr<R>(in, 2 + c);
+            a.y1[c] = arr<R>(out, c);
+            a.m1[c] = arr<R>(out, 2 + c);
+            a.cy[c] = KAHAN ? arr<R>(E->C, c) : nullptr;
+            a.cm[c] = KAHAN ? arr<R>(E->C, 2 + c) : nullptr;
+            a.K[0][c] = arr<R>(E->K, c);
+            a.K[1][c] = arr<R>(E->K, 2 + c);
+        }
+        a.time = E->d_time;
+        a.slot = slot;
+        a.h = dt;
+        if (E->family == SH_FAMILY_AXION_LAP1) {
+            axion_rkn4_kernel<R, 1, 0, KAHAN><<<nt, block, 0, s>>>(a);
+            axion_rkn4_kernel<R, 1, 1, KAHAN><<<nt, block, 0, s>>>(a);
+            axion_rkn4_kernel<R, 1, 2, KAHAN><<<nt, block, 0, s>>>(a);
+        } else {
+            axion_rkn4_kernel<R, 2, 0, KAHAN><<<nt, block, 0, s>>>(a);
+            axion_rkn4_kernel<R, 2, 1, KAHAN><<<nt, block, 0, s>>>(a);
+            axion_rkn4_kernel<R, 2, 2, KAHAN><<<nt, block, 0, s>>>(a);
+        }
+    } else {
+        FoptArgs<R> a;
+        std::memset(&a, 0, sizeof(a));
+        a.desc = E->d_desc;
+        a.tiles = E->d_tiles;
+        a.time = E->d_time;
+        a.slot = slot;
+        a.dt = dt;
+        const size_t shm = (size_t)5 * 7 * (TY + 4) * (TX + 4) * sizeof(R);
+        for (int c = 0; c < 7; ++c) {
+            a.x[c] = arr<R>(in, c);
+            a.v[c] = arr<R>(in, 7 + c);
+            a.xo[c] = arr<R>(out, c);
+            a.vo[c] = arr<R>(E->K, c); /* vh */
+            a.cx[c] = KAHAN ? arr<R>(E->C, c) : nullptr;
+            a.cv[c] = KAHAN ? arr<R>(E->C, 7 + c) : nullptr;
+        }
+        fopt_leapfrog_kernel<R, 0, KAHAN><<<nt, block, shm, s>>>(a);
+        for (int c = 0; c < 7; ++c) {
+            a.x[c] = arr<R>(out, c);
+            a.v[c] = arr<R>(E->K, c);
+            a.vo[c] = arr<R>(out, 7 + c);
+        }
+        fopt_leapfrog_kernel<R, 1, KAHAN><<<nt, block, shm, s>>>(a);
+    }
+}
+
+void step_dispatch(sh_ensemble *E, const std::vector<void *> &in,
+                   const std::vector<void *> &out, int slot, double dt, cudaStream_t s) {
+    if (E->precision == SH_PREC_FP64) step_impl<double, false>(E, in, out, slot, dt, s);
+    else if (E->precision == SH_PREC_FP32) step_impl<float, false>(E, in, out, slot, dt, s);
+    else step_impl<float, true>(E, in, out, slot, dt, s);
+    fck(cudaGetLastError(), "ensemble step launch");
+}
+
+/* One step A -> B, then swap, either by direct launches or by the graph of
+ * the current parity (captured on first use for this step size). */
+void step_once(sh_ensemble *E, double dt, cudaStream_t s) {
+    const int par = E->A[0] == E->A0 ? 0 : 1;
+    if (E->use_graph) {
+        if (E->graph[par] && E->graph_dt[par] != dt) {
+            cudaGraphExecDestroy(E->graph[par]);
+            E->graph[par] = nullptr;
+        }
+        if (!E->graph[par]) {
+            cudaStream_t cs = nullptr;
+            fck(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream");
+            cudaGraph_t g = nullptr;
+            cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                step_dispatch(E, E->A, E->B, E->slot, dt, cs);
+                e = cudaStreamEndCapture(cs, &g);
+            }
+            cudaStreamDestroy(cs);
+            fck(e, "step capture");
+            e = cudaGraphInstantiate(&E->graph[par], g, 0);
+            cudaGraphDestroy(g);
+            fck(e, "graph instantiate");
+            E->graph_dt[par] = dt;
+        }
+        fck(cudaGraphLaunch(E->graph[par], s), "graph launch");
+    } else {
+        step_dispatch(E, E->A, E->B, E->slot, dt, s);
+    }
+    E->launches += launches_per_step(E);
+    std::swap(E->A, E->B);
+    E->slot = 1 - E->slot;
+}
+
+template <class F>
+int fguard(sh_ensemble *E, F &&f) {
+    try {
+        f();
+        return SH_OK;
+    } catch (const FastErr &e) {
+        if (E) E->err = e.what();
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        if (E) E->err = "host allocation failed";
+        return SH_ERR_NOMEM;
+    } catch (const std::exception &e) {
+        if (E) E->err = e.what();
+        return SH_ERR_ARG;
+    }
+}
+
+void set_smem_limits() {
+    const int shf = 5 * 7 * (TY + 4) * (TX + 4) * (int)sizeof(float);
+    const int shd = 5 * 7 * (TY + 4) * (TX + 4) * (int)sizeof(double);
+    const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    fck(cudaFuncSetAttribute(fopt_leapfrog_kernel<float, 0, true>, at, shf), "smem limit");
+    fck(cudaFuncSetAttribute(fopt_leapfrog_kernel<float, 1, true>, at, shf), "smem limit");
+    fck(cudaFuncSetAttribute(fopt_leapfrog_kernel<float, 0, false>, at, shf), "smem limit");
+    fck(cudaFuncSetAttribute(fopt_leapfrog_kernel<float, 1, false>, at, shf), "smem limit");
+    fck(cudaFuncSetAttribute(fopt_leapfrog_kernel<double, 0, false>, at, shd), "smem limit");
+    fck(cudaFuncSetAttribute(fopt_leapfrog_kernel<double, 1, false>, at, shd), "smem limit");
+}
+
+/* Host component c (level order: fields, scalar momenta, u_ij, du_ij) to the
+ * internal array (positions, then momenta). */
+int internal_comp(const sh_ensemble *E, int c) {
+    if (E->family != SH_FAMILY_FOPT_GW) return c;
+    return c == 0 ? 0 : (c == 1 ? 7 : (c < 8 ? c - 1 : c));
+}
+
+long long cells_of(const sh_ensemble *E, int r) {
+    return (long long)E->desc[r].N * E->desc[r].N * E->desc[r].N;
+}
+
+double read_time(sh_ensemble *E) {
+    double t = 0.;
+    fck(cudaMemcpyAsync(&t, E->d_time + E->slot, sizeof(double), cudaMemcpyDeviceToHost, est(E)),
+        "time download");
+    fck(cudaStreamSynchronize(est(E)), "time");
+    return t;
+}
+
+} // namespace
+
+extern "C" {
+
+int sh_ensemble_create(sh_ctx *ctx, int family, int precision, int nreal, const int *N,
+                       const double *dx, const double *params, sh_ensemble **out) {
+    if (!ctx || !out || !N || !dx || nreal <= 0) return SH_ERR_ARG;
+    *out = nullptr;
+    if (family != SH_FAMILY_AXION_LAP1 && family != SH_FAMILY_AXION_LAP2 &&
+        family != SH_FAMILY_FOPT_GW)
+        return SH_ERR_ARG;
+    if (precision != SH_PREC_FP64 && precision != SH_PREC_FP32_KAHAN && precision != SH_PREC_FP32)
+        return SH_ERR_ARG;
+    sh_ensemble *E = new (std::nothrow) sh_ensemble();
+    if (!E) return SH_ERR_NOMEM;
+    E->ctx = ctx;
+    int rc = fguard(E, [&] {
+        set_smem_limits();
+        E->family = family;
+        E->precision = precision;
+        E->nreal = nreal;
+        E->ncomp = family == SH_FAMILY_FOPT_GW ? 14 : 4;
+        E->esize = precision == SH_PREC_FP64 ? 8 : 4;
+        long long off = 0;
+        for (int r = 0; r < nreal; ++r) {
+            freq(N[r] >= 8 && N[r] <= 4096, "realisations need 8 <= N <= 4096");
+            freq(dx[r] > 0, "dx must be positive");
+            RealDesc d;
+            d.off = off;
+            d.N = N[r];
+            d.dx = dx[r];
+            for (int q = 0; q < 4; ++q) d.p[q] = params ? params[4 * r + q] : 0.;
+            off += (long long)N[r] * N[r] * N[r];
+            E->desc.push_back(d);
+        }
+        E->total = off;
+        fck(cudaMalloc(&E->d_desc, nreal * sizeof(RealDesc)), "descriptor table");
+        fck(cudaMemcpy(E->d_desc, E->desc.data(), nreal * sizeof(RealDesc),
+                       cudaMemcpyHostToDevice),
+            "descriptor upload");
+        const size_t bytes = (size_t)E->total * E->esize;
+        auto alloc = [&](std::vector<void *> &v, int n) {
+            for (int q = 0; q < n; ++q) {
+                void *p = nullptr;
+                fck(cudaMalloc(&p, bytes), "ensemble allocation");
+                v.push_back(p);
+                fck(cudaMemset(p, 0, bytes), "ensemble clear");
+            }
+        };
+        alloc(E->A, E->ncomp);
+        alloc(E->B, E->ncomp);
+        if (precision == SH_PREC_FP32_KAHAN) alloc(E->C, E->ncomp);
+        alloc(E->K, family == SH_FAMILY_FOPT_GW ? 7 : 4);
+        E->A0 = E->A[0];
+        fck(cudaMalloc(&E->d_time, 2 * sizeof(double)), "time");
+        fck(cudaMemset(E->d_time, 0, 2 * sizeof(double)), "time clear");
+        fck(cudaMalloc(&E->d_counts, nreal * sizeof(unsigned long long)), "counts");
+        build_tiles(E, 16);
+    });
+    if (rc != SH_OK) {
+        std::string m = E->err;
+        sh_ensemble_destroy(E);
+        return rc;
+    }
+    *out = E;
+    return SH_OK;
+}
+
+int sh_ensemble_destroy(sh_ensemble *E) {
+    if (!E) return SH_ERR_ARG;
+    cudaStreamSynchronize(est(E));
+    drop_graphs(E);
+    for (auto *v : {&E->A, &E->B, &E->C, &E->K})
+        for (void *p : *v) cudaFree(p);
+    cudaFree(E->d_desc);
+    cudaFree(E->d_tiles);
+    cudaFree(E->d_time);
+    cudaFree(E->d_partial);
+    cudaFree(E->d_counts);
+    cudaFree(E->gw_scratch);
+    E->gw.release();
+    delete E;
+    return SH_OK;
+}
+
+const char *sh_ensemble_last_error(const sh_ensemble *E) { return E ? E->err.c_str() : ""; }
+
+int sh_ensemble_info(const sh_ensemble *E, int *family, int *precision, int *nreal, int *ncomp,
+                     long long *cells, long long *device_bytes, int *tile_nz) {
+    if (!E) return SH_ERR_ARG;
+    if (family) *family = E->family;
+    if (precision) *precision = E->precision;
+    if (nreal) *nreal = E->nreal;
+    if (ncomp) *ncomp = E->ncomp;
+    if (cells) *cells = E->total;
+    if (device_bytes)
+        *device_bytes =
+            (long long)(E->A.size() + E->B.size() + E->C.size() + E->K.size()) * E->total *
+            (long long)E->esize;
+    if (tile_nz) *tile_nz = E->tile_nz;
+    return SH_OK;
+}
+
+long long sh_ensemble_kernel_launches(const sh_ensemble *E) { return E ? E->launches : 0; }
+
+int sh_ensemble_set_time(sh_ensemble *E, double t) {
+    if (!E) return SH_ERR_ARG;
+    return fguard(E, [&] {
+        const double tt[2] = {t, t};
+        fck(cudaMemcpyAsync(E->d_time, tt, sizeof(tt), cudaMemcpyHostToDevice, est(E)),
+            "time upload");
+        fck(cudaStreamSynchronize(est(E)), "time");
+    });
+}
+
+int sh_ensemble_time(sh_ensemble *E, double *t) {
+    if (!E || !t) return SH_ERR_ARG;
+    return fguard(E, [&] { *t = read_time(E); });
+}
+
+int sh_ensemble_write(sh_ensemble *E, int r, const double *host) {
+    if (!E || !host || r < 0 || r >= E->nreal) return SH_ERR_ARG;
+    return fguard(E, [&] {
+        const long long n = cells_of(E, r), o = E->desc[r].off;
+        cudaStream_t s = est(E);
+        double *d = nullptr;
+        fck(cudaMalloc(&d, n * sizeof(double)), "staging");
+        std::unique_ptr<double, decltype(&cudaFree)> guard(d, &cudaFree);
+        for (int hc = 0; hc < E->ncomp; ++hc) {
+            const int c = internal_comp(E, hc);
+            fck(cudaMemcpyAsync(d, host + (size_t)hc * n, n * sizeof(double),
+                                cudaMemcpyHostToDevice, s),
+                "upload");
+            if (E->esize == 8)
+                store_kernel<double><<<fgrid(n), 256, 0, s>>>(d, (double *)E->A[c] + o, nullptr, n);
+            else
+                store_kernel<float><<<fgrid(n), 256, 0, s>>>(
+                    d, (float *)E->A[c] + o, E->C.empty() ? nullptr : (float *)E->C[c] + o, n);
+            E->launches++;
+        }
+        fck(cudaStreamSynchronize(s), "write");
+    });
+}
+
+int sh_ensemble_read(sh_ensemble *E, int r, double *host) {
+    if (!E || !host || r < 0 || r >= E->nreal) return SH_ERR_ARG;
+    return fguard(E, [&] {
+        const long long n = cells_of(E, r), o = E->desc[r].off;
+        cudaStream_t s = est(E);
+        double *d = nullptr;
+        fck(cudaMalloc(&d, n * sizeof(double)), "staging");
+        std::unique_ptr<double, decltype(&cudaFree)> guard(d, &cudaFree);
+        for (int hc = 0; hc < E->ncomp; ++hc) {
+            const int c = internal_comp(E, hc);
+            if (E->esize == 8)
+                load_kernel<double><<<fgrid(n), 256, 0, s>>>((double *)E->A[c] + o, nullptr, d, n);
+            else
+                load_kernel<float><<<fgrid(n), 256, 0, s>>>(
+                    (float *)E->A[c] + o, E->C.empty() ? nullptr : (float *)E->C[c] + o, d, n);
+            E->launches++;
+            fck(cudaMemcpyAsync(host + (size_t)hc * n, d, n * sizeof(double),
+                                cudaMemcpyDeviceToHost, s),
+                "download");
+        }
+        fck(cudaStreamSynchronize(s), "read");
+    });
+}
+
+int sh_ensemble_set_graph(sh_ensemble *E, int on) {
+    if (!E) return SH_ERR_ARG;
+    E->use_graph = on != 0;
+    if (!E->use_graph) drop_graphs(E);
+    return SH_OK;
+}
+
+int sh_ensemble_step(sh_ensemble *E, double dt, int nsteps) {
+    if (!E || nsteps < 0 || !(dt > 0)) return SH_ERR_ARG;
+    return fguard(E, [&] {
+        cudaStream_t s = est(E);
+        for (int q = 0; q < nsteps; ++q) step_once(E, dt, s);
+    });
+}
+
+int sh_ensemble_tune(sh_ensemble *E, int tile_nz, double dt, int *chosen) {
+    if (!E || tile_nz < 0 || !(dt > 0)) return SH_ERR_ARG;
+    return fguard(E, [&] {
+        if (tile_nz > 0) {
+            build_tiles(E, tile_nz);
+        } else {
+            cudaStream_t s = est(E);
+            /* the trial steps write B, K, the compensations and the other
+             * time slot: keep a copy of the compensations and the time */
+            const size_t bytes = (size_t)E->total * E->esize;
+            std::vector<void *> saved;
+            auto release = [&] {
+                for (void *p : saved) cudaFree(p);
+            };
+            try {
+                for (void *c : E->C) {
+                    void *p = nullptr;
+                    fck(cudaMalloc(&p, bytes), "tune backup");
+                    saved.push_back(p);
+                    fck(cudaMemcpyAsync(p, c, bytes, cudaMemcpyDeviceToDevice, s), "tune backup");
+                }
+                double tsave[2];
+                fck(cudaMemcpyAsync(tsave, E->d_time, sizeof(tsave), cudaMemcpyDeviceToHost, s),
+                    "time");
+                cudaEvent_t ev[2];
+                fck(cudaEventCreate(&ev[0]), "event");
+                fck(cudaEventCreate(&ev[1]), "event");
+                float best = 1e30f;
+                int bestnz = E->tile_nz;
+                for (int nz : kTuneCandidates) {
+                    build_tiles(E, nz);
+                    step_dispatch(E, E->A, E->B, E->slot, dt, s); /* warm-up */
+                    fck(cudaEventRecord(ev[0], s), "record");
+                    for (int rep = 0; rep < 3; ++rep) step_dispatch(E, E->A, E->B, E->slot, dt, s);
+                    fck(cudaEventRecord(ev[1], s), "record");
+                    fck(cudaEventSynchronize(ev[1]), "tune");
+                    E->launches += 4 * launches_per_step(E);
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, ev[0], ev[1]);
+                    if (ms < best) {
+                        best = ms;
+                        bestnz = nz;
+                    }
+                }
+                cudaEventDestroy(ev[0]);
+                cudaEventDestroy(ev[1]);
+                build_tiles(E, bestnz);
+                for (size_t q = 0; q < saved.size(); ++q)
+                    fck(cudaMemcpyAsync(E->C[q], saved[q], bytes, cudaMemcpyDeviceToDevice, s),
+                        "tune restore");
+                fck(cudaMemcpyAsync(E->d_time, tsave, sizeof(tsave), cudaMemcpyHostToDevice, s),
+                    "time");
+                fck(cudaStreamSynchronize(s), "tune");
+            } catch (...) {
+                cudaStreamSynchronize(s);
+                release();
+                throw;
+            }
+            release();
+        }
+        if (chosen) *chosen = E->tile_nz;
+    });
+}
+
+int sh_ensemble_energy(sh_ensemble *E, double *energy) {
+    if (!E || !energy) return SH_ERR_ARG;
+    return fguard(E, [&] {
+        cudaStream_t s = est(E);
+        const double eta = read_time(E);
+        const int nt = (int)E->tiles.size();
+        if (E->partial_cap < (size_t)nt) {
+            cudaFree(E->d_partial);
+            E->d_partial = nullptr;
+            E->partial_cap = 0;
+            fck(cudaMalloc(&E->d_partial, nt * sizeof(double)), "partials");
+            E->partial_cap = nt;
+        }
+        const dim3 block(TX, TY);
+        const bool fopt = E->family == SH_FAMILY_FOPT_GW;
+        const int i0 = 0, i1 = fopt ? 0 : 1, i2 = fopt ? 7 : 2, i3 = fopt ? 7 : 3;
+        auto C = [&](int c) { return E->C.empty() ? nullptr : (const float *)E->C[c]; };
+        if (E->esize == 8)
+            energy_kernel<double><<<nt, block, 0, s>>>(
+                E->d_desc, E->d_tiles, (double *)E->A[i0], (double *)E->A[i1],
+                (double *)E->A[i2], (double *)E->A[i3], nullptr, nullptr, nullptr, nullptr,
+                E->family, eta, E->d_partial);
+        else
+            energy_kernel<float><<<nt, block, 0, s>>>(
+                E->d_desc, E->d_tiles, (float *)E->A[i0], (float *)E->A[i1], (float *)E->A[i2],
+                (float *)E->A[i3], C(i0), C(i1), C(i2), C(i3), E->family, eta, E->d_partial);
+        E->launches++;
+        fck(cudaGetLastError(), "energy launch");
+        std::vector<double> part(nt);
+        fck(cudaMemcpyAsync(part.data(), E->d_partial, nt * sizeof(double),
+                            cudaMemcpyDeviceToHost, s),
+            "partials download");
+        fck(cudaStreamSynchronize(s), "energy");
+        for (int r = 0; r < E->nreal; ++r) energy[r] = 0.;
+        for (int q = 0; q < nt; ++q) energy[E->tiles[q].r] += part[q];
+    });
+}
+
+int sh_ensemble_string_count(sh_ensemble *E, long long *counts) {
+    if (!E || !counts || E->family == SH_FAMILY_FOPT_GW) return SH_ERR_ARG;
+    return fguard(E, [&] {
+        cudaStream_t s = est(E);
+        const int nt = (int)E->tiles.size();
+        fck(cudaMemsetAsync(E->d_counts, 0, E->nreal * sizeof(unsigned long long), s), "clear");
+        const dim3 block(TX, TY);
+        auto C = [&](int c) { return E->C.empty() ? nullptr : (const float *)E->C[c]; };
+        if (E->esize == 8)
+            string_count_kernel<double><<<nt, block, 0, s>>>(E->d_desc, E->d_tiles,
+                                                             (double *)E->A[0], (double *)E->A[1],
+                                                             nullptr, nullptr, E->d_counts);
+        else
+            string_count_kernel<float><<<nt, block, 0, s>>>(E->d_desc, E->d_tiles,
+                                                            (float *)E->A[0], (float *)E->A[1],
+                                                            C(0), C(1), E->d_counts);
+        E->launches++;
+        fck(cudaGetLastError(), "string count launch");
+        std::vector<unsigned long long> c(E->nreal);
+        fck(cudaMemcpyAsync(c.data(), E->d_counts, E->nreal * sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, s),
+            "counts download");
+        fck(cudaStreamSynchronize(s), "string count");
+        for (int r = 0; r < E->nreal; ++r) counts[r] = (long long)c[r];
+    });
+}
+
+int sh_ensemble_gw_spectrum(sh_ensemble *E, int r, int zero_padding, int projection_type,
+                            int unbinned, double *bins_out, long long *ks_out, int max_bins,
+                            int *nbins) {
+    if (!E || E->family != SH_FAMILY_FOPT_GW || r < 0 || r >= E->nreal || !bins_out || !nbins)
+        return SH_ERR_ARG;
+    return fguard(E, [&] {
+        freq(zero_padding >= 1, "zero_padding must be >= 1");
+        freq(projection_type >= 1 && projection_type <= 3, "projection_type must be 1..3");
+        cudaStream_t s = est(E);
+        const int N = E->desc[r].N;
+        const int P = N * zero_padding;
+        freq(P % 2 == 0, "spectrum grid size must be even");
+        const size_t sbytes = (sh::gw_scratch_bytes(N, zero_padding) + 255) & ~size_t(255);
+        const size_t maxbins = (size_t)3 * (P / 2 + 1) * (P / 2 + 1) + 16;
+        const size_t need = sbytes + maxbins * sizeof(double);
+        if (need > E->gw_scratch_cap) {
+            cudaFree(E->gw_scratch);
+            E->gw_scratch = nullptr;
+            E->gw_scratch_cap = 0;
+            fck(cudaMalloc(&E->gw_scratch, need), "gw scratch");
+            E->gw_scratch_cap = need;
+        }
+        double *scratch = (double *)E->gw_scratch;
+        double *bins_dev = (double *)((char *)E->gw_scratch + sbytes);
+        /* du_xx, du_xy, du_xz, du_yy, du_yz, du_zz among the momenta
+         * (dPhi, du_xx, du_yy, du_zz, du_xy, du_xz, du_yz) */
+        const int sel[6] = {8, 11, 12, 9, 13, 10};
+        const long long n = cells_of(E, r), o = E->desc[r].off;
+        int nb = 0;
+        std::string err;
+        cudaError_t e = sh::gw_spectrum_packed(
+            E->gw, s, P, projection_type, unbinned, scratch, bins_dev, &nb, &E->launches, err,
+            [&](int q, double *real) {
+                const int c = sel[q];
+                if (E->esize == 8)
+                    gw_pack_fast_kernel<double><<<fgrid(n), 256, 0, s>>>((double *)E->A[c],
+                                                                         nullptr, o, N, P, real);
+                else
+                    gw_pack_fast_kernel<float><<<fgrid(n), 256, 0, s>>>(
+                        (float *)E->A[c], E->C.empty() ? nullptr : (float *)E->C[c], o, N, P,
+                        real);
+            });
+        if (!err.empty()) throw FastErr(SH_ERR_CUDA, err);
+        fck(e, "gw spectrum");
+        *nbins = nb;
+        freq(nb <= max_bins, "bins_out too small");
+        fck(cudaMemcpyAsync(bins_out, bins_dev, nb * sizeof(double), cudaMemcpyDeviceToHost, s),
+            "bins download");
+        fck(cudaStreamSynchronize(s), "gw spectrum");
+        if (ks_out) std::copy(E->gw.ks.begin(), E->gw.ks.end(), ks_out);
+    });
+}
+
+} /* extern "C" */

@@ -30,6 +30,8 @@
 #include <string>
 #include <vector>
 
+#include <functional>
+
 #include "sh_gw.h"
 #include "sledgehamr_gb300.h"
 
@@ -249,13 +251,10 @@ void GwCache::release() {
     P = 0;
 }
 
-cudaError_t gw_spectrum_device(GwCache &cache, cudaStream_t stream, const BoxDev *boxes,
-                               const long long *vbase, int nbox, long long nvalid, int ncomp,
-                               const double *buf, const int comps[6], int N, const int dlo[3],
-                               int zero_padding, int projection_type, int unbinned,
-                               double *scratch, double *bins_dev, int *nbins, long long *launches,
-                               std::string &err) {
-    const int P = N * zero_padding;
+cudaError_t gw_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, int projection_type,
+                               int unbinned, double *scratch, double *bins_dev, int *nbins,
+                               long long *launches, std::string &err,
+                               const std::function<void(int, double *)> &pack) {
     cache.prepare(P, unbinned, projection_type);
     const int H = P / 2 + 1;
     const long long nreal = (long long)P * P * P;
@@ -277,10 +276,7 @@ cudaError_t gw_spectrum_device(GwCache &cache, cudaStream_t stream, const BoxDev
     double *vals = (double *)(cplx + 6 * ncplx);
     for (int q = 0; q < 6; ++q) {
         cudaMemsetAsync(real, 0, nreal * sizeof(double), stream);
-        int g = (int)std::min<long long>((nvalid + 255) / 256, 152LL * 32);
-        gw_pack_kernel<<<std::max(g, 1), 256, 0, stream>>>(boxes, vbase, nbox, nvalid, ncomp,
-                                                            comps[q], buf, real, P, dlo[0],
-                                                            dlo[1], dlo[2]);
+        pack(q, real);
         (*launches)++;
         if (cufftExecD2Z(cache.plan, real, (cufftDoubleComplex *)(cplx + q * ncplx)) !=
             CUFFT_SUCCESS) {
@@ -300,6 +296,23 @@ cudaError_t gw_spectrum_device(GwCache &cache, cudaStream_t stream, const BoxDev
     (*launches)++;
     *nbins = nb;
     return cudaGetLastError();
+}
+
+cudaError_t gw_spectrum_device(GwCache &cache, cudaStream_t stream, const BoxDev *boxes,
+                               const long long *vbase, int nbox, long long nvalid, int ncomp,
+                               const double *buf, const int comps[6], int N, const int dlo[3],
+                               int zero_padding, int projection_type, int unbinned,
+                               double *scratch, double *bins_dev, int *nbins, long long *launches,
+                               std::string &err) {
+    const int P = N * zero_padding;
+    return gw_spectrum_packed(
+        cache, stream, P, projection_type, unbinned, scratch, bins_dev, nbins, launches, err,
+        [&](int q, double *real) {
+            int g = (int)std::min<long long>((nvalid + 255) / 256, 152LL * 32);
+            gw_pack_kernel<<<std::max(g, 1), 256, 0, stream>>>(boxes, vbase, nbox, nvalid, ncomp,
+                                                                comps[q], buf, real, P, dlo[0],
+                                                                dlo[1], dlo[2]);
+        });
 }
 
 size_t gw_scratch_bytes(int N, int zero_padding) {

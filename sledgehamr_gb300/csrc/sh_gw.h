@@ -4,6 +4,7 @@
 
 #include <cufft.h>
 
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -29,6 +30,13 @@ struct GwCache {
 std::vector<long long> unique_k2_host(int dim);
 std::vector<double> index_to_k_host(int N, int type);
 size_t gw_scratch_bytes(int N, int zero_padding);
+/* FFT, TT projection and binning of six P^3 real arrays that `pack(q, real)`
+ * writes (enqueued on `stream`) into the zeroed `real` for q = 0..5 in the
+ * order du_xx, du_xy, du_xz, du_yy, du_yz, du_zz. */
+cudaError_t gw_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, int projection_type,
+                               int unbinned, double *scratch, double *bins_dev, int *nbins,
+                               long long *launches, std::string &err,
+                               const std::function<void(int, double *)> &pack);
 cudaError_t gw_spectrum_device(GwCache &cache, cudaStream_t stream, const BoxDev *boxes,
                                const long long *vbase, int nbox, long long nvalid, int ncomp,
                                const double *buf, const int comps[6], int N, const int dlo[3],
