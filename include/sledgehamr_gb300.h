@@ -110,8 +110,10 @@ SH_API int sh_ctx_synchronize(sh_ctx *ctx);
 SH_API long long sh_ctx_kernel_launches(const sh_ctx *ctx);
 /* Per-kernel timing with CUDA events recorded on the context stream around
  * every launch while enabled (the categories of sledgehamr's
- * PerformanceMonitor: "rhs" (stage kernels), "fill_patch", "average_down",
- * "tagging", "gw_spectrum", "data_move").  sh_ctx_profile(ctx, 1) clears
+ * PerformanceMonitor: "rhs" (stage kernels), "fill_patch" (same-level
+ * ghost copies and level-to-level copies), "coarse_fine" (ghost cells
+ * interpolated from the coarse level), "average_down", "tagging",
+ * "gw_spectrum", "data_move").  sh_ctx_profile(ctx, 1) clears
  * and starts, (ctx, 0) stops; sh_ctx_profile_read synchronises the stream
  * and returns the summed device time and the launch count of a category. */
 SH_API int sh_ctx_profile(sh_ctx *ctx, int enable);
@@ -196,6 +198,21 @@ SH_API int sh_level_advance(sh_ctx *ctx, sh_level *level, int integrator, const 
 SH_API int sh_level_rhs(sh_ctx *ctx, sh_level *level, int which, double time, int lev, double dt,
                  double dx, const double *params, int nparams, const double *gw_params,
                  int ngw, int ko_order, const double *ko_strength, double *host_rhs);
+
+/* FirstOrderPhaseTransition bubble injection (InjectBubbles ->
+ * AddBubbleValues, projects/FirstOrderPhaseTransition/
+ * FirstOrderPhaseTransition.cpp:308-328, 459-483; AddBubble,
+ * kernels_misc.h:27-52): every valid cell (i, j, k) at position
+ * (i dx, j dx, k dx) of the periodic cubic domain adds, for each of the nb
+ * bubbles (centres xyz[3 b + d]) in order, the profile at its periodic
+ * distance D, linearly interpolated in bins of width 1/inv_dx:
+ * profile[ind] (1 - f) + profile[ind + 1] f with D inv_dx = ind + f, to
+ * component comp_phi (profile row 0, nbins values) and comp_dphi (row 1);
+ * cells with D >= Lcut are unchanged.  nbins >= floor(Lcut inv_dx) + 2. */
+SH_API int sh_level_add_bubbles(sh_ctx *ctx, sh_level *L, int which, int comp_phi,
+                                int comp_dphi, int nb, const double *xyz,
+                                const double *profile, int nbins, double inv_dx, double Lcut,
+                                double dx);
 
 /* ---- level synchronisation ------------------------------------------------- */
 /* crse(which_c) = 2x2x2 average of fine(which_f) on every coarse cell
@@ -291,7 +308,15 @@ typedef struct sh_amr_config {
     int nparams;
     double gw_params[16];        /* SetParamsGravitationalWaveRhs */
     int ngw;
+    int clustering;              /* SH_CLUSTER_BR (default) or SH_CLUSTER_WINDOWS */
+    double grid_eff;             /* amr.grid_eff of the clustering (default 0.7) */
 } sh_amr_config;
+/* New-grid generation from the buffered tags (at blocking-factor
+ * resolution): Berger-Rigoutsos clustering to efficiency grid_eff, then
+ * chopping to max_grid_size, as AMReX's MakeNewGrids does; or tagged blocks
+ * merged inside aligned max_grid_size windows (every box fully tagged). */
+#define SH_CLUSTER_BR 0
+#define SH_CLUSTER_WINDOWS 1
 
 SH_API int sh_amr_config_defaults(sh_amr_config *cfg);
 /* Hierarchy with level 0 = level0 (canonical layout, N0^3 cells, boxes of
@@ -302,6 +327,15 @@ SH_API int sh_amr_destroy(sh_ctx *ctx, sh_amr *amr);
 /* n coarse steps (Sledgehamr::Evolve loop bodies). */
 SH_API int sh_amr_step(sh_ctx *ctx, sh_amr *amr, int n);
 SH_API int sh_amr_info(const sh_amr *amr, int *finest, long long *cell_updates, int *nregrids);
+/* Host wall-clock seconds and call counts of the time stepper's phases
+ * (q = 0, 1, ... until SH_ERR_ARG): advance, synchronize, shadow,
+ * regrid.tag, regrid.new_grids, regrid.create, regrid.fill, regrid.destroy,
+ * regrid.refresh.  With timer sync on, the device is waited for around every
+ * timed phase (slower; for profiling).  The reference's PerformanceMonitor
+ * (source/performance_monitor.h) keeps the same kind of per-phase timers. */
+SH_API int sh_amr_set_timer_sync(sh_amr *a, int on);
+SH_API int sh_amr_timer(const sh_amr *a, int q, const char **name, double *seconds,
+                        long long *calls);
 /* Level lev of the hierarchy (owned by it; valid until the next step). */
 SH_API int sh_amr_level(const sh_amr *amr, int lev, sh_level **level);
 /* Regrid record q (with record_regrids): the tagged level and time, its
@@ -377,6 +411,11 @@ SH_API int sh_ensemble_tune(sh_ensemble *e, int tile_nz, double dt, int *chosen)
  * realisation r (FOPT_GW; arguments as sh_gw_spectrum). */
 SH_API int sh_ensemble_energy(sh_ensemble *e, double *energy);
 SH_API int sh_ensemble_string_count(sh_ensemble *e, long long *counts);
+/* Bubble injection into realisation r of an FOPT_GW ensemble, as
+ * sh_level_add_bubbles (realisation side L = N dx). */
+SH_API int sh_ensemble_add_bubbles(sh_ensemble *e, int r, int nb, const double *xyz,
+                                   const double *profile, int nbins, double inv_dx,
+                                   double Lcut);
 SH_API int sh_ensemble_gw_spectrum(sh_ensemble *e, int r, int zero_padding, int projection_type,
                                    int unbinned, double *bins_out, long long *ks_out,
                                    int max_bins, int *nbins);

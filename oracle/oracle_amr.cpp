@@ -230,6 +230,7 @@ struct CpuBackend {
         fill_two_level(m, m.t, coarse ? &(*coarse)->od : nullptr,
                        coarse ? &(*coarse)->nw : nullptr);
     }
+    void sync() {}
 };
 
 struct AmrBase {
@@ -266,6 +267,8 @@ struct Amr : AmrBase {
         d.string_width_threshold = cfg.string_width_threshold;
         d.string_lambda = cfg.string_lambda;
         d.te_crit.assign(cfg.te_crit, cfg.te_crit + ncomp);
+        d.clustering = cfg.clustering;
+        d.grid_eff = cfg.grid_eff;
         drv.reset(new shamr::Driver<CpuBackend<P>>(backend, d));
         drv->record_regrids = cfg.record_regrids != 0;
         const int N = cfg.N0;
@@ -334,6 +337,23 @@ int orc_amr_info(void *h, int *finest, long long *cell_updates, int *nregrids) {
     if (cell_updates) *cell_updates = a->cell_updates();
     if (nregrids) *nregrids = a->nregrids();
     return 0;
+}
+
+/* The new-grid step alone (shamr::make_boxes): boxes in block coordinates
+ * (6 ints each) of the set blocks of tags (nb^3, x fastest) inside the
+ * allowed blocks; returns their number, or -1 if cap is too small. */
+int orc_make_boxes(const unsigned char *tags, const unsigned char *allowed, int nb,
+                   int clustering, double grid_eff, int w, int *out, int cap) {
+    const size_t n = (size_t)nb * nb * nb;
+    std::vector<uint8_t> t(tags, tags + n), a(allowed, allowed + n);
+    const auto b = shamr::make_boxes(t, a, nb, clustering, grid_eff, w);
+    if ((int)b.size() > cap) return -1;
+    for (size_t q = 0; q < b.size(); ++q)
+        for (int d = 0; d < 3; ++d) {
+            out[6 * q + d] = b[q].lo[d];
+            out[6 * q + 3 + d] = b[q].hi[d];
+        }
+    return (int)b.size();
 }
 
 /* Boxes (6 ints each) of level lev; returns their number. */

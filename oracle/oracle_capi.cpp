@@ -52,3 +52,49 @@ extern "C" int orc_stencil(int kind, int order, int N, const double *field, doub
             }
     return 0;
 }
+
+/* Bubble injection of FirstOrderPhaseTransition on a periodic N^3 level in
+ * the canonical layout (ncomp components): every cell (i, j, k) at
+ * position (i dx, j dx, k dx) takes, for every bubble b in order, the
+ * profile value at its periodic distance D from the bubble centre,
+ * linearly interpolated in bins of width 1/inv_dx, added to component
+ * comp_phi (profile row 0) and comp_dphi (row 1); cells with D >= Lcut are
+ * left alone.  Restates projects/FirstOrderPhaseTransition/
+ * kernels_misc.h:21-52 (Distance, AddBubble), bubbles.h:8-19 (GetPos,
+ * GetVal) and FirstOrderPhaseTransition.cpp:459-483 (AddBubbleValues: cells
+ * outer, bubbles inner). */
+extern "C" int orc_add_bubbles(int N, int ncomp, double *state, int comp_phi, int comp_dphi,
+                               int nb, const double *xyz, const double *profile, int nbins,
+                               double inv_dx, double Lcut, double dx) {
+    if (N <= 0 || nb < 0 || nbins < 2 || comp_phi < 0 || comp_phi >= ncomp || comp_dphi < 0 ||
+        comp_dphi >= ncomp)
+        return -1;
+    if ((long long)(Lcut * inv_dx) + 2 > nbins) return -1;
+    const double L = N * dx;
+    auto distance = [&](double a, double b) {
+        const double d = std::fabs(a - b);
+        return d < L / 2. ? d : L - d;
+    };
+    const size_t n3 = (size_t)N * N * N;
+    for (int k = 0; k < N; ++k)
+        for (int j = 0; j < N; ++j)
+            for (int i = 0; i < N; ++i) {
+                const size_t c = ((size_t)k * N + j) * N + i;
+                for (int b = 0; b < nb; ++b) {
+                    const double Dx = distance(i * dx, xyz[3 * b + 0]);
+                    const double Dy = distance(j * dx, xyz[3 * b + 1]);
+                    const double Dz = distance(k * dx, xyz[3 * b + 2]);
+                    const double D = std::sqrt(Dx * Dx + Dy * Dy + Dz * Dz);
+                    if (D >= Lcut) continue;
+                    const double pos = D * inv_dx;
+                    const int ind = (int)pos;
+                    const double frac = pos - (double)ind;
+                    for (int r = 0; r < 2; ++r) {
+                        const double *p = profile + (size_t)r * nbins;
+                        const double val = p[ind] * (1. - frac) + p[ind + 1] * frac;
+                        state[(size_t)(r == 0 ? comp_phi : comp_dphi) * n3 + c] += val;
+                    }
+                }
+            }
+    return 0;
+}

@@ -15,6 +15,7 @@
 #include <FirstOrderPhaseTransition/setup.h>
 #include <FirstOrderPhaseTransition/kernels_rhs.h>
 #include <FirstOrderPhaseTransition/kernels_tagging.h>
+#include <FirstOrderPhaseTransition/kernels_misc.h>
 #include <MinimalExample/MinimalExample.h>
 
 #include "oracle_core.h"
@@ -135,5 +136,39 @@ extern "C" int ref_stencil(int kind, int order, int N, const double *field, doub
                 }
                 out[((size_t)k * N + j) * N + i] = v;
             }
+    return 0;
+}
+
+/* The reference's AddBubble (projects/FirstOrderPhaseTransition/
+ * kernels_misc.h:27-52) over every cell of a periodic N^3 canonical array,
+ * bubbles inner, as AddBubbleValues (FirstOrderPhaseTransition.cpp:459-483).
+ * Components: Scalar::Phi and Scalar::dPhi of the project. */
+extern "C" int ref_add_bubbles(int N, int ncomp, double *state, int nb, const double *xyz,
+                               const double *profile, int nbins, double inv_dx, double Lcut,
+                               double dx) {
+    using FirstOrderPhaseTransition::Bubble;
+    std::vector<Bubble> bubbles(nb);
+    for (int b = 0; b < nb; ++b) {
+        Bubble &B = bubbles[b];
+        B.x = xyz[3 * b];
+        B.y = xyz[3 * b + 1];
+        B.z = xyz[3 * b + 2];
+        B.t = 0.;
+        B.profile.assign(2, std::vector<double>(nbins));
+        for (int r = 0; r < 2; ++r)
+            for (int q = 0; q < nbins; ++q) B.profile[r][q] = profile[(size_t)r * nbins + q];
+        B.inv_dx = inv_dx;
+        B.L = Lcut;
+        B.finest_level = 0;
+        B.p_bubble = &B;
+    }
+    const long long n3 = (long long)N * N * N;
+    amrex::Array4<double> fab(state, N, (long long)N * N, n3, amrex::Dim3{0, 0, 0}, ncomp);
+    const double L = N * dx;
+    for (int k = 0; k < N; ++k)
+        for (int j = 0; j < N; ++j)
+            for (int i = 0; i < N; ++i)
+                for (int b = 0; b < nb; ++b)
+                    FirstOrderPhaseTransition::AddBubble(i, j, k, dx, L, fab, bubbles[b]);
     return 0;
 }

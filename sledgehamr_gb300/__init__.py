@@ -311,6 +311,16 @@ class Level:
             "sh_tag")
         return mask, counts, (lst[: nt.value].copy() if want_list else None)
 
+    def add_bubbles(self, centres, profile, inv_dx: float, Lcut: float, dx: float,
+                    comp_phi: int = 0, comp_dphi: int = 1, which: int = SH_NEW):
+        """FirstOrderPhaseTransition bubble injection (sh_level_add_bubbles):
+        centres (nb, 3), profile (2, nbins) for the field and its momentum."""
+        xyz = _f64(centres)
+        prof = _f64(profile)
+        self.ctx.check(self.ctx.lib.sh_level_add_bubbles(
+            self.ctx.h, self.h, which, comp_phi, comp_dphi, xyz.size // 3, _ptr(xyz), _ptr(prof),
+            prof.size // 2, float(inv_dx), float(Lcut), float(dx)), "sh_level_add_bubbles")
+
     def gw_spectrum(self, zero_padding: int = 1, projection_type: int = 2, unbinned: bool = True,
                     comps: Sequence[int] | None = None):
         N = self.domain[1][0] - self.domain[0][0] + 1
@@ -409,6 +419,20 @@ class Amr:
         self.ctx.lib.sh_amr_info(self.h, C.byref(f), C.byref(cu), C.byref(nr))
         return {"finest": f.value, "cell_updates": cu.value, "nregrids": nr.value}
 
+    def set_timer_sync(self, on: bool = True):
+        self.ctx.check(self.ctx.lib.sh_amr_set_timer_sync(self.h, int(on)), "set_timer_sync")
+
+    def timers(self) -> dict:
+        """Host seconds and calls per time-stepper phase (sh_amr_timer)."""
+        out = {}
+        q = 0
+        name, sec, calls = C.c_char_p(), C.c_double(), C.c_longlong()
+        while self.ctx.lib.sh_amr_timer(self.h, q, C.byref(name), C.byref(sec),
+                                        C.byref(calls)) == 0:
+            out[name.value.decode()] = (sec.value, calls.value)
+            q += 1
+        return out
+
     def level(self, lev: int) -> LevelView:
         h = C.c_void_p()
         self.ctx.check(self.ctx.lib.sh_amr_level(self.h, lev, C.byref(h)), "sh_amr_level")
@@ -463,7 +487,7 @@ class Ensemble:
         self.ctx = ctx
         self.family = family
         self.N = [int(n) for n in N]
-        self.ncomp = _FAMILY_NCOMP[family]
+        self.ncomp = _FAMILY_NCOMP.get(family, 0)  # unknown families: rejected below
         n = np.ascontiguousarray(np.asarray(self.N, dtype=np.int32))
         d = _f64(dx, len(self.N))
         p = None if params is None else _f64(params, 4 * len(self.N))
@@ -530,6 +554,15 @@ class Ensemble:
         c = np.empty(len(self.N), dtype=np.int64)
         self.check(self.ctx.lib.sh_ensemble_string_count(self.h, _ptr(c)), "string_count")
         return c
+
+    def add_bubbles(self, r: int, centres, profile, inv_dx: float, Lcut: float):
+        """Bubbles into realisation r (FOPT_GW): centres (nb, 3), profile
+        (2, nbins) for Phi and dPhi (sh_level_add_bubbles)."""
+        xyz = _f64(centres)
+        prof = _f64(profile)
+        self.check(self.ctx.lib.sh_ensemble_add_bubbles(
+            self.h, r, xyz.size // 3, _ptr(xyz), _ptr(prof), prof.size // 2, float(inv_dx),
+            float(Lcut)), "add_bubbles")
 
     def gw_spectrum(self, r: int, zero_padding: int = 1, projection_type: int = 2,
                     unbinned: bool = True):

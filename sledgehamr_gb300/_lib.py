@@ -53,7 +53,8 @@ class ShAmrConfig(C.Structure):
                 ("regrid_dt", C.c_double), ("string_width_threshold", C.c_double),
                 ("string_lambda", C.c_double), ("te_crit", C.c_double * 32),
                 ("params", C.c_double * 32), ("nparams", C.c_int),
-                ("gw_params", C.c_double * 16), ("ngw", C.c_int)]
+                ("gw_params", C.c_double * 16), ("ngw", C.c_int), ("clustering", C.c_int),
+                ("grid_eff", C.c_double)]
 
 
 # name -> (restype, argtypes)
@@ -79,27 +80,33 @@ SIGNATURES = {
     "sh_level_set_time": (C.c_int, [vp, C.c_int, C.c_double, C.c_int]),
     "sh_level_boxes": (C.c_int, [vp, C.POINTER(ShBox), C.c_int, ip]),
     "sh_level_set_index": (C.c_int, [vp, C.c_int]),
-    "sh_ensemble_create": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, ip, dp, dp, C.POINTER(vp)]),
+    "sh_ensemble_create": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, C.POINTER(vp)]),
     "sh_ensemble_destroy": (C.c_int, [vp]),
     "sh_ensemble_last_error": (C.c_char_p, [vp]),
     "sh_ensemble_info": (C.c_int, [vp, ip, ip, ip, ip, llp, llp, ip]),
     "sh_ensemble_kernel_launches": (C.c_longlong, [vp]),
     "sh_ensemble_set_time": (C.c_int, [vp, C.c_double]),
     "sh_ensemble_time": (C.c_int, [vp, dp]),
-    "sh_ensemble_write": (C.c_int, [vp, C.c_int, dp]),
-    "sh_ensemble_read": (C.c_int, [vp, C.c_int, dp]),
+    "sh_ensemble_write": (C.c_int, [vp, C.c_int, vp]),
+    "sh_ensemble_read": (C.c_int, [vp, C.c_int, vp]),
     "sh_ensemble_set_graph": (C.c_int, [vp, C.c_int]),
     "sh_ensemble_step": (C.c_int, [vp, C.c_double, C.c_int]),
     "sh_ensemble_tune": (C.c_int, [vp, C.c_int, C.c_double, ip]),
-    "sh_ensemble_energy": (C.c_int, [vp, dp]),
-    "sh_ensemble_string_count": (C.c_int, [vp, llp]),
-    "sh_ensemble_gw_spectrum": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, dp, llp,
+    "sh_ensemble_energy": (C.c_int, [vp, vp]),
+    "sh_ensemble_string_count": (C.c_int, [vp, vp]),
+    "sh_ensemble_add_bubbles": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, C.c_int, C.c_double,
+                                          C.c_double]),
+    "sh_level_add_bubbles": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp,
+                                       C.c_int, C.c_double, C.c_double, C.c_double]),
+    "sh_ensemble_gw_spectrum": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp,
                                           C.c_int, ip]),
     "sh_amr_config_defaults": (C.c_int, [C.POINTER(ShAmrConfig)]),
     "sh_amr_create": (C.c_int, [vp, C.POINTER(ShAmrConfig), vp, C.POINTER(vp)]),
     "sh_amr_destroy": (C.c_int, [vp, vp]),
     "sh_amr_step": (C.c_int, [vp, vp, C.c_int]),
     "sh_amr_info": (C.c_int, [vp, ip, llp, ip]),
+    "sh_amr_set_timer_sync": (C.c_int, [vp, C.c_int]),
+    "sh_amr_timer": (C.c_int, [vp, C.c_int, C.POINTER(C.c_char_p), dp, llp]),
     "sh_amr_level": (C.c_int, [vp, C.c_int, C.POINTER(vp)]),
     "sh_amr_regrid_record": (C.c_int, [vp, C.c_int, ip, dp, C.POINTER(ShBox), C.c_int, ip, vp,
                                        C.c_longlong, llp, C.POINTER(ShBox), C.c_int, ip]),

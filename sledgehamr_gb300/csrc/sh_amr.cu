@@ -118,6 +118,7 @@ struct GpuBackend {
         link(l, coarse ? *coarse : nullptr);
         ok(sh_level_fill_patch(ctx, l->L, which), "sh_level_fill_patch");
     }
+    void sync() { ok(sh_ctx_synchronize(ctx), "sh_ctx_synchronize"); }
 };
 
 } // namespace
@@ -144,6 +145,8 @@ shamr::Config driver_config(const sh_amr_config &c, int ncomp) {
     d.string_width_threshold = c.string_width_threshold;
     d.string_lambda = c.string_lambda;
     d.te_crit.assign(c.te_crit, c.te_crit + ncomp);
+    d.clustering = c.clustering;
+    d.grid_eff = c.grid_eff;
     return d;
 }
 
@@ -179,6 +182,8 @@ int sh_amr_config_defaults(sh_amr_config *c) {
     c->cfl = 0.25;
     c->t_start = 0.1;
     c->string_lambda = 1.;
+    c->clustering = SH_CLUSTER_BR;
+    c->grid_eff = 0.7;
     for (int n = 0; n < 32; ++n) c->te_crit[n] = DBL_MAX;
     return SH_OK;
 }
@@ -190,6 +195,9 @@ int sh_amr_create(sh_ctx *ctx, const sh_amr_config *cfg, const double *level0, s
     int rc = sh_project_ncomp(cfg->project, cfg->with_gw, &ncomp, nullptr);
     if (rc != SH_OK) return rc;
     if (cfg->nparams < 0 || cfg->nparams > 32 || cfg->ngw < 0 || cfg->ngw > 16)
+        return SH_ERR_ARG;
+    if ((cfg->clustering != SH_CLUSTER_BR && cfg->clustering != SH_CLUSTER_WINDOWS) ||
+        !(cfg->grid_eff > 0. && cfg->grid_eff <= 1.))
         return SH_ERR_ARG;
     sh_amr *a = new (std::nothrow) sh_amr();
     if (!a) return SH_ERR_NOMEM;
@@ -229,6 +237,21 @@ int sh_amr_info(const sh_amr *a, int *finest, long long *cell_updates, int *nreg
     if (finest) *finest = a->driver->finest;
     if (cell_updates) *cell_updates = a->driver->cell_updates;
     if (nregrids) *nregrids = (int)a->driver->regrids.size();
+    return SH_OK;
+}
+
+int sh_amr_set_timer_sync(sh_amr *a, int on) {
+    if (!a) return SH_ERR_ARG;
+    a->driver->sync_timers = on != 0;
+    return SH_OK;
+}
+
+int sh_amr_timer(const sh_amr *a, int q, const char **name, double *seconds, long long *calls) {
+    if (!a || q < 0 || q >= shamr::Driver<GpuBackend>::kNTimers) return SH_ERR_ARG;
+    const auto &t = a->driver->timers[q];
+    if (name) *name = t.name;
+    if (seconds) *seconds = t.sec;
+    if (calls) *calls = t.calls;
     return SH_OK;
 }
 

@@ -22,9 +22,21 @@
  * local regrid): the tags of level l are buffered by n_error_buf cells,
  * coarsened to blocks of blocking_factor cells of level l+1, restricted to
  * blocks whose surroundings (ceil(nghost/2)+1 cells of level l) lie inside
- * level l, and the tagged blocks are merged, inside aligned windows of
- * max_grid_size cells, into boxes by x-runs, then equal runs along y, then
- * along z.  At most one new level is added per regrid, as in AMReX.
+ * level l.  The blocks are then turned into boxes in one of two ways:
+ *   clustering 0 (default): Berger-Rigoutsos clustering (Berger & Rigoutsos,
+ *     IEEE Trans. SMC 21 (1991) 1278) of the tagged blocks until every
+ *     cluster is at least grid_eff tagged: a cluster is shrunk to the bounding
+ *     box of its tags and, if too sparse, cut at the hole of its tag
+ *     signatures nearest its middle, else at the strongest zero crossing of
+ *     the signatures' second difference, else in half along its longest
+ *     side; the clusters are intersected with the nesting region, boxes
+ *     sharing a whole face are merged, and boxes longer than max_grid_size
+ *     are chopped into near-equal pieces - the sequence of AMReX's
+ *     MakeNewGrids (cluster, intersect, simplify, maxSize), restated;
+ *   clustering 1: tagged blocks merged inside aligned windows of
+ *     max_grid_size cells by x-runs, then equal runs along y, then along z
+ *     (every box fully tagged).
+ * At most one new level is added per regrid, as in AMReX.
  *
  * The backend B provides (Level is a handle it owns):
  *   Level create(int lev, const std::vector<IBox>&, int N);   // lev -1: shadow
@@ -39,12 +51,14 @@
  *   void fill_from_coarse(Level &fine, Level &crse, double time);
  *   void remake(Level &fresh, Level &old, Level &crse, double time);
  *   void refresh_ghosts(Level&, int which, Level *coarse);
+ *   void sync();   // wait for queued device work (timers with sync_timers)
  */
 #ifndef SH_AMR_DRIVER_H_
 #define SH_AMR_DRIVER_H_
 
 #include <algorithm>
 #include <cfloat>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <functional>
@@ -78,6 +92,8 @@ struct Config {
     std::vector<double> te_crit; /* per component; DBL_MAX: off */
     double string_width_threshold = 0.; /* > 0: AxionStrings CreateLevelIf */
     double string_lambda = 1.;  /* lambda of cosmology.h */
+    int clustering = 0;         /* 0 Berger-Rigoutsos, 1 aligned windows */
+    double grid_eff = 0.7;      /* minimum tagged fraction of a cluster */
 };
 
 struct RegridRecord {
@@ -87,6 +103,250 @@ struct RegridRecord {
     std::vector<uint8_t> mask; /* boxes layout of the tagged level */
     std::vector<IBox> new_boxes;
 };
+
+/* ---- Berger-Rigoutsos clustering on the block grid ---- */
+struct BlockSet {
+    const std::vector<uint8_t> &bits;
+    int nb;
+    bool at(int x, int y, int z) const {
+        return bits[((size_t)z * nb + y) * nb + x] != 0;
+    }
+};
+
+/* Cut of a signature h[0..n-1] (both ends non-zero): position p in
+ * [1, n-1] splitting [0, p) | [p, n); kind 2 hole, 1 inflection, 0 none. */
+inline int signature_cut(const std::vector<long long> &h, int &kind, long long &strength) {
+    const int n = (int)h.size();
+    kind = 0;
+    strength = 0;
+    if (n < 2) return -1;
+    const double mid = 0.5 * n;
+    int best = -1;
+    for (int i = 1; i < n - 1; ++i)
+        if (h[i] == 0) {
+            /* cut just after the hole; keep the hole nearest the middle */
+            const int p = i + 1 <= n - 1 ? i + 1 : i;
+            if (best < 0 || std::fabs(p - mid) < std::fabs(best - mid)) best = p;
+        }
+    if (best > 0) {
+        kind = 2;
+        return best;
+    }
+    /* second difference d[i] = h[i-1] - 2 h[i] + h[i+1], i in [1, n-2];
+     * zero crossing between i-1 and i (both interior): cut at p = i */
+    for (int i = 2; i < n - 1; ++i) {
+        const long long a = h[i - 2] - 2 * h[i - 1] + h[i];
+        const long long b = h[i - 1] - 2 * h[i] + h[i + 1];
+        if ((a < 0 && b > 0) || (a > 0 && b < 0)) {
+            const long long st = a > b ? a - b : b - a;
+            if (st > strength || (st == strength && best > 0 &&
+                                  std::fabs(i - mid) < std::fabs(best - mid))) {
+                strength = st;
+                best = i;
+            }
+        }
+    }
+    if (best > 0) kind = 1;
+    return best;
+}
+
+inline void cluster(const BlockSet &t, IBox bx, double eff, std::vector<IBox> &out) {
+    /* signatures over bx, then shrink to the tags' bounding box */
+    std::vector<long long> sig[3];
+    for (int d = 0; d < 3; ++d) sig[d].assign(bx.hi[d] - bx.lo[d] + 1, 0);
+    long long ntag = 0;
+    for (int z = bx.lo[2]; z <= bx.hi[2]; ++z)
+        for (int y = bx.lo[1]; y <= bx.hi[1]; ++y)
+            for (int x = bx.lo[0]; x <= bx.hi[0]; ++x)
+                if (t.at(x, y, z)) {
+                    ++ntag;
+                    ++sig[0][x - bx.lo[0]];
+                    ++sig[1][y - bx.lo[1]];
+                    ++sig[2][z - bx.lo[2]];
+                }
+    if (ntag == 0) return;
+    IBox b = bx;
+    for (int d = 0; d < 3; ++d) {
+        int a = 0, e = (int)sig[d].size() - 1;
+        while (sig[d][a] == 0) ++a;
+        while (sig[d][e] == 0) --e;
+        b.lo[d] = bx.lo[d] + a;
+        b.hi[d] = bx.lo[d] + e;
+        sig[d] = std::vector<long long>(sig[d].begin() + a, sig[d].begin() + e + 1);
+    }
+    if ((double)ntag >= eff * (double)b.volume()) {
+        out.push_back(b);
+        return;
+    }
+    int dir = -1, pos = -1, bestkind = -1;
+    long long beststr = -1;
+    for (int d = 0; d < 3; ++d) {
+        int kind;
+        long long st;
+        const int p = signature_cut(sig[d], kind, st);
+        if (p <= 0) continue;
+        const bool better = kind > bestkind || (kind == bestkind && kind == 1 && st > beststr) ||
+                            (kind == bestkind && kind == 2 &&
+                             b.hi[d] - b.lo[d] > b.hi[dir] - b.lo[dir]);
+        if (better) {
+            dir = d;
+            pos = p;
+            bestkind = kind;
+            beststr = st;
+        }
+    }
+    if (bestkind == 1 && beststr <= 2) bestkind = 0; /* too weak: bisect */
+    if (bestkind <= 0) {
+        dir = 0;
+        for (int d = 1; d < 3; ++d)
+            if (b.hi[d] - b.lo[d] > b.hi[dir] - b.lo[dir]) dir = d;
+        pos = (b.hi[dir] - b.lo[dir] + 1) / 2;
+        if (pos == 0) { /* a single block (cannot happen: eff <= 1) */
+            out.push_back(b);
+            return;
+        }
+    }
+    IBox l = b, r = b;
+    l.hi[dir] = b.lo[dir] + pos - 1;
+    r.lo[dir] = b.lo[dir] + pos;
+    cluster(t, l, eff, out);
+    cluster(t, r, eff, out);
+}
+
+/* Boxes sharing a whole face are merged (BoxList::simplify). */
+inline void simplify(std::vector<IBox> &v) {
+    bool any = true;
+    while (any) {
+        any = false;
+        for (int d = 0; d < 3; ++d) {
+            const int e = (d + 1) % 3, f = (d + 2) % 3;
+            std::sort(v.begin(), v.end(), [&](const IBox &a, const IBox &b) {
+                if (a.lo[e] != b.lo[e]) return a.lo[e] < b.lo[e];
+                if (a.hi[e] != b.hi[e]) return a.hi[e] < b.hi[e];
+                if (a.lo[f] != b.lo[f]) return a.lo[f] < b.lo[f];
+                if (a.hi[f] != b.hi[f]) return a.hi[f] < b.hi[f];
+                return a.lo[d] < b.lo[d];
+            });
+            std::vector<IBox> res;
+            for (const IBox &x : v) {
+                if (!res.empty()) {
+                    IBox &p = res.back();
+                    if (p.lo[e] == x.lo[e] && p.hi[e] == x.hi[e] && p.lo[f] == x.lo[f] &&
+                        p.hi[f] == x.hi[f] && p.hi[d] + 1 == x.lo[d]) {
+                        p.hi[d] = x.hi[d];
+                        any = true;
+                        continue;
+                    }
+                }
+                res.push_back(x);
+            }
+            v.swap(res);
+        }
+    }
+}
+
+/* Boxes longer than w along an axis chopped into near-equal pieces. */
+inline void max_size(std::vector<IBox> &v, int w) {
+    for (int d = 0; d < 3; ++d) {
+        std::vector<IBox> res;
+        for (const IBox &x : v) {
+            const int len = x.hi[d] - x.lo[d] + 1;
+            const int n = (len + w - 1) / w;
+            int lo = x.lo[d];
+            for (int q = 0; q < n; ++q) {
+                const int sz = len / n + (q < len % n ? 1 : 0);
+                IBox y = x;
+                y.lo[d] = lo;
+                y.hi[d] = lo + sz - 1;
+                lo += sz;
+                res.push_back(y);
+            }
+        }
+        v.swap(res);
+    }
+}
+
+/* Set blocks inside window [lo, hi] (block coordinates) as boxes: x-runs,
+ * merged along y, then along z. */
+inline void runs_to_boxes(const BlockSet &t, const int lo[3], const int hi[3],
+                          std::vector<IBox> &out) {
+    std::vector<IBox> runs;
+    for (int z = lo[2]; z <= hi[2]; ++z)
+        for (int y = lo[1]; y <= hi[1]; ++y) {
+            int x = lo[0];
+            while (x <= hi[0]) {
+                if (!t.at(x, y, z)) {
+                    ++x;
+                    continue;
+                }
+                int x1 = x;
+                while (x1 + 1 <= hi[0] && t.at(x1 + 1, y, z)) ++x1;
+                runs.push_back(IBox{{x, y, z}, {x1, y, z}});
+                x = x1 + 1;
+            }
+        }
+    auto merge = [&](int d) {
+        std::vector<IBox> res;
+        for (const IBox &r : runs) {
+            bool merged = false;
+            for (IBox &p : res) {
+                bool same = p.hi[d] + 1 == r.lo[d];
+                for (int e = 0; e < 3 && same; ++e)
+                    if (e != d) same = p.lo[e] == r.lo[e] && p.hi[e] == r.hi[e];
+                if (same) {
+                    p.hi[d] = r.hi[d];
+                    merged = true;
+                    break;
+                }
+            }
+            if (!merged) res.push_back(r);
+        }
+        runs.swap(res);
+    };
+    merge(1);
+    merge(2);
+    out.insert(out.end(), runs.begin(), runs.end());
+}
+
+/* Boxes (block coordinates) covering the set blocks of `tags` (nb^3 blocks,
+ * x fastest), inside the allowed blocks, at most w blocks per side:
+ * clustering 0 Berger-Rigoutsos to efficiency grid_eff, 1 aligned windows. */
+inline std::vector<IBox> make_boxes(const std::vector<uint8_t> &tagbits,
+                                    const std::vector<uint8_t> &allowed, int nb, int clustering,
+                                    double grid_eff, int w) {
+    const BlockSet tags{tagbits, nb};
+    std::vector<IBox> bb;
+    if (clustering == 1) {
+        for (int wz = 0; wz < nb; wz += w)
+            for (int wy = 0; wy < nb; wy += w)
+                for (int wx = 0; wx < nb; wx += w) {
+                    const int lo[3] = {wx, wy, wz};
+                    const int hi[3] = {std::min(wx + w, nb) - 1, std::min(wy + w, nb) - 1,
+                                       std::min(wz + w, nb) - 1};
+                    runs_to_boxes(tags, lo, hi, bb);
+                }
+        return bb;
+    }
+    std::vector<IBox> cl;
+    cluster(tags, IBox{{0, 0, 0}, {nb - 1, nb - 1, nb - 1}}, grid_eff, cl);
+    const BlockSet nest{allowed, nb};
+    for (const IBox &x : cl) {
+        bool all = true;
+        for (int z = x.lo[2]; z <= x.hi[2] && all; ++z)
+            for (int y = x.lo[1]; y <= x.hi[1] && all; ++y)
+                for (int xx = x.lo[0]; xx <= x.hi[0] && all; ++xx) all = nest.at(xx, y, z);
+        if (all) bb.push_back(x);
+        else runs_to_boxes(nest, x.lo, x.hi, bb); /* the cluster within the nesting */
+    }
+    simplify(bb);
+    max_size(bb, w);
+    std::sort(bb.begin(), bb.end(), [](const IBox &a, const IBox &b) {
+        for (int d = 2; d >= 0; --d)
+            if (a.lo[d] != b.lo[d]) return a.lo[d] < b.lo[d];
+        return false;
+    });
+    return bb;
+}
 
 template <class B>
 class Driver {
@@ -143,7 +403,40 @@ class Driver {
     std::vector<std::string> trace; /* advance/sync/regrid events */
     bool record_trace = false;
 
+    /* Host wall-clock time spent in the backend operations, by phase.  With
+     * sync_timers, queued device work is waited for at both ends of every
+     * timed operation, so that the times are those of the operation. */
+    struct Timer {
+        const char *name;
+        double sec;
+        long long calls;
+    };
+    enum { kTAdvance, kTSync, kTShadow, kTTag, kTGrids, kTCreate, kTFill, kTDestroy,
+           kTRefresh, kNTimers };
+    Timer timers[kNTimers] = {{"advance", 0, 0},          {"synchronize", 0, 0},
+                              {"shadow", 0, 0},           {"regrid.tag", 0, 0},
+                              {"regrid.new_grids", 0, 0}, {"regrid.create", 0, 0},
+                              {"regrid.fill", 0, 0},      {"regrid.destroy", 0, 0},
+                              {"regrid.refresh", 0, 0}};
+    bool sync_timers = false;
+
   private:
+    struct Clock {
+        Driver *d;
+        int id;
+        std::chrono::steady_clock::time_point t0;
+        Clock(Driver *dr, int i) : d(dr), id(i) {
+            if (d->sync_timers) d->b.sync();
+            t0 = std::chrono::steady_clock::now();
+        }
+        ~Clock() {
+            if (d->sync_timers) d->b.sync();
+            d->timers[id].sec +=
+                std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            d->timers[id].calls++;
+        }
+    };
+
     B &b;
     Config c;
     Level shadow{};
@@ -206,8 +499,11 @@ class Driver {
         if (shadow_hierarchy) schedule_regrid_if_needed(lev);
         else no_shadow_regrid(lev);
         note("advance " + std::to_string(lev) + " t=" + std::to_string(tnew(lev)));
-        b.advance(lev, levels[lev], lev > 0 ? &levels[lev - 1] : nullptr, dt[lev], dx[lev],
-                  false);
+        {
+            Clock ck(this, kTAdvance);
+            b.advance(lev, levels[lev], lev > 0 ? &levels[lev - 1] : nullptr, dt[lev], dx[lev],
+                      false);
+        }
         te_valid[lev] = false;
         for (const IBox &bx : boxes[lev]) cell_updates += bx.volume();
         if (lev != finest) {
@@ -222,6 +518,7 @@ class Driver {
     }
 
     void synchronize_levels(int lev) {
+        Clock ck(this, kTSync);
         const bool te = need_te(lev, tnew(lev));
         if (lev < finest) {
             if (!(shadow_hierarchy && te)) {
@@ -265,6 +562,7 @@ class Driver {
 
     /* Sledgehamr::CreateShadowLevel + Integrator::Advance(-1) */
     void create_shadow_level() {
+        Clock ck(this, kTShadow);
         std::vector<IBox> sb;
         for (const IBox &bx : boxes[0]) {
             IBox s;
@@ -332,6 +630,7 @@ class Driver {
         if (shadow_hierarchy && !te_valid[l])
             throw std::runtime_error("tagging with truncation errors but none computed on level " +
                                      std::to_string(l));
+        Clock ck(this, kTTag);
         return b.tag(levels[l], shadow_hierarchy, time, l, dt[l], dx[l]);
     }
 
@@ -364,8 +663,10 @@ class Driver {
                                     blk[((size_t)pmod(bk, nb) * nb + pmod(bj, nb)) * nb +
                                         pmod(bi, nb)] = 1;
                     }
+        /* nesting: a block is allowed when the block grown by m level-l
+         * cells lies in level l (every block on level 0) */
+        std::vector<uint8_t> allowed((size_t)nb * nb * nb, 1);
         if (l >= 1) {
-            /* nesting: the block grown by m level-l cells must lie in level l */
             const int m = (c.nghost + 1) / 2 + 1;
             const int lb = c.blocking_factor; /* level-l boxes are unions of these */
             const int nlb = Nl / lb;
@@ -378,82 +679,28 @@ class Driver {
             for (int bk = 0; bk < nb; ++bk)
                 for (int bj = 0; bj < nb; ++bj)
                     for (int bi = 0; bi < nb; ++bi) {
-                        uint8_t &v = blk[((size_t)bk * nb + bj) * nb + bi];
-                        if (!v) continue;
                         const int lo[3] = {bi * cb - m, bj * cb - m, bk * cb - m};
                         const int hi[3] = {(bi + 1) * cb + m - 1, (bj + 1) * cb + m - 1,
                                            (bk + 1) * cb + m - 1};
                         bool ok = true;
-                        for (int z = (int)std::floor((double)lo[2] / lb);
-                             ok && z <= (int)std::floor((double)hi[2] / lb); ++z)
-                            for (int y = (int)std::floor((double)lo[1] / lb);
-                                 ok && y <= (int)std::floor((double)hi[1] / lb); ++y)
-                                for (int x = (int)std::floor((double)lo[0] / lb);
-                                     ok && x <= (int)std::floor((double)hi[0] / lb); ++x)
+                        for (int z = fdiv(lo[2], lb); ok && z <= fdiv(hi[2], lb); ++z)
+                            for (int y = fdiv(lo[1], lb); ok && y <= fdiv(hi[1], lb); ++y)
+                                for (int x = fdiv(lo[0], lb); ok && x <= fdiv(hi[0], lb); ++x)
                                     ok = cov[((size_t)pmod(z, nlb) * nlb + pmod(y, nlb)) * nlb +
                                              pmod(x, nlb)] != 0;
-                        if (!ok) v = 0;
+                        const size_t q = ((size_t)bk * nb + bj) * nb + bi;
+                        allowed[q] = ok;
+                        if (!ok) blk[q] = 0;
                     }
         }
-        /* merge tagged blocks within aligned windows of max_grid_size */
-        const int w = c.max_grid_size / bf; /* blocks per window side */
+        const int w = c.max_grid_size / bf; /* blocks per box side at most */
+        const std::vector<IBox> bb = make_boxes(blk, allowed, nb, c.clustering, c.grid_eff, w);
         std::vector<IBox> out;
-        for (int wz = 0; wz < nb; wz += w)
-            for (int wy = 0; wy < nb; wy += w)
-                for (int wx = 0; wx < nb; wx += w) {
-                    struct Run {
-                        int x0, x1, y0, y1, z0, z1;
-                    };
-                    std::vector<Run> runs;
-                    for (int z = wz; z < std::min(wz + w, nb); ++z)
-                        for (int y = wy; y < std::min(wy + w, nb); ++y) {
-                            int x = wx;
-                            while (x < std::min(wx + w, nb)) {
-                                if (!blk[((size_t)z * nb + y) * nb + x]) {
-                                    ++x;
-                                    continue;
-                                }
-                                int x1 = x;
-                                while (x1 + 1 < std::min(wx + w, nb) &&
-                                       blk[((size_t)z * nb + y) * nb + x1 + 1])
-                                    ++x1;
-                                runs.push_back(Run{x, x1, y, y, z, z});
-                                x = x1 + 1;
-                            }
-                        }
-                    /* merge runs with equal x extent along y, then along z */
-                    auto merge = [&](bool along_y) {
-                        std::vector<Run> res;
-                        for (const Run &r : runs) {
-                            bool merged = false;
-                            for (Run &p : res) {
-                                if (along_y) {
-                                    if (p.x0 == r.x0 && p.x1 == r.x1 && p.z0 == r.z0 &&
-                                        p.z1 == r.z1 && p.y1 + 1 == r.y0) {
-                                        p.y1 = r.y1;
-                                        merged = true;
-                                        break;
-                                    }
-                                } else {
-                                    if (p.x0 == r.x0 && p.x1 == r.x1 && p.y0 == r.y0 &&
-                                        p.y1 == r.y1 && p.z1 + 1 == r.z0) {
-                                        p.z1 = r.z1;
-                                        merged = true;
-                                        break;
-                                    }
-                                }
-                            }
-                            if (!merged) res.push_back(r);
-                        }
-                        runs = res;
-                    };
-                    merge(true);
-                    merge(false);
-                    for (const Run &r : runs)
-                        out.push_back(IBox{{r.x0 * bf, r.y0 * bf, r.z0 * bf},
-                                           {(r.x1 + 1) * bf - 1, (r.y1 + 1) * bf - 1,
-                                            (r.z1 + 1) * bf - 1}});
-                }
+        out.reserve(bb.size());
+        for (const IBox &r : bb)
+            out.push_back(IBox{{r.lo[0] * bf, r.lo[1] * bf, r.lo[2] * bf},
+                               {(r.hi[0] + 1) * bf - 1, (r.hi[1] + 1) * bf - 1,
+                                (r.hi[2] + 1) * bf - 1}});
         return out;
     }
 
@@ -467,7 +714,10 @@ class Driver {
         int new_finest = lbase;
         for (int l = lbase; l <= top; ++l) {
             std::vector<IBox> nb;
-            if (!tags[l].empty()) nb = new_grids(l, tags[l], old_boxes[l], boxes[l]);
+            if (!tags[l].empty()) {
+                Clock ck(this, kTGrids);
+                nb = new_grids(l, tags[l], old_boxes[l], boxes[l]);
+            }
             if (record_regrids) {
                 RegridRecord rr;
                 rr.lev = l;
@@ -479,22 +729,42 @@ class Driver {
             }
             if (nb.empty()) break;
             const int f = l + 1;
-            b.refresh_ghosts(levels[l], kNew, l > 0 ? &levels[l - 1] : nullptr);
+            {
+                Clock ck(this, kTRefresh);
+                b.refresh_ghosts(levels[l], kNew, l > 0 ? &levels[l - 1] : nullptr);
+            }
             if (f <= finest) {
                 /* RemakeLevel: fill the new layout from the old one and the
                  * coarse level; the old time level is redefined, times kept */
                 const double tn = b.time(levels[f], kNew), to = b.time(levels[f], kOld);
                 const int sn = b.istep(levels[f], kNew), so = b.istep(levels[f], kOld);
-                Level fresh = b.create(f, nb, dimN[f]);
-                b.remake(fresh, levels[f], levels[l], time);
-                b.destroy(levels[f]);
+                Level fresh;
+                {
+                    Clock ck(this, kTCreate);
+                    fresh = b.create(f, nb, dimN[f]);
+                }
+                {
+                    Clock ck(this, kTFill);
+                    b.remake(fresh, levels[f], levels[l], time);
+                }
+                {
+                    Clock ck(this, kTDestroy);
+                    b.destroy(levels[f]);
+                }
                 levels[f] = fresh;
                 b.set_time(levels[f], kNew, tn, sn);
                 b.set_time(levels[f], kOld, to, so);
             } else {
                 /* MakeNewLevelFromCoarse */
-                Level fresh = b.create(f, nb, dimN[f]);
-                b.fill_from_coarse(fresh, levels[l], time);
+                Level fresh;
+                {
+                    Clock ck(this, kTCreate);
+                    fresh = b.create(f, nb, dimN[f]);
+                }
+                {
+                    Clock ck(this, kTFill);
+                    b.fill_from_coarse(fresh, levels[l], time);
+                }
                 levels[f] = fresh;
                 b.set_time(levels[f], kNew, time, 0);
                 b.set_time(levels[f], kOld, -DBL_MAX, 0);

@@ -13,8 +13,10 @@
 #include <new>
 #include <stdexcept>
 #include <string>
+#include <tuple>
 #include <vector>
 
+#include "sh_bubbles.cuh"
 #include "sh_gw.h"
 #include "sh_internal.h"
 
@@ -48,8 +50,36 @@ struct ProfRecord {
     cudaEvent_t start, stop;
 };
 static const char *const kProfCategories[] = {"rhs",     "fill_patch",  "average_down",
-                                              "tagging", "gw_spectrum", "data_move"};
-enum ProfCat { kProfRhs = 0, kProfFill, kProfAvg, kProfTag, kProfGw, kProfMove, kProfCount };
+                                              "tagging", "gw_spectrum", "data_move",
+                                              "coarse_fine"};
+enum ProfCat {
+    kProfRhs = 0,
+    kProfFill,
+    kProfAvg,
+    kProfTag,
+    kProfGw,
+    kProfMove,
+    kProfCf,
+    kProfCount
+};
+
+/* Work items of the fill kernels (one thread block each): a rectangle of
+ * cells of one destination box, at most kItemCells cells, with the flat
+ * offsets of its first cell (component 0) and its row / plane strides. */
+constexpr int kItemCells = 4096;
+struct CopyItem {
+    long long dst, src;     /* first cell in the dst / src buffers */
+    long long dgvol, sgvol; /* component strides */
+    int nx, ny, nz;
+    int dsy, dsz, ssy, ssz;
+};
+struct CfItem {
+    long long dst, dgvol;
+    int dsy, dsz;
+    int lo[3]; /* fine index of the first cell */
+    int nx, ny, nz;
+    int pad;
+};
 
 struct sh_ctx {
     int device = 0;
@@ -64,8 +94,8 @@ struct sh_ctx {
     bool profiling = false;
     std::vector<ProfRecord> prof;
     std::vector<cudaEvent_t> event_pool;
-    double prof_ms[kProfCount] = {0, 0, 0, 0, 0, 0};
-    long long prof_n[kProfCount] = {0, 0, 0, 0, 0, 0};
+    double prof_ms[kProfCount] = {};
+    long long prof_n[kProfCount] = {};
 };
 
 struct sh_level {
@@ -81,8 +111,8 @@ struct sh_level {
     BoxDev *d_boxes = nullptr;
     TileDev *d_tiles = nullptr;
     int ntiles = 0;
-    GhostCopyDev *d_ghost = nullptr;
-    int nghost_rects = 0;
+    CopyItem *d_ghost = nullptr; /* periodic / same-level ghost copies */
+    int nghost_items = 0;
     long long nghost_cells = 0;
     long long *d_vbase = nullptr; /* nbox + 1 */
     double *buf[3] = {nullptr, nullptr, nullptr}; /* SH_NEW, SH_OLD, alt */
@@ -93,9 +123,9 @@ struct sh_level {
     int istep[2] = {0, 0};
     /* coarse level for two-level ghost fills (nullptr: periodic single level) */
     sh_level *coarse = nullptr;
-    void *d_cf = nullptr; /* CfRect list of ghost cells interpolated from coarse */
-    int ncf_rects = 0;
-    long long ncf = 0;    /* cells in those rectangles */
+    CfItem *d_cf = nullptr; /* ghost cells interpolated from the coarse level */
+    int ncf_items = 0;
+    long long ncf = 0;      /* cells of those items */
     std::vector<int> owner; /* owner box of each block of owner_res cells */
     int owner_res = 1;
     int owner_nb[3] = {1, 1, 1};
@@ -251,33 +281,19 @@ __global__ void move_kernel(const BoxDev *boxes, const long long *vbase, int nbo
     }
 }
 
-/* Periodic ghost fill: one thread per ghost cell of the copy plan. */
-__global__ void ghost_copy_kernel(const BoxDev *boxes, const GhostCopyDev *rects, int nrects,
-                                  long long ncells, int ncomp, double *buf) {
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncells;
-         c += (long long)gridDim.x * blockDim.x) {
-        int lo = 0, hi = nrects - 1;
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (rects[mid].first <= c) lo = mid;
-            else hi = mid - 1;
-        }
-        const GhostCopyDev &r = rects[lo];
-        const long long lc = c - r.first;
-        const int nx = r.hi[0] - r.lo[0] + 1, ny = r.hi[1] - r.lo[1] + 1;
-        const int i = r.lo[0] + (int)(lc % nx);
-        const int j = r.lo[1] + (int)((lc / nx) % ny);
-        const int k = r.lo[2] + (int)(lc / ((long long)nx * ny));
-        const BoxDev &db = boxes[r.dbox];
-        const BoxDev &sb = boxes[r.sbox];
-        const int si = i - r.shift[0], sj = j - r.shift[1], sk = k - r.shift[2];
-        const long long di = db.off * ncomp + (i - db.glo[0]) +
-                             (long long)(j - db.glo[1]) * db.gdim[0] +
-                             (long long)(k - db.glo[2]) * db.gdim[0] * db.gdim[1];
-        const long long sidx = sb.off * ncomp + (si - sb.glo[0]) +
-                               (long long)(sj - sb.glo[1]) * sb.gdim[0] +
-                               (long long)(sk - sb.glo[2]) * sb.gdim[0] * sb.gdim[1];
-        for (int n = 0; n < ncomp; ++n) buf[di + n * db.gvol] = buf[sidx + n * sb.gvol];
+/* Copies of rectangles of cells (ghost fill from the same level, periodic
+ * images, or level-to-level copies): one thread block per item, threads
+ * over its cells (x fastest), all components. */
+__global__ void copy_items_kernel(const CopyItem *items, double *dst, const double *src,
+                                  int ncomp) {
+    const CopyItem it = items[blockIdx.x];
+    const int n = it.nx * it.ny * it.nz;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        const int i = t % it.nx, r = t / it.nx;
+        const int j = r % it.ny, k = r / it.ny;
+        const long long d = it.dst + i + (long long)j * it.dsy + (long long)k * it.dsz;
+        const long long s = it.src + i + (long long)j * it.ssy + (long long)k * it.ssz;
+        for (int c = 0; c < ncomp; ++c) dst[d + c * it.dgvol] = src[s + c * it.sgvol];
     }
 }
 
@@ -299,38 +315,6 @@ struct OwnerMapDev {
     int ext[3];
 };
 
-/* Copy rectangles between two levels (dst ghost-grown cells from src valid
- * cells shifted by a periodic image). */
-__global__ void copy_rects_kernel(const BoxDev *dboxes, double *dbuf, const BoxDev *sboxes,
-                                  const double *sbuf, const GhostCopyDev *rects, int nrects,
-                                  long long ncells, int ncomp) {
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncells;
-         c += (long long)gridDim.x * blockDim.x) {
-        int lo = 0, hi = nrects - 1;
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (rects[mid].first <= c) lo = mid;
-            else hi = mid - 1;
-        }
-        const GhostCopyDev &r = rects[lo];
-        const long long lc = c - r.first;
-        const int nx = r.hi[0] - r.lo[0] + 1, ny = r.hi[1] - r.lo[1] + 1;
-        const int i = r.lo[0] + (int)(lc % nx);
-        const int j = r.lo[1] + (int)((lc / nx) % ny);
-        const int k = r.lo[2] + (int)(lc / ((long long)nx * ny));
-        const BoxDev &db = dboxes[r.dbox];
-        const BoxDev &sb = sboxes[r.sbox];
-        const int si = i - r.shift[0], sj = j - r.shift[1], sk = k - r.shift[2];
-        const long long di = db.off * ncomp + (i - db.glo[0]) +
-                             (long long)(j - db.glo[1]) * db.gdim[0] +
-                             (long long)(k - db.glo[2]) * db.gdim[0] * db.gdim[1];
-        const long long sidx = sb.off * ncomp + (si - sb.glo[0]) +
-                               (long long)(sj - sb.glo[1]) * sb.gdim[0] +
-                               (long long)(sk - sb.glo[2]) * sb.gdim[0] * sb.gdim[1];
-        for (int n = 0; n < ncomp; ++n) dbuf[di + n * db.gvol] = sbuf[sidx + n * sb.gvol];
-    }
-}
-
 /* Quadratic (CellQuadratic) interpolation of fine cells from the 3x3x3
  * coarse cells around their parent, after linear interpolation in time
  * between the coarse old and new data (mode 0: old only, 1: new only,
@@ -340,53 +324,46 @@ __global__ void copy_rects_kernel(const BoxDev *dboxes, double *dbuf, const BoxD
  *   u = u000 + sum_d xi_d D_d + 1/2 sum_d xi_d^2 D_dd + sum_{d<e} xi_d xi_e D_de
  * with D_d = (u_+ - u_-)/2, D_dd = u_+ - 2 u_0 + u_-, and
  * D_de = (u_++ - u_+- - u_-+ + u_--)/4 in the plane of d and e.
+ * One thread per coarse parent: the 19 coarse values and the differences
+ * are formed once and evaluated for each of its children inside the item
+ * (xi_d^2 = 1/16 for every child, so the second-order term is shared).
  * The parent (periodically wrapped) is found through the coarse level's
  * block map; its neighbours are read from the parent box's ghost cells. */
-__global__ void cf_interp_kernel(const CfRect *rects, int nrects, long long ncells,
-                                 const BoxDev *fboxes, double *fbuf, const BoxDev *cboxes,
+__global__ void cf_interp_kernel(const CfItem *items, const BoxDev *cboxes, double *fbuf,
                                  OwnerMapDev cmap, const double *c_old, const double *c_new,
                                  int mode, double alpha, double beta, int ncomp) {
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < ncells;
-         q += (long long)gridDim.x * blockDim.x) {
-        int lo = 0, hi = nrects - 1;
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (rects[mid].first <= q) lo = mid;
-            else hi = mid - 1;
-        }
-        const CfRect &r = rects[lo];
-        const long long lc = q - r.first;
-        const int nx = r.hi[0] - r.lo[0] + 1, ny = r.hi[1] - r.lo[1] + 1;
-        const int fi = r.lo[0] + (int)(lc % nx);
-        const int fj = r.lo[1] + (int)((lc / nx) % ny);
-        const int fk = r.lo[2] + (int)(lc / ((long long)nx * ny));
-        const int f3[3] = {fi, fj, fk};
-        int P[3], W[3], o = 0;
+    const CfItem it = items[blockIdx.x];
+    auto fl2 = [](int a) { return a >= 0 ? a / 2 : -((-a + 1) / 2); };
+    const int lo[3] = {it.lo[0], it.lo[1], it.lo[2]};
+    const int hi[3] = {it.lo[0] + it.nx - 1, it.lo[1] + it.ny - 1, it.lo[2] + it.nz - 1};
+    int plo[3], pn[3];
+    for (int d = 0; d < 3; ++d) {
+        plo[d] = fl2(lo[d]);
+        pn[d] = fl2(hi[d]) - plo[d] + 1;
+    }
+    const int np = pn[0] * pn[1] * pn[2];
+    for (int q = threadIdx.x; q < np; q += blockDim.x) {
+        const int P[3] = {plo[0] + q % pn[0], plo[1] + (q / pn[0]) % pn[1],
+                          plo[2] + q / (pn[0] * pn[1])};
+        int W[3], c0[3], c1[3];
         for (int d = 0; d < 3; ++d) {
-            P[d] = f3[d] >= 0 ? f3[d] / 2 : -((-f3[d] + 1) / 2);
-            o |= (f3[d] - 2 * P[d]) << d;
             int w = (P[d] - cmap.dlo[d]) % cmap.ext[d];
             if (w < 0) w += cmap.ext[d];
             W[d] = cmap.dlo[d] + w;
+            c0[d] = max(2 * P[d], lo[d]);
+            c1[d] = min(2 * P[d] + 1, hi[d]);
         }
         const int cbox = cmap.owner[((long long)((W[2] - cmap.dlo[2]) / cmap.res) * cmap.nb[1] +
                                      (W[1] - cmap.dlo[1]) / cmap.res) *
                                         cmap.nb[0] +
                                     (W[0] - cmap.dlo[0]) / cmap.res];
         if (cbox < 0) continue; /* excluded by the host's coverage check */
-        const BoxDev &fb = fboxes[r.dbox];
         const BoxDev &cb = cboxes[cbox];
         const long long cx = cb.gdim[0], cxy = cx * cb.gdim[1];
-        const long long c0 = cb.off * ncomp + (W[0] - cb.glo[0]) + (W[1] - cb.glo[1]) * cx +
-                             (W[2] - cb.glo[2]) * cxy;
-        const long long f0 = fb.off * ncomp + (fi - fb.glo[0]) +
-                             (long long)(fj - fb.glo[1]) * fb.gdim[0] +
-                             (long long)(fk - fb.glo[2]) * fb.gdim[0] * fb.gdim[1];
-        const double xi = (o & 1) ? 0.25 : -0.25;
-        const double yi = (o & 2) ? 0.25 : -0.25;
-        const double zi = (o & 4) ? 0.25 : -0.25;
+        const long long cbase = cb.off * ncomp + (W[0] - cb.glo[0]) + (W[1] - cb.glo[1]) * cx +
+                                (W[2] - cb.glo[2]) * cxy;
         for (int nn = 0; nn < ncomp; ++nn) {
-            const long long base = c0 + nn * cb.gvol;
+            const long long base = cbase + nn * cb.gvol;
             auto u = [&](int a, int b2, int d) {
                 const long long e = base + a + b2 * cx + d * cxy;
                 if (mode == 0) return c_old[e];
@@ -404,11 +381,44 @@ __global__ void cf_interp_kernel(const CfRect *rects, int nrects, long long ncel
             const double Dxy = (u(1, 1, 0) - u(1, -1, 0) - u(-1, 1, 0) + u(-1, -1, 0)) * 0.25;
             const double Dxz = (u(1, 0, 1) - u(1, 0, -1) - u(-1, 0, 1) + u(-1, 0, -1)) * 0.25;
             const double Dyz = (u(0, 1, 1) - u(0, 1, -1) - u(0, -1, 1) + u(0, -1, -1)) * 0.25;
-            const double v = u0 + xi * Dx + yi * Dy + zi * Dz +
-                             0.5 * (xi * xi * Dxx + yi * yi * Dyy + zi * zi * Dzz) +
-                             xi * yi * Dxy + xi * zi * Dxz + yi * zi * Dyz;
-            fbuf[f0 + nn * fb.gvol] = v;
+            const double Q = 0.5 * (0.0625 * Dxx + 0.0625 * Dyy + 0.0625 * Dzz);
+            for (int fk = c0[2]; fk <= c1[2]; ++fk) {
+                const double zi = (fk - 2 * P[2]) ? 0.25 : -0.25;
+                for (int fj = c0[1]; fj <= c1[1]; ++fj) {
+                    const double yi = (fj - 2 * P[1]) ? 0.25 : -0.25;
+                    for (int fi = c0[0]; fi <= c1[0]; ++fi) {
+                        const double xi = (fi - 2 * P[0]) ? 0.25 : -0.25;
+                        const double v = u0 + xi * Dx + yi * Dy + zi * Dz + Q + xi * yi * Dxy +
+                                         xi * zi * Dxz + yi * zi * Dyz;
+                        fbuf[it.dst + (fi - lo[0]) + (long long)(fj - lo[1]) * it.dsy +
+                             (long long)(fk - lo[2]) * it.dsz + nn * it.dgvol] = v;
+                    }
+                }
+            }
         }
+    }
+}
+
+/* Bubble injection on the valid cells of a level (sh_level_add_bubbles). */
+__global__ void level_bubbles_kernel(const BoxDev *boxes, const long long *vbase, int nbox,
+                                     long long nvalid, int ncomp, int cphi, int cdphi,
+                                     double *buf, BubbleList bl, double dx, double L) {
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nvalid;
+         v += (long long)gridDim.x * blockDim.x) {
+        const int bx = find_box(vbase, nbox, v);
+        const BoxDev &b = boxes[bx];
+        const long long lv = v - vbase[bx];
+        const int vx = b.hi[0] - b.lo[0] + 1, vy = b.hi[1] - b.lo[1] + 1;
+        const int i = b.lo[0] + (int)(lv % vx);
+        const int j = b.lo[1] + (int)((lv / vx) % vy);
+        const int k = b.lo[2] + (int)(lv / ((long long)vx * vy));
+        const long long c = b.off * ncomp + (i - b.glo[0]) +
+                            (long long)(j - b.glo[1]) * b.gdim[0] +
+                            (long long)(k - b.glo[2]) * b.gdim[0] * b.gdim[1];
+        double phi = buf[c + cphi * b.gvol], dphi = buf[c + cdphi * b.gvol];
+        add_bubbles_at(bl, i, j, k, dx, L, phi, dphi);
+        buf[c + cphi * b.gvol] = phi;
+        buf[c + cdphi * b.gvol] = dphi;
     }
 }
 
@@ -749,16 +759,154 @@ FillPlan build_fill_plan(const sh_level *D, const sh_level *S, const sh_level *C
     return P;
 }
 
+/* Adjacent rectangles of one destination box with the same source box and
+ * periodic shift merged along x, then y, then z (the cells and their
+ * values are unchanged; fewer, larger work items). */
+void merge_copy_rects(std::vector<GhostCopyDev> &v) {
+    for (int d = 0; d < 3; ++d) {
+        const int e = (d + 1) % 3, f = (d + 2) % 3;
+        auto key = [&](const GhostCopyDev &r) {
+            return std::make_tuple(r.dbox, r.sbox, r.shift[0], r.shift[1], r.shift[2], r.lo[e],
+                                   r.hi[e], r.lo[f], r.hi[f], r.lo[d]);
+        };
+        std::sort(v.begin(), v.end(),
+                  [&](const GhostCopyDev &a, const GhostCopyDev &b) { return key(a) < key(b); });
+        std::vector<GhostCopyDev> out;
+        out.reserve(v.size());
+        for (const GhostCopyDev &r : v) {
+            if (!out.empty()) {
+                GhostCopyDev &p = out.back();
+                if (p.dbox == r.dbox && p.sbox == r.sbox && p.shift[0] == r.shift[0] &&
+                    p.shift[1] == r.shift[1] && p.shift[2] == r.shift[2] && p.lo[e] == r.lo[e] &&
+                    p.hi[e] == r.hi[e] && p.lo[f] == r.lo[f] && p.hi[f] == r.hi[f] &&
+                    p.hi[d] + 1 == r.lo[d]) {
+                    p.hi[d] = r.hi[d];
+                    continue;
+                }
+            }
+            out.push_back(r);
+        }
+        v.swap(out);
+    }
+}
+
+void merge_cf_rects(std::vector<CfRect> &v) {
+    for (int d = 0; d < 3; ++d) {
+        const int e = (d + 1) % 3, f = (d + 2) % 3;
+        auto key = [&](const CfRect &r) {
+            return std::make_tuple(r.dbox, r.lo[e], r.hi[e], r.lo[f], r.hi[f], r.lo[d]);
+        };
+        std::sort(v.begin(), v.end(),
+                  [&](const CfRect &a, const CfRect &b) { return key(a) < key(b); });
+        std::vector<CfRect> out;
+        out.reserve(v.size());
+        for (const CfRect &r : v) {
+            if (!out.empty()) {
+                CfRect &p = out.back();
+                if (p.dbox == r.dbox && p.lo[e] == r.lo[e] && p.hi[e] == r.hi[e] &&
+                    p.lo[f] == r.lo[f] && p.hi[f] == r.hi[f] && p.hi[d] + 1 == r.lo[d]) {
+                    p.hi[d] = r.hi[d];
+                    continue;
+                }
+            }
+            out.push_back(r);
+        }
+        v.swap(out);
+    }
+}
+
+/* Splits the rectangle [lo, hi] into pieces of at most kItemCells cells
+ * (whole planes, else whole rows, else row segments). */
+template <class F>
+void split_rect(const int lo[3], const int hi[3], F &&emit) {
+    const int nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
+    if ((long long)nx * ny <= kItemCells) {
+        const int pz = std::max(1, kItemCells / (nx * ny));
+        for (int z = 0; z < nz; z += pz)
+            emit(lo[0], lo[1], lo[2] + z, nx, ny, std::min(pz, nz - z));
+    } else if (nx <= kItemCells) {
+        const int py = std::max(1, kItemCells / nx);
+        for (int z = 0; z < nz; ++z)
+            for (int y = 0; y < ny; y += py)
+                emit(lo[0], lo[1] + y, lo[2] + z, nx, std::min(py, ny - y), 1);
+    } else {
+        for (int z = 0; z < nz; ++z)
+            for (int y = 0; y < ny; ++y)
+                for (int x = 0; x < nx; x += kItemCells)
+                    emit(lo[0] + x, lo[1] + y, lo[2] + z, std::min(kItemCells, nx - x), 1, 1);
+    }
+}
+
+inline long long cell_offset(const BoxDev &b, int ncomp, int i, int j, int k) {
+    return b.off * ncomp + (i - b.glo[0]) + (long long)(j - b.glo[1]) * b.gdim[0] +
+           (long long)(k - b.glo[2]) * b.gdim[0] * b.gdim[1];
+}
+
+std::vector<CopyItem> copy_items(const std::vector<GhostCopyDev> &rects, const sh_level *D,
+                                 const sh_level *S) {
+    std::vector<CopyItem> items;
+    items.reserve(rects.size());
+    for (const GhostCopyDev &r : rects) {
+        const BoxDev &db = D->hboxes[r.dbox];
+        const BoxDev &sb = S->hboxes[r.sbox];
+        split_rect(r.lo, r.hi, [&](int x, int y, int z, int nx, int ny, int nz) {
+            CopyItem it;
+            it.dst = cell_offset(db, D->ncomp, x, y, z);
+            it.src = cell_offset(sb, S->ncomp, x - r.shift[0], y - r.shift[1], z - r.shift[2]);
+            it.dgvol = db.gvol;
+            it.sgvol = sb.gvol;
+            it.nx = nx;
+            it.ny = ny;
+            it.nz = nz;
+            it.dsy = db.gdim[0];
+            it.dsz = db.gdim[0] * db.gdim[1];
+            it.ssy = sb.gdim[0];
+            it.ssz = sb.gdim[0] * sb.gdim[1];
+            items.push_back(it);
+        });
+    }
+    return items;
+}
+
+std::vector<CfItem> cf_items(const std::vector<CfRect> &rects, const sh_level *D) {
+    std::vector<CfItem> items;
+    items.reserve(rects.size());
+    for (const CfRect &r : rects) {
+        const BoxDev &db = D->hboxes[r.dbox];
+        split_rect(r.lo, r.hi, [&](int x, int y, int z, int nx, int ny, int nz) {
+            CfItem it;
+            it.dst = cell_offset(db, D->ncomp, x, y, z);
+            it.dgvol = db.gvol;
+            it.dsy = db.gdim[0];
+            it.dsz = db.gdim[0] * db.gdim[1];
+            it.lo[0] = x;
+            it.lo[1] = y;
+            it.lo[2] = z;
+            it.nx = nx;
+            it.ny = ny;
+            it.nz = nz;
+            it.pad = 0;
+            items.push_back(it);
+        });
+    }
+    return items;
+}
+
+template <class T>
+T *upload_items(const std::vector<T> &v, const char *what) {
+    if (v.empty()) return nullptr;
+    T *d = (T *)dmalloc(v.size() * sizeof(T), what);
+    ck(cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), what);
+    return d;
+}
+
 void build_ghost_plan(sh_level *L) {
     FillPlan P = build_fill_plan(L, L, nullptr, true);
-    L->nghost_rects = (int)P.rects.size();
+    merge_copy_rects(P.rects);
+    const std::vector<CopyItem> items = copy_items(P.rects, L, L);
+    L->nghost_items = (int)items.size();
     L->nghost_cells = P.rect_cells;
-    if (!P.rects.empty()) {
-        L->d_ghost = (GhostCopyDev *)dmalloc(P.rects.size() * sizeof(GhostCopyDev), "ghost plan");
-        ck(cudaMemcpy(L->d_ghost, P.rects.data(), P.rects.size() * sizeof(GhostCopyDev),
-                      cudaMemcpyHostToDevice),
-           "ghost plan upload");
-    }
+    L->d_ghost = upload_items(items, "ghost plan");
 }
 
 /* GetLevelData time selection (level_synchronizer.cpp:613-632) for data of
@@ -804,21 +952,21 @@ void ensure_kbuf(sh_level *L, size_t elems, int count) {
  * fine level linked to its coarse level, the remaining ghost cells from the
  * coarse data at time t. */
 void fill_patch(sh_ctx *ctx, sh_level *L, double *buf, double t) {
-    ProfScope ps(ctx, kProfFill);
-    if (L->nghost_cells > 0) {
-        ghost_copy_kernel<<<grid_for(L->nghost_cells), 256, 0, ctx->stream>>>(
-            L->d_boxes, L->d_ghost, L->nghost_rects, L->nghost_cells, L->ncomp, buf);
+    if (L->nghost_items > 0) {
+        ProfScope ps(ctx, kProfFill);
+        copy_items_kernel<<<L->nghost_items, 128, 0, ctx->stream>>>(L->d_ghost, buf, buf,
+                                                                   L->ncomp);
         ctx->launches++;
         ck(cudaGetLastError(), "ghost fill launch");
     }
-    if (L->coarse && L->ncf > 0) {
+    if (L->coarse && L->ncf_items > 0) {
+        ProfScope ps(ctx, kProfCf);
         int mode;
         double alpha, beta;
         coarse_time_weights(L->coarse, t, mode, alpha, beta);
-        cf_interp_kernel<<<grid_for(L->ncf), 256, 0, ctx->stream>>>(
-            (const CfRect *)L->d_cf, L->ncf_rects, L->ncf, L->d_boxes, buf, L->coarse->d_boxes,
-            owner_map_dev(L->coarse), L->coarse->buf[SH_OLD], L->coarse->buf[SH_NEW], mode,
-            alpha, beta, L->ncomp);
+        cf_interp_kernel<<<L->ncf_items, 128, 0, ctx->stream>>>(
+            L->d_cf, L->coarse->d_boxes, buf, owner_map_dev(L->coarse), L->coarse->buf[SH_OLD],
+            L->coarse->buf[SH_NEW], mode, alpha, beta, L->ncomp);
         ctx->launches++;
         ck(cudaGetLastError(), "coarse-fine fill launch");
     }
@@ -1377,18 +1525,15 @@ int sh_level_set_coarse(sh_ctx *ctx, sh_level *fine, sh_level *coarse) {
         cudaFree(fine->d_cf);
         fine->d_cf = nullptr;
         fine->ncf = 0;
-        fine->ncf_rects = 0;
+        fine->ncf_items = 0;
         fine->coarse = nullptr;
         if (!coarse) return;
         require(coarse != fine, "a level cannot be its own coarse level");
         FillPlan P = build_fill_plan(fine, fine, coarse, true);
-        if (!P.cf.empty()) {
-            fine->d_cf = dmalloc(P.cf.size() * sizeof(CfRect), "coarse-fine plan");
-            ck(cudaMemcpy(fine->d_cf, P.cf.data(), P.cf.size() * sizeof(CfRect),
-                          cudaMemcpyHostToDevice),
-               "coarse-fine plan upload");
-        }
-        fine->ncf_rects = (int)P.cf.size();
+        merge_cf_rects(P.cf);
+        const std::vector<CfItem> items = cf_items(P.cf, fine);
+        fine->d_cf = upload_items(items, "coarse-fine plan");
+        fine->ncf_items = (int)items.size();
         fine->ncf = P.cf_cells;
         fine->coarse = coarse;
     });
@@ -1403,32 +1548,30 @@ int sh_level_fill_from(sh_ctx *ctx, sh_level *dst, int which_dst, const sh_level
         require(src != dst, "source and destination must differ");
         if (src) require(src->ncomp == dst->ncomp, "source differs in components");
         FillPlan P = build_fill_plan(dst, src, coarse, false);
-        void *d_rects = nullptr, *d_cf = nullptr;
+        CopyItem *d_rects = nullptr;
+        CfItem *d_cf = nullptr;
         if (!P.rects.empty()) {
-            d_rects = dmalloc(P.rects.size() * sizeof(GhostCopyDev), "fill plan");
-            ck(cudaMemcpy(d_rects, P.rects.data(), P.rects.size() * sizeof(GhostCopyDev),
-                          cudaMemcpyHostToDevice),
-               "fill plan upload");
+            merge_copy_rects(P.rects);
+            const std::vector<CopyItem> items = copy_items(P.rects, dst, src);
+            d_rects = upload_items(items, "fill plan");
             ProfScope ps(ctx, kProfFill);
-            copy_rects_kernel<<<grid_for(P.rect_cells), 256, 0, ctx->stream>>>(
-                dst->d_boxes, dst->buf[which_dst], src->d_boxes, src->buf[which_src],
-                (const GhostCopyDev *)d_rects, (int)P.rects.size(), P.rect_cells, dst->ncomp);
+            copy_items_kernel<<<(int)items.size(), 128, 0, ctx->stream>>>(
+                d_rects, dst->buf[which_dst], src->buf[which_src], dst->ncomp);
             ctx->launches++;
             ck(cudaGetLastError(), "fill copy launch");
         }
         if (!P.cf.empty()) {
             require(coarse != nullptr, "cells not covered by the source need a coarse level");
-            d_cf = dmalloc(P.cf.size() * sizeof(CfRect), "coarse fill plan");
-            ck(cudaMemcpy(d_cf, P.cf.data(), P.cf.size() * sizeof(CfRect), cudaMemcpyHostToDevice),
-               "coarse fill plan upload");
+            merge_cf_rects(P.cf);
+            const std::vector<CfItem> items = cf_items(P.cf, dst);
+            d_cf = upload_items(items, "coarse fill plan");
             int mode;
             double alpha, beta;
             coarse_time_weights(coarse, time, mode, alpha, beta);
-            ProfScope ps(ctx, kProfFill);
-            cf_interp_kernel<<<grid_for(P.cf_cells), 256, 0, ctx->stream>>>(
-                (const CfRect *)d_cf, (int)P.cf.size(), P.cf_cells, dst->d_boxes,
-                dst->buf[which_dst], coarse->d_boxes, owner_map_dev(coarse), coarse->buf[SH_OLD],
-                coarse->buf[SH_NEW], mode, alpha, beta, dst->ncomp);
+            ProfScope ps(ctx, kProfCf);
+            cf_interp_kernel<<<(int)items.size(), 128, 0, ctx->stream>>>(
+                d_cf, coarse->d_boxes, dst->buf[which_dst], owner_map_dev(coarse),
+                coarse->buf[SH_OLD], coarse->buf[SH_NEW], mode, alpha, beta, dst->ncomp);
             ctx->launches++;
             ck(cudaGetLastError(), "coarse fill launch");
         }
@@ -1480,6 +1623,41 @@ int sh_level_rhs(sh_ctx *ctx, sh_level *L, int which, double time, int lev, doub
         ck(cudaMemcpyAsync(host_rhs, stage, bytes, cudaMemcpyDeviceToHost, ctx->stream),
            "download");
         ck(cudaStreamSynchronize(ctx->stream), "rhs");
+    });
+}
+
+int sh_level_add_bubbles(sh_ctx *ctx, sh_level *L, int which, int comp_phi, int comp_dphi,
+                         int nb, const double *xyz, const double *profile, int nbins,
+                         double inv_dx, double Lcut, double dx) {
+    if (!ctx || !L || (which != SH_NEW && which != SH_OLD) || nb < 0 ||
+        (nb > 0 && (!xyz || !profile)) || nbins < 2 || !(inv_dx > 0) || !(Lcut > 0) ||
+        !(dx > 0))
+        return SH_ERR_ARG;
+    if (nb == 0) return SH_OK;
+    return guarded(ctx, [&] {
+        set_device(ctx);
+        require(comp_phi >= 0 && comp_phi < L->ncomp && comp_dphi >= 0 &&
+                    comp_dphi < L->ncomp,
+                "component index out of range");
+        require((long long)(Lcut * inv_dx) + 2 <= nbins,
+                "profile needs at least floor(Lcut * inv_dx) + 2 bins");
+        const int N = L->dhi[0] - L->dlo[0] + 1;
+        for (int d = 0; d < 3; ++d)
+            require(L->dhi[d] - L->dlo[d] + 1 == N, "bubbles need a cubic domain");
+        const size_t nx = 3 * (size_t)nb, np = 2 * (size_t)nbins;
+        double *d = (double *)ctx_scratch(ctx, (nx + np) * sizeof(double));
+        ck(cudaMemcpyAsync(d, xyz, nx * sizeof(double), cudaMemcpyHostToDevice, ctx->stream),
+           "bubble upload");
+        ck(cudaMemcpyAsync(d + nx, profile, np * sizeof(double), cudaMemcpyHostToDevice,
+                           ctx->stream),
+           "bubble upload");
+        BubbleList bl{d, d + nx, nb, nbins, inv_dx, Lcut};
+        level_bubbles_kernel<<<grid_for(L->nvalid), 256, 0, ctx->stream>>>(
+            L->d_boxes, L->d_vbase, (int)L->boxes.size(), L->nvalid, L->ncomp, comp_phi,
+            comp_dphi, L->buf[which], bl, dx, N * dx);
+        ctx->launches++;
+        ck(cudaGetLastError(), "bubble launch");
+        ck(cudaStreamSynchronize(ctx->stream), "bubbles");
     });
 }
 

@@ -35,6 +35,7 @@
 #include <string>
 #include <vector>
 
+#include "sh_bubbles.cuh"
 #include "sh_internal.h"
 #include "sledgehamr_gb300.h"
 
@@ -470,6 +471,31 @@ __global__ void gw_pack_fast_kernel(const R *src, const R *comp, long long off, 
         const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / ((long long)N * N));
         dst[((long long)z * P + y) * P + x] =
             (double)src[off + i] - (comp ? (double)comp[off + i] : 0.);
+    }
+}
+
+/* Bubbles added to Phi (array phi) and dPhi (array dphi) of realisation r;
+ * with compensations the sum is formed from the compensated values and the
+ * new compensation holds the rounding of the stored result. */
+template <class R>
+__global__ void add_bubbles_kernel(const RealDesc *desc, int r, R *phi, R *dphi, R *cphi,
+                                   R *cdphi, BubbleList bl) {
+    const RealDesc d = desc[r];
+    const int N = d.N;
+    const long long n = (long long)N * N * N;
+    const double L = N * d.dx;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % N), j = (int)((q / N) % N), k = (int)(q / ((long long)N * N));
+        const long long e = d.off + q;
+        double a = (double)phi[e] - (cphi ? (double)cphi[e] : 0.);
+        double b = (double)dphi[e] - (cdphi ? (double)cdphi[e] : 0.);
+        add_bubbles_at(bl, i, j, k, d.dx, L, a, b);
+        const R ra = (R)a, rb = (R)b;
+        phi[e] = ra;
+        dphi[e] = rb;
+        if (cphi) cphi[e] = (R)((double)ra - a);
+        if (cdphi) cdphi[e] = (R)((double)rb - b);
     }
 }
 
@@ -1088,6 +1114,40 @@ int sh_ensemble_gw_spectrum(sh_ensemble *E, int r, int zero_padding, int project
             "bins download");
         fck(cudaStreamSynchronize(s), "gw spectrum");
         if (ks_out) std::copy(E->gw.ks.begin(), E->gw.ks.end(), ks_out);
+    });
+}
+
+int sh_ensemble_add_bubbles(sh_ensemble *E, int r, int nb, const double *xyz,
+                            const double *profile, int nbins, double inv_dx, double Lcut) {
+    if (!E || E->family != SH_FAMILY_FOPT_GW || r < 0 || r >= E->nreal || nb < 0 ||
+        (nb > 0 && (!xyz || !profile)) || nbins < 2 || !(inv_dx > 0) || !(Lcut > 0))
+        return SH_ERR_ARG;
+    if (nb == 0) return SH_OK;
+    return fguard(E, [&] {
+        freq((long long)(Lcut * inv_dx) + 2 <= nbins,
+             "profile needs at least floor(Lcut * inv_dx) + 2 bins");
+        cudaStream_t s = est(E);
+        double *d = nullptr;
+        const size_t nx = 3 * (size_t)nb, np = 2 * (size_t)nbins;
+        fck(cudaMalloc(&d, (nx + np) * sizeof(double)), "bubble list");
+        std::unique_ptr<double, decltype(&cudaFree)> guard(d, &cudaFree);
+        fck(cudaMemcpyAsync(d, xyz, nx * sizeof(double), cudaMemcpyHostToDevice, s), "upload");
+        fck(cudaMemcpyAsync(d + nx, profile, np * sizeof(double), cudaMemcpyHostToDevice, s),
+            "upload");
+        sh::BubbleList bl{d, d + nx, nb, nbins, inv_dx, Lcut};
+        const long long n = cells_of(E, r);
+        /* internal arrays: Phi 0, dPhi 7 */
+        if (E->esize == 8)
+            add_bubbles_kernel<double><<<fgrid(n), 256, 0, s>>>(
+                E->d_desc, r, (double *)E->A[0], (double *)E->A[7], nullptr, nullptr, bl);
+        else
+            add_bubbles_kernel<float><<<fgrid(n), 256, 0, s>>>(
+                E->d_desc, r, (float *)E->A[0], (float *)E->A[7],
+                E->C.empty() ? nullptr : (float *)E->C[0],
+                E->C.empty() ? nullptr : (float *)E->C[7], bl);
+        E->launches++;
+        fck(cudaGetLastError(), "bubble launch");
+        fck(cudaStreamSynchronize(s), "bubbles");
     });
 }
 

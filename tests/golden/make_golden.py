@@ -11,7 +11,9 @@ reference itself (run in a checkout where the reference sources exist).
                          by the oracle's integrator sequences: evolutions,
                          Rhs evaluations, tag masks and truncation errors.
 
-Usage: python tests/golden/make_golden.py [REFERENCE_ROOT]
+  ref_bubbles.npz      - the reference's FOPT bubble injection (AddBubble).
+
+Usage: python tests/golden/make_golden.py [REFERENCE_ROOT] [--only=spectra,evolve,bubbles]
 """
 from __future__ import annotations
 
@@ -120,8 +122,49 @@ def evolve_fixtures():
     print("ref_avgdown_te")
 
 
+def bubble_profile(nbins, inv_dx, radius, width, amplitude, velocity=0.0):
+    """Tanh wall profile phi(r) = A/2 (1 - tanh((r - R)/w)) and its time
+    derivative for a wall moving outwards at speed v (rows 0 and 1)."""
+    r = np.arange(nbins) / inv_dx
+    x = (r - radius) / width
+    phi = 0.5 * amplitude * (1.0 - np.tanh(x))
+    dphi = velocity * 0.5 * amplitude / width / np.cosh(x) ** 2
+    return np.stack([phi, dphi])
+
+
+def bubble_fixture():
+    """The reference's AddBubble (FirstOrderPhaseTransition kernels_misc.h)
+    on a 16^3 FOPT + GW state: three bubbles, one across the periodic
+    corner, cut-off 5.3 with bins of 0.25."""
+    import ctypes as C
+    ref = Oracle(ref=True)
+    N, dx = 16, 0.5
+    st = np.stack([ic.gaussian_field(N, N * dx, 3.0, 90 + q) for q in range(14)]) * 0.1
+    xyz = np.array([[3.1, 4.7, 2.2], [7.9, 0.3, 7.6], [0.0, 5.5, 4.0]])
+    inv_dx, Lcut = 4.0, 5.3
+    nbins = int(Lcut * inv_dx) + 2
+    prof = bubble_profile(nbins, inv_dx, 2.5, 1.0, 1.2, velocity=0.4)
+    out = np.ascontiguousarray(st.copy())
+    f = ref.lib.ref_add_bubbles
+    f.restype = C.c_int
+    rc = f(N, 14, C.c_void_p(out.ctypes.data), 3, C.c_void_p(np.ascontiguousarray(xyz).ctypes.data),
+           C.c_void_p(np.ascontiguousarray(prof).ctypes.data), nbins, C.c_double(inv_dx),
+           C.c_double(Lcut), C.c_double(dx))
+    assert rc == 0
+    np.savez_compressed(os.path.join(HERE, "ref_bubbles.npz"), state_in=st, state_out=out,
+                        xyz=xyz, profile=prof, inv_dx=inv_dx, Lcut=Lcut, dx=dx)
+    print("ref_bubbles", float(np.abs(out - st).max()))
+
+
 if __name__ == "__main__":
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
+    only = [x for a in sys.argv[1:] if a.startswith("--only=")
+            for x in a.split("=", 1)[1].split(",")]
+    ref_root = args[0] if args else "/root/reference"
     subprocess.run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh"), ref_root], check=True)
-    spectra_fixtures(ref_root)
-    evolve_fixtures()
+    if not only or "spectra" in only:
+        spectra_fixtures(ref_root)
+    if not only or "evolve" in only:
+        evolve_fixtures()
+    if not only or "bubbles" in only:
+        bubble_fixture()

@@ -228,3 +228,29 @@ class OracleAmr:
         if self.h:
             self.lib.orc_amr_destroy(self.h)
             self.h = None
+
+
+def oracle_add_bubbles(state, xyz, profile, inv_dx, Lcut, dx, comp_phi=0, comp_dphi=1,
+                       ref=False):
+    """Bubble injection on a periodic canonical state (orc_add_bubbles, or
+    the reference's AddBubble through ref_add_bubbles with ref=True)."""
+    st = np.ascontiguousarray(np.array(state, dtype=np.float64))
+    ncomp, N = st.shape[0], st.shape[-1]
+    x = _f(xyz)
+    p = _f(profile)
+    if ref:
+        lib = C.CDLL(REF_SO)
+        f = lib.ref_add_bubbles
+        f.restype = C.c_int
+        rc = f(N, ncomp, _p(st), x.size // 3, _p(x), _p(p), p.size // 2, C.c_double(inv_dx),
+               C.c_double(Lcut), C.c_double(dx))
+    else:
+        build_oracle()
+        lib = C.CDLL(ORACLE_SO)
+        f = lib.orc_add_bubbles
+        f.restype = C.c_int
+        rc = f(N, ncomp, _p(st), comp_phi, comp_dphi, x.size // 3, _p(x), _p(p), p.size // 2,
+               C.c_double(inv_dx), C.c_double(Lcut), C.c_double(dx))
+    if rc != 0:
+        raise RuntimeError("add_bubbles")
+    return st
