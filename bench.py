@@ -60,6 +60,261 @@ AMR = dict(N0=256, L=64.0, project="AxionStringsLap2", params=[1.0, 0.0], nghost
            n_error_buf=2, regrid_dt=0.25, te_crit=1e-3, string_width_threshold=1.5)
 
 
+ENSEMBLE = dict(nreal=192, sizes=(32, 48, 64, 96, 128), lam=(0.5, 4.0), dx=0.25, eta0=0.1,
+                total_steps=200, seed=2024)
+
+
+def ensemble_spec():
+    """Realisation sizes and couplings of the batched-ensemble workload
+    (seeded): N uniform in the size set, lambda log-uniform."""
+    e = ENSEMBLE
+    rng = np.random.default_rng(e["seed"])
+    Ns = [int(x) for x in rng.choice(e["sizes"], e["nreal"])]
+    lam = np.exp(rng.uniform(np.log(e["lam"][0]), np.log(e["lam"][1]), e["nreal"]))
+    return Ns, lam
+
+
+def ensemble_states(Ns):
+    from sledgehamr_gb300 import ic
+    dx = ENSEMBLE["dx"]
+    return [ic.axion_string_ic(N, N * dx, kmax=1.0, seed=1000 + r) for r, N in enumerate(Ns)]
+
+
+def run_ensemble_leg(sh, ctx, stream, flush, steps, warmup):
+    """Batched ensemble: FP32+Kahan (graph steps, autotuned tiles) against
+    the FP64 plain path (one drop-in level per realisation, sh_level_advance)
+    and the FP64 batched ensemble on the same realisations.  Each leg runs
+    total_steps RKN4 steps; steps [warmup, warmup + steps) are timed with CUDA
+    events (L2 flushed between steps; the working set is larger than L2).
+    Errors: per-realisation string count and energy of the FP32 run against
+    the FP64 plain run at the end, and the relative L2 of the fields."""
+    import torch
+    e = ENSEMBLE
+    Ns, lam = ensemble_spec()
+    dx, dt = e["dx"], 0.25 * e["dx"]
+    total = max(e["total_steps"], warmup + steps)
+    states = ensemble_states(Ns)
+    cells = sum(N ** 3 for N in Ns)
+    params = np.array([[l, 0.0, 0.0, 0.0] for l in lam]).ravel()
+
+    def timed(step_fn):
+        for _ in range(warmup):
+            step_fn()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(steps)]
+        for a, b in ev:
+            flush.zero_()
+            a.record(stream)
+            step_fn()
+            b.record(stream)
+        torch.cuda.synchronize()
+        ms = float(sum(a.elapsed_time(b) for a, b in ev))
+        for _ in range(total - warmup - steps):
+            step_fn()
+        torch.cuda.synchronize()
+        return ms
+
+    out = {}
+    # FP32 + Kahan, batched
+    t0 = time.perf_counter()
+    E32 = sh.Ensemble(ctx, sh.FAMILY_AXION_LAP1, sh.PREC_FP32_KAHAN, Ns, [dx] * len(Ns), params)
+    for r, st in enumerate(states):
+        E32.write(r, st)
+    E32.set_time(e["eta0"])
+    nz = E32.tune(dt)
+    E32.set_graph(True)
+    l0 = E32.kernel_launches()
+    ms32 = timed(lambda: E32.step(dt, 1))
+    launches32 = E32.kernel_launches() - l0
+    e32 = E32.energy()
+    s32 = E32.string_count()
+    f32 = [E32.read(r) for r in range(len(Ns))]
+    info32 = E32.info()
+    E32.close()
+    wall32 = time.perf_counter() - t0
+    # FP64, batched
+    E64 = sh.Ensemble(ctx, sh.FAMILY_AXION_LAP1, sh.PREC_FP64, Ns, [dx] * len(Ns), params)
+    for r, st in enumerate(states):
+        E64.write(r, st)
+    E64.set_time(e["eta0"])
+    E64.tune(dt)
+    E64.set_graph(True)
+    ms64b = timed(lambda: E64.step(dt, 1))
+    E64.close()
+    # FP64 plain: one drop-in level per realisation
+    levels = []
+    for r, (N, st) in enumerate(zip(Ns, states)):
+        lv = sh.Level.periodic(ctx, "AxionStringsLap1", N, 1)
+        lv.write(st)
+        lv.set_time(e["eta0"])
+        levels.append(lv)
+
+    def plain_step():
+        for r, lv in enumerate(levels):
+            lv.advance(sh.RKN4, dt, dx, params=[float(lam[r]), 0.0])
+
+    ms64 = timed(plain_step)
+    # reference values at the end from the plain FP64 run
+    E = sh.Ensemble(ctx, sh.FAMILY_AXION_LAP1, sh.PREC_FP64, Ns, [dx] * len(Ns), params)
+    f64 = []
+    for r, lv in enumerate(levels):
+        f = lv.read()
+        f64.append(f)
+        E.write(r, f)
+        lv.close()
+    E.set_time(e["eta0"] + total * dt)
+    e64 = E.energy()
+    s64 = E.string_count()
+    E.close()
+    rel_l2 = [float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(f32, f64)]
+    rel_e = np.abs(e32 - e64) / np.abs(e64)
+    big = s64 >= 100
+    rel_s = np.abs(s32 - s64)[big] / s64[big]
+    tot_s = abs(float(s32.sum() - s64.sum())) / float(s64.sum())
+    cu = cells * steps
+    out = {
+        "workload": f"{e['nreal']} axion-string realisations, N in {list(e['sizes'])} "
+                    f"(seeded), lambda log-uniform {list(e['lam'])}, 7-point Laplacian, RKN4, "
+                    f"dx {dx}, dt {dt}, eta0 {e['eta0']}, {total} steps",
+        "cells": cells, "timed_steps": steps,
+        "fp32_kahan_batched": {"value": cu / (ms32 / 1e3), "ms_per_step": ms32 / steps,
+                               "tile_nz": nz, "graph": True,
+                               "gpu_launches_per_step": launches32 / (warmup + steps),
+                               "device_bytes": info32["device_bytes"],
+                               "wall_s_incl_upload": wall32},
+        "fp64_batched": {"value": cu / (ms64b / 1e3), "ms_per_step": ms64b / steps},
+        "fp64_plain": {"value": cu / (ms64 / 1e3), "ms_per_step": ms64 / steps,
+                       "note": "one sh_level per realisation, sh_level_advance in turn"},
+        "speedup_fp32_batched_vs_fp64_plain": ms64 / ms32,
+        "error_vs_fp64": {
+            "at_step": total,
+            "string_count_total_rel": tot_s,
+            "string_count_rel_max": float(rel_s.max()) if rel_s.size else None,
+            "string_count_rel_median": float(np.median(rel_s)) if rel_s.size else None,
+            "realisations_with_100plus_string_cells": int(big.sum()),
+            "energy_rel_max": float(rel_e.max()),
+            "field_rel_l2_max": float(max(rel_l2)),
+            "field_rel_l2_median": float(np.median(rel_l2)),
+        },
+    }
+    return out
+
+
+FOPT = dict(N=384, dx=0.5, dt=0.1, delta=1.6, nbubbles=64, t_nuc=(0.0, 20.0), t_end=25.0,
+            radius=5.0, width=1.0, amplitude=1.0, inv_dx=4.0, seed=7, max_grid=128)
+
+
+def fopt_bubbles():
+    """Seeded bubble centres and nucleation times (sorted) and the tanh wall
+    profile phi = A/2 (1 - tanh((r - R)/w)), dphi = 0."""
+    f = FOPT
+    rng = np.random.default_rng(f["seed"])
+    L = f["N"] * f["dx"]
+    xyz = rng.uniform(0.0, L, size=(f["nbubbles"], 3))
+    tn = np.sort(rng.uniform(f["t_nuc"][0], f["t_nuc"][1], f["nbubbles"]))
+    Lcut = f["radius"] + 8.0 * f["width"]
+    nbins = int(Lcut * f["inv_dx"]) + 2
+    r = np.arange(nbins) / f["inv_dx"]
+    prof = np.stack([0.5 * f["amplitude"] * (1.0 - np.tanh((r - f["radius"]) / f["width"])),
+                     np.zeros(nbins)])
+    return xyz, tn, prof, Lcut
+
+
+def run_fopt_leg(sh, ctx, stream, flush, steps, warmup):
+    """First-order phase transition with GW tensor, 384^3 periodic, leapfrog,
+    64 bubbles injected at their nucleation times (at the first step whose
+    time has passed it, as FindBubbles does): FP32+Kahan ensemble path
+    against the FP64 plain path (drop-in level with the project's hooks).
+    Both run to t_end; steps [warmup, warmup + steps) are timed.  Errors at
+    t_end: fields, FP64 energy, GW spectrum (per bin and total)."""
+    import torch
+    f = FOPT
+    N, dx, dt = f["N"], f["dx"], f["dt"]
+    nsteps = int(round(f["t_end"] / dt))
+    xyz, tn, prof, Lcut = fopt_bubbles()
+    q = [-1.0, f["delta"], -1.0]
+    state0 = np.zeros((14, N, N, N))
+
+    def run(obj_step, inject, t_of):
+        nxt = 0
+        ev = []
+        for s in range(nsteps):
+            t = s * dt
+            due = []
+            while nxt < len(tn) and tn[nxt] <= t:
+                due.append(nxt)
+                nxt += 1
+            timed = warmup <= s < warmup + steps
+            if timed:
+                flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+            if due:
+                inject(xyz[due])
+            obj_step()
+            if timed:
+                b.record(stream)
+                ev.append((a, b))
+        torch.cuda.synchronize()
+        return float(sum(a.elapsed_time(b) for a, b in ev))
+
+    out = {}
+    # FP32 + Kahan (ensemble path, one realisation, graph steps)
+    E = sh.Ensemble(ctx, sh.FAMILY_FOPT_GW, sh.PREC_FP32_KAHAN, [N], [dx], [*q, 0.0])
+    E.write(0, state0)
+    E.set_time(0.0)
+    E.set_graph(True)
+    ms32 = run(lambda: E.step(dt, 1),
+               lambda c: E.add_bubbles(0, c, prof, f["inv_dx"], Lcut), None)
+    e32 = E.energy()[0]
+    gw32, ks = E.gw_spectrum(0, zero_padding=1, projection_type=2, unbinned=False)
+    f32 = E.read(0)
+    E.close()
+    # FP64 plain path
+    lv = sh.Level.periodic(ctx, "FirstOrderPhaseTransition", N, 2, max_grid=f["max_grid"],
+                           with_gw=True)
+    lv.write(state0)
+    lv.set_time(0.0)
+    params = [0.0, *q, 0.0, 0.0, 0.0]
+    ms64 = run(lambda: lv.advance(sh.LEAPFROG, dt, dx, params=params),
+               lambda c: lv.add_bubbles(c, prof, f["inv_dx"], Lcut, dx), None)
+    gw64, ks64 = lv.gw_spectrum(zero_padding=1, projection_type=2, unbinned=False)
+    f64 = lv.read()
+    lv.close()
+    E = sh.Ensemble(ctx, sh.FAMILY_FOPT_GW, sh.PREC_FP64, [N], [dx], [*q, 0.0])
+    E.write(0, f64)
+    E.set_time(nsteps * dt)
+    e64 = E.energy()[0]
+    E.close()
+    cu = N ** 3 * steps
+    sig = gw64 > 1e-6 * gw64.max()
+    rel_bins = np.abs(gw32 - gw64)[sig] / gw64[sig]
+    out = {
+        "workload": f"FOPT + GW tensor {N}^3 periodic, dx {dx}, dt {dt}, leapfrog, 4th-order "
+                    f"stencils, V = phi^2/2 - delta phi^3/3 + phi^4/4 (delta {f['delta']}), "
+                    f"{f['nbubbles']} tanh bubbles (R {f['radius']}, w {f['width']}, A "
+                    f"{f['amplitude']}) nucleated uniformly in t {list(f['t_nuc'])}, "
+                    f"{nsteps} steps to t {f['t_end']}",
+        "timed_steps": steps,
+        "fp32_kahan": {"value": cu / (ms32 / 1e3), "ms_per_step": ms32 / steps},
+        "fp64_plain": {"value": cu / (ms64 / 1e3), "ms_per_step": ms64 / steps,
+                       "note": f"drop-in level, boxes of {f['max_grid']}^3"},
+        "speedup_fp32_vs_fp64_plain": ms64 / ms32,
+        "error_vs_fp64": {
+            "at_t": nsteps * dt,
+            "phi_rel_l2": float(np.linalg.norm(f32[0] - f64[0]) / np.linalg.norm(f64[0])),
+            "u_rel_l2": float(np.linalg.norm(f32[2:8] - f64[2:8]) / np.linalg.norm(f64[2:8])),
+            "energy_rel": float(abs(e32 - e64) / abs(e64)),
+            "gw_total_rel": float(abs(gw32.sum() - gw64.sum()) / gw64.sum()),
+            "gw_bin_rel_max": float(rel_bins.max()) if rel_bins.size else None,
+            "gw_bin_rel_median": float(np.median(rel_bins)) if rel_bins.size else None,
+            "gw_bins_compared": int(sig.sum()),
+        },
+    }
+    return out
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -255,6 +510,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="amr", choices=["amr", "single"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--forms", default="ensemble",
+                    help="comma list of the chosen-form legs reported beside the headline "
+                         "(ensemble, fopt; empty for none)")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 91 if args.workload == "amr" else 20
@@ -347,6 +605,7 @@ def main():
         amr_info = sim.info()
         levels = [{"level": l, "boxes": sim.level(l).nbox, "cells": sim.level(l).nvalid}
                   for l in range(amr_info["finest"] + 1)]
+        amr_timers = {k: round(v[0], 4) for k, v in sim.timers().items()}
         sim.close()
 
     # e2e: the whole job through the public API with pinned host buffers
@@ -386,6 +645,14 @@ def main():
         h2d = d2h = state.size * 8 * e2e_steps
         lv.close()
 
+    forms = {}
+    legs = [f for f in args.forms.split(",") if f]
+    if "ensemble" in legs:
+        forms["batched_ensemble"] = run_ensemble_leg(sh, ctx, stream, flush, steps=20,
+                                                     warmup=args.warmup)
+    if "fopt" in legs:
+        forms["fopt_precision"] = run_fopt_leg(sh, ctx, stream, flush, steps=20,
+                                               warmup=args.warmup)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args.workload)
@@ -411,7 +678,9 @@ def main():
         }
         if amr_info:
             line["amr"] = {"finest": amr_info["finest"], "nregrids": amr_info["nregrids"],
-                           "levels_at_end": levels}
+                           "levels_at_end": levels, "host_timers_s": amr_timers}
+        if forms:
+            line["forms"] = forms
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)

@@ -411,6 +411,19 @@ SH_API int sh_ensemble_tune(sh_ensemble *e, int tile_nz, double dt, int *chosen)
  * realisation r (FOPT_GW; arguments as sh_gw_spectrum). */
 SH_API int sh_ensemble_energy(sh_ensemble *e, double *energy);
 SH_API int sh_ensemble_string_count(sh_ensemble *e, long long *counts);
+/* Pools: an ensemble with room for capacity_cells cells per array
+ * (0: 80% of the free device memory) whose members are admitted and
+ * released one by one; a member has its own N, dx, params and step dt
+ * (FOPT_GW; sh_ensemble_step with dt = 0 advances every member by its own
+ * dt).  Admission fails with SH_ERR_NOMEM while no free extent holds N^3
+ * cells.  Slot numbers of released members are reused. */
+SH_API int sh_ensemble_create_pool(sh_ctx *ctx, int family, int precision,
+                                   long long capacity_cells, sh_ensemble **out);
+SH_API int sh_ensemble_admit(sh_ensemble *e, int N, double dx, const double *params, double dt,
+                             int *slot);
+SH_API int sh_ensemble_release(sh_ensemble *e, int slot);
+SH_API int sh_ensemble_pool_info(const sh_ensemble *e, long long *capacity,
+                                 long long *free_cells, long long *largest_free, int *members);
 /* Bubble injection into realisation r of an FOPT_GW ensemble, as
  * sh_level_add_bubbles (realisation side L = N dx). */
 SH_API int sh_ensemble_add_bubbles(sh_ensemble *e, int r, int nb, const double *xyz,
@@ -419,6 +432,43 @@ SH_API int sh_ensemble_add_bubbles(sh_ensemble *e, int r, int nb, const double *
 SH_API int sh_ensemble_gw_spectrum(sh_ensemble *e, int r, int zero_padding, int projection_type,
                                    int unbinned, double *bins_out, long long *ks_out,
                                    int max_bins, int *nbins);
+
+/* ------------------------------------------------------------------------ */
+/* Serving: a request loop over one FP32+Kahan (or FP64) pool of
+ * FirstOrderPhaseTransition + GW runs (no counterpart in the reference).
+ * A request is a periodic N^3 run from a zero state with bubbles injected
+ * at t = 0 (as sh_level_add_bubbles), stepped by the leapfrog with step dt
+ * until t_end, then its GW spectrum (as sh_gw_spectrum).  sh_server_step
+ * admits queued requests while device memory is free (a request that does
+ * not fit lets later ones pass until the oldest has waited 64 iterations),
+ * advances all admitted runs by one step in shared launches, and finishes
+ * the runs that reached t_end.  Times (seconds since the server's creation,
+ * host clock): submitted, admitted, spectrum ready. */
+typedef struct sh_request {
+    int N;
+    double dx, dt, t_end;
+    double params[4];     /* q2 q3 q4 0 */
+    int nbubbles;
+    const double *xyz;    /* 3 per bubble (copied at submission) */
+    const double *profile; /* 2 x nbins (copied) */
+    int nbins;
+    double inv_dx, Lcut;
+    int zero_padding, projection_type, unbinned;
+} sh_request;
+typedef struct sh_server sh_server;
+SH_API int sh_server_create(sh_ctx *ctx, int precision, long long capacity_cells,
+                            sh_server **out);
+SH_API int sh_server_destroy(sh_server *s);
+SH_API const char *sh_server_last_error(const sh_server *s);
+SH_API int sh_server_submit(sh_server *s, const sh_request *r, long long *id);
+SH_API int sh_server_step(sh_server *s, int *running, int *queued, int *completed);
+/* state: 0 queued, 1 running, 2 done, 3 failed; times[3] as above. */
+SH_API int sh_server_status(const sh_server *s, long long id, int *state, double *times);
+SH_API int sh_server_result(const sh_server *s, long long id, double *bins, long long *ks,
+                            int cap, int *nbins);
+SH_API int sh_server_info(const sh_server *s, int *running, int *queued,
+                          long long *cell_updates, long long *iterations,
+                          long long *free_cells);
 
 #ifdef __cplusplus
 }

@@ -18,7 +18,7 @@ from typing import Sequence
 import numpy as np
 
 from . import _lib
-from ._lib import SH_NEW, SH_OLD, SH_ADVANCE_NO_SWAP, ShAmrConfig, ShBox
+from ._lib import SH_NEW, SH_OLD, SH_ADVANCE_NO_SWAP, ShAmrConfig, ShBox, ShRequest
 
 # integrator.type (source/integrators/integrator.h:12-23)
 LSSSPRK3 = 10
@@ -515,6 +515,46 @@ class Ensemble:
     def kernel_launches(self) -> int:
         return int(self.ctx.lib.sh_ensemble_kernel_launches(self.h))
 
+    @classmethod
+    def pool(cls, ctx: Context, family: int, precision: int, capacity_cells: int = 0):
+        """An empty pool (sh_ensemble_create_pool); members via admit()."""
+        self = cls.__new__(cls)
+        self.ctx = ctx
+        self.family = family
+        self.N = []
+        self.ncomp = _FAMILY_NCOMP.get(family, 0)
+        h = C.c_void_p()
+        rc = ctx.lib.sh_ensemble_create_pool(ctx.h, family, precision, int(capacity_cells),
+                                             C.byref(h))
+        if rc != 0:
+            raise ShError(rc, "sh_ensemble_create_pool failed")
+        self.h = h
+        return self
+
+    def admit(self, N: int, dx: float, params=(0, 0, 0, 0), dt: float = 0.0):
+        """A new member (zero state); None when the pool has no room."""
+        p = _f64(list(params) + [0.0] * (4 - len(params)))
+        slot = C.c_int()
+        rc = self.ctx.lib.sh_ensemble_admit(self.h, int(N), float(dx), _ptr(p), float(dt),
+                                            C.byref(slot))
+        if rc == _lib.SH_ERR_NOMEM:
+            return None
+        self.check(rc, "admit")
+        while len(self.N) <= slot.value:
+            self.N.append(0)
+        self.N[slot.value] = int(N)
+        return slot.value
+
+    def release(self, slot: int):
+        self.check(self.ctx.lib.sh_ensemble_release(self.h, int(slot)), "release")
+
+    def pool_info(self) -> dict:
+        cap, fr, big, m = C.c_longlong(), C.c_longlong(), C.c_longlong(), C.c_int()
+        self.check(self.ctx.lib.sh_ensemble_pool_info(self.h, C.byref(cap), C.byref(fr),
+                                                      C.byref(big), C.byref(m)), "pool_info")
+        return {"capacity": cap.value, "free": fr.value, "largest_free": big.value,
+                "members": m.value}
+
     def set_time(self, t: float):
         self.check(self.ctx.lib.sh_ensemble_set_time(self.h, float(t)), "set_time")
 
@@ -546,12 +586,12 @@ class Ensemble:
         return ch.value
 
     def energy(self) -> np.ndarray:
-        e = np.empty(len(self.N), dtype=np.float64)
+        e = np.empty(max(len(self.N), 1), dtype=np.float64)
         self.check(self.ctx.lib.sh_ensemble_energy(self.h, _ptr(e)), "energy")
         return e
 
     def string_count(self) -> np.ndarray:
-        c = np.empty(len(self.N), dtype=np.int64)
+        c = np.empty(max(len(self.N), 1), dtype=np.int64)
         self.check(self.ctx.lib.sh_ensemble_string_count(self.h, _ptr(c)), "string_count")
         return c
 
@@ -592,3 +632,82 @@ class Ensemble:
 
     def __exit__(self, *exc):
         self.close()
+
+
+class Server:
+    """Serving loop over a pool of FOPT + GW runs (sh_server)."""
+
+    def __init__(self, ctx: Context, precision: int = PREC_FP32_KAHAN, capacity_cells: int = 0):
+        self.ctx = ctx
+        h = C.c_void_p()
+        rc = ctx.lib.sh_server_create(ctx.h, precision, int(capacity_cells), C.byref(h))
+        if rc != 0:
+            raise ShError(rc, "sh_server_create failed")
+        self.h = h
+        self._keep = {}
+
+    def check(self, rc: int, what: str):
+        if rc != 0:
+            msg = self.ctx.lib.sh_server_last_error(self.h) or b""
+            raise ShError(rc, f"{what}: {msg.decode(errors='replace')}")
+
+    def submit(self, N: int, dx: float, dt: float, t_end: float, params, centres=None,
+               profile=None, inv_dx: float = 1.0, Lcut: float = 0.0, zero_padding: int = 1,
+               projection_type: int = 2, unbinned: bool = False) -> int:
+        r = ShRequest()
+        r.N, r.dx, r.dt, r.t_end = int(N), float(dx), float(dt), float(t_end)
+        for q, v in enumerate(list(params)[:4]):
+            r.params[q] = float(v)
+        xyz = _f64(centres) if centres is not None else None
+        prof = _f64(profile) if profile is not None else None
+        r.nbubbles = 0 if xyz is None else xyz.size // 3
+        r.xyz = None if xyz is None else xyz.ctypes.data
+        r.profile = None if prof is None else prof.ctypes.data
+        r.nbins = 0 if prof is None else prof.size // 2
+        r.inv_dx, r.Lcut = float(inv_dx), float(Lcut)
+        r.zero_padding, r.projection_type, r.unbinned = int(zero_padding), int(projection_type), \
+            int(unbinned)
+        rid = C.c_longlong()
+        self.check(self.ctx.lib.sh_server_submit(self.h, C.byref(r), C.byref(rid)), "submit")
+        return rid.value
+
+    def step(self):
+        a, q, c = C.c_int(), C.c_int(), C.c_int()
+        self.check(self.ctx.lib.sh_server_step(self.h, C.byref(a), C.byref(q), C.byref(c)), "step")
+        return a.value, q.value, c.value
+
+    def status(self, rid: int):
+        st = C.c_int()
+        t = np.zeros(3)
+        self.check(self.ctx.lib.sh_server_status(self.h, int(rid), C.byref(st), _ptr(t)),
+                   "status")
+        return st.value, t
+
+    def result(self, rid: int):
+        nb = C.c_int()
+        self.check(self.ctx.lib.sh_server_result(self.h, int(rid), None, None, 0, C.byref(nb)),
+                   "result")
+        bins = np.empty(nb.value)
+        ks = np.empty(nb.value, dtype=np.int64)
+        self.check(self.ctx.lib.sh_server_result(self.h, int(rid), _ptr(bins), _ptr(ks),
+                                                 nb.value, C.byref(nb)), "result")
+        return bins, ks
+
+    def info(self) -> dict:
+        a, q = C.c_int(), C.c_int()
+        cu, it, fr = C.c_longlong(), C.c_longlong(), C.c_longlong()
+        self.check(self.ctx.lib.sh_server_info(self.h, C.byref(a), C.byref(q), C.byref(cu),
+                                               C.byref(it), C.byref(fr)), "info")
+        return {"running": a.value, "queued": q.value, "cell_updates": cu.value,
+                "iterations": it.value, "free_cells": fr.value}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.sh_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -57,6 +57,14 @@ class ShAmrConfig(C.Structure):
                 ("grid_eff", C.c_double)]
 
 
+class ShRequest(C.Structure):
+    _fields_ = [("N", C.c_int), ("dx", C.c_double), ("dt", C.c_double), ("t_end", C.c_double),
+                ("params", C.c_double * 4), ("nbubbles", C.c_int), ("xyz", C.c_void_p),
+                ("profile", C.c_void_p), ("nbins", C.c_int), ("inv_dx", C.c_double),
+                ("Lcut", C.c_double), ("zero_padding", C.c_int), ("projection_type", C.c_int),
+                ("unbinned", C.c_int)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "sh_ctx_create": (C.c_int, [C.c_int, C.POINTER(vp)]),
@@ -94,6 +102,18 @@ SIGNATURES = {
     "sh_ensemble_tune": (C.c_int, [vp, C.c_int, C.c_double, ip]),
     "sh_ensemble_energy": (C.c_int, [vp, vp]),
     "sh_ensemble_string_count": (C.c_int, [vp, vp]),
+    "sh_ensemble_create_pool": (C.c_int, [vp, C.c_int, C.c_int, C.c_longlong, C.POINTER(vp)]),
+    "sh_ensemble_admit": (C.c_int, [vp, C.c_int, C.c_double, vp, C.c_double, ip]),
+    "sh_ensemble_release": (C.c_int, [vp, C.c_int]),
+    "sh_ensemble_pool_info": (C.c_int, [vp, llp, llp, llp, ip]),
+    "sh_server_create": (C.c_int, [vp, C.c_int, C.c_longlong, C.POINTER(vp)]),
+    "sh_server_destroy": (C.c_int, [vp]),
+    "sh_server_last_error": (C.c_char_p, [vp]),
+    "sh_server_submit": (C.c_int, [vp, C.POINTER(ShRequest), llp]),
+    "sh_server_step": (C.c_int, [vp, ip, ip, ip]),
+    "sh_server_status": (C.c_int, [vp, C.c_longlong, ip, vp]),
+    "sh_server_result": (C.c_int, [vp, C.c_longlong, vp, vp, C.c_int, ip]),
+    "sh_server_info": (C.c_int, [vp, ip, ip, llp, llp, llp]),
     "sh_ensemble_add_bubbles": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, C.c_int, C.c_double,
                                           C.c_double]),
     "sh_level_add_bubbles": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp,

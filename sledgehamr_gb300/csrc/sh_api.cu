@@ -178,6 +178,34 @@ void *dmalloc(size_t bytes, const char *what) {
     return p;
 }
 
+/* Stream-ordered allocations from the device's memory pool, for level data
+ * that regrids create and destroy often: the pool keeps freed memory for
+ * reuse (release threshold set at context creation), and neither the
+ * allocation nor the free waits for the device. */
+void *dmalloc_async(sh_ctx *ctx, size_t bytes, const char *what) {
+    void *p = nullptr;
+    if (bytes == 0) return nullptr;
+    cudaError_t e = cudaMallocAsync(&p, bytes, ctx->stream);
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        throw ShError(SH_ERR_NOMEM, std::string("device allocation failed: ") + what);
+    }
+    ck(e, what);
+    return p;
+}
+
+inline void dfree_async(sh_ctx *ctx, void *p) {
+    if (p) cudaFreeAsync(p, ctx->stream);
+}
+
+template <class T>
+T *upload_async(sh_ctx *ctx, const T *h, size_t n, const char *what) {
+    if (n == 0) return nullptr;
+    T *d = (T *)dmalloc_async(ctx, n * sizeof(T), what);
+    ck(cudaMemcpyAsync(d, h, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream), what);
+    return d;
+}
+
 void *ctx_scratch(sh_ctx *ctx, size_t bytes) {
     if (bytes > ctx->scratch_bytes) {
         if (ctx->scratch) {
@@ -594,7 +622,7 @@ bool box_intersect(const int alo[3], const int ahi[3], const int blo[3], const i
 
 /* Owner map of a level: blocks of `res` cells, res = the largest size that
  * divides the domain and every box bound (boxes are unions of blocks). */
-void build_owner_map(sh_level *L) {
+void build_owner_map(sh_ctx *ctx, sh_level *L) {
     auto gcd = [](int a, int b) {
         a = a < 0 ? -a : a;
         b = b < 0 ? -b : b;
@@ -626,10 +654,7 @@ void build_owner_map(sh_level *L) {
                     o = (int)q;
                 }
     }
-    L->d_owner = (int *)dmalloc(L->owner.size() * sizeof(int), "owner map");
-    ck(cudaMemcpy(L->d_owner, L->owner.data(), L->owner.size() * sizeof(int),
-                  cudaMemcpyHostToDevice),
-       "owner map upload");
+    L->d_owner = upload_async(ctx, L->owner.data(), L->owner.size(), "owner map");
 }
 
 OwnerMapDev owner_map_dev(const sh_level *L) {
@@ -679,64 +704,77 @@ FillPlan build_fill_plan(const sh_level *D, const sh_level *S, const sh_level *C
     const sh_level *G = S ? S : D;
     const int R = G->owner_res;
     const int g = D->nghost;
+    /* per destination box: the blocks of its ghost-grown region, each with a
+     * source (owner box and periodic shift), "interpolate" or "skip", then
+     * runs of equal source along x merged along y and z */
+    struct Blk {
+        int kind; /* 0 skip, 1 copy, 2 interpolate */
+        int own;
+        int sh[3];
+        int lo[3], hi[3];
+    };
+    std::vector<Blk> blk;
+    struct Run {
+        int kind, own, sh[3], lo[3], hi[3];
+    };
+    std::vector<Run> runs, merged;
     for (size_t b = 0; b < D->boxes.size(); ++b) {
-        int glo[3], ghi[3], blo[3], bhi[3];
+        int glo[3], ghi[3], blo[3], nbk[3];
         for (int d = 0; d < 3; ++d) {
             glo[d] = D->boxes[b].lo[d] - g;
             ghi[d] = D->boxes[b].hi[d] + g;
             blo[d] = floordiv(glo[d] - D->dlo[d], R);
-            bhi[d] = floordiv(ghi[d] - D->dlo[d], R);
+            nbk[d] = floordiv(ghi[d] - D->dlo[d], R) - blo[d] + 1;
         }
-        for (int bz = blo[2]; bz <= bhi[2]; ++bz)
-            for (int by = blo[1]; by <= bhi[1]; ++by)
-                for (int bx = blo[0]; bx <= bhi[0]; ++bx) {
-                    const int bb[3] = {bx, by, bz};
-                    int lo[3], hi[3], sh[3], wb[3];
+        blk.assign((size_t)nbk[0] * nbk[1] * nbk[2], Blk{});
+        for (int z = 0; z < nbk[2]; ++z)
+            for (int y = 0; y < nbk[1]; ++y)
+                for (int x = 0; x < nbk[0]; ++x) {
+                    const int bb[3] = {blo[0] + x, blo[1] + y, blo[2] + z};
+                    Blk &k = blk[((size_t)z * nbk[1] + y) * nbk[0] + x];
+                    int wb[3];
                     bool inside_valid = true;
                     for (int d = 0; d < 3; ++d) {
-                        lo[d] = std::max(glo[d], D->dlo[d] + bb[d] * R);
-                        hi[d] = std::min(ghi[d], D->dlo[d] + (bb[d] + 1) * R - 1);
+                        k.lo[d] = std::max(glo[d], D->dlo[d] + bb[d] * R);
+                        k.hi[d] = std::min(ghi[d], D->dlo[d] + (bb[d] + 1) * R - 1);
                         const int nbd = G->owner_nb[d];
                         wb[d] = ((bb[d] % nbd) + nbd) % nbd;
-                        sh[d] = (bb[d] - wb[d]) * R; /* periodic image offset */
-                        if (lo[d] < D->boxes[b].lo[d] || hi[d] > D->boxes[b].hi[d])
+                        k.sh[d] = (bb[d] - wb[d]) * R; /* periodic image offset */
+                        if (k.lo[d] < D->boxes[b].lo[d] || k.hi[d] > D->boxes[b].hi[d])
                             inside_valid = false;
                     }
+                    k.kind = 0;
+                    k.own = -1;
                     if (ghosts_only && inside_valid) continue;
                     const int own = S ? S->owner[((size_t)wb[2] * G->owner_nb[1] + wb[1]) *
                                                      G->owner_nb[0] +
                                                  wb[0]]
                                       : -1;
-                    const long long ncell = (long long)(hi[0] - lo[0] + 1) *
-                                            (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
                     if (own >= 0) {
-                        if (S == D && own == (int)b && sh[0] == 0 && sh[1] == 0 && sh[2] == 0)
+                        if (S == D && own == (int)b && k.sh[0] == 0 && k.sh[1] == 0 &&
+                            k.sh[2] == 0)
                             continue;
-                        GhostCopyDev r;
-                        r.dbox = (int)b;
-                        r.sbox = own;
-                        for (int d = 0; d < 3; ++d) {
-                            r.lo[d] = lo[d];
-                            r.hi[d] = hi[d];
-                            r.shift[d] = sh[d];
-                        }
-                        r.first = P.rect_cells;
-                        P.rect_cells += ncell;
-                        P.rects.push_back(r);
+                        k.kind = 1;
+                        k.own = own;
                         continue;
                     }
                     if (!C) continue; /* nothing to fill from: left as is */
-                    /* parents of the region must lie on the coarse level */
-                    for (int pz = floordiv(lo[2], 2); pz <= floordiv(hi[2], 2); ++pz)
-                        for (int py = floordiv(lo[1], 2); py <= floordiv(hi[1], 2); ++py)
-                            for (int px = floordiv(lo[0], 2); px <= floordiv(hi[0], 2); ++px) {
+                    /* the parents of the region must lie on the coarse level
+                     * (checked per coarse block) */
+                    const int Rc = C->owner_res;
+                    int pb0[3], pb1[3];
+                    for (int d = 0; d < 3; ++d) {
+                        pb0[d] = floordiv(floordiv(k.lo[d], 2) - C->dlo[d], Rc);
+                        pb1[d] = floordiv(floordiv(k.hi[d], 2) - C->dlo[d], Rc);
+                    }
+                    for (int pz = pb0[2]; pz <= pb1[2]; ++pz)
+                        for (int py = pb0[1]; py <= pb1[1]; ++py)
+                            for (int px = pb0[0]; px <= pb1[0]; ++px) {
                                 const int p3[3] = {px, py, pz};
                                 int cb[3];
                                 for (int d = 0; d < 3; ++d) {
-                                    const int cext = C->dhi[d] - C->dlo[d] + 1;
-                                    int w = (p3[d] - C->dlo[d]) % cext;
-                                    if (w < 0) w += cext;
-                                    cb[d] = w / C->owner_res;
+                                    const int n = C->owner_nb[d];
+                                    cb[d] = ((p3[d] % n) + n) % n;
                                 }
                                 if (C->owner[((size_t)cb[2] * C->owner_nb[1] + cb[1]) *
                                                  C->owner_nb[0] +
@@ -745,74 +783,87 @@ FillPlan build_fill_plan(const sh_level *D, const sh_level *S, const sh_level *C
                                                   "coarse level does not cover the cells to "
                                                   "interpolate (levels are not properly nested)");
                             }
-                    CfRect cr;
-                    cr.dbox = (int)b;
-                    for (int d = 0; d < 3; ++d) {
-                        cr.lo[d] = lo[d];
-                        cr.hi[d] = hi[d];
-                    }
-                    cr.first = P.cf_cells;
-                    P.cf_cells += ncell;
-                    P.cf.push_back(cr);
+                    k.kind = 2;
                 }
+        /* x-runs of equal kind / source */
+        runs.clear();
+        for (int z = 0; z < nbk[2]; ++z)
+            for (int y = 0; y < nbk[1]; ++y) {
+                int x = 0;
+                while (x < nbk[0]) {
+                    const Blk &k = blk[((size_t)z * nbk[1] + y) * nbk[0] + x];
+                    if (k.kind == 0) {
+                        ++x;
+                        continue;
+                    }
+                    int x1 = x;
+                    while (x1 + 1 < nbk[0]) {
+                        const Blk &n = blk[((size_t)z * nbk[1] + y) * nbk[0] + x1 + 1];
+                        if (n.kind != k.kind || n.own != k.own || n.sh[0] != k.sh[0] ||
+                            n.sh[1] != k.sh[1] || n.sh[2] != k.sh[2])
+                            break;
+                        ++x1;
+                    }
+                    const Blk &e = blk[((size_t)z * nbk[1] + y) * nbk[0] + x1];
+                    Run r{k.kind, k.own, {k.sh[0], k.sh[1], k.sh[2]},
+                          {k.lo[0], k.lo[1], k.lo[2]}, {e.hi[0], k.hi[1], k.hi[2]}};
+                    runs.push_back(r);
+                    x = x1 + 1;
+                }
+            }
+        /* merge along y, then along z (same kind, source and x extent) */
+        for (int d = 1; d <= 2; ++d) {
+            merged.clear();
+            for (const Run &r : runs) {
+                bool done = false;
+                for (size_t q = merged.size(); q-- > 0;) {
+                    Run &m = merged[q];
+                    /* runs are ordered by z: along y only the same plane */
+                    if (d == 1 && m.lo[2] != r.lo[2]) break;
+                    bool same = m.kind == r.kind && m.own == r.own && m.sh[0] == r.sh[0] &&
+                                m.sh[1] == r.sh[1] && m.sh[2] == r.sh[2] &&
+                                m.hi[d] + 1 == r.lo[d];
+                    for (int e = 0; e < 3 && same; ++e)
+                        if (e != d) same = m.lo[e] == r.lo[e] && m.hi[e] == r.hi[e];
+                    if (same) {
+                        m.hi[d] = r.hi[d];
+                        done = true;
+                        break;
+                    }
+                }
+                if (!done) merged.push_back(r);
+            }
+            runs.swap(merged);
+        }
+        for (const Run &r : runs) {
+            const long long ncell = (long long)(r.hi[0] - r.lo[0] + 1) *
+                                    (r.hi[1] - r.lo[1] + 1) * (r.hi[2] - r.lo[2] + 1);
+            if (r.kind == 1) {
+                GhostCopyDev c;
+                c.dbox = (int)b;
+                c.sbox = r.own;
+                for (int d = 0; d < 3; ++d) {
+                    c.lo[d] = r.lo[d];
+                    c.hi[d] = r.hi[d];
+                    c.shift[d] = r.sh[d];
+                }
+                c.first = P.rect_cells;
+                P.rect_cells += ncell;
+                P.rects.push_back(c);
+            } else {
+                CfRect c;
+                c.dbox = (int)b;
+                for (int d = 0; d < 3; ++d) {
+                    c.lo[d] = r.lo[d];
+                    c.hi[d] = r.hi[d];
+                }
+                c.first = P.cf_cells;
+                P.cf_cells += ncell;
+                P.cf.push_back(c);
+            }
+        }
     }
     return P;
-}
-
-/* Adjacent rectangles of one destination box with the same source box and
- * periodic shift merged along x, then y, then z (the cells and their
- * values are unchanged; fewer, larger work items). */
-void merge_copy_rects(std::vector<GhostCopyDev> &v) {
-    for (int d = 0; d < 3; ++d) {
-        const int e = (d + 1) % 3, f = (d + 2) % 3;
-        auto key = [&](const GhostCopyDev &r) {
-            return std::make_tuple(r.dbox, r.sbox, r.shift[0], r.shift[1], r.shift[2], r.lo[e],
-                                   r.hi[e], r.lo[f], r.hi[f], r.lo[d]);
-        };
-        std::sort(v.begin(), v.end(),
-                  [&](const GhostCopyDev &a, const GhostCopyDev &b) { return key(a) < key(b); });
-        std::vector<GhostCopyDev> out;
-        out.reserve(v.size());
-        for (const GhostCopyDev &r : v) {
-            if (!out.empty()) {
-                GhostCopyDev &p = out.back();
-                if (p.dbox == r.dbox && p.sbox == r.sbox && p.shift[0] == r.shift[0] &&
-                    p.shift[1] == r.shift[1] && p.shift[2] == r.shift[2] && p.lo[e] == r.lo[e] &&
-                    p.hi[e] == r.hi[e] && p.lo[f] == r.lo[f] && p.hi[f] == r.hi[f] &&
-                    p.hi[d] + 1 == r.lo[d]) {
-                    p.hi[d] = r.hi[d];
-                    continue;
-                }
-            }
-            out.push_back(r);
-        }
-        v.swap(out);
-    }
-}
-
-void merge_cf_rects(std::vector<CfRect> &v) {
-    for (int d = 0; d < 3; ++d) {
-        const int e = (d + 1) % 3, f = (d + 2) % 3;
-        auto key = [&](const CfRect &r) {
-            return std::make_tuple(r.dbox, r.lo[e], r.hi[e], r.lo[f], r.hi[f], r.lo[d]);
-        };
-        std::sort(v.begin(), v.end(),
-                  [&](const CfRect &a, const CfRect &b) { return key(a) < key(b); });
-        std::vector<CfRect> out;
-        out.reserve(v.size());
-        for (const CfRect &r : v) {
-            if (!out.empty()) {
-                CfRect &p = out.back();
-                if (p.dbox == r.dbox && p.lo[e] == r.lo[e] && p.hi[e] == r.hi[e] &&
-                    p.lo[f] == r.lo[f] && p.hi[f] == r.hi[f] && p.hi[d] + 1 == r.lo[d]) {
-                    p.hi[d] = r.hi[d];
-                    continue;
-                }
-            }
-            out.push_back(r);
-        }
-        v.swap(out);
-    }
 }
 
 /* Splits the rectangle [lo, hi] into pieces of at most kItemCells cells
@@ -893,20 +944,16 @@ std::vector<CfItem> cf_items(const std::vector<CfRect> &rects, const sh_level *D
 }
 
 template <class T>
-T *upload_items(const std::vector<T> &v, const char *what) {
-    if (v.empty()) return nullptr;
-    T *d = (T *)dmalloc(v.size() * sizeof(T), what);
-    ck(cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), what);
-    return d;
+T *upload_items(sh_ctx *ctx, const std::vector<T> &v, const char *what) {
+    return upload_async(ctx, v.data(), v.size(), what);
 }
 
-void build_ghost_plan(sh_level *L) {
+void build_ghost_plan(sh_ctx *ctx, sh_level *L) {
     FillPlan P = build_fill_plan(L, L, nullptr, true);
-    merge_copy_rects(P.rects);
     const std::vector<CopyItem> items = copy_items(P.rects, L, L);
     L->nghost_items = (int)items.size();
     L->nghost_cells = P.rect_cells;
-    L->d_ghost = upload_items(items, "ghost plan");
+    L->d_ghost = upload_items(ctx, items, "ghost plan");
 }
 
 /* GetLevelData time selection (level_synchronizer.cpp:613-632) for data of
@@ -927,22 +974,23 @@ void coarse_time_weights(const sh_level *C, double t, int &mode, double &alpha, 
     }
 }
 
-void level_free(sh_level *L) {
-    cudaFree(L->d_boxes);
-    cudaFree(L->d_tiles);
-    cudaFree(L->d_ghost);
-    cudaFree(L->d_vbase);
-    cudaFree(L->d_cf);
-    cudaFree(L->d_owner);
-    for (int q = 0; q < 3; ++q) cudaFree(L->buf[q]);
-    cudaFree(L->kbuf);
+void level_free(sh_ctx *ctx, sh_level *L) {
+    dfree_async(ctx, L->d_boxes);
+    dfree_async(ctx, L->d_tiles);
+    dfree_async(ctx, L->d_ghost);
+    dfree_async(ctx, L->d_vbase);
+    dfree_async(ctx, L->d_cf);
+    dfree_async(ctx, L->d_owner);
+    for (int q = 0; q < 3; ++q) dfree_async(ctx, L->buf[q]);
+    dfree_async(ctx, L->kbuf);
 }
 
-void ensure_kbuf(sh_level *L, size_t elems, int count) {
+void ensure_kbuf(sh_ctx *ctx, sh_level *L, size_t elems, int count) {
     if (elems * count <= L->kbuf_elems * L->kbuf_count && elems <= L->kbuf_elems) return;
-    cudaFree(L->kbuf);
+    dfree_async(ctx, L->kbuf);
     L->kbuf = nullptr;
-    L->kbuf = (double *)dmalloc(elems * count * sizeof(double), "integrator K buffers");
+    L->kbuf = (double *)dmalloc_async(ctx, elems * count * sizeof(double),
+                                      "integrator K buffers");
     L->kbuf_elems = elems;
     L->kbuf_count = count;
 }
@@ -1057,7 +1105,7 @@ void integrate(sh_ctx *ctx, sh_level *L, int type, const double *tableau, int ns
         type == SH_INTEGRATOR_RKN_TABLEAU) {
         Tableau tb = rkn_tableau(type, tableau, nstages);
         const int S = (int)tb.b.size();
-        ensure_kbuf(L, (size_t)L->total_gvol * L->npairs, S);
+        ensure_kbuf(ctx, L, (size_t)L->total_gvol * L->npairs, S);
         double *kb[kMaxStages];
         for (int s = 0; s < S; ++s) kb[s] = L->kbuf + (size_t)s * L->total_gvol * L->npairs;
         int cur = SH_OLD; /* buffer holding Y_i */
@@ -1089,7 +1137,7 @@ void integrate(sh_ctx *ctx, sh_level *L, int type, const double *tableau, int ns
         }
         if (cur != SH_NEW) std::swap(L->buf[SH_NEW], L->buf[2]);
     } else if (type == SH_INTEGRATOR_LSSSPRK3) {
-        ensure_kbuf(L, kelems, 1);
+        ensure_kbuf(ctx, L, kelems, 1);
         StageArgs s = a;
         /* k1 = f(y0); u1 = y0 + dt k1 */
         s.state = L->buf[SH_OLD];
@@ -1122,7 +1170,7 @@ void integrate(sh_ctx *ctx, sh_level *L, int type, const double *tableau, int ns
         launch_stage(ctx, L, s, ko_order);
         fill_patch(ctx, L, L->buf[SH_NEW], t0 + dt);
     } else if (type == SH_INTEGRATOR_LEAPFROG) {
-        ensure_kbuf(L, (size_t)L->total_gvol * L->npairs, 1);
+        ensure_kbuf(ctx, L, (size_t)L->total_gvol * L->npairs, 1);
         StageArgs s = a;
         s.state = L->buf[SH_OLD];
         s.time = t0;
@@ -1212,7 +1260,6 @@ void average_down_impl(sh_ctx *ctx, const sh_level *F, const double *fine, const
         d, (int)plan.size(), ncells, F->d_boxes, C->d_boxes, F->ncomp, fine, crse, te);
     ctx->launches++;
     ck(cudaGetLastError(), "average-down launch");
-    ck(cudaStreamSynchronize(ctx->stream), "average-down");
 }
 
 } // namespace
@@ -1233,6 +1280,12 @@ int sh_ctx_create(int device, sh_ctx **out) {
         set_device(ctx);
         ck(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking), "stream create");
         ctx->stream = ctx->own_stream;
+        /* keep freed level memory in this process's pool for reuse */
+        cudaMemPool_t pool;
+        ck(cudaDeviceGetDefaultMemPool(&pool, device), "default memory pool");
+        uint64_t thr = UINT64_MAX;
+        ck(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr),
+           "memory pool threshold");
     });
     if (rc != SH_OK) {
         std::fprintf(stderr, "sh_ctx_create: %s\n", ctx->err.c_str());
@@ -1247,6 +1300,9 @@ int sh_ctx_destroy(sh_ctx *ctx) {
     if (!ctx) return SH_ERR_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) == cudaSuccess)
+        cudaMemPoolTrimTo(pool, 0);
     cudaFree(ctx->scratch);
     ctx->gw.release();
     for (const ProfRecord &r : ctx->prof) {
@@ -1394,29 +1450,19 @@ int sh_level_create(sh_ctx *ctx, int project, int with_gw, const int domain_lo[3
         L->total_gvol = base;
         L->nvalid = vb;
         L->ntiles = (int)tiles.size();
-        L->d_boxes = (BoxDev *)dmalloc(L->hboxes.size() * sizeof(BoxDev), "box table");
-        ck(cudaMemcpy(L->d_boxes, L->hboxes.data(), L->hboxes.size() * sizeof(BoxDev),
-                      cudaMemcpyHostToDevice),
-           "box table upload");
-        L->d_tiles = (TileDev *)dmalloc(tiles.size() * sizeof(TileDev), "tile table");
-        ck(cudaMemcpy(L->d_tiles, tiles.data(), tiles.size() * sizeof(TileDev),
-                      cudaMemcpyHostToDevice),
-           "tile table upload");
-        L->d_vbase = (long long *)dmalloc(L->vbase.size() * sizeof(long long), "box prefix");
-        ck(cudaMemcpy(L->d_vbase, L->vbase.data(), L->vbase.size() * sizeof(long long),
-                      cudaMemcpyHostToDevice),
-           "box prefix upload");
-        build_owner_map(L);
-        build_ghost_plan(L);
+        L->d_boxes = upload_async(ctx, L->hboxes.data(), L->hboxes.size(), "box table");
+        L->d_tiles = upload_async(ctx, tiles.data(), tiles.size(), "tile table");
+        L->d_vbase = upload_async(ctx, L->vbase.data(), L->vbase.size(), "box prefix");
+        build_owner_map(ctx, L);
+        build_ghost_plan(ctx, L);
         const size_t bytes = (size_t)L->total_gvol * L->ncomp * sizeof(double);
         for (int q = 0; q < 3; ++q) {
-            L->buf[q] = (double *)dmalloc(bytes, "level buffer");
+            L->buf[q] = (double *)dmalloc_async(ctx, bytes, "level buffer");
             ck(cudaMemsetAsync(L->buf[q], 0, bytes, ctx->stream), "level buffer clear");
         }
-        ck(cudaStreamSynchronize(ctx->stream), "level create");
     });
     if (rc != SH_OK) {
-        level_free(L);
+        level_free(ctx, L);
         delete L;
         return rc;
     }
@@ -1427,8 +1473,7 @@ int sh_level_create(sh_ctx *ctx, int project, int with_gw, const int domain_lo[3
 int sh_level_destroy(sh_ctx *ctx, sh_level *L) {
     if (!ctx || !L) return SH_ERR_ARG;
     cudaSetDevice(ctx->device);
-    cudaStreamSynchronize(ctx->stream);
-    level_free(L);
+    level_free(ctx, L); /* stream-ordered: after the work queued on the level */
     delete L;
     return SH_OK;
 }
@@ -1522,7 +1567,7 @@ int sh_level_set_coarse(sh_ctx *ctx, sh_level *fine, sh_level *coarse) {
     if (!ctx || !fine) return SH_ERR_ARG;
     return guarded(ctx, [&] {
         set_device(ctx);
-        cudaFree(fine->d_cf);
+        dfree_async(ctx, fine->d_cf);
         fine->d_cf = nullptr;
         fine->ncf = 0;
         fine->ncf_items = 0;
@@ -1530,9 +1575,8 @@ int sh_level_set_coarse(sh_ctx *ctx, sh_level *fine, sh_level *coarse) {
         if (!coarse) return;
         require(coarse != fine, "a level cannot be its own coarse level");
         FillPlan P = build_fill_plan(fine, fine, coarse, true);
-        merge_cf_rects(P.cf);
         const std::vector<CfItem> items = cf_items(P.cf, fine);
-        fine->d_cf = upload_items(items, "coarse-fine plan");
+        fine->d_cf = upload_items(ctx, items, "coarse-fine plan");
         fine->ncf_items = (int)items.size();
         fine->ncf = P.cf_cells;
         fine->coarse = coarse;
@@ -1551,9 +1595,8 @@ int sh_level_fill_from(sh_ctx *ctx, sh_level *dst, int which_dst, const sh_level
         CopyItem *d_rects = nullptr;
         CfItem *d_cf = nullptr;
         if (!P.rects.empty()) {
-            merge_copy_rects(P.rects);
             const std::vector<CopyItem> items = copy_items(P.rects, dst, src);
-            d_rects = upload_items(items, "fill plan");
+            d_rects = upload_items(ctx, items, "fill plan");
             ProfScope ps(ctx, kProfFill);
             copy_items_kernel<<<(int)items.size(), 128, 0, ctx->stream>>>(
                 d_rects, dst->buf[which_dst], src->buf[which_src], dst->ncomp);
@@ -1562,9 +1605,8 @@ int sh_level_fill_from(sh_ctx *ctx, sh_level *dst, int which_dst, const sh_level
         }
         if (!P.cf.empty()) {
             require(coarse != nullptr, "cells not covered by the source need a coarse level");
-            merge_cf_rects(P.cf);
             const std::vector<CfItem> items = cf_items(P.cf, dst);
-            d_cf = upload_items(items, "coarse fill plan");
+            d_cf = upload_items(ctx, items, "coarse fill plan");
             int mode;
             double alpha, beta;
             coarse_time_weights(coarse, time, mode, alpha, beta);
@@ -1575,9 +1617,8 @@ int sh_level_fill_from(sh_ctx *ctx, sh_level *dst, int which_dst, const sh_level
             ctx->launches++;
             ck(cudaGetLastError(), "coarse fill launch");
         }
-        ck(cudaStreamSynchronize(ctx->stream), "fill_from");
-        cudaFree(d_rects);
-        cudaFree(d_cf);
+        dfree_async(ctx, d_rects);
+        dfree_async(ctx, d_cf);
     });
 }
 

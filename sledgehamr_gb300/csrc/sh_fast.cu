@@ -47,7 +47,9 @@ constexpr int TX = 32, TY = 8;
 struct RealDesc {
     long long off; /* first cell of the realisation in every array */
     int N;
+    int active;    /* 0: a released slot of a pool (no tiles) */
     double dx;     /* grid spacing */
+    double dt;     /* own step of a pool member (leapfrog; 0: the step's dt) */
     double p[4];   /* physics parameters (lambda, c) or (q2, q3, q4, -) */
 };
 
@@ -238,7 +240,8 @@ __global__ void __launch_bounds__(TX *TY) fopt_leapfrog_kernel(const __grid_cons
     const R q2 = (R)d.p[0], q3 = (R)d.p[1], q4 = (R)d.p[2];
     const R inv12dx2 = (R)(1. / (12. * d.dx * d.dx));
     const R inv12dx = (R)(1. / (12. * d.dx));
-    const R hdt = (R)(0.5 * a.dt), dt = (R)a.dt;
+    const double sdt = a.dt > 0. ? a.dt : d.dt; /* pools: every member its own step */
+    const R hdt = (R)(0.5 * sdt), dt = (R)sdt;
     if (STAGE == 1 && blockIdx.x == 0 && tid == 0) a.time[1 - a.slot] = a.time[a.slot] + a.dt;
 
     auto load_plane = [&](int z, int slot) {
@@ -505,6 +508,7 @@ __global__ void add_bubbles_kernel(const RealDesc *desc, int r, R *phi, R *dphi,
 /* ======================================================================= */
 /* Host side: ensembles (sh_ensemble_* of include/sledgehamr_gb300.h).      */
 #include <functional>
+#include <map>
 #include <memory>
 #include <stdexcept>
 
@@ -542,7 +546,13 @@ struct sh_ensemble {
     RealDesc *d_desc = nullptr;
     std::vector<FastTile> tiles;
     FastTile *d_tiles = nullptr;
+    size_t tiles_cap = 0, desc_cap = 0;
     int tile_nz = 16;
+    /* pools: capacity in cells of every array and the free extents
+     * (offset -> length) */
+    bool pool = false;
+    long long capacity = 0;
+    std::map<long long, long long> free_ext;
     /* component arrays of `total` elements: state A (current) and B, the
      * Kahan compensations C (FP32_KAHAN only) and stage scratch K */
     std::vector<void *> A, B, C, K;
@@ -552,6 +562,9 @@ struct sh_ensemble {
     double *d_partial = nullptr;
     size_t partial_cap = 0;
     unsigned long long *d_counts = nullptr;
+    size_t counts_cap = 0;
+    double *staging = nullptr; /* host transfers and bubble lists; only grows */
+    size_t staging_cap = 0;
     sh::GwCache gw;
     void *gw_scratch = nullptr;
     size_t gw_scratch_cap = 0;
@@ -575,23 +588,43 @@ void drop_graphs(sh_ensemble *E) {
         }
 }
 
+/* Device copy of a host table in a buffer that only grows, written in
+ * stream order (kernels queued earlier still read the old contents). */
+template <class T>
+void upload_table(const std::vector<T> &h, T *&d, size_t &cap, cudaStream_t s, const char *what) {
+    if (h.size() > cap) {
+        if (d) {
+            fck(cudaStreamSynchronize(s), what);
+            cudaFree(d);
+            d = nullptr;
+            cap = 0;
+        }
+        const size_t n = std::max<size_t>(h.size(), 2 * cap + 64);
+        fck(cudaMalloc(&d, n * sizeof(T)), what);
+        cap = n;
+    }
+    if (!h.empty())
+        fck(cudaMemcpyAsync(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s), what);
+}
+
 void build_tiles(sh_ensemble *E, int nz) {
     std::vector<FastTile> t;
     for (int r = 0; r < E->nreal; ++r) {
+        if (!E->desc[r].active) continue;
         const int N = E->desc[r].N;
         const int tz = std::min(nz, N);
         for (int z = 0; z < N; z += tz)
             for (int y = 0; y < N; y += TY)
                 for (int x = 0; x < N; x += TX) t.push_back(FastTile{r, x, y, z, std::min(tz, N - z)});
     }
-    FastTile *d = nullptr;
-    fck(cudaMalloc(&d, t.size() * sizeof(FastTile)), "tile table");
-    fck(cudaMemcpy(d, t.data(), t.size() * sizeof(FastTile), cudaMemcpyHostToDevice),
-        "tile table upload");
-    cudaFree(E->d_tiles);
-    E->d_tiles = d;
+    upload_table(t, E->d_tiles, E->tiles_cap, est(E), "tile table");
     E->tiles.swap(t);
     E->tile_nz = nz;
+    drop_graphs(E);
+}
+
+void upload_desc(sh_ensemble *E) {
+    upload_table(E->desc, E->d_desc, E->desc_cap, est(E), "descriptor table");
     drop_graphs(E);
 }
 
@@ -608,6 +641,7 @@ void step_impl(sh_ensemble *E, const std::vector<void *> &in, const std::vector<
                int slot, double dt, cudaStream_t s) {
     const dim3 block(TX, TY);
     const int nt = (int)E->tiles.size();
+    if (nt == 0) return; /* an empty pool */
     if (E->family != 3) {
         AxionArgs<R> a;
         std::memset(&a, 0, sizeof(a));
@@ -740,6 +774,20 @@ int internal_comp(const sh_ensemble *E, int c) {
     return c == 0 ? 0 : (c == 1 ? 7 : (c < 8 ? c - 1 : c));
 }
 
+double *staging(sh_ensemble *E, size_t elems) {
+    if (elems > E->staging_cap) {
+        if (E->staging) {
+            fck(cudaStreamSynchronize(est(E)), "staging");
+            cudaFree(E->staging);
+            E->staging = nullptr;
+            E->staging_cap = 0;
+        }
+        fck(cudaMalloc(&E->staging, elems * sizeof(double)), "staging");
+        E->staging_cap = elems;
+    }
+    return E->staging;
+}
+
 long long cells_of(const sh_ensemble *E, int r) {
     return (long long)E->desc[r].N * E->desc[r].N * E->desc[r].N;
 }
@@ -782,16 +830,15 @@ int sh_ensemble_create(sh_ctx *ctx, int family, int precision, int nreal, const 
             RealDesc d;
             d.off = off;
             d.N = N[r];
+            d.active = 1;
             d.dx = dx[r];
+            d.dt = 0.;
             for (int q = 0; q < 4; ++q) d.p[q] = params ? params[4 * r + q] : 0.;
             off += (long long)N[r] * N[r] * N[r];
             E->desc.push_back(d);
         }
         E->total = off;
-        fck(cudaMalloc(&E->d_desc, nreal * sizeof(RealDesc)), "descriptor table");
-        fck(cudaMemcpy(E->d_desc, E->desc.data(), nreal * sizeof(RealDesc),
-                       cudaMemcpyHostToDevice),
-            "descriptor upload");
+        upload_desc(E);
         const size_t bytes = (size_t)E->total * E->esize;
         auto alloc = [&](std::vector<void *> &v, int n) {
             for (int q = 0; q < n; ++q) {
@@ -809,6 +856,7 @@ int sh_ensemble_create(sh_ctx *ctx, int family, int precision, int nreal, const 
         fck(cudaMalloc(&E->d_time, 2 * sizeof(double)), "time");
         fck(cudaMemset(E->d_time, 0, 2 * sizeof(double)), "time clear");
         fck(cudaMalloc(&E->d_counts, nreal * sizeof(unsigned long long)), "counts");
+        E->counts_cap = nreal;
         build_tiles(E, 16);
     });
     if (rc != SH_OK) {
@@ -832,6 +880,7 @@ int sh_ensemble_destroy(sh_ensemble *E) {
     cudaFree(E->d_partial);
     cudaFree(E->d_counts);
     cudaFree(E->gw_scratch);
+    cudaFree(E->staging);
     E->gw.release();
     delete E;
     return SH_OK;
@@ -873,13 +922,11 @@ int sh_ensemble_time(sh_ensemble *E, double *t) {
 }
 
 int sh_ensemble_write(sh_ensemble *E, int r, const double *host) {
-    if (!E || !host || r < 0 || r >= E->nreal) return SH_ERR_ARG;
+    if (!E || !host || r < 0 || r >= E->nreal || !E->desc[r].active) return SH_ERR_ARG;
     return fguard(E, [&] {
         const long long n = cells_of(E, r), o = E->desc[r].off;
         cudaStream_t s = est(E);
-        double *d = nullptr;
-        fck(cudaMalloc(&d, n * sizeof(double)), "staging");
-        std::unique_ptr<double, decltype(&cudaFree)> guard(d, &cudaFree);
+        double *d = staging(E, (size_t)n);
         for (int hc = 0; hc < E->ncomp; ++hc) {
             const int c = internal_comp(E, hc);
             fck(cudaMemcpyAsync(d, host + (size_t)hc * n, n * sizeof(double),
@@ -897,13 +944,11 @@ int sh_ensemble_write(sh_ensemble *E, int r, const double *host) {
 }
 
 int sh_ensemble_read(sh_ensemble *E, int r, double *host) {
-    if (!E || !host || r < 0 || r >= E->nreal) return SH_ERR_ARG;
+    if (!E || !host || r < 0 || r >= E->nreal || !E->desc[r].active) return SH_ERR_ARG;
     return fguard(E, [&] {
         const long long n = cells_of(E, r), o = E->desc[r].off;
         cudaStream_t s = est(E);
-        double *d = nullptr;
-        fck(cudaMalloc(&d, n * sizeof(double)), "staging");
-        std::unique_ptr<double, decltype(&cudaFree)> guard(d, &cudaFree);
+        double *d = staging(E, (size_t)n);
         for (int hc = 0; hc < E->ncomp; ++hc) {
             const int c = internal_comp(E, hc);
             if (E->esize == 8)
@@ -928,7 +973,8 @@ int sh_ensemble_set_graph(sh_ensemble *E, int on) {
 }
 
 int sh_ensemble_step(sh_ensemble *E, double dt, int nsteps) {
-    if (!E || nsteps < 0 || !(dt > 0)) return SH_ERR_ARG;
+    if (!E || nsteps < 0 || !(dt >= 0)) return SH_ERR_ARG;
+    if (dt == 0 && !(E->pool && E->family == SH_FAMILY_FOPT_GW)) return SH_ERR_ARG;
     return fguard(E, [&] {
         cudaStream_t s = est(E);
         for (int q = 0; q < nsteps; ++q) step_once(E, dt, s);
@@ -1005,6 +1051,8 @@ int sh_ensemble_energy(sh_ensemble *E, double *energy) {
         cudaStream_t s = est(E);
         const double eta = read_time(E);
         const int nt = (int)E->tiles.size();
+        for (int r = 0; r < E->nreal; ++r) energy[r] = 0.;
+        if (nt == 0) return;
         if (E->partial_cap < (size_t)nt) {
             cudaFree(E->d_partial);
             E->d_partial = nullptr;
@@ -1042,6 +1090,8 @@ int sh_ensemble_string_count(sh_ensemble *E, long long *counts) {
     return fguard(E, [&] {
         cudaStream_t s = est(E);
         const int nt = (int)E->tiles.size();
+        for (int r = 0; r < E->nreal; ++r) counts[r] = 0;
+        if (nt == 0) return;
         fck(cudaMemsetAsync(E->d_counts, 0, E->nreal * sizeof(unsigned long long), s), "clear");
         const dim3 block(TX, TY);
         auto C = [&](int c) { return E->C.empty() ? nullptr : (const float *)E->C[c]; };
@@ -1067,7 +1117,8 @@ int sh_ensemble_string_count(sh_ensemble *E, long long *counts) {
 int sh_ensemble_gw_spectrum(sh_ensemble *E, int r, int zero_padding, int projection_type,
                             int unbinned, double *bins_out, long long *ks_out, int max_bins,
                             int *nbins) {
-    if (!E || E->family != SH_FAMILY_FOPT_GW || r < 0 || r >= E->nreal || !bins_out || !nbins)
+    if (!E || E->family != SH_FAMILY_FOPT_GW || r < 0 || r >= E->nreal ||
+        !E->desc[r].active || !bins_out || !nbins)
         return SH_ERR_ARG;
     return fguard(E, [&] {
         freq(zero_padding >= 1, "zero_padding must be >= 1");
@@ -1119,7 +1170,8 @@ int sh_ensemble_gw_spectrum(sh_ensemble *E, int r, int zero_padding, int project
 
 int sh_ensemble_add_bubbles(sh_ensemble *E, int r, int nb, const double *xyz,
                             const double *profile, int nbins, double inv_dx, double Lcut) {
-    if (!E || E->family != SH_FAMILY_FOPT_GW || r < 0 || r >= E->nreal || nb < 0 ||
+    if (!E || E->family != SH_FAMILY_FOPT_GW || r < 0 || r >= E->nreal ||
+        !E->desc[r].active || nb < 0 ||
         (nb > 0 && (!xyz || !profile)) || nbins < 2 || !(inv_dx > 0) || !(Lcut > 0))
         return SH_ERR_ARG;
     if (nb == 0) return SH_OK;
@@ -1127,10 +1179,8 @@ int sh_ensemble_add_bubbles(sh_ensemble *E, int r, int nb, const double *xyz,
         freq((long long)(Lcut * inv_dx) + 2 <= nbins,
              "profile needs at least floor(Lcut * inv_dx) + 2 bins");
         cudaStream_t s = est(E);
-        double *d = nullptr;
         const size_t nx = 3 * (size_t)nb, np = 2 * (size_t)nbins;
-        fck(cudaMalloc(&d, (nx + np) * sizeof(double)), "bubble list");
-        std::unique_ptr<double, decltype(&cudaFree)> guard(d, &cudaFree);
+        double *d = staging(E, nx + np);
         fck(cudaMemcpyAsync(d, xyz, nx * sizeof(double), cudaMemcpyHostToDevice, s), "upload");
         fck(cudaMemcpyAsync(d + nx, profile, np * sizeof(double), cudaMemcpyHostToDevice, s),
             "upload");
@@ -1149,6 +1199,159 @@ int sh_ensemble_add_bubbles(sh_ensemble *E, int r, int nb, const double *xyz,
         fck(cudaGetLastError(), "bubble launch");
         fck(cudaStreamSynchronize(s), "bubbles");
     });
+}
+
+/* ---- pools: ensembles whose members come and go ---- */
+
+int sh_ensemble_create_pool(sh_ctx *ctx, int family, int precision, long long capacity_cells,
+                            sh_ensemble **out) {
+    if (!ctx || !out || capacity_cells < 0) return SH_ERR_ARG;
+    *out = nullptr;
+    if (family != SH_FAMILY_AXION_LAP1 && family != SH_FAMILY_AXION_LAP2 &&
+        family != SH_FAMILY_FOPT_GW)
+        return SH_ERR_ARG;
+    if (precision != SH_PREC_FP64 && precision != SH_PREC_FP32_KAHAN && precision != SH_PREC_FP32)
+        return SH_ERR_ARG;
+    sh_ensemble *E = new (std::nothrow) sh_ensemble();
+    if (!E) return SH_ERR_NOMEM;
+    E->ctx = ctx;
+    int rc = fguard(E, [&] {
+        set_smem_limits();
+        E->family = family;
+        E->precision = precision;
+        E->pool = true;
+        E->ncomp = family == SH_FAMILY_FOPT_GW ? 14 : 4;
+        E->esize = precision == SH_PREC_FP64 ? 8 : 4;
+        const int narrays = 2 * E->ncomp + (precision == SH_PREC_FP32_KAHAN ? E->ncomp : 0) +
+                            (family == SH_FAMILY_FOPT_GW ? 7 : 4);
+        if (capacity_cells == 0) {
+            /* 80% of the free device memory */
+            size_t fr = 0, tot = 0;
+            fck(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+            capacity_cells = (long long)(0.8 * (double)fr / ((double)narrays * E->esize));
+        }
+        freq(capacity_cells >= 512, "pool capacity too small");
+        E->capacity = capacity_cells;
+        E->total = capacity_cells;
+        const size_t bytes = (size_t)capacity_cells * E->esize;
+        auto alloc = [&](std::vector<void *> &v, int n) {
+            for (int q = 0; q < n; ++q) {
+                void *p = nullptr;
+                fck(cudaMalloc(&p, bytes), "pool allocation");
+                v.push_back(p);
+            }
+        };
+        alloc(E->A, E->ncomp);
+        alloc(E->B, E->ncomp);
+        if (precision == SH_PREC_FP32_KAHAN) alloc(E->C, E->ncomp);
+        alloc(E->K, family == SH_FAMILY_FOPT_GW ? 7 : 4);
+        E->A0 = E->A[0];
+        E->free_ext[0] = capacity_cells;
+        fck(cudaMalloc(&E->d_time, 2 * sizeof(double)), "time");
+        fck(cudaMemset(E->d_time, 0, 2 * sizeof(double)), "time clear");
+    });
+    if (rc != SH_OK) {
+        sh_ensemble_destroy(E);
+        return rc;
+    }
+    *out = E;
+    return SH_OK;
+}
+
+/* A new member of N^3 cells (state zero) in the first free extent that
+ * holds it; SH_ERR_NOMEM when none does (the pool is full for now). */
+int sh_ensemble_admit(sh_ensemble *E, int N, double dx, const double *params, double dt,
+                      int *slot) {
+    if (!E || !E->pool || !slot || N < 8 || N > 4096 || !(dx > 0) || dt < 0) return SH_ERR_ARG;
+    return fguard(E, [&] {
+        const long long n = (long long)N * N * N;
+        auto it = E->free_ext.begin();
+        while (it != E->free_ext.end() && it->second < n) ++it;
+        if (it == E->free_ext.end()) throw FastErr(SH_ERR_NOMEM, "pool full");
+        const long long off = it->first, len = it->second;
+        E->free_ext.erase(it);
+        if (len > n) E->free_ext[off + n] = len - n;
+        RealDesc d;
+        d.off = off;
+        d.N = N;
+        d.active = 1;
+        d.dx = dx;
+        d.dt = dt;
+        for (int q = 0; q < 4; ++q) d.p[q] = params ? params[q] : 0.;
+        int r = -1;
+        for (int q = 0; q < E->nreal; ++q)
+            if (!E->desc[q].active) {
+                r = q;
+                break;
+            }
+        if (r < 0) {
+            r = E->nreal++;
+            E->desc.push_back(d);
+        } else {
+            E->desc[r] = d;
+        }
+        if ((size_t)E->nreal > E->counts_cap) {
+            cudaStream_t s = est(E);
+            fck(cudaStreamSynchronize(s), "counts");
+            cudaFree(E->d_counts);
+            E->d_counts = nullptr;
+            E->counts_cap = 0;
+            const size_t c = 2 * (size_t)E->nreal + 16;
+            fck(cudaMalloc(&E->d_counts, c * sizeof(unsigned long long)), "counts");
+            E->counts_cap = c;
+        }
+        cudaStream_t s = est(E);
+        for (auto *v : {&E->A, &E->B, &E->C, &E->K})
+            for (void *p : *v)
+                fck(cudaMemsetAsync((char *)p + off * E->esize, 0, n * E->esize, s), "clear");
+        upload_desc(E);
+        build_tiles(E, E->tile_nz);
+        *slot = r;
+    });
+}
+
+int sh_ensemble_release(sh_ensemble *E, int r) {
+    if (!E || !E->pool || r < 0 || r >= E->nreal || !E->desc[r].active) return SH_ERR_ARG;
+    return fguard(E, [&] {
+        RealDesc &d = E->desc[r];
+        long long off = d.off, len = (long long)d.N * d.N * d.N;
+        d.active = 0;
+        /* merge with the free neighbours */
+        auto nx = E->free_ext.lower_bound(off);
+        if (nx != E->free_ext.end() && nx->first == off + len) {
+            len += nx->second;
+            E->free_ext.erase(nx);
+        }
+        auto pv = E->free_ext.lower_bound(off);
+        if (pv != E->free_ext.begin()) {
+            --pv;
+            if (pv->first + pv->second == off) {
+                off = pv->first;
+                len += pv->second;
+                E->free_ext.erase(pv);
+            }
+        }
+        E->free_ext[off] = len;
+        upload_desc(E);
+        build_tiles(E, E->tile_nz);
+    });
+}
+
+int sh_ensemble_pool_info(const sh_ensemble *E, long long *capacity, long long *free_cells,
+                          long long *largest_free, int *members) {
+    if (!E || !E->pool) return SH_ERR_ARG;
+    long long fr = 0, big = 0;
+    for (const auto &kv : E->free_ext) {
+        fr += kv.second;
+        big = std::max(big, kv.second);
+    }
+    int m = 0;
+    for (const RealDesc &d : E->desc) m += d.active;
+    if (capacity) *capacity = E->capacity;
+    if (free_cells) *free_cells = fr;
+    if (largest_free) *largest_free = big;
+    if (members) *members = m;
+    return SH_OK;
 }
 
 } /* extern "C" */
