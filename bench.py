@@ -201,8 +201,18 @@ def run_ensemble_leg(sh, ctx, stream, flush, steps, warmup):
     return out
 
 
-FOPT = dict(N=384, dx=0.5, dt=0.1, delta=1.6, nbubbles=64, t_nuc=(0.0, 20.0), t_end=25.0,
-            radius=5.0, width=1.0, amplitude=1.0, inv_dx=4.0, seed=7, max_grid=128)
+FOPT = dict(N=384, dx=0.25, dt=0.05, lambda_bar=0.8, nbubbles=64, t_nuc=(0.0, 20.0),
+            t_end=25.0, radius=6.0, width=1.0, amplitude=1.0, inv_dx=8.0, seed=0,
+            max_grid=128)
+
+
+def lambda_bar_params(lambda_bar):
+    """FirstOrderPhaseTransition's pure lambda-bar potential
+    (FirstOrderPhaseTransition.cpp:19-24): q2 = -1, q3 = 3 n / (4 lb),
+    q4 = -n^2 / (8 lb), n = 3 + sqrt(9 - 8 lb); false vacuum 0, true vacuum
+    1 for lb < 9/8."""
+    n = 3.0 + np.sqrt(9.0 - 8.0 * lambda_bar)
+    return [-1.0, 3.0 * n / (4.0 * lambda_bar), -n * n / (8.0 * lambda_bar)]
 
 
 def fopt_bubbles():
@@ -233,7 +243,7 @@ def run_fopt_leg(sh, ctx, stream, flush, steps, warmup):
     N, dx, dt = f["N"], f["dx"], f["dt"]
     nsteps = int(round(f["t_end"] / dt))
     xyz, tn, prof, Lcut = fopt_bubbles()
-    q = [-1.0, f["delta"], -1.0]
+    q = lambda_bar_params(f["lambda_bar"])
     state0 = np.zeros((14, N, N, N))
 
     def run(obj_step, inject, t_of):
@@ -269,7 +279,9 @@ def run_fopt_leg(sh, ctx, stream, flush, steps, warmup):
                lambda c: E.add_bubbles(0, c, prof, f["inv_dx"], Lcut), None)
     e32 = E.energy()[0]
     gw32, ks = E.gw_spectrum(0, zero_padding=1, projection_type=2, unbinned=False)
+    gu32, _ = E.gw_spectrum(0, zero_padding=1, projection_type=2, unbinned=True)
     f32 = E.read(0)
+    t32 = E.time()
     E.close()
     # FP64 plain path
     lv = sh.Level.periodic(ctx, "FirstOrderPhaseTransition", N, 2, max_grid=f["max_grid"],
@@ -280,7 +292,9 @@ def run_fopt_leg(sh, ctx, stream, flush, steps, warmup):
     ms64 = run(lambda: lv.advance(sh.LEAPFROG, dt, dx, params=params),
                lambda c: lv.add_bubbles(c, prof, f["inv_dx"], Lcut, dx), None)
     gw64, ks64 = lv.gw_spectrum(zero_padding=1, projection_type=2, unbinned=False)
+    gu64, _ = lv.gw_spectrum(zero_padding=1, projection_type=2, unbinned=True)
     f64 = lv.read()
+    t64 = lv.time()[0]
     lv.close()
     E = sh.Ensemble(ctx, sh.FAMILY_FOPT_GW, sh.PREC_FP64, [N], [dx], [*q, 0.0])
     E.write(0, f64)
@@ -288,11 +302,19 @@ def run_fopt_leg(sh, ctx, stream, flush, steps, warmup):
     e64 = E.energy()[0]
     E.close()
     cu = N ** 3 * steps
-    sig = gw64 > 1e-6 * gw64.max()
-    rel_bins = np.abs(gw32 - gw64)[sig] / gw64[sig]
+
+    def spec_err(a, b):
+        sig = b > 1e-6 * b.max()
+        rel = np.abs(a - b)[sig] / b[sig]
+        return {"total_rel": float(abs(a.sum() - b.sum()) / b.sum()),
+                "bin_rel_max": float(rel.max()) if rel.size else None,
+                "bin_rel_median": float(np.median(rel)) if rel.size else None,
+                "bins_compared": int(sig.sum()), "bins": int(b.size)}
+
     out = {
         "workload": f"FOPT + GW tensor {N}^3 periodic, dx {dx}, dt {dt}, leapfrog, 4th-order "
-                    f"stencils, V = phi^2/2 - delta phi^3/3 + phi^4/4 (delta {f['delta']}), "
+                    f"stencils, lambda-bar potential (lambda_bar {f['lambda_bar']}: q2,q3,q4 = "
+                    f"{[round(x, 6) for x in q]}), "
                     f"{f['nbubbles']} tanh bubbles (R {f['radius']}, w {f['width']}, A "
                     f"{f['amplitude']}) nucleated uniformly in t {list(f['t_nuc'])}, "
                     f"{nsteps} steps to t {f['t_end']}",
@@ -306,13 +328,103 @@ def run_fopt_leg(sh, ctx, stream, flush, steps, warmup):
             "phi_rel_l2": float(np.linalg.norm(f32[0] - f64[0]) / np.linalg.norm(f64[0])),
             "u_rel_l2": float(np.linalg.norm(f32[2:8] - f64[2:8]) / np.linalg.norm(f64[2:8])),
             "energy_rel": float(abs(e32 - e64) / abs(e64)),
-            "gw_total_rel": float(abs(gw32.sum() - gw64.sum()) / gw64.sum()),
-            "gw_bin_rel_max": float(rel_bins.max()) if rel_bins.size else None,
-            "gw_bin_rel_median": float(np.median(rel_bins)) if rel_bins.size else None,
-            "gw_bins_compared": int(sig.sum()),
+            "time_abs": float(abs(t32 - t64)),
+            "gw_binned": spec_err(gw32, gw64),
+            "gw_unbinned": spec_err(gu32, gu64),
         },
     }
     return out
+
+
+SERVE = dict(nreq=16, rate=4.0, d=(8.0, 40.0), gamma=(1.0, 4.0), lambda_bar=(0.6, 1.0),
+             sizes=(64, 96, 128, 192, 256), max_n=128, radius=4.0, width=1.0, cfl=0.2,
+             inv_dx=16.0, seed=11)
+
+
+def serve_requests(max_n):
+    """Two-bubble collisions (seeded): separation d, wall Lorentz factor
+    gamma (radial tanh wall of width w/gamma moving outwards at v), thick or
+    thin wall (lambda_bar), Poisson arrivals; box L = d + 2R + 16 with the
+    smallest N of the size set that puts 1.5 cells across the contracted
+    wall, at most max_n; run to t = 2d."""
+    sv = SERVE
+    rng = np.random.default_rng(sv["seed"])
+    arr = np.cumsum(rng.exponential(1.0 / sv["rate"], sv["nreq"]))
+    out = []
+    for q in range(sv["nreq"]):
+        d = rng.uniform(*sv["d"])
+        gamma = rng.uniform(*sv["gamma"])
+        lb = sv["lambda_bar"][int(rng.integers(0, 2))]
+        L = d + 2 * sv["radius"] + 16.0
+        wc = sv["width"] / gamma
+        N = next((n for n in sv["sizes"] if n <= max_n and L / n <= wc / 1.5),
+                 max(n for n in sv["sizes"] if n <= max_n))
+        dx = L / N
+        v = np.sqrt(1.0 - 1.0 / gamma ** 2)
+        Lcut = sv["radius"] + 10.0 * wc
+        nb = int(Lcut * sv["inv_dx"]) + 2
+        r = np.arange(nb) / sv["inv_dx"]
+        x = (r - sv["radius"]) / wc
+        prof = np.stack([0.5 * (1 - np.tanh(x)), 0.5 * v / wc / np.cosh(x) ** 2])
+        c = np.array([[L / 2 - d / 2, L / 2, L / 2], [L / 2 + d / 2, L / 2, L / 2]])
+        out.append(dict(arrival=float(arr[q]), N=N, dx=dx, dt=sv["cfl"] * dx, t_end=2 * d,
+                        params=[*lambda_bar_params(lb), 0.0], centres=c, profile=prof,
+                        inv_dx=sv["inv_dx"], Lcut=Lcut, d=d, gamma=gamma, lambda_bar=lb))
+    return out
+
+
+def run_serve_leg(sh, ctx, max_n):
+    """The serving loop on a Poisson trace, FP32+Kahan against FP64 pools:
+    p50/p99 time-to-spectrum (submission to spectrum ready, host clock) and
+    aggregate cell-updates/s over the busy period; per-request spectrum
+    error of FP32 against FP64."""
+    reqs = serve_requests(max_n)
+
+    def trace(prec):
+        S = sh.Server(ctx, prec)
+        t0 = time.perf_counter()
+        ids = [None] * len(reqs)
+        while True:
+            now = time.perf_counter() - t0
+            for q, rq in enumerate(reqs):
+                if ids[q] is None and rq["arrival"] <= now:
+                    ids[q] = S.submit(rq["N"], rq["dx"], rq["dt"], rq["t_end"], rq["params"],
+                                      rq["centres"], rq["profile"], rq["inv_dx"], rq["Lcut"])
+            running, queued, _ = S.step()
+            if all(i is not None for i in ids) and running == 0 and queued == 0:
+                break
+            if running == 0 and queued == 0:
+                nxt = min(rq["arrival"] for q, rq in enumerate(reqs) if ids[q] is None)
+                time.sleep(max(0.0, min(0.05, nxt - (time.perf_counter() - t0))))
+        lat, first, last = [], None, 0.0
+        for i in ids:
+            st, t = S.status(i)
+            assert st == 2, f"request {i} state {st}"
+            lat.append(t[2] - t[0])
+            first = t[0] if first is None else min(first, t[0])
+            last = max(last, t[2])
+        info = S.info()
+        spectra = [S.result(i)[0] for i in ids]
+        S.close()
+        return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                "max_s": float(max(lat)),
+                "cell_updates_per_s": info["cell_updates"] / (last - first),
+                "busy_s": last - first, "iterations": info["iterations"]}, spectra
+
+    r32, s32 = trace(sh.PREC_FP32_KAHAN)
+    r64, s64 = trace(sh.PREC_FP64)
+    tot = [abs(a.sum() - b.sum()) / b.sum() for a, b in zip(s32, s64)]
+    Ns = [rq["N"] for rq in reqs]
+    return {
+        "workload": f"{len(reqs)} two-bubble requests, Poisson arrivals {SERVE['rate']}/s "
+                    f"(seed {SERVE['seed']}), d ~ U{list(SERVE['d'])}, wall gamma ~ "
+                    f"U{list(SERVE['gamma'])}, lambda_bar in {list(SERVE['lambda_bar'])}, "
+                    f"N in {sorted(set(Ns))} (cap {max_n}), run to t = 2d, GW spectrum "
+                    f"(binned, projection 2) at the end",
+        "fp32_kahan": r32, "fp64": r64,
+        "gw_total_rel_err_fp32_vs_fp64": {"max": float(max(tot)),
+                                          "median": float(np.median(tot))},
+    }
 
 
 def peaks():
@@ -512,7 +624,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--forms", default="ensemble",
                     help="comma list of the chosen-form legs reported beside the headline "
-                         "(ensemble, fopt; empty for none)")
+                         "(ensemble, fopt, serve; empty for none)")
+    ap.add_argument("--serve-max-n", type=int, default=SERVE["max_n"])
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 91 if args.workload == "amr" else 20
@@ -653,6 +766,8 @@ def main():
     if "fopt" in legs:
         forms["fopt_precision"] = run_fopt_leg(sh, ctx, stream, flush, steps=20,
                                                warmup=args.warmup)
+    if "serve" in legs:
+        forms["serving"] = run_serve_leg(sh, ctx, args.serve_max_n)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args.workload)

@@ -239,6 +239,19 @@ SH_API int sh_tag(sh_ctx *ctx, sh_level *level, int use_te, double time, int lev
            long long *counts_out, int32_t *list_out, long long list_capacity,
            long long *ntagged);
 
+/* Tagging for a regrid without the mask on the host: the tags of sh_tag
+ * (same arguments), each tagged cell grown by `buffer` cells
+ * (amr.n_error_buf) and coarsened to blocks of `block` cells of this level,
+ * periodically wrapped: blocks_out[(bz * nb + by) * nb + bx] = 1 for every
+ * block such a neighbourhood touches, nb = domain cells / block (cubic
+ * domain).  ntagged = tagged cells (the CPU statistic of sh_tag).  Replaces
+ * the host-side scan of the TagBoxArray that precedes clustering in
+ * AmrCore::regrid / Sledgehamr::ErrorEst (sledgehamr.cpp:207-229). */
+SH_API int sh_tag_blocks(sh_ctx *ctx, sh_level *level, int use_te, double time, int lev,
+                         double dt, double dx, const double *te_crit, const double *params_tag,
+                         int nparams_tag, const double *params_mod, int nparams_mod, int block,
+                         int buffer, uint8_t *blocks_out, long long *ntagged);
+
 /* Same tagging as sh_tag, for callers that must not allocate GPU memory:
  * hosts that hand out all device memory through their own pool or
  * allocator, or that cannot afford the device-wide synchronisation a

@@ -219,6 +219,14 @@ struct CpuBackend {
         for (auto &v : m) out.insert(out.end(), v.begin(), v.end());
         return out;
     }
+    std::vector<uint8_t> tag_blocks(Level &l, bool use_te, double time, int lev, double dt,
+                                    double dx, int block, int buffer, int nb) {
+        std::vector<shamr::IBox> bx;
+        for (const Fab &f : l->nw.fabs)
+            bx.push_back(shamr::IBox{{f.vbox.lo.x, f.vbox.lo.y, f.vbox.lo.z},
+                                     {f.vbox.hi.x, f.vbox.hi.y, f.vbox.hi.z}});
+        return shamr::mask_to_blocks(tag(l, use_te, time, lev, dt, dx), bx, block, buffer, nb);
+    }
     void fill_from_coarse(Level &f, Level &c, double time) {
         fill_from(f->nw, nullptr, time, c->od, c->nw);
     }

@@ -143,6 +143,8 @@ SIGNATURES = {
                                vp, C.c_int, vp, C.c_int, C.c_int, vp, vp]),
     "sh_average_down": (C.c_int, [vp, vp, C.c_int, vp, C.c_int]),
     "sh_average_down_te": (C.c_int, [vp, vp, vp]),
+    "sh_tag_blocks": (C.c_int, [vp, vp, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double,
+                                vp, vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, vp, llp]),
     "sh_tag": (C.c_int, [vp, vp, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double, vp, vp,
                          C.c_int, vp, C.c_int, vp, vp, vp, C.c_longlong, llp]),
     "sh_tag_static": (C.c_int, [vp, vp, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double,

@@ -108,6 +108,14 @@ struct GpuBackend {
            "sh_tag");
         return mask;
     }
+    std::vector<uint8_t> tag_blocks(Level &l, bool use_te, double time, int lev, double dt,
+                                    double dx, int block, int buffer, int nb) {
+        std::vector<uint8_t> blk((size_t)nb * nb * nb);
+        ok(sh_tag_blocks(ctx, l->L, use_te ? 1 : 0, time, lev, dt, dx, cfg.te_crit, nullptr, 0,
+                         nullptr, 0, block, buffer, blk.data(), nullptr),
+           "sh_tag_blocks");
+        return blk;
+    }
     void fill_from_coarse(Level &f, Level &c, double time) {
         ok(sh_level_fill_from(ctx, f->L, SH_NEW, nullptr, SH_NEW, c->L, time), "fill from coarse");
     }

@@ -48,6 +48,9 @@
  *   void average_down_te(Level &fine, Level &crse);
  *   std::vector<uint8_t> tag(Level&, bool use_te, double time, int lev,
  *                            double dt, double dx);          // boxes layout
+ *   std::vector<uint8_t> tag_blocks(Level&, bool use_te, double time, int lev,
+ *                            double dt, double dx, int block, int buffer, int nb);
+ *                            // as mask_to_blocks(tag(...), ...)
  *   void fill_from_coarse(Level &fine, Level &crse, double time);
  *   void remake(Level &fresh, Level &old, Level &crse, double time);
  *   void refresh_ghosts(Level&, int which, Level *coarse);
@@ -348,6 +351,35 @@ inline std::vector<IBox> make_boxes(const std::vector<uint8_t> &tagbits,
     return bb;
 }
 
+/* Tags of a level (mask over the valid cells of `boxes`, box after box, x
+ * fastest), each grown by buf cells and coarsened to blocks of cb cells,
+ * periodically wrapped on nb blocks per side. */
+inline std::vector<uint8_t> mask_to_blocks(const std::vector<uint8_t> &mask,
+                                           const std::vector<IBox> &boxes, int cb, int buf,
+                                           int nb) {
+    auto fdiv = [](int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); };
+    auto pmod = [](int a, int n) {
+        const int r = a % n;
+        return r < 0 ? r + n : r;
+    };
+    std::vector<uint8_t> blk((size_t)nb * nb * nb, 0);
+    size_t q = 0;
+    for (const IBox &bx : boxes)
+        for (int k = bx.lo[2]; k <= bx.hi[2]; ++k)
+            for (int j = bx.lo[1]; j <= bx.hi[1]; ++j)
+                for (int i = bx.lo[0]; i <= bx.hi[0]; ++i, ++q) {
+                    if (!mask[q]) continue;
+                    const int b0[3] = {fdiv(i - buf, cb), fdiv(j - buf, cb), fdiv(k - buf, cb)};
+                    const int b1[3] = {fdiv(i + buf, cb), fdiv(j + buf, cb), fdiv(k + buf, cb)};
+                    for (int bk = b0[2]; bk <= b1[2]; ++bk)
+                        for (int bj = b0[1]; bj <= b1[1]; ++bj)
+                            for (int bi = b0[0]; bi <= b1[0]; ++bi)
+                                blk[((size_t)pmod(bk, nb) * nb + pmod(bj, nb)) * nb +
+                                    pmod(bi, nb)] = 1;
+                }
+    return blk;
+}
+
 template <class B>
 class Driver {
   public:
@@ -624,45 +656,42 @@ class Driver {
     static int fdiv(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
 
     /* Sledgehamr::ErrorEst: tags of level l at `time` (empty if skipped). */
-    std::vector<uint8_t> error_est(int l, double time) {
-        if (time == c.t_start && shadow_hierarchy) return {};
-        if (!create_level_if(l + 1, time)) return {};
+    /* Tags of level l for the grids of level l+1: the buffered tags at
+     * block resolution (blocks of blocking_factor cells of level l+1), and
+     * with record_regrids the cell mask too.  Empty when not tagging. */
+    struct Tags {
+        std::vector<uint8_t> blocks, mask;
+    };
+    int block_cells() const { return c.blocking_factor / 2; } /* in level-l cells */
+    Tags error_est(int l, double time) {
+        Tags t;
+        if (time == c.t_start && shadow_hierarchy) return t;
+        if (!create_level_if(l + 1, time)) return t;
         if (shadow_hierarchy && !te_valid[l])
             throw std::runtime_error("tagging with truncation errors but none computed on level " +
                                      std::to_string(l));
+        const int cb = block_cells();
+        if (dimN[l] % cb != 0) throw std::runtime_error("level size not a multiple of the block");
+        const int nb = dimN[l] / cb;
         Clock ck(this, kTTag);
-        return b.tag(levels[l], shadow_hierarchy, time, l, dt[l], dx[l]);
+        if (record_regrids) {
+            t.mask = b.tag(levels[l], shadow_hierarchy, time, l, dt[l], dx[l]);
+            t.blocks = mask_to_blocks(t.mask, boxes[l], cb, c.n_error_buf, nb);
+        } else {
+            t.blocks = b.tag_blocks(levels[l], shadow_hierarchy, time, l, dt[l], dx[l], cb,
+                                    c.n_error_buf, nb);
+        }
+        return t;
     }
 
-    /* New boxes of level l+1 from the tags of level l (mask in the boxes
-     * layout of mask_boxes), nested in the (new) boxes of level l. */
-    std::vector<IBox> new_grids(int l, const std::vector<uint8_t> &mask,
-                                const std::vector<IBox> &mask_boxes,
+    /* New boxes of level l+1 from the block tags of level l, nested in the
+     * (new) boxes of level l. */
+    std::vector<IBox> new_grids(int l, std::vector<uint8_t> blk,
                                 const std::vector<IBox> &nest_boxes) {
         const int bf = c.blocking_factor;
-        const int cb = bf / 2;              /* block size in level-l cells */
+        const int cb = block_cells();       /* block size in level-l cells */
         const int Nl = dimN[l];
-        if (Nl % cb != 0) throw std::runtime_error("level size not a multiple of the block");
         const int nb = Nl / cb;             /* blocks per side */
-        std::vector<uint8_t> blk((size_t)nb * nb * nb, 0);
-        const int buf = c.n_error_buf;
-        size_t q = 0;
-        for (const IBox &bx : mask_boxes)
-            for (int k = bx.lo[2]; k <= bx.hi[2]; ++k)
-                for (int j = bx.lo[1]; j <= bx.hi[1]; ++j)
-                    for (int i = bx.lo[0]; i <= bx.hi[0]; ++i, ++q) {
-                        if (!mask[q]) continue;
-                        /* blocks touched by the buffered cell [i-buf, i+buf]^3 */
-                        const int b0[3] = {fdiv(i - buf, cb), fdiv(j - buf, cb),
-                                           fdiv(k - buf, cb)};
-                        const int b1[3] = {fdiv(i + buf, cb), fdiv(j + buf, cb),
-                                           fdiv(k + buf, cb)};
-                        for (int bk = b0[2]; bk <= b1[2]; ++bk)
-                            for (int bj = b0[1]; bj <= b1[1]; ++bj)
-                                for (int bi = b0[0]; bi <= b1[0]; ++bi)
-                                    blk[((size_t)pmod(bk, nb) * nb + pmod(bj, nb)) * nb +
-                                        pmod(bi, nb)] = 1;
-                    }
         /* nesting: a block is allowed when the block grown by m level-l
          * cells lies in level l (every block on level 0) */
         std::vector<uint8_t> allowed((size_t)nb * nb * nb, 1);
@@ -708,22 +737,22 @@ class Driver {
     void regrid(int lbase, double time) {
         const int top = std::min(finest, c.max_level - 1);
         /* tags of every level on its current grids first (ErrorEst) */
-        std::vector<std::vector<uint8_t>> tags(top + 1);
+        std::vector<Tags> tags(top + 1);
         std::vector<std::vector<IBox>> old_boxes = boxes;
         for (int l = lbase; l <= top; ++l) tags[l] = error_est(l, time);
         int new_finest = lbase;
         for (int l = lbase; l <= top; ++l) {
             std::vector<IBox> nb;
-            if (!tags[l].empty()) {
+            if (!tags[l].blocks.empty()) {
                 Clock ck(this, kTGrids);
-                nb = new_grids(l, tags[l], old_boxes[l], boxes[l]);
+                nb = new_grids(l, std::move(tags[l].blocks), boxes[l]);
             }
             if (record_regrids) {
                 RegridRecord rr;
                 rr.lev = l;
                 rr.time = time;
                 rr.boxes_tagged_level = old_boxes[l];
-                rr.mask = tags[l];
+                rr.mask = tags[l].mask;
                 rr.new_boxes = nb;
                 regrids.push_back(rr);
             }

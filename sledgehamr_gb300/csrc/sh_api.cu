@@ -7,6 +7,7 @@
 #include "sledgehamr_gb300.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <mutex>
 #include <cstring>
@@ -99,6 +100,12 @@ struct sh_ctx {
 };
 
 struct sh_level {
+    long long uid = 0; /* unique per level object of the process */
+    /* average-down plan onto the level with uid avg_for (a cache) */
+    mutable long long avg_for = -1;
+    mutable void *d_avg = nullptr; /* AvgRect list */
+    mutable int navg = 0;
+    mutable long long avg_cells = 0;
     int project = -1;
     const ProjectOps *ops = nullptr;
     bool with_gw = false;
@@ -601,6 +608,41 @@ __global__ void tag_write_kernel(const unsigned char *mask, long long n,
     }
 }
 
+/* Buffered tags coarsened to blocks: every tagged valid cell marks the
+ * blocks of `block` cells (periodically wrapped, nb per side) that its
+ * neighbourhood [i - buffer, i + buffer]^3 touches.  Concurrent writes
+ * store the same value. */
+__global__ void tag_blocks_kernel(const BoxDev *boxes, const long long *vbase, int nbox,
+                                  long long nvalid, const unsigned char *mask, int dlo0, int dlo1,
+                                  int dlo2, int block, int buffer, int nb,
+                                  unsigned char *blocks) {
+    auto fdiv = [](int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); };
+    auto pmod = [](int a, int n) {
+        const int r = a % n;
+        return r < 0 ? r + n : r;
+    };
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nvalid;
+         v += (long long)gridDim.x * blockDim.x) {
+        if (!mask[v]) continue;
+        const int bx = find_box(vbase, nbox, v);
+        const BoxDev &b = boxes[bx];
+        const long long lv = v - vbase[bx];
+        const int vx = b.hi[0] - b.lo[0] + 1, vy = b.hi[1] - b.lo[1] + 1;
+        const int c[3] = {b.lo[0] + (int)(lv % vx) - dlo0,
+                          b.lo[1] + (int)((lv / vx) % vy) - dlo1,
+                          b.lo[2] + (int)(lv / ((long long)vx * vy)) - dlo2};
+        int b0[3], b1[3];
+        for (int d = 0; d < 3; ++d) {
+            b0[d] = fdiv(c[d] - buffer, block);
+            b1[d] = fdiv(c[d] + buffer, block);
+        }
+        for (int z = b0[2]; z <= b1[2]; ++z)
+            for (int y = b0[1]; y <= b1[1]; ++y)
+                for (int x = b0[0]; x <= b1[0]; ++x)
+                    blocks[((long long)pmod(z, nb) * nb + pmod(y, nb)) * nb + pmod(x, nb)] = 1;
+    }
+}
+
 int grid_for(long long work, int block = 256) {
     long long g = (work + block - 1) / block;
     if (g < 1) g = 1;
@@ -981,6 +1023,7 @@ void level_free(sh_ctx *ctx, sh_level *L) {
     dfree_async(ctx, L->d_vbase);
     dfree_async(ctx, L->d_cf);
     dfree_async(ctx, L->d_owner);
+    dfree_async(ctx, L->d_avg);
     for (int q = 0; q < 3; ++q) dfree_async(ctx, L->buf[q]);
     dfree_async(ctx, L->kbuf);
 }
@@ -1213,22 +1256,37 @@ void move(sh_ctx *ctx, const sh_level *L, double *buf, double *arr, int layout, 
     ck(cudaGetLastError(), "data movement launch");
 }
 
+/* Rectangles of coarse cells under the fine boxes, one per (fine box,
+ * coarse box) overlap, found through the coarse level's block map. */
 std::vector<AvgRect> avg_plan(const sh_level *F, const sh_level *C, long long &ncells) {
     std::vector<AvgRect> r;
     ncells = 0;
+    const int R = C->owner_res;
+    std::vector<int> owners;
     for (size_t fb = 0; fb < F->boxes.size(); ++fb) {
-        int clo[3], chi[3];
+        int clo[3], chi[3], b0[3], b1[3];
         for (int d = 0; d < 3; ++d) {
             auto cdiv = [](int a) { return a >= 0 ? a / 2 : -((-a + 1) / 2); };
             clo[d] = cdiv(F->boxes[fb].lo[d]);
             chi[d] = cdiv(F->boxes[fb].hi[d]);
+            b0[d] = floordiv(std::max(clo[d], C->dlo[d]) - C->dlo[d], R);
+            b1[d] = floordiv(std::min(chi[d], C->dhi[d]) - C->dlo[d], R);
         }
-        for (size_t cb = 0; cb < C->boxes.size(); ++cb) {
+        owners.clear();
+        for (int z = b0[2]; z <= b1[2]; ++z)
+            for (int y = b0[1]; y <= b1[1]; ++y)
+                for (int x = b0[0]; x <= b1[0]; ++x) {
+                    const int o = C->owner[((size_t)z * C->owner_nb[1] + y) * C->owner_nb[0] + x];
+                    if (o >= 0) owners.push_back(o);
+                }
+        std::sort(owners.begin(), owners.end());
+        owners.erase(std::unique(owners.begin(), owners.end()), owners.end());
+        for (int cb : owners) {
             int lo[3], hi[3];
             if (!box_intersect(clo, chi, C->boxes[cb].lo, C->boxes[cb].hi, lo, hi)) continue;
             AvgRect a;
             a.fbox = (int)fb;
-            a.cbox = (int)cb;
+            a.cbox = cb;
             for (int d = 0; d < 3; ++d) {
                 a.lo[d] = lo[d];
                 a.hi[d] = hi[d];
@@ -1244,20 +1302,23 @@ std::vector<AvgRect> avg_plan(const sh_level *F, const sh_level *C, long long &n
 void average_down_impl(sh_ctx *ctx, const sh_level *F, const double *fine, const sh_level *C,
                        double *crse, double *te) {
     require(F->ncomp == C->ncomp, "fine and coarse levels differ in components");
-    for (const sh_box &b : F->boxes)
-        for (int d = 0; d < 3; ++d)
-            require(b.lo[d] % 2 == 0 && b.hi[d] % 2 != 0 && b.lo[d] >= 0,
-                    "fine boxes must be aligned to the refinement ratio 2");
-    long long ncells = 0;
-    std::vector<AvgRect> plan = avg_plan(F, C, ncells);
-    if (ncells == 0) return;
-    AvgRect *d = (AvgRect *)ctx_scratch(ctx, plan.size() * sizeof(AvgRect));
-    ck(cudaMemcpyAsync(d, plan.data(), plan.size() * sizeof(AvgRect), cudaMemcpyHostToDevice,
-                       ctx->stream),
-       "average-down plan upload");
+    if (F->avg_for != C->uid) {
+        for (const sh_box &b : F->boxes)
+            for (int d = 0; d < 3; ++d)
+                require(b.lo[d] % 2 == 0 && b.hi[d] % 2 != 0 && b.lo[d] >= 0,
+                        "fine boxes must be aligned to the refinement ratio 2");
+        long long ncells = 0;
+        std::vector<AvgRect> plan = avg_plan(F, C, ncells);
+        dfree_async(ctx, F->d_avg);
+        F->d_avg = upload_async(ctx, plan.data(), plan.size(), "average-down plan");
+        F->navg = (int)plan.size();
+        F->avg_cells = ncells;
+        F->avg_for = C->uid;
+    }
+    if (F->avg_cells == 0) return;
     ProfScope ps(ctx, kProfAvg);
-    avgdown_kernel<<<grid_for(ncells), 256, 0, ctx->stream>>>(
-        d, (int)plan.size(), ncells, F->d_boxes, C->d_boxes, F->ncomp, fine, crse, te);
+    avgdown_kernel<<<grid_for(F->avg_cells), 256, 0, ctx->stream>>>(
+        (const AvgRect *)F->d_avg, F->navg, F->avg_cells, F->d_boxes, C->d_boxes, F->ncomp, fine, crse, te);
     ctx->launches++;
     ck(cudaGetLastError(), "average-down launch");
 }
@@ -1395,6 +1456,8 @@ int sh_level_create(sh_ctx *ctx, int project, int with_gw, const int domain_lo[3
     if (!ctx || !out) return SH_ERR_ARG;
     *out = nullptr;
     sh_level *L = new (std::nothrow) sh_level();
+    static std::atomic<long long> next_uid{1};
+    if (L) L->uid = next_uid++;
     if (!L) return SH_ERR_NOMEM;
     int rc = guarded(ctx, [&] {
         set_device(ctx);
@@ -1443,9 +1506,12 @@ int sh_level_create(sh_ctx *ctx, int project, int with_gw, const int domain_lo[3
             L->vbase.push_back(vb);
             L->hboxes.push_back(bd);
             for (int z = bd.lo[2]; z <= bd.hi[2]; z += kTileZ)
-                for (int y = bd.lo[1]; y <= bd.hi[1]; y += kTileY)
-                    for (int x = bd.lo[0]; x <= bd.hi[0]; x += kTileX)
-                        tiles.push_back(TileDev{b, x, y, z});
+                for (int x = bd.lo[0]; x <= bd.hi[0]; x += kTileX) {
+                    const int nx = std::min(kTileX, bd.hi[0] - x + 1);
+                    const int rows = kThreads / nx;
+                    for (int y = bd.lo[1]; y <= bd.hi[1]; y += rows)
+                        tiles.push_back(TileDev{b, x, y, z, nx});
+                }
         }
         L->total_gvol = base;
         L->nvalid = vb;
@@ -1805,6 +1871,76 @@ int sh_tag(sh_ctx *ctx, sh_level *L, int use_te, double time, int lev, double dt
         if (ntagged) *ntagged = total;
         if (counts_out)
             for (int n = 0; n < 2 + L->ncomp; ++n) counts_out[n] = (long long)counts[n];
+    });
+}
+
+int sh_tag_blocks(sh_ctx *ctx, sh_level *L, int use_te, double time, int lev, double dt,
+                  double dx, const double *te_crit, const double *params_tag, int nparams_tag,
+                  const double *params_mod, int nparams_mod, int block, int buffer,
+                  uint8_t *blocks_out, long long *ntagged) {
+    if (!ctx || !L || !blocks_out || block <= 0 || buffer < 0) return SH_ERR_ARG;
+    return guarded(ctx, [&] {
+        set_device(ctx);
+        require(L->nghost >= 1, "tagging reads the +1 neighbours: nghost >= 1");
+        require(nparams_tag >= 0 && nparams_tag <= kMaxParams, "at most 32 tag parameters");
+        require(nparams_mod >= 0 && nparams_mod <= kMaxComp, "at most 32 modifier parameters");
+        require(!use_te || te_crit, "te_crit required with truncation errors");
+        const int N = L->dhi[0] - L->dlo[0] + 1;
+        for (int d = 0; d < 3; ++d)
+            require(L->dhi[d] - L->dlo[d] + 1 == N, "block tags need a cubic domain");
+        require(N % block == 0, "the domain must be a whole number of blocks");
+        const int nb = N / block;
+        const long long nblk = (long long)nb * nb * nb;
+        TagArgs a;
+        std::memset(&a, 0, sizeof(a));
+        a.boxes = L->d_boxes;
+        a.tiles = L->d_tiles;
+        a.state = L->buf[SH_NEW];
+        a.te = use_te ? L->buf[SH_OLD] : nullptr;
+        a.ncomp = L->ncomp;
+        a.lev = lev;
+        a.time = time;
+        a.dt = dt;
+        a.dx = dx;
+        for (int n = 0; n < L->ncomp; ++n) a.te_crit[n] = use_te ? te_crit[n] : 0.0;
+        for (int q = 0; q < nparams_tag; ++q) a.params_tag[q] = params_tag[q];
+        for (int q = 0; q < nparams_mod; ++q) a.params_mod[q] = params_mod[q];
+        const int nbox = (int)L->boxes.size();
+        size_t off = 0;
+        auto carve = [&](size_t bytes) {
+            size_t o = off;
+            off += (bytes + 255) & ~size_t(255);
+            return o;
+        };
+        const size_t o_mask = carve(L->nvalid);
+        const size_t o_moff = carve(nbox * sizeof(long long));
+        const size_t o_cnt = carve((2 + kMaxComp) * sizeof(unsigned long long));
+        const size_t o_blk = carve(nblk);
+        char *base = (char *)ctx_scratch(ctx, off);
+        a.mask = (unsigned char *)(base + o_mask);
+        a.mask_off = (const long long *)(base + o_moff);
+        a.counts = (unsigned long long *)(base + o_cnt);
+        unsigned char *blk = (unsigned char *)(base + o_blk);
+        ck(cudaMemcpyAsync(base + o_moff, L->vbase.data(), nbox * sizeof(long long),
+                           cudaMemcpyHostToDevice, ctx->stream),
+           "mask offsets");
+        ck(cudaMemsetAsync(a.counts, 0, (2 + kMaxComp) * sizeof(unsigned long long), ctx->stream),
+           "count clear");
+        ck(cudaMemsetAsync(blk, 0, nblk, ctx->stream), "block clear");
+        ProfScope ps(ctx, kProfTag);
+        ck(L->ops->launch_tag(a, L->ntiles, ctx->stream), "tag launch");
+        tag_blocks_kernel<<<grid_for(L->nvalid), 256, 0, ctx->stream>>>(
+            L->d_boxes, L->d_vbase, nbox, L->nvalid, a.mask, L->dlo[0], L->dlo[1], L->dlo[2],
+            block, buffer, nb, blk);
+        ctx->launches += 2;
+        ck(cudaGetLastError(), "block tag launch");
+        ck(cudaMemcpyAsync(blocks_out, blk, nblk, cudaMemcpyDeviceToHost, ctx->stream),
+           "block download");
+        unsigned long long counts[2 + kMaxComp];
+        ck(cudaMemcpyAsync(counts, a.counts, sizeof(counts), cudaMemcpyDeviceToHost, ctx->stream),
+           "count download");
+        ck(cudaStreamSynchronize(ctx->stream), "block tags");
+        if (ntagged) *ntagged = (long long)counts[0];
     });
 }
 

@@ -27,6 +27,7 @@ constexpr int kMaxStages = 8;    /* RKN stages */
 
 /* Tile of a box processed by one thread block of the stage kernels. */
 constexpr int kTileX = 32, kTileY = 4, kTileZ = 8;
+constexpr int kThreads = kTileX * kTileY;
 
 struct BoxDev {
     long long off;  /* element offset of the box in a level buffer (per comp-set) */
@@ -40,6 +41,7 @@ struct BoxDev {
 struct TileDev {
     int box;
     int x0, y0, z0; /* first cell of the tile (absolute level index) */
+    int nx;         /* cells along x (<= kTileX); the tile has kThreads / nx rows */
 };
 
 /* One rectangle of ghost cells copied from a valid region of the same

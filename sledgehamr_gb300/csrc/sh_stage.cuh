@@ -15,10 +15,12 @@
  *   leapfrog       vh = v0 + dt/2 a, x1 = x0 + dt vh; v1 = vh + dt/2 a
  *                  (leapfrog.cpp:13-57)
  *
- * Thread mapping: a block of kTileX x kTileY threads owns a tile of
- * kTileX x kTileY x kTileZ cells of one box and each thread walks its
- * z-column, so that per-thread set-up (the reciprocals of dx^2 and of the
- * time in the hooks) is paid once per column.  Hooks read the stage state
+ * Thread mapping: a block of kThreads = 128 threads owns a tile of one box,
+ * nx <= 32 cells wide in x (the box width when the box is narrower, so that
+ * the small boxes of refined levels keep every thread busy), kThreads / nx
+ * rows in y and kTileZ planes in z; each thread walks its z-column, so that
+ * per-thread set-up (the reciprocals of dx^2 and of the time in the hooks)
+ * is paid once per column.  Hooks read the stage state
  * straight from HBM through an Array4 view of the ghost-grown box; the
  * reuse of neighbour values comes from L1.  The per-cell Rhs output is an
  * Array4 over a register array (all strides zero), which the compiler keeps
@@ -59,9 +61,11 @@ __global__ void __launch_bounds__(kTileX *kTileY)
 
     const TileDev t = a.tiles[blockIdx.x];
     const BoxDev b = a.boxes[t.box];
-    const int i = t.x0 + threadIdx.x;
-    const int j = t.y0 + threadIdx.y;
-    if (i > b.hi[0] || j > b.hi[1]) return;
+    const int tid = threadIdx.x + kTileX * threadIdx.y;
+    const int ty = tid / t.nx;
+    const int i = t.x0 + (tid - ty * t.nx);
+    const int j = t.y0 + ty;
+    if (ty >= kThreads / t.nx || i > b.hi[0] || j > b.hi[1]) return;
     const int kend = min(t.z0 + kTileZ - 1, b.hi[2]);
 
     const long long gx = b.gdim[0];
@@ -186,9 +190,11 @@ template <class H, int NC>
 __global__ void __launch_bounds__(kTileX *kTileY) tag_kernel(const __grid_constant__ TagArgs a) {
     const TileDev t = a.tiles[blockIdx.x];
     const BoxDev b = a.boxes[t.box];
-    const int i = t.x0 + threadIdx.x;
-    const int j = t.y0 + threadIdx.y;
-    const bool inside = (i <= b.hi[0] && j <= b.hi[1]);
+    const int tid = threadIdx.x + kTileX * threadIdx.y;
+    const int ty = tid / t.nx;
+    const int i = t.x0 + (tid - ty * t.nx);
+    const int j = t.y0 + ty;
+    const bool inside = (ty < kThreads / t.nx && i <= b.hi[0] && j <= b.hi[1]);
     const int kend = min(t.z0 + kTileZ - 1, b.hi[2]);
     const long long gx = b.gdim[0], gxy = gx * b.gdim[1];
     const amrex::Dim3 glo{b.glo[0], b.glo[1], b.glo[2]};

@@ -38,3 +38,59 @@ def test_amr_matches_oracle(ctx, integrator):
         assert rg["new_boxes"] == ro["new_boxes"]
     g.close()
     o.close()
+
+
+@pytest.mark.parametrize("clustering", [0, 1])
+def test_amr_block_tags_match_oracle(ctx, clustering):
+    """Without recorded regrids the GPU tags straight to blocks
+    (sh_tag_blocks); the hierarchy still equals the oracle's, which coarsens
+    its CPU mask on the host."""
+    cfg = dict(record_regrids=0, clustering=clustering)
+    g = sh.Amr(ctx, config(**cfg), level0(1))
+    o = OracleAmr(config(**cfg), level0(1))
+    for step in range(3):
+        g.step(1)
+        o.step(1)
+        assert g.info() == o.info()
+        for lev in range(g.info()["finest"] + 1):
+            assert g.level(lev).boxes == o.boxes(lev)
+            od, _ = o.read(lev)
+            assert rel_l2(g.level(lev).read(), od) <= 1e-12
+    assert g.info()["finest"] >= 1
+    g.close()
+    o.close()
+
+
+def test_tag_blocks_equal_coarsened_mask(ctx):
+    """sh_tag_blocks equals the host coarsening of sh_tag's mask."""
+    import ctypes as C
+    from sledgehamr_gb300 import ic
+    N = 32
+    st = ic.axion_string_ic(N, 8.0, kmax=3.0, seed=5)
+    lv = sh.Level.periodic(ctx, "AxionStringsLap1", N, 1, max_grid=8)
+    lv.write(st)
+    mask, counts, _ = lv.tag(1.0, 0, 0.0625, 0.25)
+    for block, buf in ((4, 1), (4, 2), (8, 0)):
+        nb = N // block
+        blocks = np.zeros(nb ** 3, dtype=np.uint8)
+        nt = C.c_longlong()
+        ctx.check(ctx.lib.sh_tag_blocks(ctx.h, lv.h, 0, C.c_double(1.0), 0, C.c_double(0.0625),
+                                        C.c_double(0.25), None, None, 0, None, 0, block, buf,
+                                        C.c_void_p(blocks.ctypes.data), C.byref(nt)),
+                  "sh_tag_blocks")
+        assert nt.value == counts[0]
+        ref = np.zeros((nb, nb, nb), dtype=np.uint8)
+        off = 0
+        for lo, hi in lv.boxes:
+            n = [hi[d] - lo[d] + 1 for d in range(3)]
+            m = mask[off: off + n[0] * n[1] * n[2]].reshape(n[2], n[1], n[0])
+            off += n[0] * n[1] * n[2]
+            for k, j, i in zip(*np.nonzero(m)):
+                c = (lo[0] + i, lo[1] + j, lo[2] + k)
+                rng = [range((c[d] - buf) // block, (c[d] + buf) // block + 1) for d in range(3)]
+                for bz in rng[2]:
+                    for by in rng[1]:
+                        for bx in rng[0]:
+                            ref[bz % nb, by % nb, bx % nb] = 1
+        assert np.array_equal(blocks.reshape(nb, nb, nb), ref)
+    lv.close()
