@@ -61,7 +61,7 @@ AMR = dict(N0=256, L=64.0, project="AxionStringsLap2", params=[1.0, 0.0], nghost
 
 
 ENSEMBLE = dict(nreal=192, sizes=(32, 48, 64, 96, 128), lam=(0.5, 4.0), dx=0.25, eta0=0.1,
-                total_steps=200, seed=2024)
+                total_steps=94, seed=2024)
 
 
 def ensemble_spec():
@@ -700,7 +700,8 @@ def main():
     cus = cell_updates() - cu0
     stage_ms, stage_launches = ctx.profile_read("rhs")
     fill_ms, fill_launches = ctx.profile_read("fill_patch")
-    other = {c: ctx.profile_read(c)[0] for c in ("average_down", "tagging", "data_move")}
+    other = {c: ctx.profile_read(c)[0] for c in ("coarse_fine", "average_down", "tagging",
+                                                  "data_move")}
     ctx.profile(False)
     if world > 1:
         dist.barrier()

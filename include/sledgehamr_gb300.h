@@ -321,15 +321,19 @@ typedef struct sh_amr_config {
     int nparams;
     double gw_params[16];        /* SetParamsGravitationalWaveRhs */
     int ngw;
-    int clustering;              /* SH_CLUSTER_BR (default) or SH_CLUSTER_WINDOWS */
+    int clustering;              /* SH_CLUSTER_BR, SH_CLUSTER_WINDOWS, SH_CLUSTER_BR_WINDOWS */
     double grid_eff;             /* amr.grid_eff of the clustering (default 0.7) */
 } sh_amr_config;
 /* New-grid generation from the buffered tags (at blocking-factor
  * resolution): Berger-Rigoutsos clustering to efficiency grid_eff, then
- * chopping to max_grid_size, as AMReX's MakeNewGrids does; or tagged blocks
- * merged inside aligned max_grid_size windows (every box fully tagged). */
+ * chopping to max_grid_size, as AMReX's MakeNewGrids does (SH_CLUSTER_BR);
+ * the same clustering run independently inside every aligned window of
+ * max_grid_size cells, in parallel on the host (SH_CLUSTER_BR_WINDOWS); or
+ * tagged blocks merged inside those windows, every box fully tagged
+ * (SH_CLUSTER_WINDOWS). */
 #define SH_CLUSTER_BR 0
 #define SH_CLUSTER_WINDOWS 1
+#define SH_CLUSTER_BR_WINDOWS 2
 
 SH_API int sh_amr_config_defaults(sh_amr_config *cfg);
 /* Hierarchy with level 0 = level0 (canonical layout, N0^3 cells, boxes of

@@ -22,7 +22,7 @@ LIB = os.path.join(PKG, "libsledgehamr_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-std=c++17", "-O3", "-lineinfo", "--expt-relaxed-constexpr",
-    "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+    "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden", "-Xcompiler", "-fopenmp",
     "-I" + os.path.join(ROOT, "include"),
     "-I" + os.path.join(ROOT, "include", "sledgehamr"),
     "-diag-suppress", "177,550,20012",
@@ -80,7 +80,8 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         with cf.ThreadPoolExecutor(max_workers=jobs or min(len(todo), os.cpu_count() or 4)) as ex:
             list(ex.map(compile_one, todo))
     if todo or not os.path.exists(LIB):
-        cmd = [nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcufft", "-lcudart"]
+        cmd = [nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcufft", "-lcudart",
+                                                               "-Xcompiler", "-fopenmp"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

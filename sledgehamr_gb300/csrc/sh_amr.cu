@@ -190,7 +190,7 @@ int sh_amr_config_defaults(sh_amr_config *c) {
     c->cfl = 0.25;
     c->t_start = 0.1;
     c->string_lambda = 1.;
-    c->clustering = SH_CLUSTER_BR;
+    c->clustering = SH_CLUSTER_BR_WINDOWS;
     c->grid_eff = 0.7;
     for (int n = 0; n < 32; ++n) c->te_crit[n] = DBL_MAX;
     return SH_OK;
@@ -204,7 +204,8 @@ int sh_amr_create(sh_ctx *ctx, const sh_amr_config *cfg, const double *level0, s
     if (rc != SH_OK) return rc;
     if (cfg->nparams < 0 || cfg->nparams > 32 || cfg->ngw < 0 || cfg->ngw > 16)
         return SH_ERR_ARG;
-    if ((cfg->clustering != SH_CLUSTER_BR && cfg->clustering != SH_CLUSTER_WINDOWS) ||
+    if ((cfg->clustering != SH_CLUSTER_BR && cfg->clustering != SH_CLUSTER_WINDOWS &&
+         cfg->clustering != SH_CLUSTER_BR_WINDOWS) ||
         !(cfg->grid_eff > 0. && cfg->grid_eff <= 1.))
         return SH_ERR_ARG;
     sh_amr *a = new (std::nothrow) sh_amr();

@@ -313,41 +313,71 @@ inline void runs_to_boxes(const BlockSet &t, const int lo[3], const int hi[3],
 
 /* Boxes (block coordinates) covering the set blocks of `tags` (nb^3 blocks,
  * x fastest), inside the allowed blocks, at most w blocks per side:
- * clustering 0 Berger-Rigoutsos to efficiency grid_eff, 1 aligned windows. */
+ * clustering 0 Berger-Rigoutsos to efficiency grid_eff over the whole
+ * domain, then nesting, merging and chopping; 2 the same inside every
+ * aligned window of w^3 blocks (the windows that hold tags are clustered
+ * independently, in parallel); 1 aligned windows of fully tagged runs. */
 inline std::vector<IBox> make_boxes(const std::vector<uint8_t> &tagbits,
                                     const std::vector<uint8_t> &allowed, int nb, int clustering,
                                     double grid_eff, int w) {
     const BlockSet tags{tagbits, nb};
+    const BlockSet nest{allowed, nb};
     std::vector<IBox> bb;
-    if (clustering == 1) {
-        for (int wz = 0; wz < nb; wz += w)
-            for (int wy = 0; wy < nb; wy += w)
-                for (int wx = 0; wx < nb; wx += w) {
-                    const int lo[3] = {wx, wy, wz};
-                    const int hi[3] = {std::min(wx + w, nb) - 1, std::min(wy + w, nb) - 1,
-                                       std::min(wz + w, nb) - 1};
-                    runs_to_boxes(tags, lo, hi, bb);
-                }
+    auto nested = [&](const std::vector<IBox> &cl, std::vector<IBox> &out) {
+        for (const IBox &x : cl) {
+            bool all = true;
+            for (int z = x.lo[2]; z <= x.hi[2] && all; ++z)
+                for (int y = x.lo[1]; y <= x.hi[1] && all; ++y)
+                    for (int xx = x.lo[0]; xx <= x.hi[0] && all; ++xx) all = nest.at(xx, y, z);
+            if (all) out.push_back(x);
+            else runs_to_boxes(nest, x.lo, x.hi, out); /* the cluster within the nesting */
+        }
+    };
+    auto order = [](std::vector<IBox> &v) {
+        std::sort(v.begin(), v.end(), [](const IBox &a, const IBox &b) {
+            for (int d = 2; d >= 0; --d)
+                if (a.lo[d] != b.lo[d]) return a.lo[d] < b.lo[d];
+            return false;
+        });
+    };
+    if (clustering == 1 || clustering == 2) {
+        const int nw = (nb + w - 1) / w;
+        const long long nwin = (long long)nw * nw * nw;
+        std::vector<std::vector<IBox>> per(nwin);
+#pragma omp parallel for schedule(dynamic, 8)
+        for (long long q = 0; q < nwin; ++q) {
+            const int wx = (int)(q % nw) * w, wy = (int)((q / nw) % nw) * w,
+                      wz = (int)(q / ((long long)nw * nw)) * w;
+            const int lo[3] = {wx, wy, wz};
+            const int hi[3] = {std::min(wx + w, nb) - 1, std::min(wy + w, nb) - 1,
+                               std::min(wz + w, nb) - 1};
+            bool any = false;
+            for (int z = lo[2]; z <= hi[2] && !any; ++z)
+                for (int y = lo[1]; y <= hi[1] && !any; ++y)
+                    for (int x = lo[0]; x <= hi[0] && !any; ++x) any = tags.at(x, y, z);
+            if (!any) continue;
+            if (clustering == 1) {
+                runs_to_boxes(tags, lo, hi, per[q]);
+            } else {
+                std::vector<IBox> cl;
+                cluster(tags, IBox{{lo[0], lo[1], lo[2]}, {hi[0], hi[1], hi[2]}}, grid_eff, cl);
+                nested(cl, per[q]);
+            }
+        }
+        for (auto &v : per) bb.insert(bb.end(), v.begin(), v.end());
+        if (clustering == 2) {
+            simplify(bb);
+            max_size(bb, w);
+        }
+        order(bb);
         return bb;
     }
     std::vector<IBox> cl;
     cluster(tags, IBox{{0, 0, 0}, {nb - 1, nb - 1, nb - 1}}, grid_eff, cl);
-    const BlockSet nest{allowed, nb};
-    for (const IBox &x : cl) {
-        bool all = true;
-        for (int z = x.lo[2]; z <= x.hi[2] && all; ++z)
-            for (int y = x.lo[1]; y <= x.hi[1] && all; ++y)
-                for (int xx = x.lo[0]; xx <= x.hi[0] && all; ++xx) all = nest.at(xx, y, z);
-        if (all) bb.push_back(x);
-        else runs_to_boxes(nest, x.lo, x.hi, bb); /* the cluster within the nesting */
-    }
+    nested(cl, bb);
     simplify(bb);
     max_size(bb, w);
-    std::sort(bb.begin(), bb.end(), [](const IBox &a, const IBox &b) {
-        for (int d = 2; d >= 0; --d)
-            if (a.lo[d] != b.lo[d]) return a.lo[d] < b.lo[d];
-        return false;
-    });
+    order(bb);
     return bb;
 }
 
@@ -705,6 +735,7 @@ class Driver {
                     for (int j = bx.lo[1] / lb; j <= bx.hi[1] / lb; ++j)
                         for (int i = bx.lo[0] / lb; i <= bx.hi[0] / lb; ++i)
                             cov[((size_t)k * nlb + j) * nlb + i] = 1;
+#pragma omp parallel for schedule(static)
             for (int bk = 0; bk < nb; ++bk)
                 for (int bj = 0; bj < nb; ++bj)
                     for (int bi = 0; bi < nb; ++bi) {

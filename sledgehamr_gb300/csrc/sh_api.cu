@@ -755,12 +755,21 @@ FillPlan build_fill_plan(const sh_level *D, const sh_level *S, const sh_level *C
         int sh[3];
         int lo[3], hi[3];
     };
-    std::vector<Blk> blk;
     struct Run {
         int kind, own, sh[3], lo[3], hi[3];
     };
+    const long long nbox = (long long)D->boxes.size();
+    std::vector<std::vector<GhostCopyDev>> box_rects(nbox);
+    std::vector<std::vector<CfRect>> box_cf(nbox);
+    bool uncovered = false;
+    /* boxes are independent: host threads share them, results are
+     * concatenated in box order afterwards (the plan is deterministic) */
+#pragma omp parallel
+    {
+    std::vector<Blk> blk;
     std::vector<Run> runs, merged;
-    for (size_t b = 0; b < D->boxes.size(); ++b) {
+#pragma omp for schedule(dynamic, 16)
+    for (long long b = 0; b < nbox; ++b) {
         int glo[3], ghi[3], blo[3], nbk[3];
         for (int d = 0; d < 3; ++d) {
             glo[d] = D->boxes[b].lo[d] - g;
@@ -820,10 +829,10 @@ FillPlan build_fill_plan(const sh_level *D, const sh_level *S, const sh_level *C
                                 }
                                 if (C->owner[((size_t)cb[2] * C->owner_nb[1] + cb[1]) *
                                                  C->owner_nb[0] +
-                                             cb[0]] < 0)
-                                    throw ShError(SH_ERR_ARG,
-                                                  "coarse level does not cover the cells to "
-                                                  "interpolate (levels are not properly nested)");
+                                             cb[0]] < 0) {
+#pragma omp atomic write
+                                    uncovered = true;
+                                }
                             }
                     k.kind = 2;
                 }
@@ -878,8 +887,6 @@ FillPlan build_fill_plan(const sh_level *D, const sh_level *S, const sh_level *C
             runs.swap(merged);
         }
         for (const Run &r : runs) {
-            const long long ncell = (long long)(r.hi[0] - r.lo[0] + 1) *
-                                    (r.hi[1] - r.lo[1] + 1) * (r.hi[2] - r.lo[2] + 1);
             if (r.kind == 1) {
                 GhostCopyDev c;
                 c.dbox = (int)b;
@@ -889,9 +896,7 @@ FillPlan build_fill_plan(const sh_level *D, const sh_level *S, const sh_level *C
                     c.hi[d] = r.hi[d];
                     c.shift[d] = r.sh[d];
                 }
-                c.first = P.rect_cells;
-                P.rect_cells += ncell;
-                P.rects.push_back(c);
+                box_rects[b].push_back(c);
             } else {
                 CfRect c;
                 c.dbox = (int)b;
@@ -899,10 +904,27 @@ FillPlan build_fill_plan(const sh_level *D, const sh_level *S, const sh_level *C
                     c.lo[d] = r.lo[d];
                     c.hi[d] = r.hi[d];
                 }
-                c.first = P.cf_cells;
-                P.cf_cells += ncell;
-                P.cf.push_back(c);
+                box_cf[b].push_back(c);
             }
+        }
+    }
+    } /* omp parallel */
+    if (uncovered)
+        throw ShError(SH_ERR_ARG, "coarse level does not cover the cells to interpolate (levels "
+                                  "are not properly nested)");
+    auto cells = [](const int lo[3], const int hi[3]) {
+        return (long long)(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+    };
+    for (long long b = 0; b < nbox; ++b) {
+        for (GhostCopyDev &c : box_rects[b]) {
+            c.first = P.rect_cells;
+            P.rect_cells += cells(c.lo, c.hi);
+            P.rects.push_back(c);
+        }
+        for (CfRect &c : box_cf[b]) {
+            c.first = P.cf_cells;
+            P.cf_cells += cells(c.lo, c.hi);
+            P.cf.push_back(c);
         }
     }
     return P;

@@ -44,7 +44,7 @@ def cover_count(boxes, nb):
     return cnt
 
 
-@pytest.mark.parametrize("clustering", [0, 1])
+@pytest.mark.parametrize("clustering", [0, 1, 2])
 @pytest.mark.parametrize("seed", [0, 1, 2])
 def test_boxes_cover_tags_inside_nesting(clustering, seed):
     nb, w, eff = 24, 4, 0.7
@@ -70,8 +70,9 @@ def test_br_makes_fewer_boxes_than_windows():
     tags = blobs(nb, 7, nblob=10, r=5.0)
     allowed = np.ones_like(tags)
     br = make_boxes(tags, allowed, 0, 0.7, w)
+    brw = make_boxes(tags, allowed, 2, 0.7, w)
     win = make_boxes(tags, allowed, 1, 0.7, w)
-    assert len(br) < len(win)
+    assert len(br) < len(win) and len(brw) < len(win)
 
 
 def test_full_and_empty_tag_sets():

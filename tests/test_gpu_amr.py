@@ -40,7 +40,7 @@ def test_amr_matches_oracle(ctx, integrator):
     o.close()
 
 
-@pytest.mark.parametrize("clustering", [0, 1])
+@pytest.mark.parametrize("clustering", [0, 1, 2])
 def test_amr_block_tags_match_oracle(ctx, clustering):
     """Without recorded regrids the GPU tags straight to blocks
     (sh_tag_blocks); the hierarchy still equals the oracle's, which coarsens
