@@ -614,6 +614,59 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_case(name):
+    """Small fixed cases for profiler captures (no timing, no output line):
+    axion-fp32k / axion-fp64: one 256^3 axion realisation, 3 RKN4 steps
+    (9 stage launches); fopt-fp32k: one 192^3 FOPT + GW realisation, 3
+    leapfrog steps; amr: the AMR workload at N0 = 64 (L = 16), 40 coarse
+    steps; single: the 128^3 FP64 level, 3 RKN4 steps."""
+    import sledgehamr_gb300 as sh
+    from sledgehamr_gb300 import ic
+    ctx = sh.Context(0)
+    if name.startswith("axion"):
+        prec = sh.PREC_FP64 if name.endswith("fp64") else sh.PREC_FP32_KAHAN
+        N = 256
+        E = sh.Ensemble(ctx, sh.FAMILY_AXION_LAP1, prec, [N], [0.25], [1, 0, 0, 0])
+        E.write(0, ic.axion_string_ic(N, N * 0.25, kmax=1.0, seed=0))
+        E.set_time(0.1)
+        E.step(0.0625, 3)
+        E.close()
+    elif name == "fopt-fp32k":
+        N = 192
+        q = lambda_bar_params(0.8)
+        E = sh.Ensemble(ctx, sh.FAMILY_FOPT_GW, sh.PREC_FP32_KAHAN, [N], [0.25], [*q, 0.0])
+        st = np.zeros((14, N, N, N))
+        st[0] = 0.5 + 0.2 * ic.gaussian_field(N, N * 0.25, 2.0, 1)
+        E.write(0, st)
+        E.step(0.05, 3)
+        E.close()
+    elif name == "amr":
+        a = AMR
+        cfg = sh.amr_config(a["project"], N0=64, L=16.0, cfl=a["cfl"], t_start=a["t_start"],
+                            nghost=a["nghost"], max_level=a["max_level"],
+                            blocking_factor=a["blocking_factor"],
+                            max_grid_size=a["max_grid_size"], n_error_buf=a["n_error_buf"],
+                            regrid_dt=a["regrid_dt"], te_crit=[a["te_crit"]] * 4,
+                            params=a["params"],
+                            string_width_threshold=a["string_width_threshold"])
+        sim = sh.Amr(ctx, cfg, ic.axion_string_ic(64, 16.0, kmax=1.0, seed=0))
+        sim.step(40)
+        sim.close()
+    elif name == "single":
+        s = SINGLE
+        lv = sh.Level.periodic(ctx, s["project"], s["N"], s["nghost"])
+        lv.write(single_state())
+        lv.set_time(s["eta0"])
+        dx = s["L"] / s["N"]
+        for _ in range(3):
+            lv.advance(sh.RKN4, 0.25 * dx, dx, params=s["params"])
+        lv.close()
+    else:
+        raise SystemExit(f"unknown case {name}")
+    ctx.synchronize()
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -626,7 +679,13 @@ def main():
                     help="comma list of the chosen-form legs reported beside the headline "
                          "(ensemble, fopt, serve; empty for none)")
     ap.add_argument("--serve-max-n", type=int, default=SERVE["max_n"])
+    ap.add_argument("--case", default=None,
+                    help="run one small profiling case and exit: axion-fp32k, axion-fp64, "
+                         "fopt-fp32k, amr, single")
     args = ap.parse_args()
+    if args.case:
+        run_case(args.case)
+        return
     if args.steps is None:
         args.steps = 91 if args.workload == "amr" else 20
     args.warmup = max(args.warmup, 3)

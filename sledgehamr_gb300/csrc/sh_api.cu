@@ -76,6 +76,7 @@ struct CopyItem {
 };
 struct CfItem {
     long long dst, dgvol;
+    long long first; /* running coarse-fine cell count of the first cell */
     int dsy, dsz;
     int lo[3]; /* fine index of the first cell */
     int nx, ny, nz;
@@ -100,7 +101,13 @@ struct sh_ctx {
 };
 
 struct sh_level {
-    long long uid = 0; /* unique per level object of the process */
+    long long uid = 0;     /* unique per level object of the process */
+    long long version = 0; /* bumped by every call that may write the buffers */
+    /* coarse-fine ghost values interpolated in space from the coarse level's
+     * old and new data (cf_cells x ncomp each), valid for the coarse level
+     * with uid cf_uid at version cf_ver */
+    double *cf_old = nullptr, *cf_new = nullptr;
+    long long cf_uid = -1, cf_ver = -1;
     /* average-down plan onto the level with uid avg_for (a cache) */
     mutable long long avg_for = -1;
     mutable void *d_avg = nullptr; /* AvgRect list */
@@ -366,7 +373,8 @@ struct OwnerMapDev {
  * block map; its neighbours are read from the parent box's ghost cells. */
 __global__ void cf_interp_kernel(const CfItem *items, const BoxDev *cboxes, double *fbuf,
                                  OwnerMapDev cmap, const double *c_old, const double *c_new,
-                                 int mode, double alpha, double beta, int ncomp) {
+                                 int mode, double alpha, double beta, int ncomp, double *store,
+                                 long long ncf) {
     const CfItem it = items[blockIdx.x];
     auto fl2 = [](int a) { return a >= 0 ? a / 2 : -((-a + 1) / 2); };
     const int lo[3] = {it.lo[0], it.lo[1], it.lo[2]};
@@ -425,11 +433,40 @@ __global__ void cf_interp_kernel(const CfItem *items, const BoxDev *cboxes, doub
                         const double xi = (fi - 2 * P[0]) ? 0.25 : -0.25;
                         const double v = u0 + xi * Dx + yi * Dy + zi * Dz + Q + xi * yi * Dxy +
                                          xi * zi * Dxz + yi * zi * Dyz;
-                        fbuf[it.dst + (fi - lo[0]) + (long long)(fj - lo[1]) * it.dsy +
-                             (long long)(fk - lo[2]) * it.dsz + nn * it.dgvol] = v;
+                        if (store)
+                            store[it.first + (fi - lo[0]) +
+                                  (long long)it.nx * ((fj - lo[1]) + (long long)it.ny * (fk - lo[2])) +
+                                  nn * ncf] = v;
+                        else
+                            fbuf[it.dst + (fi - lo[0]) + (long long)(fj - lo[1]) * it.dsy +
+                                 (long long)(fk - lo[2]) * it.dsz + nn * it.dgvol] = v;
                     }
                 }
             }
+        }
+    }
+}
+
+/* Coarse-fine ghost cells from the stored spatial interpolations of the
+ * coarse old and new data: the interpolation is linear in the coarse data,
+ * so interpolating alpha old + beta new equals alpha I(old) + beta I(new). */
+__global__ void cf_combine_kernel(const CfItem *items, double *fbuf, const double *i_old,
+                                  const double *i_new, int mode, double alpha, double beta,
+                                  int ncomp, long long ncf) {
+    const CfItem it = items[blockIdx.x];
+    const int n = it.nx * it.ny * it.nz;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        const int i = q % it.nx, r = q / it.nx;
+        const int j = r % it.ny, k = r / it.ny;
+        const long long d = it.dst + i + (long long)j * it.dsy + (long long)k * it.dsz;
+        const long long c = it.first + q;
+        for (int nn = 0; nn < ncomp; ++nn) {
+            const long long e = c + nn * ncf;
+            double v;
+            if (mode == 0) v = i_old[e];
+            else if (mode == 1) v = i_new[e];
+            else v = alpha * i_old[e] + beta * i_new[e];
+            fbuf[d + nn * it.dgvol] = v;
         }
     }
 }
@@ -986,10 +1023,13 @@ std::vector<CopyItem> copy_items(const std::vector<GhostCopyDev> &rects, const s
 std::vector<CfItem> cf_items(const std::vector<CfRect> &rects, const sh_level *D) {
     std::vector<CfItem> items;
     items.reserve(rects.size());
+    long long first = 0;
     for (const CfRect &r : rects) {
         const BoxDev &db = D->hboxes[r.dbox];
         split_rect(r.lo, r.hi, [&](int x, int y, int z, int nx, int ny, int nz) {
             CfItem it;
+            it.first = first;
+            first += (long long)nx * ny * nz;
             it.dst = cell_offset(db, D->ncomp, x, y, z);
             it.dgvol = db.gvol;
             it.dsy = db.gdim[0];
@@ -1046,6 +1086,8 @@ void level_free(sh_ctx *ctx, sh_level *L) {
     dfree_async(ctx, L->d_cf);
     dfree_async(ctx, L->d_owner);
     dfree_async(ctx, L->d_avg);
+    dfree_async(ctx, L->cf_old);
+    dfree_async(ctx, L->cf_new);
     for (int q = 0; q < 3; ++q) dfree_async(ctx, L->buf[q]);
     dfree_async(ctx, L->kbuf);
 }
@@ -1074,12 +1116,30 @@ void fill_patch(sh_ctx *ctx, sh_level *L, double *buf, double t) {
     }
     if (L->coarse && L->ncf_items > 0) {
         ProfScope ps(ctx, kProfCf);
+        const sh_level *C = L->coarse;
+        if (L->cf_uid != C->uid || L->cf_ver != C->version) {
+            /* spatial interpolation of the coarse old and new data, once per
+             * coarse data version (every fine sub-step and stage between two
+             * coarse steps reuses it) */
+            if (!L->cf_old) {
+                const size_t bytes = (size_t)L->ncf * L->ncomp * sizeof(double);
+                L->cf_old = (double *)dmalloc_async(ctx, bytes, "coarse-fine values");
+                L->cf_new = (double *)dmalloc_async(ctx, bytes, "coarse-fine values");
+            }
+            for (int m = 0; m < 2; ++m) {
+                cf_interp_kernel<<<L->ncf_items, 128, 0, ctx->stream>>>(
+                    L->d_cf, C->d_boxes, nullptr, owner_map_dev(C), C->buf[SH_OLD],
+                    C->buf[SH_NEW], m, 0., 0., L->ncomp, m == 0 ? L->cf_old : L->cf_new, L->ncf);
+                ctx->launches++;
+            }
+            L->cf_uid = C->uid;
+            L->cf_ver = C->version;
+        }
         int mode;
         double alpha, beta;
-        coarse_time_weights(L->coarse, t, mode, alpha, beta);
-        cf_interp_kernel<<<L->ncf_items, 128, 0, ctx->stream>>>(
-            L->d_cf, L->coarse->d_boxes, buf, owner_map_dev(L->coarse), L->coarse->buf[SH_OLD],
-            L->coarse->buf[SH_NEW], mode, alpha, beta, L->ncomp);
+        coarse_time_weights(C, t, mode, alpha, beta);
+        cf_combine_kernel<<<L->ncf_items, 128, 0, ctx->stream>>>(
+            L->d_cf, buf, L->cf_old, L->cf_new, mode, alpha, beta, L->ncomp, L->ncf);
         ctx->launches++;
         ck(cudaGetLastError(), "coarse-fine fill launch");
     }
@@ -1606,6 +1666,7 @@ int sh_level_set_time(sh_level *L, int which, double t, int istep) {
 int sh_level_write(sh_ctx *ctx, sh_level *L, int which, int layout, const double *host) {
     if (!ctx || !L || !host || (which != SH_NEW && which != SH_OLD)) return SH_ERR_ARG;
     return guarded(ctx, [&] {
+        L->version++;
         set_device(ctx);
         const size_t bytes = (size_t)L->nvalid * L->ncomp * sizeof(double);
         double *stage = (double *)ctx_scratch(ctx, bytes);
@@ -1630,6 +1691,7 @@ int sh_level_read(sh_ctx *ctx, const sh_level *L, int which, int layout, double 
 int sh_level_write_device(sh_ctx *ctx, sh_level *L, int which, int layout, const double *dev) {
     if (!ctx || !L || !dev || (which != SH_NEW && which != SH_OLD)) return SH_ERR_ARG;
     return guarded(ctx, [&] {
+        L->version++;
         set_device(ctx);
         move(ctx, L, L->buf[which], const_cast<double *>(dev), layout, 0);
     });
@@ -1646,6 +1708,7 @@ int sh_level_read_device(sh_ctx *ctx, const sh_level *L, int which, int layout, 
 int sh_level_fill_patch(sh_ctx *ctx, sh_level *L, int which) {
     if (!ctx || !L || (which != SH_NEW && which != SH_OLD)) return SH_ERR_ARG;
     return guarded(ctx, [&] {
+        L->version++;
         set_device(ctx);
         fill_patch(ctx, L, L->buf[which], L->t[which]);
     });
@@ -1657,6 +1720,10 @@ int sh_level_set_coarse(sh_ctx *ctx, sh_level *fine, sh_level *coarse) {
         set_device(ctx);
         dfree_async(ctx, fine->d_cf);
         fine->d_cf = nullptr;
+        dfree_async(ctx, fine->cf_old);
+        dfree_async(ctx, fine->cf_new);
+        fine->cf_old = fine->cf_new = nullptr;
+        fine->cf_uid = fine->cf_ver = -1;
         fine->ncf = 0;
         fine->ncf_items = 0;
         fine->coarse = nullptr;
@@ -1676,6 +1743,7 @@ int sh_level_fill_from(sh_ctx *ctx, sh_level *dst, int which_dst, const sh_level
     if (!ctx || !dst || (which_dst != SH_NEW && which_dst != SH_OLD)) return SH_ERR_ARG;
     if (src && which_src != SH_NEW && which_src != SH_OLD) return SH_ERR_ARG;
     return guarded(ctx, [&] {
+        dst->version++;
         set_device(ctx);
         require(src != dst, "source and destination must differ");
         if (src) require(src->ncomp == dst->ncomp, "source differs in components");
@@ -1701,7 +1769,8 @@ int sh_level_fill_from(sh_ctx *ctx, sh_level *dst, int which_dst, const sh_level
             ProfScope ps(ctx, kProfCf);
             cf_interp_kernel<<<(int)items.size(), 128, 0, ctx->stream>>>(
                 d_cf, coarse->d_boxes, dst->buf[which_dst], owner_map_dev(coarse),
-                coarse->buf[SH_OLD], coarse->buf[SH_NEW], mode, alpha, beta, dst->ncomp);
+                coarse->buf[SH_OLD], coarse->buf[SH_NEW], mode, alpha, beta, dst->ncomp, nullptr,
+                0);
             ctx->launches++;
             ck(cudaGetLastError(), "coarse fill launch");
         }
@@ -1716,6 +1785,7 @@ int sh_level_advance(sh_ctx *ctx, sh_level *L, int integrator, const double *tab
                      int flags) {
     if (!ctx || !L) return SH_ERR_ARG;
     return guarded(ctx, [&] {
+        L->version++;
         set_device(ctx);
         require(dt > 0 && dx > 0, "dt and dx must be positive");
         if (!(flags & SH_ADVANCE_NO_SWAP)) {
@@ -1737,6 +1807,7 @@ int sh_level_rhs(sh_ctx *ctx, sh_level *L, int which, double time, int lev, doub
                  int ko_order, const double *ko_strength, double *host_rhs) {
     if (!ctx || !L || !host_rhs || (which != SH_NEW && which != SH_OLD)) return SH_ERR_ARG;
     return guarded(ctx, [&] {
+        L->version++;
         set_device(ctx);
         StageArgs a;
         fill_common(a, L, dt, dx, params, nparams, gw_params, ngw, ko_order, ko_strength);
@@ -1764,6 +1835,7 @@ int sh_level_add_bubbles(sh_ctx *ctx, sh_level *L, int which, int comp_phi, int 
         return SH_ERR_ARG;
     if (nb == 0) return SH_OK;
     return guarded(ctx, [&] {
+        L->version++;
         set_device(ctx);
         require(comp_phi >= 0 && comp_phi < L->ncomp && comp_dphi >= 0 &&
                     comp_dphi < L->ncomp,
@@ -1795,6 +1867,7 @@ int sh_average_down(sh_ctx *ctx, const sh_level *F, int which_f, sh_level *C, in
     if ((which_f != SH_NEW && which_f != SH_OLD) || (which_c != SH_NEW && which_c != SH_OLD))
         return SH_ERR_ARG;
     return guarded(ctx, [&] {
+        C->version++;
         set_device(ctx);
         average_down_impl(ctx, F, F->buf[which_f], C, C->buf[which_c], nullptr);
     });
@@ -1803,6 +1876,8 @@ int sh_average_down(sh_ctx *ctx, const sh_level *F, int which_f, sh_level *C, in
 int sh_average_down_te(sh_ctx *ctx, sh_level *F, sh_level *C) {
     if (!ctx || !F || !C) return SH_ERR_ARG;
     return guarded(ctx, [&] {
+        C->version++;
+        F->version++;
         set_device(ctx);
         average_down_impl(ctx, F, F->buf[SH_NEW], C, C->buf[SH_NEW], F->buf[SH_OLD]);
     });

@@ -83,13 +83,27 @@ __device__ __forceinline__ void kahan_add(R &y, R d, R &c) {
 
 /* RKN4 stage kernel for the axion family.  ORDER: Laplacian order (1: 7
  * points, 2: 13 points).  STAGE 0 and 1 write K_STAGE; STAGE 2 writes the
- * new state. */
+ * new state.
+ *
+ * Software pipeline: the loads of the next plane (y0, y0', K) are issued
+ * into registers before the current plane is computed and are combined
+ * into the stage positions and stored into the ring at the start of the
+ * next iteration; the centre values the epilogue needs are issued before
+ * the barrier.  The ring has one slot more than the stencil reads, so one
+ * barrier per plane suffices (a thread storing plane z+1 overwrites plane
+ * z-2H-1, which no thread still reads once all passed the barrier of z).
+ * The per-block constants (stage time, friction, couplings, 1/dx^2) are
+ * formed once in FP64 by one thread: FP64 work per thread would run on
+ * GB300's narrow FP64 pipe. */
 template <class R, int ORDER, int STAGE, bool KAHAN>
 __global__ void __launch_bounds__(TX *TY) axion_rkn4_kernel(const __grid_constant__ AxionArgs<R> a) {
     constexpr int H = ORDER;             /* halo */
-    constexpr int RING = 2 * H + 1;
+    constexpr int RING = 2 * H + 2;
     constexpr int W = TX + 2 * H, HH = TY + 2 * H;
+    constexpr int NT = TX * TY;
+    constexpr int NPL = (W * HH + NT - 1) / NT; /* plane elements per thread */
     __shared__ R ring[RING][2][HH][W];
+    __shared__ R kc[10];
 
     const FastTile tl = a.tiles[blockIdx.x];
     const RealDesc d = a.desc[tl.r];
@@ -101,42 +115,102 @@ __global__ void __launch_bounds__(TX *TY) axion_rkn4_kernel(const __grid_constan
 
     /* RKN4 tableau (rkn.cpp:130-139): c = {0, 1/2, 1}; a21 = 1/8; a32 = 1/2;
      * bbar = {1/6, 1/3, 0}; b = {1/6, 2/3, 1/6}. */
-    const double hh = a.h * a.h;
-    const R cm = (R)(STAGE == 0 ? 0. : (STAGE == 1 ? 0.5 * a.h : a.h));
-    const R ck = (R)(STAGE == 1 ? hh / 8. : (STAGE == 2 ? hh / 2. : 0.));
-    const double t0 = a.time[a.slot];
-    const double ts = t0 + a.h * (STAGE == 0 ? 0. : (STAGE == 1 ? 0.5 : 1.));
-    if (STAGE == 2 && blockIdx.x == 0 && tid == 0) a.time[1 - a.slot] = t0 + a.h;
-    const R friction = (R)(-2. / ts);
-    const R lam = (R)d.p[0];
-    const R cst = (R)d.p[1];
-    const R eta2 = (R)(ts * ts);
-    const R inv_dx2 = (R)(1. / (d.dx * d.dx));
+    if (tid == 0) {
+        const double hh = a.h * a.h;
+        const double t0 = a.time[a.slot];
+        const double ts = t0 + a.h * (STAGE == 0 ? 0. : (STAGE == 1 ? 0.5 : 1.));
+        if (STAGE == 2 && blockIdx.x == 0) a.time[1 - a.slot] = t0 + a.h;
+        kc[0] = (R)(STAGE == 0 ? 0. : (STAGE == 1 ? 0.5 * a.h : a.h)); /* cm */
+        kc[1] = (R)(STAGE == 1 ? hh / 8. : (STAGE == 2 ? hh / 2. : 0.)); /* ck */
+        kc[2] = (R)(-2. / ts);                                            /* friction */
+        kc[3] = (R)d.p[0];                                                /* lambda */
+        kc[4] = (R)d.p[1];                                                /* c */
+        kc[5] = (R)(ts * ts);                                             /* eta^2 */
+        const R inv_dx2 = (R)(1. / (d.dx * d.dx));
+        kc[6] = inv_dx2;
+        kc[7] = inv_dx2 / (R)12;
+        kc[8] = (R)a.h;
+        kc[9] = (R)hh;
+    }
+    __syncthreads();
+    const R cm = kc[0], ck = kc[1], friction = kc[2], lam = kc[3], cst = kc[4], eta2 = kc[5];
+    const R inv_dx2 = kc[6], inv12dx2 = kc[7];
     const R* Kin = STAGE == 1 ? a.K[0][0] : (STAGE == 2 ? a.K[1][0] : nullptr);
     const R* Kin2 = STAGE == 1 ? a.K[0][1] : (STAGE == 2 ? a.K[1][1] : nullptr);
 
-    auto load_plane = [&](int z, int slot) {
+    /* plane element q of this thread: ring position and periodic source */
+    int ppos[NPL], pgx[NPL], pgy[NPL];
+#pragma unroll
+    for (int q = 0; q < NPL; ++q) {
+        const int p = tid + q * NT;
+        ppos[q] = p < W * HH ? p : -1;
+        const int px = p % W, py = p / W;
+        pgx[q] = wrap(tl.x0 - H + px, N);
+        pgy[q] = wrap(tl.y0 - H + py, N);
+    }
+    R raw[NPL][6]; /* y0 (2), y0' (2), K (2) of the next plane */
+    auto fetch = [&](int z) {
         const int zw = wrap(z, N);
-        for (int p = tid; p < W * HH; p += TX * TY) {
-            const int px = p % W, py = p / W;
-            const int gx = wrap(tl.x0 - H + px, N), gy = wrap(tl.y0 - H + py, N);
-            const long long e = off + ((long long)zw * N + gy) * N + gx;
-            R v0 = a.y0[0][e], v1 = a.y0[1][e];
+#pragma unroll
+        for (int q = 0; q < NPL; ++q) {
+            if (ppos[q] < 0) continue;
+            const long long e = off + ((long long)zw * N + pgy[q]) * N + pgx[q];
+            raw[q][0] = a.y0[0][e];
+            raw[q][1] = a.y0[1][e];
             if (STAGE > 0) {
-                v0 += cm * a.m0[0][e] + ck * Kin[e];
-                v1 += cm * a.m0[1][e] + ck * Kin2[e];
+                raw[q][2] = a.m0[0][e];
+                raw[q][3] = a.m0[1][e];
+                raw[q][4] = Kin[e];
+                raw[q][5] = Kin2[e];
             }
+        }
+    };
+    auto commit = [&](int slot) {
+#pragma unroll
+        for (int q = 0; q < NPL; ++q) {
+            if (ppos[q] < 0) continue;
+            R v0 = raw[q][0], v1 = raw[q][1];
+            if (STAGE > 0) {
+                v0 += cm * raw[q][2] + ck * raw[q][4];
+                v1 += cm * raw[q][3] + ck * raw[q][5];
+            }
+            const int px = ppos[q] % W, py = ppos[q] / W;
             ring[slot][0][py][px] = v0;
             ring[slot][1][py][px] = v1;
         }
     };
 
     const int zb = tl.z0 - H, ze = tl.z0 + tl.nz + H; /* planes [zb, ze) */
+    fetch(zb);
     for (int z = zb; z < ze; ++z) {
-        load_plane(z, (z - zb) % RING);
-        __syncthreads();
         const int zc = z - H;
-        if (zc >= tl.z0 && active) {
+        const bool out = zc >= tl.z0 && active;
+        const long long e = off + ((long long)zc * N + y) * N + x;
+        /* centre values of the plane computed below */
+        R q0 = 0, q1 = 0, ka0 = 0, ka1 = 0, kb0 = 0, kb1 = 0, y0c = 0, y1c = 0;
+        R c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+        if (out) {
+            q0 = a.m0[0][e];
+            q1 = a.m0[1][e];
+            if (STAGE == 2) {
+                ka0 = a.K[0][0][e];
+                ka1 = a.K[0][1][e];
+                kb0 = a.K[1][0][e];
+                kb1 = a.K[1][1][e];
+                y0c = a.y0[0][e];
+                y1c = a.y0[1][e];
+                if (KAHAN) {
+                    c0 = a.cy[0][e];
+                    c1 = a.cy[1][e];
+                    c2 = a.cm[0][e];
+                    c3 = a.cm[1][e];
+                }
+            }
+        }
+        commit((z - zb) % RING);
+        if (z + 1 < ze) fetch(z + 1);
+        __syncthreads();
+        if (out) {
             const int sc = (zc - zb) % RING;
             R lap[2];
 #pragma unroll
@@ -157,12 +231,10 @@ __global__ void __launch_bounds__(TX *TY) axion_rkn4_kernel(const __grid_constan
                     s2 += ring[sc][c][ty + H + 2][tx + H] + ring[sc][c][ty + H - 2][tx + H];
                     s2 += ring[(sc + 2) % RING][c][ty + H][tx + H] +
                           ring[(sc + RING - 2) % RING][c][ty + H][tx + H];
-                    lap[c] = ((R)16 * s1 - s2 - (R)90 * u0) * (inv_dx2 / (R)12);
+                    lap[c] = ((R)16 * s1 - s2 - (R)90 * u0) * inv12dx2;
                 }
             }
-            const long long e = off + ((long long)zc * N + y) * N + x;
             const R p0 = ring[sc][0][ty + H][tx + H], p1 = ring[sc][1][ty + H][tx + H];
-            const R q0 = a.m0[0][e], q1 = a.m0[1][e];
             const R v = lam * (eta2 * (p0 * p0 + p1 * p1 - (R)1) + cst);
             const R k0 = friction * q0 + lap[0] - p0 * v;
             const R k1 = friction * q1 + lap[1] - p1 * v;
@@ -170,17 +242,14 @@ __global__ void __launch_bounds__(TX *TY) axion_rkn4_kernel(const __grid_constan
                 a.K[STAGE][0][e] = k0;
                 a.K[STAGE][1][e] = k1;
             } else {
-                const R h = (R)a.h, h2 = (R)hh;
-                const R ka0 = a.K[0][0][e], ka1 = a.K[0][1][e];
-                const R kb0 = a.K[1][0][e], kb1 = a.K[1][1][e];
+                const R h = kc[8], h2 = kc[9];
                 /* y1 = y0 + h y0' + h^2 (K0/6 + K1/3); y1' = y0' + h (K0/6 + 2K1/3 + K2/6) */
                 const R dy0 = h * q0 + h2 * (ka0 * (R)(1. / 6.) + kb0 * (R)(1. / 3.));
                 const R dy1 = h * q1 + h2 * (ka1 * (R)(1. / 6.) + kb1 * (R)(1. / 3.));
                 const R dm0 = h * ((ka0 + k0) * (R)(1. / 6.) + kb0 * (R)(2. / 3.));
                 const R dm1 = h * ((ka1 + k1) * (R)(1. / 6.) + kb1 * (R)(2. / 3.));
-                R y0v = a.y0[0][e], y1v = a.y0[1][e], m0v = q0, m1v = q1;
+                R y0v = y0c, y1v = y1c, m0v = q0, m1v = q1;
                 if (KAHAN) {
-                    R c0 = a.cy[0][e], c1 = a.cy[1][e], c2 = a.cm[0][e], c3 = a.cm[1][e];
                     kahan_add(y0v, dy0, c0);
                     kahan_add(y1v, dy1, c1);
                     kahan_add(m0v, dm0, c2);
@@ -201,7 +270,6 @@ __global__ void __launch_bounds__(TX *TY) axion_rkn4_kernel(const __grid_constan
                 a.m1[1][e] = m1v;
             }
         }
-        __syncthreads();
     }
 }
 
@@ -225,7 +293,7 @@ struct FoptArgs {
  * STAGE 1: a = f(x1); v1 = vh + dt/2 a.
  * Potential: dPhi' = lap Phi + q2 Phi + q3 Phi^2 + q4 Phi^3 (p[0..2]). */
 template <class R, int STAGE, bool KAHAN>
-__global__ void __launch_bounds__(TX *TY) fopt_leapfrog_kernel(const __grid_constant__ FoptArgs<R> a) {
+__global__ void __launch_bounds__(TX *TY, sizeof(R) == 4 ? 3 : 1) fopt_leapfrog_kernel(const __grid_constant__ FoptArgs<R> a) {
     constexpr int H = 2, RING = 5, W = TX + 2 * H, HH = TY + 2 * H, NC = 7;
     extern __shared__ unsigned char smem_raw[];
     R(*ring)[NC][HH][W] = reinterpret_cast<R(*)[NC][HH][W]>(smem_raw);
@@ -237,29 +305,73 @@ __global__ void __launch_bounds__(TX *TY) fopt_leapfrog_kernel(const __grid_cons
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
     const int x = tl.x0 + tx, y = tl.y0 + ty;
     const bool active = x < N && y < N;
-    const R q2 = (R)d.p[0], q3 = (R)d.p[1], q4 = (R)d.p[2];
-    const R inv12dx2 = (R)(1. / (12. * d.dx * d.dx));
-    const R inv12dx = (R)(1. / (12. * d.dx));
-    const double sdt = a.dt > 0. ? a.dt : d.dt; /* pools: every member its own step */
-    const R hdt = (R)(0.5 * sdt), dt = (R)sdt;
-    if (STAGE == 1 && blockIdx.x == 0 && tid == 0) a.time[1 - a.slot] = a.time[a.slot] + a.dt;
+    __shared__ R kc[7];
+    if (tid == 0) {
+        const double sdt = a.dt > 0. ? a.dt : d.dt; /* pools: every member its own step */
+        kc[0] = (R)d.p[0];
+        kc[1] = (R)d.p[1];
+        kc[2] = (R)d.p[2];
+        kc[3] = (R)(1. / (12. * d.dx * d.dx));
+        kc[4] = (R)(1. / (12. * d.dx));
+        kc[5] = (R)(0.5 * sdt);
+        kc[6] = (R)sdt;
+        if (STAGE == 1 && blockIdx.x == 0) a.time[1 - a.slot] = a.time[a.slot] + a.dt;
+    }
+    __syncthreads();
+    const R q2 = kc[0], q3 = kc[1], q4 = kc[2], inv12dx2 = kc[3], inv12dx = kc[4];
+    const R hdt = kc[5], dt = kc[6];
 
-    auto load_plane = [&](int z, int slot) {
-        const int zw = wrap(z, N);
-        for (int p = tid; p < W * HH; p += TX * TY) {
-            const int px = p % W, py = p / W;
-            const int gx = wrap(tl.x0 - H + px, N), gy = wrap(tl.y0 - H + py, N);
-            const long long e = off + ((long long)zw * N + gy) * N + gx;
+    /* software pipeline: the next plane's loads are issued into registers
+     * before the current plane is computed */
+    constexpr int NT = TX * TY;
+    constexpr int NPL = (W * HH + NT - 1) / NT;
+    int ppos[NPL];
+    long long pxy[NPL]; /* in-plane offset of the periodic source cell */
 #pragma unroll
-            for (int c = 0; c < NC; ++c) ring[slot][c][py][px] = a.x[c][e];
+    for (int q = 0; q < NPL; ++q) {
+        const int p = tid + q * NT;
+        ppos[q] = p < W * HH ? p : -1;
+        const int gx = wrap(tl.x0 - H + p % W, N), gy = wrap(tl.y0 - H + p / W, N);
+        pxy[q] = (long long)gy * N + gx;
+    }
+    R raw[NPL][NC];
+    auto fetch = [&](int z) {
+        const long long pz = off + (long long)wrap(z, N) * N * N;
+#pragma unroll
+        for (int q = 0; q < NPL; ++q) {
+            if (ppos[q] < 0) continue;
+#pragma unroll
+            for (int c = 0; c < NC; ++c) raw[q][c] = a.x[c][pz + pxy[q]];
+        }
+    };
+    auto commit = [&](int slot) {
+#pragma unroll
+        for (int q = 0; q < NPL; ++q) {
+            if (ppos[q] < 0) continue;
+            const int px = ppos[q] % W, py = ppos[q] / W;
+#pragma unroll
+            for (int c = 0; c < NC; ++c) ring[slot][c][py][px] = raw[q][c];
         }
     };
     const int zb = tl.z0 - H, ze = tl.z0 + tl.nz + H;
+    fetch(zb);
     for (int z = zb; z < ze; ++z) {
-        load_plane(z, (z - zb) % RING);
-        __syncthreads();
         const int zc = z - H;
-        if (zc >= tl.z0 && active) {
+        const bool outp = zc >= tl.z0 && active;
+        const long long e = off + ((long long)zc * N + y) * N + x;
+        /* centre values of the plane computed below */
+        R cv_[NC], cc_[NC], cx_c[NC];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            cv_[c] = outp ? a.v[c][e] : (R)0;
+            cc_[c] = (outp && KAHAN) ? a.cv[c][e] : (R)0;
+            cx_c[c] = (outp && KAHAN && STAGE == 0) ? a.cx[c][e] : (R)0;
+        }
+        __syncthreads(); /* the slot about to be written is no longer read */
+        commit((z - zb) % RING);
+        if (z + 1 < ze) fetch(z + 1);
+        __syncthreads();
+        if (outp) {
             const int s0 = (zc - zb) % RING;
             const int sp1 = (s0 + 1) % RING, sp2 = (s0 + 2) % RING;
             const int sm1 = (s0 + RING - 1) % RING, sm2 = (s0 + RING - 2) % RING;
@@ -292,12 +404,11 @@ __global__ void __launch_bounds__(TX *TY) fopt_leapfrog_kernel(const __grid_cons
             acc[4] += g[0] * g[1];
             acc[5] += g[0] * g[2];
             acc[6] += g[1] * g[2];
-            const long long e = off + ((long long)zc * N + y) * N + x;
 #pragma unroll
             for (int c = 0; c < NC; ++c) {
-                R vv = a.v[c][e];
+                R vv = cv_[c];
                 if (KAHAN) {
-                    R cvv = a.cv[c][e];
+                    R cvv = cc_[c];
                     kahan_add(vv, hdt * acc[c], cvv);
                     a.cv[c][e] = cvv;
                 } else {
@@ -307,7 +418,7 @@ __global__ void __launch_bounds__(TX *TY) fopt_leapfrog_kernel(const __grid_cons
                 if (STAGE == 0) {
                     R xx = ring[s0][c][cy_][cx_];
                     if (KAHAN) {
-                        R cxx = a.cx[c][e];
+                        R cxx = cx_c[c];
                         kahan_add(xx, dt * vv, cxx);
                         a.cx[c][e] = cxx;
                     } else {
@@ -317,7 +428,6 @@ __global__ void __launch_bounds__(TX *TY) fopt_leapfrog_kernel(const __grid_cons
                 }
             }
         }
-        __syncthreads();
     }
 }
 
