@@ -675,7 +675,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="amr", choices=["amr", "single"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--forms", default="ensemble",
+    ap.add_argument("--forms", default="ensemble,fopt,serve",
                     help="comma list of the chosen-form legs reported beside the headline "
                          "(ensemble, fopt, serve; empty for none)")
     ap.add_argument("--serve-max-n", type=int, default=SERVE["max_n"])
