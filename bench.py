@@ -618,8 +618,9 @@ def run_case(name):
     """Small fixed cases for profiler captures (no timing, no output line):
     axion-fp32k / axion-fp64: one 256^3 axion realisation, 3 RKN4 steps
     (9 stage launches); fopt-fp32k: one 192^3 FOPT + GW realisation, 3
-    leapfrog steps; amr: the AMR workload at N0 = 64 (L = 16), 40 coarse
-    steps; single: the 128^3 FP64 level, 3 RKN4 steps."""
+    leapfrog steps; amr / amr128: the AMR workload at N0 = 64 (L = 16), 40
+    coarse steps, or N0 = 128 (L = 32), 60 coarse steps; single: the 128^3
+    FP64 level, 3 RKN4 steps."""
     import sledgehamr_gb300 as sh
     from sledgehamr_gb300 import ic
     ctx = sh.Context(0)
@@ -640,17 +641,18 @@ def run_case(name):
         E.write(0, st)
         E.step(0.05, 3)
         E.close()
-    elif name == "amr":
+    elif name in ("amr", "amr128"):
         a = AMR
-        cfg = sh.amr_config(a["project"], N0=64, L=16.0, cfl=a["cfl"], t_start=a["t_start"],
+        n0 = 64 if name == "amr" else 128
+        cfg = sh.amr_config(a["project"], N0=n0, L=n0 * 0.25, cfl=a["cfl"], t_start=a["t_start"],
                             nghost=a["nghost"], max_level=a["max_level"],
                             blocking_factor=a["blocking_factor"],
                             max_grid_size=a["max_grid_size"], n_error_buf=a["n_error_buf"],
                             regrid_dt=a["regrid_dt"], te_crit=[a["te_crit"]] * 4,
                             params=a["params"],
                             string_width_threshold=a["string_width_threshold"])
-        sim = sh.Amr(ctx, cfg, ic.axion_string_ic(64, 16.0, kmax=1.0, seed=0))
-        sim.step(40)
+        sim = sh.Amr(ctx, cfg, ic.axion_string_ic(n0, n0 * 0.25, kmax=1.0, seed=0))
+        sim.step(40 if name == "amr" else 60)
         sim.close()
     elif name == "single":
         s = SINGLE
@@ -681,7 +683,7 @@ def main():
     ap.add_argument("--serve-max-n", type=int, default=SERVE["max_n"])
     ap.add_argument("--case", default=None,
                     help="run one small profiling case and exit: axion-fp32k, axion-fp64, "
-                         "fopt-fp32k, amr, single")
+                         "fopt-fp32k, amr, amr128, single")
     args = ap.parse_args()
     if args.case:
         run_case(args.case)

@@ -136,6 +136,8 @@ SH_API int sh_level_create(sh_ctx *ctx, int project, int with_gw, const int doma
                     const int domain_hi[3], const sh_box *boxes, int nbox, int nghost,
                     sh_level **out);
 SH_API int sh_level_destroy(sh_ctx *ctx, sh_level *level);
+/* Index domain of a level (lo, hi inclusive). */
+SH_API int sh_level_domain(const sh_level *level, int lo[3], int hi[3]);
 SH_API int sh_level_info(const sh_level *level, int *ncomp, int *nbox, long long *nvalid_cells);
 SH_API int sh_level_time(const sh_level *level, int which, double *t, int *istep);
 /* Box list of a level (capacity boxes; *nbox receives the count). */
@@ -198,6 +200,36 @@ SH_API int sh_level_advance(sh_ctx *ctx, sh_level *level, int integrator, const 
 SH_API int sh_level_rhs(sh_ctx *ctx, sh_level *level, int which, double time, int lev, double dt,
                  double dx, const double *params, int nparams, const double *gw_params,
                  int ngw, int ko_order, const double *ko_strength, double *host_rhs);
+
+/* Output functions for projections and scalar spectra (the projects'
+ * io_module->projections / ->spectra functions, evaluated on the device):
+ * a component, its square (FirstOrderPhaseTransition dPhi2 with comp 1),
+ * and the AxionStrings densities of kernels_energy_densities.h (components
+ * Psi1 Psi2 Pi1 Pi2 at 0..3; a_prime2 is also NextToMinimalExample's
+ * a_dot_sq). */
+#define SH_OUT_COMPONENT 0
+#define SH_OUT_COMPONENT_SQ 1
+#define SH_OUT_A_PRIME2 2
+#define SH_OUT_A_PRIME_SCREENED 3
+#define SH_OUT_R_PRIME2 4
+
+/* Spectrum::Compute (source/output_types/spectrum.cpp:12-113) of a level
+ * covering its whole cubic periodic domain: the output function per cell,
+ * its R2C FFT, and per bin of the sorted unique k^2 (as sh_spectrum_bins)
+ * the sum of multpl |F|^2 times t / (N^6 dk), dk = 2 pi / (N dx), t the
+ * level's SH_NEW time, multpl = 1 on the x planes 0 and N/2, else 2. */
+SH_API int sh_scalar_spectrum(sh_ctx *ctx, const sh_level *level, int fn, int comp, double dx,
+                              double *bins_out, long long *ks_out, int max_bins, int *nbins);
+/* Projection::Compute / Add (source/output_types/projection.cpp:10-118):
+ * line-of-sight projection along z of the output function over levels
+ * 0..nlev-1 (SH_NEW data) onto the pixel grid of the finest one (dimN^2,
+ * data_out[x dimN + y]); a cell of level l not covered by level l+1 covers
+ * ratio^2 pixels (ratio = dimN / dimN_l); mode 0 sums ratio * value, mode 1
+ * keeps the maximum (starting from 0); n_out counts the contributions.
+ * Levels must cover periodic cubic domains starting at 0, each twice the
+ * previous. */
+SH_API int sh_projection(sh_ctx *ctx, const sh_level *const *levels, int nlev, int fn,
+                         int comp, int mode, double *data_out, int *n_out);
 
 /* FirstOrderPhaseTransition bubble injection (InjectBubbles ->
  * AddBubbleValues, projects/FirstOrderPhaseTransition/

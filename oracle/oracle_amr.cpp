@@ -418,3 +418,19 @@ int orc_amr_regrid_record(void *h, int q, int *lev, double *time, int *tagged, i
 }
 
 } /* extern "C" */
+
+/* Projection::Compute over the levels 0..min(max_level, finest) of the
+ * hierarchy (grid_new), orc::projection. */
+extern "C" int orc_amr_projection(void *h, int fn, int comp, int mode, int max_level,
+                                  double *data, int *nproj) {
+    AmrBase *a = (AmrBase *)h;
+    const int ml = std::min(max_level, a->finest());
+    std::vector<const MF *> lv;
+    for (int l = 0; l <= ml; ++l) lv.push_back(a->level(l, 0));
+    std::vector<double> d;
+    std::vector<int> n;
+    orc::projection(lv, fn, comp, mode, d, n);
+    std::copy(d.begin(), d.end(), data);
+    std::copy(n.begin(), n.end(), nproj);
+    return 0;
+}

@@ -98,3 +98,29 @@ extern "C" int orc_add_bubbles(int N, int ncomp, double *state, int comp_phi, in
             }
     return 0;
 }
+
+/* Spectrum::Compute on a periodic N^3 canonical state (orc::scalar_spectrum). */
+extern "C" int orc_scalar_spectrum(const double *state, int N, int ncomp, int fn, int comp,
+                                   double L, double t, double *bins_out, long long *ks_out,
+                                   int max_bins, int *nbins) {
+    if (N <= 0 || fn < 0 || fn > 4 || (fn <= 1 && (comp < 0 || comp >= ncomp)) ||
+        (fn >= 2 && ncomp < 4))
+        return -1;
+    std::vector<long long> ks;
+    std::vector<double> s = orc::scalar_spectrum(state, N, ncomp, fn, comp, L, t, ks);
+    *nbins = (int)s.size();
+    if ((int)s.size() > max_bins) return -1;
+    std::copy(s.begin(), s.end(), bins_out);
+    if (ks_out) std::copy(ks.begin(), ks.end(), ks_out);
+    return 0;
+}
+
+/* The per-cell output function on every cell of a canonical state. */
+extern "C" int orc_out_function(const double *state, int N, int ncomp, int fn, int comp,
+                                double *out) {
+    if (N <= 0 || fn < 0 || fn > 4) return -1;
+    const long long n3 = (long long)N * N * N;
+    for (long long q = 0; q < n3; ++q) out[q] = orc::out_function(fn, comp, state + q, n3);
+    (void)ncomp;
+    return 0;
+}

@@ -766,6 +766,109 @@ inline std::vector<double> gw_spectrum(const std::vector<const double *> &comps6
     return out;
 }
 
+
+/* Per-cell output functions of the projects (values for projections and
+ * scalar spectra), components of the AxionStrings layout Psi1 Psi2 Pi1 Pi2
+ * (0..3) or one component `comp`:
+ *   0 state(comp)                    1 state(comp)^2 (FOPT dPhi2 with comp 1,
+ *                                      projects/FirstOrderPhaseTransition/
+ *                                      kernels_misc.h:10-18)
+ *   2 a'^2 = ((Psi1 Pi2 - Psi2 Pi1) / r^2)^2, r^2 = Psi1^2 + Psi2^2
+ *     (projects/AxionStrings/kernels_energy_densities.h:21-33; also
+ *     NextToMinimalExample a_dot_sq, NextToMinimalExample.h:49-61)
+ *   3 a'_screened = Psi1 Pi2 - Psi2 Pi1 (kernels_energy_densities.h:48-58)
+ *   4 r'^2 = (Psi1 Pi1 + Psi2 Pi2)^2 / r^2 (kernels_energy_densities.h:73-85) */
+inline double out_function(int fn, int comp, const double *v, long long stride) {
+    if (fn == 0) return v[comp * stride];
+    if (fn == 1) return v[comp * stride] * v[comp * stride];
+    const double Psi1 = v[0], Psi2 = v[stride], Pi1 = v[2 * stride], Pi2 = v[3 * stride];
+    if (fn == 2) {
+        double r2 = Psi1 * Psi1 + Psi2 * Psi2;
+        double prime_a = (Psi1 * Pi2 - Psi2 * Pi1) / r2;
+        return prime_a * prime_a;
+    }
+    if (fn == 3) return Psi1 * Pi2 - Psi2 * Pi1;
+    double r2 = Psi1 * Psi1 + Psi2 * Psi2;
+    double prime_r = Psi1 * Pi1 + Psi2 * Pi2;
+    return prime_r * prime_r / r2;
+}
+
+/* Spectrum::Compute (source/output_types/spectrum.cpp:12-113) for a
+ * periodic N^3 level given as a canonical array (ncomp components): the
+ * output function per cell, its R2C FFT, |F| (utils::Fft with abs,
+ * fft.h:244-250) and the sum of multpl * pre * |F| * |F| into the bins of
+ * the sorted unique k^2 (lower_bound), multpl = 1 on the x planes 0 and
+ * N/2, else 2, pre = t / (N^6 dk), dk = 2 pi / L. */
+inline std::vector<double> scalar_spectrum(const double *state, int N, int ncomp, int fn,
+                                           int comp, double L, double t,
+                                           std::vector<long long> &ks) {
+    (void)ncomp;
+    const long long n3 = (long long)N * N * N;
+    std::vector<double> f((size_t)n3);
+    for (long long q = 0; q < n3; ++q) f[q] = out_function(fn, comp, state + q, n3);
+    std::vector<std::complex<double>> F;
+    rfft3d(f.data(), N, F);
+    const int H = N / 2 + 1;
+    double fac = std::pow(1. / N, 6);
+    double dk = 2. * M_PI / L;
+    double pre = fac * t / dk;
+    ks = unique_k2(N);
+    std::vector<double> spectrum(ks.size(), 0.0);
+    /* loop order of the reference on one thread: i (x) outer, k (z) inner */
+    for (int a = 0; a < H; ++a)
+        for (int b = 0; b < N; ++b)
+            for (int c = 0; c < N; ++c) {
+                double multpl = (a == 0 || a == N / 2) ? 1. : 2.;
+                int li = a >= N / 2 ? a - N : a;
+                int lj = b >= N / 2 ? b - N : b;
+                int lk = c >= N / 2 ? c - N : c;
+                long long sq = (long long)li * li + (long long)lj * lj + (long long)lk * lk;
+                size_t index = std::lower_bound(ks.begin(), ks.end(), sq) - ks.begin();
+                const std::complex<double> &z = F[((size_t)c * N + b) * H + a];
+                double absF = std::sqrt(z.real() * z.real() + z.imag() * z.imag());
+                spectrum[index] += multpl * pre * absF * absF;
+            }
+    return spectrum;
+}
+
+/* Projection::Compute and Projection::Add (source/output_types/
+ * projection.cpp:10-118): line-of-sight projection along z onto the pixel
+ * grid of the finest of the given levels (levels[0..mlevel]); a cell of
+ * level lev not covered by level lev+1 (the cell (2i, 2j, 2k) in none of its
+ * boxes) covers ratio x ratio pixels, ratio = dimN / dimN_lev; mode 0 adds
+ * ratio * value, mode 1 keeps the maximum (data starts at 0); n counts the
+ * contributions.  Pixel index (i ratio + a) dimN + (j ratio + b). */
+inline void projection(const std::vector<const MF *> &levels, int fn, int comp, int mode,
+                       std::vector<double> &data, std::vector<int> &nproj) {
+    const int mlevel = (int)levels.size() - 1;
+    const int dimN = levels[mlevel]->domain.len(0);
+    data.assign((size_t)dimN * dimN, 0.0);
+    nproj.assign((size_t)dimN * dimN, 0);
+    for (int lev = 0; lev <= mlevel; ++lev) {
+        const MF &mf = *levels[lev];
+        const int ratio = dimN / mf.domain.len(0);
+        for (const Fab &f : mf.fabs) {
+            auto a = f.ca();
+            for (int k = f.vbox.lo.z; k <= f.vbox.hi.z; ++k)
+                for (int j = f.vbox.lo.y; j <= f.vbox.hi.y; ++j)
+                    for (int i = f.vbox.lo.x; i <= f.vbox.hi.x; ++i) {
+                        bool contd = lev == mlevel ||
+                                     find_fab(*levels[lev + 1], 2 * i, 2 * j, 2 * k) < 0;
+                        if (!contd) continue;
+                        const double val = out_function(fn, comp, &a(i, j, k, 0), a.ns);
+                        const int ii = i * ratio, jj = j * ratio;
+                        for (int ia = 0; ia < ratio; ++ia)
+                            for (int ja = 0; ja < ratio; ++ja) {
+                                const long long ind = (long long)(ii + ia) * dimN + (jj + ja);
+                                if (mode == 0) data[ind] += ratio * val;
+                                else if (mode == 1) data[ind] = std::max(data[ind], val);
+                                nproj[ind] += 1;
+                            }
+                    }
+        }
+    }
+}
+
 } // namespace orc
 
 #endif // SH_ORACLE_CORE_H_

@@ -12,6 +12,7 @@
 #include <AxionStrings/setup.h>
 #include <AxionStrings/kernels_rhs.h>
 #include <AxionStrings/kernels_tagging.h>
+#include <AxionStrings/kernels_energy_densities.h>
 #include <FirstOrderPhaseTransition/setup.h>
 #include <FirstOrderPhaseTransition/kernels_rhs.h>
 #include <FirstOrderPhaseTransition/kernels_tagging.h>
@@ -170,5 +171,27 @@ extern "C" int ref_add_bubbles(int N, int ncomp, double *state, int nb, const do
             for (int i = 0; i < N; ++i)
                 for (int b = 0; b < nb; ++b)
                     FirstOrderPhaseTransition::AddBubble(i, j, k, dx, L, fab, bubbles[b]);
+    return 0;
+}
+
+/* The reference's per-cell output functions on every cell of a canonical
+ * state: fn 1 with comp 1 = FirstOrderPhaseTransition dPhi2
+ * (kernels_misc.h:10-18), 2 = AxionStrings a_prime2, 3 = a_prime_screened,
+ * 4 = r_prime2 (kernels_energy_densities.h). */
+extern "C" int ref_out_function(const double *state, int N, int ncomp, int fn, double *out) {
+    const long long n3 = (long long)N * N * N;
+    amrex::Array4<double const> a(state, N, (long long)N * N, n3, amrex::Dim3{0, 0, 0}, ncomp);
+    std::vector<double> params;
+    for (int k = 0; k < N; ++k)
+        for (int j = 0; j < N; ++j)
+            for (int i = 0; i < N; ++i) {
+                double v = 0;
+                if (fn == 1) v = FirstOrderPhaseTransition::dPhi2(a, i, j, k, 0, 0., 0., 0., params);
+                else if (fn == 2) v = AxionStrings::a_prime2(a, i, j, k, 0, 0., 0., 0., params);
+                else if (fn == 3) v = AxionStrings::a_prime_screened(a, i, j, k, 0, 0., 0., 0., params);
+                else if (fn == 4) v = AxionStrings::r_prime2(a, i, j, k, 0, 0., 0., 0., params);
+                else return -1;
+                out[((long long)k * N + j) * N + i] = v;
+            }
     return 0;
 }

@@ -311,6 +311,19 @@ class Level:
             "sh_tag")
         return mask, counts, (lst[: nt.value].copy() if want_list else None)
 
+    def scalar_spectrum(self, fn: int, dx: float, comp: int = 0):
+        """Spectrum::Compute of an output function (sh_scalar_spectrum):
+        (bins, k^2 of the bins)."""
+        N = self.domain[1][0] - self.domain[0][0] + 1
+        cap = 3 * (N // 2 + 1) ** 2 + 16
+        bins = np.empty(cap, dtype=np.float64)
+        ks = np.empty(cap, dtype=np.int64)
+        nb = C.c_int()
+        self.ctx.check(self.ctx.lib.sh_scalar_spectrum(self.ctx.h, self.h, fn, comp, float(dx),
+                                                       _ptr(bins), _ptr(ks), cap, C.byref(nb)),
+                       "sh_scalar_spectrum")
+        return bins[: nb.value].copy(), ks[: nb.value].copy()
+
     def add_bubbles(self, centres, profile, inv_dx: float, Lcut: float, dx: float,
                     comp_phi: int = 0, comp_dphi: int = 1, which: int = SH_NEW):
         """FirstOrderPhaseTransition bubble injection (sh_level_add_bubbles):
@@ -386,6 +399,9 @@ class LevelView:
         n = C.c_int()
         ctx.lib.sh_level_boxes(handle, arr, self.nbox, C.byref(n))
         self.boxes = _boxes_of(arr, n.value)
+        lo, hi = (C.c_int * 3)(), (C.c_int * 3)()
+        ctx.lib.sh_level_domain(handle, lo, hi)
+        self.domain = (tuple(lo), tuple(hi))
 
     def read(self, which: int = SH_NEW) -> np.ndarray:
         out = np.empty(self.nvalid * self.ncomp, dtype=np.float64)
@@ -465,6 +481,29 @@ class Amr:
             self.close()
         except Exception:
             pass
+
+
+# output functions of projections and scalar spectra
+OUT_COMPONENT = _lib.SH_OUT_COMPONENT
+OUT_COMPONENT_SQ = _lib.SH_OUT_COMPONENT_SQ
+OUT_A_PRIME2 = _lib.SH_OUT_A_PRIME2
+OUT_A_PRIME_SCREENED = _lib.SH_OUT_A_PRIME_SCREENED
+OUT_R_PRIME2 = _lib.SH_OUT_R_PRIME2
+
+
+def projection(ctx: Context, levels, fn: int, comp: int = 0, mode: int = 0):
+    """Line-of-sight projection along z over the given levels (coarse to
+    fine; Level or LevelView objects): (data, n) on the finest pixel grid,
+    data[x, y] (sh_projection)."""
+    hs = (C.c_void_p * len(levels))(*[lv.h.value if isinstance(lv.h, C.c_void_p) else lv.h
+                                      for lv in levels])
+    last = levels[-1]
+    N = last.domain[1][0] - last.domain[0][0] + 1
+    data = np.empty((N, N), dtype=np.float64)
+    n = np.empty((N, N), dtype=np.int32)
+    ctx.check(ctx.lib.sh_projection(ctx.h, hs, len(levels), fn, comp, mode, _ptr(data),
+                                    _ptr(n)), "sh_projection")
+    return data, n
 
 
 # ensemble families and precisions (sh_ensemble_create)

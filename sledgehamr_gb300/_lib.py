@@ -30,6 +30,12 @@ SH_PREC_FP64 = 0
 SH_PREC_FP32_KAHAN = 1
 SH_PREC_FP32 = 2
 
+SH_OUT_COMPONENT = 0
+SH_OUT_COMPONENT_SQ = 1
+SH_OUT_A_PRIME2 = 2
+SH_OUT_A_PRIME_SCREENED = 3
+SH_OUT_R_PRIME2 = 4
+
 SH_NEW = 0
 SH_OLD = 1
 SH_ADVANCE_NO_SWAP = 1
@@ -114,6 +120,9 @@ SIGNATURES = {
     "sh_server_status": (C.c_int, [vp, C.c_longlong, ip, vp]),
     "sh_server_result": (C.c_int, [vp, C.c_longlong, vp, vp, C.c_int, ip]),
     "sh_server_info": (C.c_int, [vp, ip, ip, llp, llp, llp]),
+    "sh_level_domain": (C.c_int, [vp, vp, vp]),
+    "sh_scalar_spectrum": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_double, vp, vp, C.c_int, ip]),
+    "sh_projection": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp]),
     "sh_ensemble_add_bubbles": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, C.c_int, C.c_double,
                                           C.c_double]),
     "sh_level_add_bubbles": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp,

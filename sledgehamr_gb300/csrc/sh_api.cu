@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "sh_bubbles.cuh"
+#include "sh_out.cuh"
 #include "sh_gw.h"
 #include "sh_internal.h"
 
@@ -424,15 +425,22 @@ __global__ void cf_interp_kernel(const CfItem *items, const BoxDev *cboxes, doub
             const double Dxy = (u(1, 1, 0) - u(1, -1, 0) - u(-1, 1, 0) + u(-1, -1, 0)) * 0.25;
             const double Dxz = (u(1, 0, 1) - u(1, 0, -1) - u(-1, 0, 1) + u(-1, 0, -1)) * 0.25;
             const double Dyz = (u(0, 1, 1) - u(0, 1, -1) - u(0, -1, 1) + u(0, -1, -1)) * 0.25;
-            const double Q = 0.5 * (0.0625 * Dxx + 0.0625 * Dyy + 0.0625 * Dzz);
+            /* every child has xi_d^2 = 1/16: with s_d = +-1,
+             * u = S + sum_d s_d E_d + sum_{d<e} s_d s_e F_de,
+             * S = u000 + (Dxx + Dyy + Dzz)/32, E_d = D_d/4, F_de = D_de/16 */
+            const double S = u0 + 0.5 * (0.0625 * Dxx + 0.0625 * Dyy + 0.0625 * Dzz);
+            const double Ex = 0.25 * Dx, Ey = 0.25 * Dy, Ez = 0.25 * Dz;
+            const double Fxy = 0.0625 * Dxy, Fxz = 0.0625 * Dxz, Fyz = 0.0625 * Dyz;
             for (int fk = c0[2]; fk <= c1[2]; ++fk) {
-                const double zi = (fk - 2 * P[2]) ? 0.25 : -0.25;
+                const bool zp = (fk - 2 * P[2]) != 0;
                 for (int fj = c0[1]; fj <= c1[1]; ++fj) {
-                    const double yi = (fj - 2 * P[1]) ? 0.25 : -0.25;
+                    const bool yp = (fj - 2 * P[1]) != 0;
+                    /* the part without x, and the coefficient of s_x */
+                    const double fyz = (yp == zp) ? Fyz : -Fyz;
+                    const double base = S + (yp ? Ey : -Ey) + (zp ? Ez : -Ez) + fyz;
+                    const double slope = Ex + (yp ? Fxy : -Fxy) + (zp ? Fxz : -Fxz);
                     for (int fi = c0[0]; fi <= c1[0]; ++fi) {
-                        const double xi = (fi - 2 * P[0]) ? 0.25 : -0.25;
-                        const double v = u0 + xi * Dx + yi * Dy + zi * Dz + Q + xi * yi * Dxy +
-                                         xi * zi * Dxz + yi * zi * Dyz;
+                        const double v = (fi - 2 * P[0]) ? base + slope : base - slope;
                         if (store)
                             store[it.first + (fi - lo[0]) +
                                   (long long)it.nx * ((fj - lo[1]) + (long long)it.ny * (fk - lo[2])) +
@@ -468,6 +476,84 @@ __global__ void cf_combine_kernel(const CfItem *items, double *fbuf, const doubl
             else v = alpha * i_old[e] + beta * i_new[e];
             fbuf[d + nn * it.dgvol] = v;
         }
+    }
+}
+
+/* The output function of every valid cell into a P^3 array (x fastest). */
+__global__ void out_pack_kernel(const BoxDev *boxes, const long long *vbase, int nbox,
+                                long long nvalid, int ncomp, int fn, int comp, const double *buf,
+                                double *dst, int P, int dlo0, int dlo1, int dlo2) {
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nvalid;
+         v += (long long)gridDim.x * blockDim.x) {
+        const int bx = find_box(vbase, nbox, v);
+        const BoxDev &b = boxes[bx];
+        const long long lv = v - vbase[bx];
+        const int vx = b.hi[0] - b.lo[0] + 1, vy = b.hi[1] - b.lo[1] + 1;
+        const int i = b.lo[0] + (int)(lv % vx);
+        const int j = b.lo[1] + (int)((lv / vx) % vy);
+        const int k = b.lo[2] + (int)(lv / ((long long)vx * vy));
+        const long long c = b.off * ncomp + (i - b.glo[0]) +
+                            (long long)(j - b.glo[1]) * b.gdim[0] +
+                            (long long)(k - b.glo[2]) * b.gdim[0] * b.gdim[1];
+        dst[((long long)(k - dlo2) * P + (j - dlo1)) * P + (i - dlo0)] =
+            out_function(fn, comp, buf + c, b.gvol);
+    }
+}
+
+/* One level of a projection. */
+struct ProjLevel {
+    OwnerMapDev map;
+    const BoxDev *boxes;
+    const double *buf;
+    int ncomp, dimN;
+};
+constexpr int kMaxProjLevels = 8;
+struct ProjArgs {
+    ProjLevel lev[kMaxProjLevels];
+    int nlev, fn, comp, mode, dimN;
+};
+
+__device__ __forceinline__ int owner_at(const OwnerMapDev &m, int i, int j, int k) {
+    return m.owner[((long long)((k - m.dlo[2]) / m.res) * m.nb[1] + (j - m.dlo[1]) / m.res) *
+                       m.nb[0] +
+                   (i - m.dlo[0]) / m.res];
+}
+
+/* One thread per pixel (x, y) of the finest level: levels in order, along z
+ * in increasing k, the cells of each level that exist there and are not
+ * covered by the next level (the order in which the reference's loops over
+ * z-sorted boxes reach the pixel). */
+__global__ void projection_kernel(const __grid_constant__ ProjArgs a, double *data, int *nproj) {
+    const long long npix = (long long)a.dimN * a.dimN;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npix;
+         p += (long long)gridDim.x * blockDim.x) {
+        const int X = (int)(p / a.dimN), Y = (int)(p % a.dimN);
+        double acc = 0.;
+        int cnt = 0;
+        for (int l = 0; l < a.nlev; ++l) {
+            const ProjLevel &L = a.lev[l];
+            const int ratio = a.dimN / L.dimN;
+            const int i = X / ratio, j = Y / ratio;
+            for (int k = 0; k < L.dimN; ++k) {
+                const int own = owner_at(L.map, i, j, k);
+                if (own < 0) {
+                    k += L.map.res - 1 - (k % L.map.res); /* skip the block */
+                    continue;
+                }
+                if (l + 1 < a.nlev && owner_at(a.lev[l + 1].map, 2 * i, 2 * j, 2 * k) >= 0)
+                    continue;
+                const BoxDev &b = L.boxes[own];
+                const long long c = b.off * L.ncomp + (i - b.glo[0]) +
+                                    (long long)(j - b.glo[1]) * b.gdim[0] +
+                                    (long long)(k - b.glo[2]) * b.gdim[0] * b.gdim[1];
+                const double val = out_function(a.fn, a.comp, L.buf + c, b.gvol);
+                if (a.mode == 0) acc = __dadd_rn(acc, __dmul_rn((double)ratio, val));
+                else acc = fmax(acc, val);
+                ++cnt;
+            }
+        }
+        data[p] = acc;
+        nproj[p] = cnt;
     }
 }
 
@@ -1626,6 +1712,15 @@ int sh_level_destroy(sh_ctx *ctx, sh_level *L) {
     return SH_OK;
 }
 
+int sh_level_domain(const sh_level *L, int lo[3], int hi[3]) {
+    if (!L || !lo || !hi) return SH_ERR_ARG;
+    for (int d = 0; d < 3; ++d) {
+        lo[d] = L->dlo[d];
+        hi[d] = L->dhi[d];
+    }
+    return SH_OK;
+}
+
 int sh_level_info(const sh_level *L, int *ncomp, int *nbox, long long *nvalid) {
     if (!L) return SH_ERR_ARG;
     if (ncomp) *ncomp = L->ncomp;
@@ -1859,6 +1954,97 @@ int sh_level_add_bubbles(sh_ctx *ctx, sh_level *L, int which, int comp_phi, int 
         ctx->launches++;
         ck(cudaGetLastError(), "bubble launch");
         ck(cudaStreamSynchronize(ctx->stream), "bubbles");
+    });
+}
+
+int sh_scalar_spectrum(sh_ctx *ctx, const sh_level *L, int fn, int comp, double dx,
+                       double *bins_out, long long *ks_out, int max_bins, int *nbins) {
+    if (!ctx || !L || !bins_out || !nbins || !(dx > 0)) return SH_ERR_ARG;
+    return guarded(ctx, [&] {
+        set_device(ctx);
+        require(fn >= SH_OUT_COMPONENT && fn <= SH_OUT_R_PRIME2, "unknown output function");
+        require(fn > SH_OUT_COMPONENT_SQ ? L->ncomp >= 4 : (comp >= 0 && comp < L->ncomp),
+                "component index out of range");
+        const int N = L->dhi[0] - L->dlo[0] + 1;
+        long long dv = 1;
+        for (int d = 0; d < 3; ++d) {
+            require(L->dhi[d] - L->dlo[d] + 1 == N, "spectrum needs a cubic domain");
+            dv *= N;
+        }
+        require(dv == L->nvalid, "spectrum needs a level covering its whole domain");
+        const size_t sbytes = (gw_scratch_bytes(N, 1) + 255) & ~size_t(255);
+        const size_t maxb = (size_t)3 * (N / 2 + 1) * (N / 2 + 1) + 16;
+        char *base = (char *)ctx_scratch(ctx, sbytes + maxb * sizeof(double));
+        double *bins_dev = (double *)(base + sbytes);
+        const double fac = std::pow(1. / N, 6);
+        const double dk = 2. * M_PI / (N * dx);
+        const double pre = fac * L->t[SH_NEW] / dk;
+        int nb = 0;
+        std::string err;
+        ProfScope ps(ctx, kProfGw);
+        cudaError_t e = scalar_spectrum_packed(
+            ctx->gw, ctx->stream, N, pre, (double *)base, bins_dev, &nb, &ctx->launches, err,
+            [&](double *real) {
+                out_pack_kernel<<<grid_for(L->nvalid), 256, 0, ctx->stream>>>(
+                    L->d_boxes, L->d_vbase, (int)L->boxes.size(), L->nvalid, L->ncomp, fn, comp,
+                    L->buf[SH_NEW], real, N, L->dlo[0], L->dlo[1], L->dlo[2]);
+            });
+        if (!err.empty()) throw ShError(SH_ERR_CUDA, err);
+        ck(e, "scalar spectrum");
+        *nbins = nb;
+        require(nb <= max_bins, "bins_out too small");
+        ck(cudaMemcpyAsync(bins_out, bins_dev, nb * sizeof(double), cudaMemcpyDeviceToHost,
+                           ctx->stream),
+           "bins download");
+        ck(cudaStreamSynchronize(ctx->stream), "scalar spectrum");
+        if (ks_out) std::copy(ctx->gw.ks.begin(), ctx->gw.ks.end(), ks_out);
+    });
+}
+
+int sh_projection(sh_ctx *ctx, const sh_level *const *levels, int nlev, int fn, int comp,
+                  int mode, double *data_out, int *n_out) {
+    if (!ctx || !levels || nlev <= 0 || !data_out || !n_out) return SH_ERR_ARG;
+    return guarded(ctx, [&] {
+        set_device(ctx);
+        require(nlev <= kMaxProjLevels, "at most 8 levels");
+        require(fn >= SH_OUT_COMPONENT && fn <= SH_OUT_R_PRIME2, "unknown output function");
+        require(mode == 0 || mode == 1, "mode must be 0 (sum) or 1 (maximum)");
+        ProjArgs a;
+        std::memset(&a, 0, sizeof(a));
+        a.nlev = nlev;
+        a.fn = fn;
+        a.comp = comp;
+        a.mode = mode;
+        for (int l = 0; l < nlev; ++l) {
+            const sh_level *L = levels[l];
+            require(L != nullptr, "null level");
+            require(fn > SH_OUT_COMPONENT_SQ ? L->ncomp >= 4 : (comp >= 0 && comp < L->ncomp),
+                    "component index out of range");
+            const int N = L->dhi[0] - L->dlo[0] + 1;
+            for (int d = 0; d < 3; ++d)
+                require(L->dlo[d] == 0 && L->dhi[d] + 1 == N,
+                        "projection levels need cubic domains starting at 0");
+            if (l > 0) require(N == 2 * a.lev[l - 1].dimN, "levels must refine by 2");
+            a.lev[l].map = owner_map_dev(L);
+            a.lev[l].boxes = L->d_boxes;
+            a.lev[l].buf = L->buf[SH_NEW];
+            a.lev[l].ncomp = L->ncomp;
+            a.lev[l].dimN = N;
+        }
+        a.dimN = a.lev[nlev - 1].dimN;
+        const long long npix = (long long)a.dimN * a.dimN;
+        char *base = (char *)ctx_scratch(ctx, npix * (sizeof(double) + sizeof(int)) + 256);
+        double *d_data = (double *)base;
+        int *d_n = (int *)(base + ((npix * sizeof(double) + 255) & ~255LL));
+        projection_kernel<<<grid_for(npix), 256, 0, ctx->stream>>>(a, d_data, d_n);
+        ctx->launches++;
+        ck(cudaGetLastError(), "projection launch");
+        ck(cudaMemcpyAsync(data_out, d_data, npix * sizeof(double), cudaMemcpyDeviceToHost,
+                           ctx->stream),
+           "projection download");
+        ck(cudaMemcpyAsync(n_out, d_n, npix * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream),
+           "projection download");
+        ck(cudaStreamSynchronize(ctx->stream), "projection");
     });
 }
 

@@ -96,7 +96,7 @@ __device__ __forceinline__ void kahan_add(R &y, R d, R &c) {
  * formed once in FP64 by one thread: FP64 work per thread would run on
  * GB300's narrow FP64 pipe. */
 template <class R, int ORDER, int STAGE, bool KAHAN>
-__global__ void __launch_bounds__(TX *TY) axion_rkn4_kernel(const __grid_constant__ AxionArgs<R> a) {
+__global__ void __launch_bounds__(TX *TY, sizeof(R) == 4 ? 5 : 1) axion_rkn4_kernel(const __grid_constant__ AxionArgs<R> a) {
     constexpr int H = ORDER;             /* halo */
     constexpr int RING = 2 * H + 2;
     constexpr int W = TX + 2 * H, HH = TY + 2 * H;

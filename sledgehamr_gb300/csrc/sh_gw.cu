@@ -182,6 +182,21 @@ __global__ void gw_bin_kernel(const double *val, const long long *bin_off, const
     if (lane == 0) bins[warp] = s * scale;
 }
 
+/* multpl |F|^2 per k-cell of a scalar field's R2C transform, with
+ * |F| = sqrt(re^2 + im^2) as utils::Fft forms it (fft.h:244-250). */
+__global__ void scalar_power_kernel(const double2 *F, int P, double *out) {
+    const int H = P / 2 + 1;
+    const long long n = (long long)H * P * P;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int a = (int)(e % H);
+        const double multpl = (a == 0 || a == P / 2) ? 1. : 2.;
+        const double2 z = F[e];
+        const double absF = sqrt(__dadd_rn(__dmul_rn(z.x, z.x), __dmul_rn(z.y, z.y)));
+        out[e] = multpl * absF * absF;
+    }
+}
+
 } // namespace
 
 /* Builds (or reuses) the bin lists of a P^3 spectrum. */
@@ -293,6 +308,47 @@ cudaError_t gw_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, int p
     const double scale = 1. / std::pow((double)P, 6);
     gw_bin_kernel<<<(nb * 32 + 255) / 256, 256, 0, stream>>>(vals, cache.d_off, cache.d_cells,
                                                               nb, scale, bins_dev);
+    (*launches)++;
+    *nbins = nb;
+    return cudaGetLastError();
+}
+
+cudaError_t scalar_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, double pre,
+                                   double *scratch, double *bins_dev, int *nbins,
+                                   long long *launches, std::string &err,
+                                   const std::function<void(double *)> &pack) {
+    const int keep_type = cache.projection_type >= 1 ? cache.projection_type : 2;
+    cache.prepare(P, 1, keep_type);
+    const int H = P / 2 + 1;
+    const long long nreal = (long long)P * P * P;
+    const long long ncplx = (long long)H * P * P;
+    if (!cache.plan_ok || cache.plan_P != P) {
+        if (cache.plan_ok) cufftDestroy(cache.plan);
+        cache.plan_ok = false;
+        if (cufftPlan3d(&cache.plan, P, P, P, CUFFT_D2Z) != CUFFT_SUCCESS) {
+            err = "cufftPlan3d failed";
+            return cudaErrorUnknown;
+        }
+        cache.plan_ok = true;
+        cache.plan_P = P;
+    }
+    cufftSetStream(cache.plan, stream);
+    double *real = scratch;
+    double2 *cplx = (double2 *)(scratch + nreal);
+    double *vals = (double *)(cplx + ncplx);
+    cudaMemsetAsync(real, 0, nreal * sizeof(double), stream);
+    pack(real);
+    (*launches)++;
+    if (cufftExecD2Z(cache.plan, real, (cufftDoubleComplex *)cplx) != CUFFT_SUCCESS) {
+        err = "cufftExecD2Z failed";
+        return cudaErrorUnknown;
+    }
+    int g = (int)std::min<long long>((ncplx + 255) / 256, 152LL * 32);
+    scalar_power_kernel<<<std::max(g, 1), 256, 0, stream>>>(cplx, P, vals);
+    (*launches)++;
+    const int nb = (int)cache.ks.size();
+    gw_bin_kernel<<<(nb * 32 + 255) / 256, 256, 0, stream>>>(vals, cache.d_off, cache.d_cells,
+                                                              nb, pre, bins_dev);
     (*launches)++;
     *nbins = nb;
     return cudaGetLastError();

@@ -33,6 +33,12 @@ size_t gw_scratch_bytes(int N, int zero_padding);
 /* FFT, TT projection and binning of six P^3 real arrays that `pack(q, real)`
  * writes (enqueued on `stream`) into the zeroed `real` for q = 0..5 in the
  * order du_xx, du_xy, du_xz, du_yy, du_yz, du_zz. */
+/* Scalar power spectrum of one P^3 real field that `pack(real)` writes into
+ * the zeroed `real`: bins of the sorted unique k^2, pre * sum multpl |F|^2. */
+cudaError_t scalar_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, double pre,
+                                   double *scratch, double *bins_dev, int *nbins,
+                                   long long *launches, std::string &err,
+                                   const std::function<void(double *)> &pack);
 cudaError_t gw_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, int projection_type,
                                int unbinned, double *scratch, double *bins_dev, int *nbins,
                                long long *launches, std::string &err,

@@ -181,6 +181,7 @@ class OracleAmr:
             raise RuntimeError("orc_amr_create failed")
         self.h = C.c_void_p(self.h)
         self.ncomp = a.shape[0]
+        self.N0 = a.shape[-1]
 
     def step(self, n=1):
         if self.lib.orc_amr_step(self.h, n) != 0:
@@ -224,6 +225,19 @@ class OracleAmr:
         return {"lev": lev.value, "time": t.value, "tagged_boxes": conv(tb, nt.value),
                 "mask": mask[: nm.value].copy(), "new_boxes": conv(nb, nn.value)}
 
+    def projection(self, fn, comp=0, mode=0, max_level=100):
+        """Projection::Compute over the hierarchy (orc_amr_projection)."""
+        f = self.lib.orc_amr_projection
+        f.restype = C.c_int
+        ml = min(max_level, self.info()["finest"])
+        N = self.N0 << ml
+        data = np.empty((N, N))
+        n = np.empty((N, N), dtype=np.int32)
+        rc = f(self.h, fn, comp, mode, ml, _p(data), C.c_void_p(n.ctypes.data))
+        if rc != 0:
+            raise RuntimeError("projection")
+        return data, n
+
     def close(self):
         if self.h:
             self.lib.orc_amr_destroy(self.h)
@@ -254,3 +268,44 @@ def oracle_add_bubbles(state, xyz, profile, inv_dx, Lcut, dx, comp_phi=0, comp_d
     if rc != 0:
         raise RuntimeError("add_bubbles")
     return st
+
+
+def oracle_out_function(state, fn, comp=0, ref=False):
+    """Per-cell output function on a canonical state (orc_out_function, or
+    the reference's own functions through ref_out_function)."""
+    st = _f(state)
+    ncomp, N = st.shape[0], st.shape[-1]
+    out = np.empty((N, N, N))
+    if ref:
+        lib = C.CDLL(REF_SO)
+        f = lib.ref_out_function
+        f.restype = C.c_int
+        rc = f(_p(st), N, ncomp, fn, _p(out))
+    else:
+        build_oracle()
+        lib = C.CDLL(ORACLE_SO)
+        f = lib.orc_out_function
+        f.restype = C.c_int
+        rc = f(_p(st), N, ncomp, fn, comp, _p(out))
+    if rc != 0:
+        raise RuntimeError("out_function")
+    return out
+
+
+def oracle_scalar_spectrum(state, fn, comp, L, t):
+    """Spectrum::Compute on a canonical periodic state (orc_scalar_spectrum)."""
+    build_oracle()
+    lib = C.CDLL(ORACLE_SO)
+    st = _f(state)
+    ncomp, N = st.shape[0], st.shape[-1]
+    cap = 3 * (N // 2 + 1) ** 2 + 16
+    bins = np.empty(cap)
+    ks = np.empty(cap, dtype=np.int64)
+    nb = C.c_int()
+    f = lib.orc_scalar_spectrum
+    f.restype = C.c_int
+    rc = f(_p(st), N, ncomp, fn, comp, C.c_double(L), C.c_double(t), _p(bins), _p(ks), cap,
+           C.byref(nb))
+    if rc != 0:
+        raise RuntimeError("scalar_spectrum")
+    return bins[: nb.value].copy(), ks[: nb.value].copy()
