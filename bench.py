@@ -652,7 +652,21 @@ def run_case(name):
                             params=a["params"],
                             string_width_threshold=a["string_width_threshold"])
         sim = sh.Amr(ctx, cfg, ic.axion_string_ic(n0, n0 * 0.25, kmax=1.0, seed=0))
-        sim.step(40 if name == "amr" else 60)
+        for q in range(40 if name == "amr" else 60):
+            sim.step(1)
+            # valid cells and stage-kernel tiles (grid size) of every level,
+            # to relate a profiled launch to the cells it updated
+            rows = []
+            for lev in range(sim.info()["finest"] + 1):
+                v = sim.level(lev)
+                tiles = 0
+                for lo, hi in v.boxes:
+                    nx_, ny_, nz_ = (hi[0] - lo[0] + 1, hi[1] - lo[1] + 1, hi[2] - lo[2] + 1)
+                    for x0 in range(0, nx_, 32):
+                        w = min(32, nx_ - x0)
+                        tiles += -(-nz_ // 8) * -(-ny_ // (128 // w))
+                rows.append((lev, v.nvalid, tiles))
+            print("step", q, rows, flush=True)
         sim.close()
     elif name == "single":
         s = SINGLE
