@@ -619,6 +619,21 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def replica_aggregate(total_ms, cell_updates, world, device):
+    """Whole-job throughput of `world` independent replicas (one per rank):
+    the cell-updates of all ranks over the slowest rank's timed region.
+    Returns (cell-updates/s, max time in ms)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        c = torch.tensor([float(cell_updates)], dtype=torch.float64, device=device)
+        dist.all_reduce(c, op=dist.ReduceOp.SUM)
+        total_ms, cell_updates = float(t.item()), float(c.item())
+    return cell_updates / (total_ms / 1e3), total_ms
+
+
 def run_case(name):
     """Small fixed cases for profiler captures (no timing, no output line):
     axion-fp32k / axion-fp64: one 256^3 axion realisation, 3 RKN4 steps
@@ -787,11 +802,7 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     total_ms = float(sum(a.elapsed_time(b) for a, b in zip(starts, ends)))
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * cus / (total_ms / 1e3)
+    value, total_ms = replica_aggregate(total_ms, cus, world, "cuda")
     achieved = WORDS_PER_CELL_UPDATE * 8 * cus / (stage_ms / 1e3) / 1e9
     cells_per_launch = 3.0 * cus / max(stage_launches, 1)
     traffic = TRAFFIC_B_PER_CELL_UPDATE / 3.0 * cells_per_launch if args.workload == "amr" else None
