@@ -68,7 +68,7 @@ enum ProfCat {
 /* Work items of the fill kernels (one thread block each): a rectangle of
  * cells of one destination box, at most kItemCells cells, with the flat
  * offsets of its first cell (component 0) and its row / plane strides. */
-constexpr int kItemCells = 4096;
+constexpr int kItemCells = 512;
 struct CopyItem {
     long long dst, src;     /* first cell in the dst / src buffers */
     long long dgvol, sgvol; /* component strides */
