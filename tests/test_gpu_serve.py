@@ -133,3 +133,31 @@ def test_served_fp32_spectra_close_to_fp64(ctx):
         assert abs(b32.sum() - b64.sum()) <= 1e-2 * b64.sum()
         big = b64 >= 1e-3 * b64.max()
         assert np.all(np.abs(b32[big] - b64[big]) <= 5e-2 * b64[big])
+
+
+def test_fp64_pool_member_matches_oracle(ctx):
+    """A member of an FP64 pool (own N, dx and step) follows the drop-in
+    FirstOrderPhaseTransition leapfrog of the oracle to 1e-12."""
+    from tests.conftest import rel_l2
+    from tests.oracle_lib import Oracle, oracle_add_bubbles
+    P = sh.Ensemble.pool(ctx, sh.FAMILY_FOPT_GW, sh.PREC_FP64, capacity_cells=60000)
+    runs = []
+    for rq in (request(16, 6.0, 1), request(24, 8.0, 2)):
+        s = P.admit(rq["N"], rq["dx"], rq["params"], rq["dt"])
+        P.add_bubbles(s, rq["centres"], rq["profile"], rq["inv_dx"], rq["Lcut"])
+        runs.append((s, rq))
+    P.step(0.0, 6)
+    orc = Oracle()
+    for s, rq in runs:
+        N = rq["N"]
+        st = oracle_add_bubbles(np.zeros((14, N, N, N)), rq["centres"], rq["profile"],
+                                rq["inv_dx"], rq["Lcut"], rq["dx"])
+        q = rq["params"]
+        ref = orc.evolve_periodic("FirstOrderPhaseTransition", sh.LEAPFROG, st, t0=0.0,
+                                  dt=rq["dt"], dx=rq["dx"], nsteps=6,
+                                  params=[0.0, q[0], q[1], q[2], 0.0, 0.0, 0.0], with_gw=True,
+                                  nghost=2)
+        out = P.read(s)
+        assert rel_l2(out, ref) <= 1e-12
+        assert rel_l2(out[2:], ref[2:]) <= 1e-12
+    P.close()
