@@ -69,7 +69,6 @@ struct AxionArgs {
     double *time;           /* two slots; the step reads slot `slot` and the */
     int slot;               /* last stage writes slot 1 - slot = t + h */
     double h;
-    int ntiles;
 };
 
 __device__ __forceinline__ int wrap(int a, int N) { return a < 0 ? a + N : (a >= N ? a - N : a); }
@@ -97,7 +96,7 @@ __device__ __forceinline__ void kahan_add(R &y, R d, R &c) {
  * formed once in FP64 by one thread: FP64 work per thread would run on
  * GB300's narrow FP64 pipe. */
 template <class R, int ORDER, int STAGE, bool KAHAN>
-__device__ __forceinline__ void axion_rkn4_tile(const AxionArgs<R> &a, const int tile) {
+__global__ void __launch_bounds__(TX *TY, sizeof(R) == 4 ? 5 : 1) axion_rkn4_kernel(const __grid_constant__ AxionArgs<R> a) {
     constexpr int H = ORDER;             /* halo */
     constexpr int RING = 2 * H + 2;
     constexpr int W = TX + 2 * H, HH = TY + 2 * H;
@@ -106,7 +105,7 @@ __device__ __forceinline__ void axion_rkn4_tile(const AxionArgs<R> &a, const int
     __shared__ R ring[RING][2][HH][W];
     __shared__ R kc[10];
 
-    const FastTile tl = a.tiles[tile];
+    const FastTile tl = a.tiles[blockIdx.x];
     const RealDesc d = a.desc[tl.r];
     const int N = d.N;
     const long long off = d.off;
@@ -120,7 +119,7 @@ __device__ __forceinline__ void axion_rkn4_tile(const AxionArgs<R> &a, const int
         const double hh = a.h * a.h;
         const double t0 = a.time[a.slot];
         const double ts = t0 + a.h * (STAGE == 0 ? 0. : (STAGE == 1 ? 0.5 : 1.));
-        if (STAGE == 2 && tile == 0) a.time[1 - a.slot] = t0 + a.h;
+        if (STAGE == 2 && blockIdx.x == 0) a.time[1 - a.slot] = t0 + a.h;
         kc[0] = (R)(STAGE == 0 ? 0. : (STAGE == 1 ? 0.5 * a.h : a.h)); /* cm */
         kc[1] = (R)(STAGE == 1 ? hh / 8. : (STAGE == 2 ? hh / 2. : 0.)); /* ck */
         kc[2] = (R)(-2. / ts);                                            /* friction */
@@ -274,19 +273,6 @@ __device__ __forceinline__ void axion_rkn4_tile(const AxionArgs<R> &a, const int
     }
 }
 
-/* All tiles of all realisations of the ensemble in one grid.  The launches
- * use one block per tile; the grid-stride loop also serves smaller
- * (persistent) grids, which measured about 20 % slower on GB300 (blocks of
- * a full grid start as soon as others retire). */
-template <class R, int ORDER, int STAGE, bool KAHAN>
-__global__ void __launch_bounds__(TX *TY, sizeof(R) == 4 ? 5 : 1)
-    axion_rkn4_kernel(const __grid_constant__ AxionArgs<R> a) {
-    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
-        axion_rkn4_tile<R, ORDER, STAGE, KAHAN>(a, t);
-        __syncthreads(); /* the ring and the constants are reused by the next tile */
-    }
-}
-
 template <class R>
 struct FoptArgs {
     const RealDesc *desc;
@@ -299,7 +285,6 @@ struct FoptArgs {
     double *time; /* two slots, as for AxionArgs; STAGE 1 writes slot 1 - slot */
     int slot;
     double dt;
-    int ntiles;
 };
 
 /* Leapfrog kick-drift-kick stage kernel for Phi + GW tensor (7 position and
@@ -308,12 +293,12 @@ struct FoptArgs {
  * STAGE 1: a = f(x1); v1 = vh + dt/2 a.
  * Potential: dPhi' = lap Phi + q2 Phi + q3 Phi^2 + q4 Phi^3 (p[0..2]). */
 template <class R, int STAGE, bool KAHAN>
-__device__ __forceinline__ void fopt_leapfrog_tile(const FoptArgs<R> &a, const int tile) {
+__global__ void __launch_bounds__(TX *TY, sizeof(R) == 4 ? 3 : 1) fopt_leapfrog_kernel(const __grid_constant__ FoptArgs<R> a) {
     constexpr int H = 2, RING = 5, W = TX + 2 * H, HH = TY + 2 * H, NC = 7;
     extern __shared__ unsigned char smem_raw[];
     R(*ring)[NC][HH][W] = reinterpret_cast<R(*)[NC][HH][W]>(smem_raw);
 
-    const FastTile tl = a.tiles[tile];
+    const FastTile tl = a.tiles[blockIdx.x];
     const RealDesc d = a.desc[tl.r];
     const int N = d.N;
     const long long off = d.off;
@@ -330,7 +315,7 @@ __device__ __forceinline__ void fopt_leapfrog_tile(const FoptArgs<R> &a, const i
         kc[4] = (R)(1. / (12. * d.dx));
         kc[5] = (R)(0.5 * sdt);
         kc[6] = (R)sdt;
-        if (STAGE == 1 && tile == 0) a.time[1 - a.slot] = a.time[a.slot] + a.dt;
+        if (STAGE == 1 && blockIdx.x == 0) a.time[1 - a.slot] = a.time[a.slot] + a.dt;
     }
     __syncthreads();
     const R q2 = kc[0], q3 = kc[1], q4 = kc[2], inv12dx2 = kc[3], inv12dx = kc[4];
@@ -443,15 +428,6 @@ __device__ __forceinline__ void fopt_leapfrog_tile(const FoptArgs<R> &a, const i
                 }
             }
         }
-    }
-}
-
-template <class R, int STAGE, bool KAHAN>
-__global__ void __launch_bounds__(TX *TY, sizeof(R) == 4 ? 3 : 1)
-    fopt_leapfrog_kernel(const __grid_constant__ FoptArgs<R> a) {
-    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
-        fopt_leapfrog_tile<R, STAGE, KAHAN>(a, t);
-        __syncthreads();
     }
 }
 
@@ -794,16 +770,14 @@ void step_impl(sh_ensemble *E, const std::vector<void *> &in, const std::vector<
         a.time = E->d_time;
         a.slot = slot;
         a.h = dt;
-        a.ntiles = nt;
-        auto run = [&](auto k) { k<<<nt, block, 0, s>>>(a); };
         if (E->family == SH_FAMILY_AXION_LAP1) {
-            run(axion_rkn4_kernel<R, 1, 0, KAHAN>);
-            run(axion_rkn4_kernel<R, 1, 1, KAHAN>);
-            run(axion_rkn4_kernel<R, 1, 2, KAHAN>);
+            axion_rkn4_kernel<R, 1, 0, KAHAN><<<nt, block, 0, s>>>(a);
+            axion_rkn4_kernel<R, 1, 1, KAHAN><<<nt, block, 0, s>>>(a);
+            axion_rkn4_kernel<R, 1, 2, KAHAN><<<nt, block, 0, s>>>(a);
         } else {
-            run(axion_rkn4_kernel<R, 2, 0, KAHAN>);
-            run(axion_rkn4_kernel<R, 2, 1, KAHAN>);
-            run(axion_rkn4_kernel<R, 2, 2, KAHAN>);
+            axion_rkn4_kernel<R, 2, 0, KAHAN><<<nt, block, 0, s>>>(a);
+            axion_rkn4_kernel<R, 2, 1, KAHAN><<<nt, block, 0, s>>>(a);
+            axion_rkn4_kernel<R, 2, 2, KAHAN><<<nt, block, 0, s>>>(a);
         }
     } else {
         FoptArgs<R> a;
@@ -813,7 +787,6 @@ void step_impl(sh_ensemble *E, const std::vector<void *> &in, const std::vector<
         a.time = E->d_time;
         a.slot = slot;
         a.dt = dt;
-        a.ntiles = nt;
         const size_t shm = (size_t)5 * 7 * (TY + 4) * (TX + 4) * sizeof(R);
         for (int c = 0; c < 7; ++c) {
             a.x[c] = arr<R>(in, c);
