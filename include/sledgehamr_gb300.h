@@ -355,6 +355,10 @@ typedef struct sh_amr_config {
     int ngw;
     int clustering;              /* SH_CLUSTER_BR, SH_CLUSTER_WINDOWS, SH_CLUSTER_BR_WINDOWS */
     double grid_eff;             /* amr.grid_eff of the clustering (default 0.7) */
+    double params_tag[32];       /* SetParamsTagCellForRefinement */
+    int nparams_tag;
+    double params_mod[32];       /* SetParamsTruncationModifier */
+    int nparams_mod;
 } sh_amr_config;
 /* New-grid generation from the buffered tags (at blocking-factor
  * resolution): Berger-Rigoutsos clustering to efficiency grid_eff, then
@@ -375,6 +379,11 @@ SH_API int sh_amr_create(sh_ctx *ctx, const sh_amr_config *cfg, const double *le
 SH_API int sh_amr_destroy(sh_ctx *ctx, sh_amr *amr);
 /* n coarse steps (Sledgehamr::Evolve loop bodies). */
 SH_API int sh_amr_step(sh_ctx *ctx, sh_amr *amr, int n);
+/* New tagging parameters from the next regrid on (projects whose hooks
+ * change them between steps, e.g. FirstOrderPhaseTransition's field maxima
+ * for its TruncationModifier, FirstOrderPhaseTransition.cpp:133-157). */
+SH_API int sh_amr_set_tag_params(sh_amr *amr, const double *params_tag, int nparams_tag,
+                                 const double *params_mod, int nparams_mod);
 SH_API int sh_amr_info(const sh_amr *amr, int *finest, long long *cell_updates, int *nregrids);
 /* Host wall-clock seconds and call counts of the time stepper's phases
  * (q = 0, 1, ... until SH_ERR_ARG): advance, synchronize, shadow,

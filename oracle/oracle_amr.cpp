@@ -212,9 +212,8 @@ struct CpuBackend {
     }
     std::vector<uint8_t> tag(Level &l, bool use_te, double time, int lev, double dt, double dx) {
         std::vector<std::vector<uint8_t>> m;
-        double ptag = 0, pmod_ = 0;
         tag_cpu_literal<P>(l->nw, use_te ? &l->od : nullptr, time, lev, dt, dx, cfg.te_crit,
-                           ncomp, &ptag, &pmod_, m, nullptr, nullptr, nullptr);
+                           ncomp, cfg.params_tag, cfg.params_mod, m, nullptr, nullptr, nullptr);
         std::vector<uint8_t> out;
         for (auto &v : m) out.insert(out.end(), v.begin(), v.end());
         return out;
@@ -250,6 +249,7 @@ struct AmrBase {
     virtual const shamr::RegridRecord &record(int q) const = 0;
     virtual const MF *level(int lev, int which) const = 0;
     virtual const std::vector<shamr::IBox> &boxes(int lev) const = 0;
+    virtual void set_tag_params(const double *pt, int nt, const double *pm, int nm) = 0;
 };
 
 template <class P>
@@ -301,6 +301,12 @@ struct Amr : AmrBase {
         return which == 0 ? &drv->levels[lev]->nw : &drv->levels[lev]->od;
     }
     const std::vector<shamr::IBox> &boxes(int lev) const override { return drv->boxes[lev]; }
+    void set_tag_params(const double *pt, int nt, const double *pm, int nm) override {
+        for (int q = 0; q < nt; ++q) backend.cfg.params_tag[q] = pt[q];
+        for (int q = 0; q < nm; ++q) backend.cfg.params_mod[q] = pm[q];
+        backend.cfg.nparams_tag = nt;
+        backend.cfg.nparams_mod = nm;
+    }
 };
 
 } // namespace orc
@@ -328,6 +334,13 @@ void *orc_amr_create(const sh_amr_config *cfg, const double *level0) {
 }
 
 void orc_amr_destroy(void *h) { delete (AmrBase *)h; }
+
+int orc_amr_set_tag_params(void *h, const double *params_tag, int ntag, const double *params_mod,
+                           int nmod) {
+    if (ntag < 0 || ntag > 32 || nmod < 0 || nmod > 32) return -1;
+    ((AmrBase *)h)->set_tag_params(params_tag, ntag, params_mod, nmod);
+    return 0;
+}
 
 int orc_amr_step(void *h, int n) {
     try {

@@ -377,6 +377,11 @@ def amr_config(project: str, **kw) -> ShAmrConfig:
             for n, x in enumerate(v):
                 cfg.gw_params[n] = x
             cfg.ngw = len(v)
+        elif k in ("params_tag", "params_mod"):
+            arr = getattr(cfg, k)
+            for n, x in enumerate(v):
+                arr[n] = x
+            setattr(cfg, "n" + k, len(v))
         else:
             setattr(cfg, k, v)
     return cfg
@@ -434,6 +439,13 @@ class Amr:
         f, cu, nr = C.c_int(), C.c_longlong(), C.c_int()
         self.ctx.lib.sh_amr_info(self.h, C.byref(f), C.byref(cu), C.byref(nr))
         return {"finest": f.value, "cell_updates": cu.value, "nregrids": nr.value}
+
+    def set_tag_params(self, params_tag=(), params_mod=()):
+        pt = _f64(list(params_tag) or [0.0])
+        pm = _f64(list(params_mod) or [0.0])
+        self.ctx.check(self.ctx.lib.sh_amr_set_tag_params(self.h, _ptr(pt), len(params_tag),
+                                                          _ptr(pm), len(params_mod)),
+                       "sh_amr_set_tag_params")
 
     def set_timer_sync(self, on: bool = True):
         self.ctx.check(self.ctx.lib.sh_amr_set_timer_sync(self.h, int(on)), "set_timer_sync")

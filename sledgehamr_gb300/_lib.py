@@ -60,7 +60,9 @@ class ShAmrConfig(C.Structure):
                 ("string_lambda", C.c_double), ("te_crit", C.c_double * 32),
                 ("params", C.c_double * 32), ("nparams", C.c_int),
                 ("gw_params", C.c_double * 16), ("ngw", C.c_int), ("clustering", C.c_int),
-                ("grid_eff", C.c_double)]
+                ("grid_eff", C.c_double), ("params_tag", C.c_double * 32),
+                ("nparams_tag", C.c_int), ("params_mod", C.c_double * 32),
+                ("nparams_mod", C.c_int)]
 
 
 class ShRequest(C.Structure):
@@ -134,6 +136,7 @@ SIGNATURES = {
     "sh_amr_destroy": (C.c_int, [vp, vp]),
     "sh_amr_step": (C.c_int, [vp, vp, C.c_int]),
     "sh_amr_info": (C.c_int, [vp, ip, llp, ip]),
+    "sh_amr_set_tag_params": (C.c_int, [vp, vp, C.c_int, vp, C.c_int]),
     "sh_amr_set_timer_sync": (C.c_int, [vp, C.c_int]),
     "sh_amr_timer": (C.c_int, [vp, C.c_int, C.POINTER(C.c_char_p), dp, llp]),
     "sh_amr_level": (C.c_int, [vp, C.c_int, C.POINTER(vp)]),

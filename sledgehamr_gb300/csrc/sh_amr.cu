@@ -103,16 +103,18 @@ struct GpuBackend {
         long long nv = 0;
         sh_level_info(l->L, &nc, &nb, &nv);
         std::vector<uint8_t> mask((size_t)nv);
-        ok(sh_tag(ctx, l->L, use_te ? 1 : 0, time, lev, dt, dx, cfg.te_crit, nullptr, 0,
-                  nullptr, 0, mask.data(), nullptr, nullptr, 0, nullptr),
+        ok(sh_tag(ctx, l->L, use_te ? 1 : 0, time, lev, dt, dx, cfg.te_crit, cfg.params_tag,
+                  cfg.nparams_tag, cfg.params_mod, cfg.nparams_mod, mask.data(), nullptr,
+                  nullptr, 0, nullptr),
            "sh_tag");
         return mask;
     }
     std::vector<uint8_t> tag_blocks(Level &l, bool use_te, double time, int lev, double dt,
                                     double dx, int block, int buffer, int nb) {
         std::vector<uint8_t> blk((size_t)nb * nb * nb);
-        ok(sh_tag_blocks(ctx, l->L, use_te ? 1 : 0, time, lev, dt, dx, cfg.te_crit, nullptr, 0,
-                         nullptr, 0, block, buffer, blk.data(), nullptr),
+        ok(sh_tag_blocks(ctx, l->L, use_te ? 1 : 0, time, lev, dt, dx, cfg.te_crit,
+                         cfg.params_tag, cfg.nparams_tag, cfg.params_mod, cfg.nparams_mod, block,
+                         buffer, blk.data(), nullptr),
            "sh_tag_blocks");
         return blk;
     }
@@ -204,6 +206,9 @@ int sh_amr_create(sh_ctx *ctx, const sh_amr_config *cfg, const double *level0, s
     if (rc != SH_OK) return rc;
     if (cfg->nparams < 0 || cfg->nparams > 32 || cfg->ngw < 0 || cfg->ngw > 16)
         return SH_ERR_ARG;
+    if (cfg->nparams_tag < 0 || cfg->nparams_tag > 32 || cfg->nparams_mod < 0 ||
+        cfg->nparams_mod > 32)
+        return SH_ERR_ARG;
     if ((cfg->clustering != SH_CLUSTER_BR && cfg->clustering != SH_CLUSTER_WINDOWS &&
          cfg->clustering != SH_CLUSTER_BR_WINDOWS) ||
         !(cfg->grid_eff > 0. && cfg->grid_eff <= 1.))
@@ -225,6 +230,19 @@ int sh_amr_create(sh_ctx *ctx, const sh_amr_config *cfg, const double *level0, s
         return rc;
     }
     *out = a;
+    return SH_OK;
+}
+
+int sh_amr_set_tag_params(sh_amr *a, const double *params_tag, int nparams_tag,
+                          const double *params_mod, int nparams_mod) {
+    if (!a || nparams_tag < 0 || nparams_tag > 32 || nparams_mod < 0 || nparams_mod > 32 ||
+        (nparams_tag > 0 && !params_tag) || (nparams_mod > 0 && !params_mod))
+        return SH_ERR_ARG;
+    sh_amr_config &c = a->backend.cfg;
+    for (int q = 0; q < nparams_tag; ++q) c.params_tag[q] = params_tag[q];
+    for (int q = 0; q < nparams_mod; ++q) c.params_mod[q] = params_mod[q];
+    c.nparams_tag = nparams_tag;
+    c.nparams_mod = nparams_mod;
     return SH_OK;
 }
 

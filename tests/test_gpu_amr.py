@@ -94,3 +94,40 @@ def test_tag_blocks_equal_coarsened_mask(ctx):
                             ref[bz % nb, by % nb, bx % nb] = 1
         assert np.array_equal(blocks.reshape(nb, nb, nb), ref)
     lv.close()
+
+
+def test_fopt_gw_amr_with_tag_params_matches_oracle(ctx):
+    """FirstOrderPhaseTransition + GW tensor on an AMR hierarchy (leapfrog,
+    truncation-error tags scaled by the field maxima passed as the
+    TruncationModifier parameters) against the oracle's hierarchy."""
+    from sledgehamr_gb300 import ic
+    from tests.oracle_lib import oracle_add_bubbles
+    N0, L = 16, 8.0
+    nb = 60
+    r = np.arange(nb) / 8.0
+    prof = np.stack([0.5 * (1 - np.tanh((r - 2.0) / 0.7)), np.zeros(nb)])
+    st = np.zeros((14, N0, N0, N0))
+    st[2:8] = 1e-3 * np.stack([ic.gaussian_field(N0, L, 3.0, 50 + q) for q in range(6)])
+    st = oracle_add_bubbles(st, [[4.1, 3.9, 4.2]], prof, 8.0, 7.0, L / N0)
+    n = np.arange(1.0)
+    lb = 0.8
+    num = 3.0 + np.sqrt(9.0 - 8.0 * lb)
+    params = [0.0, -1.0, 3.0 * num / (4.0 * lb), -num * num / (8.0 * lb), 0.0, 0.0, 0.0]
+    te = [1e-2, 1e-2] + [1e300] * 12
+    pmod = [float(np.abs(st[c]).max()) or 1.0 for c in range(14)]
+    kw = dict(N0=N0, L=L, cfl=0.2, t_start=0.0, nghost=2, max_level=2, blocking_factor=8,
+              max_grid_size=16, n_error_buf=1, regrid_dt=0.0, te_crit=te, params=params,
+              with_gw=1, integrator=sh.LEAPFROG, params_mod=pmod, record_regrids=1)
+    g = sh.Amr(ctx, sh.amr_config("FirstOrderPhaseTransition", **kw), st)
+    o = OracleAmr(sh.amr_config("FirstOrderPhaseTransition", **kw), st)
+    for step in range(5):
+        g.step(1)
+        o.step(1)
+        assert g.info() == o.info()
+        for lev in range(g.info()["finest"] + 1):
+            assert g.level(lev).boxes == o.boxes(lev)
+            od, _ = o.read(lev)
+            assert rel_l2(g.level(lev).read(), od) <= 1e-12
+    assert g.info()["finest"] >= 1
+    g.close()
+    o.close()
