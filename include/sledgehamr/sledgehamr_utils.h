@@ -24,6 +24,7 @@
 #include <utility>
 
 #include "sh_amrex.h"
+#include "sh_fixed_stencil.h"
 
 namespace sledgehamr {
 namespace utils {
@@ -77,6 +78,36 @@ along(const A4 &s, int i, int j, int k, int c, char axis, int d) {
                        : (axis == 'y' ? s(i, j + d, k, c) : s(i, j, k + d, c));
 }
 
+/* The Laplacian with its ring sums accumulated exactly in 64-bit integers
+ * (sh_fixed_stencil.h): centre, then the rings r = 1..Order with the integer
+ * weights of lap_ring, one rounding of the sum, then the product with
+ * 1 / (denominator dx^2). */
+template <int Order, class A4>
+AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE double
+laplacian_fixed(const A4 &s, int i, int j, int k, int c, double dx2) {
+    constexpr int NV = 6 * Order + 1;
+    double v[NV];
+    int n[Order + 1];
+    long long w[Order + 1];
+    v[0] = s(i, j, k, c);
+    n[0] = 1;
+    w[0] = (long long)lap_ring<Order>(0);
+#pragma unroll
+    for (int r = 1; r <= Order; ++r) {
+        v[6 * r - 5] = s(i + r, j, k, c);
+        v[6 * r - 4] = s(i - r, j, k, c);
+        v[6 * r - 3] = s(i, j + r, k, c);
+        v[6 * r - 2] = s(i, j - r, k, c);
+        v[6 * r - 1] = s(i, j, k + r, c);
+        v[6 * r] = s(i, j, k - r, c);
+        n[r] = 6;
+        w[r] = (long long)lap_ring<Order>(r);
+    }
+    /* guard bits: 2^53 * sum |w| n = 2^53 * {12, 192, 3264} */
+    return fixed::weighted_sum<NV, Order + 1, Order == 3 ? 2 : 0>(
+        v, n, w, 1. / (lap_denom<Order>() * dx2));
+}
+
 } // namespace detail
 
 template <int Order>
@@ -86,6 +117,9 @@ Laplacian(amrex::Array4<amrex::Real const> const &state, const int i,
     if constexpr (Order == 0) {
         return 0.;
     } else {
+#if defined(__CUDA_ARCH__) && !defined(SH_STENCIL_FP64)
+        return detail::laplacian_fixed<Order>(state, i, j, k, c, dx2);
+#else
         /* outermost ring first, centre last */
         double acc = detail::lap_ring<Order>(Order) *
                      detail::axis_ring_sum(state, i, j, k, c, Order);
@@ -96,6 +130,7 @@ Laplacian(amrex::Array4<amrex::Real const> const &state, const int i,
         });
         acc += detail::lap_ring<Order>(0) * state(i, j, k, c);
         return acc * (1. / (detail::lap_denom<Order>() * dx2));
+#endif
     }
 }
 
