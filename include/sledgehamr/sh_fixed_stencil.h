@@ -5,18 +5,18 @@
  * ring sums of a Laplacian are therefore accumulated here in 64-bit
  * integers instead of FP64: every stencil value x = +-M 2^(e-1075) (M the
  * 53-bit significand, e the biased exponent, e >= 1) is written as the
- * integer +-round(M / 2^(A+G-e)) in units of 2^(A+G-1075), where A is the
- * largest exponent among the values of this one stencil and G guard bits
- * keep the weighted sum below 2^63.  Integer adds and the small integer
- * weights of the stencil are exact; the only roundings are the shifted-out
- * significand bits of values smaller than the largest one (each at most
- * 2^(A+G-1076), half a unit in the last place of the largest value for
- * G = 0) and one final conversion of the 64-bit sum to FP64.  The FP64
- * evaluation rounds after every add instead; on stencils with strong
- * cancellation the integer sum's error is below the FP64 sum's for the 7-
- * and 13-point Laplacians and comparable for the 19-point one (two guard
- * bits).  The result scales exactly with powers of two of the input and is
- * independent of the cell's position.
+ * integer +-M 2^(e-A-G) in units of 2^(A+G-1075), where A is the largest
+ * exponent among the values of this one stencil and G is chosen per stencil
+ * so that the weighted sum stays below 2^63 (G = -6 for the 7-point, -2 for
+ * the 13-point and +2 for the 19-point Laplacian).  Integer adds and the
+ * small integer weights of the stencil are exact; the only roundings are
+ * the significand bits shifted out of values smaller than the largest one
+ * (each below 2^G units in the last place of the largest value) and one
+ * final conversion of the 64-bit sum to FP64.  The FP64 evaluation rounds
+ * after every add instead; on stencils with strong cancellation the integer
+ * sum's error is below the FP64 sum's for the 7- and 13-point Laplacians
+ * and comparable for the 19-point one.  The result scales exactly with
+ * powers of two of the input and is independent of the cell's position.
  *
  * A stencil whose largest value is not finite falls back to FP64 so that
  * NaN and infinity propagate as they do in the reference; values below
@@ -54,19 +54,33 @@ AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE double from_bits(long long b) {
 #endif
 }
 
-/* Biased exponent, at least 1 (subnormals share the exponent of 2^-1022). */
-AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE int expo(long long b) {
-    const int e = (int)((b >> 52) & 0x7FF);
-    return e > 0 ? e : 1;
+/* High and low 32-bit words of a double. */
+AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE int hi_word(double x) {
+#if defined(__CUDA_ARCH__)
+    return __double2hiint(x);
+#else
+    return (int)(bits(x) >> 32);
+#endif
+}
+AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE unsigned lo_word(double x) {
+#if defined(__CUDA_ARCH__)
+    return (unsigned)__double2loint(x);
+#else
+    return (unsigned)bits(x);
+#endif
 }
 
-/* +-round(M / 2^shift) (halves away from zero) for the value with bit
- * pattern b; shift in [0, 63]. */
-AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE long long term(long long b, int shift) {
-    const unsigned long long frac = (unsigned long long)b & 0xFFFFFFFFFFFFFull;
-    const unsigned long long M = frac | ((b & 0x7FF0000000000000ll) ? (1ull << 52) : 0ull);
-    const unsigned long long m = (M + ((1ull << shift) >> 1)) >> shift;
-    return b < 0 ? -(long long)m : (long long)m;
+/* Biased exponent from the high word (0 for zeros and subnormals). */
+AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE int expo(int hi) { return (hi >> 20) & 0x7FF; }
+
+/* Significand with the implicit bit, times 2^P.  The implicit bit is set for
+ * zeros and subnormals too: their exponent is at least kMinAnchor below the
+ * anchor, so the shift below removes them entirely. */
+template <int P>
+AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE unsigned long long significand(int hi, unsigned lo) {
+    const unsigned long long m =
+        ((unsigned long long)(((unsigned)hi & 0xFFFFFu) | 0x100000u) << 32) | lo;
+    return m << P;
 }
 
 /* Smallest anchor exponent: values below 2^(kMinAnchor - 1075) vanish. */
@@ -75,17 +89,26 @@ constexpr int kMinAnchor = 128;
 /* Exact weighted sum  sum_r w[r] * (sum of the values of ring r)  times
  * `scale` (a positive FP64 factor applied after the single rounding of the
  * integer sum).  Ring r has n[r] values; v lists the rings one after the
- * other.  G guard bits must satisfy 2^53 * sum_r |w[r]| n[r] < 2^(63+G). */
+ * other.  The unit of the integer sum is 2^(A+G-1075) with A the largest
+ * exponent of the stencil:
+ *   G <= 0: every significand is shifted left by -G (the headroom that the
+ *           stencil's weights leave below 2^63) and then right by A - e with
+ *           truncation, so each term is low by less than 2^G units in the
+ *           last place of the largest value;
+ *   G > 0:  significands are shifted right by A + G - e with rounding to
+ *           nearest (at most half a unit of 2^G ulps).
+ * G must satisfy 2^(53-G) * sum_r |w[r]| n[r] < 2^63.  Positive and negative
+ * terms go to separate accumulators, so no term is negated. */
 template <int NV, int NR, int G>
 AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE double
 weighted_sum(const double (&v)[NV], const int (&n)[NR], const long long (&w)[NR],
              double scale) {
-    long long b[NV];
+    int hi[NV];
     int A = kMinAnchor;
 #pragma unroll
     for (int q = 0; q < NV; ++q) {
-        b[q] = bits(v[q]);
-        const int e = expo(b[q]);
+        hi[q] = hi_word(v[q]);
+        const int e = expo(hi[q]);
         A = e > A ? e : A;
     }
     if (A == 0x7FF) {
@@ -100,28 +123,37 @@ weighted_sum(const double (&v)[NV], const int (&n)[NR], const long long (&w)[NR]
         }
         return acc * scale;
     }
-    const int top = A + G;
+    constexpr int P = G < 0 ? -G : 0;
+    constexpr int R = G > 0 ? G : 0;
     long long acc = 0;
     int q = 0;
 #pragma unroll
     for (int r = 0; r < NR; ++r) {
-        long long s = 0;
+        unsigned long long sp = 0, sn = 0;
 #pragma unroll
         for (int t = 0; t < n[r]; ++t, ++q) {
-            const int sh = top - expo(b[q]);
-            s += term(b[q], sh < 63 ? sh : 63);
+            const int d = A + R - expo(hi[q]);
+            const int sh = d < 63 ? d : 63;
+            const unsigned long long M = significand<P>(hi[q], lo_word(v[q]));
+            const unsigned long long m =
+                R > 0 ? (M + ((1ull << sh) >> 1)) >> sh : M >> sh;
+            if (hi[q] < 0)
+                sn += m;
+            else
+                sp += m;
         }
-        acc += w[r] * s;
+        acc += w[r] * (long long)(sp - sn);
     }
-    /* acc * 2^(top - 1075) * scale, rounded once by the conversion and once
+    /* acc * 2^(A + G - 1075) * scale, rounded once by the conversion and once
      * by the product with scale; the power of two goes straight into the
      * exponent field when the result is a normal number */
-    const double r = (double)acc * scale;
-    if (r == 0.) return r;
-    const long long rb = bits(r);
-    const int er = (int)((rb >> 52) & 0x7FF) + (top - 1075);
-    if (er >= 1 && er <= 2046) return from_bits(rb + ((long long)(top - 1075) << 52));
-    return scalbn(r, top - 1075);
+    if (acc == 0) return 0.;
+    const int pw = A + G - 1075;
+    const double res = (double)acc * scale;
+    const long long rb = bits(res);
+    const int er = (int)((rb >> 52) & 0x7FF) + pw;
+    if (er >= 1 && er <= 2046) return from_bits(rb + ((long long)pw << 52));
+    return scalbn(res, pw);
 }
 
 } // namespace fixed

@@ -103,8 +103,9 @@ laplacian_fixed(const A4 &s, int i, int j, int k, int c, double dx2) {
         n[r] = 6;
         w[r] = (long long)lap_ring<Order>(r);
     }
-    /* guard bits: 2^53 * sum |w| n = 2^53 * {12, 192, 3264} */
-    return fixed::weighted_sum<NV, Order + 1, Order == 3 ? 2 : 0>(
+    /* 2^53 * sum |w| n = 2^53 * {12, 192, 3264}: headroom of 6 and 2 bits
+     * below 2^63 for orders 1 and 2, two bits short for order 3 */
+    return fixed::weighted_sum<NV, Order + 1, Order == 1 ? -6 : (Order == 2 ? -2 : 2)>(
         v, n, w, 1. / (lap_denom<Order>() * dx2));
 }
 
