@@ -16,6 +16,13 @@
  * matters on GB300 where an FP64 division costs about as much as ten FP64
  * fused multiply-adds.  The result differs from a true division by at most
  * one rounding.
+ *
+ * Device code (unless SH_STENCIL_FP64 is defined) evaluates the Laplacians
+ * and the Gradients of orders 2 and 3 with their weighted sums accumulated
+ * exactly in 64-bit integers (sh_fixed_stencil.h) instead of FP64 adds: the
+ * same formulas, one rounding of the sum instead of one per add, and far
+ * fewer FP64 instructions, which GB300 issues at 1/64 of its FP32 rate.
+ * Host code keeps the FP64 evaluation order above.
  */
 #ifndef SLEDGEHAMR_SLEDGEHAMR_UTILS_H_
 #define SLEDGEHAMR_SLEDGEHAMR_UTILS_H_
@@ -109,6 +116,44 @@ laplacian_fixed(const A4 &s, int i, int j, int k, int c, double dx2) {
         v, n, w, 1. / (lap_denom<Order>() * dx2));
 }
 
+/* Gradient<2> and <3> the same way: the 4 or 6 values along the axis with
+ * the integer weights of the central difference, one rounding of the sum,
+ * then the product with 1 / (denominator dx). */
+template <int Order, class A4>
+AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE double
+gradient_fixed(const A4 &s, int i, int j, int k, int c, double dx, char axis) {
+    static_assert(Order == 2 || Order == 3, "orders 2 and 3");
+    constexpr int NV = 2 * Order;
+    double v[NV];
+    int n[NV];
+    long long w[NV];
+    if constexpr (Order == 2) {
+        /* -f(+2) + 8 f(+1) + f(-2) - 8 f(-1) */
+        constexpr int off[4] = {2, 1, -2, -1};
+        constexpr long long wt[4] = {-1, 8, 1, -8};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            v[q] = along(s, i, j, k, c, axis, off[q]);
+            n[q] = 1;
+            w[q] = wt[q];
+        }
+        /* 2^53 * sum |w| = 2^53 * 18: five bits of headroom */
+        return fixed::weighted_sum<NV, NV, -5>(v, n, w, 1. / (12. * dx));
+    } else {
+        /* f(+3) - f(-3) - 9 f(+2) + 9 f(-2) + 45 f(+1) - 45 f(-1) */
+        constexpr int off[6] = {3, -3, 2, -2, 1, -1};
+        constexpr long long wt[6] = {1, -1, -9, 9, 45, -45};
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            v[q] = along(s, i, j, k, c, axis, off[q]);
+            n[q] = 1;
+            w[q] = wt[q];
+        }
+        /* 2^53 * sum |w| = 2^53 * 110: three bits of headroom */
+        return fixed::weighted_sum<NV, NV, -3>(v, n, w, 1. / (60. * dx));
+    }
+}
+
 } // namespace detail
 
 template <int Order>
@@ -141,6 +186,11 @@ Gradient(amrex::Array4<amrex::Real const> const &state, const int i,
          const int j, const int k, const int c, const double dx,
          const char axis) {
     using detail::along;
+#if defined(__CUDA_ARCH__) && !defined(SH_STENCIL_FP64)
+    if constexpr (Order >= 2) {
+        return detail::gradient_fixed<Order>(state, i, j, k, c, dx, axis);
+    } else
+#endif
     if constexpr (Order == 0) {
         return 0.;
     } else if constexpr (Order == 1) {

@@ -52,8 +52,16 @@ struct Pairs {
     }
 };
 
+/* Six resident blocks per SM (at most 80 registers) for the plain stages,
+ * whose instruction mix leaves memory latency to hide; the GW and
+ * Kreiss-Oliger variants keep every register they need. */
+template <bool GW, int KO>
+constexpr int stage_min_blocks() {
+    return (GW || KO != 0) ? 1 : 6;
+}
+
 template <class H, bool GW, int KO>
-__global__ void __launch_bounds__(kTileX *kTileY)
+__global__ void __launch_bounds__(kTileX *kTileY, (stage_min_blocks<GW, KO>()))
     stage_kernel(const __grid_constant__ StageArgs a) {
     using PR = Pairs<H::kNScalars, GW>;
     constexpr int NC = PR::kNC;

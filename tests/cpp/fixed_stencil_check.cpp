@@ -89,10 +89,58 @@ bool run(std::mt19937_64 &g) {
     return true;
 }
 
+template <int Order>
+bool run_gradient(std::mt19937_64 &g) {
+    std::normal_distribution<double> nd;
+    double ef = 0, e64 = 0;
+    const double dx = 0.0625;
+    double a[N * N * N], b[N * N * N];
+    amrex::Array4<const double> s(a, N, N * N, N * N * N, amrex::Dim3{0, 0, 0},
+                                  amrex::Dim3{N, N, N}, 1);
+    amrex::Array4<const double> sb(b, N, N * N, N * N * N, amrex::Dim3{0, 0, 0},
+                                   amrex::Dim3{N, N, N}, 1);
+    const double w2[4] = {-1, 8, 1, -8};
+    const int o2[4] = {2, 1, -2, -1};
+    const double w3[6] = {1, -1, -9, 9, 45, -45};
+    const int o3[6] = {3, -3, 2, -2, 1, -1};
+    for (int it = 0; it < 100000; ++it) {
+        const double base = nd(g) * std::pow(10., (int)(g() % 40) - 20);
+        for (int q = 0; q < N * N * N; ++q)
+            a[q] = base * (1 + 1e-3 * nd(g)) + (it % 7 == 0 ? base * nd(g) : 0.);
+        const char axis = "xyz"[it % 3];
+        const int stride = axis == 'x' ? 1 : (axis == 'y' ? N : N * N);
+        __float128 acc = 0;
+        double mx = 0;
+        for (int t = 0; t < 2 * Order; ++t) {
+            const int o = Order == 2 ? o2[t] : o3[t];
+            acc += (__float128)(Order == 2 ? w2[t] : w3[t]) * a[C0 + o * stride];
+            mx = std::fmax(mx, std::fabs(a[C0 + o * stride]));
+        }
+        const double den = Order == 2 ? 12. : 60.;
+        const double ex = (double)(acc / ((__float128)den * dx));
+        const double unit = std::ldexp(1.0, std::ilogb(mx) - 52) / (den * dx);
+        const double f = detail::gradient_fixed<Order>(s, 3, 3, 3, 0, dx, axis);
+        ef = std::fmax(ef, std::fabs(f - ex) / unit);
+        e64 = std::fmax(e64, std::fabs(Gradient<Order>(s, 3, 3, 3, 0, dx, axis) - ex) / unit);
+        for (int q = 0; q < N * N * N; ++q) b[q] = -4. * a[q];
+        if (detail::gradient_fixed<Order>(sb, 3, 3, 3, 0, dx, axis) != -4. * f) {
+            std::printf("gradient scaling failed, order %d\n", Order);
+            return false;
+        }
+    }
+    std::printf("g%d %.3f %.3f\n", Order, ef, e64);
+    if (ef > e64 * 1.0001 + 1.0) {
+        std::printf("fixed gradient error above the FP64 error, order %d\n", Order);
+        return false;
+    }
+    return true;
+}
+
 } // namespace
 
 int main() {
     std::mt19937_64 g(12345);
-    const bool ok = run<1>(g) && run<2>(g) && run<3>(g);
+    const bool ok = run<1>(g) && run<2>(g) && run<3>(g) && run_gradient<2>(g) &&
+                    run_gradient<3>(g);
     return ok ? 0 : 1;
 }
