@@ -86,6 +86,42 @@ AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE unsigned long long significand(int hi, 
 /* Smallest anchor exponent: values below 2^(kMinAnchor - 1075) vanish. */
 constexpr int kMinAnchor = 128;
 
+/* acc * 2^pw * scale: one rounding in the conversion of acc, one in the
+ * product with scale (a positive factor); the power of two goes straight
+ * into the exponent field when the result is a normal number. */
+AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE double to_double(long long acc, int pw,
+                                                          double scale = 1.) {
+    if (acc == 0) return 0.;
+    const double res = (double)acc * scale;
+    const long long rb = bits(res);
+    const int er = (int)((rb >> 52) & 0x7FF) + pw;
+    if (er >= 1 && er <= 2046) return from_bits(rb + ((long long)pw << 52));
+    return scalbn(res, pw);
+}
+
+/* +-M 2^(e-A+P) truncated toward zero: the value with high word hi and low
+ * word lo in units of 2^(A-P-1075), for an anchor A >= its exponent. */
+template <int P>
+AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE long long to_fixed(int hi, unsigned lo, int A) {
+    const int d = A - expo(hi);
+    const unsigned long long m = significand<P>(hi, lo) >> (d < 63 ? d : 63);
+    return hi < 0 ? -(long long)m : (long long)m;
+}
+
+/* Largest exponent of n values (at least kMinAnchor); hi receives their
+ * high words. */
+template <int NV>
+AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE int anchor(const double (&v)[NV], int (&hi)[NV]) {
+    int A = kMinAnchor;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        hi[q] = hi_word(v[q]);
+        const int e = expo(hi[q]);
+        A = e > A ? e : A;
+    }
+    return A;
+}
+
 /* Exact weighted sum  sum_r w[r] * (sum of the values of ring r)  times
  * `scale` (a positive FP64 factor applied after the single rounding of the
  * integer sum).  Ring r has n[r] values; v lists the rings one after the
@@ -104,13 +140,7 @@ AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE double
 weighted_sum(const double (&v)[NV], const int (&n)[NR], const long long (&w)[NR],
              double scale) {
     int hi[NV];
-    int A = kMinAnchor;
-#pragma unroll
-    for (int q = 0; q < NV; ++q) {
-        hi[q] = hi_word(v[q]);
-        const int e = expo(hi[q]);
-        A = e > A ? e : A;
-    }
+    const int A = anchor(v, hi);
     if (A == 0x7FF) {
         /* NaN or infinity: FP64 sums in ring order */
         double acc = 0.;
@@ -145,15 +175,8 @@ weighted_sum(const double (&v)[NV], const int (&n)[NR], const long long (&w)[NR]
         acc += w[r] * (long long)(sp - sn);
     }
     /* acc * 2^(A + G - 1075) * scale, rounded once by the conversion and once
-     * by the product with scale; the power of two goes straight into the
-     * exponent field when the result is a normal number */
-    if (acc == 0) return 0.;
-    const int pw = A + G - 1075;
-    const double res = (double)acc * scale;
-    const long long rb = bits(res);
-    const int er = (int)((rb >> 52) & 0x7FF) + pw;
-    if (er >= 1 && er <= 2046) return from_bits(rb + ((long long)pw << 52));
-    return scalbn(res, pw);
+     * by the product with scale */
+    return to_double(acc, A + G - 1075, scale);
 }
 
 } // namespace fixed

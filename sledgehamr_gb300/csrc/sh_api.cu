@@ -19,6 +19,7 @@
 
 #include "sh_bubbles.cuh"
 #include "sh_out.cuh"
+#include "sh_fixed_stencil.h"
 #include "sh_gw.h"
 #include "sh_internal.h"
 
@@ -358,6 +359,53 @@ struct OwnerMapDev {
     int ext[3];
 };
 
+/* The children of one coarse parent from the 19 coarse values of src
+ * around index `base` (x stride 1, y stride cx, z stride cxy), evaluated
+ * exactly in 64-bit integers: every weight of the quadratic interpolation
+ * below is a multiple of 1/64 (u000: 52, the face neighbours 2 +- 8 s_d,
+ * the edge neighbours +-1 s_d s_e), so each child is an integer
+ * combination of the values written as multiples of 2^(A-3-1075)
+ * (sh_fixed_stencil.h, A their largest exponent), rounded once to FP64.
+ * The partial sums stay below 124 * 2^56 < 2^63.  Returns false (and writes
+ * nothing) when a value is not finite; the FP64 formula then runs. */
+template <class Put>
+__device__ __forceinline__ bool cf_children_fixed(const double *src, long long base, long long cx,
+                                                  long long cxy, const int P[3], const int c0[3],
+                                                  const int c1[3], Put &put) {
+    namespace fx = sledgehamr::utils::fixed;
+    const long long off[19] = {0,
+                               1, -1, cx, -cx, cxy, -cxy,
+                               1 + cx, 1 - cx, -1 + cx, -1 - cx,
+                               1 + cxy, 1 - cxy, -1 + cxy, -1 - cxy,
+                               cx + cxy, cx - cxy, -cx + cxy, -cx - cxy};
+    double v[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) v[q] = src[base + off[q]];
+    int hi[19];
+    const int A = fx::anchor(v, hi);
+    if (A == 0x7FF) return false;
+    long long t[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) t[q] = fx::to_fixed<3>(hi[q], fx::lo_word(v[q]), A);
+    const long long S = 52 * t[0] + 2 * (t[1] + t[2] + t[3] + t[4] + t[5] + t[6]);
+    const long long Ex = 8 * (t[1] - t[2]), Ey = 8 * (t[3] - t[4]), Ez = 8 * (t[5] - t[6]);
+    const long long Fxy = t[7] - t[8] - t[9] + t[10];
+    const long long Fxz = t[11] - t[12] - t[13] + t[14];
+    const long long Fyz = t[15] - t[16] - t[17] + t[18];
+    const int pw = A - 3 - 1075 - 6;
+    for (int fk = c0[2]; fk <= c1[2]; ++fk) {
+        const bool zp = (fk - 2 * P[2]) != 0;
+        for (int fj = c0[1]; fj <= c1[1]; ++fj) {
+            const bool yp = (fj - 2 * P[1]) != 0;
+            const long long yz = S + (yp ? Ey : -Ey) + (zp ? Ez : -Ez) + (yp == zp ? Fyz : -Fyz);
+            const long long slope = Ex + (yp ? Fxy : -Fxy) + (zp ? Fxz : -Fxz);
+            for (int fi = c0[0]; fi <= c1[0]; ++fi)
+                put(fi, fj, fk, fx::to_double((fi - 2 * P[0]) ? yz + slope : yz - slope, pw));
+        }
+    }
+    return true;
+}
+
 /* Quadratic (CellQuadratic) interpolation of fine cells from the 3x3x3
  * coarse cells around their parent, after linear interpolation in time
  * between the coarse old and new data (mode 0: old only, 1: new only,
@@ -408,6 +456,18 @@ __global__ void cf_interp_kernel(const CfItem *items, const BoxDev *cboxes, doub
                                 (W[2] - cb.glo[2]) * cxy;
         for (int nn = 0; nn < ncomp; ++nn) {
             const long long base = cbase + nn * cb.gvol;
+            auto put = [&](int fi, int fj, int fk, double v) {
+                if (store)
+                    store[it.first + (fi - lo[0]) +
+                          (long long)it.nx * ((fj - lo[1]) + (long long)it.ny * (fk - lo[2])) +
+                          nn * ncf] = v;
+                else
+                    fbuf[it.dst + (fi - lo[0]) + (long long)(fj - lo[1]) * it.dsy +
+                         (long long)(fk - lo[2]) * it.dsz + nn * it.dgvol] = v;
+            };
+            if (mode != 2 && cf_children_fixed(mode == 0 ? c_old : c_new, base, cx, cxy, P, c0,
+                                               c1, put))
+                continue;
             auto u = [&](int a, int b2, int d) {
                 const long long e = base + a + b2 * cx + d * cxy;
                 if (mode == 0) return c_old[e];
@@ -439,16 +499,8 @@ __global__ void cf_interp_kernel(const CfItem *items, const BoxDev *cboxes, doub
                     const double fyz = (yp == zp) ? Fyz : -Fyz;
                     const double base = S + (yp ? Ey : -Ey) + (zp ? Ez : -Ez) + fyz;
                     const double slope = Ex + (yp ? Fxy : -Fxy) + (zp ? Fxz : -Fxz);
-                    for (int fi = c0[0]; fi <= c1[0]; ++fi) {
-                        const double v = (fi - 2 * P[0]) ? base + slope : base - slope;
-                        if (store)
-                            store[it.first + (fi - lo[0]) +
-                                  (long long)it.nx * ((fj - lo[1]) + (long long)it.ny * (fk - lo[2])) +
-                                  nn * ncf] = v;
-                        else
-                            fbuf[it.dst + (fi - lo[0]) + (long long)(fj - lo[1]) * it.dsy +
-                                 (long long)(fk - lo[2]) * it.dsz + nn * it.dgvol] = v;
-                    }
+                    for (int fi = c0[0]; fi <= c1[0]; ++fi)
+                        put(fi, fj, fk, (fi - 2 * P[0]) ? base + slope : base - slope);
                 }
             }
         }
