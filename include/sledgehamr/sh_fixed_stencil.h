@@ -18,8 +18,8 @@
  * and comparable for the 19-point one.  The result scales exactly with
  * powers of two of the input and is independent of the cell's position.
  *
- * A stencil whose largest value is not finite falls back to FP64 so that
- * NaN and infinity propagate as they do in the reference; values below
+ * A stencil holding NaN or infinity gives NaN (the FP64 evaluation gives
+ * NaN or an infinity there: either way the run has diverged); values below
  * 2^-947 are treated as zero.
  */
 #ifndef SH_FIXED_STENCIL_H_
@@ -89,14 +89,30 @@ constexpr int kMinAnchor = 128;
 /* acc * 2^pw * scale: one rounding in the conversion of acc, one in the
  * product with scale (a positive factor); the power of two goes straight
  * into the exponent field when the result is a normal number. */
-AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE double to_double(long long acc, int pw,
-                                                          double scale = 1.) {
+#if defined(__CUDA_ARCH__)
+/* The rare paths live in functions of their own so that the compiler keeps
+ * them behind a branch instead of predicating their FP64 instructions into
+ * every call. */
+__device__ __noinline__ double scale_pow2_slow(double res, int pw) { return scalbn(res, pw); }
+#else
+inline double scale_pow2_slow(double res, int pw) { return std::scalbn(res, pw); }
+#endif
+
+AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE double to_double(long long acc, int pw) {
+    if (acc == 0) return 0.;
+    const double res = (double)acc;
+    const long long rb = bits(res);
+    const int er = (int)((rb >> 52) & 0x7FF) + pw;
+    if (er >= 1 && er <= 2046) return from_bits(rb + ((long long)pw << 52));
+    return scale_pow2_slow(res, pw);
+}
+AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE double to_double(long long acc, int pw, double scale) {
     if (acc == 0) return 0.;
     const double res = (double)acc * scale;
     const long long rb = bits(res);
     const int er = (int)((rb >> 52) & 0x7FF) + pw;
     if (er >= 1 && er <= 2046) return from_bits(rb + ((long long)pw << 52));
-    return scalbn(res, pw);
+    return scale_pow2_slow(res, pw);
 }
 
 /* +-M 2^(e-A+P) truncated toward zero: the value with high word hi and low
@@ -141,18 +157,7 @@ weighted_sum(const double (&v)[NV], const int (&n)[NR], const long long (&w)[NR]
              double scale) {
     int hi[NV];
     const int A = anchor(v, hi);
-    if (A == 0x7FF) {
-        /* NaN or infinity: FP64 sums in ring order */
-        double acc = 0.;
-        int q = 0;
-#pragma unroll
-        for (int r = 0; r < NR; ++r) {
-            double s = 0.;
-            for (int t = 0; t < n[r]; ++t) s += v[q++];
-            acc += (double)w[r] * s;
-        }
-        return acc * scale;
-    }
+    if (A == 0x7FF) return from_bits(0x7FF8000000000000ll); /* NaN or infinity: NaN */
     constexpr int P = G < 0 ? -G : 0;
     constexpr int R = G > 0 ? G : 0;
     long long acc = 0;

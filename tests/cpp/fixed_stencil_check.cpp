@@ -84,8 +84,7 @@ bool run(std::mt19937_64 &g) {
     a[C0] = NAN;
     if (!std::isnan(fixed_lap<Order>(a, dx2))) return false;
     a[C0] = INFINITY;
-    if (!std::isinf(fixed_lap<Order>(a, dx2)) && !std::isnan(fixed_lap<Order>(a, dx2)))
-        return false;
+    if (!std::isnan(fixed_lap<Order>(a, dx2))) return false;
     return true;
 }
 
