@@ -326,18 +326,55 @@ __global__ void move_kernel(const BoxDev *boxes, const long long *vbase, int nbo
 }
 
 /* Copies of rectangles of cells (ghost fill from the same level, periodic
- * images, or level-to-level copies): one thread block per item, threads
- * over its cells (x fastest), all components. */
-__global__ void copy_items_kernel(const CopyItem *items, double *dst, const double *src,
-                                  int ncomp) {
+ * images, or level-to-level copies): one thread block per item (at most
+ * kItemCells = 512 cells), each thread at most four of its cells.  Cell t
+ * of an item (x fastest) is split into (i, j, k) with FP32 reciprocals of
+ * nx and nx*ny taken once per item instead of integer divisions per cell:
+ * for t < 512 the product (t + 1/2) * (1/m) is within 512 * 2^-23 of
+ * (t + 1/2) / m, whose distance to the nearest integer is at least
+ * 1/(2m) >= 2^-10, so the truncation is exact (checked for every item
+ * shape).  Four components of all the thread's cells are loaded before any
+ * is stored, so the copy is not bound by load latency.  dst and src may be
+ * the same buffer: the cells written (ghost cells) are never read by the
+ * same launch. */
+constexpr int kCopyThreads = 128;
+__global__ void __launch_bounds__(kCopyThreads)
+    copy_items_kernel(const CopyItem *__restrict__ items, double *__restrict__ dst,
+                      const double *__restrict__ src, int ncomp) {
     const CopyItem it = items[blockIdx.x];
-    const int n = it.nx * it.ny * it.nz;
-    for (int t = threadIdx.x; t < n; t += blockDim.x) {
-        const int i = t % it.nx, r = t / it.nx;
-        const int j = r % it.ny, k = r / it.ny;
-        const long long d = it.dst + i + (long long)j * it.dsy + (long long)k * it.dsz;
-        const long long s = it.src + i + (long long)j * it.ssy + (long long)k * it.ssz;
-        for (int c = 0; c < ncomp; ++c) dst[d + c * it.dgvol] = src[s + c * it.sgvol];
+    const int nxy = it.nx * it.ny;
+    const int n = nxy * it.nz;
+    const float inv_nx = 1.f / (float)it.nx, inv_nxy = 1.f / (float)nxy;
+    /* the (at most four) cells of this thread, then four components of all
+     * of them in flight at once */
+    constexpr int kCells = kItemCells / kCopyThreads;
+    long long d[kCells], s[kCells];
+    int nc = 0;
+#pragma unroll
+    for (int q = 0; q < kCells; ++q) {
+        const int t = threadIdx.x + q * kCopyThreads;
+        if (t < n) {
+            const int k = (int)(((float)t + 0.5f) * inv_nxy);
+            const int r = t - k * nxy;
+            const int j = (int)(((float)r + 0.5f) * inv_nx);
+            const int i = r - j * it.nx;
+            d[q] = it.dst + i + (long long)j * it.dsy + (long long)k * it.dsz;
+            s[q] = it.src + i + (long long)j * it.ssy + (long long)k * it.ssz;
+            nc = q + 1;
+        }
+    }
+    for (int c0 = 0; c0 < ncomp; c0 += 4) {
+        double v[kCells][4];
+#pragma unroll
+        for (int q = 0; q < kCells; ++q)
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                if (q < nc && c0 + c < ncomp) v[q][c] = __ldg(src + s[q] + (c0 + c) * it.sgvol);
+#pragma unroll
+        for (int q = 0; q < kCells; ++q)
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                if (q < nc && c0 + c < ncomp) dst[d[q] + (c0 + c) * it.dgvol] = v[q][c];
     }
 }
 
@@ -1247,7 +1284,7 @@ void ensure_kbuf(sh_ctx *ctx, sh_level *L, size_t elems, int count) {
 void fill_patch(sh_ctx *ctx, sh_level *L, double *buf, double t) {
     if (L->nghost_items > 0) {
         ProfScope ps(ctx, kProfFill);
-        copy_items_kernel<<<L->nghost_items, 128, 0, ctx->stream>>>(L->d_ghost, buf, buf,
+        copy_items_kernel<<<L->nghost_items, kCopyThreads, 0, ctx->stream>>>(L->d_ghost, buf, buf,
                                                                    L->ncomp);
         ctx->launches++;
         ck(cudaGetLastError(), "ghost fill launch");
@@ -1901,7 +1938,7 @@ int sh_level_fill_from(sh_ctx *ctx, sh_level *dst, int which_dst, const sh_level
             const std::vector<CopyItem> items = copy_items(P.rects, dst, src);
             d_rects = upload_items(ctx, items, "fill plan");
             ProfScope ps(ctx, kProfFill);
-            copy_items_kernel<<<(int)items.size(), 128, 0, ctx->stream>>>(
+            copy_items_kernel<<<(int)items.size(), kCopyThreads, 0, ctx->stream>>>(
                 d_rects, dst->buf[which_dst], src->buf[which_src], dst->ncomp);
             ctx->launches++;
             ck(cudaGetLastError(), "fill copy launch");
