@@ -327,54 +327,27 @@ __global__ void move_kernel(const BoxDev *boxes, const long long *vbase, int nbo
 
 /* Copies of rectangles of cells (ghost fill from the same level, periodic
  * images, or level-to-level copies): one thread block per item (at most
- * kItemCells = 512 cells), each thread at most four of its cells.  Cell t
- * of an item (x fastest) is split into (i, j, k) with FP32 reciprocals of
- * nx and nx*ny taken once per item instead of integer divisions per cell:
- * for t < 512 the product (t + 1/2) * (1/m) is within 512 * 2^-23 of
+ * kItemCells = 512 cells), threads over its cells (x fastest), all
+ * components.  Cell t is split into (i, j, k) with FP32 reciprocals of nx
+ * and nx*ny taken once per item instead of integer divisions per cell: for
+ * t < 512 the product (t + 1/2) * (1/m) is within 512 * 2^-23 of
  * (t + 1/2) / m, whose distance to the nearest integer is at least
  * 1/(2m) >= 2^-10, so the truncation is exact (checked for every item
- * shape).  Four components of all the thread's cells are loaded before any
- * is stored, so the copy is not bound by load latency.  dst and src may be
- * the same buffer: the cells written (ghost cells) are never read by the
- * same launch. */
-constexpr int kCopyThreads = 128;
-__global__ void __launch_bounds__(kCopyThreads)
-    copy_items_kernel(const CopyItem *__restrict__ items, double *__restrict__ dst,
-                      const double *__restrict__ src, int ncomp) {
+ * shape). */
+__global__ void copy_items_kernel(const CopyItem *items, double *dst, const double *src,
+                                  int ncomp) {
     const CopyItem it = items[blockIdx.x];
     const int nxy = it.nx * it.ny;
     const int n = nxy * it.nz;
     const float inv_nx = 1.f / (float)it.nx, inv_nxy = 1.f / (float)nxy;
-    /* the (at most four) cells of this thread, then four components of all
-     * of them in flight at once */
-    constexpr int kCells = kItemCells / kCopyThreads;
-    long long d[kCells], s[kCells];
-    int nc = 0;
-#pragma unroll
-    for (int q = 0; q < kCells; ++q) {
-        const int t = threadIdx.x + q * kCopyThreads;
-        if (t < n) {
-            const int k = (int)(((float)t + 0.5f) * inv_nxy);
-            const int r = t - k * nxy;
-            const int j = (int)(((float)r + 0.5f) * inv_nx);
-            const int i = r - j * it.nx;
-            d[q] = it.dst + i + (long long)j * it.dsy + (long long)k * it.dsz;
-            s[q] = it.src + i + (long long)j * it.ssy + (long long)k * it.ssz;
-            nc = q + 1;
-        }
-    }
-    for (int c0 = 0; c0 < ncomp; c0 += 4) {
-        double v[kCells][4];
-#pragma unroll
-        for (int q = 0; q < kCells; ++q)
-#pragma unroll
-            for (int c = 0; c < 4; ++c)
-                if (q < nc && c0 + c < ncomp) v[q][c] = __ldg(src + s[q] + (c0 + c) * it.sgvol);
-#pragma unroll
-        for (int q = 0; q < kCells; ++q)
-#pragma unroll
-            for (int c = 0; c < 4; ++c)
-                if (q < nc && c0 + c < ncomp) dst[d[q] + (c0 + c) * it.dgvol] = v[q][c];
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        const int k = (int)(((float)t + 0.5f) * inv_nxy);
+        const int r = t - k * nxy;
+        const int j = (int)(((float)r + 0.5f) * inv_nx);
+        const int i = r - j * it.nx;
+        const long long d = it.dst + i + (long long)j * it.dsy + (long long)k * it.dsz;
+        const long long s = it.src + i + (long long)j * it.ssy + (long long)k * it.ssz;
+        for (int c = 0; c < ncomp; ++c) dst[d + c * it.dgvol] = src[s + c * it.sgvol];
     }
 }
 
@@ -1284,7 +1257,7 @@ void ensure_kbuf(sh_ctx *ctx, sh_level *L, size_t elems, int count) {
 void fill_patch(sh_ctx *ctx, sh_level *L, double *buf, double t) {
     if (L->nghost_items > 0) {
         ProfScope ps(ctx, kProfFill);
-        copy_items_kernel<<<L->nghost_items, kCopyThreads, 0, ctx->stream>>>(L->d_ghost, buf, buf,
+        copy_items_kernel<<<L->nghost_items, 128, 0, ctx->stream>>>(L->d_ghost, buf, buf,
                                                                    L->ncomp);
         ctx->launches++;
         ck(cudaGetLastError(), "ghost fill launch");
@@ -1413,23 +1386,34 @@ void integrate(sh_ctx *ctx, sh_level *L, int type, const double *tableau, int ns
             StageArgs s = a;
             s.state = L->buf[cur];
             s.time = t0 + dt * tb.nodes[i];
-            s.nkin = i;
-            for (int j = 0; j < i; ++j) s.kin[j] = kb[j];
             const int next = (cur == SH_NEW) ? 2 : SH_NEW;
             s.out = L->buf[next];
+            /* earlier K with a zero coefficient (RKN4: a_31) would add an
+             * exact zero for finite data: they are left out of the stage's
+             * list, so their buffers are not read */
+            s.nkin = 0;
             if (i < S - 1) {
                 s.epi = kEpiRknStage;
                 s.kout = kb[i];
                 s.c_mom = dt * tb.nodes[i + 1];
-                for (int j = 0; j <= i; ++j) s.c_k[j] = dt * dt * tb.a[i + 1][j];
+                for (int j = 0; j < i; ++j)
+                    if (tb.a[i + 1][j] != 0.) {
+                        s.kin[s.nkin] = kb[j];
+                        s.c_k[s.nkin++] = dt * dt * tb.a[i + 1][j];
+                    }
+                s.c_k[s.nkin] = dt * dt * tb.a[i + 1][i];
             } else {
                 s.epi = kEpiRknFinal;
                 s.kout = nullptr;
                 s.c_mom = dt;
-                for (int j = 0; j < S; ++j) {
-                    s.c_k[j] = dt * dt * tb.bbar[j];
-                    s.c_k2[j] = dt * tb.b[j];
-                }
+                for (int j = 0; j < S - 1; ++j)
+                    if (tb.bbar[j] != 0. || tb.b[j] != 0.) {
+                        s.kin[s.nkin] = kb[j];
+                        s.c_k[s.nkin] = dt * dt * tb.bbar[j];
+                        s.c_k2[s.nkin++] = dt * tb.b[j];
+                    }
+                s.c_k[s.nkin] = dt * dt * tb.bbar[S - 1];
+                s.c_k2[s.nkin] = dt * tb.b[S - 1];
             }
             launch_stage(ctx, L, s, ko_order);
             fill_patch(ctx, L, L->buf[next], i < S - 1 ? t0 + dt * tb.nodes[i + 1] : t0 + dt);
@@ -1938,7 +1922,7 @@ int sh_level_fill_from(sh_ctx *ctx, sh_level *dst, int which_dst, const sh_level
             const std::vector<CopyItem> items = copy_items(P.rects, dst, src);
             d_rects = upload_items(ctx, items, "fill plan");
             ProfScope ps(ctx, kProfFill);
-            copy_items_kernel<<<(int)items.size(), kCopyThreads, 0, ctx->stream>>>(
+            copy_items_kernel<<<(int)items.size(), 128, 0, ctx->stream>>>(
                 d_rects, dst->buf[which_dst], src->buf[which_src], dst->ncomp);
             ctx->launches++;
             ck(cudaGetLastError(), "fill copy launch");

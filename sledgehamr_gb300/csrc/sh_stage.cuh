@@ -119,11 +119,8 @@ __global__ void __launch_bounds__(kTileX *kTileY, (stage_min_blocks<GW, KO>()))
                 double y = a.y0[sbase + PR::pos(q) * gvol];
                 const double m = a.y0[sbase + PR::mom(q) * gvol];
                 y += a.c_mom * m;
-                /* terms with a zero tableau coefficient (RKN4: a_31) add an
-                 * exact zero for finite data: their K buffer is not read */
-                for (int s = 0; s < a.nkin; ++s)
-                    if (a.c_k[s] != 0.) y += a.c_k[s] * a.kin[s][kb + q * gvol];
-                if (a.c_k[a.nkin] != 0.) y += a.c_k[a.nkin] * kq;
+                for (int s = 0; s < a.nkin; ++s) y += a.c_k[s] * a.kin[s][kb + q * gvol];
+                y += a.c_k[a.nkin] * kq;
                 a.out[sbase + PR::pos(q) * gvol] = y;
                 a.out[sbase + PR::mom(q) * gvol] = m;
             }
@@ -137,14 +134,13 @@ __global__ void __launch_bounds__(kTileX *kTileY, (stage_min_blocks<GW, KO>()))
                 double m = a.y0[sbase + PR::mom(q) * gvol];
                 y += a.c_mom * m;
                 for (int s = 0; s < a.nkin; ++s) {
-                    if (a.c_k[s] == 0. && a.c_k2[s] == 0.) continue;
                     const double ks = a.kin[s][kb + q * gvol];
-                    if (a.c_k[s] != 0.) y += a.c_k[s] * ks;
-                    if (a.c_k2[s] != 0.) m += a.c_k2[s] * ks;
+                    y += a.c_k[s] * ks;
+                    m += a.c_k2[s] * ks;
                 }
                 const double kq = r[PR::mom(q)];
-                if (a.c_k[a.nkin] != 0.) y += a.c_k[a.nkin] * kq; /* RKN4: bbar_3 = 0 */
-                if (a.c_k2[a.nkin] != 0.) m += a.c_k2[a.nkin] * kq;
+                y += a.c_k[a.nkin] * kq;
+                m += a.c_k2[a.nkin] * kq;
                 a.out[sbase + PR::pos(q) * gvol] = y;
                 a.out[sbase + PR::mom(q) * gvol] = m;
             }
