@@ -870,17 +870,29 @@ void build_owner_map(sh_ctx *ctx, sh_level *L) {
     if (res <= 0) res = 1;
     L->owner_res = res;
     for (int d = 0; d < 3; ++d) L->owner_nb[d] = (L->dhi[d] - L->dlo[d] + 1) / res;
-    L->owner.assign((size_t)L->owner_nb[0] * L->owner_nb[1] * L->owner_nb[2], -1);
-    for (size_t q = 0; q < L->boxes.size(); ++q) {
+    const long long nmap = (long long)L->owner_nb[0] * L->owner_nb[1] * L->owner_nb[2];
+    L->owner.resize((size_t)nmap);
+    int *own = L->owner.data();
+#pragma omp parallel for schedule(static)
+    for (long long q = 0; q < nmap; ++q) own[q] = -1;
+    /* boxes in parallel; overlapping boxes would leave fewer owned blocks
+     * than the boxes hold, which the count below detects */
+    const long long nbx = (long long)L->boxes.size();
+    long long want = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : want)
+    for (long long q = 0; q < nbx; ++q) {
         const sh_box &b = L->boxes[q];
         for (int z = (b.lo[2] - L->dlo[2]) / res; z <= (b.hi[2] - L->dlo[2]) / res; ++z)
             for (int y = (b.lo[1] - L->dlo[1]) / res; y <= (b.hi[1] - L->dlo[1]) / res; ++y)
                 for (int x = (b.lo[0] - L->dlo[0]) / res; x <= (b.hi[0] - L->dlo[0]) / res; ++x) {
-                    int &o = L->owner[((size_t)z * L->owner_nb[1] + y) * L->owner_nb[0] + x];
-                    if (o >= 0) throw ShError(SH_ERR_ARG, "boxes of a level overlap");
-                    o = (int)q;
+                    own[((size_t)z * L->owner_nb[1] + y) * L->owner_nb[0] + x] = (int)q;
+                    ++want;
                 }
     }
+    long long have = 0;
+#pragma omp parallel for schedule(static) reduction(+ : have)
+    for (long long q = 0; q < nmap; ++q) have += own[q] >= 0;
+    if (have != want) throw ShError(SH_ERR_ARG, "boxes of a level overlap");
     L->d_owner = upload_async(ctx, L->owner.data(), L->owner.size(), "owner map");
 }
 
@@ -912,7 +924,7 @@ struct FillPlan {
 };
 
 FillPlan build_fill_plan(const sh_level *D, const sh_level *S, const sh_level *C,
-                         bool ghosts_only) {
+                         bool ghosts_only, bool want_copies = true) {
     FillPlan P;
     const int ext[3] = {D->dhi[0] - D->dlo[0] + 1, D->dhi[1] - D->dlo[1] + 1,
                         D->dhi[2] - D->dlo[2] + 1};
@@ -995,31 +1007,7 @@ FillPlan build_fill_plan(const sh_level *D, const sh_level *S, const sh_level *C
                         continue;
                     }
                     if (!C) continue; /* nothing to fill from: left as is */
-                    /* the parents of the region must lie on the coarse level
-                     * (checked per coarse block) */
-                    const int Rc = C->owner_res;
-                    int pb0[3], pb1[3];
-                    for (int d = 0; d < 3; ++d) {
-                        pb0[d] = floordiv(floordiv(k.lo[d], 2) - C->dlo[d], Rc);
-                        pb1[d] = floordiv(floordiv(k.hi[d], 2) - C->dlo[d], Rc);
-                    }
-                    for (int pz = pb0[2]; pz <= pb1[2]; ++pz)
-                        for (int py = pb0[1]; py <= pb1[1]; ++py)
-                            for (int px = pb0[0]; px <= pb1[0]; ++px) {
-                                const int p3[3] = {px, py, pz};
-                                int cb[3];
-                                for (int d = 0; d < 3; ++d) {
-                                    const int n = C->owner_nb[d];
-                                    cb[d] = ((p3[d] % n) + n) % n;
-                                }
-                                if (C->owner[((size_t)cb[2] * C->owner_nb[1] + cb[1]) *
-                                                 C->owner_nb[0] +
-                                             cb[0]] < 0) {
-#pragma omp atomic write
-                                    uncovered = true;
-                                }
-                            }
-                    k.kind = 2;
+                    k.kind = 2; /* parents checked per merged rectangle below */
                 }
         /* x-runs of equal kind / source */
         runs.clear();
@@ -1073,6 +1061,7 @@ FillPlan build_fill_plan(const sh_level *D, const sh_level *S, const sh_level *C
         }
         for (const Run &r : runs) {
             if (r.kind == 1) {
+                if (!want_copies) continue;
                 GhostCopyDev c;
                 c.dbox = (int)b;
                 c.sbox = r.own;
@@ -1083,6 +1072,30 @@ FillPlan build_fill_plan(const sh_level *D, const sh_level *S, const sh_level *C
                 }
                 box_rects[b].push_back(c);
             } else {
+                /* the parents of the region must lie on the coarse level
+                 * (checked per coarse block) */
+                const int Rc = C->owner_res;
+                int pb0[3], pb1[3];
+                for (int d = 0; d < 3; ++d) {
+                    pb0[d] = floordiv(floordiv(r.lo[d], 2) - C->dlo[d], Rc);
+                    pb1[d] = floordiv(floordiv(r.hi[d], 2) - C->dlo[d], Rc);
+                }
+                for (int pz = pb0[2]; pz <= pb1[2]; ++pz)
+                    for (int py = pb0[1]; py <= pb1[1]; ++py)
+                        for (int px = pb0[0]; px <= pb1[0]; ++px) {
+                            const int p3[3] = {px, py, pz};
+                            int cb[3];
+                            for (int d = 0; d < 3; ++d) {
+                                const int n = C->owner_nb[d];
+                                cb[d] = ((p3[d] % n) + n) % n;
+                            }
+                            if (C->owner[((size_t)cb[2] * C->owner_nb[1] + cb[1]) *
+                                             C->owner_nb[0] +
+                                         cb[0]] < 0) {
+#pragma omp atomic write
+                                uncovered = true;
+                            }
+                        }
                 CfRect c;
                 c.dbox = (int)b;
                 for (int d = 0; d < 3; ++d) {
@@ -1137,6 +1150,39 @@ void split_rect(const int lo[3], const int hi[3], F &&emit) {
     }
 }
 
+/* Number of pieces split_rect makes of [lo, hi]. */
+inline long long split_count(const int lo[3], const int hi[3]) {
+    const long long nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
+    if (nx * ny <= kItemCells) {
+        const long long pz = std::max<long long>(1, kItemCells / (nx * ny));
+        return (nz + pz - 1) / pz;
+    }
+    if (nx <= kItemCells) {
+        const long long py = std::max<long long>(1, kItemCells / nx);
+        return nz * ((ny + py - 1) / py);
+    }
+    return nz * ny * ((nx + kItemCells - 1) / kItemCells);
+}
+
+/* Items of all rectangles, in rectangle order, made by host threads:
+ * make(rect, x, y, z, nx, ny, nz, cells of the rectangle's earlier pieces). */
+template <class Item, class Rect, class Make>
+std::vector<Item> expand_items(const std::vector<Rect> &rects, Make make) {
+    const long long n = (long long)rects.size();
+    std::vector<long long> off(n + 1, 0);
+    for (long long q = 0; q < n; ++q) off[q + 1] = off[q] + split_count(rects[q].lo, rects[q].hi);
+    std::vector<Item> items((size_t)off[n]);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (long long q = 0; q < n; ++q) {
+        long long at = off[q], before = 0;
+        split_rect(rects[q].lo, rects[q].hi, [&](int x, int y, int z, int nx, int ny, int nz) {
+            items[at++] = make(rects[q], x, y, z, nx, ny, nz, before);
+            before += (long long)nx * ny * nz;
+        });
+    }
+    return items;
+}
+
 inline long long cell_offset(const BoxDev &b, int ncomp, int i, int j, int k) {
     return b.off * ncomp + (i - b.glo[0]) + (long long)(j - b.glo[1]) * b.gdim[0] +
            (long long)(k - b.glo[2]) * b.gdim[0] * b.gdim[1];
@@ -1144,12 +1190,10 @@ inline long long cell_offset(const BoxDev &b, int ncomp, int i, int j, int k) {
 
 std::vector<CopyItem> copy_items(const std::vector<GhostCopyDev> &rects, const sh_level *D,
                                  const sh_level *S) {
-    std::vector<CopyItem> items;
-    items.reserve(rects.size());
-    for (const GhostCopyDev &r : rects) {
-        const BoxDev &db = D->hboxes[r.dbox];
-        const BoxDev &sb = S->hboxes[r.sbox];
-        split_rect(r.lo, r.hi, [&](int x, int y, int z, int nx, int ny, int nz) {
+    return expand_items<CopyItem>(
+        rects, [&](const GhostCopyDev &r, int x, int y, int z, int nx, int ny, int nz, long long) {
+            const BoxDev &db = D->hboxes[r.dbox];
+            const BoxDev &sb = S->hboxes[r.sbox];
             CopyItem it;
             it.dst = cell_offset(db, D->ncomp, x, y, z);
             it.src = cell_offset(sb, S->ncomp, x - r.shift[0], y - r.shift[1], z - r.shift[2]);
@@ -1162,22 +1206,16 @@ std::vector<CopyItem> copy_items(const std::vector<GhostCopyDev> &rects, const s
             it.dsz = db.gdim[0] * db.gdim[1];
             it.ssy = sb.gdim[0];
             it.ssz = sb.gdim[0] * sb.gdim[1];
-            items.push_back(it);
+            return it;
         });
-    }
-    return items;
 }
 
 std::vector<CfItem> cf_items(const std::vector<CfRect> &rects, const sh_level *D) {
-    std::vector<CfItem> items;
-    items.reserve(rects.size());
-    long long first = 0;
-    for (const CfRect &r : rects) {
-        const BoxDev &db = D->hboxes[r.dbox];
-        split_rect(r.lo, r.hi, [&](int x, int y, int z, int nx, int ny, int nz) {
+    return expand_items<CfItem>(
+        rects, [&](const CfRect &r, int x, int y, int z, int nx, int ny, int nz, long long before) {
+            const BoxDev &db = D->hboxes[r.dbox];
             CfItem it;
-            it.first = first;
-            first += (long long)nx * ny * nz;
+            it.first = r.first + before;
             it.dst = cell_offset(db, D->ncomp, x, y, z);
             it.dgvol = db.gvol;
             it.dsy = db.gdim[0];
@@ -1189,10 +1227,8 @@ std::vector<CfItem> cf_items(const std::vector<CfRect> &rects, const sh_level *D
             it.ny = ny;
             it.nz = nz;
             it.pad = 0;
-            items.push_back(it);
+            return it;
         });
-    }
-    return items;
 }
 
 template <class T>
@@ -1897,7 +1933,7 @@ int sh_level_set_coarse(sh_ctx *ctx, sh_level *fine, sh_level *coarse) {
         fine->coarse = nullptr;
         if (!coarse) return;
         require(coarse != fine, "a level cannot be its own coarse level");
-        FillPlan P = build_fill_plan(fine, fine, coarse, true);
+        FillPlan P = build_fill_plan(fine, fine, coarse, true, false);
         const std::vector<CfItem> items = cf_items(P.cf, fine);
         fine->d_cf = upload_items(ctx, items, "coarse-fine plan");
         fine->ncf_items = (int)items.size();

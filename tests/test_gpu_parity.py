@@ -248,3 +248,21 @@ def test_errors_are_reported_not_raised_on_device(ctx):
     # the context is still usable
     out = ctx.evolve_periodic("AxionStrings", sh.RKN4, st, t0=1.0, dt=0.06, dx=0.25, nsteps=1)
     assert np.isfinite(out).all()
+
+
+def test_level_errors_overlap_and_nesting(ctx):
+    """Overlapping boxes are rejected at level creation, and a coarse level
+    that does not cover the cells to interpolate is rejected by the fill."""
+    with pytest.raises(sh.ShError):
+        sh.Level(ctx, "AxionStringsLap1", [((0, 0, 0), (15, 15, 15)), ((8, 8, 8), (23, 23, 23))],
+                 (0, 0, 0), (31, 31, 31), 1)
+    coarse = sh.Level(ctx, "AxionStringsLap1", [((0, 0, 0), (7, 7, 7))], (0, 0, 0),
+                      (15, 15, 15), 1)
+    fine = sh.Level(ctx, "AxionStringsLap1", [((16, 16, 16), (23, 23, 23))], (0, 0, 0),
+                    (31, 31, 31), 1)
+    import ctypes as C
+    rc = ctx.lib.sh_level_fill_from(ctx.h, fine.h, sh.SH_NEW, None, sh.SH_NEW, coarse.h,
+                                    C.c_double(0.0))
+    assert rc != 0 and "nested" in ctx.lib.sh_ctx_last_error(ctx.h).decode()
+    fine.close()
+    coarse.close()
