@@ -216,20 +216,45 @@ inline void cluster(const BlockSet &t, IBox bx, double eff, std::vector<IBox> &o
     cluster(t, r, eff, out);
 }
 
-/* Boxes sharing a whole face are merged (BoxList::simplify). */
+/* Boxes sharing a whole face are merged (BoxList::simplify).  Each pass
+ * orders the boxes by (lo[e], hi[e], lo[f], hi[f], lo[d]); the boxes are
+ * disjoint, so that key is unique and any sort gives the same order.  With
+ * coordinates in [0, 4096) the key is packed into one 64-bit integer. */
 inline void simplify(std::vector<IBox> &v) {
+    bool small = true;
+    for (const IBox &x : v)
+        for (int d = 0; d < 3; ++d) small = small && x.lo[d] >= 0 && x.hi[d] < 4096;
+    std::vector<std::pair<unsigned long long, unsigned>> keyed;
+    std::vector<IBox> sorted;
     bool any = true;
     while (any) {
         any = false;
         for (int d = 0; d < 3; ++d) {
             const int e = (d + 1) % 3, f = (d + 2) % 3;
-            std::sort(v.begin(), v.end(), [&](const IBox &a, const IBox &b) {
-                if (a.lo[e] != b.lo[e]) return a.lo[e] < b.lo[e];
-                if (a.hi[e] != b.hi[e]) return a.hi[e] < b.hi[e];
-                if (a.lo[f] != b.lo[f]) return a.lo[f] < b.lo[f];
-                if (a.hi[f] != b.hi[f]) return a.hi[f] < b.hi[f];
-                return a.lo[d] < b.lo[d];
-            });
+            if (small) {
+                keyed.resize(v.size());
+                for (size_t q = 0; q < v.size(); ++q) {
+                    const IBox &a = v[q];
+                    keyed[q].first = ((unsigned long long)a.lo[e] << 48) |
+                                     ((unsigned long long)a.hi[e] << 36) |
+                                     ((unsigned long long)a.lo[f] << 24) |
+                                     ((unsigned long long)a.hi[f] << 12) |
+                                     (unsigned long long)a.lo[d];
+                    keyed[q].second = (unsigned)q;
+                }
+                std::sort(keyed.begin(), keyed.end());
+                sorted.resize(v.size());
+                for (size_t q = 0; q < v.size(); ++q) sorted[q] = v[keyed[q].second];
+                v.swap(sorted);
+            } else {
+                std::sort(v.begin(), v.end(), [&](const IBox &a, const IBox &b) {
+                    if (a.lo[e] != b.lo[e]) return a.lo[e] < b.lo[e];
+                    if (a.hi[e] != b.hi[e]) return a.hi[e] < b.hi[e];
+                    if (a.lo[f] != b.lo[f]) return a.lo[f] < b.lo[f];
+                    if (a.hi[f] != b.hi[f]) return a.hi[f] < b.hi[f];
+                    return a.lo[d] < b.lo[d];
+                });
+            }
             std::vector<IBox> res;
             for (const IBox &x : v) {
                 if (!res.empty()) {
