@@ -334,6 +334,7 @@ __global__ void move_kernel(const BoxDev *boxes, const long long *vbase, int nbo
  * (t + 1/2) / m, whose distance to the nearest integer is at least
  * 1/(2m) >= 2^-10, so the truncation is exact (checked for every item
  * shape). */
+constexpr int kItemThreads = 128; /* threads per item of the copy and combine kernels */
 __global__ void copy_items_kernel(const CopyItem *items, double *dst, const double *src,
                                   int ncomp) {
     const CopyItem it = items[blockIdx.x];
@@ -524,10 +525,15 @@ __global__ void cf_combine_kernel(const CfItem *items, double *fbuf, const doubl
                                   const double *i_new, int mode, double alpha, double beta,
                                   int ncomp, long long ncf) {
     const CfItem it = items[blockIdx.x];
-    const int n = it.nx * it.ny * it.nz;
+    const int nxy = it.nx * it.ny;
+    const int n = nxy * it.nz;
+    const float inv_nx = 1.f / (float)it.nx, inv_nxy = 1.f / (float)nxy;
     for (int q = threadIdx.x; q < n; q += blockDim.x) {
-        const int i = q % it.nx, r = q / it.nx;
-        const int j = r % it.ny, k = r / it.ny;
+        /* exact for q < kItemCells (see copy_items_kernel) */
+        const int k = (int)(((float)q + 0.5f) * inv_nxy);
+        const int r = q - k * nxy;
+        const int j = (int)(((float)r + 0.5f) * inv_nx);
+        const int i = r - j * it.nx;
         const long long d = it.dst + i + (long long)j * it.dsy + (long long)k * it.dsz;
         const long long c = it.first + q;
         for (int nn = 0; nn < ncomp; ++nn) {
@@ -1293,7 +1299,7 @@ void ensure_kbuf(sh_ctx *ctx, sh_level *L, size_t elems, int count) {
 void fill_patch(sh_ctx *ctx, sh_level *L, double *buf, double t) {
     if (L->nghost_items > 0) {
         ProfScope ps(ctx, kProfFill);
-        copy_items_kernel<<<L->nghost_items, 128, 0, ctx->stream>>>(L->d_ghost, buf, buf,
+        copy_items_kernel<<<L->nghost_items, kItemThreads, 0, ctx->stream>>>(L->d_ghost, buf, buf,
                                                                    L->ncomp);
         ctx->launches++;
         ck(cudaGetLastError(), "ghost fill launch");
@@ -1322,7 +1328,7 @@ void fill_patch(sh_ctx *ctx, sh_level *L, double *buf, double t) {
         int mode;
         double alpha, beta;
         coarse_time_weights(C, t, mode, alpha, beta);
-        cf_combine_kernel<<<L->ncf_items, 128, 0, ctx->stream>>>(
+        cf_combine_kernel<<<L->ncf_items, kItemThreads, 0, ctx->stream>>>(
             L->d_cf, buf, L->cf_old, L->cf_new, mode, alpha, beta, L->ncomp, L->ncf);
         ctx->launches++;
         ck(cudaGetLastError(), "coarse-fine fill launch");
@@ -1958,7 +1964,7 @@ int sh_level_fill_from(sh_ctx *ctx, sh_level *dst, int which_dst, const sh_level
             const std::vector<CopyItem> items = copy_items(P.rects, dst, src);
             d_rects = upload_items(ctx, items, "fill plan");
             ProfScope ps(ctx, kProfFill);
-            copy_items_kernel<<<(int)items.size(), 128, 0, ctx->stream>>>(
+            copy_items_kernel<<<(int)items.size(), kItemThreads, 0, ctx->stream>>>(
                 d_rects, dst->buf[which_dst], src->buf[which_src], dst->ncomp);
             ctx->launches++;
             ck(cudaGetLastError(), "fill copy launch");
