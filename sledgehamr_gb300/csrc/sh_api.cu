@@ -333,10 +333,13 @@ __global__ void move_kernel(const BoxDev *boxes, const long long *vbase, int nbo
  * t < 512 the product (t + 1/2) * (1/m) is within 512 * 2^-23 of
  * (t + 1/2) / m, whose distance to the nearest integer is at least
  * 1/(2m) >= 2^-10, so the truncation is exact (checked for every item
- * shape). */
+ * shape).  dst and src may be the same buffer (ghost fill): the cells
+ * written (ghost cells) are never read by the same launch, so the
+ * pointers are restrict-qualified and a cell's components are all loaded
+ * before any is stored. */
 constexpr int kItemThreads = 128; /* threads per item of the copy and combine kernels */
-__global__ void copy_items_kernel(const CopyItem *items, double *dst, const double *src,
-                                  int ncomp) {
+__global__ void copy_items_kernel(const CopyItem *__restrict__ items, double *__restrict__ dst,
+                                  const double *__restrict__ src, int ncomp) {
     const CopyItem it = items[blockIdx.x];
     const int nxy = it.nx * it.ny;
     const int n = nxy * it.nz;
@@ -348,7 +351,16 @@ __global__ void copy_items_kernel(const CopyItem *items, double *dst, const doub
         const int i = r - j * it.nx;
         const long long d = it.dst + i + (long long)j * it.dsy + (long long)k * it.dsz;
         const long long s = it.src + i + (long long)j * it.ssy + (long long)k * it.ssz;
-        for (int c = 0; c < ncomp; ++c) dst[d + c * it.dgvol] = src[s + c * it.sgvol];
+        /* four components in flight: loaded before any is stored */
+        for (int c0 = 0; c0 < ncomp; c0 += 4) {
+            double v[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                if (c0 + c < ncomp) v[c] = __ldg(src + s + (c0 + c) * it.sgvol);
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                if (c0 + c < ncomp) dst[d + (c0 + c) * it.dgvol] = v[c];
+        }
     }
 }
 
@@ -521,9 +533,10 @@ __global__ void cf_interp_kernel(const CfItem *items, const BoxDev *cboxes, doub
 /* Coarse-fine ghost cells from the stored spatial interpolations of the
  * coarse old and new data: the interpolation is linear in the coarse data,
  * so interpolating alpha old + beta new equals alpha I(old) + beta I(new). */
-__global__ void cf_combine_kernel(const CfItem *items, double *fbuf, const double *i_old,
-                                  const double *i_new, int mode, double alpha, double beta,
-                                  int ncomp, long long ncf) {
+__global__ void cf_combine_kernel(const CfItem *__restrict__ items, double *__restrict__ fbuf,
+                                  const double *__restrict__ i_old,
+                                  const double *__restrict__ i_new, int mode, double alpha,
+                                  double beta, int ncomp, long long ncf) {
     const CfItem it = items[blockIdx.x];
     const int nxy = it.nx * it.ny;
     const int n = nxy * it.nz;
@@ -536,13 +549,20 @@ __global__ void cf_combine_kernel(const CfItem *items, double *fbuf, const doubl
         const int i = r - j * it.nx;
         const long long d = it.dst + i + (long long)j * it.dsy + (long long)k * it.dsz;
         const long long c = it.first + q;
-        for (int nn = 0; nn < ncomp; ++nn) {
-            const long long e = c + nn * ncf;
-            double v;
-            if (mode == 0) v = i_old[e];
-            else if (mode == 1) v = i_new[e];
-            else v = alpha * i_old[e] + beta * i_new[e];
-            fbuf[d + nn * it.dgvol] = v;
+        /* four components in flight: loaded before any is stored */
+        for (int c0 = 0; c0 < ncomp; c0 += 4) {
+            double v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (c0 + u >= ncomp) continue;
+                const long long e = c + (c0 + u) * ncf;
+                if (mode == 0) v[u] = __ldg(i_old + e);
+                else if (mode == 1) v[u] = __ldg(i_new + e);
+                else v[u] = alpha * __ldg(i_old + e) + beta * __ldg(i_new + e);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (c0 + u < ncomp) fbuf[d + (c0 + u) * it.dgvol] = v[u];
         }
     }
 }

@@ -26,7 +26,7 @@ constexpr int kMaxComp = 32;     /* components per level */
 constexpr int kMaxStages = 8;    /* RKN stages */
 
 /* Tile of a box processed by one thread block of the stage kernels. */
-constexpr int kTileX = 32, kTileY = 4, kTileZ = 8;
+constexpr int kTileX = 32, kTileY = 4, kTileZ = 32;
 constexpr int kThreads = kTileX * kTileY;
 
 struct BoxDev {
