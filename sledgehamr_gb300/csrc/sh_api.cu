@@ -1490,6 +1490,7 @@ void integrate(sh_ctx *ctx, sh_level *L, int type, const double *tableau, int ns
                     }
                 s.c_k[s.nkin] = dt * dt * tb.bbar[S - 1];
                 s.c_k2[s.nkin] = dt * tb.b[S - 1];
+                if (tb.bbar[S - 1] == 0.) s.epi = kEpiRknFinalNoKqPos;
             }
             launch_stage(ctx, L, s, ko_order);
             fill_patch(ctx, L, L->buf[next], i < S - 1 ? t0 + dt * tb.nodes[i + 1] : t0 + dt);

@@ -62,7 +62,8 @@ enum EpilogueKind : int {
     kEpiSsp0 = 3,     /* K = f; u = y0 + a K */
     kEpiSspAdd = 4,   /* K = f + w K_old; u = y0 + a K (write K if kout) */
     kEpiLf0 = 5,      /* vh = v0 + dt/2 a; x1 = x0 + dt vh */
-    kEpiLf1 = 6       /* v1 = vh + dt/2 a; positions copied */
+    kEpiLf1 = 6,      /* v1 = vh + dt/2 a; positions copied */
+    kEpiRknFinalNoKqPos = 7 /* kEpiRknFinal when the last bbar is zero */
 };
 
 /* Kernel argument block of a stage kernel (passed by value as a

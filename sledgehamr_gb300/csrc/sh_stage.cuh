@@ -126,24 +126,33 @@ __global__ void __launch_bounds__(kTileX *kTileY, (stage_min_blocks<GW, KO>()))
             }
             break;
         }
-        case kEpiRknFinal: {
-            const long long kb = b.off * NP + lc;
+        case kEpiRknFinal:
+        case kEpiRknFinalNoKqPos: {
+            /* kEpiRknFinalNoKqPos: the tableau's last bbar is zero (RKN4), so
+             * the current stage's K adds nothing to the positions */
+            auto final_update = [&](auto kq_pos) {
+                const long long kb = b.off * NP + lc;
 #pragma unroll
-            for (int q = 0; q < NP; ++q) {
-                double y = a.y0[sbase + PR::pos(q) * gvol];
-                double m = a.y0[sbase + PR::mom(q) * gvol];
-                y += a.c_mom * m;
-                for (int s = 0; s < a.nkin; ++s) {
-                    const double ks = a.kin[s][kb + q * gvol];
-                    y += a.c_k[s] * ks;
-                    m += a.c_k2[s] * ks;
+                for (int q = 0; q < NP; ++q) {
+                    double y = a.y0[sbase + PR::pos(q) * gvol];
+                    double m = a.y0[sbase + PR::mom(q) * gvol];
+                    y += a.c_mom * m;
+                    for (int s = 0; s < a.nkin; ++s) {
+                        const double ks = a.kin[s][kb + q * gvol];
+                        y += a.c_k[s] * ks;
+                        m += a.c_k2[s] * ks;
+                    }
+                    const double kq = r[PR::mom(q)];
+                    if constexpr (decltype(kq_pos)::value) y += a.c_k[a.nkin] * kq;
+                    m += a.c_k2[a.nkin] * kq;
+                    a.out[sbase + PR::pos(q) * gvol] = y;
+                    a.out[sbase + PR::mom(q) * gvol] = m;
                 }
-                const double kq = r[PR::mom(q)];
-                y += a.c_k[a.nkin] * kq;
-                m += a.c_k2[a.nkin] * kq;
-                a.out[sbase + PR::pos(q) * gvol] = y;
-                a.out[sbase + PR::mom(q) * gvol] = m;
-            }
+            };
+            if (a.epi == kEpiRknFinal)
+                final_update(std::true_type{});
+            else
+                final_update(std::false_type{});
             break;
         }
         case kEpiSsp0:
