@@ -252,7 +252,8 @@ def test_errors_are_reported_not_raised_on_device(ctx):
 
 def test_level_errors_overlap_and_nesting(ctx):
     """Overlapping boxes are rejected at level creation, and a coarse level
-    that does not cover the cells to interpolate is rejected by the fill."""
+    that does not cover the cells to interpolate is rejected by the fill and
+    by the coarse link."""
     with pytest.raises(sh.ShError):
         sh.Level(ctx, "AxionStringsLap1", [((0, 0, 0), (15, 15, 15)), ((8, 8, 8), (23, 23, 23))],
                  (0, 0, 0), (31, 31, 31), 1)
@@ -263,6 +264,8 @@ def test_level_errors_overlap_and_nesting(ctx):
     import ctypes as C
     rc = ctx.lib.sh_level_fill_from(ctx.h, fine.h, sh.SH_NEW, None, sh.SH_NEW, coarse.h,
                                     C.c_double(0.0))
+    assert rc != 0 and "nested" in ctx.lib.sh_ctx_last_error(ctx.h).decode()
+    rc = ctx.lib.sh_level_set_coarse(ctx.h, fine.h, coarse.h)
     assert rc != 0 and "nested" in ctx.lib.sh_ctx_last_error(ctx.h).decode()
     fine.close()
     coarse.close()
