@@ -246,6 +246,23 @@ SH_API int sh_level_add_bubbles(sh_ctx *ctx, sh_level *L, int which, int comp_ph
                                 const double *profile, int nbins, double inv_dx, double Lcut,
                                 double dx);
 
+/* Reduction of component comp over the valid cells of a time level:
+ * SH_REDUCE_MAX_ABS (AMReX MultiFab::norm0, which FirstOrderPhaseTransition
+ * uses for its TruncationModifier parameters, FirstOrderPhaseTransition.cpp:
+ * 133-157), SH_REDUCE_MIN, SH_REDUCE_MAX, SH_REDUCE_SUM, SH_REDUCE_SUM_SQ
+ * (MultiFab::sum of the component or of its square).  Sums are formed in
+ * FP64 in a fixed order (per box, then over the boxes in order), so a
+ * result is reproducible bit for bit.  Synchronises the context's stream.
+ * Replaces the norm0 / sum calls of the reference's host code
+ * (FirstOrderPhaseTransition.cpp:147, NextToMinimalExample.cpp:35). */
+#define SH_REDUCE_MAX_ABS 0
+#define SH_REDUCE_MIN 1
+#define SH_REDUCE_MAX 2
+#define SH_REDUCE_SUM 3
+#define SH_REDUCE_SUM_SQ 4
+SH_API int sh_level_reduce(sh_ctx *ctx, const sh_level *level, int which, int op, int comp,
+                           double *out);
+
 /* ---- level synchronisation ------------------------------------------------- */
 /* crse(which_c) = 2x2x2 average of fine(which_f) on every coarse cell
  * covered by a fine box. */
@@ -359,6 +376,12 @@ typedef struct sh_amr_config {
     int nparams_tag;
     double params_mod[32];       /* SetParamsTruncationModifier */
     int nparams_mod;
+    /* 1: before the tagging of each regrid, params_mod[c] = max |comp c|
+     * over the valid cells of level 0 (new time level), for every
+     * component, as FirstOrderPhaseTransition's SetParamsTruncationModifier
+     * does with norm0 (FirstOrderPhaseTransition.cpp:133-157); 0: params_mod
+     * as given */
+    int params_mod_norm0;
 } sh_amr_config;
 /* New-grid generation from the buffered tags (at blocking-factor
  * resolution): Berger-Rigoutsos clustering to efficiency grid_eff, then

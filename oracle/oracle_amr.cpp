@@ -238,6 +238,25 @@ struct CpuBackend {
                        coarse ? &(*coarse)->nw : nullptr);
     }
     void sync() {}
+    /* FirstOrderPhaseTransition.cpp:133-157: params_mod = norm0 of every
+     * component of level 0's new data, once per time */
+    double maxima_time = -DBL_MAX;
+    void params_mod_from_norm0(Level &l0, double time) {
+        if (time == maxima_time) return;
+        for (int n = 0; n < ncomp; ++n) {
+            double m = 0.;
+            for (Fab &f : l0->nw.fabs) {
+                auto a = f.a();
+                for_cells(f.vbox, [&](int i, int j, int k) {
+                    const double v = std::fabs(a(i, j, k, n));
+                    if (v > m) m = v;
+                });
+            }
+            cfg.params_mod[n] = m;
+        }
+        cfg.nparams_mod = ncomp;
+        maxima_time = time;
+    }
 };
 
 struct AmrBase {
@@ -277,6 +296,7 @@ struct Amr : AmrBase {
         d.te_crit.assign(cfg.te_crit, cfg.te_crit + ncomp);
         d.clustering = cfg.clustering;
         d.grid_eff = cfg.grid_eff;
+        d.params_mod_norm0 = cfg.params_mod_norm0 != 0;
         drv.reset(new shamr::Driver<CpuBackend<P>>(backend, d));
         drv->record_regrids = cfg.record_regrids != 0;
         const int N = cfg.N0;

@@ -27,6 +27,13 @@ RKN_TABLEAU = 20
 RKN4 = 21
 RKN5 = 22
 
+# sh_level_reduce operations
+REDUCE_MAX_ABS = 0  # AMReX MultiFab::norm0
+REDUCE_MIN = 1
+REDUCE_MAX = 2
+REDUCE_SUM = 3
+REDUCE_SUM_SQ = 4
+
 # project ids compiled into the library
 PROJECTS = ("AxionStrings", "MinimalExample", "NextToMinimalExample",
             "FirstOrderPhaseTransition", "AxionStringsLap1", "AxionStringsLap2",
@@ -249,6 +256,11 @@ class Level:
         self.ctx.check(self.ctx.lib.sh_level_write(self.ctx.h, self.h, which, layout, _ptr(a)),
                        "sh_level_write")
 
+    def reduce(self, op: int, comp: int, which: int = SH_NEW) -> float:
+        """sh_level_reduce: op (REDUCE_*) of component comp over the valid
+        cells (fixed FP64 order, reproducible bit for bit)."""
+        return _reduce(self.ctx, self.h, which, op, comp)
+
     def read(self, which: int = SH_NEW, layout: int = 0) -> np.ndarray:
         out = np.empty(self.nvalid * self.ncomp, dtype=np.float64)
         self.ctx.check(self.ctx.lib.sh_level_read(self.ctx.h, self.h, which, layout, _ptr(out)),
@@ -358,6 +370,12 @@ def average_down_te(ctx: Context, fine: Level, crse: Level):
     ctx.check(ctx.lib.sh_average_down_te(ctx.h, fine.h, crse.h), "sh_average_down_te")
 
 
+def _reduce(ctx: Context, h, which: int, op: int, comp: int) -> float:
+    out = C.c_double()
+    ctx.check(ctx.lib.sh_level_reduce(ctx.h, h, which, op, comp, C.byref(out)), "sh_level_reduce")
+    return out.value
+
+
 def amr_config(project: str, **kw) -> ShAmrConfig:
     """sh_amr_config with the library defaults, then the given fields
     (te_crit, params, gw_params as sequences)."""
@@ -407,6 +425,9 @@ class LevelView:
         lo, hi = (C.c_int * 3)(), (C.c_int * 3)()
         ctx.lib.sh_level_domain(handle, lo, hi)
         self.domain = (tuple(lo), tuple(hi))
+
+    def reduce(self, op: int, comp: int, which: int = SH_NEW) -> float:
+        return _reduce(self.ctx, self.h, which, op, comp)
 
     def read(self, which: int = SH_NEW) -> np.ndarray:
         out = np.empty(self.nvalid * self.ncomp, dtype=np.float64)

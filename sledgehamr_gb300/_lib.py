@@ -62,7 +62,7 @@ class ShAmrConfig(C.Structure):
                 ("gw_params", C.c_double * 16), ("ngw", C.c_int), ("clustering", C.c_int),
                 ("grid_eff", C.c_double), ("params_tag", C.c_double * 32),
                 ("nparams_tag", C.c_int), ("params_mod", C.c_double * 32),
-                ("nparams_mod", C.c_int)]
+                ("nparams_mod", C.c_int), ("params_mod_norm0", C.c_int)]
 
 
 class ShRequest(C.Structure):
@@ -144,6 +144,7 @@ SIGNATURES = {
                                        C.c_longlong, llp, C.POINTER(ShBox), C.c_int, ip]),
     "sh_level_write": (C.c_int, [vp, vp, C.c_int, C.c_int, vp]),
     "sh_level_read": (C.c_int, [vp, vp, C.c_int, C.c_int, vp]),
+    "sh_level_reduce": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]),
     "sh_level_write_device": (C.c_int, [vp, vp, C.c_int, C.c_int, vp]),
     "sh_level_read_device": (C.c_int, [vp, vp, C.c_int, C.c_int, vp]),
     "sh_level_fill_patch": (C.c_int, [vp, vp, C.c_int]),

@@ -129,6 +129,17 @@ struct GpuBackend {
         ok(sh_level_fill_patch(ctx, l->L, which), "sh_level_fill_patch");
     }
     void sync() { ok(sh_ctx_synchronize(ctx), "sh_ctx_synchronize"); }
+    /* params_mod = per-component max |value| of level 0's new data, once
+     * per time */
+    double maxima_time = -DBL_MAX;
+    void params_mod_from_norm0(Level &l0, double time) {
+        if (time == maxima_time) return;
+        for (int c = 0; c < ncomp; ++c)
+            ok(sh_level_reduce(ctx, l0->L, SH_NEW, SH_REDUCE_MAX_ABS, c, &cfg.params_mod[c]),
+               "sh_level_reduce");
+        cfg.nparams_mod = ncomp;
+        maxima_time = time;
+    }
 };
 
 } // namespace
@@ -157,6 +168,7 @@ shamr::Config driver_config(const sh_amr_config &c, int ncomp) {
     d.te_crit.assign(c.te_crit, c.te_crit + ncomp);
     d.clustering = c.clustering;
     d.grid_eff = c.grid_eff;
+    d.params_mod_norm0 = c.params_mod_norm0 != 0;
     return d;
 }
 

@@ -97,6 +97,7 @@ struct Config {
     double string_lambda = 1.;  /* lambda of cosmology.h */
     int clustering = 0;         /* 0 Berger-Rigoutsos, 1 aligned windows */
     double grid_eff = 0.7;      /* minimum tagged fraction of a cluster */
+    bool params_mod_norm0 = false; /* TruncationModifier params from level 0 */
 };
 
 struct RegridRecord {
@@ -729,6 +730,10 @@ class Driver {
         if (dimN[l] % cb != 0) throw std::runtime_error("level size not a multiple of the block");
         const int nb = dimN[l] / cb;
         Clock ck(this, kTTag);
+        /* FirstOrderPhaseTransition::SetParamsTruncationModifier: the field
+         * maxima of level 0 at this time (FirstOrderPhaseTransition.cpp:
+         * 133-157) */
+        if (c.params_mod_norm0) b.params_mod_from_norm0(levels[0], time);
         if (record_regrids) {
             t.mask = b.tag(levels[l], shadow_hierarchy, time, l, dt[l], dx[l]);
             t.blocks = mask_to_blocks(t.mask, boxes[l], cb, c.n_error_buf, nb);

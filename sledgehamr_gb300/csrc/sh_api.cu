@@ -694,6 +694,69 @@ struct AvgRect {
  * average-down with truncation error of kernels::AverageDownWithTruncationError
  * (summation order (0,0,0) (1,0,0) (0,1,0) (0,0,1) (1,1,0) (1,0,1) (0,1,1)
  * (1,1,1)). */
+/* Reductions of one component over the valid cells of a level
+ * (sh_level_reduce).  One block per box: thread t combines the box's cells
+ * t, t + 256, ... in order, then a fixed tree over the block gives the
+ * box's partial; a single block combines the partials in box order the same
+ * way.  The order of every FP64 addition is fixed, so sums are
+ * deterministic. */
+constexpr int kReduceThreads = 256;
+
+__device__ __forceinline__ double reduce_identity(int op) {
+    if (op == SH_REDUCE_MIN) return __longlong_as_double(0x7FF0000000000000ll);  /* +inf */
+    if (op == SH_REDUCE_MAX) return __longlong_as_double((long long)0xFFF0000000000000ull); /* -inf */
+    return 0.;
+}
+__device__ __forceinline__ double reduce_value(int op, double v) {
+    if (op == SH_REDUCE_MAX_ABS) return fabs(v);
+    if (op == SH_REDUCE_SUM_SQ) return v * v;
+    return v;
+}
+__device__ __forceinline__ double reduce_combine(int op, double a, double b) {
+    if (op == SH_REDUCE_MAX_ABS || op == SH_REDUCE_MAX) return b > a ? b : a;
+    if (op == SH_REDUCE_MIN) return b < a ? b : a;
+    return a + b;
+}
+__device__ double reduce_block(int op, double acc) {
+    __shared__ double sm[kReduceThreads];
+    sm[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = kReduceThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sm[threadIdx.x] = reduce_combine(op, sm[threadIdx.x], sm[threadIdx.x + w]);
+        __syncthreads();
+    }
+    return sm[0];
+}
+
+__global__ void __launch_bounds__(kReduceThreads)
+    reduce_boxes_kernel(const BoxDev *boxes, const double *buf, int ncomp, int comp, int op,
+                        double *partial) {
+    const BoxDev b = boxes[blockIdx.x];
+    const int nx = b.hi[0] - b.lo[0] + 1, ny = b.hi[1] - b.lo[1] + 1;
+    const int n = nx * ny * (b.hi[2] - b.lo[2] + 1);
+    const long long gx = b.gdim[0], gxy = gx * b.gdim[1];
+    const double *base = buf + b.off * ncomp + (long long)comp * b.gvol +
+                         (b.lo[0] - b.glo[0]) + (b.lo[1] - b.glo[1]) * gx +
+                         (b.lo[2] - b.glo[2]) * gxy;
+    double acc = reduce_identity(op);
+    for (int t = threadIdx.x; t < n; t += kReduceThreads) {
+        const int i = t % nx, r = t / nx;
+        const int j = r % ny, k = r / ny;
+        acc = reduce_combine(op, acc, reduce_value(op, base[i + j * gx + k * gxy]));
+    }
+    const double v = reduce_block(op, acc);
+    if (threadIdx.x == 0) partial[blockIdx.x] = v;
+}
+
+__global__ void __launch_bounds__(kReduceThreads)
+    reduce_final_kernel(const double *partial, int n, int op, double *out) {
+    double acc = reduce_identity(op);
+    for (int t = threadIdx.x; t < n; t += kReduceThreads)
+        acc = reduce_combine(op, acc, partial[t]);
+    const double v = reduce_block(op, acc);
+    if (threadIdx.x == 0) out[0] = v;
+}
+
 __global__ void avgdown_kernel(const AvgRect *rects, int nrects, long long ncells,
                                const BoxDev *fboxes, const BoxDev *cboxes, int ncomp,
                                const double *fine, double *crse, double *te) {
@@ -2195,6 +2258,25 @@ int sh_projection(sh_ctx *ctx, const sh_level *const *levels, int nlev, int fn, 
         ck(cudaMemcpyAsync(n_out, d_n, npix * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream),
            "projection download");
         ck(cudaStreamSynchronize(ctx->stream), "projection");
+    });
+}
+
+int sh_level_reduce(sh_ctx *ctx, const sh_level *L, int which, int op, int comp, double *out) {
+    if (!ctx || !L || !out || (which != SH_NEW && which != SH_OLD)) return SH_ERR_ARG;
+    if (op < SH_REDUCE_MAX_ABS || op > SH_REDUCE_SUM_SQ) return SH_ERR_ARG;
+    if (comp < 0 || comp >= L->ncomp) return SH_ERR_ARG;
+    return guarded(ctx, [&] {
+        set_device(ctx);
+        const int nbox = (int)L->boxes.size();
+        double *d = (double *)ctx_scratch(ctx, ((size_t)nbox + 1) * sizeof(double));
+        reduce_boxes_kernel<<<nbox, kReduceThreads, 0, ctx->stream>>>(L->d_boxes, L->buf[which],
+                                                                     L->ncomp, comp, op, d + 1);
+        reduce_final_kernel<<<1, kReduceThreads, 0, ctx->stream>>>(d + 1, nbox, op, d);
+        ctx->launches += 2;
+        ck(cudaGetLastError(), "reduce launch");
+        ck(cudaMemcpyAsync(out, d, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
+           "reduce download");
+        ck(cudaStreamSynchronize(ctx->stream), "reduce");
     });
 }
 

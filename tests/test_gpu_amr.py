@@ -96,10 +96,12 @@ def test_tag_blocks_equal_coarsened_mask(ctx):
     lv.close()
 
 
-def test_fopt_gw_amr_with_tag_params_matches_oracle(ctx):
+@pytest.mark.parametrize("norm0", [0, 1])
+def test_fopt_gw_amr_with_tag_params_matches_oracle(ctx, norm0):
     """FirstOrderPhaseTransition + GW tensor on an AMR hierarchy (leapfrog,
-    truncation-error tags scaled by the field maxima passed as the
-    TruncationModifier parameters) against the oracle's hierarchy."""
+    truncation-error tags scaled by the field maxima as the
+    TruncationModifier parameters: given once, or taken from level 0 at
+    every regrid as the project does) against the oracle's hierarchy."""
     from sledgehamr_gb300 import ic
     from tests.oracle_lib import oracle_add_bubbles
     N0, L = 16, 8.0
@@ -117,7 +119,8 @@ def test_fopt_gw_amr_with_tag_params_matches_oracle(ctx):
     pmod = [float(np.abs(st[c]).max()) or 1.0 for c in range(14)]
     kw = dict(N0=N0, L=L, cfl=0.2, t_start=0.0, nghost=2, max_level=2, blocking_factor=8,
               max_grid_size=16, n_error_buf=1, regrid_dt=0.0, te_crit=te, params=params,
-              with_gw=1, integrator=sh.LEAPFROG, params_mod=pmod, record_regrids=1)
+              with_gw=1, integrator=sh.LEAPFROG, params_mod=pmod, record_regrids=1,
+              params_mod_norm0=norm0)
     g = sh.Amr(ctx, sh.amr_config("FirstOrderPhaseTransition", **kw), st)
     o = OracleAmr(sh.amr_config("FirstOrderPhaseTransition", **kw), st)
     for step in range(5):
