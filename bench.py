@@ -367,17 +367,26 @@ def run_fopt_leg(sh, ctx, stream, flush, steps, warmup):
 
 SERVE = dict(nreq=16, rate=4.0, d=(8.0, 40.0), gamma=(1.0, 4.0), lambda_bar=(0.6, 1.0),
              sizes=(64, 96, 128, 192, 256), max_n=128, radius=4.0, width=1.0, cfl=0.2,
-             inv_dx=16.0, seed=11)
+             inv_dx=16.0, seed=11, levels=(0, 1, 2), min_base=32, te_crit=1e-2,
+             regrid_steps=8)
 
 
-def serve_requests(max_n):
+def serve_requests(max_n, amr=False):
     """Two-bubble collisions (seeded): separation d, wall Lorentz factor
     gamma (radial tanh wall of width w/gamma moving outwards at v), thick or
     thin wall (lambda_bar), Poisson arrivals; box L = d + 2R + 16 with the
     smallest N of the size set that puts 1.5 cells across the contracted
-    wall, at most max_n; run to t = 2d."""
+    wall, at most max_n; run to t = 2d.  With amr, each request draws 0, 1
+    or 2 refinement levels (from a stream of its own, so the requests are
+    otherwise the same): with m levels the base grid has N / 2^m cells per
+    side (at least min_base), the finest level has the single-level
+    request's resolution where the truncation errors of Phi and dPhi exceed
+    te_crit (relative to their maxima, as FirstOrderPhaseTransition's
+    TruncationModifier scales them), and the grids are remade every
+    regrid_steps coarse steps."""
     sv = SERVE
     rng = np.random.default_rng(sv["seed"])
+    rng_levels = np.random.default_rng(sv["seed"] + 1)
     arr = np.cumsum(rng.exponential(1.0 / sv["rate"], sv["nreq"]))
     out = []
     for q in range(sv["nreq"]):
@@ -396,9 +405,16 @@ def serve_requests(max_n):
         x = (r - sv["radius"]) / wc
         prof = np.stack([0.5 * (1 - np.tanh(x)), 0.5 * v / wc / np.cosh(x) ** 2])
         c = np.array([[L / 2 - d / 2, L / 2, L / 2], [L / 2 + d / 2, L / 2, L / 2]])
-        out.append(dict(arrival=float(arr[q]), N=N, dx=dx, dt=sv["cfl"] * dx, t_end=2 * d,
+        m = int(sv["levels"][int(rng_levels.integers(0, len(sv["levels"])))]) if amr else 0
+        while m > 0 and N >> m < sv["min_base"]:
+            m -= 1
+        Nb = N >> m
+        dxb = L / Nb
+        out.append(dict(arrival=float(arr[q]), N=Nb, dx=dxb, dt=sv["cfl"] * dxb, t_end=2 * d,
                         params=[*lambda_bar_params(lb), 0.0], centres=c, profile=prof,
-                        inv_dx=sv["inv_dx"], Lcut=Lcut, d=d, gamma=gamma, lambda_bar=lb))
+                        inv_dx=sv["inv_dx"], Lcut=Lcut, d=d, gamma=gamma, lambda_bar=lb,
+                        max_level=m, te_crit=(sv["te_crit"], sv["te_crit"]),
+                        regrid_dt=sv["regrid_steps"] * sv["cfl"] * dxb))
     return out
 
 
@@ -407,9 +423,7 @@ def run_serve_leg(sh, ctx, max_n):
     p50/p99 time-to-spectrum (submission to spectrum ready, host clock) and
     aggregate cell-updates/s over the busy period; per-request spectrum
     error of FP32 against FP64."""
-    reqs = serve_requests(max_n)
-
-    def trace(prec):
+    def trace(prec, reqs):
         S = sh.Server(ctx, prec)
         t0 = time.perf_counter()
         ids = [None] * len(reqs)
@@ -418,7 +432,9 @@ def run_serve_leg(sh, ctx, max_n):
             for q, rq in enumerate(reqs):
                 if ids[q] is None and rq["arrival"] <= now:
                     ids[q] = S.submit(rq["N"], rq["dx"], rq["dt"], rq["t_end"], rq["params"],
-                                      rq["centres"], rq["profile"], rq["inv_dx"], rq["Lcut"])
+                                      rq["centres"], rq["profile"], rq["inv_dx"], rq["Lcut"],
+                                      max_level=rq["max_level"], te_crit=rq["te_crit"],
+                                      regrid_dt=rq["regrid_dt"])
             running, queued, _ = S.step()
             if all(i is not None for i in ids) and running == 0 and queued == 0:
                 break
@@ -435,15 +451,26 @@ def run_serve_leg(sh, ctx, max_n):
         info = S.info()
         spectra = [S.result(i)[0] for i in ids]
         S.close()
+        by_levels = {}
+        for m in sorted(set(rq["max_level"] for rq in reqs)):
+            lm = [x for x, rq in zip(lat, reqs) if rq["max_level"] == m]
+            by_levels[str(m)] = {"requests": len(lm), "p50_s": float(np.percentile(lm, 50)),
+                                 "p99_s": float(np.percentile(lm, 99))}
         return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
                 "max_s": float(max(lat)),
                 "cell_updates_per_s": info["cell_updates"] / (last - first),
-                "busy_s": last - first, "iterations": info["iterations"]}, spectra
+                "busy_s": last - first, "iterations": info["iterations"],
+                "by_refinement_levels": by_levels}, spectra
 
-    r32, s32 = trace(sh.PREC_FP32_KAHAN)
-    r64, s64 = trace(sh.PREC_FP64)
+    reqs = serve_requests(max_n)
+    r32, s32 = trace(sh.PREC_FP32_KAHAN, reqs)
+    r64, s64 = trace(sh.PREC_FP64, reqs)
     tot = [abs(a.sum() - b.sum()) / b.sum() for a, b in zip(s32, s64)]
     Ns = [rq["N"] for rq in reqs]
+    # the same requests with 0-2 refinement levels (AMR requests in FP64)
+    reqs_amr = serve_requests(max_n, amr=True)
+    r_amr, _ = trace(sh.PREC_FP32_KAHAN, reqs_amr)
+    levels = [rq["max_level"] for rq in reqs_amr]
     return {
         "workload": f"{len(reqs)} two-bubble requests, Poisson arrivals {SERVE['rate']}/s "
                     f"(seed {SERVE['seed']}), d ~ U{list(SERVE['d'])}, wall gamma ~ "
@@ -451,6 +478,14 @@ def run_serve_leg(sh, ctx, max_n):
                     f"N in {sorted(set(Ns))} (cap {max_n}), run to t = 2d, GW spectrum "
                     f"(binned, projection 2) at the end",
         "fp32_kahan": r32, "fp64": r64,
+        "with_refinement": {
+            "workload": f"the same requests with {levels.count(0)} / {levels.count(1)} / "
+                        f"{levels.count(2)} of them at 0 / 1 / 2 refinement levels (base grid "
+                        f"N / 2^levels, at least {SERVE['min_base']}; AMR requests as FP64 "
+                        f"hierarchies, te_crit {SERVE['te_crit']}, regrid every "
+                        f"{SERVE['regrid_steps']} coarse steps; spectrum of level 0), "
+                        f"single-level requests in the FP32+Kahan pool",
+            **r_amr},
         "gw_total_rel_err_fp32_vs_fp64": {"max": float(max(tot)),
                                           "median": float(np.median(tot))},
     }

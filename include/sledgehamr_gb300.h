@@ -396,7 +396,9 @@ typedef struct sh_amr_config {
 
 SH_API int sh_amr_config_defaults(sh_amr_config *cfg);
 /* Hierarchy with level 0 = level0 (canonical layout, N0^3 cells, boxes of
- * max_grid_size) at t_start. */
+ * max_grid_size) at t_start; level0 = NULL starts from a zero state (for
+ * example to add bubbles to level 0 through sh_amr_level before the first
+ * step). */
 SH_API int sh_amr_create(sh_ctx *ctx, const sh_amr_config *cfg, const double *level0,
                          sh_amr **out);
 SH_API int sh_amr_destroy(sh_ctx *ctx, sh_amr *amr);
@@ -523,8 +525,17 @@ SH_API int sh_ensemble_gw_spectrum(sh_ensemble *e, int r, int zero_padding, int 
  * admits queued requests while device memory is free (a request that does
  * not fit lets later ones pass until the oldest has waited 64 iterations),
  * advances all admitted runs by one step in shared launches, and finishes
- * the runs that reached t_end.  Times (seconds since the server's creation,
- * host clock): submitted, admitted, spectrum ready. */
+ * the runs that reached t_end.  A request with max_level >= 1 runs instead
+ * as its own FP64 AMR hierarchy (sh_amr: leapfrog with subcycling,
+ * refinement by the truncation errors of Phi and dPhi against te_crit with
+ * the TruncationModifier maxima of level 0, params_mod_norm0), admitted
+ * while the device has room for 16 times its level-0 state and advanced to
+ * t_end in a context (CUDA stream) and host thread of its own, so that its
+ * kernels overlap with the pool's; its spectrum is taken from level 0 (the
+ * fine levels averaged down) and collected by the next sh_server_step.
+ * sh_server_destroy stops running hierarchies after their current step.
+ * Times (seconds since the server's creation, host clock): submitted,
+ * admitted, spectrum ready. */
 typedef struct sh_request {
     int N;
     double dx, dt, t_end;
@@ -535,6 +546,11 @@ typedef struct sh_request {
     int nbins;
     double inv_dx, Lcut;
     int zero_padding, projection_type, unbinned;
+    int max_level;        /* 0: single level in the pool; 1, 2: AMR hierarchy */
+    int blocking_factor;  /* AMR requests: amr.blocking_factor (0: 8) */
+    int max_grid_size;    /* AMR requests: amr.max_grid_size (0: 32) */
+    double te_crit[2];    /* AMR requests: te_crit of Phi and dPhi */
+    double regrid_dt;     /* AMR requests: amr.regrid_dt */
 } sh_request;
 typedef struct sh_server sh_server;
 SH_API int sh_server_create(sh_ctx *ctx, int precision, long long capacity_cells,

@@ -429,6 +429,14 @@ class LevelView:
     def reduce(self, op: int, comp: int, which: int = SH_NEW) -> float:
         return _reduce(self.ctx, self.h, which, op, comp)
 
+    def gw_spectrum(self, zero_padding: int = 1, projection_type: int = 2, unbinned: bool = True,
+                    comps: Sequence[int] | None = None):
+        return Level.gw_spectrum(self, zero_padding, projection_type, unbinned, comps)
+
+    def add_bubbles(self, centres, profile, inv_dx: float, Lcut: float, dx: float,
+                    comp_phi: int = 0, comp_dphi: int = 1, which: int = SH_NEW):
+        Level.add_bubbles(self, centres, profile, inv_dx, Lcut, dx, comp_phi, comp_dphi, which)
+
     def read(self, which: int = SH_NEW) -> np.ndarray:
         out = np.empty(self.nvalid * self.ncomp, dtype=np.float64)
         self.ctx.check(self.ctx.lib.sh_level_read(self.ctx.h, self.h, which, 1, _ptr(out)),
@@ -444,10 +452,12 @@ class LevelView:
 class Amr:
     """AMR hierarchy advanced by the library's time stepper (sh_amr)."""
 
-    def __init__(self, ctx: Context, cfg: ShAmrConfig, level0: np.ndarray):
+    def __init__(self, ctx: Context, cfg: ShAmrConfig, level0: np.ndarray | None):
+        """level0 None: a zero state (bubbles etc. go onto level(0) before the
+        first step)."""
         self.ctx = ctx
         self.cfg = cfg
-        a = _f64(level0)
+        a = None if level0 is None else _f64(level0)
         h = C.c_void_p()
         ctx.check(ctx.lib.sh_amr_create(ctx.h, C.byref(cfg), _ptr(a), C.byref(h)),
                   "sh_amr_create")
@@ -725,8 +735,16 @@ class Server:
 
     def submit(self, N: int, dx: float, dt: float, t_end: float, params, centres=None,
                profile=None, inv_dx: float = 1.0, Lcut: float = 0.0, zero_padding: int = 1,
-               projection_type: int = 2, unbinned: bool = False) -> int:
+               projection_type: int = 2, unbinned: bool = False, max_level: int = 0,
+               te_crit=(1e300, 1e300), regrid_dt: float = 0.0, blocking_factor: int = 0,
+               max_grid_size: int = 0) -> int:
+        """A run; max_level >= 1 makes it an AMR hierarchy refined by the
+        truncation errors of Phi and dPhi against te_crit."""
         r = ShRequest()
+        r.max_level, r.blocking_factor, r.max_grid_size = int(max_level), int(blocking_factor), \
+            int(max_grid_size)
+        r.te_crit[0], r.te_crit[1] = float(te_crit[0]), float(te_crit[1])
+        r.regrid_dt = float(regrid_dt)
         r.N, r.dx, r.dt, r.t_end = int(N), float(dx), float(dt), float(t_end)
         for q, v in enumerate(list(params)[:4]):
             r.params[q] = float(v)

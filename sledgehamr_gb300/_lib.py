@@ -70,7 +70,9 @@ class ShRequest(C.Structure):
                 ("params", C.c_double * 4), ("nbubbles", C.c_int), ("xyz", C.c_void_p),
                 ("profile", C.c_void_p), ("nbins", C.c_int), ("inv_dx", C.c_double),
                 ("Lcut", C.c_double), ("zero_padding", C.c_int), ("projection_type", C.c_int),
-                ("unbinned", C.c_int)]
+                ("unbinned", C.c_int), ("max_level", C.c_int), ("blocking_factor", C.c_int),
+                ("max_grid_size", C.c_int), ("te_crit", C.c_double * 2),
+                ("regrid_dt", C.c_double)]
 
 
 # name -> (restype, argtypes)

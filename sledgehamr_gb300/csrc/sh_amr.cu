@@ -211,7 +211,7 @@ int sh_amr_config_defaults(sh_amr_config *c) {
 }
 
 int sh_amr_create(sh_ctx *ctx, const sh_amr_config *cfg, const double *level0, sh_amr **out) {
-    if (!ctx || !cfg || !level0 || !out) return SH_ERR_ARG;
+    if (!ctx || !cfg || !out) return SH_ERR_ARG;
     *out = nullptr;
     int ncomp = 0;
     int rc = sh_project_ncomp(cfg->project, cfg->with_gw, &ncomp, nullptr);
@@ -234,7 +234,9 @@ int sh_amr_create(sh_ctx *ctx, const sh_amr_config *cfg, const double *level0, s
         a->driver.reset(new shamr::Driver<GpuBackend>(a->backend, driver_config(*cfg, ncomp)));
         a->driver->record_regrids = cfg->record_regrids != 0;
         a->driver->init_coarse([&](GpuLevel *&l) {
-            a->backend.ok(sh_level_write(ctx, l->L, SH_NEW, 0, level0), "sh_level_write");
+            /* without level0 the new level keeps its zeroed buffers */
+            if (level0)
+                a->backend.ok(sh_level_write(ctx, l->L, SH_NEW, 0, level0), "sh_level_write");
         });
     });
     if (rc != SH_OK) {

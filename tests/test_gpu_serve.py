@@ -161,3 +161,62 @@ def test_fp64_pool_member_matches_oracle(ctx):
         assert rel_l2(out, ref) <= 1e-12
         assert rel_l2(out[2:], ref[2:]) <= 1e-12
     P.close()
+
+
+def amr_request(N, d, seed, max_level=1):
+    rq = request(N, d, seed)
+    rq.update(max_level=max_level, te_crit=(1e-3, 1e-3), regrid_dt=0.0)
+    return rq
+
+
+def run_amr_alone(ctx, rq):
+    """The AMR request's hierarchy built directly: FirstOrderPhaseTransition
+    + GW, leapfrog, TruncationModifier maxima from level 0, bubbles on
+    level 0 of a zero state, ceil(t_end / dt) coarse steps, spectrum of
+    level 0."""
+    q = rq["params"]
+    cfg = sh.amr_config("FirstOrderPhaseTransition", N0=rq["N"], L=rq["N"] * rq["dx"],
+                        cfl=rq["dt"] / rq["dx"], t_start=0.0, nghost=2,
+                        max_level=rq["max_level"], blocking_factor=8, max_grid_size=32,
+                        n_error_buf=1, regrid_dt=rq["regrid_dt"],
+                        te_crit=list(rq["te_crit"]) + [1e300] * 12,
+                        params=[0.0, q[0], q[1], q[2], 0.0, 0.0, 0.0], with_gw=1,
+                        integrator=sh.LEAPFROG, params_mod_norm0=1)
+    A = sh.Amr(ctx, cfg, None)
+    A.level(0).add_bubbles(rq["centres"], rq["profile"], rq["inv_dx"], rq["Lcut"], rq["dx"])
+    A.step(int(np.ceil(rq["t_end"] / rq["dt"] - 1e-9)))
+    out = A.level(0).gw_spectrum(zero_padding=1, projection_type=2, unbinned=False)
+    finest = A.info()["finest"]
+    A.close()
+    return out, finest
+
+
+def submit_all(S, reqs):
+    return [S.submit(rq["N"], rq["dx"], rq["dt"], rq["t_end"], rq["params"], rq["centres"],
+                     rq["profile"], rq["inv_dx"], rq["Lcut"], max_level=rq.get("max_level", 0),
+                     te_crit=rq.get("te_crit", (1e300, 1e300)),
+                     regrid_dt=rq.get("regrid_dt", 0.0)) for rq in reqs]
+
+
+def test_amr_requests_equal_alone_and_in_the_mix(ctx):
+    """A request with a refinement level runs as its own hierarchy: its
+    spectrum equals the hierarchy's run outside the server bitwise, alone
+    and beside single-level requests in the same server."""
+    ra = amr_request(32, 6.0, 11)
+    alone, finest = run_amr_alone(ctx, ra)
+    assert finest >= 1  # the walls were refined
+    mixes = ([ra], [request(16, 6.0, 1), ra, request(24, 8.0, 2)])
+    for reqs in mixes:
+        S = sh.Server(ctx, sh.PREC_FP32_KAHAN, capacity_cells=60000)
+        ids = submit_all(S, reqs)
+        it = 0
+        while True:
+            running, queued, _ = S.step()
+            it += 1
+            if running == 0 and queued == 0:
+                break
+            assert it < 10000
+        b, k = S.result(ids[reqs.index(ra)])
+        assert np.array_equal(b, alone[0]) and np.array_equal(k, alone[1])
+        assert S.info()["cell_updates"] > 0
+        S.close()
