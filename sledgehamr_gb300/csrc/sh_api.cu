@@ -1886,14 +1886,29 @@ int sh_level_create(sh_ctx *ctx, int project, int with_gw, const int domain_lo[3
             vb += nv;
             L->vbase.push_back(vb);
             L->hboxes.push_back(bd);
-            for (int z = bd.lo[2]; z <= bd.hi[2]; z += kTileZ)
-                for (int x = bd.lo[0]; x <= bd.hi[0]; x += kTileX) {
-                    const int nx = std::min(kTileX, bd.hi[0] - x + 1);
-                    const int rows = kThreads / nx;
-                    for (int y = bd.lo[1]; y <= bd.hi[1]; y += rows)
-                        tiles.push_back(TileDev{b, x, y, z, nx});
-                }
         }
+        /* deep tiles amortise the per-column set-up of the hooks; a level
+         * whose deep tiles would not fill two waves of six blocks per SM
+         * gets shallow ones */
+        auto make_tiles = [&](int depth) {
+            tiles.clear();
+            for (int b = 0; b < nbox; ++b) {
+                const BoxDev &bd = L->hboxes[b];
+                for (int z = bd.lo[2]; z <= bd.hi[2]; z += depth)
+                    for (int x = bd.lo[0]; x <= bd.hi[0]; x += kTileX) {
+                        const int nx = std::min(kTileX, bd.hi[0] - x + 1);
+                        const int rows = kThreads / nx;
+                        const int nz = std::min(depth, bd.hi[2] - z + 1);
+                        for (int y = bd.lo[1]; y <= bd.hi[1]; y += rows)
+                            tiles.push_back(TileDev{b, x, y, z, nx, nz});
+                    }
+            }
+        };
+        int nsm = 0;
+        ck(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device),
+           "SM count");
+        make_tiles(kTileZ);
+        if ((long long)tiles.size() < 2LL * 6 * nsm) make_tiles(kTileZShallow);
         L->total_gvol = base;
         L->nvalid = vb;
         L->ntiles = (int)tiles.size();

@@ -26,7 +26,10 @@ constexpr int kMaxComp = 32;     /* components per level */
 constexpr int kMaxStages = 8;    /* RKN stages */
 
 /* Tile of a box processed by one thread block of the stage kernels. */
-constexpr int kTileX = 32, kTileY = 4, kTileZ = 32;
+/* Stage tiles: up to kTileX cells in x, kThreads / nx rows in y and
+ * kTileZ planes in z (kTileZShallow on levels whose deep tiles would not
+ * fill two waves of the GPU). */
+constexpr int kTileX = 32, kTileY = 4, kTileZ = 32, kTileZShallow = 8;
 constexpr int kThreads = kTileX * kTileY;
 
 struct BoxDev {
@@ -42,6 +45,7 @@ struct TileDev {
     int box;
     int x0, y0, z0; /* first cell of the tile (absolute level index) */
     int nx;         /* cells along x (<= kTileX); the tile has kThreads / nx rows */
+    int nz;         /* planes along z */
 };
 
 /* One rectangle of ghost cells copied from a valid region of the same

@@ -18,7 +18,7 @@
  * Thread mapping: a block of kThreads = 128 threads owns a tile of one box,
  * nx <= 32 cells wide in x (the box width when the box is narrower, so that
  * the small boxes of refined levels keep every thread busy), kThreads / nx
- * rows in y and kTileZ planes in z; each thread walks its z-column, so that
+ * rows in y and t.nz planes in z; each thread walks its z-column, so that
  * per-thread set-up (the reciprocals of dx^2 and of the time in the hooks)
  * is paid once per column.  Hooks read the stage state
  * straight from HBM through an Array4 view of the ghost-grown box; the
@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(kTileX *kTileY, (stage_min_blocks<GW, KO>()))
     const int i = t.x0 + (tid - ty * t.nx);
     const int j = t.y0 + ty;
     if (ty >= kThreads / t.nx || i > b.hi[0] || j > b.hi[1]) return;
-    const int kend = min(t.z0 + kTileZ - 1, b.hi[2]);
+    const int kend = min(t.z0 + t.nz - 1, b.hi[2]);
 
     const long long gx = b.gdim[0];
     const long long gxy = gx * b.gdim[1];
@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(kTileX *kTileY) tag_kernel(const __grid_consta
     const int i = t.x0 + (tid - ty * t.nx);
     const int j = t.y0 + ty;
     const bool inside = (ty < kThreads / t.nx && i <= b.hi[0] && j <= b.hi[1]);
-    const int kend = min(t.z0 + kTileZ - 1, b.hi[2]);
+    const int kend = min(t.z0 + t.nz - 1, b.hi[2]);
     const long long gx = b.gdim[0], gxy = gx * b.gdim[1];
     const amrex::Dim3 glo{b.glo[0], b.glo[1], b.glo[2]};
     const amrex::Dim3 ghi{b.glo[0] + b.gdim[0], b.glo[1] + b.gdim[1], b.glo[2] + b.gdim[2]};
