@@ -110,6 +110,14 @@ struct sh_level {
      * with uid cf_uid at version cf_ver */
     double *cf_old = nullptr, *cf_new = nullptr;
     long long cf_uid = -1, cf_ver = -1;
+    /* the last ghost fill of each buffer: the level's version and the
+     * coarse level's uid and version then, and the time filled for */
+    struct FillSig {
+        const double *buf = nullptr;
+        long long ver = -1, cuid = -1, cver = -1;
+        double t = 0.;
+    } fill_sig[3];
+    int fill_sig_next = 0;
     /* average-down plan onto the level with uid avg_for (a cache) */
     mutable long long avg_for = -1;
     mutable void *d_avg = nullptr; /* AvgRect list */
@@ -1393,6 +1401,33 @@ void ensure_kbuf(sh_ctx *ctx, sh_level *L, size_t elems, int count) {
  * cells from the valid cells of the same level (periodic images), then, on a
  * fine level linked to its coarse level, the remaining ghost cells from the
  * coarse data at time t. */
+/* Records that buf's ghost cells were filled for time t with the level at
+ * its current version and the coarse level as it is now. */
+void note_fill(sh_level *L, const double *buf, double t) {
+    int q = 0;
+    while (q < 3 && L->fill_sig[q].buf != buf) ++q;
+    if (q == 3) {
+        q = L->fill_sig_next;
+        L->fill_sig_next = (q + 1) % 3;
+    }
+    L->fill_sig[q].buf = buf;
+    L->fill_sig[q].ver = L->version;
+    L->fill_sig[q].cuid = L->coarse ? L->coarse->uid : -1;
+    L->fill_sig[q].cver = L->coarse ? L->coarse->version : -1;
+    L->fill_sig[q].t = t;
+}
+
+/* Whether buf's ghost cells already hold what a fill for time t would
+ * write: filled for t while the level was at version ver and the coarse
+ * level (if any) at its present version. */
+bool fill_current(const sh_level *L, const double *buf, double t, long long ver) {
+    for (const auto &f : L->fill_sig)
+        if (f.buf == buf)
+            return f.ver == ver && f.t == t && f.cuid == (L->coarse ? L->coarse->uid : -1) &&
+                   f.cver == (L->coarse ? L->coarse->version : -1);
+    return false;
+}
+
 void fill_patch(sh_ctx *ctx, sh_level *L, double *buf, double t) {
     if (L->nghost_items > 0) {
         ProfScope ps(ctx, kProfFill);
@@ -1430,6 +1465,7 @@ void fill_patch(sh_ctx *ctx, sh_level *L, double *buf, double t) {
         ctx->launches++;
         ck(cudaGetLastError(), "coarse-fine fill launch");
     }
+    note_fill(L, buf, t);
 }
 
 void launch_stage(sh_ctx *ctx, sh_level *L, StageArgs &a, int ko_order) {
@@ -2108,6 +2144,7 @@ int sh_level_advance(sh_ctx *ctx, sh_level *L, int integrator, const double *tab
                      int flags) {
     if (!ctx || !L) return SH_ERR_ARG;
     return guarded(ctx, [&] {
+        const long long ver = L->version;
         L->version++;
         set_device(ctx);
         require(dt > 0 && dx > 0, "dt and dx must be positive");
@@ -2116,7 +2153,12 @@ int sh_level_advance(sh_ctx *ctx, sh_level *L, int integrator, const double *tab
             std::swap(L->t[SH_NEW], L->t[SH_OLD]);
             std::swap(L->istep[SH_NEW], L->istep[SH_OLD]);
         }
-        fill_patch(ctx, L, L->buf[SH_OLD], L->t[SH_OLD]);
+        /* FillPatch at t_old, unless the last stage of the previous step
+         * filled this buffer for the same time and neither this level nor
+         * its coarse level changed since (the finest level between its two
+         * sub-steps): the ghost values would be the same */
+        if (!fill_current(L, L->buf[SH_OLD], L->t[SH_OLD], ver))
+            fill_patch(ctx, L, L->buf[SH_OLD], L->t[SH_OLD]);
         integrate(ctx, L, integrator, tableau, nstages, dt, dx, params, nparams, gw_params, ngw,
                   ko_order, ko_strength);
         L->t[SH_NEW] = L->t[SH_OLD] + dt;
