@@ -48,16 +48,18 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "cell-updates/s"
-# Algorithmic HBM words per cell-update of the fused RKN4 schedule for 2
-# position + 2 momentum components: stage i reads the stage state, y0 and
-# K_0..K_{i-1} and writes K_i and the next stage state; the last stage writes
-# y1: 10 + 16 + 16 = 42 FP64 words.
-WORDS_PER_CELL_UPDATE = 42
+# Algorithmic HBM words per cell-update of the fused RKN4 schedule as run,
+# for 2 position + 2 momentum components: stage i reads the stage state, y0
+# and the K_j with a non-zero tableau coefficient, writes K_i and the next
+# stage state; the last stage writes y1.  Stage 0: 4 + 2 + 4 = 10; stage 1
+# (a_31 = 0: K_0 not read): 4 + 4 + 2 + 4 = 14; final: 4 + 4 + 2 + 2 + 4 =
+# 16; 40 FP64 words.
+WORDS_PER_CELL_UPDATE = 40
 # Measured DRAM traffic of the stage kernels per cell-update (ncu, dram
-# bytes read + written, three launches of RKN4 on level 1 of the AMR run at
-# N0 = 128: 5.85 GB for 12,729,344 cells), scaled to a launch of the
-# benchmark by the cells it updates.
-TRAFFIC_B_PER_CELL_UPDATE = 460.0
+# bytes read + written, the three launches of one RKN4 step on level 1 of
+# the AMR run at N0 = 128: 5.55 GB for 12,729,344 cells), scaled to a launch
+# of the benchmark by the cells it updates.
+TRAFFIC_B_PER_CELL_UPDATE = 436.0
 
 SINGLE = dict(N=128, L=32.0, project="AxionStringsLap1", params=[1.0, 0.0], nghost=1,
               eta0=0.1)
@@ -949,7 +951,7 @@ def main():
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": WORDS_PER_CELL_UPDATE * 8 / 3.0 *
                          cells_per_launch,
-                         "fp64_pipe_busy_ncu": 0.82,
+                         "fp64_pipe_busy_ncu": {"stage0": 0.72, "stage1": 0.63, "final": 0.70},
                          "kernel": "stage_kernel (fused Rhs + RKN4 stage update)",
                          "bytes_per_cell_update": WORDS_PER_CELL_UPDATE * 8,
                          "stage_ms_total": stage_ms, "stage_launches": stage_launches,
