@@ -36,6 +36,7 @@
 #include <vector>
 
 #include "sh_bubbles.cuh"
+#include "sh_fixed_stencil.h"
 #include "sh_internal.h"
 #include "sledgehamr_gb300.h"
 
@@ -216,7 +217,31 @@ __global__ void __launch_bounds__(TX *TY, sizeof(R) == 4 ? 5 : 1) axion_rkn4_ker
 #pragma unroll
             for (int c = 0; c < 2; ++c) {
                 const R u0 = ring[sc][c][ty + H][tx + H];
-                if (ORDER == 1) {
+                if constexpr (sizeof(R) == 8) {
+                    /* FP64 members: the ring sums exactly in 64-bit integers
+                     * (sh_fixed_stencil.h), as the drop-in path's stencils */
+                    namespace fx = sledgehamr::utils::fixed;
+                    const double r1[7] = {
+                        u0, ring[sc][c][ty + H][tx + H + 1], ring[sc][c][ty + H][tx + H - 1],
+                        ring[sc][c][ty + H + 1][tx + H], ring[sc][c][ty + H - 1][tx + H],
+                        ring[(sc + 1) % RING][c][ty + H][tx + H],
+                        ring[(sc + RING - 1) % RING][c][ty + H][tx + H]};
+                    if (ORDER == 1) {
+                        const int n[2] = {1, 6};
+                        const long long w[2] = {-6, 1};
+                        lap[c] = fx::weighted_sum<7, 2, -6>(r1, n, w, inv_dx2);
+                    } else {
+                        const double r2[13] = {
+                            r1[0], r1[1], r1[2], r1[3], r1[4], r1[5], r1[6],
+                            ring[sc][c][ty + H][tx + H + 2], ring[sc][c][ty + H][tx + H - 2],
+                            ring[sc][c][ty + H + 2][tx + H], ring[sc][c][ty + H - 2][tx + H],
+                            ring[(sc + 2) % RING][c][ty + H][tx + H],
+                            ring[(sc + RING - 2) % RING][c][ty + H][tx + H]};
+                        const int n[3] = {1, 6, 6};
+                        const long long w[3] = {-90, 16, -1};
+                        lap[c] = fx::weighted_sum<13, 3, -2>(r2, n, w, inv12dx2);
+                    }
+                } else if (ORDER == 1) {
                     R s = ring[sc][c][ty + H][tx + H + 1] + ring[sc][c][ty + H][tx + H - 1];
                     s += ring[sc][c][ty + H + 1][tx + H] + ring[sc][c][ty + H - 1][tx + H];
                     s += ring[(sc + 1) % RING][c][ty + H][tx + H] +
@@ -380,6 +405,20 @@ __global__ void __launch_bounds__(TX *TY, sizeof(R) == 4 ? 3 : 1) fopt_leapfrog_
 #pragma unroll
             for (int c = 0; c < NC; ++c) {
                 const R u0 = ring[s0][c][cy_][cx_];
+                if constexpr (sizeof(R) == 8) {
+                    /* FP64 members: exact integer ring sums (sh_fixed_stencil.h) */
+                    const double v[13] = {
+                        u0, ring[s0][c][cy_][cx_ + 1], ring[s0][c][cy_][cx_ - 1],
+                        ring[s0][c][cy_ + 1][cx_], ring[s0][c][cy_ - 1][cx_],
+                        ring[sp1][c][cy_][cx_], ring[sm1][c][cy_][cx_],
+                        ring[s0][c][cy_][cx_ + 2], ring[s0][c][cy_][cx_ - 2],
+                        ring[s0][c][cy_ + 2][cx_], ring[s0][c][cy_ - 2][cx_],
+                        ring[sp2][c][cy_][cx_], ring[sm2][c][cy_][cx_]};
+                    const int n[3] = {1, 6, 6};
+                    const long long w[3] = {-90, 16, -1};
+                    acc[c] = sledgehamr::utils::fixed::weighted_sum<13, 3, -2>(v, n, w, inv12dx2);
+                    continue;
+                }
                 R s1 = ring[s0][c][cy_][cx_ + 1] + ring[s0][c][cy_][cx_ - 1];
                 s1 += ring[s0][c][cy_ + 1][cx_] + ring[s0][c][cy_ - 1][cx_];
                 s1 += ring[sp1][c][cy_][cx_] + ring[sm1][c][cy_][cx_];
@@ -390,12 +429,28 @@ __global__ void __launch_bounds__(TX *TY, sizeof(R) == 4 ? 3 : 1) fopt_leapfrog_
             }
             /* 4th-order gradient of Phi */
             R g[3];
+            if constexpr (sizeof(R) == 8) {
+                /* FP64 members: exact integer sums (sh_fixed_stencil.h) */
+                const int n[4] = {1, 1, 1, 1};
+                const long long w[4] = {8, -8, -1, 1};
+                const double gx[4] = {ring[s0][0][cy_][cx_ + 1], ring[s0][0][cy_][cx_ - 1],
+                                      ring[s0][0][cy_][cx_ + 2], ring[s0][0][cy_][cx_ - 2]};
+                const double gy[4] = {ring[s0][0][cy_ + 1][cx_], ring[s0][0][cy_ - 1][cx_],
+                                      ring[s0][0][cy_ + 2][cx_], ring[s0][0][cy_ - 2][cx_]};
+                const double gz[4] = {ring[sp1][0][cy_][cx_], ring[sm1][0][cy_][cx_],
+                                      ring[sp2][0][cy_][cx_], ring[sm2][0][cy_][cx_]};
+                namespace fx = sledgehamr::utils::fixed;
+                g[0] = fx::weighted_sum<4, 4, -5>(gx, n, w, inv12dx);
+                g[1] = fx::weighted_sum<4, 4, -5>(gy, n, w, inv12dx);
+                g[2] = fx::weighted_sum<4, 4, -5>(gz, n, w, inv12dx);
+            } else {
             g[0] = ((R)8 * (ring[s0][0][cy_][cx_ + 1] - ring[s0][0][cy_][cx_ - 1]) -
                     (ring[s0][0][cy_][cx_ + 2] - ring[s0][0][cy_][cx_ - 2])) * inv12dx;
             g[1] = ((R)8 * (ring[s0][0][cy_ + 1][cx_] - ring[s0][0][cy_ - 1][cx_]) -
                     (ring[s0][0][cy_ + 2][cx_] - ring[s0][0][cy_ - 2][cx_])) * inv12dx;
             g[2] = ((R)8 * (ring[sp1][0][cy_][cx_] - ring[sm1][0][cy_][cx_]) -
                     (ring[sp2][0][cy_][cx_] - ring[sm2][0][cy_][cx_])) * inv12dx;
+            }
             const R phi = ring[s0][0][cy_][cx_];
             acc[0] += phi * (q2 + phi * (q3 + phi * q4));
             acc[1] += g[0] * g[0];
