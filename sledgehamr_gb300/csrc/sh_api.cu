@@ -1924,7 +1924,7 @@ int sh_level_create(sh_ctx *ctx, int project, int with_gw, const int domain_lo[3
             L->hboxes.push_back(bd);
         }
         /* deep tiles amortise the per-column set-up of the hooks; a level
-         * whose deep tiles would not fill two waves of six blocks per SM
+         * whose deep tiles would not fill two waves of seven blocks per SM
          * gets shallow ones */
         auto make_tiles = [&](int depth) {
             tiles.clear();
@@ -1944,7 +1944,7 @@ int sh_level_create(sh_ctx *ctx, int project, int with_gw, const int domain_lo[3
         ck(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device),
            "SM count");
         make_tiles(kTileZ);
-        if ((long long)tiles.size() < 2LL * 6 * nsm) make_tiles(kTileZShallow);
+        if ((long long)tiles.size() < 2LL * 7 * nsm) make_tiles(kTileZShallow);
         L->total_gvol = base;
         L->nvalid = vb;
         L->ntiles = (int)tiles.size();

@@ -52,12 +52,15 @@ struct Pairs {
     }
 };
 
-/* Six resident blocks per SM (at most 80 registers) for the plain stages,
- * whose instruction mix leaves memory latency to hide; the GW and
- * Kreiss-Oliger variants keep every register they need. */
+/* Seven resident blocks per SM (at most 72 registers) for the plain
+ * stages, whose instruction mix leaves memory latency to hide (measured on
+ * the AMR workload: 5 blocks 5.04 s, 6 blocks 4.67 s, 7 blocks 4.44 s, 8
+ * blocks 4.39 s of stage kernels, the last with 140-224 byte spills in the
+ * 13- and 19-point variants); the GW and Kreiss-Oliger variants keep every
+ * register they need. */
 template <bool GW, int KO>
 constexpr int stage_min_blocks() {
-    return (GW || KO != 0) ? 1 : 6;
+    return (GW || KO != 0) ? 1 : 7;
 }
 
 template <class H, bool GW, int KO>
