@@ -171,13 +171,19 @@ void amr_worker(sh_server *S, AmrJob *job, sh_ctx *actx, sh_amr *amr, sh_request
 int admit_amr(sh_server *S, Req &q) {
     const sh_request &r = q.spec;
     size_t free_b = 0, total_b = 0;
-    if (cudaSetDevice(S->device) != cudaSuccess || cudaMemGetInfo(&free_b, &total_b) != cudaSuccess)
+    if (cudaSetDevice(S->device) != cudaSuccess ||
+        cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        S->err = "cudaMemGetInfo failed";
         return SH_ERR_CUDA;
+    }
     const double need = kAmrMemoryFactor * (double)r.N * r.N * r.N * kFoptComps * sizeof(double);
     if ((double)free_b < need) return SH_ERR_NOMEM;
     int project = -1;
     int rc = sh_project_find("FirstOrderPhaseTransition", &project);
-    if (rc != SH_OK) return rc;
+    if (rc != SH_OK) {
+        S->err = "FirstOrderPhaseTransition is not compiled into the library";
+        return rc;
+    }
     sh_amr_config c;
     sh_amr_config_defaults(&c);
     c.project = project;
@@ -325,7 +331,8 @@ int sh_server_step(sh_server *S, int *running, int *queued, int *completed) {
                                          q.profile.data(), q.spec.nbins, q.spec.inv_dx,
                                          q.spec.Lcut);
         if (rc != SH_OK) {
-            S->err = sh_ensemble_last_error(S->pool);
+            /* admit_amr has set the message of an AMR request's failure */
+            if (q.spec.max_level == 0) S->err = sh_ensemble_last_error(S->pool);
             q.state = 3;
             q.rc = rc;
             q.t_done = S->now();
