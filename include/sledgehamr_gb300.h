@@ -27,6 +27,12 @@
  *   sh_index_to_k ........... Sledgehamr::ReadSpectrumKs / ReadProj data
  *                             (sledgehamr.cpp:554-615, generated as
  *                              pySledgehamr/Sledgehamr.py:7-27)
+ *   sh_level_reduce ......... LevelData::norm0 / MultiFab::sum of the
+ *                             projects' host code
+ *                             (FirstOrderPhaseTransition.cpp:133-157,
+ *                              NextToMinimalExample.cpp:35)
+ *   sh_amr_* ................ TimeStepper::Advance / Sledgehamr::Evolve over
+ *                             a whole hierarchy (time_stepper.cpp:90-397)
  *   sh_evolve_periodic ...... host-to-host convenience: upload, nsteps x
  *                             Advance(0), download, for a periodic cubic level
  *
