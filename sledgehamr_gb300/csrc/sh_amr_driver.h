@@ -217,60 +217,85 @@ inline void cluster(const BlockSet &t, IBox bx, double eff, std::vector<IBox> &o
     cluster(t, r, eff, out);
 }
 
-/* Boxes sharing a whole face are merged (BoxList::simplify).  Each pass
- * orders the boxes by (lo[e], hi[e], lo[f], hi[f], lo[d]); the boxes are
- * disjoint, so that key is unique and any sort gives the same order.  With
- * coordinates in [0, 4096) the key is packed into one 64-bit integer. */
+/* Stable LSD radix sort of (key, index) pairs by key, 11 bits per pass. */
+inline void radix_sort_keyed(std::vector<std::pair<unsigned long long, unsigned>> &v,
+                             std::vector<std::pair<unsigned long long, unsigned>> &tmp,
+                             int key_bits) {
+    constexpr int kBits = 11, kBuckets = 1 << kBits;
+    tmp.resize(v.size());
+    std::vector<size_t> count(kBuckets);
+    for (int shift = 0; shift < key_bits; shift += kBits) {
+        std::fill(count.begin(), count.end(), 0);
+        for (const auto &e : v) ++count[(e.first >> shift) & (kBuckets - 1)];
+        size_t sum = 0;
+        for (size_t &c : count) {
+            const size_t n = c;
+            c = sum;
+            sum += n;
+        }
+        for (const auto &e : v) tmp[count[(e.first >> shift) & (kBuckets - 1)]++] = e;
+        v.swap(tmp);
+    }
+}
+
+/* Boxes sharing a whole face are merged (BoxList::simplify): along each
+ * direction d in turn, the boxes ordered by (lo[e], hi[e], lo[f], hi[f],
+ * lo[d]) and neighbours in that order merged, until no direction merges
+ * anything.  The boxes are disjoint, so that key is unique and any sort
+ * gives the same order; with coordinates in [0, 4096) it is packed into one
+ * 64-bit integer and radix-sorted.  A direction is skipped while the boxes
+ * have not changed since it last merged nothing (it would merge nothing
+ * again), so the merges, and the result, are those of full passes. */
 inline void simplify(std::vector<IBox> &v) {
     bool small = true;
     for (const IBox &x : v)
         for (int d = 0; d < 3; ++d) small = small && x.lo[d] >= 0 && x.hi[d] < 4096;
-    std::vector<std::pair<unsigned long long, unsigned>> keyed;
+    std::vector<std::pair<unsigned long long, unsigned>> keyed, tmp;
     std::vector<IBox> sorted;
-    bool any = true;
-    while (any) {
-        any = false;
-        for (int d = 0; d < 3; ++d) {
-            const int e = (d + 1) % 3, f = (d + 2) % 3;
-            if (small) {
-                keyed.resize(v.size());
-                for (size_t q = 0; q < v.size(); ++q) {
-                    const IBox &a = v[q];
-                    keyed[q].first = ((unsigned long long)a.lo[e] << 48) |
-                                     ((unsigned long long)a.hi[e] << 36) |
-                                     ((unsigned long long)a.lo[f] << 24) |
-                                     ((unsigned long long)a.hi[f] << 12) |
-                                     (unsigned long long)a.lo[d];
-                    keyed[q].second = (unsigned)q;
-                }
-                std::sort(keyed.begin(), keyed.end());
-                sorted.resize(v.size());
-                for (size_t q = 0; q < v.size(); ++q) sorted[q] = v[keyed[q].second];
-                v.swap(sorted);
-            } else {
-                std::sort(v.begin(), v.end(), [&](const IBox &a, const IBox &b) {
-                    if (a.lo[e] != b.lo[e]) return a.lo[e] < b.lo[e];
-                    if (a.hi[e] != b.hi[e]) return a.hi[e] < b.hi[e];
-                    if (a.lo[f] != b.lo[f]) return a.lo[f] < b.lo[f];
-                    if (a.hi[f] != b.hi[f]) return a.hi[f] < b.hi[f];
-                    return a.lo[d] < b.lo[d];
-                });
+    int clean = 0; /* directions in a row known to merge nothing */
+    for (int d = 0; clean < 3; d = (d + 1) % 3) {
+        const int e = (d + 1) % 3, f = (d + 2) % 3;
+        if (small) {
+            keyed.resize(v.size());
+            for (size_t q = 0; q < v.size(); ++q) {
+                const IBox &a = v[q];
+                keyed[q].first = ((unsigned long long)a.lo[e] << 48) |
+                                 ((unsigned long long)a.hi[e] << 36) |
+                                 ((unsigned long long)a.lo[f] << 24) |
+                                 ((unsigned long long)a.hi[f] << 12) |
+                                 (unsigned long long)a.lo[d];
+                keyed[q].second = (unsigned)q;
             }
-            std::vector<IBox> res;
-            for (const IBox &x : v) {
-                if (!res.empty()) {
-                    IBox &p = res.back();
-                    if (p.lo[e] == x.lo[e] && p.hi[e] == x.hi[e] && p.lo[f] == x.lo[f] &&
-                        p.hi[f] == x.hi[f] && p.hi[d] + 1 == x.lo[d]) {
-                        p.hi[d] = x.hi[d];
-                        any = true;
-                        continue;
-                    }
-                }
-                res.push_back(x);
-            }
-            v.swap(res);
+            radix_sort_keyed(keyed, tmp, 60);
+            sorted.resize(v.size());
+            for (size_t q = 0; q < v.size(); ++q) sorted[q] = v[keyed[q].second];
+            v.swap(sorted);
+        } else {
+            std::sort(v.begin(), v.end(), [&](const IBox &a, const IBox &b) {
+                if (a.lo[e] != b.lo[e]) return a.lo[e] < b.lo[e];
+                if (a.hi[e] != b.hi[e]) return a.hi[e] < b.hi[e];
+                if (a.lo[f] != b.lo[f]) return a.lo[f] < b.lo[f];
+                if (a.hi[f] != b.hi[f]) return a.hi[f] < b.hi[f];
+                return a.lo[d] < b.lo[d];
+            });
         }
+        std::vector<IBox> res;
+        bool merged = false;
+        for (const IBox &x : v) {
+            if (!res.empty()) {
+                IBox &p = res.back();
+                if (p.lo[e] == x.lo[e] && p.hi[e] == x.hi[e] && p.lo[f] == x.lo[f] &&
+                    p.hi[f] == x.hi[f] && p.hi[d] + 1 == x.lo[d]) {
+                    p.hi[d] = x.hi[d];
+                    merged = true;
+                    continue;
+                }
+            }
+            res.push_back(x);
+        }
+        v.swap(res);
+        /* merging along d leaves nothing to merge along d */
+        clean = merged ? 1 : clean + 1;
     }
 }
 
