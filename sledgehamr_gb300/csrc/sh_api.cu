@@ -19,6 +19,7 @@
 
 #include "sh_bubbles.cuh"
 #include "sh_out.cuh"
+#include "sh_fill_plan.h"
 #include "sh_fixed_stencil.h"
 #include "sh_gw.h"
 #include "sh_internal.h"
@@ -386,13 +387,6 @@ __global__ void copy_items_kernel(const CopyItem *__restrict__ items, double *__
     }
 }
 
-/* A rectangle [lo, hi] of cells of box dbox (ghost-grown) filled by
- * quadratic interpolation from the coarse level. */
-struct CfRect {
-    int dbox;
-    int lo[3], hi[3];
-    long long first; /* running cell count */
-};
 
 /* Block map of a level: owner box of every aligned block of `res` cells
  * (-1 where no box). */
@@ -961,49 +955,15 @@ bool box_intersect(const int alo[3], const int ahi[3], const int blo[3], const i
 /* Owner map of a level: blocks of `res` cells, res = the largest size that
  * divides the domain and every box bound (boxes are unions of blocks). */
 void build_owner_map(sh_ctx *ctx, sh_level *L) {
-    auto gcd = [](int a, int b) {
-        a = a < 0 ? -a : a;
-        b = b < 0 ? -b : b;
-        while (b) {
-            int r = a % b;
-            a = b;
-            b = r;
-        }
-        return a;
-    };
-    int res = 0;
-    for (int d = 0; d < 3; ++d) res = gcd(res, L->dhi[d] - L->dlo[d] + 1);
-    for (const sh_box &b : L->boxes)
-        for (int d = 0; d < 3; ++d) {
-            res = gcd(res, b.lo[d] - L->dlo[d]);
-            res = gcd(res, b.hi[d] + 1 - L->dlo[d]);
-        }
-    if (res <= 0) res = 1;
-    L->owner_res = res;
-    for (int d = 0; d < 3; ++d) L->owner_nb[d] = (L->dhi[d] - L->dlo[d] + 1) / res;
-    const long long nmap = (long long)L->owner_nb[0] * L->owner_nb[1] * L->owner_nb[2];
-    L->owner.resize((size_t)nmap);
-    int *own = L->owner.data();
-#pragma omp parallel for schedule(static)
-    for (long long q = 0; q < nmap; ++q) own[q] = -1;
-    /* boxes in parallel; overlapping boxes would leave fewer owned blocks
-     * than the boxes hold, which the count below detects */
-    const long long nbx = (long long)L->boxes.size();
-    long long want = 0;
-#pragma omp parallel for schedule(dynamic, 64) reduction(+ : want)
-    for (long long q = 0; q < nbx; ++q) {
-        const sh_box &b = L->boxes[q];
-        for (int z = (b.lo[2] - L->dlo[2]) / res; z <= (b.hi[2] - L->dlo[2]) / res; ++z)
-            for (int y = (b.lo[1] - L->dlo[1]) / res; y <= (b.hi[1] - L->dlo[1]) / res; ++y)
-                for (int x = (b.lo[0] - L->dlo[0]) / res; x <= (b.hi[0] - L->dlo[0]) / res; ++x) {
-                    own[((size_t)z * L->owner_nb[1] + y) * L->owner_nb[0] + x] = (int)q;
-                    ++want;
-                }
+    OwnerMap m;
+    try {
+        sh::build_owner_map(L->dlo, L->dhi, L->boxes.data(), (int)L->boxes.size(), m);
+    } catch (const PlanError &e) {
+        throw ShError(SH_ERR_ARG, e.what());
     }
-    long long have = 0;
-#pragma omp parallel for schedule(static) reduction(+ : have)
-    for (long long q = 0; q < nmap; ++q) have += own[q] >= 0;
-    if (have != want) throw ShError(SH_ERR_ARG, "boxes of a level overlap");
+    L->owner.swap(m.owner);
+    L->owner_res = m.res;
+    for (int d = 0; d < 3; ++d) L->owner_nb[d] = m.nb[d];
     L->d_owner = upload_async(ctx, L->owner.data(), L->owner.size(), "owner map");
 }
 
@@ -1019,224 +979,35 @@ OwnerMapDev owner_map_dev(const sh_level *L) {
     return m;
 }
 
-inline int floordiv(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
-
-/* Fill plan of dst's ghost-grown boxes, built on the block grid of src:
- * every block region of a dst box takes the valid cells of its owner box in
- * src (periodic images included) and regions no src box owns are
- * interpolated from the coarse level (FillPatchTwoLevels /
- * InterpFromCoarseLevel).  With ghosts_only (src == dst: ghost fill) the
- * valid region of every dst box is skipped. */
-struct FillPlan {
-    std::vector<GhostCopyDev> rects;
-    long long rect_cells = 0;
-    std::vector<CfRect> cf;
-    long long cf_cells = 0;
-};
+/* The fill planning of sh_fill_plan.h on the levels' host metadata; its
+ * errors become SH_ERR_ARG. */
+PlanLevel plan_level(const sh_level *L) {
+    PlanLevel p;
+    for (int d = 0; d < 3; ++d) {
+        p.dlo[d] = L->dlo[d];
+        p.dhi[d] = L->dhi[d];
+        p.owner_nb[d] = L->owner_nb[d];
+    }
+    p.boxes = L->boxes.data();
+    p.nbox = (int)L->boxes.size();
+    p.nghost = L->nghost;
+    p.ncomp = L->ncomp;
+    p.owner = L->owner.data();
+    p.owner_res = L->owner_res;
+    return p;
+}
 
 FillPlan build_fill_plan(const sh_level *D, const sh_level *S, const sh_level *C,
                          bool ghosts_only, bool want_copies = true) {
-    FillPlan P;
-    const int ext[3] = {D->dhi[0] - D->dlo[0] + 1, D->dhi[1] - D->dlo[1] + 1,
-                        D->dhi[2] - D->dlo[2] + 1};
-    if (S)
-        for (int d = 0; d < 3; ++d)
-            require(S->dlo[d] == D->dlo[d] && S->dhi[d] == D->dhi[d],
-                    "fill source has a different domain");
-    if (C) {
-        require(C->ncomp == D->ncomp, "coarse level differs in components");
-        require(C->nghost >= 1, "coarse level needs at least one ghost cell");
-        for (int d = 0; d < 3; ++d)
-            require(2 * (C->dhi[d] - C->dlo[d] + 1) == ext[d] && 2 * C->dlo[d] == D->dlo[d],
-                    "coarse domain is not the fine domain coarsened by 2");
+    const PlanLevel d = plan_level(D);
+    const PlanLevel s = S ? plan_level(S) : PlanLevel{};
+    const PlanLevel c = C ? plan_level(C) : PlanLevel{};
+    try {
+        return sh::build_fill_plan(d, S == D ? &d : (S ? &s : nullptr), C ? &c : nullptr,
+                                   ghosts_only, want_copies);
+    } catch (const PlanError &e) {
+        throw ShError(SH_ERR_ARG, e.what());
     }
-    /* blocks: those of src, or (no src) those of dst */
-    const sh_level *G = S ? S : D;
-    const int R = G->owner_res;
-    const int g = D->nghost;
-    /* per destination box: the blocks of its ghost-grown region, each with a
-     * source (owner box and periodic shift), "interpolate" or "skip", then
-     * runs of equal source along x merged along y and z */
-    struct Blk {
-        int kind; /* 0 skip, 1 copy, 2 interpolate */
-        int own;
-        int sh[3];
-        int lo[3], hi[3];
-    };
-    struct Run {
-        int kind, own, sh[3], lo[3], hi[3];
-    };
-    const long long nbox = (long long)D->boxes.size();
-    std::vector<std::vector<GhostCopyDev>> box_rects(nbox);
-    std::vector<std::vector<CfRect>> box_cf(nbox);
-    bool uncovered = false;
-    /* boxes are independent: host threads share them, results are
-     * concatenated in box order afterwards (the plan is deterministic) */
-#pragma omp parallel
-    {
-    std::vector<Blk> blk;
-    std::vector<Run> runs, merged;
-#pragma omp for schedule(dynamic, 16)
-    for (long long b = 0; b < nbox; ++b) {
-        int glo[3], ghi[3], blo[3], nbk[3];
-        for (int d = 0; d < 3; ++d) {
-            glo[d] = D->boxes[b].lo[d] - g;
-            ghi[d] = D->boxes[b].hi[d] + g;
-            blo[d] = floordiv(glo[d] - D->dlo[d], R);
-            nbk[d] = floordiv(ghi[d] - D->dlo[d], R) - blo[d] + 1;
-        }
-        blk.assign((size_t)nbk[0] * nbk[1] * nbk[2], Blk{});
-        for (int z = 0; z < nbk[2]; ++z)
-            for (int y = 0; y < nbk[1]; ++y)
-                for (int x = 0; x < nbk[0]; ++x) {
-                    const int bb[3] = {blo[0] + x, blo[1] + y, blo[2] + z};
-                    Blk &k = blk[((size_t)z * nbk[1] + y) * nbk[0] + x];
-                    int wb[3];
-                    bool inside_valid = true;
-                    for (int d = 0; d < 3; ++d) {
-                        k.lo[d] = std::max(glo[d], D->dlo[d] + bb[d] * R);
-                        k.hi[d] = std::min(ghi[d], D->dlo[d] + (bb[d] + 1) * R - 1);
-                        const int nbd = G->owner_nb[d];
-                        wb[d] = ((bb[d] % nbd) + nbd) % nbd;
-                        k.sh[d] = (bb[d] - wb[d]) * R; /* periodic image offset */
-                        if (k.lo[d] < D->boxes[b].lo[d] || k.hi[d] > D->boxes[b].hi[d])
-                            inside_valid = false;
-                    }
-                    k.kind = 0;
-                    k.own = -1;
-                    if (ghosts_only && inside_valid) continue;
-                    const int own = S ? S->owner[((size_t)wb[2] * G->owner_nb[1] + wb[1]) *
-                                                     G->owner_nb[0] +
-                                                 wb[0]]
-                                      : -1;
-                    if (own >= 0) {
-                        if (S == D && own == (int)b && k.sh[0] == 0 && k.sh[1] == 0 &&
-                            k.sh[2] == 0)
-                            continue;
-                        k.kind = 1;
-                        k.own = own;
-                        continue;
-                    }
-                    if (!C) continue; /* nothing to fill from: left as is */
-                    k.kind = 2; /* parents checked per merged rectangle below */
-                }
-        /* x-runs of equal kind / source */
-        runs.clear();
-        for (int z = 0; z < nbk[2]; ++z)
-            for (int y = 0; y < nbk[1]; ++y) {
-                int x = 0;
-                while (x < nbk[0]) {
-                    const Blk &k = blk[((size_t)z * nbk[1] + y) * nbk[0] + x];
-                    if (k.kind == 0) {
-                        ++x;
-                        continue;
-                    }
-                    int x1 = x;
-                    while (x1 + 1 < nbk[0]) {
-                        const Blk &n = blk[((size_t)z * nbk[1] + y) * nbk[0] + x1 + 1];
-                        if (n.kind != k.kind || n.own != k.own || n.sh[0] != k.sh[0] ||
-                            n.sh[1] != k.sh[1] || n.sh[2] != k.sh[2])
-                            break;
-                        ++x1;
-                    }
-                    const Blk &e = blk[((size_t)z * nbk[1] + y) * nbk[0] + x1];
-                    Run r{k.kind, k.own, {k.sh[0], k.sh[1], k.sh[2]},
-                          {k.lo[0], k.lo[1], k.lo[2]}, {e.hi[0], k.hi[1], k.hi[2]}};
-                    runs.push_back(r);
-                    x = x1 + 1;
-                }
-            }
-        /* merge along y, then along z (same kind, source and x extent) */
-        for (int d = 1; d <= 2; ++d) {
-            merged.clear();
-            for (const Run &r : runs) {
-                bool done = false;
-                for (size_t q = merged.size(); q-- > 0;) {
-                    Run &m = merged[q];
-                    /* runs are ordered by z: along y only the same plane */
-                    if (d == 1 && m.lo[2] != r.lo[2]) break;
-                    bool same = m.kind == r.kind && m.own == r.own && m.sh[0] == r.sh[0] &&
-                                m.sh[1] == r.sh[1] && m.sh[2] == r.sh[2] &&
-                                m.hi[d] + 1 == r.lo[d];
-                    for (int e = 0; e < 3 && same; ++e)
-                        if (e != d) same = m.lo[e] == r.lo[e] && m.hi[e] == r.hi[e];
-                    if (same) {
-                        m.hi[d] = r.hi[d];
-                        done = true;
-                        break;
-                    }
-                }
-                if (!done) merged.push_back(r);
-            }
-            runs.swap(merged);
-        }
-        for (const Run &r : runs) {
-            if (r.kind == 1) {
-                if (!want_copies) continue;
-                GhostCopyDev c;
-                c.dbox = (int)b;
-                c.sbox = r.own;
-                for (int d = 0; d < 3; ++d) {
-                    c.lo[d] = r.lo[d];
-                    c.hi[d] = r.hi[d];
-                    c.shift[d] = r.sh[d];
-                }
-                box_rects[b].push_back(c);
-            } else {
-                /* the parents of the region must lie on the coarse level
-                 * (checked per coarse block) */
-                const int Rc = C->owner_res;
-                int pb0[3], pb1[3];
-                for (int d = 0; d < 3; ++d) {
-                    pb0[d] = floordiv(floordiv(r.lo[d], 2) - C->dlo[d], Rc);
-                    pb1[d] = floordiv(floordiv(r.hi[d], 2) - C->dlo[d], Rc);
-                }
-                for (int pz = pb0[2]; pz <= pb1[2]; ++pz)
-                    for (int py = pb0[1]; py <= pb1[1]; ++py)
-                        for (int px = pb0[0]; px <= pb1[0]; ++px) {
-                            const int p3[3] = {px, py, pz};
-                            int cb[3];
-                            for (int d = 0; d < 3; ++d) {
-                                const int n = C->owner_nb[d];
-                                cb[d] = ((p3[d] % n) + n) % n;
-                            }
-                            if (C->owner[((size_t)cb[2] * C->owner_nb[1] + cb[1]) *
-                                             C->owner_nb[0] +
-                                         cb[0]] < 0) {
-#pragma omp atomic write
-                                uncovered = true;
-                            }
-                        }
-                CfRect c;
-                c.dbox = (int)b;
-                for (int d = 0; d < 3; ++d) {
-                    c.lo[d] = r.lo[d];
-                    c.hi[d] = r.hi[d];
-                }
-                box_cf[b].push_back(c);
-            }
-        }
-    }
-    } /* omp parallel */
-    if (uncovered)
-        throw ShError(SH_ERR_ARG, "coarse level does not cover the cells to interpolate (levels "
-                                  "are not properly nested)");
-    auto cells = [](const int lo[3], const int hi[3]) {
-        return (long long)(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
-    };
-    for (long long b = 0; b < nbox; ++b) {
-        for (GhostCopyDev &c : box_rects[b]) {
-            c.first = P.rect_cells;
-            P.rect_cells += cells(c.lo, c.hi);
-            P.rects.push_back(c);
-        }
-        for (CfRect &c : box_cf[b]) {
-            c.first = P.cf_cells;
-            P.cf_cells += cells(c.lo, c.hi);
-            P.cf.push_back(c);
-        }
-    }
-    return P;
 }
 
 /* Splits the rectangle [lo, hi] into pieces of at most kItemCells cells

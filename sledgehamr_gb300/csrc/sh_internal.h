@@ -18,6 +18,8 @@
 #include <string>
 #include <vector>
 
+#include "sh_fill_plan.h" /* GhostCopyDev, CfRect, FillPlan */
+
 namespace sh {
 
 constexpr int kMaxParams = 32;   /* doubles of Rhs parameters per call */
@@ -48,15 +50,6 @@ struct TileDev {
     int nz;         /* planes along z */
 };
 
-/* One rectangle of ghost cells copied from a valid region of the same
- * level: dst cells [lo, hi] of box dbox take the values of cells
- * [lo - shift, hi - shift] of box sbox. */
-struct GhostCopyDev {
-    int dbox, sbox;
-    int lo[3], hi[3];
-    int shift[3];
-    long long first; /* running cell count (prefix sum) */
-};
 
 /* Which epilogue follows the per-cell Rhs evaluation in a stage kernel. */
 enum EpilogueKind : int {
