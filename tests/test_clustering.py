@@ -81,3 +81,24 @@ def test_full_and_empty_tag_sets():
     b = make_boxes(full, full, 0, 0.7, w)
     assert len(b) == (nb // w) ** 3
     assert len(make_boxes(np.zeros_like(full), full, 0, 0.7, w)) == 0
+
+
+def test_simplify_equals_plain_full_passes(tmp_path):
+    """shamr::simplify (radix-sorted keys, merge-free directions skipped)
+    gives the boxes of plain full passes of the same merging rule."""
+    import os
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    here = os.path.dirname(os.path.abspath(__file__))
+    root = os.path.dirname(here)
+    exe = str(tmp_path / "sc")
+    r = subprocess.run([gxx, "-O2", "-std=c++17", "-fopenmp",
+                        "-I" + os.path.join(root, "sledgehamr_gb300", "csrc"),
+                        os.path.join(here, "cpp", "simplify_check.cpp"), "-o", exe],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0 and out.stdout.strip() == "ok", out.stdout
