@@ -137,7 +137,7 @@ void amr_worker(sh_server *S, AmrJob *job, sh_ctx *actx, sh_amr *amr, sh_request
         rc = sh_amr_step(actx, amr, 1);
         long long cu = 0;
         if (rc == SH_OK) rc = sh_amr_info(amr, nullptr, &cu, nullptr);
-        job->cu = cu;
+        if (rc == SH_OK) job->cu = cu;
     }
     if (rc == SH_OK && !job->cancel) {
         const int P = r.N * r.zero_padding;
