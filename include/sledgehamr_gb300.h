@@ -31,6 +31,12 @@
  *                             projects' host code
  *                             (FirstOrderPhaseTransition.cpp:133-157,
  *                              NextToMinimalExample.cpp:35)
+ *   sh_h5_*, sh_output_* .... the HDF5 files of the output types: the
+ *                             dataset writer utils::hdf5::Write
+ *                             (source/utils/hdf5_utils.h:80-104),
+ *                             LevelWriter::WriteSingleLevel
+ *                             (output_types/level_writer.h:80-171) and
+ *                             Slices::Write (output_types/slices.cpp:13-145)
  *   sh_amr_* ................ TimeStepper::Advance / Sledgehamr::Evolve over
  *                             a whole hierarchy (time_stepper.cpp:90-397)
  *   sh_evolve_periodic ...... host-to-host convenience: upload, nsteps x
@@ -133,6 +139,11 @@ SH_API int sh_project_find(const char *name, int *id);
 /* Components of a level of the project (with_gw adds the 12 tensor
  * components) and the number of field/momentum pairs. */
 SH_API int sh_project_ncomp(int id, int with_gw, int *ncomp, int *npairs);
+/* Name of component comp of a level of the project: the names given to
+ * SLEDGEHAMR_ADD_SCALARS / ADD_CONJUGATE_MOMENTA, then u_xx ... du_yz
+ * (Sledgehamr::GetScalarFieldName, source/sledgehamr.h:142-144).  The
+ * string is owned by the library. */
+SH_API int sh_project_comp_name(int id, int comp, const char **name);
 
 /* ---- levels ---------------------------------------------------------------- */
 /* A level of one project: boxes inside the periodic domain [dlo, dhi], with
@@ -144,6 +155,8 @@ SH_API int sh_level_create(sh_ctx *ctx, int project, int with_gw, const int doma
 SH_API int sh_level_destroy(sh_ctx *ctx, sh_level *level);
 /* Index domain of a level (lo, hi inclusive). */
 SH_API int sh_level_domain(const sh_level *level, int lo[3], int hi[3]);
+/* Project id of a level and whether it carries the tensor components. */
+SH_API int sh_level_project(const sh_level *level, int *project, int *with_gw);
 SH_API int sh_level_info(const sh_level *level, int *ncomp, int *nbox, long long *nvalid_cells);
 SH_API int sh_level_time(const sh_level *level, int which, double *t, int *istep);
 /* Box list of a level (capacity boxes; *nbox receives the count). */
@@ -341,6 +354,58 @@ SH_API int sh_index_to_k(int dim, int projection_type, double *out);
 SH_API int sh_gw_spectrum(sh_ctx *ctx, const sh_level *level, const int *comps, int zero_padding,
                    int projection_type, int unbinned, double *bins_out, long long *ks_out,
                    int max_bins, int *nbins);
+
+/* ---- output files ------------------------------------------------------------ */
+/* An HDF5 file of one-dimensional datasets in the root group, as sledgehamr's
+ * utils::hdf5::Write creates them (source/utils/hdf5_utils.h:80-104): IEEE
+ * little-endian F32 or F64 data, integers stored as F64.  Datasets are
+ * collected by sh_h5_add and the file is written by sh_h5_write in the HDF5
+ * library's default (earliest) file format; no HDF5 library is needed.
+ * Names are unique, non-empty and without '/'.  Errors of the sh_h5_* and
+ * sh_output_* calls are reported by sh_h5_last_error. */
+typedef struct sh_h5file sh_h5file;
+#define SH_H5_F32 4   /* float data, stored as F32LE */
+#define SH_H5_F64 8   /* double data, stored as F64LE */
+#define SH_H5_I32 -4  /* int32 data, stored as F64LE */
+#define SH_H5_I64 -8  /* int64 data, stored as F64LE */
+SH_API int sh_h5_create(sh_h5file **out);
+SH_API int sh_h5_destroy(sh_h5file *f);
+SH_API const char *sh_h5_last_error(const sh_h5file *f);
+SH_API int sh_h5_add(sh_h5file *f, const char *name, int type, const void *data, long long n);
+SH_API int sh_h5_count(const sh_h5file *f, long long *n);
+SH_API int sh_h5_write(sh_h5file *f, const char *path);
+
+/* The datasets of a level file (LevelWriter::WriteSingleLevel,
+ * source/output_types/level_writer.h:80-171) added to f: time level NEW
+ * under ident "data", or with truncation_error the truncation errors that
+ * sh_average_down_te left in time level OLD under ident "te" (even cells
+ * only, maximum per output cell).  Per box b (from 1) and component a
+ * dataset "<name>_<ident>_<b>" of the box's cells, x slowest, averaged over
+ * blocks of downsample^3 cells (a power of 2 dividing every box extent) in
+ * precision 32 or 64; then Header_<ident> = {t, 1, finest_level, N,
+ * downsample, boxes} and the box bounds lex_ ley_ lez_ hex_ hey_ hez_
+ * (upper bounds exclusive).  sledgehamr writes one such file per level as
+ * <folder>/Level_<lev>/0.hdf5. */
+SH_API int sh_output_level(sh_ctx *ctx, const sh_level *level, int truncation_error,
+                           int finest_level, int downsample, int precision, sh_h5file *f);
+/* The three slices of a level file (Slices::Write,
+ * source/output_types/slices.cpp:13-145): planes at index
+ * floor(N * location[d]) (made even) normal to x, y and z, idents "x", "y",
+ * "z" (or "te_x", "te_y", "te_z" for truncation errors), 32-bit floats per
+ * box cutting the plane, Header_<ident> = {t, 1, finest_level, N, boxes}
+ * and the bounds le1_ le2_ he1_ he2_. */
+SH_API int sh_output_slices(sh_ctx *ctx, const sh_level *level, int truncation_error,
+                            int finest_level, const double location[3], sh_h5file *f);
+/* The same from host data: boxes and their valid cells in the boxes layout,
+ * ncomp component names, the time and N of the level. */
+SH_API int sh_output_level_host(const sh_box *boxes, int nbox, int ncomp, const double *cells,
+                                const char *const *names, double t, int finest_level,
+                                int dim_n, int truncation_error, int downsample, int precision,
+                                sh_h5file *f);
+SH_API int sh_output_slices_host(const sh_box *boxes, int nbox, int ncomp, const double *cells,
+                                 const char *const *names, double t, int finest_level,
+                                 int dim_n, int truncation_error, const double location[3],
+                                 sh_h5file *f);
 
 /* ---- AMR time stepping ---------------------------------------------------- */
 /* A hierarchy of levels advanced with sledgehamr's recursive subcycling

@@ -90,6 +90,22 @@ SIGNATURES = {
     "sh_project_name": (C.c_char_p, [C.c_int]),
     "sh_project_find": (C.c_int, [C.c_char_p, ip]),
     "sh_project_ncomp": (C.c_int, [C.c_int, C.c_int, ip, ip]),
+    "sh_project_comp_name": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_char_p)]),
+    "sh_level_project": (C.c_int, [vp, ip, ip]),
+    "sh_h5_create": (C.c_int, [C.POINTER(vp)]),
+    "sh_h5_destroy": (C.c_int, [vp]),
+    "sh_h5_last_error": (C.c_char_p, [vp]),
+    "sh_h5_add": (C.c_int, [vp, C.c_char_p, C.c_int, vp, C.c_longlong]),
+    "sh_h5_count": (C.c_int, [vp, llp]),
+    "sh_h5_write": (C.c_int, [vp, C.c_char_p]),
+    "sh_output_level": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp]),
+    "sh_output_slices": (C.c_int, [vp, vp, C.c_int, C.c_int, vp, vp]),
+    "sh_output_level_host": (C.c_int, [C.POINTER(ShBox), C.c_int, C.c_int, vp,
+                                       C.POINTER(C.c_char_p), C.c_double, C.c_int, C.c_int,
+                                       C.c_int, C.c_int, C.c_int, vp]),
+    "sh_output_slices_host": (C.c_int, [C.POINTER(ShBox), C.c_int, C.c_int, vp,
+                                        C.POINTER(C.c_char_p), C.c_double, C.c_int, C.c_int,
+                                        C.c_int, vp, vp]),
     "sh_level_create": (C.c_int, [vp, C.c_int, C.c_int, ip, ip, C.POINTER(ShBox), C.c_int,
                                   C.c_int, C.POINTER(vp)]),
     "sh_level_destroy": (C.c_int, [vp, vp]),

@@ -1638,6 +1638,24 @@ int sh_project_ncomp(int id, int with_gw, int *ncomp, int *npairs) {
     return SH_OK;
 }
 
+int sh_project_comp_name(int id, int comp, const char **name) {
+    const ProjectOps *p = project_by_id(id);
+    if (!p) return SH_ERR_PROJECT;
+    if (!name) return SH_ERR_ARG;
+    /* appended after the user fields (gravitational_waves.cpp:20-31) */
+    static const char *const kGw[12] = {"u_xx",  "u_yy",  "u_zz",  "u_xy",  "u_xz",  "u_yz",
+                                        "du_xx", "du_yy", "du_zz", "du_xy", "du_xz", "du_yz"};
+    if (comp >= 0 && comp < p->nscalars) {
+        *name = p->field_name(comp);
+        return *name ? SH_OK : SH_ERR_PROJECT;
+    }
+    if (p->has_gw && comp >= p->nscalars && comp < p->nscalars + 12) {
+        *name = kGw[comp - p->nscalars];
+        return SH_OK;
+    }
+    return SH_ERR_ARG;
+}
+
 int sh_level_create(sh_ctx *ctx, int project, int with_gw, const int domain_lo[3],
                     const int domain_hi[3], const sh_box *boxes, int nbox, int nghost,
                     sh_level **out) {
@@ -1744,6 +1762,13 @@ int sh_level_destroy(sh_ctx *ctx, sh_level *L) {
     cudaSetDevice(ctx->device);
     level_free(ctx, L); /* stream-ordered: after the work queued on the level */
     delete L;
+    return SH_OK;
+}
+
+int sh_level_project(const sh_level *L, int *project, int *with_gw) {
+    if (!L) return SH_ERR_ARG;
+    if (project) *project = L->project;
+    if (with_gw) *with_gw = L->with_gw ? 1 : 0;
     return SH_OK;
 }
 

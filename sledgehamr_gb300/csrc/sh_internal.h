@@ -124,7 +124,7 @@ struct ProjectOps {
     int nfields;   /* position fields */
     bool has_gw;   /* the project supplies GravitationalWavesRhs<true> */
     int reach;     /* largest neighbour offset its hooks read */
-    const char *const *field_names;
+    const char *(*field_name)(int comp); /* user field names, NULL past them */
     cudaError_t (*launch_stage)(const StageLaunch &, cudaStream_t);
     cudaError_t (*launch_tag)(const TagArgs &, int ntiles, cudaStream_t);
 };

@@ -317,7 +317,10 @@ cudaError_t launch_tag_impl(const TagArgs &a, int ntiles, cudaStream_t s) {
     struct Hooks_##NAME : NS::ShHooks {                                        \
         static constexpr bool kHasGw = HAS_GW;                                 \
     };                                                                         \
-    static const char *const kFieldNames_##NAME[] = {nullptr};                 \
+    static const char *field_name_##NAME(int c) {                              \
+        const auto &f = NS::ShHooks::fields();                                 \
+        return c >= 0 && c < (int)f.size() ? f[c]->name.c_str() : nullptr;    \
+    }                                                                          \
     extern const ProjectOps project_##NAME;                                    \
     const ProjectOps project_##NAME = {                                        \
         #NAME,                                                                 \
@@ -325,7 +328,7 @@ cudaError_t launch_tag_impl(const TagArgs &a, int ntiles, cudaStream_t s) {
         NS::ShHooks::kNFields,                                                 \
         HAS_GW,                                                                \
         REACH,                                                                 \
-        kFieldNames_##NAME,                                                    \
+        &field_name_##NAME,                                                    \
         &launch_stage_impl<Hooks_##NAME>,                                      \
         &launch_tag_impl<Hooks_##NAME>};                                       \
     }

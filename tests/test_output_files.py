@@ -1,0 +1,219 @@
+"""Output files in sledgehamr's formats (no GPU).
+
+* The HDF5 parser of the tests (tests/hdf5_read.py) is pinned on the
+  reference's own HDF5 file data/spectra_ks.hdf5 (written by h5py), whose
+  datasets must equal the spectrum bins and k maps the library generates.
+* The library's HDF5 writer (sh_h5_*) round-trips datasets of every stored
+  type and count through that parser, lays out the same structures and
+  message sequence as the reference's file, and rejects bad names.
+* The level and slice writers on host data (sh_output_*_host) equal the
+  numpy restatement of LevelWriter::WriteSingleLevel and
+  Slices::WriteSingleSlice (oracle/output_oracle.py) bit for bit, for both
+  precisions, downsample factors 1, 2 and 4, and truncation errors.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import output_oracle as oo
+from tests import hdf5_read
+
+REF_DATA = "/root/reference/data/spectra_ks.hdf5"
+
+
+def _sh():
+    import sledgehamr_gb300 as sh
+    return sh
+
+
+@pytest.mark.skipif(not os.path.exists(REF_DATA), reason="reference data file absent")
+def test_reader_pinned_on_reference_file():
+    sh = _sh()
+    f = hdf5_read.File(REF_DATA)
+    dims = sorted({int(k.split("_")[0]) for k in f.keys()})
+    assert dims == [32, 64, 128, 256, 512]
+    for N in dims:
+        bins = f[f"{N}_bins"]
+        assert bins.dtype == np.int64
+        np.testing.assert_array_equal(bins, sh.spectrum_bins(N))
+        assert f[f"{N}_nks"].tolist() == [bins.size]
+        for p in (1, 2):
+            k = f[f"{N}_k{p}"]
+            assert k.dtype == np.float64 and k.shape == (N,)
+            np.testing.assert_allclose(k, sh.index_to_k(N, p), rtol=0, atol=1e-15)
+
+
+def _roundtrip(tmp_path, sets):
+    from sledgehamr_gb300.output import H5File
+    f = H5File()
+    for name, a in sets.items():
+        f.add(name, a)
+    assert len(f) == len(sets)
+    p = str(tmp_path / "x.hdf5")
+    f.write(p)
+    return hdf5_read.File(p)
+
+
+@pytest.mark.parametrize("count", [0, 1, 7, 8, 9, 33, 300, 1200])
+def test_writer_roundtrip(tmp_path, count):
+    rng = np.random.default_rng(count)
+    sets = {}
+    for q in range(count):
+        kind = q % 4
+        n = int(rng.integers(0, 50)) if q % 7 else 0
+        name = "d%0*d_%s" % (int(rng.integers(1, 6)), q, "x" * int(rng.integers(0, 12)))
+        if kind == 0:
+            sets[name] = rng.standard_normal(n).astype(np.float32)
+        elif kind == 1:
+            sets[name] = rng.standard_normal(n)
+        elif kind == 2:
+            sets[name] = rng.integers(-2**31, 2**31, n).astype(np.int32)
+        else:
+            sets[name] = rng.integers(-2**53, 2**53, n).astype(np.int64)
+    r = _roundtrip(tmp_path, sets)
+    assert r.keys() == sorted(sets)
+    for name, a in sets.items():
+        got = r[name]
+        want_type = np.float32 if a.dtype == np.float32 else np.float64
+        assert got.dtype == want_type and got.shape == a.shape
+        np.testing.assert_array_equal(got, a.astype(want_type))
+
+
+def test_writer_layout_matches_reference_file(tmp_path):
+    r = _roundtrip(tmp_path, {"a": np.arange(5.0), "b": np.arange(3, dtype=np.float32)})
+    assert (r.leaf_k, r.internal_k) == (4, 16)
+    assert r.message_types("a") == [1, 3, 5, 8, 0] == r.message_types("b")
+    if os.path.exists(REF_DATA):
+        ref = hdf5_read.File(REF_DATA)
+        assert (ref.leaf_k, ref.internal_k) == (r.leaf_k, r.internal_k)
+        name = ref.keys()[0]
+        assert ref.message_types(name) == r.message_types("a")
+        # same dataspace, fill value and layout message forms
+        for mtype in (1, 5):
+            rm = [m for m in ref.datasets[name].messages if m.type == mtype][0]
+            wm = [m for m in r.datasets["a"].messages if m.type == mtype][0]
+            assert (rm.flags, rm.data[:4]) == (wm.flags, wm.data[:4])
+        hdr_ref = ref.buf[ref.entries[name]:ref.entries[name] + 16]
+        hdr_new = r.buf[r.entries["a"]:r.entries["a"] + 16]
+        assert hdr_ref[:2] == hdr_new[:2] and hdr_ref[4:12] == hdr_new[4:12]
+
+
+def test_writer_rejects_bad_names(tmp_path):
+    from sledgehamr_gb300.output import H5Error, H5File
+    f = H5File()
+    f.add("ok", np.zeros(2))
+    for bad in ["", "a/b", "."]:
+        with pytest.raises(H5Error):
+            f.add(bad, np.zeros(2))
+    with pytest.raises(H5Error):
+        f.add("ok", np.zeros(2))
+    assert len(f) == 1
+
+
+def test_comp_names():
+    from sledgehamr_gb300.output import comp_names
+    assert comp_names("AxionStrings") == ["Psi1", "Psi2", "Pi1", "Pi2"]
+    names = comp_names("FirstOrderPhaseTransition", with_gw=True)
+    assert names[:2] == ["Phi", "dPhi"]
+    assert names[2:] == ["u_xx", "u_yy", "u_zz", "u_xy", "u_xz", "u_yz",
+                         "du_xx", "du_yy", "du_zz", "du_xy", "du_xz", "du_yz"]
+
+
+def _level(rng, N=32, bf=8, nbox=5):
+    """Disjoint boxes aligned to the blocking factor inside an N^3 domain."""
+    boxes = []
+    taken = set()
+    while len(boxes) < nbox:
+        size = [int(rng.choice([bf, 2 * bf])) for _ in range(3)]
+        lo = [int(rng.integers(0, (N - s) // bf + 1)) * bf for s in size]
+        cells = {(x, y, z) for x in range(lo[0] // bf, (lo[0] + size[0]) // bf)
+                 for y in range(lo[1] // bf, (lo[1] + size[1]) // bf)
+                 for z in range(lo[2] // bf, (lo[2] + size[2]) // bf)}
+        if cells & taken:
+            continue
+        taken |= cells
+        boxes.append((tuple(lo), tuple(lo[d] + size[d] - 1 for d in range(3))))
+    return boxes
+
+
+def _compare(got_file, want):
+    assert got_file.keys() == sorted(want)
+    for name, a in want.items():
+        g = got_file[name]
+        assert g.dtype == a.dtype, name
+        np.testing.assert_array_equal(g, a, err_msg=name)
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+@pytest.mark.parametrize("downsample", [1, 2, 4])
+@pytest.mark.parametrize("te", [False, True])
+def test_level_datasets_match_oracle(tmp_path, precision, downsample, te):
+    from sledgehamr_gb300.output import level_datasets_host
+    rng = np.random.default_rng(100 * precision + 10 * downsample + te)
+    boxes = _level(rng)
+    names = ["Psi1", "Psi2", "Pi1"]
+    nv = sum(np.prod([hi[d] - lo[d] + 1 for d in range(3)]) for lo, hi in boxes)
+    cells = rng.standard_normal(nv * len(names)) * 10.0 ** rng.integers(-3, 4, nv * len(names))
+    if te:
+        cells = np.abs(cells)
+    f = level_datasets_host(boxes, cells, names, 3.25, 1, 32, te, downsample, precision)
+    p = str(tmp_path / "0.hdf5")
+    f.write(p)
+    want = oo.level_datasets(boxes, cells, names, 3.25, 1, 32, "te" if te else "data", te,
+                             downsample, precision)
+    _compare(hdf5_read.File(p), want)
+
+
+@pytest.mark.parametrize("te", [False, True])
+def test_slice_datasets_match_oracle(tmp_path, te):
+    from sledgehamr_gb300.output import slices_datasets_host
+    rng = np.random.default_rng(7 + te)
+    boxes = _level(rng, nbox=7)
+    names = ["Phi", "dPhi"]
+    nv = sum(np.prod([hi[d] - lo[d] + 1 for d in range(3)]) for lo, hi in boxes)
+    cells = rng.standard_normal(nv * len(names))
+    for loc in [(0., 0., 0.), (0.3, 0.52, 0.9), (0.999, 0.25, 0.5), (1.0, 1.0, 1.0)]:
+        f = slices_datasets_host(boxes, cells, names, 1.5, 2, 32, te, loc)
+        p = str(tmp_path / "s.hdf5")
+        f.write(p)
+        want = oo.slices_datasets(boxes, cells, names, 1.5, 2, 32, te, loc)
+        _compare(hdf5_read.File(p), want)
+
+
+def test_level_writer_errors():
+    from sledgehamr_gb300.output import H5Error, level_datasets_host
+    boxes = [((0, 0, 0), (7, 7, 5))]
+    cells = np.zeros(8 * 8 * 6)
+    with pytest.raises(H5Error):  # 6 cells are not a multiple of 4
+        level_datasets_host(boxes, cells, ["a"], 0., 0, 8, False, 4, 32)
+    with pytest.raises(H5Error):  # not a power of 2
+        level_datasets_host(boxes, cells, ["a"], 0., 0, 8, False, 3, 32)
+    with pytest.raises(H5Error):
+        level_datasets_host(boxes, cells, ["a"], 0., 0, 8, False, 1, 16)
+    f = level_datasets_host(boxes, cells, ["a"], 0., 0, 8, False, 2, 64)
+    assert len(f) == 1 + 1 + 6
+
+
+def test_spectra_files(tmp_path):
+    from sledgehamr_gb300 import output
+    ks = np.array([0, 1, 2, 3, 4, 5, 6, 8])
+    p = str(tmp_path / "spectra.hdf5")
+    output.write_spectra(p, 2.5, 16, ks, {"phi": np.arange(8.0), "dphi": np.ones(8)})
+    r = hdf5_read.File(p)
+    assert r.keys() == ["Header", "dphi", "k_sq", "phi"]
+    assert r["Header"].tolist() == [2.5, 16.0, 8.0]
+    assert r["k_sq"].tolist() == ks.tolist()
+    p = str(tmp_path / "gw.hdf5")
+    output.write_gw_spectrum(p, 2.5, 16, 8.0, 2, True, ks, np.arange(8.0) ** 2)
+    r = hdf5_read.File(p)
+    assert r["Header"].tolist() == [2.5, 16.0, 8.0, 8.0, 2.0, 1.0]
+    assert r["Spectrum"].tolist() == (np.arange(8.0) ** 2).tolist()
+    p = str(tmp_path / "proj.hdf5")
+    d = np.arange(16.0).reshape(4, 4)
+    n = np.full((4, 4), 3, dtype=np.int32)
+    output.write_projections(p, 1.0, 4, {"energy": (d, n)})
+    r = hdf5_read.File(p)
+    assert r.keys() == ["Header", "energy_data", "energy_n"]
+    assert r["energy_data"].tolist() == d.reshape(-1).tolist()
+    assert r["energy_n"].dtype == np.float64 and r["energy_n"].tolist() == [3.0] * 16
