@@ -111,6 +111,16 @@ def test_writer_rejects_bad_names(tmp_path):
     assert len(f) == 1
 
 
+def test_writer_reports_io_errors(tmp_path):
+    from sledgehamr_gb300.output import H5Error, H5File
+    f = H5File()
+    f.add("a", np.ones(3))
+    with pytest.raises(H5Error):
+        f.write(str(tmp_path / "missing_dir" / "x.hdf5"))
+    f.write(str(tmp_path / "x.hdf5"))
+    assert hdf5_read.File(str(tmp_path / "x.hdf5"))["a"].tolist() == [1.0, 1.0, 1.0]
+
+
 def test_comp_names():
     from sledgehamr_gb300.output import comp_names
     assert comp_names("AxionStrings") == ["Psi1", "Psi2", "Pi1", "Pi2"]
