@@ -227,3 +227,61 @@ def test_spectra_files(tmp_path):
     assert r.keys() == ["Header", "energy_data", "energy_n"]
     assert r["energy_data"].tolist() == d.reshape(-1).tolist()
     assert r["energy_n"].dtype == np.float64 and r["energy_n"].tolist() == [3.0] * 16
+
+
+def _chop(N, mg):
+    return [((x, y, z), (x + mg - 1, y + mg - 1, z + mg - 1))
+            for z in range(0, N, mg) for y in range(0, N, mg) for x in range(0, N, mg)]
+
+
+def _to_boxes_layout(field, boxes):
+    """field[n, x, y, z] -> boxes layout (per box, per component, x fastest)."""
+    out = []
+    for lo, hi in boxes:
+        blk = field[:, lo[0]:hi[0] + 1, lo[1]:hi[1] + 1, lo[2]:hi[2] + 1]
+        out.append(blk.transpose(0, 3, 2, 1).reshape(-1))
+    return np.concatenate(out)
+
+
+@pytest.mark.parametrize("downsample", [1, 2])
+def test_files_reassemble_as_pysledgehamr_reads_them(tmp_path, downsample):
+    """pySledgehamr's Output reassembles a level from the per-box datasets
+    and their bounds (Output.py __Read3dField / __Read2dField); done here on
+    the written files, it gives back the level's field (block-averaged for
+    downsample 2) and its planes."""
+    from sledgehamr_gb300.output import level_datasets_host, slices_datasets_host
+    rng = np.random.default_rng(5)
+    N, names = 32, ["Phi", "dPhi"]
+    field = rng.standard_normal((2, N, N, N))
+    boxes = _chop(N, 16)
+    rng.shuffle(boxes)
+    cells = _to_boxes_layout(field, boxes)
+    p = str(tmp_path / "0.hdf5")
+    level_datasets_host(boxes, cells, names, 0.5, 0, N, False, downsample, 64).write(p)
+    r = hdf5_read.File(p)
+    for f, name in enumerate(names):
+        d = N // downsample
+        got = np.full((d, d, d), np.nan)
+        lx, ly, lz = (r[f"le{a}_data"].astype(int) // downsample for a in "xyz")
+        hx, hy, hz = (r[f"he{a}_data"].astype(int) // downsample for a in "xyz")
+        for b in range(len(lx)):
+            got[lx[b]:hx[b], ly[b]:hy[b], lz[b]:hz[b]] = r[f"{name}_data_{b + 1}"].reshape(
+                hx[b] - lx[b], hy[b] - ly[b], hz[b] - lz[b])
+        want = field[f].reshape(d, downsample, d, downsample, d, downsample).mean(axis=(1, 3, 5))
+        np.testing.assert_allclose(got, want, rtol=0, atol=1e-14)
+    loc = (0.25, 0.5, 0.75)
+    p = str(tmp_path / "s.hdf5")
+    slices_datasets_host(boxes, cells, names, 0.5, 0, N, False, loc).write(p)
+    r = hdf5_read.File(p)
+    for f, name in enumerate(names):
+        for a, ax in enumerate("xyz"):
+            got = np.full((N, N), np.nan, dtype=np.float32)
+            le1, le2 = r[f"le1_{ax}"].astype(int), r[f"le2_{ax}"].astype(int)
+            he1, he2 = r[f"he1_{ax}"].astype(int), r[f"he2_{ax}"].astype(int)
+            for b in range(len(le1)):
+                got[le1[b]:he1[b], le2[b]:he2[b]] = r[f"{name}_{ax}_{b + 1}"].reshape(
+                    he1[b] - le1[b], he2[b] - le2[b])
+            s = int(N * loc[a])
+            s += s % 2
+            want = np.take(field[f], s, axis=a).astype(np.float32)
+            np.testing.assert_array_equal(got, want)
