@@ -97,6 +97,13 @@ def test_writer_layout_matches_reference_file(tmp_path):
         hdr_ref = ref.buf[ref.entries[name]:ref.entries[name] + 16]
         hdr_new = r.buf[r.entries["a"]:r.entries["a"] + 16]
         assert hdr_ref[:2] == hdr_new[:2] and hdr_ref[4:12] == hdr_new[4:12]
+        # the F64 datatype message is byte for byte the one h5py wrote for
+        # the reference's float64 k maps
+        dt_ref = [m for m in ref.datasets["32_k1"].messages if m.type == 3][0]
+        dt_new = [m for m in r.datasets["a"].messages if m.type == 3][0]
+        assert (dt_ref.flags, dt_ref.data) == (dt_new.flags, dt_new.data)
+        # superblock fields other than the end-of-file address are equal
+        assert ref.buf[8:40] == r.buf[8:40] and ref.buf[48:56] == r.buf[48:56]
 
 
 def test_writer_rejects_bad_names(tmp_path):
