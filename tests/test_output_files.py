@@ -292,3 +292,47 @@ def test_files_reassemble_as_pysledgehamr_reads_them(tmp_path, downsample):
             s += s % 2
             want = np.take(field[f], s, axis=a).astype(np.float32)
             np.testing.assert_array_equal(got, want)
+
+
+def test_output_abi_rejects_bad_arguments():
+    import ctypes as C
+    from sledgehamr_gb300 import _lib
+    from sledgehamr_gb300._lib import ShBox
+    lib = _lib.load()
+    assert lib.sh_h5_create(None) < 0
+    h = C.c_void_p()
+    assert lib.sh_h5_create(C.byref(h)) == 0
+    x = np.zeros(4)
+    px = C.c_void_p(x.ctypes.data)
+    assert lib.sh_h5_add(None, b"a", 8, px, 4) < 0
+    assert lib.sh_h5_add(h, None, 8, px, 4) < 0
+    assert lib.sh_h5_add(h, b"a", 8, None, 4) < 0
+    assert lib.sh_h5_add(h, b"a", 8, px, -1) < 0
+    assert lib.sh_h5_add(h, b"a", 3, px, 4) < 0
+    assert lib.sh_h5_add(h, b"a", 8, None, 0) == 0  # an empty dataset
+    assert lib.sh_h5_write(h, None) < 0
+    assert lib.sh_h5_last_error(h)
+    box = (ShBox * 1)()
+    box[0].hi[:] = [7, 7, 7]
+    names = (C.c_char_p * 1)(b"phi")
+    cells = np.zeros(512)
+    pc = C.c_void_p(cells.ctypes.data)
+    loc = (C.c_double * 3)(0.5, 0.5, 0.5)
+    assert lib.sh_output_level_host(box, 1, 1, pc, names, 0.0, 0, 8, 0, 1, 32, None) < 0
+    assert lib.sh_output_level_host(box, 1, 1, None, names, 0.0, 0, 8, 0, 1, 32, h) < 0
+    assert lib.sh_output_level_host(box, 1, 1, pc, None, 0.0, 0, 8, 0, 1, 32, h) < 0
+    assert lib.sh_output_level_host(box, -1, 1, pc, names, 0.0, 0, 8, 0, 1, 32, h) < 0
+    bad = (C.c_char_p * 1)(b"a/b")
+    assert lib.sh_output_level_host(box, 1, 1, pc, bad, 0.0, 0, 8, 0, 1, 32, h) < 0
+    assert lib.sh_output_slices_host(box, 1, 1, pc, names, 0.0, 0, 8, 0, None, h) < 0
+    assert lib.sh_output_slices_host(box, 1, 1, pc, names, 0.0, 0, 8, 0, loc, h) == 0
+    n = C.c_longlong()
+    assert lib.sh_h5_count(h, C.byref(n)) == 0 and n.value == 1 + 3 * (1 + 1 + 4)
+    assert lib.sh_output_level(None, None, 0, 0, 1, 32, h) < 0
+    assert lib.sh_output_slices(None, None, 0, 0, loc, h) < 0
+    s = C.c_char_p()
+    assert lib.sh_project_comp_name(0, -1, C.byref(s)) < 0
+    assert lib.sh_project_comp_name(0, 4, C.byref(s)) == 0 and s.value == b"u_xx"
+    assert lib.sh_project_comp_name(0, 16, C.byref(s)) < 0
+    assert lib.sh_project_comp_name(99, 0, C.byref(s)) < 0
+    assert lib.sh_h5_destroy(h) == 0
