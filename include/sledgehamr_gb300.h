@@ -362,7 +362,8 @@ SH_API int sh_gw_spectrum(sh_ctx *ctx, const sh_level *level, const int *comps, 
  * collected by sh_h5_add and the file is written by sh_h5_write in the HDF5
  * library's default (earliest) file format; no HDF5 library is needed.
  * Names are unique, non-empty and without '/'.  Errors of the sh_h5_* and
- * sh_output_* calls are reported by sh_h5_last_error. */
+ * sh_output_* calls are reported by sh_h5_last_error.  One sh_h5file is
+ * used by one thread at a time; separate files are independent. */
 typedef struct sh_h5file sh_h5file;
 #define SH_H5_F32 4   /* float data, stored as F32LE */
 #define SH_H5_F64 8   /* double data, stored as F64LE */
