@@ -336,3 +336,22 @@ def test_output_abi_rejects_bad_arguments():
     assert lib.sh_project_comp_name(0, 16, C.byref(s)) < 0
     assert lib.sh_project_comp_name(99, 0, C.byref(s)) < 0
     assert lib.sh_h5_destroy(h) == 0
+
+
+def test_output_headers_build_without_cuda(tmp_path):
+    """The HDF5 writer and the dataset assembly are plain C++ (g++, no CUDA
+    headers)."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = tmp_path / "t.cpp"
+    src.write_text('#include "sh_output.h"\nint main() { sh::h5::Writer w; '
+                   'return (int)w.size(); }\n')
+    r = subprocess.run([gxx, "-std=c++17", "-Wall", "-Werror", "-fsyntax-only",
+                        "-I" + os.path.join(root, "include"),
+                        "-I" + os.path.join(root, "sledgehamr_gb300", "csrc"), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
