@@ -55,7 +55,7 @@ def _roundtrip(tmp_path, sets):
     return hdf5_read.File(p)
 
 
-@pytest.mark.parametrize("count", [0, 1, 7, 8, 9, 33, 300, 1200])
+@pytest.mark.parametrize("count", [0, 1, 7, 8, 9, 33, 300, 1200, 9000])
 def test_writer_roundtrip(tmp_path, count):
     rng = np.random.default_rng(count)
     sets = {}
@@ -73,6 +73,9 @@ def test_writer_roundtrip(tmp_path, count):
             sets[name] = rng.integers(-2**53, 2**53, n).astype(np.int64)
     r = _roundtrip(tmp_path, sets)
     assert r.keys() == sorted(sets)
+    # symbol-table nodes hold 8 names and B-tree nodes 32 children: 9000
+    # names need a B-tree of three levels
+    assert len(r.btree_nodes) == (3 if count > 8 * 32 * 32 else 2 if count > 8 * 32 else 1)
     for name, a in sets.items():
         got = r[name]
         want_type = np.float32 if a.dtype == np.float32 else np.float64
