@@ -12,8 +12,14 @@ reference itself (run in a checkout where the reference sources exist).
                          Rhs evaluations, tag masks and truncation errors.
 
   ref_bubbles.npz      - the reference's FOPT bubble injection (AddBubble).
+  hdf5_format.npz      - format fields of data/spectra_ks.hdf5 as h5py wrote
+                         them, read with tests/hdf5_read.py: superblock bytes
+                         8-39 and 48-55, the message types of a dataset's
+                         header, its header prefix, and the dataspace,
+                         fill-value and float64 datatype messages.
 
 Usage: python tests/golden/make_golden.py [REFERENCE_ROOT] [--only=spectra,evolve,bubbles]
+(the spectra step also writes hdf5_format.npz)
 """
 from __future__ import annotations
 
@@ -47,6 +53,24 @@ def spectra_fixtures(ref_root: str):
             out[name + "_offset"] = np.int64(off)
         np.savez_compressed(os.path.join(HERE, f"spectra_ks_{N}.npz"), **out)
         print(f"spectra_ks_{N}.npz: {len(out['bins'])} bins")
+
+
+def hdf5_format_fixture(ref_root: str):
+    from tests import hdf5_read
+    f = hdf5_read.File(os.path.join(ref_root, "data", "spectra_ks.hdf5"))
+    ds = f.datasets["32_k1"]
+    msg = {m.type: m for m in ds.messages}
+    hdr = f.buf[f.entries["32_k1"]:f.entries["32_k1"] + 16]
+    u8 = lambda b: np.frombuffer(bytes(b), dtype=np.uint8).copy()  # noqa: E731
+    np.savez_compressed(
+        os.path.join(HERE, "hdf5_format.npz"),
+        superblock_8_40=u8(f.buf[8:40]), superblock_48_56=u8(f.buf[48:56]),
+        message_types=np.array([m.type for m in ds.messages], dtype=np.int64),
+        message_flags=np.array([m.flags for m in ds.messages], dtype=np.int64),
+        header_prefix=u8(hdr[:2] + hdr[4:12]), dataspace_head=u8(msg[1].data[:4]),
+        fill_value=u8(msg[5].data), datatype_f64=u8(msg[3].data),
+        layout_head=u8(msg[8].data[:2]))
+    print("hdf5_format.npz")
 
 
 def fopt_params(lambda_bar=0.8):
@@ -164,6 +188,7 @@ if __name__ == "__main__":
     subprocess.run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh"), ref_root], check=True)
     if not only or "spectra" in only:
         spectra_fixtures(ref_root)
+        hdf5_format_fixture(ref_root)
     if not only or "evolve" in only:
         evolve_fixtures()
     if not only or "bubbles" in only:

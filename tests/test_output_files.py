@@ -109,6 +109,28 @@ def test_writer_layout_matches_reference_file(tmp_path):
         assert ref.buf[8:40] == r.buf[8:40] and ref.buf[48:56] == r.buf[48:56]
 
 
+def test_writer_format_fields_equal_reference_fixture(tmp_path):
+    """Format fields of the reference's h5py-written file (committed as
+    tests/golden/hdf5_format.npz by tests/golden/make_golden.py) equal the
+    writer's, byte for byte, without the reference present."""
+    from tests.conftest import golden
+    g = golden("hdf5_format")
+    r = _roundtrip(tmp_path, {"a": np.arange(5.0)})
+    u8 = lambda b: np.frombuffer(bytes(b), dtype=np.uint8)  # noqa: E731
+    np.testing.assert_array_equal(u8(r.buf[8:40]), g["superblock_8_40"])
+    np.testing.assert_array_equal(u8(r.buf[48:56]), g["superblock_48_56"])
+    ds = r.datasets["a"]
+    msg = {m.type: m for m in ds.messages}
+    assert [m.type for m in ds.messages] == g["message_types"].tolist()
+    assert [m.flags for m in ds.messages] == g["message_flags"].tolist()
+    hdr = r.buf[r.entries["a"]:r.entries["a"] + 16]
+    np.testing.assert_array_equal(u8(hdr[:2] + hdr[4:12]), g["header_prefix"])
+    np.testing.assert_array_equal(u8(msg[1].data[:4]), g["dataspace_head"])
+    np.testing.assert_array_equal(u8(msg[5].data), g["fill_value"])
+    np.testing.assert_array_equal(u8(msg[3].data), g["datatype_f64"])
+    np.testing.assert_array_equal(u8(msg[8].data[:2]), g["layout_head"])
+
+
 def test_writer_rejects_bad_names(tmp_path):
     from sledgehamr_gb300.output import H5Error, H5File
     f = H5File()
