@@ -6,7 +6,9 @@ time levels (grid_new / grid_old), :meth:`Level.advance` is
 Integrator::Advance, :meth:`Level.fill_patch` is LevelSynchronizer::FillPatch,
 :func:`average_down` / :func:`average_down_te` are AverageDownTo /
 ComputeTruncationErrors, :meth:`Level.tag` is ErrorEst and
-:meth:`Level.gw_spectrum` is GravitationalWaves::ComputeSpectrum.
+:meth:`Level.gw_spectrum` is GravitationalWaves::ComputeSpectrum.  The
+output files of sledgehamr's IOModule are written by
+:mod:`sledgehamr_gb300.output`.
 
 All compute runs in libsledgehamr_gb300.so on the GPU; there is no CPU path.
 """
