@@ -154,20 +154,37 @@ inline int signature_cut(const std::vector<long long> &h, int &kind, long long &
     return best;
 }
 
-inline void cluster(const BlockSet &t, IBox bx, double eff, std::vector<IBox> &out) {
+/* Halves with at least this many blocks between them are clustered as
+ * separate OpenMP tasks when the caller runs cluster_impl<true> inside a
+ * parallel region; the clusters come out in the same order either way. */
+constexpr long long kClusterTaskBlocks = 1 << 15;
+
+template <bool Tasks>
+inline void cluster_impl(const BlockSet &t, IBox bx, double eff, std::vector<IBox> &out) {
     /* signatures over bx, then shrink to the tags' bounding box */
     std::vector<long long> sig[3];
     for (int d = 0; d < 3; ++d) sig[d].assign(bx.hi[d] - bx.lo[d] + 1, 0);
     long long ntag = 0;
-    for (int z = bx.lo[2]; z <= bx.hi[2]; ++z)
-        for (int y = bx.lo[1]; y <= bx.hi[1]; ++y)
-            for (int x = bx.lo[0]; x <= bx.hi[0]; ++x)
-                if (t.at(x, y, z)) {
-                    ++ntag;
-                    ++sig[0][x - bx.lo[0]];
-                    ++sig[1][y - bx.lo[1]];
-                    ++sig[2][z - bx.lo[2]];
+    {
+        /* row by row without branches: x counts per element, y and z
+         * counts per row sum */
+        const int nx = bx.hi[0] - bx.lo[0] + 1;
+        std::vector<int> sx(nx, 0);
+        for (int z = bx.lo[2]; z <= bx.hi[2]; ++z)
+            for (int y = bx.lo[1]; y <= bx.hi[1]; ++y) {
+                const uint8_t *p = &t.bits[((size_t)z * t.nb + y) * t.nb + bx.lo[0]];
+                int row = 0;
+                for (int x = 0; x < nx; ++x) {
+                    const int v = p[x] != 0;
+                    sx[x] += v;
+                    row += v;
                 }
+                sig[1][y - bx.lo[1]] += row;
+                sig[2][z - bx.lo[2]] += row;
+                ntag += row;
+            }
+        for (int x = 0; x < nx; ++x) sig[0][x] = sx[x];
+    }
     if (ntag == 0) return;
     IBox b = bx;
     for (int d = 0; d < 3; ++d) {
@@ -213,8 +230,30 @@ inline void cluster(const BlockSet &t, IBox bx, double eff, std::vector<IBox> &o
     IBox l = b, r = b;
     l.hi[dir] = b.lo[dir] + pos - 1;
     r.lo[dir] = b.lo[dir] + pos;
-    cluster(t, l, eff, out);
-    cluster(t, r, eff, out);
+    if (Tasks && b.volume() >= kClusterTaskBlocks) {
+        std::vector<IBox> lo_out, hi_out;
+#pragma omp task default(none) shared(t, lo_out) firstprivate(l, eff)
+        cluster_impl<true>(t, l, eff, lo_out);
+#pragma omp task default(none) shared(t, hi_out) firstprivate(r, eff)
+        cluster_impl<true>(t, r, eff, hi_out);
+#pragma omp taskwait
+        out.insert(out.end(), lo_out.begin(), lo_out.end());
+        out.insert(out.end(), hi_out.begin(), hi_out.end());
+        return;
+    }
+    cluster_impl<Tasks>(t, l, eff, out);
+    cluster_impl<Tasks>(t, r, eff, out);
+}
+
+inline void cluster(const BlockSet &t, IBox bx, double eff, std::vector<IBox> &out) {
+    cluster_impl<false>(t, bx, eff, out);
+}
+
+/* cluster() with the large halves as OpenMP tasks of a team of its own. */
+inline void cluster_parallel(const BlockSet &t, IBox bx, double eff, std::vector<IBox> &out) {
+#pragma omp parallel default(none) shared(t, bx, eff, out)
+#pragma omp single
+    cluster_impl<true>(t, bx, eff, out);
 }
 
 /* Stable LSD radix sort of (key, index) pairs by key, 11 bits per pass. */
@@ -424,7 +463,7 @@ inline std::vector<IBox> make_boxes(const std::vector<uint8_t> &tagbits,
         return bb;
     }
     std::vector<IBox> cl;
-    cluster(tags, IBox{{0, 0, 0}, {nb - 1, nb - 1, nb - 1}}, grid_eff, cl);
+    cluster_parallel(tags, IBox{{0, 0, 0}, {nb - 1, nb - 1, nb - 1}}, grid_eff, cl);
     nested(cl, bb);
     simplify(bb);
     max_size(bb, w);

@@ -102,3 +102,26 @@ def test_simplify_equals_plain_full_passes(tmp_path):
     assert r.returncode == 0, r.stderr
     out = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert out.returncode == 0 and out.stdout.strip() == "ok", out.stdout
+
+
+def test_cluster_tasks_equal_serial_recursion(tmp_path):
+    """Berger-Rigoutsos with the large halves as OpenMP tasks
+    (shamr::cluster_parallel) gives the serial recursion's clusters in the
+    same order."""
+    import os
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    here = os.path.dirname(os.path.abspath(__file__))
+    root = os.path.dirname(here)
+    exe = str(tmp_path / "ctc")
+    r = subprocess.run([gxx, "-O2", "-std=c++17", "-fopenmp",
+                        "-I" + os.path.join(root, "sledgehamr_gb300", "csrc"),
+                        os.path.join(here, "cpp", "cluster_tasks_check.cpp"), "-o", exe],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=300,
+                         env=dict(os.environ, OMP_NUM_THREADS="4"))
+    assert out.returncode == 0 and out.stdout.strip().endswith("ok"), out.stdout
