@@ -85,13 +85,12 @@ bool level_datasets_t(h5::Writer &w, const HostLevel &L, const std::string &iden
     const int gd = downsample * ndist;
     const double volfac = 1. / ((double)downsample * downsample * downsample);
     std::vector<double> lo[3], hi[3];
-    long long base = 0;
+    std::vector<long long> base(L.nbox + 1, 0);
     for (int b = 0; b < L.nbox; ++b) {
         const sh_box &bx = L.boxes[b];
-        const int ext[3] = {bx.hi[0] - bx.lo[0] + 1, bx.hi[1] - bx.lo[1] + 1,
-                            bx.hi[2] - bx.lo[2] + 1};
         for (int d = 0; d < 3; ++d) {
-            if (ext[d] % gd != 0 || (te && bx.lo[d] % 2 != 0)) {
+            const int ext = bx.hi[d] - bx.lo[d] + 1;
+            if (ext % gd != 0 || (te && bx.lo[d] % 2 != 0)) {
                 *err = "level output: box " + std::to_string(b) +
                        " is not a multiple of the downsample factor" +
                        (te ? " times 2 at even offsets" : "");
@@ -100,35 +99,46 @@ bool level_datasets_t(h5::Writer &w, const HostLevel &L, const std::string &iden
             lo[d].push_back(bx.lo[d]);
             hi[d].push_back(bx.hi[d] + 1);
         }
-        const int dx = ext[0] / gd, dy = ext[1] / gd, dz = ext[2] / gd;
-        const long long len = (long long)dx * dy * dz;
-        const long long vol = box_cells(bx);
-        for (int f = 0; f < L.ncomp; ++f) {
-            const double *src = L.cells + base + (long long)f * vol;
-            std::vector<T> o((size_t)len, T(0));
-            for (int k = 0; k < ext[2]; ++k)
-                for (int j = 0; j < ext[1]; ++j)
-                    for (int i = 0; i < ext[0]; ++i) {
-                        const int gi = bx.lo[0] + i, gj = bx.lo[1] + j, gk = bx.lo[2] + k;
-                        if (te && (gi % 2 != 0 || gj % 2 != 0 || gk % 2 != 0)) continue;
-                        const long long ind =
-                            (long long)(i / gd) * dy * dz + (long long)(j / gd) * dz + k / gd;
-                        const double v = src[i + (long long)ext[0] * (j + (long long)ext[1] * k)];
-                        if (te) {
-                            const T c = static_cast<T>(v);
-                            o[ind] = c < o[ind] ? o[ind] : c; /* std::max(c, o) */
-                        } else {
-                            o[ind] = static_cast<T>(o[ind] + v * volfac);
-                        }
+        base[b + 1] = base[b] + box_cells(bx) * L.ncomp;
+    }
+    /* every (box, component) dataset independently on the host threads,
+     * then added in the reference's order */
+    const long long nset = (long long)L.nbox * L.ncomp;
+    std::vector<std::vector<unsigned char>> bytes(nset);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (long long q = 0; q < nset; ++q) {
+        const int b = (int)(q / L.ncomp), f = (int)(q % L.ncomp);
+        const sh_box &bx = L.boxes[b];
+        const int ext[3] = {bx.hi[0] - bx.lo[0] + 1, bx.hi[1] - bx.lo[1] + 1,
+                            bx.hi[2] - bx.lo[2] + 1};
+        const int dy = ext[1] / gd, dz = ext[2] / gd;
+        const long long len = (long long)(ext[0] / gd) * dy * dz;
+        const double *src = L.cells + base[b] + (long long)f * box_cells(bx);
+        std::vector<T> o((size_t)len, T(0));
+        for (int k = 0; k < ext[2]; ++k)
+            for (int j = 0; j < ext[1]; ++j)
+                for (int i = 0; i < ext[0]; ++i) {
+                    const int gi = bx.lo[0] + i, gj = bx.lo[1] + j, gk = bx.lo[2] + k;
+                    if (te && (gi % 2 != 0 || gj % 2 != 0 || gk % 2 != 0)) continue;
+                    const long long ind =
+                        (long long)(i / gd) * dy * dz + (long long)(j / gd) * dz + k / gd;
+                    const double v = src[i + (long long)ext[0] * (j + (long long)ext[1] * k)];
+                    if (te) {
+                        const T c = static_cast<T>(v);
+                        o[ind] = c < o[ind] ? o[ind] : c; /* std::max(c, o) */
+                    } else {
+                        o[ind] = static_cast<T>(o[ind] + v * volfac);
                     }
-            const std::string name =
-                std::string(L.names[f]) + "_" + ident + "_" + std::to_string(b + 1);
-            std::vector<unsigned char> bytes(sizeof(T) * (size_t)len);
-            if (len) std::memcpy(bytes.data(), o.data(), bytes.size());
-            if (!w.add_bytes(name, (int)sizeof(T), std::move(bytes), (uint64_t)len, err))
-                return false;
-        }
-        base += vol * L.ncomp;
+                }
+        bytes[q].resize(sizeof(T) * (size_t)len);
+        if (len) std::memcpy(bytes[q].data(), o.data(), bytes[q].size());
+    }
+    for (long long q = 0; q < nset; ++q) {
+        const int b = (int)(q / L.ncomp), f = (int)(q % L.ncomp);
+        const std::string name =
+            std::string(L.names[f]) + "_" + ident + "_" + std::to_string(b + 1);
+        const uint64_t len = bytes[q].size() / sizeof(T);
+        if (!w.add_bytes(name, (int)sizeof(T), std::move(bytes[q]), len, err)) return false;
     }
     const double header[6] = {L.t, (double)L.ranks, (double)L.finest_level, (double)L.dim_n,
                               (double)downsample, (double)L.nbox};

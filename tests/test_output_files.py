@@ -375,7 +375,7 @@ def test_output_headers_build_without_cuda(tmp_path):
     src = tmp_path / "t.cpp"
     src.write_text('#include "sh_output.h"\nint main() { sh::h5::Writer w; '
                    'return (int)w.size(); }\n')
-    r = subprocess.run([gxx, "-std=c++17", "-Wall", "-Werror", "-fsyntax-only",
+    r = subprocess.run([gxx, "-std=c++17", "-fopenmp", "-Wall", "-Werror", "-fsyntax-only",
                         "-I" + os.path.join(root, "include"),
                         "-I" + os.path.join(root, "sledgehamr_gb300", "csrc"), str(src)],
                        capture_output=True, text=True)
