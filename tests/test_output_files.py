@@ -380,3 +380,57 @@ def test_output_headers_build_without_cuda(tmp_path):
                         "-I" + os.path.join(root, "sledgehamr_gb300", "csrc"), str(src)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def _literal_level_loop(boxes, cells, names, ident, te, downsample, precision):
+    """level_writer.h:88-148 as literal per-cell loops (k, j, i), small
+    cases only: pins the vectorised oracle's order of operations."""
+    T = np.float32 if precision == 32 else np.float64
+    ndist = 2 if te else 1
+    gd = downsample * ndist
+    volfac = 1.0 / float(downsample) ** 3
+    out = {}
+    base = 0
+    for b, (lo, hi) in enumerate(boxes):
+        lx, ly, lz = lo
+        hx, hy, hz = (hi[d] + 1 for d in range(3))
+        dimx, dimy, dimz = (hx - lx) // gd, (hy - ly) // gd, (hz - lz) // gd
+        vol = (hx - lx) * (hy - ly) * (hz - lz)
+        for f, name in enumerate(names):
+            arr = [T(0)] * (dimx * dimy * dimz)
+            src = cells[base + f * vol: base + (f + 1) * vol]
+            for k in range(lz, hz):
+                for j in range(ly, hy):
+                    for i in range(lx, hx):
+                        if te and (i % 2 or j % 2 or k % 2):
+                            continue
+                        ind = (i - lx) // gd * dimy * dimz + (j - ly) // gd * dimz + (k - lz) // gd
+                        v = float(src[(i - lx) + (hx - lx) * ((j - ly) + (hy - ly) * (k - lz))])
+                        if te:
+                            c = T(v)
+                            arr[ind] = arr[ind] if c < arr[ind] else c
+                        else:
+                            arr[ind] = T(float(arr[ind]) + v * volfac)
+            out[f"{name}_{ident}_{b + 1}"] = np.array(arr, dtype=T)
+        base += vol * len(names)
+    return out
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+@pytest.mark.parametrize("downsample,te", [(1, False), (2, False), (4, False), (1, True),
+                                           (2, True)])
+def test_vectorised_level_oracle_equals_literal_loops(precision, downsample, te):
+    rng = np.random.default_rng(3)
+    boxes = [((0, 0, 0), (7, 7, 7)), ((8, 0, 0), (15, 7, 15))]
+    names = ["a", "b"]
+    nv = 8 ** 3 + 8 * 8 * 16
+    cells = rng.standard_normal(nv * 2) * 10.0 ** rng.integers(-8, 9, nv * 2)
+    cells[::17] = -0.0
+    if te:
+        cells = np.abs(cells)
+    ident = "te" if te else "data"
+    want = _literal_level_loop(boxes, cells, names, ident, te, downsample, precision)
+    got = oo.level_datasets(boxes, cells, names, 0., 0, 16, ident, te, downsample, precision)
+    for k, v in want.items():
+        assert got[k].dtype == v.dtype
+        np.testing.assert_array_equal(got[k].view(np.uint8), v.view(np.uint8), err_msg=k)
