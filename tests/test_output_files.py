@@ -434,3 +434,50 @@ def test_vectorised_level_oracle_equals_literal_loops(precision, downsample, te)
     for k, v in want.items():
         assert got[k].dtype == v.dtype
         np.testing.assert_array_equal(got[k].view(np.uint8), v.view(np.uint8), err_msg=k)
+
+
+def _literal_slice_loop(boxes, cells, names, ident, d1, d2, d3, te, location, dim_n):
+    """slices.cpp:61-128 as literal loops, small cases only."""
+    ndist = 2 if te else 1
+    s = int(float(dim_n) * location[d1])
+    if s % 2 == 1:
+        s += 1
+    out, count, base = {}, 0, 0
+    for lo, hi in boxes:
+        ext = [hi[d] - lo[d] + 1 for d in range(3)]
+        vol = ext[0] * ext[1] * ext[2]
+        if lo[d1] <= s <= hi[d1]:
+            count += 1
+            l1, l2, h1, h2 = lo[d2], lo[d3], hi[d2] + 1, hi[d3] + 1
+            dim2 = (h2 - l2) // ndist
+            arr = np.zeros(((h1 - l1) // ndist) * dim2, dtype=np.float32)
+            for f, name in enumerate(names):
+                src = cells[base + f * vol: base + (f + 1) * vol]
+                for j in range(l2, h2):
+                    for i in range(l1, h1):
+                        if te and (i % 2 or j % 2):
+                            continue
+                        c = [0, 0, 0]
+                        c[d1], c[d2], c[d3] = s, i, j
+                        at = (c[0] - lo[0]) + ext[0] * ((c[1] - lo[1]) + ext[1] * (c[2] - lo[2]))
+                        arr[(i - l1) // ndist * dim2 + (j - l2) // ndist] = np.float32(src[at])
+                out[f"{name}_{ident}_{count}"] = arr.copy()
+        base += vol * len(names)
+    return out
+
+
+@pytest.mark.parametrize("te", [False, True])
+def test_vectorised_slice_oracle_equals_literal_loops(te):
+    rng = np.random.default_rng(4)
+    boxes = [((0, 0, 0), (7, 7, 7)), ((8, 0, 0), (15, 7, 15)), ((0, 8, 0), (7, 15, 7))]
+    names = ["a", "b"]
+    nv = sum((hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1) for lo, hi in boxes)
+    cells = rng.standard_normal(nv * 2)
+    for loc in [(0.0, 0.3, 0.9), (0.45, 0.5, 0.2)]:
+        for ident, d1, d2, d3 in (("x", 0, 1, 2), ("y", 1, 0, 2), ("z", 2, 0, 1)):
+            want = _literal_slice_loop(boxes, cells, names, ident, d1, d2, d3, te, loc, 16)
+            got = oo.slice_datasets(boxes, cells, names, 0., 0, 16, ident, d1, d2, d3, te, loc)
+            for k, v in want.items():
+                np.testing.assert_array_equal(got[k].view(np.uint8), v.view(np.uint8), err_msg=k)
+            assert sorted(k for k in got if not k.startswith(("Header", "le", "he"))) == \
+                sorted(want)
