@@ -1,40 +1,51 @@
 """Benchmark of the time-stepping hot path: cell-updates/s on one GPU.
 
-Workloads (--workload):
-  amr (default): axion strings with AMR - 256^3 coarse grid (L = 64,
-      dx = 0.25) plus up to 2 refinement levels (ratio 2, blocking factor 8,
-      max grid size 32), 4th-order Laplacian, lambda = 1, RKN4 with
-      subcycling, eta from 0.1; tags = plaquette winding OR truncation error
-      (te_crit = 1e-3, shadow level), string-width threshold 1.5, regrid
-      interval 0.25; one step = one coarse step (Advance(0) with every finer
-      sub-step, level synchronisation and regrid).  The default
-      --steps 91 --warmup 3 runs eta 0.1 -> 6.0.
-  single: 128^3 periodic single level, L = 32, 2nd-order Laplacian,
-      lambda = 1, eta0 = 0.1, dt = 0.0625, one RKN4 step per step.
+Headline (the JSON line's value, e2e, roofline, cpu_baseline): axion
+strings, 128^3 periodic single level, L = 32 (dx = 0.25), 2nd-order
+(7-point) Laplacian, lambda = 1, RKN4, eta0 = 0.1, dt = 0.25 dx, FP64, on
+the drop-in level path (sh_level_advance); one step = one RKN4 step of the
+level.  The whole job is 200 steps.
+
+Legs reported beside it under "legs" (each with its own workload, timed
+window and errors):
+  amr: 256^3 coarse grid (L = 64, dx = 0.25) plus 2 refinement levels
+      (ratio 2, blocking factor 8, max grid size 32), 4th-order Laplacian,
+      RKN4 with subcycling, tags = plaquette winding OR truncation error
+      (te_crit 1e-3, shadow level).  AxionStrings creates level 1 at
+      eta ~ 1.9 and level 2 at eta ~ 3.8, so the leg first steps (untimed)
+      until the hierarchy holds every level, then times coarse steps with
+      all three levels; one step = one coarse step (Advance(0) with every
+      finer sub-step, synchronisation and regrid).
+  batched_ensemble, fopt_precision, serving: the three chosen forms (FP32 +
+      Kahan batched ensemble, FOPT + GW precision form, serving loop).
 One cell-update = one valid cell of one level advanced by one full step of
-that level, all components.  FP64, seeded band-limited Gaussian initial
-state (|k| <= 1, unit variance, Pi = 0).
+that level, all components.  Seeded band-limited Gaussian initial state
+(|k| <= 1, unit variance, Pi = 0).
 
 value   : device-resident state; each timed step bracketed by CUDA events on
           the library's stream, L2 flushed (512 MB write) between timed steps
           outside the events.
 e2e     : the whole job through the public C ABI with host buffers: the
-          initial state uploaded from pinned host memory, the steps, every
-          level read back to pinned host memory allocated before the clock
-          starts (per-step bytes = totals / K).
+          level created and the initial state uploaded from pinned host
+          memory, every step, the final state read back to pinned host
+          memory (per-step bytes = totals / steps of the job).
 roofline: the fused stage kernels (Rhs + RKN4 stage update): algorithmic bytes
           of all their launches over their summed duration (CUDA events the
           library records around each launch on its stream), against the
-          measured HBM copy bandwidth.
+          measured HBM copy bandwidth; fp64_roofline: the same kernels'
+          FP64 instruction issue (ncu counts per cell-update) against the
+          FP64 FMA rate measured by `--case fp64-peak`.
 cpu_baseline: the CPU oracle (FP64 restatement, OpenMP, all host cores) on a
           bounded sample of the same workload.
 
 --impl reference: the reference's CPU path on the host cores (the oracle
-port; the reference itself cannot be built without AMReX).
+port; the reference itself cannot be built without AMReX), on the headline
+workload and config; it loads no library of this package.
 """
 from __future__ import annotations
 
 import argparse
+import importlib.util
 import json
 import os
 import subprocess
@@ -56,16 +67,29 @@ METRIC = "cell-updates/s"
 # 16; 40 FP64 words.
 WORDS_PER_CELL_UPDATE = 40
 # Measured DRAM traffic of the stage kernels per cell-update (ncu, dram
-# bytes read + written, the three launches of one RKN4 step on level 1 of
-# the AMR run at N0 = 128: 5.55 GB for 12,729,344 cells), scaled to a launch
-# of the benchmark by the cells it updates.
-TRAFFIC_B_PER_CELL_UPDATE = 436.0
+# bytes read + written of the three launches of one RKN4 step), scaled to a
+# launch of the benchmark by the cells it updates.  AMR: level 1 of the AMR
+# run at N0 = 128 (5.55 GB for 12,729,344 cells); 128^3 level: the launches
+# of `--case single`.
+TRAFFIC_B_PER_CELL_UPDATE = {"amr": 436.0, "single": None}
 
 SINGLE = dict(N=128, L=32.0, project="AxionStringsLap1", params=[1.0, 0.0], nghost=1,
-              eta0=0.1)
+              eta0=0.1, total_steps=200, seed=0)
 AMR = dict(N0=256, L=64.0, project="AxionStringsLap2", params=[1.0, 0.0], nghost=2,
            t_start=0.1, cfl=0.25, max_level=2, blocking_factor=8, max_grid_size=32,
-           n_error_buf=2, regrid_dt=0.25, te_crit=1e-3, string_width_threshold=1.5)
+           n_error_buf=2, regrid_dt=0.25, te_crit=1e-3, string_width_threshold=1.5,
+           t_end=6.0)
+
+
+def load_ic():
+    """The seeded initial-condition module (numpy only), loaded from its
+    file without importing the package, so that the reference arm touches
+    no code of the library."""
+    spec = importlib.util.spec_from_file_location(
+        "sh_ic_standalone", os.path.join(ROOT, "sledgehamr_gb300", "ic.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
 
 
 ENSEMBLE = dict(nreal=192, sizes=(32, 48, 64, 96, 128), lam=(0.5, 4.0), dx=0.25, eta0=0.1,
@@ -559,53 +583,48 @@ def amr_config(sh):
 
 
 def amr_state():
-    from sledgehamr_gb300 import ic
-    return ic.axion_string_ic(AMR["N0"], AMR["L"], kmax=1.0, seed=0)
+    return load_ic().axion_string_ic(AMR["N0"], AMR["L"], kmax=1.0, seed=0)
 
 
 def single_state():
-    from sledgehamr_gb300 import ic
-    return ic.axion_string_ic(SINGLE["N"], SINGLE["L"], kmax=1.0, seed=0)
-
-
-def workload_config(name):
-    if name == "amr":
-        a = AMR
-        return {"workload": "axion strings AMR: 256^3 coarse + 2 refinement levels (ratio 2, "
-                            "blocking factor 8, max grid 32), 4th-order Laplacian, lambda=1, "
-                            "RKN4 with subcycling, winding + truncation-error tags "
-                            "(te_crit 1e-3), FP64",
-                "N0": a["N0"], "L": a["L"], "dx0": a["L"] / a["N0"], "cfl": a["cfl"],
-                "eta0": a["t_start"], "string_width_threshold": a["string_width_threshold"],
-                "regrid_dt": a["regrid_dt"], "n_error_buf": a["n_error_buf"],
-                "project": a["project"], "integrator": "RKN4 (type 21)",
-                "l2": "flushed between timed steps (512 MB write, outside events)"}
     s = SINGLE
-    return {"workload": "axion strings 128^3 periodic single level, RKN4, 7-point Laplacian, "
-                        "lambda=1, FP64", "N": s["N"], "L": s["L"], "dx": s["L"] / s["N"],
-            "dt": 0.25 * s["L"] / s["N"], "project": s["project"],
-            "integrator": "RKN4 (type 21)",
+    return load_ic().axion_string_ic(s["N"], s["L"], kmax=1.0, seed=s["seed"])
+
+
+def single_config():
+    """The headline workload's config; both arms print exactly this dict."""
+    s = SINGLE
+    dx = s["L"] / s["N"]
+    return {"workload": "axion strings 128^3 periodic single level, L=32, 7-point Laplacian, "
+                        "lambda=1, RKN4, eta0=0.1, dt=0.25 dx, FP64 (200-step job)",
+            "N": s["N"], "L": s["L"], "dx": dx, "dt": 0.25 * dx, "eta0": s["eta0"],
+            "job_steps": s["total_steps"], "project": s["project"],
+            "integrator": "RKN4 (type 21)", "ic": "seeded Gaussian field, |k|<=1, seed 0",
             "l2": "flushed between timed steps (512 MB write, outside events)"}
 
 
-def cpu_baseline(workload, budget_s=12.0, max_steps=400):
-    """The oracle on the host cores, steps until about budget_s seconds."""
-    from tests.oracle_lib import Oracle, OracleAmr
-    import sledgehamr_gb300 as sh
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    if workload == "amr":
-        o = OracleAmr(amr_config(sh), amr_state())
-        steps, el = 0, 0.0
-        while el < budget_s and steps < max_steps:
-            t0 = time.perf_counter()
-            o.step(1)
-            el += time.perf_counter() - t0
-            steps += 1
-        cu = o.info()["cell_updates"]
-        o.close()
-        return {"value": cu / el, "unit": METRIC, "cores": cores, "kind": "port",
-                "sample": f"first {steps} coarse steps of the AMR run (oracle, FP64, OpenMP), "
-                          f"{cu} cell-updates in {el:.1f} s"}
+def amr_leg_config():
+    a = AMR
+    return {"workload": "axion strings AMR: 256^3 coarse + 2 refinement levels (ratio 2, "
+                        "blocking factor 8, max grid 32), 4th-order Laplacian, lambda=1, "
+                        "RKN4 with subcycling, winding + truncation-error tags "
+                        "(te_crit 1e-3), FP64; timed coarse steps all hold 3 levels",
+            "N0": a["N0"], "L": a["L"], "dx0": a["L"] / a["N0"], "cfl": a["cfl"],
+            "eta0": a["t_start"], "eta_end": a["t_end"],
+            "string_width_threshold": a["string_width_threshold"],
+            "regrid_dt": a["regrid_dt"], "n_error_buf": a["n_error_buf"],
+            "project": a["project"], "integrator": "RKN4 (type 21)",
+            "l2": "flushed between timed steps (512 MB write, outside events)"}
+
+
+def host_cores():
+    return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+
+
+def cpu_baseline_single(budget_s=12.0, max_steps=400):
+    """The oracle on the host cores: RKN4 steps of the 128^3 level until
+    about budget_s seconds."""
+    from tests.oracle_lib import Oracle
     s = SINGLE
     dx = s["L"] / s["N"]
     orc = Oracle()
@@ -619,61 +638,50 @@ def cpu_baseline(workload, budget_s=12.0, max_steps=400):
         el += time.perf_counter() - t0
         steps += batch
         batch = min(2 * batch, 64)
-    return {"value": s["N"] ** 3 * steps / el, "unit": METRIC, "cores": cores, "kind": "port",
+    return {"value": s["N"] ** 3 * steps / el, "unit": METRIC, "cores": host_cores(),
+            "kind": "port",
             "sample": f"{steps} RKN4 steps of the 128^3 level (oracle, FP64, OpenMP), {el:.1f} s"}
 
 
 def run_reference(args):
     """The reference's CPU implementation of the path (oracle port) on the
-    host cores: each step one step of the same workload, within a time
-    budget."""
+    host cores, on the headline workload: each step one RKN4 step of the
+    128^3 level.  Only the oracle library and numpy are loaded."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import sledgehamr_gb300 as sh
-    from tests.oracle_lib import Oracle, OracleAmr
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    times, cus = [], []
+    from tests.oracle_lib import Oracle
+    s = SINGLE
+    dx = s["L"] / s["N"]
+    orc = Oracle()
+    st = single_state()
+    t = s["eta0"]
+    for _ in range(args.warmup):
+        st = orc.evolve_periodic(s["project"], 21, st, t0=t, dt=0.25 * dx, dx=dx,
+                                 nsteps=1, params=s["params"], nghost=s["nghost"])
+        t += 0.25 * dx
+    times = []
     budget = 150.0
-    if args.workload == "amr":
-        o = OracleAmr(amr_config(sh), amr_state())
-        for _ in range(args.warmup):
-            o.step(1)
-        spent = 0.0
-        for _ in range(args.steps):
-            c0 = o.info()["cell_updates"]
-            t0 = time.perf_counter()
-            o.step(1)
-            dt = time.perf_counter() - t0
-            times.append(dt)
-            cus.append(o.info()["cell_updates"] - c0)
-            spent += dt
-            if spent > budget:
-                break
-        o.close()
-    else:
-        s = SINGLE
-        dx = s["L"] / s["N"]
-        orc = Oracle()
-        st = single_state()
-        for _ in range(args.warmup):
-            st = orc.evolve_periodic(s["project"], 21, st, t0=s["eta0"], dt=0.25 * dx, dx=dx,
-                                     nsteps=1, params=s["params"], nghost=s["nghost"])
-        for _ in range(args.steps):
-            t0 = time.perf_counter()
-            st = orc.evolve_periodic(s["project"], 21, st, t0=s["eta0"], dt=0.25 * dx, dx=dx,
-                                     nsteps=1, params=s["params"], nghost=s["nghost"])
-            times.append(time.perf_counter() - t0)
-            cus.append(s["N"] ** 3)
-    value = float(sum(cus) / sum(times))
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        st = orc.evolve_periodic(s["project"], 21, st, t0=t, dt=0.25 * dx, dx=dx,
+                                 nsteps=1, params=s["params"], nghost=s["nghost"])
+        times.append(time.perf_counter() - t0)
+        t += 0.25 * dx
+        if sum(times) > budget:
+            break
+    value = float(s["N"] ** 3 * len(times) / sum(times))
+    cores = host_cores()
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 0,
         "steps": len(times), "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(times)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": workload_config(args.workload),
+        "data": "synthetic (seeded Gaussian random field, |k|<=1)",
+        "config": single_config(),
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
-                         "sample": f"{len(times)} steps of the workload on the oracle port "
-                                   f"(reference build unavailable: AMReX absent)"},
+                         "sample": f"{len(times)} RKN4 steps of the 128^3 level on the oracle "
+                                   f"port, {cores} threads (reference build unavailable: "
+                                   f"AMReX absent)"},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -701,9 +709,14 @@ def run_case(name):
     (9 stage launches); fopt-fp32k: one 192^3 FOPT + GW realisation, 3
     leapfrog steps; amr / amr128: the AMR workload at N0 = 64 (L = 16), 40
     coarse steps, or N0 = 128 (L = 32), 60 coarse steps; single: the 128^3
-    FP64 level, 3 RKN4 steps."""
+    FP64 level, 3 RKN4 steps; fp64-peak: prints the measured FP64 FMA issue
+    rate (the FP64 roofline's peak)."""
     import sledgehamr_gb300 as sh
     from sledgehamr_gb300 import ic
+    if name == "fp64-peak":
+        r = fp64_probe(0)
+        print(json.dumps({"fp64_fma_per_s": r, "fp64_tflops": 2 * r / 1e12 if r else None}))
+        return
     ctx = sh.Context(0)
     if name.startswith("axion"):
         prec = sh.PREC_FP64 if name.endswith("fp64") else sh.PREC_FP32_KAHAN
@@ -764,27 +777,171 @@ def run_case(name):
     ctx.close()
 
 
+def timed_steps(step, steps, warmup, stream, flush, clk=None, before=None):
+    """W untimed steps, then K steps each bracketed by CUDA events on the
+    library's stream with an L2 flush outside the events; returns the summed
+    milliseconds (and the per-step values of `before`, called before each
+    timed step)."""
+    import torch
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    seen = []
+    for q in range(steps):
+        flush.zero_()
+        if before is not None:
+            seen.append(before())
+        starts[q].record(stream)
+        step()
+        ends[q].record(stream)
+    torch.cuda.synchronize()
+    return float(sum(a.elapsed_time(b) for a, b in zip(starts, ends))), seen
+
+
+# FP64 thread instructions (DFMA + DMUL + DADD) per cell-update of the stage
+# kernels of the 128^3 level (ncu sass instruction counters of the three
+# launches of one RKN4 step, `--case single`, divided by the cells).
+FP64_INSTR_PER_CELL_UPDATE = {"single": None, "amr": None}
+
+
+def fp64_probe(device):
+    """Measured FP64 FMA issue rate of the GPU (thread instructions/s)."""
+    import ctypes as C
+    from sledgehamr_gb300 import _lib
+    r = C.c_double()
+    rc = _lib.load().sh_probe_fp64_fma_rate(device, C.byref(r))
+    return r.value if rc == 0 else None
+
+
+def fp64_roofline(roof, workload, device):
+    """The stage kernels' FP64 instruction issue over their duration against
+    the measured FP64 FMA rate."""
+    per = FP64_INSTR_PER_CELL_UPDATE.get(workload)
+    peak = fp64_probe(device)
+    out = {"bound": "fp64", "unit": "FP64 thread instructions/s", "peak": peak,
+           "peak_kind": "measured (sh_probe_fp64_fma_rate: dependent DFMA chains, all SMs)",
+           "instructions_per_cell_update": per}
+    if per and peak and roof.get("stage_ms_total"):
+        cu = roof["_cell_updates"]
+        ach = per * cu / (roof["stage_ms_total"] / 1e3)
+        out.update({"achieved": ach, "frac": ach / peak})
+    return out
+
+
+def stage_roofline(ctx, words, cell_updates, traffic_b, peak, peak_kind):
+    """HBM roofline of the stage kernels from the library's per-launch CUDA
+    events (profile category "rhs") over the timed region."""
+    stage_ms, stage_launches = ctx.profile_read("rhs")
+    fill_ms, fill_launches = ctx.profile_read("fill_patch")
+    other = {c: ctx.profile_read(c)[0] for c in ("coarse_fine", "average_down", "tagging",
+                                                  "data_move")}
+    achieved = words * 8 * cell_updates / (stage_ms / 1e3) / 1e9
+    cells_per_launch = 3.0 * cell_updates / max(stage_launches, 1)
+    traffic = traffic_b / 3.0 * cells_per_launch if traffic_b else None
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+            "algorithmic_bytes_per_launch": words * 8 / 3.0 * cells_per_launch,
+            "kernel": "stage_kernel (fused Rhs + RKN4 stage update)",
+            "bytes_per_cell_update": words * 8, "stage_ms_total": stage_ms,
+            "stage_launches": stage_launches, "stage_ms_per_launch":
+            stage_ms / max(stage_launches, 1), "fill_ms_total": fill_ms,
+            "fill_launches": fill_launches, "other_ms": other, "_cell_updates": cell_updates}
+
+
+def run_amr_leg(sh, ctx, stream, flush, steps, warmup, peak, peak_kind):
+    """The AMR workload with every level present in the timed window: coarse
+    steps (untimed) until the hierarchy reaches max_level, W more warm-up
+    steps, then K timed coarse steps (at most up to eta_end).  e2e: the same
+    job (from the host initial state to the end of the timed window) through
+    the C ABI with the final hierarchy read back to pinned host memory."""
+    import torch
+    a = AMR
+    dt0 = a["cfl"] * a["L"] / a["N0"]
+    job = int(np.ceil((a["t_end"] - a["t_start"]) / dt0 - 1e-9))
+    state = amr_state()
+    sim = sh.Amr(ctx, amr_config(sh), state)
+    pre = 0
+    while sim.info()["finest"] < a["max_level"] and pre < job:
+        sim.step(1)
+        pre += 1
+    for _ in range(warmup):
+        sim.step(1)
+        pre += 1
+    K = max(1, min(steps, job - pre))
+    l0 = ctx.kernel_launches
+    cu0 = sim.info()["cell_updates"]
+    ctx.profile(True)
+    ms, finest = timed_steps(lambda: sim.step(1), K, 0, stream, flush,
+                             before=lambda: sim.info()["finest"])
+    launches = ctx.kernel_launches - l0
+    cus = sim.info()["cell_updates"] - cu0
+    roof = stage_roofline(ctx, WORDS_PER_CELL_UPDATE, cus, TRAFFIC_B_PER_CELL_UPDATE["amr"],
+                          peak, peak_kind)
+    ctx.profile(False)
+    roof["fp64_roofline"] = fp64_roofline(roof, "amr", torch.cuda.current_device())
+    roof.pop("_cell_updates", None)
+    info = sim.info()
+    levels = [{"level": l, "boxes": sim.level(l).nbox, "cells": sim.level(l).nvalid}
+              for l in range(info["finest"] + 1)]
+    timers = {k: round(v[0], 4) for k, v in sim.timers().items()}
+    sim.close()
+    # e2e: the same job from pinned host memory, read back at the end
+    host_in = torch.from_numpy(np.ascontiguousarray(state)).pin_memory()
+    host_levels = [torch.empty(lv_["cells"] * 4, dtype=torch.float64).pin_memory()
+                   for lv_ in levels]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim2 = sh.Amr(ctx, amr_config(sh), host_in.numpy())
+    for _ in range(pre + K):
+        sim2.step(1)
+    e2e_cus = sim2.info()["cell_updates"]
+    d2h = 0
+    for l in range(sim2.info()["finest"] + 1):
+        v = sim2.level(l)
+        n = v.nvalid * v.ncomp
+        out = host_levels[l] if (l < len(host_levels) and host_levels[l].numel() == n) else \
+            torch.empty(n, dtype=torch.float64).pin_memory()
+        ctx.check(ctx.lib.sh_level_read(ctx.h, v.h, sh.SH_NEW, 1, out.data_ptr()), "read")
+        d2h += n * 8
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    sim2.close()
+    out = {"config": amr_leg_config(), "value": cus / (ms / 1e3), "unit": METRIC,
+           "timed_steps": K, "ms_per_step": ms / K, "untimed_steps_before": pre,
+           "eta_timed": [a["t_start"] + pre * dt0, a["t_start"] + (pre + K) * dt0],
+           "levels_in_timed_window": sorted({f + 1 for f in finest}),
+           "gpu_launches_per_step": launches / K,
+           "stage_launches_per_step": roof["stage_launches"] / K,
+           "cell_updates_timed": cus, "levels_at_end": levels, "nregrids": info["nregrids"],
+           "host_timers_s": timers, "roofline": roof,
+           "e2e": {"value": e2e_cus / e2e_s, "unit": METRIC, "job_steps": pre + K,
+                   "h2d_bytes_per_step": state.size * 8 / (pre + K),
+                   "d2h_bytes_per_step": d2h / (pre + K),
+                   "note": "whole job from the host initial state: the pre-roll to full "
+                           "depth and the timed window, hierarchy read back at the end"}}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=None)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="amr", choices=["amr", "single"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--forms", default="ensemble,fopt,serve",
-                    help="comma list of the chosen-form legs reported beside the headline "
-                         "(ensemble, fopt, serve; empty for none)")
+    ap.add_argument("--legs", default="amr,ensemble,fopt,serve",
+                    help="comma list of the legs reported beside the headline (amr, "
+                         "ensemble, fopt, serve; empty for none)")
     ap.add_argument("--serve-max-n", type=int, default=SERVE["max_n"])
     ap.add_argument("--case", default=None,
                     help="run one small profiling case and exit: axion-fp32k, axion-fp64, "
-                         "fopt-fp32k, amr, amr128, single")
+                         "fopt-fp32k, amr, amr128, single, fp64-peak")
     args = ap.parse_args()
     if args.case:
         run_case(args.case)
         return
-    if args.steps is None:
-        args.steps = 91 if args.workload == "amr" else 20
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         run_reference(args)
@@ -808,165 +965,92 @@ def main():
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    peak, peak_kind = peaks()
 
-    if args.workload == "amr":
-        state = amr_state()
-        sim = sh.Amr(ctx, amr_config(sh), state)
-
-        def step():
-            sim.step(1)
-
-        def cell_updates():
-            return sim.info()["cell_updates"]
-    else:
-        s = SINGLE
-        state = single_state()
-        dx = s["L"] / s["N"]
-        lv = sh.Level.periodic(ctx, s["project"], s["N"], s["nghost"])
-        lv.write(state)
-        lv.set_time(s["eta0"])
-        count = [0]
-
-        def step():
-            lv.advance(sh.RKN4, 0.25 * dx, dx, params=s["params"])
-            count[0] += s["N"] ** 3
-
-        def cell_updates():
-            return count[0]
-
+    # ---- headline: the 128^3 level on the drop-in path -------------------
+    s = SINGLE
+    N = s["N"]
+    dx = s["L"] / N
+    dt = 0.25 * dx
+    state = single_state()
+    lv = sh.Level.periodic(ctx, s["project"], N, s["nghost"])
+    lv.write(state)
+    lv.set_time(s["eta0"])
     for _ in range(args.warmup):
-        step()
+        lv.advance(sh.RKN4, dt, dx, params=s["params"])
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     l0 = ctx.kernel_launches
-    cu0 = cell_updates()
     ctx.profile(True)
     with ClockSampler(local) as clk:
-        for q in range(args.steps):
-            flush.zero_()
-            starts[q].record(stream)
-            step()
-            ends[q].record(stream)
-        torch.cuda.synchronize()
+        total_ms, _ = timed_steps(lambda: lv.advance(sh.RKN4, dt, dx, params=s["params"]),
+                                  args.steps, 0, stream, flush)
     launches = ctx.kernel_launches - l0
-    cus = cell_updates() - cu0
-    stage_ms, stage_launches = ctx.profile_read("rhs")
-    fill_ms, fill_launches = ctx.profile_read("fill_patch")
-    other = {c: ctx.profile_read(c)[0] for c in ("coarse_fine", "average_down", "tagging",
-                                                  "data_move")}
+    cus = N ** 3 * args.steps
+    roof = stage_roofline(ctx, WORDS_PER_CELL_UPDATE, cus, TRAFFIC_B_PER_CELL_UPDATE["single"],
+                          peak, peak_kind)
     ctx.profile(False)
+    lv.close()
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    total_ms = float(sum(a.elapsed_time(b) for a, b in zip(starts, ends)))
     value, total_ms = replica_aggregate(total_ms, cus, world, "cuda")
-    achieved = WORDS_PER_CELL_UPDATE * 8 * cus / (stage_ms / 1e3) / 1e9
-    cells_per_launch = 3.0 * cus / max(stage_launches, 1)
-    traffic = TRAFFIC_B_PER_CELL_UPDATE / 3.0 * cells_per_launch if args.workload == "amr" else None
-    peak, peak_kind = peaks()
-    amr_info = None
-    if args.workload == "amr":
-        amr_info = sim.info()
-        levels = [{"level": l, "boxes": sim.level(l).nbox, "cells": sim.level(l).nvalid}
-                  for l in range(amr_info["finest"] + 1)]
-        amr_timers = {k: round(v[0], 4) for k, v in sim.timers().items()}
-        sim.close()
+    roof["fp64_roofline"] = fp64_roofline(roof, "single", local)
+    roof.pop("_cell_updates", None)
 
-    # e2e: the whole job through the public API with pinned host buffers
+    # e2e: the whole 200-step job through the C ABI with pinned host buffers
     host_in = torch.from_numpy(np.ascontiguousarray(state)).pin_memory()
-    host_levels = []
-    if args.workload == "amr":
-        # the hierarchy is deterministic: the read-back buffers are sized from
-        # the device-resident run and pinned before the clock starts
-        ncomp = 4
-        host_levels = [torch.empty(lv_["cells"] * ncomp, dtype=torch.float64).pin_memory()
-                       for lv_ in levels]
+    host_out = torch.empty_like(host_in).pin_memory()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    if args.workload == "amr":
-        sim2 = sh.Amr(ctx, amr_config(sh), host_in.numpy())
-        for _ in range(args.warmup + args.steps):
-            sim2.step(1)
-        e2e_cus = sim2.info()["cell_updates"]
-        d2h = 0
-        for l in range(sim2.info()["finest"] + 1):
-            v = sim2.level(l)
-            n = v.nvalid * v.ncomp
-            if l < len(host_levels) and host_levels[l].numel() == n:
-                out = host_levels[l]
-            else:
-                out = torch.empty(n, dtype=torch.float64).pin_memory()
-            ctx.check(ctx.lib.sh_level_read(ctx.h, v.h, sh.SH_NEW, 1, out.data_ptr()), "read")
-            d2h += n * 8
-        torch.cuda.synchronize()
-        e2e_s = time.perf_counter() - t0
-        e2e_steps = args.warmup + args.steps
-        sim2.close()
-        h2d = state.size * 8
-    else:
-        host_out = torch.empty_like(host_in).pin_memory()
-        e2e_steps = max(3, min(args.steps, 10))
-        s = SINGLE
-        dx = s["L"] / s["N"]
-        for _ in range(e2e_steps):
-            ctx.check(ctx.lib.sh_level_write(ctx.h, lv.h, sh.SH_NEW, 0, host_in.data_ptr()),
-                      "write")
-            lv.advance(sh.RKN4, 0.25 * dx, dx, params=s["params"])
-            ctx.check(ctx.lib.sh_level_read(ctx.h, lv.h, sh.SH_NEW, 0, host_out.data_ptr()),
-                      "read")
-        torch.cuda.synchronize()
-        e2e_s = time.perf_counter() - t0
-        e2e_cus = s["N"] ** 3 * e2e_steps
-        h2d = d2h = state.size * 8 * e2e_steps
-        lv.close()
+    lv2 = sh.Level.periodic(ctx, s["project"], N, s["nghost"])
+    ctx.check(ctx.lib.sh_level_write(ctx.h, lv2.h, sh.SH_NEW, 0, host_in.data_ptr()), "write")
+    lv2.set_time(s["eta0"])
+    for _ in range(s["total_steps"]):
+        lv2.advance(sh.RKN4, dt, dx, params=s["params"])
+    ctx.check(ctx.lib.sh_level_read(ctx.h, lv2.h, sh.SH_NEW, 0, host_out.data_ptr()), "read")
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    lv2.close()
+    e2e = {"value": world * N ** 3 * s["total_steps"] / e2e_s, "unit": METRIC,
+           "h2d_bytes_per_step": state.size * 8 / s["total_steps"],
+           "d2h_bytes_per_step": state.size * 8 / s["total_steps"],
+           "job_steps": s["total_steps"],
+           "note": "level created, initial state uploaded from pinned host memory, 200 RKN4 "
+                   "steps, final state read back to pinned host memory"}
 
-    forms = {}
-    legs = [f for f in args.forms.split(",") if f]
-    if "ensemble" in legs:
-        forms["batched_ensemble"] = run_ensemble_leg(sh, ctx, stream, flush, steps=20,
-                                                     warmup=args.warmup)
-    if "fopt" in legs:
-        forms["fopt_precision"] = run_fopt_leg(sh, ctx, stream, flush, steps=20,
-                                               warmup=args.warmup)
-    if "serve" in legs:
-        forms["serving"] = run_serve_leg(sh, ctx, args.serve_max_n)
-    cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(args.workload)
+    legs = {}
+    want = [f for f in args.legs.split(",") if f]
+    cpu_ok = rank == 0 and not args.no_cpu_baseline
+    if "amr" in want:
+        legs["amr"] = run_amr_leg(sh, ctx, stream, flush, args.steps, args.warmup, peak,
+                                  peak_kind)
+    if "ensemble" in want:
+        legs["batched_ensemble"] = run_ensemble_leg(sh, ctx, stream, flush, steps=20,
+                                                    warmup=args.warmup)
+    if "fopt" in want:
+        legs["fopt_precision"] = run_fopt_leg(sh, ctx, stream, flush, steps=20,
+                                              warmup=args.warmup)
+    if "serve" in want:
+        legs["serving"] = run_serve_leg(sh, ctx, args.serve_max_n)
+    cpu = cpu_baseline_single() if cpu_ok else None
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded Gaussian random field, |k|<=1)",
-            "config": dict(workload_config(args.workload), parallelism=f"replicas x{world}"),
-            "e2e": {"value": world * e2e_cus / e2e_s, "unit": METRIC,
-                    "h2d_bytes_per_step": h2d / e2e_steps, "d2h_bytes_per_step": d2h / e2e_steps},
-            "gpu_launches": launches,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "algorithmic_bytes_per_launch": WORDS_PER_CELL_UPDATE * 8 / 3.0 *
-                         cells_per_launch,
-                         "fp64_pipe_busy_ncu": {"stage0": 0.72, "stage1": 0.63, "final": 0.70},
-                         "kernel": "stage_kernel (fused Rhs + RKN4 stage update)",
-                         "bytes_per_cell_update": WORDS_PER_CELL_UPDATE * 8,
-                         "stage_ms_total": stage_ms, "stage_launches": stage_launches,
-                         "fill_ms_total": fill_ms, "fill_launches": fill_launches,
-                         "other_ms": other},
-            "clocks": clk.summary(),
-            "cell_updates_timed": cus,
+            "config": single_config(), "parallelism": f"replicas x{world}",
+            "e2e": e2e, "gpu_launches": launches,
+            "gpu_launches_per_step": launches / args.steps,
+            "roofline": roof, "clocks": clk.summary(), "cell_updates_timed": cus,
         }
-        if amr_info:
-            line["amr"] = {"finest": amr_info["finest"], "nregrids": amr_info["nregrids"],
-                           "levels_at_end": levels, "host_timers_s": amr_timers}
-        if forms:
-            line["forms"] = forms
         if cpu:
             line["cpu_baseline"] = cpu
+        if legs:
+            line["legs"] = legs
         print(json.dumps(line), flush=True)
     ctx.close()
     if world > 1:

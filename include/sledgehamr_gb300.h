@@ -500,6 +500,13 @@ SH_API int sh_amr_regrid_record(const sh_amr *amr, int q, int *lev, double *time
                                 uint8_t *mask, long long cap_mask, long long *n_mask,
                                 sh_box *new_boxes, int cap_new, int *n_new);
 
+/* ---- diagnostics ---------------------------------------------------------------- */
+/* Measured issue rate of FP64 fused multiply-adds on `device` (thread
+ * instructions per second, all SMs, dependent chains with enough warps to
+ * hide their latency): the peak of the FP64 roofline of the stage kernels.
+ * No counterpart in the reference. */
+SH_API int sh_probe_fp64_fma_rate(int device, double *fma_per_s);
+
 /* ---- convenience --------------------------------------------------------------- */
 /* Evolve a periodic cubic level of N^3 cells (boxes of max_grid cells per
  * side, max_grid <= 0: one box) by nsteps steps; host arrays in canonical

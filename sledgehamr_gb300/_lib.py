@@ -183,6 +183,7 @@ SIGNATURES = {
     "sh_spectrum_bins": (C.c_int, [C.c_int, vp, C.c_int, ip]),
     "sh_index_to_k": (C.c_int, [C.c_int, C.c_int, vp]),
     "sh_gw_spectrum": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, C.c_int, ip]),
+    "sh_probe_fp64_fma_rate": (C.c_int, [C.c_int, dp]),
     "sh_evolve_periodic": (C.c_int, [vp, C.c_int, C.c_int, vp, C.c_int, C.c_int, C.c_int,
                                      C.c_int, C.c_int, C.c_int, vp, vp, vp, C.c_double,
                                      C.c_double, C.c_double, C.c_int, vp, C.c_int, vp, C.c_int,

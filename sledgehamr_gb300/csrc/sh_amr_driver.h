@@ -60,6 +60,7 @@
 #define SH_AMR_DRIVER_H_
 
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <chrono>
 #include <cmath>
@@ -68,6 +69,10 @@
 #include <stdexcept>
 #include <string>
 #include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 namespace shamr {
 
@@ -249,9 +254,42 @@ inline void cluster(const BlockSet &t, IBox bx, double eff, std::vector<IBox> &o
     cluster_impl<false>(t, bx, eff, out);
 }
 
-/* cluster() with the large halves as OpenMP tasks of a team of its own. */
-inline void cluster_parallel(const BlockSet &t, IBox bx, double eff, std::vector<IBox> &out) {
-#pragma omp parallel default(none) shared(t, bx, eff, out)
+/* Host threads for the parallel parts of one regrid.  Hierarchies stepped
+ * on several host threads at once (one per served request) regrid
+ * concurrently; each then takes an equal share of the cores instead of a
+ * full team of its own, and a regrid inside a parallel region takes one. */
+class RegridTeam {
+  public:
+    RegridTeam() : n_(active().fetch_add(1) + 1) {}
+    ~RegridTeam() { active().fetch_sub(1); }
+    RegridTeam(const RegridTeam &) = delete;
+    RegridTeam &operator=(const RegridTeam &) = delete;
+    int threads() const {
+#ifdef _OPENMP
+        if (omp_in_parallel()) return 1;
+        return std::max(1, omp_get_max_threads() / std::max(1, n_));
+#else
+        return 1;
+#endif
+    }
+
+  private:
+    static std::atomic<int> &active() {
+        static std::atomic<int> a{0};
+        return a;
+    }
+    int n_;
+};
+
+/* cluster() with the large halves as OpenMP tasks of a team of its own
+ * (threads: the caller's share of the host cores). */
+inline void cluster_parallel(const BlockSet &t, IBox bx, double eff, std::vector<IBox> &out,
+                             int threads) {
+    if (threads <= 1) {
+        cluster_impl<false>(t, bx, eff, out);
+        return;
+    }
+#pragma omp parallel num_threads(threads) default(none) shared(t, bx, eff, out)
 #pragma omp single
     cluster_impl<true>(t, bx, eff, out);
 }
@@ -412,6 +450,8 @@ inline std::vector<IBox> make_boxes(const std::vector<uint8_t> &tagbits,
                                     double grid_eff, int w) {
     const BlockSet tags{tagbits, nb};
     const BlockSet nest{allowed, nb};
+    const RegridTeam team;
+    const int nthreads = team.threads();
     std::vector<IBox> bb;
     auto nested = [&](const std::vector<IBox> &cl, std::vector<IBox> &out) {
         for (const IBox &x : cl) {
@@ -434,7 +474,7 @@ inline std::vector<IBox> make_boxes(const std::vector<uint8_t> &tagbits,
         const int nw = (nb + w - 1) / w;
         const long long nwin = (long long)nw * nw * nw;
         std::vector<std::vector<IBox>> per(nwin);
-#pragma omp parallel for schedule(dynamic, 8)
+#pragma omp parallel for schedule(dynamic, 8) num_threads(nthreads)
         for (long long q = 0; q < nwin; ++q) {
             const int wx = (int)(q % nw) * w, wy = (int)((q / nw) % nw) * w,
                       wz = (int)(q / ((long long)nw * nw)) * w;
@@ -463,7 +503,7 @@ inline std::vector<IBox> make_boxes(const std::vector<uint8_t> &tagbits,
         return bb;
     }
     std::vector<IBox> cl;
-    cluster_parallel(tags, IBox{{0, 0, 0}, {nb - 1, nb - 1, nb - 1}}, grid_eff, cl);
+    cluster_parallel(tags, IBox{{0, 0, 0}, {nb - 1, nb - 1, nb - 1}}, grid_eff, cl, nthreads);
     nested(cl, bb);
     simplify(bb);
     max_size(bb, w);
@@ -829,7 +869,9 @@ class Driver {
                     for (int j = bx.lo[1] / lb; j <= bx.hi[1] / lb; ++j)
                         for (int i = bx.lo[0] / lb; i <= bx.hi[0] / lb; ++i)
                             cov[((size_t)k * nlb + j) * nlb + i] = 1;
-#pragma omp parallel for schedule(static)
+            const RegridTeam team;
+            const int nthreads = team.threads();
+#pragma omp parallel for schedule(static) num_threads(nthreads)
             for (int bk = 0; bk < nb; ++bk)
                 for (int bj = 0; bj < nb; ++bj)
                     for (int bi = 0; bi < nb; ++bi) {

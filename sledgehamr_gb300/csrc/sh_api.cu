@@ -2166,6 +2166,12 @@ int sh_tag(sh_ctx *ctx, sh_level *L, int use_te, double time, int lev, double dt
         require(nparams_mod >= 0 && nparams_mod <= kMaxComp, "at most 32 modifier parameters");
         require(!use_te || te_crit, "te_crit required with truncation errors");
         require(L->nvalid < (1LL << 31), "tag list indices are 32-bit");
+        if (L->nvalid == 0) { /* nothing to tag (and no empty launch) */
+            if (ntagged) *ntagged = 0;
+            if (counts_out)
+                for (int n = 0; n < 2 + L->ncomp; ++n) counts_out[n] = 0;
+            return;
+        }
         TagArgs a;
         std::memset(&a, 0, sizeof(a));
         a.boxes = L->d_boxes;
@@ -2462,6 +2468,12 @@ extern "C" int sh_tag_static(sh_ctx *ctx, sh_level *L, int use_te, double time, 
         require(nparams_tag >= 0 && nparams_tag <= kMaxParams, "at most 32 tag parameters");
         require(nparams_mod >= 0 && nparams_mod <= kMaxComp, "at most 32 modifier parameters");
         require(!use_te || te_crit, "te_crit required with truncation errors");
+        if (L->nvalid == 0) { /* nothing to tag (and no empty launch) */
+            if (ntagged) *ntagged = 0;
+            if (counts_out)
+                for (int n = 0; n < 2 + L->ncomp; ++n) counts_out[n] = 0;
+            return;
+        }
         unsigned char *base = tag_static_base(ctx);
         TagArgs a;
         std::memset(&a, 0, sizeof(a));

@@ -32,6 +32,7 @@
 #ifndef SH_OUTPUT_H_
 #define SH_OUTPUT_H_
 
+#include <new>
 #include <string>
 #include <vector>
 
@@ -105,8 +106,12 @@ bool level_datasets_t(h5::Writer &w, const HostLevel &L, const std::string &iden
      * then added in the reference's order */
     const long long nset = (long long)L.nbox * L.ncomp;
     std::vector<std::vector<unsigned char>> bytes(nset);
+    /* an exception must not leave the OpenMP region (std::terminate): an
+     * allocation failure on a host thread is recorded and rethrown after it,
+     * so the entry point still returns SH_ERR_NOMEM */
+    bool out_of_memory = false;
 #pragma omp parallel for schedule(dynamic, 1)
-    for (long long q = 0; q < nset; ++q) {
+    for (long long q = 0; q < nset; ++q) try {
         const int b = (int)(q / L.ncomp), f = (int)(q % L.ncomp);
         const sh_box &bx = L.boxes[b];
         const int ext[3] = {bx.hi[0] - bx.lo[0] + 1, bx.hi[1] - bx.lo[1] + 1,
@@ -132,7 +137,11 @@ bool level_datasets_t(h5::Writer &w, const HostLevel &L, const std::string &iden
                 }
         bytes[q].resize(sizeof(T) * (size_t)len);
         if (len) std::memcpy(bytes[q].data(), o.data(), bytes[q].size());
+    } catch (const std::bad_alloc &) {
+#pragma omp atomic write
+        out_of_memory = true;
     }
+    if (out_of_memory) throw std::bad_alloc();
     for (long long q = 0; q < nset; ++q) {
         const int b = (int)(q / L.ncomp), f = (int)(q % L.ncomp);
         const std::string name =

@@ -7,6 +7,12 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
+# The sledgehamr source tree (only where it is present, for the tests that
+# pin the oracle to the reference's own code): $SLEDGEHAMR_REF_ROOT, else a
+# directory named "reference" beside this repository.
+REF_ROOT = os.environ.get("SLEDGEHAMR_REF_ROOT") or os.path.join(os.path.dirname(ROOT),
+                                                                 "reference")
+
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")

@@ -53,7 +53,7 @@ int main() {
                     const IBox all{{0, 0, 0}, {nb - 1, nb - 1, nb - 1}};
                     std::vector<IBox> a, b;
                     shamr::cluster(t, all, eff, a);
-                    shamr::cluster_parallel(t, all, eff, b);
+                    shamr::cluster_parallel(t, all, eff, b, 8);
                     bool same = a.size() == b.size();
                     for (size_t q = 0; same && q < a.size(); ++q)
                         for (int d = 0; d < 3; ++d)

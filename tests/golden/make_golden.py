@@ -184,7 +184,8 @@ if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
     only = [x for a in sys.argv[1:] if a.startswith("--only=")
             for x in a.split("=", 1)[1].split(",")]
-    ref_root = args[0] if args else "/root/reference"
+    ref_root = args[0] if args else (os.environ.get("SLEDGEHAMR_REF_ROOT") or
+                                     os.path.join(os.path.dirname(ROOT), "reference"))
     subprocess.run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh"), ref_root], check=True)
     if not only or "spectra" in only:
         spectra_fixtures(ref_root)

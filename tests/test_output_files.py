@@ -18,8 +18,9 @@ import pytest
 
 from oracle import output_oracle as oo
 from tests import hdf5_read
+from tests.conftest import REF_ROOT
 
-REF_DATA = "/root/reference/data/spectra_ks.hdf5"
+REF_DATA = os.path.join(REF_ROOT, "data", "spectra_ks.hdf5")
 
 
 def _sh():

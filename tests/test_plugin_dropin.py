@@ -10,9 +10,9 @@ import subprocess
 import numpy as np
 import pytest
 
-from tests.conftest import ROOT
+from tests.conftest import REF_ROOT, ROOT
 
-REF = "/root/reference"
+REF = REF_ROOT
 pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "projects")),
                                 reason="sledgehamr sources not present")
 

@@ -30,6 +30,23 @@ def _call(ctx, fn, lv, use_te, te_crit, dt, dx):
     return mask, counts, lst[: nt.value].copy()
 
 
+def _device_memory():
+    """(free bytes of the device, bytes in use in its default memory pool),
+    read through the CUDA driver: a cudaMalloc lowers the first, a
+    cudaMallocAsync from the pool raises the second."""
+    cu = C.CDLL("libcuda.so.1")
+    free, total = C.c_size_t(), C.c_size_t()
+    assert cu.cuMemGetInfo_v2(C.byref(free), C.byref(total)) == 0
+    dev = C.c_int()
+    assert cu.cuCtxGetDevice(C.byref(dev)) == 0
+    pool = C.c_void_p()
+    assert cu.cuDeviceGetDefaultMemPool(C.byref(pool), dev) == 0
+    used = C.c_uint64()
+    CU_MEMPOOL_ATTR_USED_MEM_CURRENT = 7
+    assert cu.cuMemPoolGetAttribute(pool, CU_MEMPOOL_ATTR_USED_MEM_CURRENT, C.byref(used)) == 0
+    return free.value, used.value
+
+
 def test_tag_static_matches_tag_on_consecutive_calls(ctx):
     lib = _lib.load()
     g = golden("ref_tag")
@@ -39,9 +56,17 @@ def test_tag_static_matches_tag_on_consecutive_calls(ctx):
     lv.write(st)
     lv.fill_patch()
     lv.write(te, which=sh.SH_OLD)
-    for use_te in (True, False):  # two calls in a row with different results
+    for q, use_te in enumerate((True, False)):  # two calls in a row, different results
         want = _call(ctx, lib.sh_tag, lv, use_te, crit, dt, dx)
+        ctx.synchronize()
+        before = _device_memory()
         got = _call(ctx, lib.sh_tag_static, lv, use_te, crit, dt, dx)
+        ctx.synchronize()
+        after = _device_memory()
+        if q > 0:
+            # the first call may load the library's device code lazily; from
+            # the second on, the call takes no device memory of any kind
+            assert after == before, (before, after)
         assert want[0].sum() > 0
         for w, h in zip(want, got):
             assert np.array_equal(w, h)
