@@ -492,6 +492,15 @@ SH_API int sh_amr_set_timer_sync(sh_amr *a, int on);
 SH_API int sh_amr_timer(const sh_amr *a, int q, const char **name, double *seconds,
                         long long *calls);
 /* Level lev of the hierarchy (owned by it; valid until the next step). */
+/* Operation trace of the time stepper (TimeStepper::Advance,
+ * SynchronizeLevels, ScheduleRegrid, DoRegrid, CreateShadowLevel;
+ * source/time_stepper.cpp:90-397, sledgehamr.cpp:234-251): with tracing on,
+ * every operation appends one line "<op> <level> <time>" (op one of advance,
+ * schedule, shadow, average_down, truncation_errors, regrid; times printed
+ * exactly).  sh_amr_trace copies the lines so far (NUL-terminated) into buf
+ * of cap bytes and stores their length; buf NULL: length only. */
+SH_API int sh_amr_set_trace(sh_amr *amr, int on);
+SH_API int sh_amr_trace(const sh_amr *amr, char *buf, long long cap, long long *len);
 SH_API int sh_amr_level(const sh_amr *amr, int lev, sh_level **level);
 /* Regrid record q (with record_regrids): the tagged level and time, its
  * boxes, its tag mask (boxes layout) and the new boxes of the level above. */

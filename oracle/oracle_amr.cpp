@@ -269,6 +269,8 @@ struct AmrBase {
     virtual const MF *level(int lev, int which) const = 0;
     virtual const std::vector<shamr::IBox> &boxes(int lev) const = 0;
     virtual void set_tag_params(const double *pt, int nt, const double *pm, int nm) = 0;
+    virtual void set_trace(bool on) = 0;
+    virtual const std::vector<std::string> &trace() const = 0;
 };
 
 template <class P>
@@ -321,6 +323,8 @@ struct Amr : AmrBase {
         return which == 0 ? &drv->levels[lev]->nw : &drv->levels[lev]->od;
     }
     const std::vector<shamr::IBox> &boxes(int lev) const override { return drv->boxes[lev]; }
+    void set_trace(bool on) override { drv->record_trace = on; }
+    const std::vector<std::string> &trace() const override { return drv->trace; }
     void set_tag_params(const double *pt, int nt, const double *pm, int nm) override {
         for (int q = 0; q < nt; ++q) backend.cfg.params_tag[q] = pt[q];
         for (int q = 0; q < nm; ++q) backend.cfg.params_mod[q] = pm[q];
@@ -395,6 +399,22 @@ int orc_make_boxes(const unsigned char *tags, const unsigned char *allowed, int 
             out[6 * q + 3 + d] = b[q].hi[d];
         }
     return (int)b.size();
+}
+
+/* The time stepper's operation trace (shamr::Driver::trace): record_trace
+ * on or off, and the events so far as one string, newline-separated, into
+ * buf (capacity cap); returns the string's length (-1 if cap is too small). */
+int orc_amr_set_trace(void *h, int on) {
+    ((AmrBase *)h)->set_trace(on != 0);
+    return 0;
+}
+long long orc_amr_trace(void *h, char *buf, long long cap) {
+    std::string all;
+    for (const std::string &e : ((AmrBase *)h)->trace()) all += e + "\n";
+    if (!buf) return (long long)all.size();
+    if ((long long)all.size() + 1 > cap) return -1;
+    std::memcpy(buf, all.c_str(), all.size() + 1);
+    return (long long)all.size();
 }
 
 /* Boxes (6 ints each) of level lev; returns their number. */

@@ -407,6 +407,15 @@ def amr_config(project: str, **kw) -> ShAmrConfig:
     return cfg
 
 
+def parse_trace(text: str) -> list[tuple[str, int, float]]:
+    """Lines "<op> <level> <time>" of an AMR operation trace."""
+    out = []
+    for line in text.splitlines():
+        op, lev, t = line.split()
+        out.append((op, int(lev), float(t)))
+    return out
+
+
 def _boxes_of(arr, n):
     return [((arr[q].lo[0], arr[q].lo[1], arr[q].lo[2]), (arr[q].hi[0], arr[q].hi[1], arr[q].hi[2]))
             for q in range(n)]
@@ -493,6 +502,18 @@ class Amr:
             out[name.value.decode()] = (sec.value, calls.value)
             q += 1
         return out
+
+    def set_trace(self, on: bool = True):
+        self.ctx.check(self.ctx.lib.sh_amr_set_trace(self.h, int(on)), "sh_amr_set_trace")
+
+    def trace(self) -> list[tuple[str, int, float]]:
+        """The time stepper's operations so far: (op, level, time)."""
+        n = C.c_longlong()
+        self.ctx.check(self.ctx.lib.sh_amr_trace(self.h, None, 0, C.byref(n)), "sh_amr_trace")
+        buf = C.create_string_buffer(n.value + 1)
+        self.ctx.check(self.ctx.lib.sh_amr_trace(self.h, buf, n.value + 1, C.byref(n)),
+                       "sh_amr_trace")
+        return parse_trace(buf.value.decode())
 
     def level(self, lev: int) -> LevelView:
         h = C.c_void_p()

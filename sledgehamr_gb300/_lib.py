@@ -158,6 +158,8 @@ SIGNATURES = {
     "sh_amr_set_timer_sync": (C.c_int, [vp, C.c_int]),
     "sh_amr_timer": (C.c_int, [vp, C.c_int, C.POINTER(C.c_char_p), dp, llp]),
     "sh_amr_level": (C.c_int, [vp, C.c_int, C.POINTER(vp)]),
+    "sh_amr_set_trace": (C.c_int, [vp, C.c_int]),
+    "sh_amr_trace": (C.c_int, [vp, C.c_char_p, C.c_longlong, llp]),
     "sh_amr_regrid_record": (C.c_int, [vp, C.c_int, ip, dp, C.POINTER(ShBox), C.c_int, ip, vp,
                                        C.c_longlong, llp, C.POINTER(ShBox), C.c_int, ip]),
     "sh_level_write": (C.c_int, [vp, vp, C.c_int, C.c_int, vp]),

@@ -296,6 +296,23 @@ int sh_amr_timer(const sh_amr *a, int q, const char **name, double *seconds, lon
     return SH_OK;
 }
 
+int sh_amr_set_trace(sh_amr *a, int on) {
+    if (!a) return SH_ERR_ARG;
+    a->driver->record_trace = on != 0;
+    return SH_OK;
+}
+
+int sh_amr_trace(const sh_amr *a, char *buf, long long cap, long long *len) {
+    if (!a) return SH_ERR_ARG;
+    std::string all;
+    for (const std::string &e : a->driver->trace) all += e + "\n";
+    if (len) *len = (long long)all.size();
+    if (!buf) return SH_OK;
+    if ((long long)all.size() + 1 > cap) return SH_ERR_ARG;
+    std::memcpy(buf, all.c_str(), all.size() + 1);
+    return SH_OK;
+}
+
 int sh_amr_level(const sh_amr *a, int lev, sh_level **level) {
     if (!a || !level || lev < 0 || lev > a->driver->finest) return SH_ERR_ARG;
     *level = a->driver->levels[lev]->L;

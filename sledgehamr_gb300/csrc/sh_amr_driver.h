@@ -65,6 +65,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <functional>
 #include <stdexcept>
 #include <string>
@@ -592,7 +593,12 @@ class Driver {
     std::vector<RegridRecord> regrids;
     bool record_regrids = false;
     long long cell_updates = 0;
-    std::vector<std::string> trace; /* advance/sync/regrid events */
+    /* With record_trace, the time stepper's operations in order, one string
+     * "<op> <level> <time>" each: advance (level, time before the step),
+     * schedule (level, regrid time), shadow (-1, shadow time after its
+     * step), average_down (coarse level, its time), truncation_errors
+     * (level, time), regrid (base level, time). */
+    std::vector<std::string> trace;
     bool record_trace = false;
 
     /* Host wall-clock time spent in the backend operations, by phase.  With
@@ -645,8 +651,12 @@ class Driver {
     std::vector<Sched> schedule;
     std::vector<double> regrid_dt, last_regrid_time;
 
-    void note(const std::string &s) {
-        if (record_trace) trace.push_back(s);
+    /* One trace event: "<op> <level> <time>", the time printed exactly. */
+    void note(const char *op, int lev, double t) {
+        if (!record_trace) return;
+        char buf[96];
+        std::snprintf(buf, sizeof(buf), "%s %d %.17g", op, lev, t);
+        trace.push_back(buf);
     }
 
     /* ---- RegridScheduler ---- */
@@ -690,7 +700,7 @@ class Driver {
     void advance(int lev) {
         if (shadow_hierarchy) schedule_regrid_if_needed(lev);
         else no_shadow_regrid(lev);
-        note("advance " + std::to_string(lev) + " t=" + std::to_string(tnew(lev)));
+        note("advance", lev, tnew(lev));
         {
             Clock ck(this, kTAdvance);
             b.advance(lev, levels[lev], lev > 0 ? &levels[lev - 1] : nullptr, dt[lev], dx[lev],
@@ -714,13 +724,13 @@ class Driver {
         const bool te = need_te(lev, tnew(lev));
         if (lev < finest) {
             if (!(shadow_hierarchy && te)) {
-                note("average_down " + std::to_string(lev + 1) + "->" + std::to_string(lev));
+                note("average_down", lev, tnew(lev));
                 b.average_down(levels[lev + 1], kNew, levels[lev], kNew);
                 te_valid[lev + 1] = false;
             }
         }
         if (lev >= 1 - (shadow_hierarchy ? 1 : 0) && te) {
-            note("truncation_errors " + std::to_string(lev));
+            note("truncation_errors", lev, tnew(lev));
             if (lev == 0) {
                 const double ts = b.time(shadow, kNew);
                 if (!(std::fabs(ts - tnew(0)) < tnew(0) * 1e-8))
@@ -748,7 +758,7 @@ class Driver {
         if (next <= last_regrid_time[lev] + regrid_dt[lev]) return;
         if (lev == 0 && b.time(levels[0], kOld) == -DBL_MAX) return;
         schedule_regrid(lev, time + dt[lev]);
-        note("schedule " + std::to_string(lev) + " at " + std::to_string(time + dt[lev]));
+        note("schedule", lev, time + dt[lev]);
         if (lev == 0) create_shadow_level();
     }
 
@@ -771,7 +781,7 @@ class Driver {
         b.average_down(levels[0], kOld, shadow, kOld);
         b.set_time(shadow, kOld, t_old, 0);
         b.advance(-1, shadow, nullptr, 2. * dt[0], 2. * dx[0], true);
-        note("shadow advanced to " + std::to_string(b.time(shadow, kNew)));
+        note("shadow", -1, b.time(shadow, kNew));
     }
 
     void do_regrid_if_scheduled(int lev) {
@@ -792,7 +802,7 @@ class Driver {
 
     /* TimeStepper::DoRegrid with the global regrid path. */
     void do_regrid(int lev, double time) {
-        note("regrid " + std::to_string(lev) + " at " + std::to_string(time));
+        note("regrid", lev, time);
         regrid(lev, time);
         for (int l = lev; l <= finest; ++l) last_regrid_time[l] = time;
     }

@@ -192,6 +192,25 @@ class OracleAmr:
         self.lib.orc_amr_info(self.h, C.byref(f), C.byref(cu), C.byref(nr))
         return {"finest": f.value, "cell_updates": cu.value, "nregrids": nr.value}
 
+    def set_trace(self, on=True):
+        self.lib.orc_amr_set_trace.restype = C.c_int
+        self.lib.orc_amr_set_trace(self.h, int(on))
+
+    def trace(self):
+        """The time stepper's operations so far: (op, level, time)."""
+        f = self.lib.orc_amr_trace
+        f.restype = C.c_longlong
+        f.argtypes = [C.c_void_p, C.c_char_p, C.c_longlong]
+        n = f(self.h, None, 0)
+        buf = C.create_string_buffer(n + 1)
+        if f(self.h, buf, n + 1) < 0:
+            raise RuntimeError("orc_amr_trace")
+        out = []
+        for line in buf.value.decode().splitlines():
+            op, lev, t = line.split()
+            out.append((op, int(lev), float(t)))
+        return out
+
     def boxes(self, lev):
         out = np.empty(6 * 100000, dtype=np.int32)
         n = self.lib.orc_amr_boxes(self.h, lev, _p(out), 100000)

@@ -134,3 +134,17 @@ def test_fopt_gw_amr_with_tag_params_matches_oracle(ctx, norm0):
     assert g.info()["finest"] >= 1
     g.close()
     o.close()
+
+
+def test_amr_operation_order_equals_known_answer(ctx):
+    """The GPU hierarchy's time stepper performs sledgehamr's operations in
+    the order written out by hand from source/time_stepper.cpp
+    (tests/test_amr_sequence.py)."""
+    from tests.test_amr_sequence import KAT
+    g = sh.Amr(ctx, config(te_crit=[0.0] * 4, regrid_dt=0.0, string_width_threshold=0.0),
+               level0(0))
+    g.set_trace(True)
+    g.step(4)
+    assert g.info()["finest"] == 2
+    assert g.trace() == KAT
+    g.close()
