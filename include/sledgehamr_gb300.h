@@ -279,8 +279,36 @@ SH_API int sh_level_add_bubbles(sh_ctx *ctx, sh_level *L, int which, int comp_ph
 #define SH_REDUCE_MAX 2
 #define SH_REDUCE_SUM 3
 #define SH_REDUCE_SUM_SQ 4
+/* SH_REDUCE_COUNT_NONFINITE: the number of NaN or infinite values of comp
+ * (no counterpart in the reference; see sh_level_check_finite).
+ * SH_REDUCE_SUM_MODULUS: the sum over the cells of sqrt(comp^2 +
+ * (comp+1)^2), the radial mode r = |Psi| of NextToMinimalExample::WriteAvg
+ * (projects/NextToMinimalExample/NextToMinimalExample.cpp:10-49), whose
+ * <r> is this sum over the number of cells. */
+#define SH_REDUCE_COUNT_NONFINITE 5
+#define SH_REDUCE_SUM_MODULUS 6
 SH_API int sh_level_reduce(sh_ctx *ctx, const sh_level *level, int which, int op, int comp,
                            double *out);
+/* Every component of a time level checked for NaN and infinite values on
+ * the valid cells: SH_OK, or SH_ERR_NONFINITE with *nonfinite (may be NULL)
+ * the number of such values and the first affected component named in
+ * sh_ctx_last_error.  The reference has no such check (a non-finite field
+ * runs on silently). */
+SH_API int sh_level_check_finite(sh_ctx *ctx, const sh_level *level, int which,
+                                 long long *nonfinite);
+/* Cosmology::GetStringTags (projects/AxionStrings/cosmology.cpp:114-142):
+ * the number of valid cells of time level NEW whose project
+ * TagCellForRefinement<true> hook is true (for the axion projects: cells
+ * whose plaquettes are pierced by a string) at the given time, level index,
+ * dt and dx.  Ghost cells must be current (+1 neighbours are read). */
+SH_API int sh_level_string_tags(sh_ctx *ctx, sh_level *level, double time, int lev, double dt,
+                                double dx, const double *params_tag, int nparams_tag,
+                                long long *ntags);
+/* Cosmology::Xi (cosmology.cpp:89-108, cosmology.h:77-97): the string
+ * length parameter xi from a string-tag count on a level of spacing dx in a
+ * box of comoving size L at conformal time eta (T1 = 5.4954174414835757e17,
+ * m_pl = 1.22e19, g_* = 106).  Host arithmetic only. */
+SH_API int sh_string_xi(long long string_tags, double dx, double L, double eta, double *xi);
 
 /* ---- level synchronisation ------------------------------------------------- */
 /* crse(which_c) = 2x2x2 average of fine(which_f) on every coarse cell
@@ -454,6 +482,11 @@ typedef struct sh_amr_config {
      * does with norm0 (FirstOrderPhaseTransition.cpp:133-157); 0: params_mod
      * as given */
     int params_mod_norm0;
+    /* 1: after every coarse step, every level's new time level is checked
+     * for NaN and infinite values (sh_level_check_finite); sh_amr_step then
+     * stops with SH_ERR_NONFINITE naming the level and component.  No
+     * counterpart in the reference. */
+    int check_finite;
 } sh_amr_config;
 /* New-grid generation from the buffered tags (at blocking-factor
  * resolution): Berger-Rigoutsos clustering to efficiency grid_eff, then

@@ -35,6 +35,8 @@ REDUCE_MIN = 1
 REDUCE_MAX = 2
 REDUCE_SUM = 3
 REDUCE_SUM_SQ = 4
+REDUCE_COUNT_NONFINITE = 5
+REDUCE_SUM_MODULUS = 6  # sum of sqrt(c^2 + (c+1)^2): the radial mode |Psi|
 
 # project ids compiled into the library
 PROJECTS = ("AxionStrings", "MinimalExample", "NextToMinimalExample",
@@ -263,6 +265,19 @@ class Level:
         cells (fixed FP64 order, reproducible bit for bit)."""
         return _reduce(self.ctx, self.h, which, op, comp)
 
+    def check_finite(self, which: int = SH_NEW) -> int:
+        """sh_level_check_finite: 0, else raises ShError(SH_ERR_NONFINITE)."""
+        return _check_finite(self.ctx, self.h, which)
+
+    def string_tags(self, time: float, lev: int, dt: float, dx: float, params_tag=()) -> int:
+        """Cosmology::GetStringTags: cells whose project tag hook is true."""
+        return _string_tags(self.ctx, self.h, time, lev, dt, dx, params_tag)
+
+    def mean_radial_mode(self, comp: int = 0, which: int = SH_NEW) -> float:
+        """<r> = mean sqrt(Psi1^2 + Psi2^2) over the valid cells
+        (NextToMinimalExample::WriteAvg), Psi1 = comp, Psi2 = comp + 1."""
+        return self.reduce(REDUCE_SUM_MODULUS, comp, which) / self.nvalid
+
     def read(self, which: int = SH_NEW, layout: int = 0) -> np.ndarray:
         out = np.empty(self.nvalid * self.ncomp, dtype=np.float64)
         self.ctx.check(self.ctx.lib.sh_level_read(self.ctx.h, self.h, which, layout, _ptr(out)),
@@ -372,6 +387,31 @@ def average_down_te(ctx: Context, fine: Level, crse: Level):
     ctx.check(ctx.lib.sh_average_down_te(ctx.h, fine.h, crse.h), "sh_average_down_te")
 
 
+def _check_finite(ctx: Context, h, which: int) -> int:
+    n = C.c_longlong()
+    ctx.check(ctx.lib.sh_level_check_finite(ctx.h, h, which, C.byref(n)), "sh_level_check_finite")
+    return n.value
+
+
+def _string_tags(ctx: Context, h, time, lev, dt, dx, params_tag=()) -> int:
+    n = C.c_longlong()
+    pt = _f64(list(params_tag) or [0.0])
+    ctx.check(ctx.lib.sh_level_string_tags(ctx.h, h, float(time), int(lev), float(dt), float(dx),
+                                           _ptr(pt), len(params_tag), C.byref(n)),
+              "sh_level_string_tags")
+    return n.value
+
+
+def string_xi(string_tags: int, dx: float, L: float, eta: float) -> float:
+    """Cosmology::Xi: string length parameter from a string-tag count."""
+    lib = _lib.load()
+    out = C.c_double()
+    rc = lib.sh_string_xi(int(string_tags), float(dx), float(L), float(eta), C.byref(out))
+    if rc != 0:
+        raise ShError(rc, "sh_string_xi")
+    return out.value
+
+
 def _reduce(ctx: Context, h, which: int, op: int, comp: int) -> float:
     out = C.c_double()
     ctx.check(ctx.lib.sh_level_reduce(ctx.h, h, which, op, comp, C.byref(out)), "sh_level_reduce")
@@ -448,11 +488,28 @@ class LevelView:
                     comp_phi: int = 0, comp_dphi: int = 1, which: int = SH_NEW):
         Level.add_bubbles(self, centres, profile, inv_dx, Lcut, dx, comp_phi, comp_dphi, which)
 
+    def check_finite(self, which: int = SH_NEW) -> int:
+        return _check_finite(self.ctx, self.h, which)
+
+    def string_tags(self, time: float, lev: int, dt: float, dx: float, params_tag=()) -> int:
+        return _string_tags(self.ctx, self.h, time, lev, dt, dx, params_tag)
+
+    def mean_radial_mode(self, comp: int = 0, which: int = SH_NEW) -> float:
+        return self.reduce(REDUCE_SUM_MODULUS, comp, which) / self.nvalid
+
     def read(self, which: int = SH_NEW) -> np.ndarray:
         out = np.empty(self.nvalid * self.ncomp, dtype=np.float64)
         self.ctx.check(self.ctx.lib.sh_level_read(self.ctx.h, self.h, which, 1, _ptr(out)),
                        "sh_level_read")
         return out
+
+    def write(self, data: np.ndarray, which: int = SH_NEW):
+        """Valid cells in the boxes layout (as read returns them)."""
+        a = _f64(data)
+        if a.size != self.nvalid * self.ncomp:
+            raise ValueError("data size does not match the level")
+        self.ctx.check(self.ctx.lib.sh_level_write(self.ctx.h, self.h, which, 1, _ptr(a)),
+                       "sh_level_write")
 
     def time(self, which: int = SH_NEW):
         t, s = C.c_double(), C.c_int()

@@ -62,7 +62,8 @@ class ShAmrConfig(C.Structure):
                 ("gw_params", C.c_double * 16), ("ngw", C.c_int), ("clustering", C.c_int),
                 ("grid_eff", C.c_double), ("params_tag", C.c_double * 32),
                 ("nparams_tag", C.c_int), ("params_mod", C.c_double * 32),
-                ("nparams_mod", C.c_int), ("params_mod_norm0", C.c_int)]
+                ("nparams_mod", C.c_int), ("params_mod_norm0", C.c_int),
+                ("check_finite", C.c_int)]
 
 
 class ShRequest(C.Structure):
@@ -186,6 +187,10 @@ SIGNATURES = {
     "sh_index_to_k": (C.c_int, [C.c_int, C.c_int, vp]),
     "sh_gw_spectrum": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, C.c_int, ip]),
     "sh_probe_fp64_fma_rate": (C.c_int, [C.c_int, dp]),
+    "sh_level_check_finite": (C.c_int, [vp, vp, C.c_int, llp]),
+    "sh_level_string_tags": (C.c_int, [vp, vp, C.c_double, C.c_int, C.c_double, C.c_double, vp,
+                                       C.c_int, llp]),
+    "sh_string_xi": (C.c_int, [C.c_longlong, C.c_double, C.c_double, C.c_double, dp]),
     "sh_evolve_periodic": (C.c_int, [vp, C.c_int, C.c_int, vp, C.c_int, C.c_int, C.c_int,
                                      C.c_int, C.c_int, C.c_int, vp, vp, vp, C.c_double,
                                      C.c_double, C.c_double, C.c_int, vp, C.c_int, vp, C.c_int,

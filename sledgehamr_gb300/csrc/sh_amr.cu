@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "sh_amr_driver.h"
+#include "sh_internal.h"
 #include "sledgehamr_gb300.h"
 
 namespace {
@@ -178,11 +179,13 @@ int amr_guard(sh_ctx *ctx, F &&f) {
         f();
         return SH_OK;
     } catch (const ShFail &e) {
+        sh::set_ctx_error(ctx, e.what());
         return e.code;
     } catch (const std::bad_alloc &) {
+        sh::set_ctx_error(ctx, "host allocation failed");
         return SH_ERR_NOMEM;
     } catch (const std::exception &e) {
-        (void)e;
+        sh::set_ctx_error(ctx, e.what());
         return SH_ERR_ARG;
     }
 }
@@ -269,7 +272,17 @@ int sh_amr_destroy(sh_ctx *ctx, sh_amr *a) {
 int sh_amr_step(sh_ctx *ctx, sh_amr *a, int n) {
     if (!ctx || !a || n < 0) return SH_ERR_ARG;
     return amr_guard(ctx, [&] {
-        for (int q = 0; q < n; ++q) a->driver->step();
+        for (int q = 0; q < n; ++q) {
+            a->driver->step();
+            if (!a->backend.cfg.check_finite) continue;
+            for (int l = 0; l <= a->driver->finest; ++l) {
+                long long bad = 0;
+                const int rc = sh_level_check_finite(ctx, a->driver->levels[l]->L, SH_NEW, &bad);
+                if (rc != SH_OK)
+                    throw ShFail(rc, "level " + std::to_string(l) + ": " +
+                                         sh_ctx_last_error(ctx));
+            }
+        }
     });
 }
 

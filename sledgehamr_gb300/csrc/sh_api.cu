@@ -709,9 +709,12 @@ __device__ __forceinline__ double reduce_identity(int op) {
     if (op == SH_REDUCE_MAX) return __longlong_as_double((long long)0xFFF0000000000000ull); /* -inf */
     return 0.;
 }
-__device__ __forceinline__ double reduce_value(int op, double v) {
+/* v: the cell's value of comp; w: of comp + 1 (SH_REDUCE_SUM_MODULUS) */
+__device__ __forceinline__ double reduce_value(int op, double v, double w) {
     if (op == SH_REDUCE_MAX_ABS) return fabs(v);
     if (op == SH_REDUCE_SUM_SQ) return v * v;
+    if (op == SH_REDUCE_COUNT_NONFINITE) return isfinite(v) ? 0. : 1.;
+    if (op == SH_REDUCE_SUM_MODULUS) return sqrt(v * v + w * w);
     return v;
 }
 __device__ __forceinline__ double reduce_combine(int op, double a, double b) {
@@ -740,11 +743,13 @@ __global__ void __launch_bounds__(kReduceThreads)
     const double *base = buf + b.off * ncomp + (long long)comp * b.gvol +
                          (b.lo[0] - b.glo[0]) + (b.lo[1] - b.glo[1]) * gx +
                          (b.lo[2] - b.glo[2]) * gxy;
+    const double *base2 = op == SH_REDUCE_SUM_MODULUS ? base + b.gvol : base;
     double acc = reduce_identity(op);
     for (int t = threadIdx.x; t < n; t += kReduceThreads) {
         const int i = t % nx, r = t / nx;
         const int j = r % ny, k = r / ny;
-        acc = reduce_combine(op, acc, reduce_value(op, base[i + j * gx + k * gxy]));
+        const long long e = i + j * gx + k * gxy;
+        acc = reduce_combine(op, acc, reduce_value(op, base[e], base2[e]));
     }
     const double v = reduce_block(op, acc);
     if (threadIdx.x == 0) partial[blockIdx.x] = v;
@@ -1513,6 +1518,12 @@ void average_down_impl(sh_ctx *ctx, const sh_level *F, const double *fine, const
 
 } // namespace
 
+namespace sh {
+void set_ctx_error(::sh_ctx *ctx, const std::string &msg) {
+    if (ctx) ctx->err = msg;
+}
+} // namespace sh
+
 /* ====================================================================== */
 extern "C" {
 
@@ -2116,8 +2127,9 @@ int sh_projection(sh_ctx *ctx, const sh_level *const *levels, int nlev, int fn, 
 
 int sh_level_reduce(sh_ctx *ctx, const sh_level *L, int which, int op, int comp, double *out) {
     if (!ctx || !L || !out || (which != SH_NEW && which != SH_OLD)) return SH_ERR_ARG;
-    if (op < SH_REDUCE_MAX_ABS || op > SH_REDUCE_SUM_SQ) return SH_ERR_ARG;
+    if (op < SH_REDUCE_MAX_ABS || op > SH_REDUCE_SUM_MODULUS) return SH_ERR_ARG;
     if (comp < 0 || comp >= L->ncomp) return SH_ERR_ARG;
+    if (op == SH_REDUCE_SUM_MODULUS && comp + 1 >= L->ncomp) return SH_ERR_ARG;
     return guarded(ctx, [&] {
         set_device(ctx);
         const int nbox = (int)L->boxes.size();
@@ -2131,6 +2143,97 @@ int sh_level_reduce(sh_ctx *ctx, const sh_level *L, int which, int op, int comp,
            "reduce download");
         ck(cudaStreamSynchronize(ctx->stream), "reduce");
     });
+}
+
+int sh_level_check_finite(sh_ctx *ctx, const sh_level *L, int which, long long *nonfinite) {
+    if (nonfinite) *nonfinite = 0;
+    if (!ctx || !L || (which != SH_NEW && which != SH_OLD)) return SH_ERR_ARG;
+    std::vector<double> counts(L->ncomp, 0.);
+    int rc = guarded(ctx, [&] {
+        set_device(ctx);
+        const int nbox = (int)L->boxes.size();
+        double *d = (double *)ctx_scratch(ctx, ((size_t)nbox + L->ncomp) * sizeof(double));
+        for (int c = 0; c < L->ncomp; ++c) {
+            reduce_boxes_kernel<<<nbox, kReduceThreads, 0, ctx->stream>>>(
+                L->d_boxes, L->buf[which], L->ncomp, c, SH_REDUCE_COUNT_NONFINITE, d + L->ncomp);
+            reduce_final_kernel<<<1, kReduceThreads, 0, ctx->stream>>>(
+                d + L->ncomp, nbox, SH_REDUCE_COUNT_NONFINITE, d + c);
+            ctx->launches += 2;
+        }
+        ck(cudaGetLastError(), "finite check launch");
+        ck(cudaMemcpyAsync(counts.data(), d, L->ncomp * sizeof(double), cudaMemcpyDeviceToHost,
+                           ctx->stream),
+           "finite check download");
+        ck(cudaStreamSynchronize(ctx->stream), "finite check");
+    });
+    if (rc != SH_OK) return rc;
+    long long total = 0;
+    int first = -1;
+    for (int c = 0; c < L->ncomp; ++c) {
+        total += (long long)counts[c];
+        if (counts[c] > 0 && first < 0) first = c;
+    }
+    if (nonfinite) *nonfinite = total;
+    if (total == 0) return SH_OK;
+    const char *name = L->ops->field_name ? L->ops->field_name(first) : nullptr;
+    ctx->err = std::to_string(total) + " non-finite values, the first in component " +
+               std::to_string(first) + (name ? std::string(" (") + name + ")" : std::string());
+    return SH_ERR_NONFINITE;
+}
+
+int sh_level_string_tags(sh_ctx *ctx, sh_level *L, double time, int lev, double dt, double dx,
+                         const double *params_tag, int nparams_tag, long long *ntags) {
+    if (!ctx || !L || !ntags) return SH_ERR_ARG;
+    return guarded(ctx, [&] {
+        set_device(ctx);
+        require(L->nghost >= 1, "string tags read the +1 neighbours: nghost >= 1");
+        require(nparams_tag >= 0 && nparams_tag <= kMaxParams, "at most 32 tag parameters");
+        require(nparams_tag == 0 || params_tag, "params_tag required");
+        TagArgs a;
+        std::memset(&a, 0, sizeof(a));
+        a.boxes = L->d_boxes;
+        a.tiles = L->d_tiles;
+        a.state = L->buf[SH_NEW];
+        a.te = nullptr;
+        a.ncomp = L->ncomp;
+        a.lev = lev;
+        a.time = time;
+        a.dt = dt;
+        a.dx = dx;
+        for (int q = 0; q < nparams_tag; ++q) a.params_tag[q] = params_tag[q];
+        const size_t cnt_bytes = (2 + kMaxComp) * sizeof(unsigned long long);
+        const size_t mask_off = (cnt_bytes + 255) & ~size_t(255);
+        char *base = (char *)ctx_scratch(ctx, mask_off + (size_t)L->nvalid);
+        a.counts = (unsigned long long *)base;
+        a.mask = (unsigned char *)(base + mask_off);
+        a.mask_off = L->d_vbase;
+        ck(cudaMemsetAsync(a.counts, 0, cnt_bytes, ctx->stream), "count clear");
+        {
+            ProfScope ps(ctx, kProfTag);
+            ck(L->ops->launch_tag(a, L->ntiles, ctx->stream), "tag launch");
+            ctx->launches++;
+        }
+        unsigned long long counts[2];
+        ck(cudaMemcpyAsync(counts, a.counts, sizeof(counts), cudaMemcpyDeviceToHost, ctx->stream),
+           "count download");
+        ck(cudaStreamSynchronize(ctx->stream), "string tags");
+        *ntags = (long long)counts[1];
+    });
+}
+
+int sh_string_xi(long long string_tags, double dx, double L, double eta, double *xi) {
+    if (!xi || !(eta > 0.) || !(dx > 0.) || !(L > 0.) || string_tags < 0) return SH_ERR_ARG;
+    /* Cosmology::Xi with BoxToPhysical, Hubble, XiTemp and XiTime */
+    const double T1 = 5.4954174414835757e+17, mpl = 1.22e19, gstar = 106.;
+    const double hubble =
+        std::sqrt(4. * std::pow(M_PI, 3) / 45. * gstar * std::pow(T1, 4) / std::pow(mpl, 2));
+    const double length_sim = static_cast<double>(string_tags) * 2. / 3. * dx;
+    const double length_phys = length_sim * eta / hubble;
+    const double box_phys = L * eta / hubble;
+    const double T = T1 / eta;
+    const double time = 0.3012 / std::sqrt(gstar) * mpl / std::pow(T, 2);
+    *xi = length_phys * std::pow(time, 2) / std::pow(box_phys, 3);
+    return SH_OK;
 }
 
 int sh_average_down(sh_ctx *ctx, const sh_level *F, int which_f, sh_level *C, int which_c) {

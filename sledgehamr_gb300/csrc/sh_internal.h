@@ -20,7 +20,14 @@
 
 #include "sh_fill_plan.h" /* GhostCopyDev, CfRect, FillPlan */
 
+struct sh_ctx;
+
 namespace sh {
+
+/* Replaces the context's last error message (sh_ctx_last_error); for the
+ * library's host layers (the AMR hierarchy) that report their own errors
+ * through a context. */
+void set_ctx_error(::sh_ctx *ctx, const std::string &msg);
 
 constexpr int kMaxParams = 32;   /* doubles of Rhs parameters per call */
 constexpr int kMaxGwParams = 16; /* doubles of GW Rhs parameters per call */

@@ -70,3 +70,19 @@ def test_bad_arguments_rejected(lib):
     out = np.empty(8)
     assert lib.sh_index_to_k(8, 7, C.c_void_p(out.ctypes.data)) == _lib.SH_ERR_ARG
     assert lib.sh_ctx_create(0, None) == _lib.SH_ERR_ARG
+
+
+def test_string_xi_restates_cosmology_xi():
+    """sh_string_xi against Cosmology::Xi (projects/AxionStrings/
+    cosmology.cpp:89-108, cosmology.h:77-97) written out here."""
+    import math
+
+    import sledgehamr_gb300 as sh
+    T1, mpl, g = 5.4954174414835757e+17, 1.22e19, 106.0
+    hub = math.sqrt(4.0 * math.pi ** 3 / 45.0 * g * T1 ** 4 / mpl ** 2)
+    for tags, dx, L, eta in [(12345, 0.25, 64.0, 3.0), (1, 0.0625, 32.0, 0.5)]:
+        length = tags * 2.0 / 3.0 * dx * eta / hub
+        box = L * eta / hub
+        t = 0.3012 / math.sqrt(g) * mpl / (T1 / eta) ** 2
+        want = length * t ** 2 / box ** 3
+        assert abs(sh.string_xi(tags, dx, L, eta) - want) <= 1e-14 * want
