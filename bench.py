@@ -280,6 +280,28 @@ def fopt_bubbles():
     return xyz, tn, prof, Lcut
 
 
+def spectrum_times(call):
+    """Time-to-spectrum in ms (host clock around the synchronous call, bins
+    on the host at the end): the first (cold) call of each kind builds its
+    bin lists and FFT plan; warm is the median of three calls after both
+    kinds were built, alternating binned and unbinned.  Returns the times
+    and the (binned, unbinned) spectra."""
+    out, spec = {}, {}
+    for ub in (False, True):
+        t0 = time.perf_counter()
+        spec[ub] = call(ub)[0]
+        out["unbinned_cold" if ub else "binned_cold"] = 1e3 * (time.perf_counter() - t0)
+    warm = {False: [], True: []}
+    for _ in range(3):
+        for ub in (False, True):
+            t0 = time.perf_counter()
+            call(ub)
+            warm[ub].append(1e3 * (time.perf_counter() - t0))
+    out["binned_warm"] = float(np.median(warm[False]))
+    out["unbinned_warm"] = float(np.median(warm[True]))
+    return out, (spec[False], spec[True])
+
+
 def run_fopt_leg(sh, ctx, stream, flush, steps, warmup):
     """First-order phase transition with GW tensor, 384^3 periodic, leapfrog,
     64 bubbles injected at their nucleation times (at the first step whose
@@ -327,10 +349,8 @@ def run_fopt_leg(sh, ctx, stream, flush, steps, warmup):
     ms32 = run(lambda: E.step(dt, 1),
                lambda c: E.add_bubbles(0, c, prof, f["inv_dx"], Lcut), None)
     e32 = E.energy()[0]
-    ts = time.perf_counter()
-    gw32, ks = E.gw_spectrum(0, zero_padding=1, projection_type=2, unbinned=False)
-    spec32_ms = 1e3 * (time.perf_counter() - ts)
-    gu32, _ = E.gw_spectrum(0, zero_padding=1, projection_type=2, unbinned=True)
+    spec32_ms, (gw32, gu32) = spectrum_times(lambda ub: E.gw_spectrum(
+        0, zero_padding=1, projection_type=2, unbinned=ub))
     f32 = E.read(0)
     t32 = E.time()
     E.close()
@@ -342,10 +362,8 @@ def run_fopt_leg(sh, ctx, stream, flush, steps, warmup):
     params = [0.0, *q, 0.0, 0.0, 0.0]
     ms64 = run(lambda: lv.advance(sh.LEAPFROG, dt, dx, params=params),
                lambda c: lv.add_bubbles(c, prof, f["inv_dx"], Lcut, dx), None)
-    ts = time.perf_counter()
-    gw64, ks64 = lv.gw_spectrum(zero_padding=1, projection_type=2, unbinned=False)
-    spec64_ms = 1e3 * (time.perf_counter() - ts)
-    gu64, _ = lv.gw_spectrum(zero_padding=1, projection_type=2, unbinned=True)
+    spec64_ms, (gw64, gu64) = spectrum_times(lambda ub: lv.gw_spectrum(
+        zero_padding=1, projection_type=2, unbinned=ub))
     f64 = lv.read()
     t64 = lv.time()[0]
     lv.close()

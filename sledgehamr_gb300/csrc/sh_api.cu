@@ -2074,7 +2074,7 @@ int sh_scalar_spectrum(sh_ctx *ctx, const sh_level *L, int fn, int comp, double 
                            ctx->stream),
            "bins download");
         ck(cudaStreamSynchronize(ctx->stream), "scalar spectrum");
-        if (ks_out) std::copy(ctx->gw.ks.begin(), ctx->gw.ks.end(), ks_out);
+        if (ks_out) std::copy(ctx->gw.ks().begin(), ctx->gw.ks().end(), ks_out);
     });
 }
 
@@ -2466,7 +2466,7 @@ int sh_gw_spectrum(sh_ctx *ctx, const sh_level *L, const int *comps, int zero_pa
                            ctx->stream),
            "spectrum download");
         ck(cudaStreamSynchronize(ctx->stream), "gw spectrum");
-        if (ks_out) std::copy(ctx->gw.ks.begin(), ctx->gw.ks.end(), ks_out);
+        if (ks_out) std::copy(ctx->gw.ks().begin(), ctx->gw.ks().end(), ks_out);
     });
 }
 

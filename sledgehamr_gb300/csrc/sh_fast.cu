@@ -1329,7 +1329,7 @@ int sh_ensemble_gw_spectrum(sh_ensemble *E, int r, int zero_padding, int project
         fck(cudaMemcpyAsync(bins_out, bins_dev, nb * sizeof(double), cudaMemcpyDeviceToHost, s),
             "bins download");
         fck(cudaStreamSynchronize(s), "gw spectrum");
-        if (ks_out) std::copy(E->gw.ks.begin(), E->gw.ks.end(), ks_out);
+        if (ks_out) std::copy(E->gw.ks().begin(), E->gw.ks().end(), ks_out);
     });
 }
 

@@ -31,6 +31,11 @@
 #include <vector>
 
 #include <functional>
+#include <new>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #include "sh_gw.h"
 #include "sledgehamr_gb300.h"
@@ -169,17 +174,39 @@ __global__ void gw_project_kernel(const double2 *u0, const double2 *u1, const do
     }
 }
 
-/* One warp per bin: fixed-order sum of the bin's cells, scaled. */
-__global__ void gw_bin_kernel(const double *val, const long long *bin_off, const int *bin_cells,
-                              int nbins, double scale, double *bins) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (warp >= nbins) return;
-    const long long o0 = bin_off[warp], o1 = bin_off[warp + 1];
-    double s = 0.;
-    for (long long q = o0 + lane; q < o1; q += 32) s += val[bin_cells[q]];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (lane == 0) bins[warp] = s * scale;
+/* Deterministic sums of the bins' cells, scaled: a block of kBinThreads
+ * threads per bin (blocks loop over bins), thread t summing the cells t,
+ * t + kBinThreads, ... of the bin in order, then a fixed warp-shuffle and
+ * shared-memory tree.  A whole block per bin keeps the 85 K-cell bins of a
+ * 384^3 binned spectrum from running on a few hundred warps. */
+constexpr int kBinThreads = 256;
+__global__ void __launch_bounds__(kBinThreads)
+    gw_bin_kernel(const double *val, const long long *bin_off, const int *bin_cells, int nbins,
+                  double scale, double *bins) {
+    __shared__ double part[kBinThreads / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int bin = blockIdx.x; bin < nbins; bin += gridDim.x) {
+        const long long o0 = bin_off[bin], o1 = bin_off[bin + 1];
+        double s = 0.;
+        for (long long q = o0 + threadIdx.x; q < o1; q += kBinThreads) s += val[bin_cells[q]];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) part[wid] = s;
+        __syncthreads();
+        if (wid == 0) {
+            double t = lane < kBinThreads / 32 ? part[lane] : 0.;
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+            if (lane == 0) bins[bin] = t * scale;
+        }
+        __syncthreads();
+    }
+}
+
+void launch_bins(const double *vals, const GwBins &g, double scale, double *bins_dev,
+                 cudaStream_t stream) {
+    const int nb = (int)g.ks.size();
+    const int grid = std::max(1, std::min(nb, 152 * 8));
+    gw_bin_kernel<<<grid, kBinThreads, 0, stream>>>(vals, g.d_off, g.d_cells, nb, scale,
+                                                    bins_dev);
 }
 
 /* multpl |F|^2 per k-cell of a scalar field's R2C transform, with
@@ -200,26 +227,41 @@ __global__ void scalar_power_kernel(const double2 *F, int P, double *out) {
 } // namespace
 
 /* Builds (or reuses) the bin lists of a P^3 spectrum. */
-void GwCache::prepare(int P_, int unbinned_, int projection_type_) {
-    if (P_ == P && unbinned_ == unbinned && projection_type_ == projection_type && d_off) return;
-    release();
-    P = P_;
-    unbinned = unbinned_;
-    projection_type = projection_type_;
+void GwCache::prepare(int P, int unbinned, int projection_type) {
+    ++clock;
+    for (GwBins &b : bins)
+        if (b.P == P && b.unbinned == unbinned && b.projection_type == projection_type) {
+            b.used = clock;
+            cur = &b;
+            return;
+        }
+    if ((int)bins.size() >= kMaxBins) { /* evict the least recently used */
+        size_t lru = 0;
+        for (size_t q = 1; q < bins.size(); ++q)
+            if (bins[q].used < bins[lru].used) lru = q;
+        cudaFree(bins[lru].d_off);
+        cudaFree(bins[lru].d_cells);
+        cudaFree(bins[lru].d_itk);
+        bins.erase(bins.begin() + lru);
+    }
+    GwBins g;
+    g.P = P;
+    g.unbinned = unbinned;
+    g.projection_type = projection_type;
+    g.used = clock;
     const int H = P / 2 + 1;
     const long long ncell = (long long)H * P * P;
     if (unbinned) {
-        ks = unique_k2_host(P);
+        g.ks = unique_k2_host(P);
     } else {
-        ks.clear();
         for (int k = 0; k <= std::sqrt(3.) / 2. * static_cast<double>(P) + .5; ++k)
-            ks.push_back((long long)k * k);
+            g.ks.push_back((long long)k * k);
     }
-    const int nb = (int)ks.size();
+    const int nb = (int)g.ks.size();
     const long long maxsq = 3LL * (P / 2) * (P / 2);
     std::vector<int> lut((size_t)maxsq + 1, -1);
     if (unbinned) {
-        for (int q = 0; q < nb; ++q) lut[(size_t)ks[q]] = q;
+        for (int q = 0; q < nb; ++q) lut[(size_t)g.ks[q]] = q;
     } else {
         for (long long sq = 0; sq <= maxsq; ++sq) {
             long long r = (long long)std::llround(std::sqrt((double)sq));
@@ -229,41 +271,94 @@ void GwCache::prepare(int P_, int unbinned_, int projection_type_) {
             lut[(size_t)sq] = (int)r;
         }
     }
-    std::vector<long long> off(nb + 1, 0);
-    std::vector<int> binof((size_t)ncell);
-    for (long long e = 0; e < ncell; ++e) {
+    auto bin_of = [&](long long e) {
         const int a = (int)(e % H), b = (int)((e / H) % P), c = (int)(e / ((long long)H * P));
         const long long li = a >= P / 2 ? a - P : a;
         const long long lj = b >= P / 2 ? b - P : b;
         const long long lk = c >= P / 2 ? c - P : c;
-        const int bin = lut[(size_t)(li * li + lj * lj + lk * lk)];
-        binof[(size_t)e] = bin;
-        off[bin + 1]++;
+        return lut[(size_t)(li * li + lj * lj + lk * lk)];
+    };
+    /* stable counting sort over contiguous chunks of cells, one per thread */
+    int nt = 1;
+#ifdef _OPENMP
+    nt = std::max(1, std::min(omp_get_max_threads(), 64));
+#endif
+    const long long chunk = (ncell + nt - 1) / nt;
+    std::vector<long long> cnt((size_t)nt * nb, 0);
+#pragma omp parallel for num_threads(nt) schedule(static, 1)
+    for (int t = 0; t < nt; ++t) {
+        long long *c = cnt.data() + (size_t)t * nb;
+        const long long e1 = std::min(ncell, (t + 1) * chunk);
+        for (long long e = t * chunk; e < e1; ++e) c[bin_of(e)]++;
     }
-    for (int q = 0; q < nb; ++q) off[q + 1] += off[q];
-    std::vector<long long> fillp(off.begin(), off.end() - 1);
+    std::vector<long long> off(nb + 1, 0);
+    for (int q = 0; q < nb; ++q) {
+        long long run = off[q];
+        for (int t = 0; t < nt; ++t) {
+            const long long c = cnt[(size_t)t * nb + q];
+            cnt[(size_t)t * nb + q] = run; /* start of thread t's cells in bin q */
+            run += c;
+        }
+        off[q + 1] = run;
+    }
     std::vector<int> cells((size_t)ncell);
-    for (long long e = 0; e < ncell; ++e) cells[(size_t)fillp[binof[(size_t)e]]++] = (int)e;
+#pragma omp parallel for num_threads(nt) schedule(static, 1)
+    for (int t = 0; t < nt; ++t) {
+        long long *pos = cnt.data() + (size_t)t * nb;
+        const long long e1 = std::min(ncell, (t + 1) * chunk);
+        for (long long e = t * chunk; e < e1; ++e) cells[(size_t)pos[bin_of(e)]++] = (int)e;
+    }
     std::vector<double> itk = index_to_k_host(P, projection_type);
-    cudaMalloc(&d_off, off.size() * sizeof(long long));
-    cudaMalloc(&d_cells, cells.size() * sizeof(int));
-    cudaMalloc(&d_itk, itk.size() * sizeof(double));
-    cudaMemcpy(d_off, off.data(), off.size() * sizeof(long long), cudaMemcpyHostToDevice);
-    cudaMemcpy(d_cells, cells.data(), cells.size() * sizeof(int), cudaMemcpyHostToDevice);
-    cudaMemcpy(d_itk, itk.data(), itk.size() * sizeof(double), cudaMemcpyHostToDevice);
+    if (cudaMalloc(&g.d_off, off.size() * sizeof(long long)) != cudaSuccess ||
+        cudaMalloc(&g.d_cells, cells.size() * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&g.d_itk, itk.size() * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(g.d_off);
+        cudaFree(g.d_cells);
+        cudaFree(g.d_itk);
+        throw std::bad_alloc();
+    }
+    cudaMemcpy(g.d_off, off.data(), off.size() * sizeof(long long), cudaMemcpyHostToDevice);
+    cudaMemcpy(g.d_cells, cells.data(), cells.size() * sizeof(int), cudaMemcpyHostToDevice);
+    cudaMemcpy(g.d_itk, itk.data(), itk.size() * sizeof(double), cudaMemcpyHostToDevice);
+    bins.push_back(std::move(g));
+    cur = &bins.back();
+}
+
+bool GwCache::plan(int P, cufftHandle *out) {
+    ++clock;
+    for (Plan &p : plans)
+        if (p.P == P) {
+            p.used = clock;
+            *out = p.h;
+            return true;
+        }
+    if ((int)plans.size() >= kMaxPlans) {
+        size_t lru = 0;
+        for (size_t q = 1; q < plans.size(); ++q)
+            if (plans[q].used < plans[lru].used) lru = q;
+        cufftDestroy(plans[lru].h);
+        plans.erase(plans.begin() + lru);
+    }
+    Plan p;
+    p.P = P;
+    p.used = clock;
+    if (cufftPlan3d(&p.h, P, P, P, CUFFT_D2Z) != CUFFT_SUCCESS) return false;
+    plans.push_back(p);
+    *out = p.h;
+    return true;
 }
 
 void GwCache::release() {
-    cudaFree(d_off);
-    cudaFree(d_cells);
-    cudaFree(d_itk);
-    d_off = nullptr;
-    d_cells = nullptr;
-    d_itk = nullptr;
-    if (plan_ok) cufftDestroy(plan);
-    plan_ok = false;
-    plan_P = 0;
-    P = 0;
+    for (GwBins &b : bins) {
+        cudaFree(b.d_off);
+        cudaFree(b.d_cells);
+        cudaFree(b.d_itk);
+    }
+    bins.clear();
+    for (Plan &p : plans) cufftDestroy(p.h);
+    plans.clear();
+    cur = nullptr;
 }
 
 cudaError_t gw_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, int projection_type,
@@ -274,17 +369,12 @@ cudaError_t gw_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, int p
     const int H = P / 2 + 1;
     const long long nreal = (long long)P * P * P;
     const long long ncplx = (long long)H * P * P;
-    if (!cache.plan_ok || cache.plan_P != P) {
-        if (cache.plan_ok) cufftDestroy(cache.plan);
-        cache.plan_ok = false;
-        if (cufftPlan3d(&cache.plan, P, P, P, CUFFT_D2Z) != CUFFT_SUCCESS) {
-            err = "cufftPlan3d failed";
-            return cudaErrorUnknown;
-        }
-        cache.plan_ok = true;
-        cache.plan_P = P;
+    cufftHandle plan;
+    if (!cache.plan(P, &plan)) {
+        err = "cufftPlan3d failed";
+        return cudaErrorUnknown;
     }
-    cufftSetStream(cache.plan, stream);
+    cufftSetStream(plan, stream);
     /* scratch: real (pN)^3 | 6 complex arrays | per-cell values */
     double *real = scratch;
     double2 *cplx = (double2 *)(scratch + nreal);
@@ -293,7 +383,7 @@ cudaError_t gw_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, int p
         cudaMemsetAsync(real, 0, nreal * sizeof(double), stream);
         pack(q, real);
         (*launches)++;
-        if (cufftExecD2Z(cache.plan, real, (cufftDoubleComplex *)(cplx + q * ncplx)) !=
+        if (cufftExecD2Z(plan, real, (cufftDoubleComplex *)(cplx + q * ncplx)) !=
             CUFFT_SUCCESS) {
             err = "cufftExecD2Z failed";
             return cudaErrorUnknown;
@@ -302,12 +392,11 @@ cudaError_t gw_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, int p
     int g = (int)std::min<long long>((ncplx + 255) / 256, 152LL * 32);
     gw_project_kernel<<<std::max(g, 1), 256, 0, stream>>>(
         cplx, cplx + ncplx, cplx + 2 * ncplx, cplx + 3 * ncplx, cplx + 4 * ncplx,
-        cplx + 5 * ncplx, cache.d_itk, P, vals);
+        cplx + 5 * ncplx, cache.cur->d_itk, P, vals);
     (*launches)++;
-    const int nb = (int)cache.ks.size();
+    const int nb = (int)cache.ks().size();
     const double scale = 1. / std::pow((double)P, 6);
-    gw_bin_kernel<<<(nb * 32 + 255) / 256, 256, 0, stream>>>(vals, cache.d_off, cache.d_cells,
-                                                              nb, scale, bins_dev);
+    launch_bins(vals, *cache.cur, scale, bins_dev, stream);
     (*launches)++;
     *nbins = nb;
     return cudaGetLastError();
@@ -317,38 +406,32 @@ cudaError_t scalar_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, d
                                    double *scratch, double *bins_dev, int *nbins,
                                    long long *launches, std::string &err,
                                    const std::function<void(double *)> &pack) {
-    const int keep_type = cache.projection_type >= 1 ? cache.projection_type : 2;
-    cache.prepare(P, 1, keep_type);
+    /* unbinned bins of k^2 (the k-map of the entry is not used) */
+    cache.prepare(P, 1, 2);
     const int H = P / 2 + 1;
     const long long nreal = (long long)P * P * P;
     const long long ncplx = (long long)H * P * P;
-    if (!cache.plan_ok || cache.plan_P != P) {
-        if (cache.plan_ok) cufftDestroy(cache.plan);
-        cache.plan_ok = false;
-        if (cufftPlan3d(&cache.plan, P, P, P, CUFFT_D2Z) != CUFFT_SUCCESS) {
-            err = "cufftPlan3d failed";
-            return cudaErrorUnknown;
-        }
-        cache.plan_ok = true;
-        cache.plan_P = P;
+    cufftHandle plan;
+    if (!cache.plan(P, &plan)) {
+        err = "cufftPlan3d failed";
+        return cudaErrorUnknown;
     }
-    cufftSetStream(cache.plan, stream);
+    cufftSetStream(plan, stream);
     double *real = scratch;
     double2 *cplx = (double2 *)(scratch + nreal);
     double *vals = (double *)(cplx + ncplx);
     cudaMemsetAsync(real, 0, nreal * sizeof(double), stream);
     pack(real);
     (*launches)++;
-    if (cufftExecD2Z(cache.plan, real, (cufftDoubleComplex *)cplx) != CUFFT_SUCCESS) {
+    if (cufftExecD2Z(plan, real, (cufftDoubleComplex *)cplx) != CUFFT_SUCCESS) {
         err = "cufftExecD2Z failed";
         return cudaErrorUnknown;
     }
     int g = (int)std::min<long long>((ncplx + 255) / 256, 152LL * 32);
     scalar_power_kernel<<<std::max(g, 1), 256, 0, stream>>>(cplx, P, vals);
     (*launches)++;
-    const int nb = (int)cache.ks.size();
-    gw_bin_kernel<<<(nb * 32 + 255) / 256, 256, 0, stream>>>(vals, cache.d_off, cache.d_cells,
-                                                              nb, pre, bins_dev);
+    const int nb = (int)cache.ks().size();
+    launch_bins(vals, *cache.cur, pre, bins_dev, stream);
     (*launches)++;
     *nbins = nb;
     return cudaGetLastError();

@@ -12,18 +12,39 @@
 
 namespace sh {
 
-/* Bin lists, index_to_k table and cuFFT plan of the last spectrum size,
- * kept per context. */
-struct GwCache {
+/* Bin lists of one spectrum kind: grid size P, binned or unbinned, with the
+ * index_to_k table of a projection type. */
+struct GwBins {
     int P = 0, unbinned = -1, projection_type = -1;
-    std::vector<long long> ks;
+    std::vector<long long> ks; /* k^2 of every bin */
     long long *d_off = nullptr; /* nbins + 1 */
     int *d_cells = nullptr;     /* cells sorted by bin, ascending within a bin */
     double *d_itk = nullptr;    /* index_to_k[P] */
-    cufftHandle plan = 0;
-    bool plan_ok = false;
-    int plan_P = 0;
+    long long used = 0;         /* last use (for eviction) */
+};
+
+/* Bin lists and cuFFT plans of the recent spectrum kinds, kept per context
+ * (or ensemble) so that alternating binned and unbinned spectra, or several
+ * grid sizes, reuse them.  Bin lists are built on the host threads (a
+ * stable parallel counting sort, so cells stay in ascending order within a
+ * bin and sums are reproducible). */
+struct GwCache {
+    static constexpr int kMaxBins = 4, kMaxPlans = 2;
+    std::vector<GwBins> bins;
+    struct Plan {
+        int P = 0;
+        cufftHandle h = 0;
+        long long used = 0;
+    };
+    std::vector<Plan> plans;
+    long long clock = 0;
+    GwBins *cur = nullptr;
+    /* k^2 of the bins of the last prepared kind */
+    const std::vector<long long> &ks() const { return cur->ks; }
     void prepare(int P, int unbinned, int projection_type);
+    /* cuFFT D2Z plan of a P^3 transform (created on first use); false if
+     * cuFFT fails */
+    bool plan(int P, cufftHandle *out);
     void release();
 };
 
