@@ -98,17 +98,65 @@ __device__ __noinline__ double scale_pow2_slow(double res, int pw) { return scal
 inline double scale_pow2_slow(double res, int pw) { return std::scalbn(res, pw); }
 #endif
 
+AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE int clz64(unsigned long long u) {
+#if defined(__CUDA_ARCH__)
+    return __clzll((long long)u);
+#else
+    return __builtin_clzll(u);
+#endif
+}
+
+/* Bits of the FP64 value nearest to acc * 2^pw (ties to even), for acc != 0
+ * with |acc| < 2^63, formed with integer instructions only; the biased
+ * exponent goes to *e (the bits are valid when 1 <= *e <= 2046).  On
+ * GB300 the integer-to-FP64 conversion instruction issues on the narrow
+ * FP64 pipe; these integer steps issue on the integer pipe. */
+AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE unsigned long long int_to_f64_bits(long long acc, int pw,
+                                                                            int *e) {
+    const unsigned long long sign = acc < 0 ? (1ull << 63) : 0ull;
+    const unsigned long long u = acc < 0 ? 0ull - (unsigned long long)acc : (unsigned long long)acc;
+    const int lz = clz64(u);
+    const unsigned long long nrm = u << lz; /* leading one at bit 63 */
+    unsigned long long mant = nrm >> 11;    /* 53 bits with the leading one */
+    const unsigned rem = (unsigned)(nrm & 0x7FFull);
+    mant += (unsigned long long)((rem > 0x400u) | ((rem == 0x400u) & (unsigned)(mant & 1ull)));
+    const int carry = (int)(mant >> 53); /* rounded up to 2^53 */
+    mant >>= carry;
+    *e = 63 - lz + 1023 + pw + carry;
+    return sign | ((unsigned long long)(unsigned)*e << 52) | (mant & 0xFFFFFFFFFFFFFull);
+}
+
+/* log2 of x when x is a positive normal power of two, else -2000. */
+AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE int pow2_exponent(double x) {
+    const long long b = bits(x);
+    const int ex = (int)((b >> 52) & 0x7FF);
+    return (b > 0 && (b & 0xFFFFFFFFFFFFFll) == 0 && ex >= 1 && ex <= 2046) ? ex - 1023 : -2000;
+}
+
 AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE double to_double(long long acc, int pw) {
     if (acc == 0) return 0.;
-    const double res = (double)acc;
-    const long long rb = bits(res);
-    const int er = (int)((rb >> 52) & 0x7FF) + pw;
-    if (er >= 1 && er <= 2046) return from_bits(rb + ((long long)pw << 52));
-    return scale_pow2_slow(res, pw);
+    int e;
+    const unsigned long long rb = int_to_f64_bits(acc, pw, &e);
+    if (e >= 1 && e <= 2046) return from_bits((long long)rb);
+    return scale_pow2_slow((double)acc, pw);
 }
+/* acc * 2^pw * scale: a power-of-two scale (1 / dx^2 for dx a power of two)
+ * joins the exponent, so the result takes one rounding and no FP64
+ * instruction; any other scale costs one FP64 product after the rounded
+ * conversion. */
 AMREX_GPU_HOST_DEVICE AMREX_FORCE_INLINE double to_double(long long acc, int pw, double scale) {
     if (acc == 0) return 0.;
-    const double res = (double)acc * scale;
+    const int ps = pow2_exponent(scale);
+    const bool p2 = ps != -2000;
+    int e;
+    /* one conversion for both cases: with the power of two folded in, or
+     * of acc alone (|acc| < 2^63 converts to a normal number) */
+    const unsigned long long cb = int_to_f64_bits(acc, p2 ? pw + ps : 0, &e);
+    if (p2) {
+        if (e >= 1 && e <= 2046) return from_bits((long long)cb);
+        return scale_pow2_slow((double)acc, pw + ps);
+    }
+    const double res = from_bits((long long)cb) * scale;
     const long long rb = bits(res);
     const int er = (int)((rb >> 52) & 0x7FF) + pw;
     if (er >= 1 && er <= 2046) return from_bits(rb + ((long long)pw << 52));

@@ -135,11 +135,45 @@ bool run_gradient(std::mt19937_64 &g) {
     return true;
 }
 
+/* The integer-only conversion equals the FP64 conversion (round to nearest,
+ * ties to even) times 2^pw, on random magnitudes, exact ties and carries. */
+bool run_conversion(std::mt19937_64 &g) {
+    long long checked = 0;
+    for (int it = 0; it < 2000000; ++it) {
+        const int nb = 1 + (int)(g() % 63);
+        unsigned long long u = g() >> (64 - nb);
+        if (it % 5 == 1 && nb > 54) { /* exact tie below the 53 kept bits */
+            const int k = nb - 53;
+            u = ((u | 1ull << (nb - 1)) & ~((1ull << k) - 1)) | (1ull << (k - 1));
+        }
+        if (it % 5 == 2 && nb > 54) u = (1ull << nb) - 1; /* rounds up into a carry */
+        if (u == 0 || u >= (1ull << 63)) continue;
+        const long long acc = (g() & 1) ? -(long long)u : (long long)u;
+        const int pw = (int)(g() % 1200) - 700;
+        const double want = std::ldexp((double)acc, pw);
+        if (!std::isnormal(want)) continue;
+        const double got = fixed::to_double(acc, pw);
+        if (got != want) {
+            std::printf("conversion failed: %lld * 2^%d\n", acc, pw);
+            return false;
+        }
+        const double sc = (it % 3 == 0) ? 0.25 : 1.0 / 12.0;
+        const double ws = std::ldexp((double)acc * sc, pw);
+        if (std::isnormal(ws) && fixed::to_double(acc, pw, sc) != ws) {
+            std::printf("scaled conversion failed: %lld * %g * 2^%d\n", acc, sc, pw);
+            return false;
+        }
+        ++checked;
+    }
+    std::printf("c %lld\n", checked);
+    return true;
+}
+
 } // namespace
 
 int main() {
     std::mt19937_64 g(12345);
-    const bool ok = run<1>(g) && run<2>(g) && run<3>(g) && run_gradient<2>(g) &&
-                    run_gradient<3>(g);
+    const bool ok = run_conversion(g) && run<1>(g) && run<2>(g) && run<3>(g) &&
+                    run_gradient<2>(g) && run_gradient<3>(g);
     return ok ? 0 : 1;
 }
