@@ -532,6 +532,18 @@ SH_API int sh_amr_timer(const sh_amr *a, int q, const char **name, double *secon
  * schedule, shadow, average_down, truncation_errors, regrid; times printed
  * exactly).  sh_amr_trace copies the lines so far (NUL-terminated) into buf
  * of cap bytes and stores their length; buf NULL: length only. */
+/* Checkpoint::Write / Checkpoint::Read (source/output_types/checkpoint.cpp:
+ * 18-187): the hierarchy's state between coarse steps to a folder (created
+ * if missing): Meta.hdf5 with the reference's header datasets (Header,
+ * blocking_factors, isteps, next_id, last_time_written) and this library's
+ * (boxes, times, regrid schedule), and both time levels of every level as
+ * raw FP64 files (the reference writes AMReX VisMF files there).
+ * sh_amr_restart creates a hierarchy from such a folder with a
+ * configuration describing the same grid; stepping it continues exactly as
+ * the checkpointed hierarchy would have. */
+SH_API int sh_amr_checkpoint(sh_ctx *ctx, sh_amr *amr, const char *folder);
+SH_API int sh_amr_restart(sh_ctx *ctx, const sh_amr_config *cfg, const char *folder,
+                          sh_amr **out);
 SH_API int sh_amr_set_trace(sh_amr *amr, int on);
 SH_API int sh_amr_trace(const sh_amr *amr, char *buf, long long cap, long long *len);
 SH_API int sh_amr_level(const sh_amr *amr, int lev, sh_level **level);
@@ -548,6 +560,11 @@ SH_API int sh_amr_regrid_record(const sh_amr *amr, int q, int *lev, double *time
  * hide their latency): the peak of the FP64 roofline of the stage kernels.
  * No counterpart in the reference. */
 SH_API int sh_probe_fp64_fma_rate(int device, double *fma_per_s);
+/* The bounded wait of the tensor-copy stage kernels run on an mbarrier that
+ * nothing completes, with a 2 ms limit: *status is SH_ERR_TIMEOUT when the
+ * limit ended the wait (and the device stays usable).  No counterpart in
+ * the reference. */
+SH_API int sh_probe_wait_timeout(int device, int *status);
 
 /* ---- convenience --------------------------------------------------------------- */
 /* Evolve a periodic cubic level of N^3 cells (boxes of max_grid cells per
@@ -607,8 +624,19 @@ SH_API int sh_ensemble_read(sh_ensemble *e, int r, double *host);
 SH_API int sh_ensemble_set_graph(sh_ensemble *e, int on);
 SH_API int sh_ensemble_step(sh_ensemble *e, double dt, int nsteps);
 /* Tile depth along z; 0 times {4, 8, 16, 32, 64} on the current state
- * (leaving state, compensation and time unchanged) and keeps the fastest. */
+ * (leaving state, compensation and time unchanged) and keeps the fastest,
+ * for each stencil-plane staging the ensemble allows (see below). */
 SH_API int sh_ensemble_tune(sh_ensemble *e, int tile_nz, double dt, int *chosen);
+/* Stencil-plane staging of the axion stage kernels: 0 planes loaded through
+ * registers into a shared-memory ring; 1 planes brought into shared memory
+ * by the Tensor Memory Accelerator (tiled tensor copies, two planes in
+ * flight; FP32 storage, every realisation's N a multiple of 4 and at most
+ * 256, else SH_ERR_UNSUPPORTED).  Both give the same results.  A stage
+ * kernel whose wait for its copies runs out (one second) records
+ * SH_ERR_TIMEOUT, which the next synchronising call of the ensemble
+ * returns. */
+SH_API int sh_ensemble_set_staging(sh_ensemble *e, int staging);
+SH_API int sh_ensemble_staging(const sh_ensemble *e, int *staging);
 /* Diagnostics per realisation: total energy (FP64 sums of the densities
  * listed at energy_kernel), number of string-pierced cells (axion
  * families; plaquette winding as in AxionStrings tagging), GW spectrum of

@@ -28,6 +28,7 @@
 
 #include "../include/sledgehamr_gb300.h"
 #include "../sledgehamr_gb300/csrc/sh_amr_driver.h"
+#include "../sledgehamr_gb300/csrc/sh_checkpoint.h"
 #include "oracle_projects.h"
 
 namespace orc {
@@ -238,6 +239,30 @@ struct CpuBackend {
                        coarse ? &(*coarse)->nw : nullptr);
     }
     void sync() {}
+    /* valid cells in the boxes layout (box after box, comp-major) */
+    std::vector<double> read_valid(Level &l, int which) {
+        const MF &m = buf(l, which);
+        std::vector<double> v;
+        for (const Fab &f : m.fabs) {
+            auto a = f.ca();
+            for (int n = 0; n < m.nc; ++n)
+                for_cells(f.vbox, [&](int i, int j, int k) { v.push_back(a(i, j, k, n)); });
+        }
+        return v;
+    }
+    void write_valid(Level &l, int which, const std::vector<double> &v) {
+        MF &m = buf(l, which);
+        size_t q = 0;
+        for (Fab &f : m.fabs) {
+            auto a = f.a();
+            for (int n = 0; n < m.nc; ++n)
+                for_cells(f.vbox, [&](int i, int j, int k) {
+                    if (q >= v.size()) throw std::runtime_error("checkpoint data too short");
+                    a(i, j, k, n) = v[q++];
+                });
+        }
+        if (q != v.size()) throw std::runtime_error("checkpoint data too long");
+    }
     /* FirstOrderPhaseTransition.cpp:133-157: params_mod = norm0 of every
      * component of level 0's new data, once per time */
     double maxima_time = -DBL_MAX;
@@ -270,6 +295,8 @@ struct AmrBase {
     virtual const std::vector<shamr::IBox> &boxes(int lev) const = 0;
     virtual void set_tag_params(const double *pt, int nt, const double *pm, int nm) = 0;
     virtual void set_trace(bool on) = 0;
+    virtual shamr::Checkpoint checkpoint() = 0;
+    virtual void restart(const shamr::Checkpoint &k) = 0;
     virtual const std::vector<std::string> &trace() const = 0;
 };
 
@@ -324,6 +351,8 @@ struct Amr : AmrBase {
     }
     const std::vector<shamr::IBox> &boxes(int lev) const override { return drv->boxes[lev]; }
     void set_trace(bool on) override { drv->record_trace = on; }
+    shamr::Checkpoint checkpoint() override { return drv->checkpoint(); }
+    void restart(const shamr::Checkpoint &k) override { drv->restart(k); }
     const std::vector<std::string> &trace() const override { return drv->trace; }
     void set_tag_params(const double *pt, int nt, const double *pm, int nm) override {
         for (int q = 0; q < nt; ++q) backend.cfg.params_tag[q] = pt[q];
@@ -399,6 +428,41 @@ int orc_make_boxes(const unsigned char *tags, const unsigned char *allowed, int 
             out[6 * q + 3 + d] = b[q].hi[d];
         }
     return (int)b.size();
+}
+
+/* Checkpoint files of the hierarchy (shamr::write_checkpoint) and a new
+ * hierarchy restarted from them (level0 of the creation is replaced). */
+int orc_amr_checkpoint(void *h, const char *folder) {
+    try {
+        std::string err;
+        if (!shamr::write_checkpoint(((AmrBase *)h)->checkpoint(), folder, &err)) {
+            fprintf(stderr, "orc_amr_checkpoint: %s\n", err.c_str());
+            return -1;
+        }
+        return 0;
+    } catch (const std::exception &e) {
+        fprintf(stderr, "orc_amr_checkpoint: %s\n", e.what());
+        return -1;
+    }
+}
+void *orc_amr_restart(const sh_amr_config *cfg, const char *folder) {
+    shamr::Checkpoint k;
+    std::string err;
+    if (!shamr::read_checkpoint(folder, &k, &err)) {
+        fprintf(stderr, "orc_amr_restart: %s\n", err.c_str());
+        return nullptr;
+    }
+    std::vector<double> zero((size_t)k.ncomp * cfg->N0 * cfg->N0 * cfg->N0, 0.);
+    AmrBase *a = (AmrBase *)orc_amr_create(cfg, zero.data());
+    if (!a) return nullptr;
+    try {
+        a->restart(k);
+    } catch (const std::exception &e) {
+        fprintf(stderr, "orc_amr_restart: %s\n", e.what());
+        delete a;
+        return nullptr;
+    }
+    return a;
 }
 
 /* The time stepper's operation trace (shamr::Driver::trace): record_trace

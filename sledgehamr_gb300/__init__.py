@@ -531,6 +531,23 @@ class Amr:
                   "sh_amr_create")
         self.h = h
 
+    @classmethod
+    def restart(cls, ctx: Context, cfg: ShAmrConfig, folder: str) -> "Amr":
+        """A hierarchy from a checkpoint folder (sh_amr_restart)."""
+        self = cls.__new__(cls)
+        self.ctx = ctx
+        self.cfg = cfg
+        h = C.c_void_p()
+        ctx.check(ctx.lib.sh_amr_restart(ctx.h, C.byref(cfg), str(folder).encode(), C.byref(h)),
+                  "sh_amr_restart")
+        self.h = h
+        return self
+
+    def checkpoint(self, folder: str):
+        """Checkpoint::Write of the hierarchy into folder (sh_amr_checkpoint)."""
+        self.ctx.check(self.ctx.lib.sh_amr_checkpoint(self.ctx.h, self.h, str(folder).encode()),
+                       "sh_amr_checkpoint")
+
     def step(self, n: int = 1):
         self.ctx.check(self.ctx.lib.sh_amr_step(self.ctx.h, self.h, n), "sh_amr_step")
 
@@ -740,6 +757,15 @@ class Ensemble:
 
     def step(self, dt: float, nsteps: int = 1):
         self.check(self.ctx.lib.sh_ensemble_step(self.h, float(dt), int(nsteps)), "step")
+
+    def set_staging(self, staging: int):
+        """0: stencil planes through registers; 1: tensor copies (TMA)."""
+        self.check(self.ctx.lib.sh_ensemble_set_staging(self.h, int(staging)), "set_staging")
+
+    def staging(self) -> int:
+        s = C.c_int()
+        self.check(self.ctx.lib.sh_ensemble_staging(self.h, C.byref(s)), "staging")
+        return s.value
 
     def tune(self, dt: float, tile_nz: int = 0) -> int:
         ch = C.c_int()

@@ -160,6 +160,8 @@ SIGNATURES = {
     "sh_amr_timer": (C.c_int, [vp, C.c_int, C.POINTER(C.c_char_p), dp, llp]),
     "sh_amr_level": (C.c_int, [vp, C.c_int, C.POINTER(vp)]),
     "sh_amr_set_trace": (C.c_int, [vp, C.c_int]),
+    "sh_amr_checkpoint": (C.c_int, [vp, vp, C.c_char_p]),
+    "sh_amr_restart": (C.c_int, [vp, C.POINTER(ShAmrConfig), C.c_char_p, C.POINTER(vp)]),
     "sh_amr_trace": (C.c_int, [vp, C.c_char_p, C.c_longlong, llp]),
     "sh_amr_regrid_record": (C.c_int, [vp, C.c_int, ip, dp, C.POINTER(ShBox), C.c_int, ip, vp,
                                        C.c_longlong, llp, C.POINTER(ShBox), C.c_int, ip]),
@@ -187,6 +189,9 @@ SIGNATURES = {
     "sh_index_to_k": (C.c_int, [C.c_int, C.c_int, vp]),
     "sh_gw_spectrum": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, C.c_int, ip]),
     "sh_probe_fp64_fma_rate": (C.c_int, [C.c_int, dp]),
+    "sh_probe_wait_timeout": (C.c_int, [C.c_int, ip]),
+    "sh_ensemble_set_staging": (C.c_int, [vp, C.c_int]),
+    "sh_ensemble_staging": (C.c_int, [vp, ip]),
     "sh_level_check_finite": (C.c_int, [vp, vp, C.c_int, llp]),
     "sh_level_string_tags": (C.c_int, [vp, vp, C.c_double, C.c_int, C.c_double, C.c_double, vp,
                                        C.c_int, llp]),

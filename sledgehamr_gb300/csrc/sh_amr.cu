@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "sh_amr_driver.h"
+#include "sh_checkpoint.h"
 #include "sh_internal.h"
 #include "sledgehamr_gb300.h"
 
@@ -130,6 +131,22 @@ struct GpuBackend {
         ok(sh_level_fill_patch(ctx, l->L, which), "sh_level_fill_patch");
     }
     void sync() { ok(sh_ctx_synchronize(ctx), "sh_ctx_synchronize"); }
+    std::vector<double> read_valid(Level &l, int which) {
+        int nc = 0, nb = 0;
+        long long nv = 0;
+        sh_level_info(l->L, &nc, &nb, &nv);
+        std::vector<double> v((size_t)nv * nc);
+        ok(sh_level_read(ctx, l->L, which, 1, v.data()), "sh_level_read");
+        return v;
+    }
+    void write_valid(Level &l, int which, const std::vector<double> &v) {
+        int nc = 0, nb = 0;
+        long long nv = 0;
+        sh_level_info(l->L, &nc, &nb, &nv);
+        if ((long long)v.size() != nv * nc)
+            throw ShFail(SH_ERR_ARG, "checkpoint data does not match the level's boxes");
+        ok(sh_level_write(ctx, l->L, which, 1, v.data()), "sh_level_write");
+    }
     /* params_mod = per-component max |value| of level 0's new data, once
      * per time */
     double maxima_time = -DBL_MAX;
@@ -306,6 +323,44 @@ int sh_amr_timer(const sh_amr *a, int q, const char **name, double *seconds, lon
     if (name) *name = t.name;
     if (seconds) *seconds = t.sec;
     if (calls) *calls = t.calls;
+    return SH_OK;
+}
+
+int sh_amr_checkpoint(sh_ctx *ctx, sh_amr *a, const char *folder) {
+    if (!ctx || !a || !folder) return SH_ERR_ARG;
+    return amr_guard(ctx, [&] {
+        const shamr::Checkpoint k = a->driver->checkpoint();
+        std::string err;
+        if (!shamr::write_checkpoint(k, folder, &err)) throw ShFail(SH_ERR_ARG, err);
+    });
+}
+
+int sh_amr_restart(sh_ctx *ctx, const sh_amr_config *cfg, const char *folder, sh_amr **out) {
+    if (!ctx || !cfg || !folder || !out) return SH_ERR_ARG;
+    *out = nullptr;
+    shamr::Checkpoint k;
+    std::string err;
+    if (!shamr::read_checkpoint(folder, &k, &err)) {
+        sh::set_ctx_error(ctx, err);
+        return SH_ERR_ARG;
+    }
+    int ncomp = 0;
+    int rc = sh_project_ncomp(cfg->project, cfg->with_gw, &ncomp, nullptr);
+    if (rc != SH_OK) return rc;
+    if (ncomp != k.ncomp) {
+        sh::set_ctx_error(ctx, "checkpoint has " + std::to_string(k.ncomp) +
+                                   " components, the project " + std::to_string(ncomp));
+        return SH_ERR_ARG;
+    }
+    sh_amr *a = nullptr;
+    rc = sh_amr_create(ctx, cfg, nullptr, &a);
+    if (rc != SH_OK) return rc;
+    rc = amr_guard(ctx, [&] { a->driver->restart(k); });
+    if (rc != SH_OK) {
+        delete a;
+        return rc;
+    }
+    *out = a;
     return SH_OK;
 }
 

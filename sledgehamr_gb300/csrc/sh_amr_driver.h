@@ -55,6 +55,8 @@
  *   void remake(Level &fresh, Level &old, Level &crse, double time);
  *   void refresh_ghosts(Level&, int which, Level *coarse);
  *   void sync();   // wait for queued device work (timers with sync_timers)
+ *   std::vector<double> read_valid(Level&, int which);   // boxes layout
+ *   void write_valid(Level&, int which, const std::vector<double>&);
  */
 #ifndef SH_AMR_DRIVER_H_
 #define SH_AMR_DRIVER_H_
@@ -104,6 +106,27 @@ struct Config {
     int clustering = 0;         /* 0 Berger-Rigoutsos, 1 aligned windows */
     double grid_eff = 0.7;      /* minimum tagged fraction of a cluster */
     bool params_mod_norm0 = false; /* TruncationModifier params from level 0 */
+};
+
+/* The whole state of a hierarchy between two coarse steps: what the
+ * reference's Checkpoint::Write saves (source/output_types/checkpoint.cpp:
+ * 18-98: level-0 time, finest level, box arrays, isteps, grid_new of every
+ * level) plus what this time stepper needs to continue exactly as if it
+ * had not stopped (both time levels with their times and steps, the regrid
+ * schedule, the last regrid times, which levels hold truncation errors). */
+struct LevelState {
+    std::vector<IBox> boxes;
+    double t_new = 0., t_old = 0.;
+    int s_new = 0, s_old = 0;
+    std::vector<double> data_new, data_old; /* valid cells, box after box, comp-major */
+};
+struct Checkpoint {
+    int finest = 0, ncomp = 0, N0 = 0, nghost = 0, max_level = 0, blocking_factor = 0;
+    std::vector<LevelState> levels;
+    std::vector<double> last_regrid_time;
+    std::vector<std::pair<int, double>> schedule; /* (lowest level, time) */
+    std::vector<uint8_t> te_valid;
+    long long cell_updates = 0;
 };
 
 struct RegridRecord {
@@ -582,6 +605,70 @@ class Driver {
 
     /* One coarse step (Evolve's loop body). */
     void step() { advance(0); }
+
+    /* The hierarchy's state between coarse steps (Checkpoint::Write). */
+    Checkpoint checkpoint() {
+        if (shadow_defined) throw std::runtime_error("checkpoint with a shadow level pending");
+        Checkpoint k;
+        k.finest = finest;
+        k.N0 = c.N0;
+        k.nghost = c.nghost;
+        k.max_level = c.max_level;
+        k.blocking_factor = c.blocking_factor;
+        for (int l = 0; l <= finest; ++l) {
+            LevelState s;
+            s.boxes = boxes[l];
+            s.t_new = b.time(levels[l], kNew);
+            s.t_old = b.time(levels[l], kOld);
+            s.s_new = b.istep(levels[l], kNew);
+            s.s_old = b.istep(levels[l], kOld);
+            s.data_new = b.read_valid(levels[l], kNew);
+            s.data_old = b.read_valid(levels[l], kOld);
+            long long cells = 0;
+            for (const IBox &x : boxes[l]) cells += x.volume();
+            k.ncomp = cells ? (int)((long long)s.data_new.size() / cells) : 0;
+            k.levels.push_back(std::move(s));
+        }
+        k.last_regrid_time = last_regrid_time;
+        for (const Sched &q : schedule) k.schedule.push_back({q.lowest, q.t});
+        for (bool v : te_valid) k.te_valid.push_back(v ? 1 : 0);
+        k.cell_updates = cell_updates;
+        return k;
+    }
+
+    /* Replaces the hierarchy by a checkpoint's (Checkpoint::Read); the
+     * configuration must describe the same grid (coarse size, levels,
+     * blocking factor). */
+    void restart(const Checkpoint &k) {
+        if (k.N0 != c.N0 || k.max_level != c.max_level || k.blocking_factor != c.blocking_factor ||
+            k.finest < 0 || k.finest > c.max_level || (int)k.levels.size() != k.finest + 1 ||
+            (int)k.last_regrid_time.size() != c.max_level + 1 ||
+            (int)k.te_valid.size() != c.max_level + 1)
+            throw std::invalid_argument("checkpoint does not match the hierarchy's configuration");
+        for (int l = finest; l >= 0; --l)
+            if (levels[l]) b.destroy(levels[l]);
+        if (shadow_defined) b.destroy(shadow);
+        shadow_defined = false;
+        for (int l = 0; l <= c.max_level; ++l) {
+            levels[l] = Level{};
+            boxes[l].clear();
+        }
+        finest = k.finest;
+        for (int l = 0; l <= finest; ++l) {
+            const LevelState &s = k.levels[l];
+            boxes[l] = s.boxes;
+            levels[l] = b.create(l, boxes[l], dimN[l]);
+            b.write_valid(levels[l], kNew, s.data_new);
+            b.write_valid(levels[l], kOld, s.data_old);
+            b.set_time(levels[l], kNew, s.t_new, s.s_new);
+            b.set_time(levels[l], kOld, s.t_old, s.s_old);
+        }
+        last_regrid_time = k.last_regrid_time;
+        schedule.clear();
+        for (const auto &q : k.schedule) schedule.push_back(Sched{q.first, q.second});
+        for (int l = 0; l <= c.max_level; ++l) te_valid[l] = k.te_valid[l] != 0;
+        cell_updates = k.cell_updates;
+    }
 
     /* ---- queries ---- */
     int finest = 0;

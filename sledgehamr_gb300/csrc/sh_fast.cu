@@ -489,6 +489,8 @@ __global__ void __launch_bounds__(TX *TY, sizeof(R) == 4 ? 3 : 1) fopt_leapfrog_
 } // namespace fast
 } // namespace sh
 
+#include "sh_fast_tma.cuh"
+
 /* ======================================================================= */
 /* Diagnostics: FP64 energy per realisation and string (winding) counts.   */
 namespace sh {
@@ -739,6 +741,17 @@ struct sh_ensemble {
     bool use_graph = false;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     double graph_dt[2] = {0., 0.};
+    /* stencil-plane staging of the axion stage kernels in FP32: 0 planes
+     * loaded through registers (axion_rkn4_kernel), 1 tensor copies into
+     * shared memory (axion_rkn4_tma_kernel) with their tiles and maps */
+    int plane_staging = 0;
+    std::vector<sh::fast::tma::TmaTile> ttiles;
+    sh::fast::tma::TmaTile *d_ttiles = nullptr;
+    size_t ttiles_cap = 0;
+    CUtensorMap *d_maps = nullptr;
+    size_t maps_cap = 0;
+    int tma_slab = 0; /* largest shared-memory slab of the tiles (floats) */
+    int *d_err = nullptr; /* SH_ERR_TIMEOUT from a kernel whose wait ran out */
 };
 
 namespace {
@@ -772,6 +785,101 @@ void upload_table(const std::vector<T> &h, T *&d, size_t &cap, cudaStream_t s, c
         fck(cudaMemcpyAsync(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s), what);
 }
 
+/* Rows per tile of the tensor-copy kernels for a realisation of N cells
+ * per side and stencil reach H: the largest of 16, 8, 4, 2 that divides N,
+ * covers the reach, keeps a plane of the tile at most kMaxCells cells and
+ * its shared-memory slab (rows with halo times the padded pitch) at most
+ * 1024 floats; 0 when none does (or N is not a multiple of 4, which the
+ * 16-byte row strides of a tensor map need, or wider than a copy box). */
+int tma_rows(int N, int H) {
+    namespace T = sh::fast::tma;
+    if (N % 4 != 0 || N > 256 || N < 2 * H + 1) return 0;
+    for (int t : {16, 8, 4, 2})
+        if (N % t == 0 && t >= H && N * t <= T::kMaxCells && (t + 2 * H) * T::pitch_of(N) <= 1024)
+            return t;
+    return 0;
+}
+
+int family_reach(const sh_ensemble *E) { return E->family == SH_FAMILY_AXION_LAP2 ? 2 : 1; }
+
+/* Whether the tensor-copy kernels can run this ensemble: axion family in
+ * FP32 storage, every member of a size tma_rows accepts, every member's
+ * arrays 16-byte aligned. */
+bool tma_possible(const sh_ensemble *E) {
+    if (E->family == SH_FAMILY_FOPT_GW || E->esize != 4) return false;
+    for (const RealDesc &d : E->desc)
+        if (d.active && (tma_rows(d.N, family_reach(E)) == 0 || d.off % 4 != 0)) return false;
+    return true;
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+/* cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+ * against the driver library); null when unavailable. */
+EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return (EncodeTiledFn) nullptr;
+        }
+        return (EncodeTiledFn)p;
+    }();
+    return fn;
+}
+
+/* Tiles and tensor maps of the tensor-copy kernels (tiles of nz planes). */
+void build_tma(sh_ensemble *E, int nz) {
+    namespace T = sh::fast::tma;
+    const int H = family_reach(E);
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc) throw FastErr(SH_ERR_UNSUPPORTED, "tensor map encoding unavailable");
+    std::vector<T::TmaTile> tiles;
+    std::vector<CUtensorMap> maps((size_t)E->nreal * T::kMapsPerReal);
+    std::memset(maps.data(), 0, maps.size() * sizeof(CUtensorMap));
+    int slab = 0;
+    for (int r = 0; r < E->nreal; ++r) {
+        const RealDesc &d = E->desc[r];
+        if (!d.active) continue;
+        const int N = d.N, t = tma_rows(N, H), P = T::pitch_of(N);
+        if (t == 0) throw FastErr(SH_ERR_UNSUPPORTED, "realisation size unsuited to tensor copies");
+        slab = std::max(slab, (t + 2 * H) * P);
+        const int tz = std::min(nz, N);
+        for (int z = 0; z < N; z += tz)
+            for (int y = 0; y < N; y += t) tiles.push_back(T::TmaTile{r, y, z, std::min(tz, N - z), t});
+        const cuuint64_t dims[3] = {(cuuint64_t)N, (cuuint64_t)N, (cuuint64_t)N};
+        const cuuint64_t strides[2] = {(cuuint64_t)N * 4, (cuuint64_t)N * N * 4};
+        const cuuint32_t estr[3] = {1, 1, 1};
+        for (int a = 0; a < 12; ++a) {
+            float *base = (float *)(a < 4 ? E->A0 == E->A[0] ? E->A[a] : E->B[a]
+                                          : a < 8 ? (E->A0 == E->A[0] ? E->B[a - 4] : E->A[a - 4])
+                                                  : E->K[a - 8]) +
+                          d.off;
+            for (int sh = 0; sh < 2; ++sh) {
+                const cuuint32_t box[3] = {(cuuint32_t)P, (cuuint32_t)(sh == 0 ? t : H), 1};
+                const CUresult rc =
+                    enc(&maps[T::map_slot(r, a, sh)], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base,
+                        dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                if (rc != CUDA_SUCCESS)
+                    throw FastErr(SH_ERR_UNSUPPORTED,
+                                  "cuTensorMapEncodeTiled failed (" + std::to_string((int)rc) + ")");
+            }
+        }
+    }
+    upload_table(tiles, E->d_ttiles, E->ttiles_cap, est(E), "tensor-copy tiles");
+    upload_table(maps, E->d_maps, E->maps_cap, est(E), "tensor maps");
+    E->ttiles.swap(tiles);
+    E->tma_slab = slab;
+}
+
 void build_tiles(sh_ensemble *E, int nz) {
     std::vector<FastTile> t;
     for (int r = 0; r < E->nreal; ++r) {
@@ -785,6 +893,10 @@ void build_tiles(sh_ensemble *E, int nz) {
     upload_table(t, E->d_tiles, E->tiles_cap, est(E), "tile table");
     E->tiles.swap(t);
     E->tile_nz = nz;
+    if (E->plane_staging == 1) {
+        if (tma_possible(E)) build_tma(E, nz);
+        else E->plane_staging = 0;
+    }
     drop_graphs(E);
 }
 
@@ -825,6 +937,45 @@ void step_impl(sh_ensemble *E, const std::vector<void *> &in, const std::vector<
         a.time = E->d_time;
         a.slot = slot;
         a.h = dt;
+        if constexpr (sizeof(R) == 4) {
+            if (E->plane_staging == 1) {
+                namespace T = sh::fast::tma;
+                T::AxionTmaArgs t;
+                std::memset(&t, 0, sizeof(t));
+                t.desc = E->d_desc;
+                t.tiles = E->d_ttiles;
+                t.maps = E->d_maps;
+                for (int c = 0; c < 2; ++c) {
+                    t.y0[c] = a.y0[c];
+                    t.m0[c] = a.m0[c];
+                    t.y1[c] = a.y1[c];
+                    t.m1[c] = a.m1[c];
+                    t.cy[c] = a.cy[c];
+                    t.cm[c] = a.cm[c];
+                    t.K[0][c] = a.K[0][c];
+                    t.K[1][c] = a.K[1][c];
+                }
+                t.time = a.time;
+                t.slot = slot;
+                t.h = dt;
+                /* maps 0-3 describe the buffer that was A at creation */
+                t.in_base = in[0] == E->A0 ? 0 : 4;
+                t.err = E->d_err;
+                const int ntt = (int)E->ttiles.size();
+                const size_t s0 = T::smem_bytes(family_reach(E), 2, E->tma_slab);
+                const size_t s1 = T::smem_bytes(family_reach(E), 6, E->tma_slab);
+                if (E->family == SH_FAMILY_AXION_LAP1) {
+                    T::axion_rkn4_tma_kernel<1, 0, KAHAN><<<ntt, T::kThreads, s0, s>>>(t);
+                    T::axion_rkn4_tma_kernel<1, 1, KAHAN><<<ntt, T::kThreads, s1, s>>>(t);
+                    T::axion_rkn4_tma_kernel<1, 2, KAHAN><<<ntt, T::kThreads, s1, s>>>(t);
+                } else {
+                    T::axion_rkn4_tma_kernel<2, 0, KAHAN><<<ntt, T::kThreads, s0, s>>>(t);
+                    T::axion_rkn4_tma_kernel<2, 1, KAHAN><<<ntt, T::kThreads, s1, s>>>(t);
+                    T::axion_rkn4_tma_kernel<2, 2, KAHAN><<<ntt, T::kThreads, s1, s>>>(t);
+                }
+                return;
+            }
+        }
         if (E->family == SH_FAMILY_AXION_LAP1) {
             axion_rkn4_kernel<R, 1, 0, KAHAN><<<nt, block, 0, s>>>(a);
             axion_rkn4_kernel<R, 1, 1, KAHAN><<<nt, block, 0, s>>>(a);
@@ -921,6 +1072,21 @@ int fguard(sh_ensemble *E, F &&f) {
 }
 
 void set_smem_limits() {
+    namespace T = sh::fast::tma;
+    const cudaFuncAttribute dyn = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    const int t1 = (int)T::smem_bytes(1, 6, 1024), t2 = (int)T::smem_bytes(2, 6, 1024);
+    fck(cudaFuncSetAttribute(T::axion_rkn4_tma_kernel<1, 0, false>, dyn, t1), "smem limit");
+    fck(cudaFuncSetAttribute(T::axion_rkn4_tma_kernel<1, 1, false>, dyn, t1), "smem limit");
+    fck(cudaFuncSetAttribute(T::axion_rkn4_tma_kernel<1, 2, false>, dyn, t1), "smem limit");
+    fck(cudaFuncSetAttribute(T::axion_rkn4_tma_kernel<1, 0, true>, dyn, t1), "smem limit");
+    fck(cudaFuncSetAttribute(T::axion_rkn4_tma_kernel<1, 1, true>, dyn, t1), "smem limit");
+    fck(cudaFuncSetAttribute(T::axion_rkn4_tma_kernel<1, 2, true>, dyn, t1), "smem limit");
+    fck(cudaFuncSetAttribute(T::axion_rkn4_tma_kernel<2, 0, false>, dyn, t2), "smem limit");
+    fck(cudaFuncSetAttribute(T::axion_rkn4_tma_kernel<2, 1, false>, dyn, t2), "smem limit");
+    fck(cudaFuncSetAttribute(T::axion_rkn4_tma_kernel<2, 2, false>, dyn, t2), "smem limit");
+    fck(cudaFuncSetAttribute(T::axion_rkn4_tma_kernel<2, 0, true>, dyn, t2), "smem limit");
+    fck(cudaFuncSetAttribute(T::axion_rkn4_tma_kernel<2, 1, true>, dyn, t2), "smem limit");
+    fck(cudaFuncSetAttribute(T::axion_rkn4_tma_kernel<2, 2, true>, dyn, t2), "smem limit");
     const int shf = 5 * 7 * (TY + 4) * (TX + 4) * (int)sizeof(float);
     const int shd = 5 * 7 * (TY + 4) * (TX + 4) * (int)sizeof(double);
     const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
@@ -957,12 +1123,33 @@ long long cells_of(const sh_ensemble *E, int r) {
     return (long long)E->desc[r].N * E->desc[r].N * E->desc[r].N;
 }
 
+/* A wait of a stage kernel that ran out (SH_ERR_TIMEOUT recorded on the
+ * device) is reported by the next call that synchronises; the flag is
+ * cleared then. */
+void check_device_error(sh_ensemble *E) {
+    int e = 0;
+    fck(cudaMemcpyAsync(&e, E->d_err, sizeof(int), cudaMemcpyDeviceToHost, est(E)),
+        "error flag download");
+    fck(cudaStreamSynchronize(est(E)), "error flag");
+    if (e != 0) {
+        fck(cudaMemsetAsync(E->d_err, 0, sizeof(int), est(E)), "error flag clear");
+        throw FastErr(e, "a stage kernel's wait for its tensor copies ran out; the state of "
+                         "the steps since the last check is not valid");
+    }
+}
+
 double read_time(sh_ensemble *E) {
     double t = 0.;
     fck(cudaMemcpyAsync(&t, E->d_time + E->slot, sizeof(double), cudaMemcpyDeviceToHost, est(E)),
         "time download");
     fck(cudaStreamSynchronize(est(E)), "time");
+    check_device_error(E);
     return t;
+}
+
+void alloc_error_flag(sh_ensemble *E) {
+    fck(cudaMalloc(&E->d_err, sizeof(int)), "error flag");
+    fck(cudaMemset(E->d_err, 0, sizeof(int)), "error flag clear");
 }
 
 } // namespace
@@ -1022,6 +1209,7 @@ int sh_ensemble_create(sh_ctx *ctx, int family, int precision, int nreal, const 
         fck(cudaMemset(E->d_time, 0, 2 * sizeof(double)), "time clear");
         fck(cudaMalloc(&E->d_counts, nreal * sizeof(unsigned long long)), "counts");
         E->counts_cap = nreal;
+        alloc_error_flag(E);
         build_tiles(E, 16);
     });
     if (rc != SH_OK) {
@@ -1041,6 +1229,9 @@ int sh_ensemble_destroy(sh_ensemble *E) {
         for (void *p : *v) cudaFree(p);
     cudaFree(E->d_desc);
     cudaFree(E->d_tiles);
+    cudaFree(E->d_ttiles);
+    cudaFree(E->d_maps);
+    cudaFree(E->d_err);
     cudaFree(E->d_time);
     cudaFree(E->d_partial);
     cudaFree(E->d_counts);
@@ -1127,6 +1318,7 @@ int sh_ensemble_read(sh_ensemble *E, int r, double *host) {
                 "download");
         }
         fck(cudaStreamSynchronize(s), "read");
+        check_device_error(E);
     });
 }
 
@@ -1144,6 +1336,43 @@ int sh_ensemble_step(sh_ensemble *E, double dt, int nsteps) {
         cudaStream_t s = est(E);
         for (int q = 0; q < nsteps; ++q) step_once(E, dt, s);
     });
+}
+
+int sh_ensemble_set_staging(sh_ensemble *E, int staging) {
+    if (!E || (staging != 0 && staging != 1)) return SH_ERR_ARG;
+    return fguard(E, [&] {
+        if (staging == 1 && !(tma_possible(E) && encode_tiled()))
+            throw FastErr(SH_ERR_UNSUPPORTED,
+                          "tensor-copy staging needs the axion family in FP32 storage with "
+                          "every realisation's N a multiple of 4 and at most 256");
+        E->plane_staging = staging;
+        build_tiles(E, E->tile_nz);
+    });
+}
+
+int sh_ensemble_staging(const sh_ensemble *E, int *staging) {
+    if (!E || !staging) return SH_ERR_ARG;
+    *staging = E->plane_staging;
+    return SH_OK;
+}
+
+int sh_probe_wait_timeout(int device, int *status) {
+    if (!status) return SH_ERR_ARG;
+    *status = SH_OK;
+    if (cudaSetDevice(device) != cudaSuccess) return SH_ERR_CUDA;
+    int *d = nullptr;
+    if (cudaMalloc(&d, sizeof(int)) != cudaSuccess) return SH_ERR_NOMEM;
+    int h = -1;
+    cudaError_t e = cudaMemset(d, 0xFF, sizeof(int));
+    if (e == cudaSuccess) {
+        sh::fast::tma::wait_timeout_probe_kernel<<<1, 32>>>(d, 2000000ull); /* 2 ms */
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return SH_ERR_CUDA;
+    *status = h;
+    return SH_OK;
 }
 
 int sh_ensemble_tune(sh_ensemble *E, int tile_nz, double dt, int *chosen) {
@@ -1174,24 +1403,34 @@ int sh_ensemble_tune(sh_ensemble *E, int tile_nz, double dt, int *chosen) {
                 fck(cudaEventCreate(&ev[0]), "event");
                 fck(cudaEventCreate(&ev[1]), "event");
                 float best = 1e30f;
-                int bestnz = E->tile_nz;
-                for (int nz : kTuneCandidates) {
-                    build_tiles(E, nz);
-                    step_dispatch(E, E->A, E->B, E->slot, dt, s); /* warm-up */
-                    fck(cudaEventRecord(ev[0], s), "record");
-                    for (int rep = 0; rep < 3; ++rep) step_dispatch(E, E->A, E->B, E->slot, dt, s);
-                    fck(cudaEventRecord(ev[1], s), "record");
-                    fck(cudaEventSynchronize(ev[1]), "tune");
-                    E->launches += 4 * launches_per_step(E);
-                    float ms = 0.f;
-                    cudaEventElapsedTime(&ms, ev[0], ev[1]);
-                    if (ms < best) {
-                        best = ms;
-                        bestnz = nz;
+                int bestnz = E->tile_nz, best_staging = E->plane_staging;
+                /* two dimensions: the stencil-plane staging (registers, or
+                 * tensor copies where the ensemble allows them) and the
+                 * planes per tile */
+                const int nstaging = tma_possible(E) && encode_tiled() ? 2 : 1;
+                for (int stg = 0; stg < nstaging; ++stg)
+                    for (int nz : kTuneCandidates) {
+                        E->plane_staging = stg;
+                        build_tiles(E, nz);
+                        step_dispatch(E, E->A, E->B, E->slot, dt, s); /* warm-up */
+                        fck(cudaEventRecord(ev[0], s), "record");
+                        for (int rep = 0; rep < 3; ++rep)
+                            step_dispatch(E, E->A, E->B, E->slot, dt, s);
+                        fck(cudaEventRecord(ev[1], s), "record");
+                        fck(cudaEventSynchronize(ev[1]), "tune");
+                        E->launches += 4 * launches_per_step(E);
+                        float ms = 0.f;
+                        cudaEventElapsedTime(&ms, ev[0], ev[1]);
+                        if (ms < best) {
+                            best = ms;
+                            bestnz = nz;
+                            best_staging = stg;
+                        }
                     }
-                }
                 cudaEventDestroy(ev[0]);
                 cudaEventDestroy(ev[1]);
+                check_device_error(E);
+                E->plane_staging = best_staging;
                 build_tiles(E, bestnz);
                 for (size_t q = 0; q < saved.size(); ++q)
                     fck(cudaMemcpyAsync(E->C[q], saved[q], bytes, cudaMemcpyDeviceToDevice, s),
@@ -1275,6 +1514,7 @@ int sh_ensemble_string_count(sh_ensemble *E, long long *counts) {
                             cudaMemcpyDeviceToHost, s),
             "counts download");
         fck(cudaStreamSynchronize(s), "string count");
+        check_device_error(E);
         for (int r = 0; r < E->nreal; ++r) counts[r] = (long long)c[r];
     });
 }
@@ -1414,6 +1654,7 @@ int sh_ensemble_create_pool(sh_ctx *ctx, int family, int precision, long long ca
         E->free_ext[0] = capacity_cells;
         fck(cudaMalloc(&E->d_time, 2 * sizeof(double)), "time");
         fck(cudaMemset(E->d_time, 0, 2 * sizeof(double)), "time clear");
+        alloc_error_flag(E);
     });
     if (rc != SH_OK) {
         sh_ensemble_destroy(E);

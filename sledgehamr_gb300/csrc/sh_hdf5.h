@@ -399,6 +399,154 @@ inline std::vector<unsigned char> Writer::metadata(std::vector<uint64_t> *data_a
     return im.data();
 }
 
+/* Reader of the files this writer produces (the structures listed at the
+ * top: superblock version 0, a root group of version-1 B-tree nodes over
+ * symbol-table nodes with a local heap of names, version-1 object headers
+ * with dataspace, datatype and contiguous layout messages): every 1-D
+ * F32LE or F64LE dataset of the root group, by name.  Other structures are
+ * rejected with a message.  Used to restart from checkpoint headers. */
+class Reader {
+  public:
+    bool open(const std::string &path, std::string *err) {
+        FILE *f = std::fopen(path.c_str(), "rb");
+        if (!f) return fail(err, "cannot open " + path);
+        std::fseek(f, 0, SEEK_END);
+        const long n = std::ftell(f);
+        std::fseek(f, 0, SEEK_SET);
+        buf_.assign(n > 0 ? (size_t)n : 0, 0);
+        const bool ok = n > 0 && std::fread(buf_.data(), 1, buf_.size(), f) == buf_.size();
+        std::fclose(f);
+        if (!ok) return fail(err, "cannot read " + path);
+        static const unsigned char sig[8] = {0x89, 'H', 'D', 'F', '\r', '\n', 0x1a, '\n'};
+        if (buf_.size() < kSuperblockBytes || std::memcmp(buf_.data(), sig, 8) != 0 ||
+            buf_[8] != 0 || buf_[13] != 8 || buf_[14] != 8)
+            return fail(err, path + ": not an HDF5 file with a version-0 superblock");
+        uint64_t btree = 0, heap = 0;
+        if (!u64(80, &btree) || !u64(88, &heap)) return fail(err, path + ": truncated");
+        uint64_t heap_data = 0;
+        if (!has(heap, 32) || std::memcmp(&buf_[heap], "HEAP", 4) != 0 ||
+            !u64(heap + 24, &heap_data))
+            return fail(err, path + ": no local heap of the root group");
+        heap_data_ = heap_data;
+        sets_.clear();
+        if (!walk(btree, 0, err)) return false;
+        return true;
+    }
+    bool has_dataset(const std::string &name) const { return sets_.count(name) != 0; }
+    /* values of dataset `name` as FP64 (F32 data widened) */
+    bool get(const std::string &name, std::vector<double> *out, std::string *err) const {
+        auto it = sets_.find(name);
+        if (it == sets_.end()) return fail(err, "no dataset " + name);
+        const Entry &e = it->second;
+        out->resize(e.n);
+        if (e.n == 0) return true;
+        if (!has(e.addr, e.n * (uint64_t)e.type)) return fail(err, name + ": data out of file");
+        for (uint64_t q = 0; q < e.n; ++q) {
+            if (e.type == kF64) {
+                double v;
+                std::memcpy(&v, &buf_[e.addr + 8 * q], 8);
+                (*out)[q] = v;
+            } else {
+                float v;
+                std::memcpy(&v, &buf_[e.addr + 4 * q], 4);
+                (*out)[q] = v;
+            }
+        }
+        return true;
+    }
+
+  private:
+    struct Entry {
+        int type = kF64;
+        uint64_t n = 0, addr = 0;
+    };
+    static bool fail(std::string *err, const std::string &m) {
+        if (err) *err = m;
+        return false;
+    }
+    bool has(uint64_t at, uint64_t n) const { return at <= buf_.size() && n <= buf_.size() - at; }
+    bool u64(uint64_t at, uint64_t *v) const {
+        if (!has(at, 8)) return false;
+        uint64_t x = 0;
+        for (int q = 7; q >= 0; --q) x = (x << 8) | buf_[at + q];
+        *v = x;
+        return true;
+    }
+    uint64_t un(uint64_t at, int n) const {
+        uint64_t x = 0;
+        for (int q = n - 1; q >= 0; --q) x = (x << 8) | buf_[at + q];
+        return x;
+    }
+    bool walk(uint64_t node, int depth, std::string *err) {
+        if (depth > 16 || !has(node, 24)) return fail(err, "bad group B-tree node");
+        if (std::memcmp(&buf_[node], "TREE", 4) == 0) {
+            if (buf_[node + 4] != 0) return fail(err, "not a group B-tree");
+            const unsigned used = (unsigned)un(node + 6, 2);
+            for (unsigned c = 0; c < used; ++c) {
+                uint64_t child = 0;
+                if (!u64(node + 24 + 8 + 16 * c, &child)) return fail(err, "truncated B-tree");
+                if (!walk(child, depth + 1, err)) return false;
+            }
+            return true;
+        }
+        if (std::memcmp(&buf_[node], "SNOD", 4) == 0) {
+            const unsigned n = (unsigned)un(node + 6, 2);
+            for (unsigned q = 0; q < n; ++q) {
+                const uint64_t e = node + 8 + 40 * q;
+                uint64_t name_off = 0, hdr = 0;
+                if (!u64(e, &name_off) || !u64(e + 8, &hdr)) return fail(err, "truncated SNOD");
+                const uint64_t at = heap_data_ + name_off;
+                std::string name;
+                while (has(at + name.size(), 1) && buf_[at + name.size()] != 0)
+                    name.push_back((char)buf_[at + name.size()]);
+                if (!dataset(name, hdr, err)) return false;
+            }
+            return true;
+        }
+        return fail(err, "unknown group node");
+    }
+    bool dataset(const std::string &name, uint64_t h, std::string *err) {
+        if (!has(h, 16) || buf_[h] != 1) return fail(err, name + ": not a version-1 object header");
+        const unsigned nmsg = (unsigned)un(h + 2, 2);
+        const uint64_t size = un(h + 8, 4);
+        uint64_t m = h + 16;
+        const uint64_t end = h + 16 + size;
+        if (!has(h + 16, size)) return fail(err, name + ": truncated object header");
+        Entry e;
+        bool space = false, type = false, layout = false;
+        for (unsigned q = 0; q < nmsg && m + 8 <= end; ++q) {
+            const unsigned mt = (unsigned)un(m, 2), ms = (unsigned)un(m + 2, 2);
+            const uint64_t d = m + 8;
+            if (mt == 0x01) { /* dataspace */
+                const unsigned ver = buf_[d], rank = buf_[d + 1];
+                if (rank != 1) return fail(err, name + ": not one-dimensional");
+                e.n = un(d + (ver == 1 ? 8 : 4), 8);
+                space = true;
+            } else if (mt == 0x03) { /* datatype */
+                if ((buf_[d] & 0x0F) != 1) return fail(err, name + ": not a floating-point type");
+                const uint64_t sz = un(d + 4, 4);
+                if (sz != 4 && sz != 8) return fail(err, name + ": float size");
+                if (buf_[d + 1] & 1) return fail(err, name + ": big-endian data");
+                e.type = (int)sz;
+                type = true;
+            } else if (mt == 0x08) { /* data layout */
+                if (buf_[d] != 3 || buf_[d + 1] != 1)
+                    return fail(err, name + ": not a version-3 contiguous layout");
+                e.addr = un(d + 2, 8);
+                layout = true;
+            }
+            m = d + ms;
+        }
+        if (!space || !type || !layout) return fail(err, name + ": incomplete dataset header");
+        if (e.n == 0) e.addr = 0;
+        sets_[name] = e;
+        return true;
+    }
+    std::vector<unsigned char> buf_;
+    uint64_t heap_data_ = 0;
+    std::map<std::string, Entry> sets_;
+};
+
 } // namespace h5
 } // namespace sh
 

@@ -192,6 +192,34 @@ class OracleAmr:
         self.lib.orc_amr_info(self.h, C.byref(f), C.byref(cu), C.byref(nr))
         return {"finest": f.value, "cell_updates": cu.value, "nregrids": nr.value}
 
+    @classmethod
+    def restart(cls, cfg, folder):
+        """A hierarchy from a checkpoint folder (orc_amr_restart)."""
+        build_oracle()
+        self = cls.__new__(cls)
+        self.lib = C.CDLL(ORACLE_SO)
+        self.lib.orc_amr_restart.restype = C.c_void_p
+        self.lib.orc_amr_restart.argtypes = [C.c_void_p, C.c_char_p]
+        for n in ("orc_amr_step", "orc_amr_info", "orc_amr_boxes", "orc_amr_read",
+                  "orc_amr_regrid_record"):
+            getattr(self.lib, n).restype = C.c_int
+        self.lib.orc_amr_destroy.argtypes = [C.c_void_p]
+        h = self.lib.orc_amr_restart(C.byref(cfg), str(folder).encode())
+        if not h:
+            raise RuntimeError("orc_amr_restart failed")
+        self.h = C.c_void_p(h)
+        self.N0 = cfg.N0
+        from tests import hdf5_read
+        self.ncomp = int(hdf5_read.File(os.path.join(str(folder), "Meta.hdf5"))["Header"][5])
+        return self
+
+    def checkpoint(self, folder):
+        f = self.lib.orc_amr_checkpoint
+        f.restype = C.c_int
+        f.argtypes = [C.c_void_p, C.c_char_p]
+        if f(self.h, str(folder).encode()) != 0:
+            raise RuntimeError("orc_amr_checkpoint failed")
+
     def set_trace(self, on=True):
         self.lib.orc_amr_set_trace.restype = C.c_int
         self.lib.orc_amr_set_trace(self.h, int(on))

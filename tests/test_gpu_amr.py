@@ -148,3 +148,30 @@ def test_amr_operation_order_equals_known_answer(ctx):
     assert g.info()["finest"] == 2
     assert g.trace() == KAT
     g.close()
+
+
+def test_checkpoint_restart_on_gpu_and_in_the_oracle(ctx, tmp_path):
+    """A GPU hierarchy checkpointed after 3 coarse steps (sh_amr_checkpoint)
+    and restarted (sh_amr_restart) continues bit for bit like the hierarchy
+    that did not stop; the oracle restarted from the same folder takes the
+    same regrid decisions and stays within 1e-12 of it."""
+    cfg = dict(record_regrids=0)
+    g = sh.Amr(ctx, config(**cfg), level0(3))
+    g.step(3)
+    assert g.info()["finest"] >= 1
+    g.checkpoint(str(tmp_path))
+    r = sh.Amr.restart(ctx, config(**cfg), str(tmp_path))
+    o = OracleAmr.restart(config(**cfg), tmp_path)
+    for _ in range(3):
+        g.step(1)
+        r.step(1)
+        o.step(1)
+    assert g.info() == r.info() == o.info()
+    for lev in range(g.info()["finest"] + 1):
+        assert g.level(lev).boxes == r.level(lev).boxes == o.boxes(lev)
+        gd = g.level(lev).read()
+        assert np.array_equal(gd, r.level(lev).read())
+        assert rel_l2(gd, o.read(lev)[0]) <= 1e-12
+    g.close()
+    r.close()
+    o.close()
