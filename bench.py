@@ -775,6 +775,23 @@ def run_case(name):
                 rows.append((lev, v.nvalid, tiles))
             print("step", q, rows, flush=True)
         sim.close()
+    elif name == "gw384":
+        # the GW spectrum of a 384^3 FOPT + GW level (FP64, binned and
+        # unbinned, each twice: the second call of each kind is warm)
+        N = 384
+        lv = sh.Level.periodic(ctx, "FirstOrderPhaseTransition", N, 2, max_grid=128,
+                               with_gw=True)
+        st = np.zeros((14, N, N, N))
+        for q in range(6):
+            st[8 + q] = 1e-3 * ic.gaussian_field(N, N * 0.25, 2.0, 40 + q)
+        lv.write(st)
+        del st
+        for ub in (False, True, False, True):
+            t0 = time.perf_counter()
+            lv.gw_spectrum(zero_padding=1, projection_type=2, unbinned=ub)
+            print("gw spectrum", "unbinned" if ub else "binned",
+                  f"{1e3 * (time.perf_counter() - t0):.1f} ms", flush=True)
+        lv.close()
     elif name == "single":
         s = SINGLE
         lv = sh.Level.periodic(ctx, s["project"], s["N"], s["nghost"])
@@ -950,7 +967,7 @@ def main():
     ap.add_argument("--serve-max-n", type=int, default=SERVE["max_n"])
     ap.add_argument("--case", default=None,
                     help="run one small profiling case and exit: axion-fp32k, axion-fp64, "
-                         "fopt-fp32k, amr, amr128, single, fp64-peak")
+                         "fopt-fp32k, amr, amr128, single, gw384, fp64-peak")
     args = ap.parse_args()
     if args.case:
         run_case(args.case)

@@ -20,3 +20,14 @@ ${CXX:-g++} -std=c++17 -O2 -ffp-contract=off -fPIC -shared -fopenmp \
     -I"$HERE/ref_shim" -I"$REF/source/utils" -I"$REF/source" -I"$REF/projects" -I"$HERE" \
     "$HERE/ref_harness.cpp" -o "$HERE/_ref/libshref.so"
 echo "built $HERE/_ref/libshref.so"
+# the reference's integrators (rkn.cpp, lsssprk3.cpp, leapfrog.cpp) compiled
+# unchanged against the AMReX stand-in of ref_shim_int, driven by
+# ref_integrators.cpp with the Rhs of libshref.so
+${CXX:-g++} -std=c++17 -O2 -ffp-contract=off -fPIC -shared \
+    -include "$HERE/ref_shim/ref_prelude.h" \
+    -I"$HERE/ref_shim_int" -I"$REF/source/integrators" -I"$REF/source" -I"$REF/source/utils" \
+    "$HERE/ref_integrators.cpp" "$REF/source/integrators/rkn.cpp" \
+    "$REF/source/integrators/lsssprk3.cpp" "$REF/source/integrators/leapfrog.cpp" \
+    -L"$HERE/_ref" -lshref -Wl,-rpath,'$ORIGIN' -Wl,--no-undefined \
+    -o "$HERE/_ref/libshref_int.so"
+echo "built $HERE/_ref/libshref_int.so"

@@ -280,6 +280,26 @@ int ORC_API(index_to_k)(int N, int projection_type, double *out) {
     return 0;
 }
 
+/* The TT projector contraction weights Lambda_ijlm of every k-cell of a
+ * P^3 R2C grid ((P/2+1) x P x P cells, a fastest), 81 per cell in (i, j, l,
+ * m) order, with the k-map of projection_type (the oracle's gw_lambda). */
+int ORC_API(gw_lambda_table)(int P, int projection_type, double *out) {
+    auto itk = orc::index_to_k(P, projection_type);
+    const int H = P / 2 + 1;
+    size_t q = 0;
+    for (int c = 0; c < P; ++c)
+        for (int b = 0; b < P; ++b)
+            for (int a = 0; a < H; ++a) {
+                int abc[3] = {a, b, c};
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j)
+                        for (int l = 0; l < 3; ++l)
+                            for (int m = 0; m < 3; ++m)
+                                out[q++] = orc::gw_lambda(i, j, l, m, abc, itk.data());
+            }
+    return 0;
+}
+
 } /* extern "C" */
 
 #endif // SH_ORACLE_CAPI_BODY_H_

@@ -74,12 +74,74 @@ struct AxionArgs {
 
 __device__ __forceinline__ int wrap(int a, int N) { return a < 0 ? a + N : (a >= N ? a - N : a); }
 
+/* FP32 arithmetic of the axion stage kernels with every operation rounded
+ * on its own (no contraction into fused multiply-adds), so that the
+ * register-pipelined and the tensor-copy kernels, which share these
+ * functions, give bit-identical results whatever the compiler fuses in its
+ * surroundings. */
+namespace f32 {
+__device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+/* stage position y + cm y' + ck K */
+__device__ __forceinline__ float stage_pos(float y, float m, float k, float cm, float ck) {
+    return add(y, add(mul(cm, m), mul(ck, k)));
+}
+/* 7-point Laplacian from the centre and the six neighbours (x+, x-, y+,
+ * y-, z+, z-) */
+__device__ __forceinline__ float lap7(float c, float xp, float xm, float yp, float ym, float zp,
+                                      float zm, float inv_dx2) {
+    float s = add(xp, xm);
+    s = add(s, add(yp, ym));
+    s = add(s, add(zp, zm));
+    return mul(sub(s, mul(6.f, c)), inv_dx2);
+}
+/* 13-point Laplacian: s1 and s2 the sums of the first and second rings */
+__device__ __forceinline__ float lap13(float c, float s1, float s2, float inv12dx2) {
+    return mul(sub(sub(mul(16.f, s1), s2), mul(90.f, c)), inv12dx2);
+}
+/* sum of a ring: (x+, x-), (y+, y-), (z+, z-) */
+__device__ __forceinline__ float ring(float xp, float xm, float yp, float ym, float zp,
+                                      float zm) {
+    float s = add(xp, xm);
+    s = add(s, add(yp, ym));
+    return add(s, add(zp, zm));
+}
+/* lambda (eta^2 (|Psi|^2 - 1) + c) */
+__device__ __forceinline__ float potential(float p0, float p1, float lam, float eta2, float cst) {
+    return mul(lam, add(mul(eta2, sub(add(mul(p0, p0), mul(p1, p1)), 1.f)), cst));
+}
+/* friction Pi + lap - Psi v */
+__device__ __forceinline__ float accel(float q, float lap, float p, float v, float friction) {
+    return sub(add(mul(friction, q), lap), mul(p, v));
+}
+/* RKN4 final increments: position h y0' + h^2 (K0/6 + K1/3), momentum
+ * h ((K0 + K2)/6 + 2 K1/3) */
+__device__ __forceinline__ float dpos(float q, float ka, float kb, float h, float h2) {
+    return add(mul(h, q), mul(h2, add(mul(ka, 1.f / 6.f), mul(kb, 1.f / 3.f))));
+}
+__device__ __forceinline__ float dmom(float ka, float kb, float k, float h) {
+    return mul(h, add(mul(add(ka, k), 1.f / 6.f), mul(kb, 2.f / 3.f)));
+}
+/* compensated y += d (c holds minus the lost low part) */
+__device__ __forceinline__ void kahan(float &y, float d, float &c) {
+    const float v = sub(d, c);
+    const float t = add(y, v);
+    c = sub(sub(t, y), v);
+    y = t;
+}
+} // namespace f32
+
 template <class R>
 __device__ __forceinline__ void kahan_add(R &y, R d, R &c) {
-    const R v = d - c;
-    const R t = y + v;
-    c = (t - y) - v;
-    y = t;
+    if constexpr (sizeof(R) == 4) {
+        f32::kahan(y, d, c);
+    } else {
+        const R v = d - c;
+        const R t = y + v;
+        c = (t - y) - v;
+        y = t;
+    }
 }
 
 /* RKN4 stage kernel for the axion family.  ORDER: Laplacian order (1: 7
@@ -172,8 +234,13 @@ __global__ void __launch_bounds__(TX *TY, sizeof(R) == 4 ? 5 : 1) axion_rkn4_ker
             if (ppos[q] < 0) continue;
             R v0 = raw[q][0], v1 = raw[q][1];
             if (STAGE > 0) {
-                v0 += cm * raw[q][2] + ck * raw[q][4];
-                v1 += cm * raw[q][3] + ck * raw[q][5];
+                if constexpr (sizeof(R) == 4) {
+                    v0 = f32::stage_pos(v0, raw[q][2], raw[q][4], cm, ck);
+                    v1 = f32::stage_pos(v1, raw[q][3], raw[q][5], cm, ck);
+                } else {
+                    v0 += cm * raw[q][2] + ck * raw[q][4];
+                    v1 += cm * raw[q][3] + ck * raw[q][5];
+                }
             }
             const int px = ppos[q] % W, py = ppos[q] / W;
             ring[slot][0][py][px] = v0;
@@ -242,37 +309,54 @@ __global__ void __launch_bounds__(TX *TY, sizeof(R) == 4 ? 5 : 1) axion_rkn4_ker
                         lap[c] = fx::weighted_sum<13, 3, -2>(r2, n, w, inv12dx2);
                     }
                 } else if (ORDER == 1) {
-                    R s = ring[sc][c][ty + H][tx + H + 1] + ring[sc][c][ty + H][tx + H - 1];
-                    s += ring[sc][c][ty + H + 1][tx + H] + ring[sc][c][ty + H - 1][tx + H];
-                    s += ring[(sc + 1) % RING][c][ty + H][tx + H] +
-                         ring[(sc + RING - 1) % RING][c][ty + H][tx + H];
-                    lap[c] = (s - (R)6 * u0) * inv_dx2;
+                    lap[c] = f32::lap7(
+                        u0, ring[sc][c][ty + H][tx + H + 1], ring[sc][c][ty + H][tx + H - 1],
+                        ring[sc][c][ty + H + 1][tx + H], ring[sc][c][ty + H - 1][tx + H],
+                        ring[(sc + 1) % RING][c][ty + H][tx + H],
+                        ring[(sc + RING - 1) % RING][c][ty + H][tx + H], inv_dx2);
                 } else {
-                    R s1 = ring[sc][c][ty + H][tx + H + 1] + ring[sc][c][ty + H][tx + H - 1];
-                    s1 += ring[sc][c][ty + H + 1][tx + H] + ring[sc][c][ty + H - 1][tx + H];
-                    s1 += ring[(sc + 1) % RING][c][ty + H][tx + H] +
-                          ring[(sc + RING - 1) % RING][c][ty + H][tx + H];
-                    R s2 = ring[sc][c][ty + H][tx + H + 2] + ring[sc][c][ty + H][tx + H - 2];
-                    s2 += ring[sc][c][ty + H + 2][tx + H] + ring[sc][c][ty + H - 2][tx + H];
-                    s2 += ring[(sc + 2) % RING][c][ty + H][tx + H] +
-                          ring[(sc + RING - 2) % RING][c][ty + H][tx + H];
-                    lap[c] = ((R)16 * s1 - s2 - (R)90 * u0) * inv12dx2;
+                    const R s1 = f32::ring(
+                        ring[sc][c][ty + H][tx + H + 1], ring[sc][c][ty + H][tx + H - 1],
+                        ring[sc][c][ty + H + 1][tx + H], ring[sc][c][ty + H - 1][tx + H],
+                        ring[(sc + 1) % RING][c][ty + H][tx + H],
+                        ring[(sc + RING - 1) % RING][c][ty + H][tx + H]);
+                    const R s2 = f32::ring(
+                        ring[sc][c][ty + H][tx + H + 2], ring[sc][c][ty + H][tx + H - 2],
+                        ring[sc][c][ty + H + 2][tx + H], ring[sc][c][ty + H - 2][tx + H],
+                        ring[(sc + 2) % RING][c][ty + H][tx + H],
+                        ring[(sc + RING - 2) % RING][c][ty + H][tx + H]);
+                    lap[c] = f32::lap13(u0, s1, s2, inv12dx2);
                 }
             }
             const R p0 = ring[sc][0][ty + H][tx + H], p1 = ring[sc][1][ty + H][tx + H];
-            const R v = lam * (eta2 * (p0 * p0 + p1 * p1 - (R)1) + cst);
-            const R k0 = friction * q0 + lap[0] - p0 * v;
-            const R k1 = friction * q1 + lap[1] - p1 * v;
+            R k0, k1;
+            if constexpr (sizeof(R) == 4) {
+                const float v = f32::potential(p0, p1, lam, eta2, cst);
+                k0 = f32::accel(q0, lap[0], p0, v, friction);
+                k1 = f32::accel(q1, lap[1], p1, v, friction);
+            } else {
+                const R v = lam * (eta2 * (p0 * p0 + p1 * p1 - (R)1) + cst);
+                k0 = friction * q0 + lap[0] - p0 * v;
+                k1 = friction * q1 + lap[1] - p1 * v;
+            }
             if (STAGE < 2) {
                 a.K[STAGE][0][e] = k0;
                 a.K[STAGE][1][e] = k1;
             } else {
                 const R h = kc[8], h2 = kc[9];
                 /* y1 = y0 + h y0' + h^2 (K0/6 + K1/3); y1' = y0' + h (K0/6 + 2K1/3 + K2/6) */
-                const R dy0 = h * q0 + h2 * (ka0 * (R)(1. / 6.) + kb0 * (R)(1. / 3.));
-                const R dy1 = h * q1 + h2 * (ka1 * (R)(1. / 6.) + kb1 * (R)(1. / 3.));
-                const R dm0 = h * ((ka0 + k0) * (R)(1. / 6.) + kb0 * (R)(2. / 3.));
-                const R dm1 = h * ((ka1 + k1) * (R)(1. / 6.) + kb1 * (R)(2. / 3.));
+                R dy0, dy1, dm0, dm1;
+                if constexpr (sizeof(R) == 4) {
+                    dy0 = f32::dpos(q0, ka0, kb0, h, h2);
+                    dy1 = f32::dpos(q1, ka1, kb1, h, h2);
+                    dm0 = f32::dmom(ka0, kb0, k0, h);
+                    dm1 = f32::dmom(ka1, kb1, k1, h);
+                } else {
+                    dy0 = h * q0 + h2 * (ka0 * (R)(1. / 6.) + kb0 * (R)(1. / 3.));
+                    dy1 = h * q1 + h2 * (ka1 * (R)(1. / 6.) + kb1 * (R)(1. / 3.));
+                    dm0 = h * ((ka0 + k0) * (R)(1. / 6.) + kb0 * (R)(2. / 3.));
+                    dm1 = h * ((ka1 + k1) * (R)(1. / 6.) + kb1 * (R)(2. / 3.));
+                }
                 R y0v = y0c, y1v = y1c, m0v = q0, m1v = q1;
                 if (KAHAN) {
                     kahan_add(y0v, dy0, c0);

@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(kThreads)
         kc[4] = (float)d.p[1];                                               /* c */
         kc[5] = (float)(ts * ts);                                            /* eta^2 */
         kc[6] = (float)(1. / (d.dx * d.dx));
-        kc[7] = (float)(1. / (12. * d.dx * d.dx));
+        kc[7] = kc[6] / 12.f; /* as the register-pipelined kernel forms it */
 #pragma unroll
         for (int q = 0; q < NA; ++q) {
             tensormap_acquire(mp[q][0]);
@@ -278,7 +278,9 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
                 for (int c = 0; c < 2; ++c) {
                     float v = rs[c * slab + o];
-                    if (STAGE > 0) v += cm * rs[(2 + c) * slab + o] + ck * rs[(4 + c) * slab + o];
+                    if (STAGE > 0)
+                        v = f32::stage_pos(v, rs[(2 + c) * slab + o], rs[(4 + c) * slab + o], cm,
+                                           ck);
                     ys[c * slab + o] = v;
                 }
             }
@@ -301,35 +303,34 @@ __global__ void __launch_bounds__(kThreads)
                 const float *ym1 = Yr + ((p - H - 1 + RING) % RING) * 2 * slab + c * slab;
                 const float u0 = y0p[o + x];
                 pc[c] = u0;
-                float s1 = y0p[o + xp] + y0p[o + xm];
-                s1 += y0p[o + P + x] + y0p[o - P + x];
-                s1 += yp1[o + x] + ym1[o + x];
                 if (H == 1) {
-                    lap[c] = (s1 - 6.f * u0) * inv_dx2;
+                    lap[c] = f32::lap7(u0, y0p[o + xp], y0p[o + xm], y0p[o + P + x],
+                                       y0p[o - P + x], yp1[o + x], ym1[o + x], inv_dx2);
                 } else {
                     const float *yp2 = Yr + ((p - H + 2) % RING) * 2 * slab + c * slab;
                     const float *ym2 = Yr + ((p - H - 2 + RING) % RING) * 2 * slab + c * slab;
                     const int xpp = xp + 1 < N ? xp + 1 : xp + 1 - N;
                     const int xmm = xm > 0 ? xm - 1 : xm - 1 + N;
-                    float s2 = y0p[o + xpp] + y0p[o + xmm];
-                    s2 += y0p[o + 2 * P + x] + y0p[o - 2 * P + x];
-                    s2 += yp2[o + x] + ym2[o + x];
-                    lap[c] = (16.f * s1 - s2 - 90.f * u0) * inv12dx2;
+                    const float s1 = f32::ring(y0p[o + xp], y0p[o + xm], y0p[o + P + x],
+                                               y0p[o - P + x], yp1[o + x], ym1[o + x]);
+                    const float s2 = f32::ring(y0p[o + xpp], y0p[o + xmm], y0p[o + 2 * P + x],
+                                               y0p[o - 2 * P + x], yp2[o + x], ym2[o + x]);
+                    lap[c] = f32::lap13(u0, s1, s2, inv12dx2);
                 }
             }
-            const float v = lam * (eta2 * (pc[0] * pc[0] + pc[1] * pc[1] - 1.f) + cst);
-            const float k0 = friction * q0[k] + lap[0] - pc[0] * v;
-            const float k1 = friction * q1[k] + lap[1] - pc[1] * v;
+            const float v = f32::potential(pc[0], pc[1], lam, eta2, cst);
+            const float k0 = f32::accel(q0[k], lap[0], pc[0], v, friction);
+            const float k1 = f32::accel(q1[k], lap[1], pc[1], v, friction);
             const long long e = off + ((long long)zc * N + tl.y0 + row) * N + x;
             if (STAGE < 2) {
                 a.K[STAGE][0][e] = k0;
                 a.K[STAGE][1][e] = k1;
             } else {
                 /* y1 = y0 + h y0' + h^2 (K0/6 + K1/3); y1' = y0' + h (K0/6 + 2K1/3 + K2/6) */
-                const float dy0 = h * q0[k] + h2 * (ka0[k] * (1.f / 6.f) + kb0[k] * (1.f / 3.f));
-                const float dy1 = h * q1[k] + h2 * (ka1[k] * (1.f / 6.f) + kb1[k] * (1.f / 3.f));
-                const float dm0 = h * ((ka0[k] + k0) * (1.f / 6.f) + kb0[k] * (2.f / 3.f));
-                const float dm1 = h * ((ka1[k] + k1) * (1.f / 6.f) + kb1[k] * (2.f / 3.f));
+                const float dy0 = f32::dpos(q0[k], ka0[k], kb0[k], h, h2);
+                const float dy1 = f32::dpos(q1[k], ka1[k], kb1[k], h, h2);
+                const float dm0 = f32::dmom(ka0[k], kb0[k], k0, h);
+                const float dm1 = f32::dmom(ka1[k], kb1[k], k1, h);
                 float y0v = yc0[k], y1v = yc1[k], m0v = q0[k], m1v = q1[k];
                 if (KAHAN) {
                     kahan_add(y0v, dy0, c0[k]);

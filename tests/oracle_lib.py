@@ -37,8 +37,35 @@ def build_oracle():
         subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
 
 
+REF_INT_SO = os.path.join(ROOT, "oracle", "_ref", "libshref_int.so")
+
+
 def ref_available() -> bool:
     return os.path.exists(REF_SO)
+
+
+def ref_integrators_available() -> bool:
+    return os.path.exists(REF_INT_SO)
+
+
+def ref_int_evolve(project, integrator, state, t0, dt, dx, nsteps, params=(), gw_params=(),
+                   with_gw=False, nghost=2):
+    """nsteps steps of a periodic level by the reference's own integrators
+    (rkn.cpp, lsssprk3.cpp, leapfrog.cpp compiled unchanged into
+    oracle/_ref/libshref_int.so) with the reference's per-cell Rhs."""
+    lib = C.CDLL(REF_INT_SO)
+    f = lib.ref_int_evolve
+    f.restype = C.c_int
+    st = _f(state)
+    out = np.empty_like(st)
+    p = _f(list(params) or [0.0])
+    g = _f(list(gw_params) or [0.0])
+    rc = f(PROJECT_IDS[project], integrator, st.shape[-1], nghost, st.shape[0], int(with_gw),
+           _p(st), _p(out), C.c_double(t0), C.c_double(dt), C.c_double(dx), nsteps, _p(p),
+           len(params), _p(g), len(gw_params))
+    if rc != 0:
+        raise RuntimeError(f"ref_int_evolve rc={rc}")
+    return out
 
 
 class Oracle:

@@ -1,5 +1,8 @@
-"""The oracle's restatement against the reference's own per-cell code
-(oracle/_ref, compiled from the sledgehamr headers): bit-for-bit equality."""
+"""The oracle's restatement against the reference's own code (oracle/_ref,
+compiled from the sledgehamr sources): the per-cell headers, and the
+integrators rkn.cpp, lsssprk3.cpp and leapfrog.cpp themselves (their
+MultiFab Copy / Saxpy / LinComb sequences and FillIntermediatePatch calls
+over an AMReX stand-in): bit-for-bit equality."""
 import numpy as np
 import pytest
 
@@ -81,3 +84,53 @@ def test_avgdown_te_bitwise(oracle, ref):
     ref.lib.ref_avgdown_te_kernel(4, 4, C.c_void_p(fine.ctypes.data), C.c_void_p(c2.ctypes.data),
                                   C.c_void_p(t2.ctypes.data))
     assert np.array_equal(c1, c2) and np.array_equal(t1, t2)
+
+
+@pytest.mark.parametrize("project,integ", [("AxionStrings", 21), ("AxionStrings", 22),
+                                           ("AxionStrings", 11), ("AxionStrings", 10),
+                                           ("MinimalExample", 10), ("MinimalExample", 21)])
+def test_integrator_sequencing_equals_the_reference_integrators(oracle, project, integ):
+    from tests.oracle_lib import ref_int_evolve, ref_integrators_available
+    if not ref_integrators_available():
+        pytest.skip("oracle/_ref/libshref_int.so not built (sledgehamr sources absent)")
+    st = _axion_state()
+    kw = dict(t0=1.0, dt=0.0625, dx=0.25, nsteps=4, nghost=2)
+    assert np.array_equal(oracle.evolve_periodic(project, integ, st, **kw),
+                          ref_int_evolve(project, integ, st, **kw))
+
+
+@pytest.mark.parametrize("integ", [11, 21])
+def test_integrator_sequencing_with_gw_tensor_equals_the_reference(oracle, integ):
+    from tests.golden.make_golden import fopt_params
+    from tests.oracle_lib import ref_int_evolve, ref_integrators_available
+    if not ref_integrators_available():
+        pytest.skip("oracle/_ref/libshref_int.so not built (sledgehamr sources absent)")
+    s = np.zeros((14, 10, 10, 10))
+    s[0] = 0.8 * ic.gaussian_field(10, 2.5, 9.0, 1)
+    s[1] = 0.2 * ic.gaussian_field(10, 2.5, 9.0, 2)
+    s[2:8] = 0.05 * np.stack([ic.gaussian_field(10, 2.5, 9.0, 5 + q) for q in range(6)])
+    kw = dict(t0=0.0, dt=0.05, dx=0.25, nsteps=3, nghost=2, params=fopt_params(),
+              gw_params=[0.0, 1.0], with_gw=True)
+    assert np.array_equal(oracle.evolve_periodic("FirstOrderPhaseTransition", integ, s, **kw),
+                          ref_int_evolve("FirstOrderPhaseTransition", integ, s, **kw))
+
+
+@pytest.mark.parametrize("P,ptype", [(8, 2), (12, 1), (10, 3)])
+def test_gw_lambda_equals_the_reference_header(oracle, P, ptype):
+    """The oracle's Lambda_ijlm (gw_lambda) equals the reference's own
+    gw_GetLambda / gw_GetProjection (source/gravitational_waves.h:101-133,
+    compiled into oracle/_ref) on every k-cell and (i, j, l, m)."""
+    import ctypes as C
+
+    from tests.oracle_lib import ORACLE_SO, REF_INT_SO, ref_integrators_available
+    if not ref_integrators_available():
+        pytest.skip("oracle/_ref/libshref_int.so not built (sledgehamr sources absent)")
+    n = 81 * (P // 2 + 1) * P * P
+    a, b = np.empty(n), np.empty(n)
+    itk = oracle.index_to_k(P, ptype)
+    olib, rlib = C.CDLL(ORACLE_SO), C.CDLL(REF_INT_SO)
+    assert olib.orc_gw_lambda_table(P, ptype, C.c_void_p(a.ctypes.data)) == 0
+    assert rlib.ref_gw_lambda_table(P, C.c_void_p(itk.ctypes.data),
+                                    C.c_void_p(b.ctypes.data)) == 0
+    assert np.array_equal(a, b)
+    assert np.abs(a).max() > 0.5
