@@ -26,23 +26,41 @@
 
 /* ---- project registry --------------------------------------------------- */
 namespace sh {
-extern const ProjectOps project_AxionStrings;
-extern const ProjectOps project_MinimalExample;
-extern const ProjectOps project_NextToMinimalExample;
-extern const ProjectOps project_FirstOrderPhaseTransition;
-extern const ProjectOps project_AxionStringsLap1;
-extern const ProjectOps project_AxionStringsLap2;
-extern const ProjectOps project_AxionStringsLap3;
+namespace registry {
+std::vector<const ProjectOps *> &registered() {
+    static std::vector<const ProjectOps *> v; /* filled by static initialisers */
+    return v;
+}
+/* Ids: the built-in projects first, in the oracle's numbering; every other
+ * registered project after them in name order (so that ids do not depend
+ * on the order in which the linker runs the initialisers). */
+const std::vector<const ProjectOps *> &table() {
+    static const std::vector<const ProjectOps *> t = [] {
+        static const char *const kBuiltin[] = {
+            "AxionStrings",     "MinimalExample",   "NextToMinimalExample",
+            "FirstOrderPhaseTransition", "AxionStringsLap1", "AxionStringsLap2",
+            "AxionStringsLap3"};
+        std::vector<const ProjectOps *> reg = registered(), out;
+        for (const char *name : kBuiltin)
+            for (const ProjectOps *p : reg)
+                if (std::strcmp(p->name, name) == 0) out.push_back(p);
+        std::vector<const ProjectOps *> rest;
+        for (const ProjectOps *p : reg)
+            if (std::find(out.begin(), out.end(), p) == out.end()) rest.push_back(p);
+        std::sort(rest.begin(), rest.end(), [](const ProjectOps *a, const ProjectOps *b) {
+            return std::strcmp(a->name, b->name) < 0;
+        });
+        out.insert(out.end(), rest.begin(), rest.end());
+        return out;
+    }();
+    return t;
+}
+} // namespace registry
 
-/* Ids match the oracle's project numbering. */
-static const ProjectOps *const kProjects[] = {
-    &project_AxionStrings,   &project_MinimalExample,   &project_NextToMinimalExample,
-    &project_FirstOrderPhaseTransition, &project_AxionStringsLap1, &project_AxionStringsLap2,
-    &project_AxionStringsLap3};
-
-int project_count() { return (int)(sizeof(kProjects) / sizeof(kProjects[0])); }
+void register_project(const ProjectOps *p) { registry::registered().push_back(p); }
+int project_count() { return (int)registry::table().size(); }
 const ProjectOps *project_by_id(int id) {
-    return (id >= 0 && id < project_count()) ? kProjects[id] : nullptr;
+    return (id >= 0 && id < project_count()) ? registry::table()[id] : nullptr;
 }
 } // namespace sh
 

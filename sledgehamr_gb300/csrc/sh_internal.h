@@ -139,6 +139,14 @@ struct ProjectOps {
 const ProjectOps *project_by_id(int id);
 int project_count();
 
+/* Projects register themselves when the library loads (SH_DEFINE_PROJECT
+ * makes one of these per project translation unit), so that adding a
+ * project is adding its headers and one .cu file, without editing a list. */
+void register_project(const ProjectOps *p);
+struct ProjectRegistrar {
+    explicit ProjectRegistrar(const ProjectOps *p) { register_project(p); }
+};
+
 } // namespace sh
 
 #endif // SH_INTERNAL_H_

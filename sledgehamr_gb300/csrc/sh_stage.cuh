@@ -309,7 +309,8 @@ cudaError_t launch_tag_impl(const TagArgs &a, int ntiles, cudaStream_t s) {
 } // namespace sh
 
 /* Defines the ProjectOps table `sh::project_<NAME>` for the project namespace
- * NS (after its hooks and SLEDGEHAMR_FINISH_SETUP).  HAS_GW: the project
+ * NS (after its hooks and SLEDGEHAMR_FINISH_SETUP) and registers it with the
+ * library when it loads.  HAS_GW: the project
  * specialises GravitationalWavesRhs<true>; REACH: the largest neighbour
  * offset its hooks read (levels need at least that many ghost cells). */
 #define SH_DEFINE_PROJECT(NAME, NS, HAS_GW, REACH)                                    \
@@ -331,6 +332,7 @@ cudaError_t launch_tag_impl(const TagArgs &a, int ntiles, cudaStream_t s) {
         &field_name_##NAME,                                                    \
         &launch_stage_impl<Hooks_##NAME>,                                      \
         &launch_tag_impl<Hooks_##NAME>};                                       \
+    static const ProjectRegistrar registrar_##NAME(&project_##NAME);          \
     }
 
 #endif // SH_STAGE_CUH_
