@@ -78,7 +78,7 @@ SINGLE = dict(N=128, L=32.0, project="AxionStringsLap1", params=[1.0, 0.0], ngho
 AMR = dict(N0=256, L=64.0, project="AxionStringsLap2", params=[1.0, 0.0], nghost=2,
            t_start=0.1, cfl=0.25, max_level=2, blocking_factor=8, max_grid_size=32,
            n_error_buf=2, regrid_dt=0.25, te_crit=1e-3, string_width_threshold=1.5,
-           t_end=6.0)
+           t_end=6.0, max_local_regrids=0)
 
 
 def load_ic():
@@ -597,7 +597,8 @@ def amr_config(sh):
                          blocking_factor=a["blocking_factor"], max_grid_size=a["max_grid_size"],
                          n_error_buf=a["n_error_buf"], regrid_dt=a["regrid_dt"],
                          te_crit=[a["te_crit"]] * 4, params=a["params"],
-                         string_width_threshold=a["string_width_threshold"])
+                         string_width_threshold=a["string_width_threshold"],
+                         max_local_regrids=a["max_local_regrids"])
 
 
 def amr_state():
@@ -631,6 +632,7 @@ def amr_leg_config():
             "eta0": a["t_start"], "eta_end": a["t_end"],
             "string_width_threshold": a["string_width_threshold"],
             "regrid_dt": a["regrid_dt"], "n_error_buf": a["n_error_buf"],
+            "regrids": "global (amr.max_local_regrids = 0)",
             "project": a["project"], "integrator": "RKN4 (type 21)",
             "l2": "flushed between timed steps (512 MB write, outside events)"}
 

@@ -487,6 +487,19 @@ typedef struct sh_amr_config {
      * stops with SH_ERR_NONFINITE naming the level and component.  No
      * counterpart in the reference. */
     int check_finite;
+    /* LocalRegrid (source/local_regrid/local_regrid.cpp): before a global
+     * regrid, levels first grow by blocking-factor blocks next to their
+     * coarse/fine boundaries where tagged cells come closer than
+     * n_error_buf + 1 fine cells (lower levels growing to keep them
+     * nested), keeping every existing box; at most max_local_regrids times
+     * between global regrids (amr.max_local_regrids, 0: global regrids
+     * only), vetoed in favour of a global regrid when a level would exceed
+     * volume_threshold_weak times its volume at the last global regrid
+     * (amr.volume_threshold_weak; volume_threshold_strong picks the level
+     * to regrid globally). */
+    int max_local_regrids;
+    double volume_threshold_strong;
+    double volume_threshold_weak;
 } sh_amr_config;
 /* New-grid generation from the buffered tags (at blocking-factor
  * resolution): Berger-Rigoutsos clustering to efficiency grid_eff, then

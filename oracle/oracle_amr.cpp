@@ -233,6 +233,10 @@ struct CpuBackend {
     void remake(Level &fresh, Level &old, Level &c, double time) {
         fill_from(fresh->nw, &old->nw, time, c->od, c->nw);
     }
+    void extend(Level &fresh, Level &old, Level &c, double t_new, double t_old) {
+        fill_from(fresh->nw, &old->nw, t_new, c->od, c->nw);
+        fill_from(fresh->od, &old->od, t_old, c->od, c->nw);
+    }
     void refresh_ghosts(Level &l, int which, Level *coarse) {
         MF &m = buf(l, which);
         fill_two_level(m, m.t, coarse ? &(*coarse)->od : nullptr,
@@ -326,6 +330,9 @@ struct Amr : AmrBase {
         d.clustering = cfg.clustering;
         d.grid_eff = cfg.grid_eff;
         d.params_mod_norm0 = cfg.params_mod_norm0 != 0;
+        d.max_local_regrids = cfg.max_local_regrids;
+        d.volume_threshold_strong = cfg.volume_threshold_strong;
+        d.volume_threshold_weak = cfg.volume_threshold_weak;
         drv.reset(new shamr::Driver<CpuBackend<P>>(backend, d));
         drv->record_regrids = cfg.record_regrids != 0;
         const int N = cfg.N0;

@@ -63,7 +63,8 @@ class ShAmrConfig(C.Structure):
                 ("grid_eff", C.c_double), ("params_tag", C.c_double * 32),
                 ("nparams_tag", C.c_int), ("params_mod", C.c_double * 32),
                 ("nparams_mod", C.c_int), ("params_mod_norm0", C.c_int),
-                ("check_finite", C.c_int)]
+                ("check_finite", C.c_int), ("max_local_regrids", C.c_int),
+                ("volume_threshold_strong", C.c_double), ("volume_threshold_weak", C.c_double)]
 
 
 class ShRequest(C.Structure):

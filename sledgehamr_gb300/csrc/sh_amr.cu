@@ -126,6 +126,10 @@ struct GpuBackend {
     void remake(Level &fresh, Level &old, Level &c, double time) {
         ok(sh_level_fill_from(ctx, fresh->L, SH_NEW, old->L, SH_NEW, c->L, time), "remake");
     }
+    void extend(Level &fresh, Level &old, Level &c, double t_new, double t_old) {
+        ok(sh_level_fill_from(ctx, fresh->L, SH_NEW, old->L, SH_NEW, c->L, t_new), "extend");
+        ok(sh_level_fill_from(ctx, fresh->L, SH_OLD, old->L, SH_OLD, c->L, t_old), "extend");
+    }
     void refresh_ghosts(Level &l, int which, Level *coarse) {
         link(l, coarse ? *coarse : nullptr);
         ok(sh_level_fill_patch(ctx, l->L, which), "sh_level_fill_patch");
@@ -187,6 +191,9 @@ shamr::Config driver_config(const sh_amr_config &c, int ncomp) {
     d.clustering = c.clustering;
     d.grid_eff = c.grid_eff;
     d.params_mod_norm0 = c.params_mod_norm0 != 0;
+    d.max_local_regrids = c.max_local_regrids;
+    d.volume_threshold_strong = c.volume_threshold_strong;
+    d.volume_threshold_weak = c.volume_threshold_weak;
     return d;
 }
 
@@ -227,6 +234,10 @@ int sh_amr_config_defaults(sh_amr_config *c) {
     c->clustering = SH_CLUSTER_BR_WINDOWS;
     c->grid_eff = 0.7;
     for (int n = 0; n < 32; ++n) c->te_crit[n] = DBL_MAX;
+    /* LocalRegrid's defaults (local_regrid.h:97-122) */
+    c->max_local_regrids = 10;
+    c->volume_threshold_strong = 1.05;
+    c->volume_threshold_weak = 1.1;
     return SH_OK;
 }
 

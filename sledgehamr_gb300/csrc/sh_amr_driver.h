@@ -57,6 +57,9 @@
  *   void sync();   // wait for queued device work (timers with sync_timers)
  *   std::vector<double> read_valid(Level&, int which);   // boxes layout
  *   void write_valid(Level&, int which, const std::vector<double>&);
+ *   void extend(Level &fresh, Level &old, Level &crse, double t_new, double t_old);
+ *        // both time levels of fresh from old where old has cells, else
+ *        // from the coarse level at t_new / t_old (LocalRegrid::AddBoxes)
  */
 #ifndef SH_AMR_DRIVER_H_
 #define SH_AMR_DRIVER_H_
@@ -106,6 +109,11 @@ struct Config {
     int clustering = 0;         /* 0 Berger-Rigoutsos, 1 aligned windows */
     double grid_eff = 0.7;      /* minimum tagged fraction of a cluster */
     bool params_mod_norm0 = false; /* TruncationModifier params from level 0 */
+    /* LocalRegrid (source/local_regrid/local_regrid.h:97-122): attempts
+     * before a global regrid is forced, and the volume thresholds */
+    int max_local_regrids = 0;
+    double volume_threshold_strong = 1.05; /* amr.volume_threshold_strong */
+    double volume_threshold_weak = 1.1;    /* amr.volume_threshold_weak */
 };
 
 /* The whole state of a hierarchy between two coarse steps: what the
@@ -127,6 +135,12 @@ struct Checkpoint {
     std::vector<std::pair<int, double>> schedule; /* (lowest level, time) */
     std::vector<uint8_t> te_valid;
     long long cell_updates = 0;
+    /* LocalRegrid state: attempts since the last global regrid, per level
+     * the no-local / global-requested flags and the cells at the last
+     * global regrid */
+    int lr_nregrids = 0;
+    std::vector<uint8_t> lr_no_local, lr_do_global;
+    std::vector<long long> lr_last_numpts;
 };
 
 struct RegridRecord {
@@ -633,6 +647,10 @@ class Driver {
         for (const Sched &q : schedule) k.schedule.push_back({q.lowest, q.t});
         for (bool v : te_valid) k.te_valid.push_back(v ? 1 : 0);
         k.cell_updates = cell_updates;
+        k.lr_nregrids = lr_nregrids;
+        k.lr_no_local = lr_no_local;
+        k.lr_do_global = lr_do_global;
+        k.lr_last_numpts = lr_last_numpts;
         return k;
     }
 
@@ -668,6 +686,10 @@ class Driver {
         for (const auto &q : k.schedule) schedule.push_back(Sched{q.first, q.second});
         for (int l = 0; l <= c.max_level; ++l) te_valid[l] = k.te_valid[l] != 0;
         cell_updates = k.cell_updates;
+        lr_nregrids = k.lr_nregrids;
+        lr_no_local = k.lr_no_local;
+        lr_do_global = k.lr_do_global;
+        lr_last_numpts = k.lr_last_numpts;
     }
 
     /* ---- queries ---- */
@@ -842,7 +864,7 @@ class Driver {
         if (istep % 2 == 0 && lev > 0) return;
         const double next = lev > 0 ? time + 3. * dt[lev] : time + 2. * dt[lev];
         if (!create_level_if(lev + 1, next)) return;
-        if (next <= last_regrid_time[lev] + regrid_dt[lev]) return;
+        if (next <= last_regrid_time[lev] + regrid_dt[lev] && !lr_global_requested(lev)) return;
         if (lev == 0 && b.time(levels[0], kOld) == -DBL_MAX) return;
         schedule_regrid(lev, time + dt[lev]);
         note("schedule", lev, time + dt[lev]);
@@ -882,16 +904,335 @@ class Driver {
     void no_shadow_regrid(int lev) {
         const double time = tnew(lev);
         if (lev >= c.max_level) return;
-        if (time + dt[lev] <= last_regrid_time[lev] + regrid_dt[lev]) return;
+        if (time + dt[lev] <= last_regrid_time[lev] + regrid_dt[lev] && !lr_global_requested(lev))
+            return;
         if (!create_level_if(lev + 1, time + dt[lev])) return;
         do_regrid(lev, time);
     }
 
-    /* TimeStepper::DoRegrid with the global regrid path. */
+    /* TimeStepper::DoRegrid: a local regrid first, the global one if it
+     * does not succeed (time_stepper.cpp:346-397). */
     void do_regrid(int lev, double time) {
-        note("regrid", lev, time);
-        regrid(lev, time);
+        if (attempt_local_regrid(lev)) {
+            note("local_regrid", lev, time);
+        } else {
+            note("regrid", lev, time);
+            regrid(lev, time);
+            did_global_regrid(lev);
+        }
         for (int l = lev; l <= finest; ++l) last_regrid_time[l] = time;
+    }
+
+    /* ---- LocalRegrid (source/local_regrid/local_regrid.cpp) ----
+     * Levels grow by blocking-factor blocks next to their coarse/fine
+     * boundaries where tagged cells of the level below come closer than
+     * n_error_buf + 1 fine cells, lower levels grow to keep them nested, and
+     * the hierarchy keeps every existing box; volume thresholds veto it in
+     * favour of a global regrid (now, or at the next opportunity of the
+     * level that asked for it). */
+    std::vector<uint8_t> lr_no_local, lr_do_global;
+    std::vector<long long> lr_last_numpts;
+    int lr_nregrids = 0, lr_veto_level = -1;
+
+    bool lr_global_requested(int lev) const {
+        return lev < (int)lr_do_global.size() && lr_do_global[lev];
+    }
+    long long level_cells(int l) const {
+        long long n = 0;
+        for (const IBox &x : boxes[l]) n += x.volume();
+        return n;
+    }
+    /* LocalRegrid::DidGlobalRegrid */
+    void did_global_regrid(int lev) {
+        lr_no_local.assign(c.max_level + 1, 0);
+        lr_do_global.assign(c.max_level + 1, 0);
+        lr_nregrids = 0;
+        for (int l = lev + 1; l < (int)lr_last_numpts.size(); ++l)
+            lr_last_numpts[l] = l <= finest ? level_cells(l) : 0;
+    }
+    /* wrapped_index of LocalRegrid::WrapIndices: for block b of level l
+     * (1-based, 0 and N+1 wrapping around) a cell inside it */
+    int lr_wrapped(int l, int b) const {
+        const int bf = c.blocking_factor, nb = dimN[l] / bf;
+        if (b == 0) return dimN[l] - bf / 2;
+        if (b == nb + 1) return bf / 2;
+        return (int)((static_cast<double>(b) - 0.5) * static_cast<double>(bf));
+    }
+    /* owner map of a level at block resolution (1: a box covers the block) */
+    std::vector<uint8_t> block_cover(int l) const {
+        const int bf = c.blocking_factor, nb = dimN[l] / bf;
+        std::vector<uint8_t> cov((size_t)nb * nb * nb, 0);
+        for (const IBox &x : boxes[l])
+            for (int k = x.lo[2] / bf; k <= x.hi[2] / bf; ++k)
+                for (int j = x.lo[1] / bf; j <= x.hi[1] / bf; ++j)
+                    for (int i = x.lo[0] / bf; i <= x.hi[0] / bf; ++i)
+                        cov[((size_t)k * nb + j) * nb + i] = 1;
+        return cov;
+    }
+    bool covers_cell(const std::vector<uint8_t> &cov, int l, int i, int j, int k) const {
+        const int bf = c.blocking_factor, nb = dimN[l] / bf;
+        return cov[((size_t)(k / bf) * nb + j / bf) * nb + i / bf] != 0;
+    }
+
+    /* LocalRegrid::DetermineNewBoxArray(lev): blocks of level lev+1 to add
+     * (into add[lev+1]) next to tagged cells of level lev closer than
+     * (n_error_buf + 1) fine cells to a coarse/fine boundary; returns the
+     * shortest distance found (-1 if none). */
+    double lr_new_blocks(int lev, std::vector<std::vector<uint8_t>> &add) {
+        const double threshold = (double)(c.n_error_buf + 1) * (c.n_error_buf + 1);
+        const int ibff = c.blocking_factor;
+        const double bff = static_cast<double>(ibff);
+        const int nbf = dimN[lev + 1] / ibff;
+        const std::vector<uint8_t> cov = block_cover(lev + 1);
+        const double time = tnew(lev);
+        /* ErrorEst of level lev (its cell mask, boxes layout) */
+        if (c.params_mod_norm0) b.params_mod_from_norm0(levels[0], time);
+        const std::vector<uint8_t> mask =
+            b.tag(levels[lev], shadow_hierarchy, time, lev, dt[lev], dx[lev]);
+        long long best = -1;
+        size_t q0 = 0;
+        for (const IBox &bx : boxes[lev]) {
+            const int nx = bx.hi[0] - bx.lo[0] + 1, ny = bx.hi[1] - bx.lo[1] + 1;
+            int c0[3], c1[3], xs[3];
+            for (int d = 0; d < 3; ++d) {
+                c0[d] = static_cast<int>(static_cast<double>(bx.lo[d] * 2) / bff) + 1;
+                c1[d] = static_cast<int>(static_cast<double>(bx.hi[d] * 2) / bff) + 1;
+                xs[d] = c1[d] - c0[d] + 1;
+            }
+            /* GetBoxCoarseFineBorders: blocks around the box's blocks that
+             * level lev+1 does not cover */
+            const int bx0 = xs[0] + 2, bx1 = xs[1] + 2;
+            std::vector<uint8_t> border((size_t)bx0 * bx1 * (xs[2] + 2));
+            auto bref = [&](int i, int j, int k) -> uint8_t & {
+                return border[((size_t)k * bx1 + j) * bx0 + i];
+            };
+            int remaining = 0;
+            for (int k = -1; k <= xs[2]; ++k)
+                for (int j = -1; j <= xs[1]; ++j)
+                    for (int i = -1; i <= xs[0]; ++i) {
+                        const bool open = !covers_cell(cov, lev + 1, lr_wrapped(lev + 1, c0[0] + i),
+                                                       lr_wrapped(lev + 1, c0[1] + j),
+                                                       lr_wrapped(lev + 1, c0[2] + k));
+                        bref(i + 1, j + 1, k + 1) = open;
+                        remaining += open;
+                    }
+            if (remaining > 0) {
+                /* TagAndMeasure / CheckBorders over the tagged cells */
+                for (int k = bx.lo[2]; k <= bx.hi[2]; ++k)
+                    for (int j = bx.lo[1]; j <= bx.hi[1]; ++j)
+                        for (int i = bx.lo[0]; i <= bx.hi[0]; ++i) {
+                            const size_t m = q0 + (size_t)(i - bx.lo[0]) +
+                                             (size_t)nx * ((j - bx.lo[1]) + (size_t)ny * (k - bx.lo[2]));
+                            if (!mask[m]) continue;
+                            const int ci[3] = {i, j, k};
+                            int fi[3], cfi[3];
+                            for (int d = 0; d < 3; ++d) {
+                                fi[d] = ci[d] * 2;
+                                cfi[d] = static_cast<int>(static_cast<double>(fi[d]) / bff) + 1;
+                            }
+                            for (int kk = -1; kk <= 1; ++kk)
+                                for (int jj = -1; jj <= 1; ++jj)
+                                    for (int ii = -1; ii <= 1; ++ii) {
+                                        const int cii[3] = {ii, jj, kk};
+                                        int ref[3];
+                                        for (int d = 0; d < 3; ++d) ref[d] = cfi[d] - c0[d] + cii[d] + 1;
+                                        if (!bref(ref[0], ref[1], ref[2])) continue;
+                                        long long d_sq = 0;
+                                        for (int d = 0; d < 3; ++d) {
+                                            const long long smt = (long long)ibff * (cfi[d] + cii[d] - 1);
+                                            const long long bgt = (long long)ibff * (cfi[d] + cii[d]) - 1;
+                                            const long long f = fi[d];
+                                            d_sq += (smt < f && f < bgt)
+                                                        ? 0
+                                                        : std::min((f - smt) * (f - smt), (f - bgt) * (f - bgt));
+                                        }
+                                        if (best < 0 || d_sq < best) best = d_sq;
+                                        if ((double)d_sq < threshold) {
+                                            bref(ref[0], ref[1], ref[2]) = 0;
+                                            int blk[3];
+                                            for (int d = 0; d < 3; ++d)
+                                                blk[d] = static_cast<int>(
+                                                    static_cast<double>(lr_wrapped(lev + 1, cfi[d] + cii[d])) / bff - 0.5);
+                                            add[lev + 1][((size_t)blk[2] * nbf + blk[1]) * nbf + blk[0]] = 1;
+                                        }
+                                    }
+                        }
+            }
+            q0 += (size_t)bx.volume();
+        }
+        return best >= 0 ? std::sqrt(static_cast<double>(best)) : -1.;
+    }
+
+    /* LocalRegrid::FixNesting(lev): blocks of level lev-1 to add so that the
+     * blocks added to level lev, grown by nghost + 4 cells, lie in it */
+    void lr_fix_nesting(int lev, std::vector<std::vector<uint8_t>> &add) {
+        const int bf = c.blocking_factor, nb = dimN[lev] / bf, nbc = dimN[lev - 1] / bf;
+        const std::vector<uint8_t> cov = block_cover(lev - 1);
+        const int g = c.nghost + 4, Nc = dimN[lev - 1];
+        const double bfc = static_cast<double>(bf);
+        auto cdiv = [](int a) { return a >= 0 ? a / 2 : -((-a + 1) / 2); };
+        for (int k = 0; k < nb; ++k)
+            for (int j = 0; j < nb; ++j)
+                for (int i = 0; i < nb; ++i) {
+                    if (!add[lev][((size_t)k * nb + j) * nb + i]) continue;
+                    /* the block grown by g cells, coarsened by 2 */
+                    int lo[3], hi[3];
+                    const int bl[3] = {i, j, k};
+                    for (int d = 0; d < 3; ++d) {
+                        lo[d] = cdiv(bl[d] * bf - g);
+                        hi[d] = cdiv((bl[d] + 1) * bf - 1 + g);
+                    }
+                    /* WrapBoxArray: the periodic pieces inside [0, Nc) */
+                    for (int sz = -1; sz <= 1; ++sz)
+                        for (int sy = -1; sy <= 1; ++sy)
+                            for (int sx = -1; sx <= 1; ++sx) {
+                                const int sh[3] = {sx, sy, sz};
+                                int plo[3], phi[3];
+                                bool empty = false;
+                                for (int d = 0; d < 3; ++d) {
+                                    plo[d] = std::max(lo[d], sh[d] * Nc) - sh[d] * Nc;
+                                    phi[d] = std::min(hi[d], (sh[d] + 1) * Nc - 1) - sh[d] * Nc;
+                                    empty = empty || plo[d] > phi[d];
+                                }
+                                if (empty) continue;
+                                int cl[3], ch[3];
+                                for (int d = 0; d < 3; ++d) {
+                                    cl[d] = static_cast<int>(static_cast<double>(plo[d]) / bfc + 1.);
+                                    ch[d] = static_cast<int>(static_cast<double>(phi[d]) / bfc + 2.);
+                                }
+                                for (int cx = cl[0]; cx <= ch[0]; ++cx)
+                                    for (int cy = cl[1]; cy <= ch[1]; ++cy)
+                                        for (int cz = cl[2]; cz <= ch[2]; ++cz) {
+                                            const int ct[3] = {lr_wrapped(lev - 1, cx),
+                                                               lr_wrapped(lev - 1, cy),
+                                                               lr_wrapped(lev - 1, cz)};
+                                            if (covers_cell(cov, lev - 1, ct[0], ct[1], ct[2])) continue;
+                                            int blk[3];
+                                            for (int d = 0; d < 3; ++d)
+                                                blk[d] = static_cast<int>(static_cast<double>(ct[d]) / bfc - 0.5);
+                                            add[lev - 1][((size_t)blk[2] * nbc + blk[1]) * nbc + blk[0]] = 1;
+                                        }
+                            }
+                }
+    }
+
+    /* the added blocks of a level as boxes (cells) */
+    std::vector<IBox> lr_boxes(int l, const std::vector<uint8_t> &blk) const {
+        const int bf = c.blocking_factor, nb = dimN[l] / bf;
+        const BlockSet t{blk, nb};
+        const int lo[3] = {0, 0, 0}, hi[3] = {nb - 1, nb - 1, nb - 1};
+        std::vector<IBox> bb;
+        runs_to_boxes(t, lo, hi, bb);
+        simplify(bb);
+        max_size(bb, c.max_grid_size / bf);
+        std::vector<IBox> out;
+        for (const IBox &r : bb)
+            out.push_back(IBox{{r.lo[0] * bf, r.lo[1] * bf, r.lo[2] * bf},
+                               {(r.hi[0] + 1) * bf - 1, (r.hi[1] + 1) * bf - 1,
+                                (r.hi[2] + 1) * bf - 1}});
+        return out;
+    }
+
+    /* LocalRegrid::AttemptRegrid / DoAttemptRegrid: true when the local
+     * regrid succeeded (boxes added, or deliberately nothing done) */
+    bool attempt_local_regrid(int lev) {
+        if ((int)lr_no_local.size() != c.max_level + 1) {
+            lr_no_local.assign(c.max_level + 1, 0);
+            lr_do_global.assign(c.max_level + 1, 0);
+        }
+        /* Prechecks */
+        if (lr_nregrids++ >= c.max_local_regrids) return false;
+        if (c.volume_threshold_weak <= 1.) {
+            lr_veto_level = lev - 1;
+            return false;
+        }
+        lr_veto_level = -1;
+        if (lr_do_global[lev]) return false;
+        if (lev == finest) return false;
+        /* InitializeLocalRegrid */
+        while ((int)lr_last_numpts.size() <= finest)
+            lr_last_numpts.push_back(level_cells((int)lr_last_numpts.size()));
+        /* DetermineAllBoxArrays */
+        std::vector<std::vector<uint8_t>> add(finest + 1);
+        for (int l = 0; l <= finest; ++l) {
+            const int nb = dimN[l] / c.blocking_factor;
+            add[l].assign((size_t)nb * nb * nb, 0);
+        }
+        std::vector<double> min_distance(finest + 1, -1.);
+        {
+            Clock ck(this, kTTag);
+            for (int l = lev; l < finest && !lr_no_local[l]; ++l)
+                min_distance[l + 1] = lr_new_blocks(l, add);
+        }
+        /* FixAllNesting */
+        for (int l = finest; l > 1; --l) lr_fix_nesting(l, add);
+        std::vector<std::vector<IBox>> nbx(finest + 1);
+        for (int l = 1; l <= finest; ++l) nbx[l] = lr_boxes(l, add[l]);
+        /* CheckForVeto */
+        bool veto = false;
+        std::vector<double> latest(finest + 1, -1.);
+        for (int l = 1; l <= finest; ++l) {
+            long long Nb = 0;
+            for (const IBox &x : nbx[l]) Nb += x.volume();
+            const double Nc = (double)level_cells(l);
+            double Nr = (double)lr_last_numpts[l];
+            if (Nr == 0) Nr = Nc;
+            const double fV = ((double)Nb + Nc) / Nr;
+            if (fV > c.volume_threshold_weak) veto = true;
+            if (fV > c.volume_threshold_strong && lr_veto_level == -1) lr_veto_level = l - 1;
+            if (l > lev) { /* ComputeLatestPossibleRegridTime */
+                const double dt_delay = min_distance[l] >= 0
+                                            ? min_distance[l] / c.n_error_buf * regrid_dt[l]
+                                            : DBL_MAX;
+                latest[l] = tnew(l) + dt_delay;
+            }
+        }
+        if (veto) { /* DealWithVeto */
+            if (lr_veto_level >= lev || lr_veto_level == 0) return false;
+            lr_do_global[lr_veto_level] = 1;
+            double nsteps = istep_new(lr_veto_level) % 2 == 0 ? 1 : 2;
+            if (shadow_hierarchy) nsteps = 0;
+            const double target = tnew(lr_veto_level) + nsteps * dt[lr_veto_level];
+            bool can_wait = true;
+            for (int l = lev + 1; l <= finest; ++l)
+                if (latest[l] < target) can_wait = false;
+            if (can_wait) {
+                for (int l = lev; l <= finest; ++l) lr_no_local[l] = 1;
+                return true;
+            }
+        }
+        /* AddAllBoxes */
+        for (int l = 1; l <= finest; ++l)
+            if (!nbx[l].empty()) lr_add_boxes(l, nbx[l]);
+        return true;
+    }
+
+    /* LocalRegrid::AddBoxes: level l with its boxes followed by the new
+     * ones, both time levels of the new boxes filled at their times (from
+     * the coarse level), the existing cells kept */
+    void lr_add_boxes(int l, const std::vector<IBox> &add) {
+        std::vector<IBox> nb = boxes[l];
+        nb.insert(nb.end(), add.begin(), add.end());
+        const double tn = b.time(levels[l], kNew), to = b.time(levels[l], kOld);
+        const int sn = b.istep(levels[l], kNew), so = b.istep(levels[l], kOld);
+        Level fresh;
+        {
+            Clock ck(this, kTCreate);
+            fresh = b.create(l, nb, dimN[l]);
+        }
+        {
+            Clock ck(this, kTFill);
+            b.extend(fresh, levels[l], levels[l - 1], tn, to);
+        }
+        {
+            Clock ck(this, kTDestroy);
+            b.destroy(levels[l]);
+        }
+        levels[l] = fresh;
+        boxes[l] = nb;
+        b.set_time(levels[l], kNew, tn, sn);
+        b.set_time(levels[l], kOld, to, so);
+        te_valid[l] = false;
     }
 
     /* ---- new grids ---- */

@@ -16,7 +16,9 @@
  *                 sh_last_regrid_time[max_level+1], sh_schedule[2 per entry]
  *                 (lowest level, time), sh_te_valid[max_level+1],
  *                 sh_cell_updates[1], sh_grid[3] (max_level, blocking factor,
- *                 components);
+ *                 components), sh_local_regrid (attempts, the sizes and
+ *                 contents of the per-level no-local and global-requested
+ *                 flags and of the cells at the last global regrid);
  *   Level_<l>_new.bin, Level_<l>_old.bin
  *               the valid cells of both time levels of level l as raw FP64
  *               (little endian), box after box, component-major inside a
@@ -97,7 +99,14 @@ inline bool write_checkpoint(const Checkpoint &k, const std::string &folder, std
     for (uint8_t v : k.te_valid) tev.push_back(v);
     const double cu = (double)k.cell_updates;
     const double grid[3] = {(double)k.max_level, (double)k.blocking_factor, (double)k.ncomp};
-    ok = ok &&
+    /* local regrid state: attempts, then per level no-local, global
+     * requested, cells at the last global regrid */
+    std::vector<double> lr = {(double)k.lr_nregrids, (double)k.lr_no_local.size(),
+                              (double)k.lr_do_global.size(), (double)k.lr_last_numpts.size()};
+    for (uint8_t v : k.lr_no_local) lr.push_back(v);
+    for (uint8_t v : k.lr_do_global) lr.push_back(v);
+    for (long long v : k.lr_last_numpts) lr.push_back((double)v);
+    ok = ok && w.add_f64("sh_local_regrid", lr.data(), lr.size(), err) &&
          w.add_f64("sh_last_regrid_time", k.last_regrid_time.data(), k.last_regrid_time.size(),
                    err) &&
          w.add_f64("sh_schedule", sched.data(), sched.size(), err) &&
@@ -138,6 +147,18 @@ inline bool read_checkpoint(const std::string &folder, Checkpoint *k, std::strin
     for (size_t q = 0; q < sched.size(); q += 2) k->schedule.push_back({(int)sched[q], sched[q + 1]});
     k->te_valid.assign(tev.begin(), tev.end());
     k->cell_updates = (long long)cu[0];
+    std::vector<double> lr;
+    if (!r.get("sh_local_regrid", &lr, err)) return false;
+    if (lr.size() < 4 || lr.size() != 4 + (size_t)lr[1] + (size_t)lr[2] + (size_t)lr[3])
+        return ck_fail(err, folder + ": bad local regrid state");
+    k->lr_nregrids = (int)lr[0];
+    size_t q = 4;
+    k->lr_no_local.assign(lr.begin() + q, lr.begin() + q + (size_t)lr[1]);
+    q += (size_t)lr[1];
+    k->lr_do_global.assign(lr.begin() + q, lr.begin() + q + (size_t)lr[2]);
+    q += (size_t)lr[2];
+    k->lr_last_numpts.clear();
+    for (size_t e = 0; e < (size_t)lr[3]; ++e) k->lr_last_numpts.push_back((long long)lr[q + e]);
     k->levels.assign(k->finest + 1, LevelState());
     for (int l = 0; l <= k->finest; ++l) {
         LevelState &s = k->levels[l];

@@ -1,6 +1,7 @@
 """Shared AMR test configuration: AxionStringsLap2 (4th-order Laplacian,
 lambda = 1, plain quartic potential), 16^3 coarse grid with dx = 0.25, up to
-two refinement levels, truncation-error and string-winding tags."""
+two refinement levels, truncation-error and string-winding tags, global
+regrids only unless a test asks for local ones (max_local_regrids)."""
 import sledgehamr_gb300 as sh
 from sledgehamr_gb300 import ic
 
@@ -10,7 +11,8 @@ N0, L = 16, 4.0
 def config(**kw):
     base = dict(N0=N0, L=L, cfl=0.25, t_start=3.0, nghost=2, max_level=2, blocking_factor=8,
                 max_grid_size=16, n_error_buf=1, regrid_dt=0.0, te_crit=[1e-2] * 4,
-                params=[1.0, 0.0], string_width_threshold=2.0, record_regrids=1)
+                params=[1.0, 0.0], string_width_threshold=2.0, record_regrids=1,
+                max_local_regrids=0)
     base.update(kw)
     return sh.amr_config("AxionStringsLap2", **base)
 

@@ -7,9 +7,11 @@ through the oracle's hierarchy, against sledgehamr's TimeStepper:
   source/regrid_scheduler.cpp for the first four coarse steps of a
   hierarchy with a shadow level that refines everywhere (every cell's
   truncation error passes te_crit = 0), regrid_dt = 0, max_level 2;
+* the same with local regrids (LocalRegrid::AttemptRegrid before every
+  global regrid, source/local_regrid/local_regrid.cpp:22-401);
 * an independent restatement of the same functions (tests/timestepper_model.py)
   over longer runs, with and without the shadow hierarchy, with the regrid
-  interval and with the project's CreateLevelIf gate.
+  interval, with the project's CreateLevelIf gate and with local regrids.
 Times are compared exactly: both sides add the same doubles in the same
 order."""
 import pytest
@@ -59,19 +61,46 @@ def _run(cfg_kw, steps, seed=0):
     return tr, finest
 
 
+# The same hierarchy with local regrids (LocalRegrid::AttemptRegrid before
+# every global regrid, local_regrid.cpp:22-401): the regrid of step 2 creates
+# level 1 globally (a level above is needed to grow locally); from step 3 on
+# level 1 covers the domain, so the local regrid finds no coarse/fine
+# boundary to push, succeeds without adding boxes, and level 2 is not made.
+KAT_LOCAL = KAT[:14] + [
+    # step 3 as above up to the regrid, which is local
+    ("local_regrid", 0, T + 3 * D),
+    # step 4: level 1 is still the finest level
+    ("schedule", 0, T + 4 * D), ("shadow", -1, T + 4 * D), ("advance", 0, T + 3 * D),
+    ("advance", 1, T + 3 * D),
+    ("schedule", 1, T + 4 * D), ("advance", 1, T + 3 * D + H),
+    ("truncation_errors", 1, T + 4 * D), ("truncation_errors", 0, T + 4 * D),
+    ("local_regrid", 0, T + 4 * D),
+]
+assert KAT_LOCAL[13] == ("truncation_errors", 0, T + 3 * D)
+
+
 def test_time_stepper_known_answer_sequence():
-    tr, finest = _run(dict(te_crit=[0.0] * 4, regrid_dt=0.0, string_width_threshold=0.0), 4)
+    tr, finest = _run(dict(te_crit=[0.0] * 4, regrid_dt=0.0, string_width_threshold=0.0,
+                           max_local_regrids=0), 4)
     assert finest == [0, 1, 2, 2]
     assert tr == KAT
 
 
+def test_time_stepper_known_answer_sequence_with_local_regrids():
+    tr, finest = _run(dict(te_crit=[0.0] * 4, regrid_dt=0.0, string_width_threshold=0.0,
+                           max_local_regrids=10), 4)
+    assert finest == [0, 1, 1, 1]
+    assert tr == KAT_LOCAL
+
+
 def _model(cfg_kw, grows=lambda lev, t: True):
     c = dict(N0=16, L=4.0, cfl=0.25, t_start=3.0, max_level=2, regrid_dt=0.0,
-             string_width_threshold=2.0)
+             string_width_threshold=2.0, max_local_regrids=0)
     c.update({k: v for k, v in cfg_kw.items() if k in c})
     shadow = any(x != DBL_MAX for x in cfg_kw.get("te_crit", [DBL_MAX]))
     return TimeStepperModel(c["N0"], c["L"], c["cfl"], c["t_start"], c["max_level"],
-                            c["regrid_dt"], shadow, c["string_width_threshold"], grows=grows)
+                            c["regrid_dt"], shadow, c["string_width_threshold"], grows=grows,
+                            max_local_regrids=c["max_local_regrids"])
 
 
 @pytest.mark.parametrize("cfg_kw", [
@@ -86,8 +115,13 @@ def _model(cfg_kw, grows=lambda lev, t: True):
     # no shadow hierarchy: regrids at the start of steps (NoShadowRegrid)
     dict(te_crit=[DBL_MAX] * 4, regrid_dt=0.0, string_width_threshold=0.0),
     dict(te_crit=[DBL_MAX] * 4, regrid_dt=2 * 0.0625, string_width_threshold=0.0),
+    # local regrids with a small attempt budget: global regrids after every
+    # third attempt (the hierarchy refined everywhere never needs new boxes)
+    dict(te_crit=[0.0] * 4, regrid_dt=0.0, string_width_threshold=0.0, max_local_regrids=2),
 ])
 def test_time_stepper_sequence_equals_restated_model(cfg_kw):
+    cfg_kw = dict(cfg_kw)
+    cfg_kw.setdefault("max_local_regrids", 0)
     steps = 7
     tr, finest = _run(cfg_kw, steps, seed=4)
     m = _model(cfg_kw)

@@ -141,8 +141,8 @@ def test_amr_operation_order_equals_known_answer(ctx):
     the order written out by hand from source/time_stepper.cpp
     (tests/test_amr_sequence.py)."""
     from tests.test_amr_sequence import KAT
-    g = sh.Amr(ctx, config(te_crit=[0.0] * 4, regrid_dt=0.0, string_width_threshold=0.0),
-               level0(0))
+    g = sh.Amr(ctx, config(te_crit=[0.0] * 4, regrid_dt=0.0, string_width_threshold=0.0,
+                           max_local_regrids=0), level0(0))
     g.set_trace(True)
     g.step(4)
     assert g.info()["finest"] == 2
@@ -174,4 +174,28 @@ def test_checkpoint_restart_on_gpu_and_in_the_oracle(ctx, tmp_path):
         assert rel_l2(gd, o.read(lev)[0]) <= 1e-12
     g.close()
     r.close()
+    o.close()
+
+
+def test_amr_local_regrids_match_oracle(ctx):
+    """Local regrids (LocalRegrid::AttemptRegrid before each global regrid)
+    on the GPU hierarchy take the oracle's decisions: the same boxes after
+    every coarse step (including a level grown by a block), fields within
+    1e-12."""
+    kw = dict(record_regrids=0, regrid_dt=0.125, max_local_regrids=10)
+    g = sh.Amr(ctx, config(**kw), level0(1))
+    o = OracleAmr(config(**kw), level0(1))
+    g.set_trace(True)
+    o.set_trace(True)
+    for step in range(10):
+        g.step(1)
+        o.step(1)
+        assert g.info() == o.info(), step
+        for lev in range(g.info()["finest"] + 1):
+            assert g.level(lev).boxes == o.boxes(lev), (step, lev)
+            assert rel_l2(g.level(lev).read(), o.read(lev)[0]) <= 1e-12
+    assert g.trace() == o.trace()
+    assert any(e[0] == "local_regrid" for e in g.trace())
+    assert len(g.level(2).boxes) == 66  # level 2 grew by one block locally
+    g.close()
     o.close()

@@ -8,7 +8,9 @@ It restates, from the reference's source:
   TimeStepper::ScheduleRegrid .... time_stepper.cpp:221-295
   TimeStepper::DoRegridIfScheduled time_stepper.cpp:301-311
   TimeStepper::NoShadowRegrid .... time_stepper.cpp:317-339
-  TimeStepper::DoRegrid .......... time_stepper.cpp:346-397 (global regrid)
+  TimeStepper::DoRegrid .......... time_stepper.cpp:346-397 (local regrid
+                                   attempt, then the global regrid)
+  LocalRegrid prechecks .......... source/local_regrid/local_regrid.cpp:109-146
   RegridScheduler ................ source/regrid_scheduler.cpp
   Integrator::Advance ............ source/integrators/integrator.cpp:11-31
                                    (swap, t_new = t_old + dt, istep + 1)
@@ -37,7 +39,8 @@ DBL_MAX = 1.7976931348623157e308
 
 class TimeStepperModel:
     def __init__(self, N0, L, cfl, t_start, max_level, regrid_dt, shadow_hierarchy,
-                 string_width_threshold=0.0, string_lambda=1.0, grows=lambda lev, t: True):
+                 string_width_threshold=0.0, string_lambda=1.0, grows=lambda lev, t: True,
+                 max_local_regrids=0, local_succeeds=lambda lev, t: True):
         self.max_level = max_level
         self.t_start = t_start
         self.shadow_hierarchy = shadow_hierarchy
@@ -56,6 +59,12 @@ class TimeStepperModel:
         self.finest = 0
         self.schedule: list[list] = []  # [lowest_level, time]
         self.events: list[tuple[str, int, float]] = []
+        # LocalRegrid (source/local_regrid/local_regrid.cpp:22-401): attempts
+        # since the last global regrid; whether an attempt that passes the
+        # prechecks succeeds is a parameter (the model does not tag)
+        self.max_local_regrids = max_local_regrids
+        self.local_succeeds = local_succeeds
+        self.local_attempts = 0
 
     # ---- RegridScheduler (regrid_scheduler.cpp) -------------------------
     def _find(self, t):
@@ -165,7 +174,18 @@ class TimeStepperModel:
         self._regrid(lev, time)
 
     def _regrid(self, lbase, time):
+        # TimeStepper::DoRegrid: LocalRegrid::AttemptRegrid first
+        # (Prechecks, local_regrid.cpp:109-146: attempts left, a level above
+        # to grow), the global regrid when it does not succeed
+        attempt = self.local_attempts < self.max_local_regrids
+        self.local_attempts += 1
+        if attempt and lbase != self.finest and self.local_succeeds(lbase, time):
+            self.events.append(("local_regrid", lbase, time))
+            for l in range(lbase, self.finest + 1):
+                self.last_regrid_time[l] = time
+            return
         self.events.append(("regrid", lbase, time))
+        self.local_attempts = 0  # LocalRegrid::DidGlobalRegrid
         top = min(self.finest, self.max_level - 1)
         new_finest = lbase
         for l in range(lbase, top + 1):
