@@ -69,9 +69,9 @@ WORDS_PER_CELL_UPDATE = 40
 # Measured DRAM traffic of the stage kernels per cell-update (ncu, dram
 # bytes read + written of the three launches of one RKN4 step), scaled to a
 # launch of the benchmark by the cells it updates.  AMR: level 1 of the AMR
-# run at N0 = 128 (5.55 GB for 12,729,344 cells); 128^3 level: the launches
-# of `--case single`.
-TRAFFIC_B_PER_CELL_UPDATE = {"amr": 436.0, "single": None}
+# run at N0 = 128 (5.55 GB for 12,729,344 cells); 128^3 level: the three
+# launches of one step of `--case single` (602.3 MB for 2,097,152 cells).
+TRAFFIC_B_PER_CELL_UPDATE = {"amr": 436.0, "single": 287.2}
 
 SINGLE = dict(N=128, L=32.0, project="AxionStringsLap1", params=[1.0, 0.0], nghost=1,
               eta0=0.1, total_steps=200, seed=0)
@@ -720,9 +720,11 @@ def replica_aggregate(total_ms, cell_updates, world, device):
 
 def run_case(name):
     """Small fixed cases for profiler captures (no timing, no output line):
-    axion-fp32k / axion-fp64: one 256^3 axion realisation, 3 RKN4 steps
-    (9 stage launches); fopt-fp32k: one 192^3 FOPT + GW realisation, 3
-    leapfrog steps; amr / amr128: the AMR workload at N0 = 64 (L = 16), 40
+    axion-fp32k / axion-fp32k-tma / axion-fp64: one 256^3 axion
+    realisation, 3 RKN4 steps (9 stage launches; -tma with the stencil planes
+    staged by tensor copies); fopt-fp32k: one 192^3 FOPT + GW realisation, 3
+    leapfrog steps; gw384 / gw256: GW spectra of an FP64 FOPT + GW level
+    (binned and unbinned, twice each); amr / amr128: the AMR workload at N0 = 64 (L = 16), 40
     coarse steps, or N0 = 128 (L = 32), 60 coarse steps; single: the 128^3
     FP64 level, 3 RKN4 steps; fp64-peak: prints the measured FP64 FMA issue
     rate (the FP64 roofline's peak)."""
@@ -739,6 +741,8 @@ def run_case(name):
         E = sh.Ensemble(ctx, sh.FAMILY_AXION_LAP1, prec, [N], [0.25], [1, 0, 0, 0])
         E.write(0, ic.axion_string_ic(N, N * 0.25, kmax=1.0, seed=0))
         E.set_time(0.1)
+        if name.endswith("tma"):
+            E.set_staging(1)
         E.step(0.0625, 3)
         E.close()
     elif name == "fopt-fp32k":
@@ -777,10 +781,10 @@ def run_case(name):
                 rows.append((lev, v.nvalid, tiles))
             print("step", q, rows, flush=True)
         sim.close()
-    elif name == "gw384":
-        # the GW spectrum of a 384^3 FOPT + GW level (FP64, binned and
-        # unbinned, each twice: the second call of each kind is warm)
-        N = 384
+    elif name in ("gw384", "gw256"):
+        # the GW spectrum of a 384^3 (256^3) FOPT + GW level (FP64, binned
+        # and unbinned, each twice: the second call of each kind is warm)
+        N = int(name[2:])
         lv = sh.Level.periodic(ctx, "FirstOrderPhaseTransition", N, 2, max_grid=128,
                                with_gw=True)
         st = np.zeros((14, N, N, N))
@@ -835,7 +839,7 @@ def timed_steps(step, steps, warmup, stream, flush, clk=None, before=None):
 # FP64 thread instructions (DFMA + DMUL + DADD) per cell-update of the stage
 # kernels of the 128^3 level (ncu sass instruction counters of the three
 # launches of one RKN4 step, `--case single`, divided by the cells).
-FP64_INSTR_PER_CELL_UPDATE = {"single": None, "amr": None}
+FP64_INSTR_PER_CELL_UPDATE = {"single": 55.25, "amr": None}
 
 
 def fp64_probe(device):
@@ -969,7 +973,8 @@ def main():
     ap.add_argument("--serve-max-n", type=int, default=SERVE["max_n"])
     ap.add_argument("--case", default=None,
                     help="run one small profiling case and exit: axion-fp32k, axion-fp64, "
-                         "fopt-fp32k, amr, amr128, single, gw384, fp64-peak")
+                         "axion-fp32k-tma, fopt-fp32k, amr, amr128, single, gw384, gw256, "
+                         "fp64-peak")
     args = ap.parse_args()
     if args.case:
         run_case(args.case)

@@ -1635,7 +1635,7 @@ int sh_ensemble_gw_spectrum(sh_ensemble *E, int r, int zero_padding, int project
         int nb = 0;
         std::string err;
         cudaError_t e = sh::gw_spectrum_packed(
-            E->gw, s, P, projection_type, unbinned, scratch, bins_dev, &nb, &E->launches, err,
+            E->gw, s, P, N, projection_type, unbinned, scratch, bins_dev, &nb, &E->launches, err,
             [&](int q, double *real) {
                 const int c = sel[q];
                 if (E->esize == 8)

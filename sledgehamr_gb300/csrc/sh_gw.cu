@@ -103,7 +103,18 @@ __global__ void gw_pack_kernel(const BoxDev *boxes, const long long *vbase, int 
     }
 }
 
-/* Per k-cell TT power (unnormalised); layout ((c*P + b)*H + a). */
+/* Per k-cell TT power (unnormalised); layout ((c*P + b)*H + a).
+ *
+ * The reference sums Lambda_ijlm(k) u_lm conj(u_ij) over i,j,l,m
+ * (gravitational_waves.cpp:251-276) with Lambda_ijlm = P_il P_jm -
+ * 1/2 P_ij P_lm and P = 1 - k k^T / k^2 (gravitational_waves.h:101-133).  As
+ * Lambda is the TT projector this equals |W|^2 - 1/2 |tr W|^2 with
+ * W = P U P, which is formed here without the 3x3 products: with v = U k,
+ * s = k.v and w = v / k^2 - (s / 2k^4) k,
+ *     W = U - k w^T - w k^T,
+ * about 90 FP64 operations per cell instead of the ~160 of P U P.  W is
+ * the projected tensor itself, so |W|^2 carries rounding of the order of
+ * eps |U| |W| (not eps |U|^2), as the explicit form does. */
 __global__ void gw_project_kernel(const double2 *u0, const double2 *u1, const double2 *u2,
                                   const double2 *u3, const double2 *u4, const double2 *u5,
                                   const double *index_to_k, int P, double *out) {
@@ -118,56 +129,40 @@ __global__ void gw_project_kernel(const double2 *u0, const double2 *u1, const do
             out[e] = 0.;
             continue;
         }
-        const double kx = index_to_k[a], ky = index_to_k[b], kz = index_to_k[c];
-        const double inv = 1. / (kx * kx + ky * ky + kz * kz);
-        const double kv[3] = {kx, ky, kz};
-        double Pm[3][3];
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) Pm[i][j] = (i == j ? 1. : 0.) - kv[i] * kv[j] * inv;
+        const double k[3] = {index_to_k[a], index_to_k[b], index_to_k[c]};
+        const double inv = 1. / (k[0] * k[0] + k[1] * k[1] + k[2] * k[2]);
         /* symmetric tensor from the component slots xx xy xz yy yz zz */
-        const double2 s[6] = {u0[e], u1[e], u2[e], u3[e], u4[e], u5[e]};
+        const double2 s6[6] = {u0[e], u1[e], u2[e], u3[e], u4[e], u5[e]};
         const int slot[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
-        double2 U[3][3];
+        double2 v[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            v[i].x = s6[slot[i][0]].x * k[0] + s6[slot[i][1]].x * k[1] + s6[slot[i][2]].x * k[2];
+            v[i].y = s6[slot[i][0]].y * k[0] + s6[slot[i][1]].y * k[1] + s6[slot[i][2]].y * k[2];
+        }
+        const double sx = k[0] * v[0].x + k[1] * v[1].x + k[2] * v[2].x;
+        const double sy = k[0] * v[0].y + k[1] * v[1].y + k[2] * v[2].y;
+        const double h = 0.5 * inv * inv;
+        double2 w[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            w[i].x = inv * v[i].x - h * sx * k[i];
+            w[i].y = inv * v[i].y - h * sy * k[i];
+        }
+        double first = 0., tr_re = 0., tr_im = 0.;
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
-            for (int j = 0; j < 3; ++j) U[i][j] = s[slot[i][j]];
-        /* W = P U P (complex, symmetric) */
-        double2 PU[3][3];
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                double re = 0., im = 0.;
-#pragma unroll
-                for (int l = 0; l < 3; ++l) {
-                    re += Pm[i][l] * U[l][j].x;
-                    im += Pm[i][l] * U[l][j].y;
+            for (int j = i; j < 3; ++j) {
+                const double2 u = s6[slot[i][j]];
+                const double re = u.x - (k[i] * w[j].x + w[i].x * k[j]);
+                const double im = u.y - (k[i] * w[j].y + w[i].y * k[j]);
+                const double wt = i == j ? 1. : 2.;
+                first += wt * (re * re + im * im);
+                if (i == j) {
+                    tr_re += re;
+                    tr_im += im;
                 }
-                PU[i][j] = make_double2(re, im);
-            }
-        double first = 0.;
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int m = 0; m < 3; ++m) {
-                double re = 0., im = 0.;
-#pragma unroll
-                for (int j = 0; j < 3; ++j) {
-                    re += PU[i][j].x * Pm[j][m];
-                    im += PU[i][j].y * Pm[j][m];
-                }
-                first += re * U[i][m].x + im * U[i][m].y;
-            }
-        double tr_re = 0., tr_im = 0.;
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                tr_re += Pm[i][j] * U[i][j].x;
-                tr_im += Pm[i][j] * U[i][j].y;
             }
         const double multpl = (a == 0 || a == P / 2) ? 1. : 2.;
         out[e] = multpl * (first - 0.5 * (tr_re * tr_re + tr_im * tr_im));
@@ -361,8 +356,8 @@ void GwCache::release() {
     cur = nullptr;
 }
 
-cudaError_t gw_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, int projection_type,
-                               int unbinned, double *scratch, double *bins_dev, int *nbins,
+cudaError_t gw_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, int N,
+                               int projection_type, int unbinned, double *scratch, double *bins_dev, int *nbins,
                                long long *launches, std::string &err,
                                const std::function<void(int, double *)> &pack) {
     cache.prepare(P, unbinned, projection_type);
@@ -380,7 +375,8 @@ cudaError_t gw_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, int p
     double2 *cplx = (double2 *)(scratch + nreal);
     double *vals = (double *)(cplx + 6 * ncplx);
     for (int q = 0; q < 6; ++q) {
-        cudaMemsetAsync(real, 0, nreal * sizeof(double), stream);
+        /* the pack covers all of P^3 without zero padding */
+        if (P != N) cudaMemsetAsync(real, 0, nreal * sizeof(double), stream);
         pack(q, real);
         (*launches)++;
         if (cufftExecD2Z(plan, real, (cufftDoubleComplex *)(cplx + q * ncplx)) !=
@@ -445,7 +441,7 @@ cudaError_t gw_spectrum_device(GwCache &cache, cudaStream_t stream, const BoxDev
                                std::string &err) {
     const int P = N * zero_padding;
     return gw_spectrum_packed(
-        cache, stream, P, projection_type, unbinned, scratch, bins_dev, nbins, launches, err,
+        cache, stream, P, N, projection_type, unbinned, scratch, bins_dev, nbins, launches, err,
         [&](int q, double *real) {
             int g = (int)std::min<long long>((nvalid + 255) / 256, 152LL * 32);
             gw_pack_kernel<<<std::max(g, 1), 256, 0, stream>>>(boxes, vbase, nbox, nvalid, ncomp,

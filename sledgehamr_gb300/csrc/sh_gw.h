@@ -51,17 +51,19 @@ struct GwCache {
 std::vector<long long> unique_k2_host(int dim);
 std::vector<double> index_to_k_host(int N, int type);
 size_t gw_scratch_bytes(int N, int zero_padding);
-/* FFT, TT projection and binning of six P^3 real arrays that `pack(q, real)`
- * writes (enqueued on `stream`) into the zeroed `real` for q = 0..5 in the
- * order du_xx, du_xy, du_xz, du_yy, du_yz, du_zz. */
 /* Scalar power spectrum of one P^3 real field that `pack(real)` writes into
  * the zeroed `real`: bins of the sorted unique k^2, pre * sum multpl |F|^2. */
 cudaError_t scalar_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, double pre,
                                    double *scratch, double *bins_dev, int *nbins,
                                    long long *launches, std::string &err,
                                    const std::function<void(double *)> &pack);
-cudaError_t gw_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, int projection_type,
-                               int unbinned, double *scratch, double *bins_dev, int *nbins,
+/* FFT, TT projection and binning of six P^3 real arrays that `pack(q, real)`
+ * writes (enqueued on `stream`) into the zeroed `real` for q = 0..5 in the
+ * order du_xx, du_xy, du_xz, du_yy, du_yz, du_zz; `real` is zeroed first
+ * only when the packed N^3 block does not fill it (N < P). */
+cudaError_t gw_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, int N,
+                               int projection_type, int unbinned, double *scratch,
+                               double *bins_dev, int *nbins,
                                long long *launches, std::string &err,
                                const std::function<void(int, double *)> &pack);
 cudaError_t gw_spectrum_device(GwCache &cache, cudaStream_t stream, const BoxDev *boxes,
