@@ -155,6 +155,7 @@ def run_ensemble_leg(sh, ctx, stream, flush, steps, warmup):
         E32.write(r, st)
     E32.set_time(e["eta0"])
     nz = E32.tune(dt)
+    staging32 = ["registers", "tensor copies"][E32.staging()]
     E32.set_graph(True)
     l0 = E32.kernel_launches()
     ms32 = timed(lambda: E32.step(dt, 1))
@@ -223,7 +224,7 @@ def run_ensemble_leg(sh, ctx, stream, flush, steps, warmup):
                     f"dx {dx}, dt {dt}, eta0 {e['eta0']}, {total} steps",
         "cells": cells, "timed_steps": steps,
         "fp32_kahan_batched": {"value": cu / (ms32 / 1e3), "ms_per_step": ms32 / steps,
-                               "tile_nz": nz, "graph": True,
+                               "tile_nz": nz, "plane_staging": staging32, "graph": True,
                                "gpu_launches_per_step": launches32 / (warmup + steps),
                                "device_bytes": info32["device_bytes"],
                                "wall_s_incl_upload": wall32},

@@ -1201,7 +1201,18 @@ class Driver {
                 return true;
             }
         }
-        /* AddAllBoxes */
+        /* AddAllBoxes.  The new boxes are interpolated from their coarse
+         * level, which the GPU reads with its ghost cells; the average-down
+         * at the end of the step left those stale, so they are refreshed
+         * from the coarsest level up first, as the global regrid refreshes
+         * a level before remaking the one above it */
+        bool grows = false;
+        for (int l = 1; l <= finest; ++l) grows = grows || !nbx[l].empty();
+        if (grows) {
+            Clock ck(this, kTRefresh);
+            for (int l = 0; l < finest; ++l)
+                b.refresh_ghosts(levels[l], kNew, l > 0 ? &levels[l - 1] : nullptr);
+        }
         for (int l = 1; l <= finest; ++l)
             if (!nbx[l].empty()) lr_add_boxes(l, nbx[l]);
         return true;
@@ -1209,7 +1220,11 @@ class Driver {
 
     /* LocalRegrid::AddBoxes: level l with its boxes followed by the new
      * ones, both time levels of the new boxes filled at their times (from
-     * the coarse level), the existing cells kept */
+     * the coarse level), the existing cells kept.  With truncation-error
+     * tags the old time levels of this level and of the coarse one hold the
+     * errors after a regrid step, so what the new boxes receive there is as
+     * meaningless as the rest of that buffer; the next step swaps the time
+     * levels and overwrites it before anything reads it */
     void lr_add_boxes(int l, const std::vector<IBox> &add) {
         std::vector<IBox> nb = boxes[l];
         nb.insert(nb.end(), add.begin(), add.end());
@@ -1233,6 +1248,10 @@ class Driver {
         b.set_time(levels[l], kNew, tn, sn);
         b.set_time(levels[l], kOld, to, so);
         te_valid[l] = false;
+        if (l < finest) { /* the coarse level of the next extension */
+            Clock ck(this, kTRefresh);
+            b.refresh_ghosts(levels[l], kNew, &levels[l - 1]);
+        }
     }
 
     /* ---- new grids ---- */

@@ -718,12 +718,12 @@ __global__ void load_kernel(const R *src, const R *comp, double *dst, long long 
  * array for the spectrum (compensation included). */
 template <class R>
 __global__ void gw_pack_fast_kernel(const R *src, const R *comp, long long off, int N, int P,
-                                    double *dst) {
+                                    double *dst, int stride) {
     const long long n = (long long)N * N * N;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
         const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / ((long long)N * N));
-        dst[((long long)z * P + y) * P + x] =
+        dst[stride * (((long long)z * P + y) * P + x)] =
             (double)src[off + i] - (comp ? (double)comp[off + i] : 0.);
     }
 }
@@ -1636,15 +1636,15 @@ int sh_ensemble_gw_spectrum(sh_ensemble *E, int r, int zero_padding, int project
         std::string err;
         cudaError_t e = sh::gw_spectrum_packed(
             E->gw, s, P, N, projection_type, unbinned, scratch, bins_dev, &nb, &E->launches, err,
-            [&](int q, double *real) {
+            [&](int q, double *dst, int stride) {
                 const int c = sel[q];
                 if (E->esize == 8)
-                    gw_pack_fast_kernel<double><<<fgrid(n), 256, 0, s>>>((double *)E->A[c],
-                                                                         nullptr, o, N, P, real);
+                    gw_pack_fast_kernel<double><<<fgrid(n), 256, 0, s>>>(
+                        (double *)E->A[c], nullptr, o, N, P, dst, stride);
                 else
                     gw_pack_fast_kernel<float><<<fgrid(n), 256, 0, s>>>(
                         (float *)E->A[c], E->C.empty() ? nullptr : (float *)E->C[c], o, N, P,
-                        real);
+                        dst, stride);
             });
         if (!err.empty()) throw FastErr(SH_ERR_CUDA, err);
         fck(e, "gw spectrum");

@@ -78,10 +78,10 @@ namespace {
 
 /* Pack component `comp` of a level buffer (valid cells, any box layout
  * covering [0,N)^3) into the first N^3 block of a zero-initialised (pN)^3
- * real array. */
+ * array whose elements are `stride` doubles apart. */
 __global__ void gw_pack_kernel(const BoxDev *boxes, const long long *vbase, int nbox,
                                long long nvalid, int ncomp, int comp, const double *buf,
-                               double *dst, int P, int dlo0, int dlo1, int dlo2) {
+                               double *dst, int stride, int P, int dlo0, int dlo1, int dlo2) {
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nvalid;
          v += (long long)gridDim.x * blockDim.x) {
         int lo = 0, hi = nbox - 1;
@@ -99,11 +99,19 @@ __global__ void gw_pack_kernel(const BoxDev *boxes, const long long *vbase, int 
         const long long bi = b.off * ncomp + (long long)comp * b.gvol + (i - b.glo[0]) +
                              (long long)(j - b.glo[1]) * b.gdim[0] +
                              (long long)(k - b.glo[2]) * b.gdim[0] * b.gdim[1];
-        dst[((long long)(k - dlo2) * P + (j - dlo1)) * P + (i - dlo0)] = buf[bi];
+        dst[stride * (((long long)(k - dlo2) * P + (j - dlo1)) * P + (i - dlo0))] = buf[bi];
     }
 }
 
-/* Per k-cell TT power (unnormalised); layout ((c*P + b)*H + a).
+/* Per k-cell TT power, four times unnormalised; layout ((c*P + b)*H + a).
+ *
+ * The six real components arrive in pairs, each pair transformed as one
+ * complex field Z = u + i u' (a complex-to-complex transform costs what the
+ * two real-to-complex ones cost together, and runs faster than cuFFT's
+ * real-to-complex pass); with conj Z(-k) the conjugate of the transform's
+ * value at -k,
+ *     2 U(k) = Z(k) + conj Z(-k),   2 U'(k) = -i (Z(k) - conj Z(-k)),
+ * and the factor 2 (4 in the power) is taken out by the bins' scale.
  *
  * The reference sums Lambda_ijlm(k) u_lm conj(u_ij) over i,j,l,m
  * (gravitational_waves.cpp:251-276) with Lambda_ijlm = P_il P_jm -
@@ -112,12 +120,17 @@ __global__ void gw_pack_kernel(const BoxDev *boxes, const long long *vbase, int 
  * W = P U P, which is formed here without the 3x3 products: with v = U k,
  * s = k.v and w = v / k^2 - (s / 2k^4) k,
  *     W = U - k w^T - w k^T,
- * about 90 FP64 operations per cell instead of the ~160 of P U P.  W is
+ * about 100 FP64 operations per cell instead of the ~170 of P U P.  W is
  * the projected tensor itself, so |W|^2 carries rounding of the order of
  * eps |U| |W| (not eps |U|^2), as the explicit form does. */
-__global__ void gw_project_kernel(const double2 *u0, const double2 *u1, const double2 *u2,
-                                  const double2 *u3, const double2 *u4, const double2 *u5,
-                                  const double *index_to_k, int P, double *out) {
+__device__ __forceinline__ void split_pair(double2 z, double2 m, double2 &u, double2 &v) {
+    u = make_double2(z.x + m.x, z.y - m.y);
+    v = make_double2(z.y + m.y, m.x - z.x);
+}
+
+__global__ void gw_project_kernel(const double2 *__restrict__ Z0, const double2 *__restrict__ Z1,
+                                  const double2 *__restrict__ Z2,
+                                  const double *__restrict__ index_to_k, int P, double *out) {
     const int H = P / 2 + 1;
     const long long n = (long long)H * P * P;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
@@ -129,10 +142,16 @@ __global__ void gw_project_kernel(const double2 *u0, const double2 *u1, const do
             out[e] = 0.;
             continue;
         }
+        const long long f = ((long long)c * P + b) * P + a;
+        const long long g =
+            ((long long)(c ? P - c : 0) * P + (b ? P - b : 0)) * P + (a ? P - a : 0);
+        /* twice the transforms of the slots xx xy xz yy yz zz */
+        double2 s6[6];
+        split_pair(Z0[f], Z0[g], s6[0], s6[1]);
+        split_pair(Z1[f], Z1[g], s6[2], s6[3]);
+        split_pair(Z2[f], Z2[g], s6[4], s6[5]);
         const double k[3] = {index_to_k[a], index_to_k[b], index_to_k[c]};
         const double inv = 1. / (k[0] * k[0] + k[1] * k[1] + k[2] * k[2]);
-        /* symmetric tensor from the component slots xx xy xz yy yz zz */
-        const double2 s6[6] = {u0[e], u1[e], u2[e], u3[e], u4[e], u5[e]};
         const int slot[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
         double2 v[3];
 #pragma unroll
@@ -320,10 +339,10 @@ void GwCache::prepare(int P, int unbinned, int projection_type) {
     cur = &bins.back();
 }
 
-bool GwCache::plan(int P, cufftHandle *out) {
+bool GwCache::plan(int P, int kind, cufftHandle *out) {
     ++clock;
     for (Plan &p : plans)
-        if (p.P == P) {
+        if (p.P == P && p.kind == kind) {
             p.used = clock;
             *out = p.h;
             return true;
@@ -337,8 +356,21 @@ bool GwCache::plan(int P, cufftHandle *out) {
     }
     Plan p;
     p.P = P;
+    p.kind = kind;
     p.used = clock;
-    if (cufftPlan3d(&p.h, P, P, P, CUFFT_D2Z) != CUFFT_SUCCESS) return false;
+    if (cufftCreate(&p.h) != CUFFT_SUCCESS) return false;
+    long long n[3] = {P, P, P};
+    const long long dist = (long long)P * P * P;
+    size_t work = 0;
+    const cufftResult r =
+        kind == kPlanD2Z
+            ? cufftMakePlanMany64(p.h, 3, n, nullptr, 1, 0, nullptr, 1, 0, CUFFT_D2Z, 1, &work)
+            : cufftMakePlanMany64(p.h, 3, n, nullptr, 1, dist, nullptr, 1, dist, CUFFT_Z2Z, 3,
+                                  &work);
+    if (r != CUFFT_SUCCESS) {
+        cufftDestroy(p.h);
+        return false;
+    }
     plans.push_back(p);
     *out = p.h;
     return true;
@@ -357,41 +389,41 @@ void GwCache::release() {
 }
 
 cudaError_t gw_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, int N,
-                               int projection_type, int unbinned, double *scratch, double *bins_dev, int *nbins,
-                               long long *launches, std::string &err,
-                               const std::function<void(int, double *)> &pack) {
+                               int projection_type, int unbinned, double *scratch,
+                               double *bins_dev, int *nbins, long long *launches,
+                               std::string &err,
+                               const std::function<void(int, double *, int)> &pack) {
     cache.prepare(P, unbinned, projection_type);
     const int H = P / 2 + 1;
-    const long long nreal = (long long)P * P * P;
-    const long long ncplx = (long long)H * P * P;
+    const long long nfull = (long long)P * P * P;
+    const long long nhalf = (long long)H * P * P;
     cufftHandle plan;
-    if (!cache.plan(P, &plan)) {
-        err = "cufftPlan3d failed";
+    if (!cache.plan(P, GwCache::kPlanZ2Z3, &plan)) {
+        err = "cuFFT plan of three P^3 complex transforms failed";
         return cudaErrorUnknown;
     }
     cufftSetStream(plan, stream);
-    /* scratch: real (pN)^3 | 6 complex arrays | per-cell values */
-    double *real = scratch;
-    double2 *cplx = (double2 *)(scratch + nreal);
-    double *vals = (double *)(cplx + 6 * ncplx);
+    /* scratch: three complex P^3 arrays (component pairs) | per-cell values */
+    double2 *Z = (double2 *)scratch;
+    double *vals = (double *)(Z + 3 * nfull);
+    /* the pack covers all of P^3 without zero padding */
+    if (P != N) cudaMemsetAsync(Z, 0, 3 * nfull * sizeof(double2), stream);
     for (int q = 0; q < 6; ++q) {
-        /* the pack covers all of P^3 without zero padding */
-        if (P != N) cudaMemsetAsync(real, 0, nreal * sizeof(double), stream);
-        pack(q, real);
+        pack(q, (double *)(Z + (q / 2) * nfull) + (q & 1), 2);
         (*launches)++;
-        if (cufftExecD2Z(plan, real, (cufftDoubleComplex *)(cplx + q * ncplx)) !=
-            CUFFT_SUCCESS) {
-            err = "cufftExecD2Z failed";
-            return cudaErrorUnknown;
-        }
     }
-    int g = (int)std::min<long long>((ncplx + 255) / 256, 152LL * 32);
-    gw_project_kernel<<<std::max(g, 1), 256, 0, stream>>>(
-        cplx, cplx + ncplx, cplx + 2 * ncplx, cplx + 3 * ncplx, cplx + 4 * ncplx,
-        cplx + 5 * ncplx, cache.cur->d_itk, P, vals);
+    if (cufftExecZ2Z(plan, (cufftDoubleComplex *)Z, (cufftDoubleComplex *)Z, CUFFT_FORWARD) !=
+        CUFFT_SUCCESS) {
+        err = "cufftExecZ2Z failed";
+        return cudaErrorUnknown;
+    }
+    int g = (int)std::min<long long>((nhalf + 255) / 256, 152LL * 32);
+    gw_project_kernel<<<std::max(g, 1), 256, 0, stream>>>(Z, Z + nfull, Z + 2 * nfull,
+                                                          cache.cur->d_itk, P, vals);
     (*launches)++;
     const int nb = (int)cache.ks().size();
-    const double scale = 1. / std::pow((double)P, 6);
+    /* 1/P^6, and 1/4 for the pairs' factor 2 (exact) */
+    const double scale = 0.25 / std::pow((double)P, 6);
     launch_bins(vals, *cache.cur, scale, bins_dev, stream);
     (*launches)++;
     *nbins = nb;
@@ -408,8 +440,8 @@ cudaError_t scalar_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, d
     const long long nreal = (long long)P * P * P;
     const long long ncplx = (long long)H * P * P;
     cufftHandle plan;
-    if (!cache.plan(P, &plan)) {
-        err = "cufftPlan3d failed";
+    if (!cache.plan(P, GwCache::kPlanD2Z, &plan)) {
+        err = "cuFFT plan of a P^3 real-to-complex transform failed";
         return cudaErrorUnknown;
     }
     cufftSetStream(plan, stream);
@@ -442,18 +474,20 @@ cudaError_t gw_spectrum_device(GwCache &cache, cudaStream_t stream, const BoxDev
     const int P = N * zero_padding;
     return gw_spectrum_packed(
         cache, stream, P, N, projection_type, unbinned, scratch, bins_dev, nbins, launches, err,
-        [&](int q, double *real) {
+        [&](int q, double *dst, int stride) {
             int g = (int)std::min<long long>((nvalid + 255) / 256, 152LL * 32);
             gw_pack_kernel<<<std::max(g, 1), 256, 0, stream>>>(boxes, vbase, nbox, nvalid, ncomp,
-                                                                comps[q], buf, real, P, dlo[0],
-                                                                dlo[1], dlo[2]);
+                                                                comps[q], buf, dst, stride, P,
+                                                                dlo[0], dlo[1], dlo[2]);
         });
 }
 
 size_t gw_scratch_bytes(int N, int zero_padding) {
     const long long P = (long long)N * zero_padding;
     const long long H = P / 2 + 1;
-    return (size_t)(P * P * P + 12 * H * P * P + H * P * P) * sizeof(double);
+    /* GW: three complex P^3 arrays + per-cell values; scalar spectra: a real
+     * P^3 array + a half-spectrum + per-cell values (smaller) */
+    return (size_t)(6 * P * P * P + H * P * P) * sizeof(double);
 }
 
 } // namespace sh

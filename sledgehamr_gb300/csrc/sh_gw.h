@@ -29,10 +29,13 @@ struct GwBins {
  * stable parallel counting sort, so cells stay in ascending order within a
  * bin and sums are reproducible). */
 struct GwCache {
-    static constexpr int kMaxBins = 4, kMaxPlans = 2;
+    static constexpr int kMaxBins = 4, kMaxPlans = 3;
+    /* plan kinds: one real-to-complex P^3 transform (scalar spectra), three
+     * in-place complex P^3 transforms (the GW components in pairs) */
+    static constexpr int kPlanD2Z = 0, kPlanZ2Z3 = 1;
     std::vector<GwBins> bins;
     struct Plan {
-        int P = 0;
+        int P = 0, kind = 0;
         cufftHandle h = 0;
         long long used = 0;
     };
@@ -42,9 +45,9 @@ struct GwCache {
     /* k^2 of the bins of the last prepared kind */
     const std::vector<long long> &ks() const { return cur->ks; }
     void prepare(int P, int unbinned, int projection_type);
-    /* cuFFT D2Z plan of a P^3 transform (created on first use); false if
-     * cuFFT fails */
-    bool plan(int P, cufftHandle *out);
+    /* cuFFT plan of a kind for P^3 (created on first use); false if cuFFT
+     * fails */
+    bool plan(int P, int kind, cufftHandle *out);
     void release();
 };
 
@@ -57,15 +60,16 @@ cudaError_t scalar_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, d
                                    double *scratch, double *bins_dev, int *nbins,
                                    long long *launches, std::string &err,
                                    const std::function<void(double *)> &pack);
-/* FFT, TT projection and binning of six P^3 real arrays that `pack(q, real)`
- * writes (enqueued on `stream`) into the zeroed `real` for q = 0..5 in the
- * order du_xx, du_xy, du_xz, du_yy, du_yz, du_zz; `real` is zeroed first
- * only when the packed N^3 block does not fill it (N < P). */
+/* FFT, TT projection and binning of six P^3 real fields that
+ * `pack(q, dst, stride)` writes (enqueued on `stream`) for q = 0..5 in the
+ * order du_xx, du_xy, du_xz, du_yy, du_yz, du_zz, element (x, y, z) at
+ * dst[stride * ((z P + y) P + x)]; the destination is zeroed first only
+ * when the packed N^3 block does not fill it (N < P). */
 cudaError_t gw_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, int N,
                                int projection_type, int unbinned, double *scratch,
-                               double *bins_dev, int *nbins,
-                               long long *launches, std::string &err,
-                               const std::function<void(int, double *)> &pack);
+                               double *bins_dev, int *nbins, long long *launches,
+                               std::string &err,
+                               const std::function<void(int, double *, int)> &pack);
 cudaError_t gw_spectrum_device(GwCache &cache, cudaStream_t stream, const BoxDev *boxes,
                                const long long *vbase, int nbox, long long nvalid, int ncomp,
                                const double *buf, const int comps[6], int N, const int dlo[3],
