@@ -591,9 +591,10 @@ class ClockSampler:
                 "samples": len(self.samples)}
 
 
-def amr_config(sh):
+def amr_config(sh, precision=0):
     a = AMR
-    return sh.amr_config(a["project"], N0=a["N0"], L=a["L"], cfl=a["cfl"], t_start=a["t_start"],
+    return sh.amr_config(a["project"], precision=precision, N0=a["N0"], L=a["L"], cfl=a["cfl"],
+                         t_start=a["t_start"],
                          nghost=a["nghost"], max_level=a["max_level"],
                          blocking_factor=a["blocking_factor"], max_grid_size=a["max_grid_size"],
                          n_error_buf=a["n_error_buf"], regrid_dt=a["regrid_dt"],
@@ -923,6 +924,9 @@ def run_amr_leg(sh, ctx, stream, flush, steps, warmup, peak, peak_kind):
     levels = [{"level": l, "boxes": sim.level(l).nbox, "cells": sim.level(l).nvalid}
               for l in range(info["finest"] + 1)]
     timers = {k: round(v[0], 4) for k, v in sim.timers().items()}
+    # the precision form on the same hierarchy: FP32 + Kahan levels, FP64
+    # truncation errors and tags, the same pre-roll and timed window
+    fp32 = run_amr_fp32(sh, ctx, stream, flush, K, pre, sim, ms)
     sim.close()
     # e2e: the same job from pinned host memory, read back at the end
     host_in = torch.from_numpy(np.ascontiguousarray(state)).pin_memory()
@@ -952,13 +956,67 @@ def run_amr_leg(sh, ctx, stream, flush, steps, warmup, peak, peak_kind):
            "gpu_launches_per_step": launches / K,
            "stage_launches_per_step": roof["stage_launches"] / K,
            "cell_updates_timed": cus, "levels_at_end": levels,
-           "host_timers_s": timers, "roofline": roof,
+           "host_timers_s": timers, "roofline": roof, "fp32_kahan": fp32,
            "e2e": {"value": e2e_cus / e2e_s, "unit": METRIC, "job_steps": pre + K,
                    "h2d_bytes_per_step": state.size * 8 / (pre + K),
                    "d2h_bytes_per_step": d2h / (pre + K),
                    "note": "whole job from the host initial state: the pre-roll to full "
                            "depth and the timed window, hierarchy read back at the end"}}
     return out
+
+
+def amr_levels(sh, ctx, sim):
+    """Boxes, FP64 values (boxes layout, on the device) and string-tag
+    counts of every level of a hierarchy."""
+    import torch
+    a = AMR
+    dt0 = a["cfl"] * a["L"] / a["N0"]
+    out = []
+    for l in range(sim.info()["finest"] + 1):
+        v = sim.level(l)
+        d = torch.empty(v.nvalid * v.ncomp, dtype=torch.float64, device="cuda")
+        ctx.check(ctx.lib.sh_level_read_device(ctx.h, v.h, sh.SH_NEW, 1, d.data_ptr()), "read")
+        t = v.time()[0]
+        tags = v.string_tags(t, l, dt0 / 2 ** l, a["L"] / a["N0"] / 2 ** l)
+        out.append((v.boxes, d, tags))
+    return out
+
+
+def run_amr_fp32(sh, ctx, stream, flush, K, pre, sim64, ms64):
+    """The AMR workload on FP32 + Kahan levels (sh_amr_config.precision):
+    the FP64 leg's pre-roll, then its K timed coarse steps; errors at the
+    end against the FP64 hierarchy (which has run the same steps): relative
+    L2 per level where the boxes agree, and the string-tag counts."""
+    import torch
+    sim = sh.Amr(ctx, amr_config(sh, sh.PREC_FP32_KAHAN), amr_state())
+    for _ in range(pre):
+        sim.step(1)
+    cu0 = sim.info()["cell_updates"]
+    ctx.profile(True)
+    ms, finest = timed_steps(lambda: sim.step(1), K, 0, stream, flush,
+                             before=lambda: sim.info()["finest"])
+    cus = sim.info()["cell_updates"] - cu0
+    stage_ms, stage_n = ctx.profile_read("rhs")
+    fill_ms, _ = ctx.profile_read("fill_patch")
+    cf_ms, _ = ctx.profile_read("coarse_fine")
+    ctx.profile(False)
+    mine, ref = amr_levels(sh, ctx, sim), amr_levels(sh, ctx, sim64)
+    err = []
+    for l, ((b32, d32, t32), (b64, d64, t64)) in enumerate(zip(mine, ref)):
+        row = {"level": l, "boxes_equal": b32 == b64, "string_tags_fp32": t32,
+               "string_tags_fp64": t64}
+        if b32 == b64:
+            row["rel_l2"] = float(torch.linalg.norm(d32 - d64) / torch.linalg.norm(d64))
+        err.append(row)
+    sim.close()
+    del mine, ref
+    return {"value": cus / (ms / 1e3), "unit": METRIC, "ms_per_step": ms / K,
+            "speedup_vs_fp64": ms64 / ms, "levels_in_timed_window": sorted({f + 1 for f in finest}),
+            "stage_ms_total": stage_ms, "stage_launches": stage_n, "fill_ms_total": fill_ms,
+            "coarse_fine_ms_total": cf_ms, "error_vs_fp64": err,
+            "note": "FP32 values with FP32 Kahan compensations on every level, FP32 stage "
+                    "arithmetic (csrc/sh_stage32.cuh); truncation errors, tags through the "
+                    "project hooks, average-down sums and time in FP64"}
 
 
 def main():

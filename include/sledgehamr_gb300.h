@@ -152,6 +152,22 @@ SH_API int sh_project_comp_name(int id, int comp, const char **name);
 SH_API int sh_level_create(sh_ctx *ctx, int project, int with_gw, const int domain_lo[3],
                     const int domain_hi[3], const sh_box *boxes, int nbox, int nghost,
                     sh_level **out);
+/* sh_level_create with a storage precision: SH_PREC_FP64 (the reference's
+ * FArrayBox data), or SH_PREC_FP32_KAHAN, the precision form on levels:
+ * FP32 values with FP32 Kahan compensations (value v and compensation c
+ * stand for v - c), advanced by FP32 stage kernels written against the
+ * equations (RKN4 only; the axion-string projects AxionStringsLap1 / Lap2
+ * without GW tensor), while time, average-down, truncation errors (kept in
+ * FP64), tagging through the project's hooks, reductions, spectra and
+ * outputs work on the FP64 values v - c.  Reads and writes convert; the
+ * Rhs hook (sh_level_rhs), bubble injection and sh_tag_static need FP64
+ * levels (SH_ERR_UNSUPPORTED).  No reference counterpart (sledgehamr
+ * stores FP64 only). */
+SH_API int sh_level_create_prec(sh_ctx *ctx, int project, int with_gw,
+                                const int domain_lo[3], const int domain_hi[3],
+                                const sh_box *boxes, int nbox, int nghost, int precision,
+                                sh_level **out);
+SH_API int sh_level_precision(const sh_level *level, int *precision);
 SH_API int sh_level_destroy(sh_ctx *ctx, sh_level *level);
 /* Index domain of a level (lo, hi inclusive). */
 SH_API int sh_level_domain(const sh_level *level, int lo[3], int hi[3]);
@@ -500,6 +516,11 @@ typedef struct sh_amr_config {
     int max_local_regrids;
     double volume_threshold_strong;
     double volume_threshold_weak;
+    /* storage of every level: SH_PREC_FP64 (default) or SH_PREC_FP32_KAHAN
+     * (sh_level_create_prec; RKN4, AxionStringsLap1 / Lap2): the precision
+     * form on hierarchies, with the truncation errors, tags, average-down
+     * sums and time in FP64 */
+    int precision;
 } sh_amr_config;
 /* New-grid generation from the buffered tags (at blocking-factor
  * resolution): Berger-Rigoutsos clustering to efficiency grid_eff, then

@@ -208,9 +208,12 @@ class Level:
     """A level of boxes with two time levels (sh_level)."""
 
     def __init__(self, ctx: Context, project: str, boxes, domain_lo, domain_hi, nghost: int,
-                 with_gw: bool = False):
+                 with_gw: bool = False, precision: int = 0):
+        """precision: PREC_FP64 (default) or PREC_FP32_KAHAN (FP32 values with
+        Kahan compensations; RKN4 axion-string levels, sh_level_create_prec)."""
         self.ctx = ctx
         self.project = project
+        self.precision = precision
         arr = (ShBox * len(boxes))()
         for q, (lo, hi) in enumerate(boxes):
             arr[q].lo[:] = list(lo)
@@ -218,8 +221,9 @@ class Level:
         dlo = (C.c_int * 3)(*domain_lo)
         dhi = (C.c_int * 3)(*domain_hi)
         h = C.c_void_p()
-        ctx.check(ctx.lib.sh_level_create(ctx.h, project_id(project), int(with_gw), dlo, dhi,
-                                          arr, len(boxes), nghost, C.byref(h)),
+        ctx.check(ctx.lib.sh_level_create_prec(ctx.h, project_id(project), int(with_gw), dlo,
+                                               dhi, arr, len(boxes), nghost, precision,
+                                               C.byref(h)),
                   "sh_level_create")
         self.h = h
         self.boxes = [(tuple(lo), tuple(hi)) for lo, hi in boxes]
@@ -230,9 +234,9 @@ class Level:
 
     @classmethod
     def periodic(cls, ctx: Context, project: str, N: int, nghost: int, max_grid: int = 0,
-                 with_gw: bool = False) -> "Level":
+                 with_gw: bool = False, precision: int = 0) -> "Level":
         return cls(ctx, project, chop_boxes(N, max_grid), (0, 0, 0), (N - 1, N - 1, N - 1),
-                   nghost, with_gw)
+                   nghost, with_gw, precision)
 
     def close(self):
         if getattr(self, "h", None):

@@ -64,7 +64,8 @@ class ShAmrConfig(C.Structure):
                 ("nparams_tag", C.c_int), ("params_mod", C.c_double * 32),
                 ("nparams_mod", C.c_int), ("params_mod_norm0", C.c_int),
                 ("check_finite", C.c_int), ("max_local_regrids", C.c_int),
-                ("volume_threshold_strong", C.c_double), ("volume_threshold_weak", C.c_double)]
+                ("volume_threshold_strong", C.c_double), ("volume_threshold_weak", C.c_double),
+                ("precision", C.c_int)]
 
 
 class ShRequest(C.Structure):
@@ -110,6 +111,9 @@ SIGNATURES = {
                                         C.c_int, vp, vp]),
     "sh_level_create": (C.c_int, [vp, C.c_int, C.c_int, ip, ip, C.POINTER(ShBox), C.c_int,
                                   C.c_int, C.POINTER(vp)]),
+    "sh_level_create_prec": (C.c_int, [vp, C.c_int, C.c_int, ip, ip, C.POINTER(ShBox), C.c_int,
+                                       C.c_int, C.c_int, C.POINTER(vp)]),
+    "sh_level_precision": (C.c_int, [vp, ip]),
     "sh_level_destroy": (C.c_int, [vp, vp]),
     "sh_level_info": (C.c_int, [vp, ip, ip, llp]),
     "sh_level_time": (C.c_int, [vp, C.c_int, dp, ip]),

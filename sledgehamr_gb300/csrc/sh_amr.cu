@@ -50,8 +50,8 @@ struct GpuBackend {
             }
         const int lo[3] = {0, 0, 0}, hi[3] = {N - 1, N - 1, N - 1};
         GpuLevel *g = new GpuLevel();
-        ok(sh_level_create(ctx, cfg.project, cfg.with_gw, lo, hi, bx.data(), (int)bx.size(),
-                           cfg.nghost, &g->L),
+        ok(sh_level_create_prec(ctx, cfg.project, cfg.with_gw, lo, hi, bx.data(),
+                                (int)bx.size(), cfg.nghost, cfg.precision, &g->L),
            "sh_level_create");
         sh_level_set_index(g->L, lev);
         g->gen = next_gen++;

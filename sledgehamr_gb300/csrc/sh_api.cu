@@ -23,6 +23,7 @@
 #include "sh_fixed_stencil.h"
 #include "sh_gw.h"
 #include "sh_internal.h"
+#include "sh_stage32.cuh"
 
 /* ---- project registry --------------------------------------------------- */
 namespace sh {
@@ -158,7 +159,19 @@ struct sh_level {
     int nghost_items = 0;
     long long nghost_cells = 0;
     long long *d_vbase = nullptr; /* nbox + 1 */
-    double *buf[3] = {nullptr, nullptr, nullptr}; /* SH_NEW, SH_OLD, alt */
+    /* SH_NEW, SH_OLD, alt.  FP32 levels (esize 4) keep FP32 values here,
+     * read through f32buf(); the pointer type stays double * so that the
+     * FP64 path is untouched */
+    double *buf[3] = {nullptr, nullptr, nullptr};
+    int esize = 8; /* 8: FP64 storage; 4: FP32 values with FP32 Kahan compensations */
+    /* FP32 levels: compensations of SH_NEW / SH_OLD (the value v and its
+     * compensation c stand for v - c), the truncation errors in FP64 (an
+     * FP64 level keeps them in its SH_OLD buffer, as the reference does),
+     * and an FP64 copy of one buffer for the read-only operations that go
+     * through the FP64 hooks and kernels (tagging, reductions, outputs) */
+    float *cmp[2] = {nullptr, nullptr};
+    double *te64 = nullptr;
+    double *view64 = nullptr;
     double *kbuf = nullptr;  /* K buffers, kbuf_elems each */
     size_t kbuf_elems = 0;
     int kbuf_count = 0;
@@ -324,9 +337,10 @@ __device__ __forceinline__ int find_box(const long long *vbase, int nbox, long l
 
 /* layout 0: canonical domain array; layout 1: boxes (packed valid cells).
  * dir 0: host-side array -> level buffer; dir 1: level buffer -> array. */
+template <class T>
 __global__ void move_kernel(const BoxDev *boxes, const long long *vbase, int nbox, int ncomp,
-                            long long nvalid, double *buf, double *arr, int layout, int dir,
-                            int N0, int N1, int N2, int dlo0, int dlo1, int dlo2) {
+                            long long nvalid, T *buf, float *cmp, double *arr, int layout,
+                            int dir, int N0, int N1, int N2, int dlo0, int dlo1, int dlo2) {
     const long long total = nvalid * ncomp;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
          e += (long long)gridDim.x * blockDim.x) {
@@ -347,9 +361,29 @@ __global__ void move_kernel(const BoxDev *boxes, const long long *vbase, int nbo
             ai = (((long long)n * N2 + (k - dlo2)) * N1 + (j - dlo1)) * N0 + (i - dlo0);
         else
             ai = vbase[bx] * ncomp + (long long)n * (vbase[bx + 1] - vbase[bx]) + lv;
-        if (dir == 0) buf[bi] = arr[ai];
-        else arr[ai] = buf[bi];
+        if constexpr (sizeof(T) == 8) {
+            if (dir == 0) buf[bi] = arr[ai];
+            else arr[ai] = buf[bi];
+        } else {
+            /* FP32 value and compensation of an FP64 value x: v = fl32(x),
+             * c = fl32(v - x), so that v - c is x to about 2^-48 */
+            if (dir == 0) {
+                const double x = arr[ai];
+                const float v = (float)x;
+                buf[bi] = v;
+                cmp[bi] = (float)((double)v - x);
+            } else {
+                arr[ai] = (double)buf[bi] - (double)cmp[bi];
+            }
+        }
     }
+}
+
+/* FP64 copy v - c of a whole FP32 buffer (ghost cells included). */
+__global__ void widen_kernel(const float *v, const float *c, double *out, long long n) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x)
+        out[e] = (double)v[e] - (c ? (double)c[e] : 0.);
 }
 
 /* Copies of rectangles of cells (ghost fill from the same level, periodic
@@ -366,8 +400,9 @@ __global__ void move_kernel(const BoxDev *boxes, const long long *vbase, int nbo
  * components before it stores any (measured against one cell, and against
  * four cells at 128 registers, which lost occupancy). */
 constexpr int kItemThreads = 128; /* threads per item of the copy and combine kernels */
-__global__ void copy_items_kernel(const CopyItem *__restrict__ items, double *__restrict__ dst,
-                                  const double *__restrict__ src, int ncomp) {
+template <class T>
+__global__ void copy_items_kernel(const CopyItem *__restrict__ items, T *__restrict__ dst,
+                                  const T *__restrict__ src, int ncomp) {
     const CopyItem it = items[blockIdx.x];
     const int nxy = it.nx * it.ny;
     const int n = nxy * it.nz;
@@ -388,7 +423,7 @@ __global__ void copy_items_kernel(const CopyItem *__restrict__ items, double *__
         offsets(t0, d0, s0);
         if (two) offsets(t1, d1, s1);
         for (int c0 = 0; c0 < ncomp; c0 += 4) {
-            double v0[4], v1[4];
+            T v0[4], v1[4];
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
                 if (c0 + c >= ncomp) continue;
@@ -425,8 +460,8 @@ struct OwnerMapDev {
  * (sh_fixed_stencil.h, A their largest exponent), rounded once to FP64.
  * The partial sums stay below 124 * 2^56 < 2^63.  Returns false (and writes
  * nothing) when a value is not finite; the FP64 formula then runs. */
-template <class Put>
-__device__ __forceinline__ bool cf_children_fixed(const double *src, long long base, long long cx,
+template <class T, class Put>
+__device__ __forceinline__ bool cf_children_fixed(const T *src, long long base, long long cx,
                                                   long long cxy, const int P[3], const int c0[3],
                                                   const int c1[3], Put &put) {
     namespace fx = sledgehamr::utils::fixed;
@@ -437,7 +472,7 @@ __device__ __forceinline__ bool cf_children_fixed(const double *src, long long b
                                cx + cxy, cx - cxy, -cx + cxy, -cx - cxy};
     double v[19];
 #pragma unroll
-    for (int q = 0; q < 19; ++q) v[q] = src[base + off[q]];
+    for (int q = 0; q < 19; ++q) v[q] = (double)src[base + off[q]];
     int hi[19];
     const int A = fx::anchor(v, hi);
     if (A == 0x7FF) return false;
@@ -477,10 +512,11 @@ __device__ __forceinline__ bool cf_children_fixed(const double *src, long long b
  * (xi_d^2 = 1/16 for every child, so the second-order term is shared).
  * The parent (periodically wrapped) is found through the coarse level's
  * block map; its neighbours are read from the parent box's ghost cells. */
-__global__ void cf_interp_kernel(const CfItem *items, const BoxDev *cboxes, double *fbuf,
-                                 OwnerMapDev cmap, const double *c_old, const double *c_new,
-                                 int mode, double alpha, double beta, int ncomp, double *store,
-                                 long long ncf) {
+template <class T>
+__global__ void cf_interp_kernel(const CfItem *items, const BoxDev *cboxes, T *fbuf,
+                                 OwnerMapDev cmap, const T *c_old, const T *c_new, int mode,
+                                 double alpha, double beta, int ncomp, T *store, long long ncf,
+                                 float *fcmp) {
     const CfItem it = items[blockIdx.x];
     auto fl2 = [](int a) { return a >= 0 ? a / 2 : -((-a + 1) / 2); };
     const int lo[3] = {it.lo[0], it.lo[1], it.lo[2]};
@@ -514,22 +550,26 @@ __global__ void cf_interp_kernel(const CfItem *items, const BoxDev *cboxes, doub
         for (int nn = 0; nn < ncomp; ++nn) {
             const long long base = cbase + nn * cb.gvol;
             auto put = [&](int fi, int fj, int fk, double v) {
-                if (store)
+                if (store) {
                     store[it.first + (fi - lo[0]) +
                           (long long)it.nx * ((fj - lo[1]) + (long long)it.ny * (fk - lo[2])) +
-                          nn * ncf] = v;
-                else
-                    fbuf[it.dst + (fi - lo[0]) + (long long)(fj - lo[1]) * it.dsy +
-                         (long long)(fk - lo[2]) * it.dsz + nn * it.dgvol] = v;
+                          nn * ncf] = (T)v;
+                } else {
+                    const long long d = it.dst + (fi - lo[0]) + (long long)(fj - lo[1]) * it.dsy +
+                                        (long long)(fk - lo[2]) * it.dsz + nn * it.dgvol;
+                    fbuf[d] = (T)v;
+                    /* FP32 levels: the compensation of a cell filled for good */
+                    if (fcmp) fcmp[d] = (float)((double)(T)v - v);
+                }
             };
             if (mode != 2 && cf_children_fixed(mode == 0 ? c_old : c_new, base, cx, cxy, P, c0,
                                                c1, put))
                 continue;
             auto u = [&](int a, int b2, int d) {
                 const long long e = base + a + b2 * cx + d * cxy;
-                if (mode == 0) return c_old[e];
-                if (mode == 1) return c_new[e];
-                return alpha * c_old[e] + beta * c_new[e];
+                if (mode == 0) return (double)c_old[e];
+                if (mode == 1) return (double)c_new[e];
+                return alpha * (double)c_old[e] + beta * (double)c_new[e];
             };
             const double u0 = u(0, 0, 0);
             const double dxp = u(1, 0, 0), dxm = u(-1, 0, 0);
@@ -567,10 +607,11 @@ __global__ void cf_interp_kernel(const CfItem *items, const BoxDev *cboxes, doub
 /* Coarse-fine ghost cells from the stored spatial interpolations of the
  * coarse old and new data: the interpolation is linear in the coarse data,
  * so interpolating alpha old + beta new equals alpha I(old) + beta I(new). */
-__global__ void cf_combine_kernel(const CfItem *__restrict__ items, double *__restrict__ fbuf,
-                                  const double *__restrict__ i_old,
-                                  const double *__restrict__ i_new, int mode, double alpha,
-                                  double beta, int ncomp, long long ncf) {
+template <class T>
+__global__ void cf_combine_kernel(const CfItem *__restrict__ items, T *__restrict__ fbuf,
+                                  const T *__restrict__ i_old, const T *__restrict__ i_new,
+                                  int mode, double alpha, double beta, int ncomp,
+                                  long long ncf) {
     const CfItem it = items[blockIdx.x];
     const int nxy = it.nx * it.ny;
     const int n = nxy * it.nz;
@@ -590,13 +631,13 @@ __global__ void cf_combine_kernel(const CfItem *__restrict__ items, double *__re
             for (int u = 0; u < 4; ++u) {
                 if (c0 + u >= ncomp) continue;
                 const long long e = c + (c0 + u) * ncf;
-                if (mode == 0) v[u] = __ldg(i_old + e);
-                else if (mode == 1) v[u] = __ldg(i_new + e);
-                else v[u] = alpha * __ldg(i_old + e) + beta * __ldg(i_new + e);
+                if (mode == 0) v[u] = (double)__ldg(i_old + e);
+                else if (mode == 1) v[u] = (double)__ldg(i_new + e);
+                else v[u] = alpha * (double)__ldg(i_old + e) + beta * (double)__ldg(i_new + e);
             }
 #pragma unroll
             for (int u = 0; u < 4; ++u)
-                if (c0 + u < ncomp) fbuf[d + (c0 + u) * it.dgvol] = v[u];
+                if (c0 + u < ncomp) fbuf[d + (c0 + u) * it.dgvol] = (T)v[u];
         }
     }
 }
@@ -782,9 +823,13 @@ __global__ void __launch_bounds__(kReduceThreads)
     if (threadIdx.x == 0) out[0] = v;
 }
 
+/* FP32 levels (T = float): the fine values are read as v - c with their
+ * compensations fc, the average is formed in FP64 and stored as a value and
+ * compensation (cc), the truncation error goes to an FP64 array. */
+template <class T>
 __global__ void avgdown_kernel(const AvgRect *rects, int nrects, long long ncells,
                                const BoxDev *fboxes, const BoxDev *cboxes, int ncomp,
-                               const double *fine, double *crse, double *te) {
+                               const T *fine, const float *fc, T *crse, float *cc, double *te) {
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncells;
          c += (long long)gridDim.x * blockDim.x) {
         int lo = 0, hi = nrects - 1;
@@ -807,6 +852,25 @@ __global__ void avgdown_kernel(const AvgRect *rects, int nrects, long long ncell
         const long long c0 = cb.off * ncomp + (i - cb.glo[0]) +
                              (long long)(j - cb.glo[1]) * cb.gdim[0] +
                              (long long)(k - cb.glo[2]) * cb.gdim[0] * cb.gdim[1];
+        if constexpr (sizeof(T) == 4) {
+            for (int n = 0; n < ncomp; ++n) {
+                const long long fo = f0 + n * fb.gvol;
+                double s = 0.0;
+                for (int dk = 0; dk < 2; ++dk)
+                    for (int dj = 0; dj < 2; ++dj)
+                        for (int di = 0; di < 2; ++di) {
+                            const long long e = fo + di + dj * fx + dk * fxy;
+                            s += (double)fine[e] - (double)fc[e];
+                        }
+                const double avg = 0.125 * s;
+                const long long co = c0 + n * cb.gvol;
+                if (te) te[fo] = fabs(((double)crse[co] - (double)cc[co]) - avg);
+                const float v = (float)avg;
+                crse[co] = v;
+                cc[co] = (float)((double)v - avg);
+            }
+            continue;
+        } else
         for (int n = 0; n < ncomp; ++n) {
             const double *f = fine + f0 + n * fb.gvol;
             if (te) {
@@ -1179,6 +1243,35 @@ void level_free(sh_ctx *ctx, sh_level *L) {
     dfree_async(ctx, L->cf_new);
     for (int q = 0; q < 3; ++q) dfree_async(ctx, L->buf[q]);
     dfree_async(ctx, L->kbuf);
+    dfree_async(ctx, L->cmp[0]);
+    dfree_async(ctx, L->cmp[1]);
+    dfree_async(ctx, L->te64);
+    dfree_async(ctx, L->view64);
+}
+
+/* An FP64 view of buffer `which` of L for read-only work through the FP64
+ * kernels and hooks: the buffer itself on an FP64 level; on an FP32 level
+ * v - c of every element (ghost cells included) in the level's FP64 copy,
+ * valid until the next call of this function on L. */
+const double *state64(sh_ctx *ctx, const sh_level *L, int which) {
+    if (L->esize == 8) return L->buf[which];
+    sh_level *Lm = const_cast<sh_level *>(L);
+    const long long n = L->total_gvol * L->ncomp;
+    if (!Lm->view64) Lm->view64 = (double *)dmalloc_async(ctx, n * sizeof(double), "FP64 view");
+    widen_kernel<<<grid_for(n), 256, 0, ctx->stream>>>(
+        (const float *)L->buf[which], which == SH_NEW || which == SH_OLD ? L->cmp[which] : nullptr,
+        Lm->view64, n);
+    ctx->launches++;
+    ck(cudaGetLastError(), "FP64 view launch");
+    return Lm->view64;
+}
+
+/* The truncation errors of L (FP64 levels: its old buffer). */
+const double *te_of(const sh_level *L) { return L->esize == 8 ? L->buf[SH_OLD] : L->te64; }
+
+inline void require_fp64(const sh_level *L, const char *what) {
+    if (L->esize != 8)
+        throw ShError(SH_ERR_UNSUPPORTED, std::string(what) + " needs an FP64 level");
 }
 
 void ensure_kbuf(sh_ctx *ctx, sh_level *L, size_t elems, int count) {
@@ -1222,11 +1315,12 @@ bool fill_current(const sh_level *L, const double *buf, double t, long long ver)
     return false;
 }
 
-void fill_patch(sh_ctx *ctx, sh_level *L, double *buf, double t) {
+template <class T>
+void fill_patch_t(sh_ctx *ctx, sh_level *L, T *buf, double t) {
     if (L->nghost_items > 0) {
         ProfScope ps(ctx, kProfFill);
-        copy_items_kernel<<<L->nghost_items, kItemThreads, 0, ctx->stream>>>(L->d_ghost, buf, buf,
-                                                                   L->ncomp);
+        copy_items_kernel<T><<<L->nghost_items, kItemThreads, 0, ctx->stream>>>(L->d_ghost, buf,
+                                                                              buf, L->ncomp);
         ctx->launches++;
         ck(cudaGetLastError(), "ghost fill launch");
     }
@@ -1238,14 +1332,15 @@ void fill_patch(sh_ctx *ctx, sh_level *L, double *buf, double t) {
              * coarse data version (every fine sub-step and stage between two
              * coarse steps reuses it) */
             if (!L->cf_old) {
-                const size_t bytes = (size_t)L->ncf * L->ncomp * sizeof(double);
+                const size_t bytes = (size_t)L->ncf * L->ncomp * sizeof(T);
                 L->cf_old = (double *)dmalloc_async(ctx, bytes, "coarse-fine values");
                 L->cf_new = (double *)dmalloc_async(ctx, bytes, "coarse-fine values");
             }
             for (int m = 0; m < 2; ++m) {
-                cf_interp_kernel<<<L->ncf_items, 128, 0, ctx->stream>>>(
-                    L->d_cf, C->d_boxes, nullptr, owner_map_dev(C), C->buf[SH_OLD],
-                    C->buf[SH_NEW], m, 0., 0., L->ncomp, m == 0 ? L->cf_old : L->cf_new, L->ncf);
+                cf_interp_kernel<T><<<L->ncf_items, 128, 0, ctx->stream>>>(
+                    L->d_cf, C->d_boxes, nullptr, owner_map_dev(C), (const T *)C->buf[SH_OLD],
+                    (const T *)C->buf[SH_NEW], m, 0., 0., L->ncomp,
+                    (T *)(m == 0 ? L->cf_old : L->cf_new), L->ncf, nullptr);
                 ctx->launches++;
             }
             L->cf_uid = C->uid;
@@ -1254,11 +1349,19 @@ void fill_patch(sh_ctx *ctx, sh_level *L, double *buf, double t) {
         int mode;
         double alpha, beta;
         coarse_time_weights(C, t, mode, alpha, beta);
-        cf_combine_kernel<<<L->ncf_items, kItemThreads, 0, ctx->stream>>>(
-            L->d_cf, buf, L->cf_old, L->cf_new, mode, alpha, beta, L->ncomp, L->ncf);
+        cf_combine_kernel<T><<<L->ncf_items, kItemThreads, 0, ctx->stream>>>(
+            L->d_cf, buf, (const T *)L->cf_old, (const T *)L->cf_new, mode, alpha, beta, L->ncomp,
+            L->ncf);
         ctx->launches++;
         ck(cudaGetLastError(), "coarse-fine fill launch");
     }
+}
+
+/* FP32 levels store floats behind the double pointers of their buffers
+ * (and of the coarse-fine value caches): same layout, element size 4. */
+void fill_patch(sh_ctx *ctx, sh_level *L, double *buf, double t) {
+    if (L->esize == 4) fill_patch_t<float>(ctx, L, (float *)buf, t);
+    else fill_patch_t<double>(ctx, L, buf, t);
     note_fill(L, buf, t);
 }
 
@@ -1450,7 +1553,81 @@ void integrate(sh_ctx *ctx, sh_level *L, int type, const double *tableau, int ns
     }
 }
 
-void move(sh_ctx *ctx, const sh_level *L, double *buf, double *arr, int layout, int dir) {
+/* 1 (7-point) or 2 (13-point Laplacian) for the projects whose FP32
+ * levels have stage kernels (sh_stage32.cuh), else 0. */
+int stage32_family(const ProjectOps *ops) {
+    if (!ops || !ops->name) return 0;
+    if (std::strcmp(ops->name, "AxionStringsLap1") == 0) return 1;
+    if (std::strcmp(ops->name, "AxionStringsLap2") == 0) return 2;
+    return 0;
+}
+
+/* One RKN4 step of an FP32 level (the old buffer's ghost cells filled):
+ * the stage schedule of integrate() with the FP32 axion kernels; the stage
+ * buffers' ghost cells are filled at the stage times between launches.
+ * Stage 0 writes Y1 into SH_NEW, stage 1 Y2 into the third buffer, the
+ * last stage y1 into SH_NEW with its compensations. */
+void integrate32(sh_ctx *ctx, sh_level *L, int type, double dt, double dx,
+                 const double *params, int nparams, int ko_order) {
+    require(type == SH_INTEGRATOR_RKN4, "FP32 levels integrate with RKN4 (type 21)");
+    require(ko_order == 0, "FP32 levels have no Kreiss-Oliger dissipation");
+    require(params && nparams >= 2, "FP32 axion levels need the parameters (lambda, c)");
+    const int order = stage32_family(L->ops);
+    require(order != 0, "no FP32 stage kernel for this project");
+    ensure_kbuf(ctx, L, (size_t)L->total_gvol, 2); /* two K of 2 FP32 components */
+    float *k0 = (float *)L->kbuf, *k1 = k0 + (size_t)L->total_gvol * 2;
+    const double t0 = L->t[SH_OLD];
+    Stage32Args a;
+    std::memset(&a, 0, sizeof(a));
+    a.tiles = L->d_tiles;
+    a.boxes = L->d_boxes;
+    a.y0 = (const float *)L->buf[SH_OLD];
+    a.k0 = k0;
+    a.k1 = k1;
+    a.c_old = L->cmp[SH_OLD];
+    a.c_new = L->cmp[SH_NEW];
+    a.h = (float)dt;
+    a.h2 = (float)(dt * dt);
+    const float inv_dx2 = (float)(1. / (dx * dx));
+    a.inv = order == 1 ? inv_dx2 : inv_dx2 / 12.f;
+    a.lam = (float)params[0];
+    a.cst = (float)params[1];
+    double *const src[3] = {L->buf[SH_OLD], L->buf[SH_NEW], L->buf[2]};
+    double *const dst[3] = {L->buf[SH_NEW], L->buf[2], L->buf[SH_NEW]};
+    const double node[3] = {0., 0.5, 1.};
+    for (int st = 0; st < 3; ++st) {
+        const double ts = t0 + dt * node[st];
+        a.state = (const float *)src[st];
+        a.out = (float *)dst[st];
+        a.friction = (float)(-2. / ts);
+        a.eta2 = (float)(ts * ts);
+        a.kout = st == 0 ? k0 : (st == 1 ? k1 : nullptr);
+        a.cm = (float)(st == 0 ? 0.5 * dt : dt);
+        a.ck = (float)(st == 0 ? dt * dt / 8. : dt * dt / 2.);
+        {
+            ProfScope ps(ctx, kProfRhs);
+            if (L->ntiles > 0) {
+                dim3 block(kTileX, kTileY, 1);
+#define SH_STAGE32(O, S) stage32_axion_kernel<O, S><<<L->ntiles, block, 0, ctx->stream>>>(a)
+                if (order == 1) {
+                    if (st == 0) SH_STAGE32(1, 0);
+                    else if (st == 1) SH_STAGE32(1, 1);
+                    else SH_STAGE32(1, 2);
+                } else {
+                    if (st == 0) SH_STAGE32(2, 0);
+                    else if (st == 1) SH_STAGE32(2, 1);
+                    else SH_STAGE32(2, 2);
+                }
+#undef SH_STAGE32
+                ctx->launches++;
+                ck(cudaGetLastError(), "FP32 stage kernel launch");
+            }
+        }
+        fill_patch(ctx, L, dst[st], st < 2 ? t0 + dt * node[st + 1] : t0 + dt);
+    }
+}
+
+void move(sh_ctx *ctx, const sh_level *L, int which, double *arr, int layout, int dir) {
     require(layout == 0 || layout == 1, "layout must be 0 (canonical) or 1 (boxes)");
     if (layout == 0) {
         long long dv = 1;
@@ -1459,10 +1636,19 @@ void move(sh_ctx *ctx, const sh_level *L, double *buf, double *arr, int layout, 
     }
     const long long work = L->nvalid * L->ncomp;
     ProfScope ps(ctx, kProfMove);
-    move_kernel<<<grid_for(work), 256, 0, ctx->stream>>>(
-        L->d_boxes, L->d_vbase, (int)L->boxes.size(), L->ncomp, L->nvalid, buf, arr, layout,
-        dir, L->dhi[0] - L->dlo[0] + 1, L->dhi[1] - L->dlo[1] + 1, L->dhi[2] - L->dlo[2] + 1,
-        L->dlo[0], L->dlo[1], L->dlo[2]);
+    const int n0 = L->dhi[0] - L->dlo[0] + 1, n1 = L->dhi[1] - L->dlo[1] + 1,
+              n2 = L->dhi[2] - L->dlo[2] + 1;
+    if (L->esize == 4) {
+        require(which == SH_NEW || which == SH_OLD, "FP32 levels move their two time levels");
+        move_kernel<float><<<grid_for(work), 256, 0, ctx->stream>>>(
+            L->d_boxes, L->d_vbase, (int)L->boxes.size(), L->ncomp, L->nvalid,
+            (float *)L->buf[which], L->cmp[which], arr, layout, dir, n0, n1, n2, L->dlo[0],
+            L->dlo[1], L->dlo[2]);
+    } else {
+        move_kernel<double><<<grid_for(work), 256, 0, ctx->stream>>>(
+            L->d_boxes, L->d_vbase, (int)L->boxes.size(), L->ncomp, L->nvalid, L->buf[which],
+            nullptr, arr, layout, dir, n0, n1, n2, L->dlo[0], L->dlo[1], L->dlo[2]);
+    }
     ctx->launches++;
     ck(cudaGetLastError(), "data movement launch");
 }
@@ -1510,9 +1696,10 @@ std::vector<AvgRect> avg_plan(const sh_level *F, const sh_level *C, long long &n
     return r;
 }
 
-void average_down_impl(sh_ctx *ctx, const sh_level *F, const double *fine, const sh_level *C,
-                       double *crse, double *te) {
+void average_down_impl(sh_ctx *ctx, const sh_level *F, int which_f, sh_level *C, int which_c,
+                       bool with_te) {
     require(F->ncomp == C->ncomp, "fine and coarse levels differ in components");
+    require(F->esize == C->esize, "fine and coarse levels differ in precision");
     if (F->avg_for != C->uid) {
         for (const sh_box &b : F->boxes)
             for (int d = 0; d < 3; ++d)
@@ -1528,8 +1715,28 @@ void average_down_impl(sh_ctx *ctx, const sh_level *F, const double *fine, const
     }
     if (F->avg_cells == 0) return;
     ProfScope ps(ctx, kProfAvg);
-    avgdown_kernel<<<grid_for(F->avg_cells), 256, 0, ctx->stream>>>(
-        (const AvgRect *)F->d_avg, F->navg, F->avg_cells, F->d_boxes, C->d_boxes, F->ncomp, fine, crse, te);
+    if (F->esize == 4) {
+        /* truncation errors of an FP32 level go to its FP64 array */
+        double *te = nullptr;
+        if (with_te) {
+            sh_level *Fm = const_cast<sh_level *>(F);
+            if (!Fm->te64) {
+                const size_t bytes = (size_t)F->total_gvol * F->ncomp * sizeof(double);
+                Fm->te64 = (double *)dmalloc_async(ctx, bytes, "truncation errors");
+                ck(cudaMemsetAsync(Fm->te64, 0, bytes, ctx->stream), "truncation errors clear");
+            }
+            te = Fm->te64;
+        }
+        avgdown_kernel<float><<<grid_for(F->avg_cells), 256, 0, ctx->stream>>>(
+            (const AvgRect *)F->d_avg, F->navg, F->avg_cells, F->d_boxes, C->d_boxes, F->ncomp,
+            (const float *)F->buf[which_f], F->cmp[which_f], (float *)C->buf[which_c],
+            C->cmp[which_c], te);
+    } else {
+        avgdown_kernel<double><<<grid_for(F->avg_cells), 256, 0, ctx->stream>>>(
+            (const AvgRect *)F->d_avg, F->navg, F->avg_cells, F->d_boxes, C->d_boxes, F->ncomp,
+            F->buf[which_f], nullptr, C->buf[which_c], nullptr,
+            with_te ? F->buf[SH_OLD] : nullptr);
+    }
     ctx->launches++;
     ck(cudaGetLastError(), "average-down launch");
 }
@@ -1688,7 +1895,21 @@ int sh_project_comp_name(int id, int comp, const char **name) {
 int sh_level_create(sh_ctx *ctx, int project, int with_gw, const int domain_lo[3],
                     const int domain_hi[3], const sh_box *boxes, int nbox, int nghost,
                     sh_level **out) {
+    return sh_level_create_prec(ctx, project, with_gw, domain_lo, domain_hi, boxes, nbox, nghost,
+                                SH_PREC_FP64, out);
+}
+
+int sh_level_precision(const sh_level *L, int *precision) {
+    if (!L || !precision) return SH_ERR_ARG;
+    *precision = L->esize == 8 ? SH_PREC_FP64 : SH_PREC_FP32_KAHAN;
+    return SH_OK;
+}
+
+int sh_level_create_prec(sh_ctx *ctx, int project, int with_gw, const int domain_lo[3],
+                         const int domain_hi[3], const sh_box *boxes, int nbox, int nghost,
+                         int precision, sh_level **out) {
     if (!ctx || !out) return SH_ERR_ARG;
+    if (precision != SH_PREC_FP64 && precision != SH_PREC_FP32_KAHAN) return SH_ERR_ARG;
     *out = nullptr;
     sh_level *L = new (std::nothrow) sh_level();
     static std::atomic<long long> next_uid{1};
@@ -1705,6 +1926,13 @@ int sh_level_create(sh_ctx *ctx, int project, int with_gw, const int domain_lo[3
                 "nghost must cover the project's stencil reach and be at most 8");
         L->project = project;
         L->with_gw = with_gw != 0;
+        if (precision == SH_PREC_FP32_KAHAN) {
+            require(stage32_family(L->ops) != 0,
+                    "FP32 levels are available for the axion-string projects AxionStringsLap1 "
+                    "and AxionStringsLap2");
+            require(!L->with_gw, "FP32 levels carry no GW tensor");
+            L->esize = 4;
+        }
         L->ncomp = L->ops->nscalars + (L->with_gw ? 12 : 0);
         L->npairs = L->ops->nscalars / 2 + (L->with_gw ? 6 : 0);
         require(L->ncomp <= kMaxComp, "too many components");
@@ -1771,11 +1999,16 @@ int sh_level_create(sh_ctx *ctx, int project, int with_gw, const int domain_lo[3
         L->d_vbase = upload_async(ctx, L->vbase.data(), L->vbase.size(), "box prefix");
         build_owner_map(ctx, L);
         build_ghost_plan(ctx, L);
-        const size_t bytes = (size_t)L->total_gvol * L->ncomp * sizeof(double);
+        const size_t bytes = (size_t)L->total_gvol * L->ncomp * L->esize;
         for (int q = 0; q < 3; ++q) {
             L->buf[q] = (double *)dmalloc_async(ctx, bytes, "level buffer");
             ck(cudaMemsetAsync(L->buf[q], 0, bytes, ctx->stream), "level buffer clear");
         }
+        if (L->esize == 4)
+            for (int q = 0; q < 2; ++q) {
+                L->cmp[q] = (float *)dmalloc_async(ctx, bytes, "level compensations");
+                ck(cudaMemsetAsync(L->cmp[q], 0, bytes, ctx->stream), "compensations clear");
+            }
     });
     if (rc != SH_OK) {
         level_free(ctx, L);
@@ -1855,7 +2088,7 @@ int sh_level_write(sh_ctx *ctx, sh_level *L, int which, int layout, const double
         const size_t bytes = (size_t)L->nvalid * L->ncomp * sizeof(double);
         double *stage = (double *)ctx_scratch(ctx, bytes);
         ck(cudaMemcpyAsync(stage, host, bytes, cudaMemcpyHostToDevice, ctx->stream), "upload");
-        move(ctx, L, L->buf[which], stage, layout, 0);
+        move(ctx, L, which, stage, layout, 0);
         ck(cudaStreamSynchronize(ctx->stream), "upload");
     });
 }
@@ -1866,7 +2099,7 @@ int sh_level_read(sh_ctx *ctx, const sh_level *L, int which, int layout, double 
         set_device(ctx);
         const size_t bytes = (size_t)L->nvalid * L->ncomp * sizeof(double);
         double *stage = (double *)ctx_scratch(ctx, bytes);
-        move(ctx, L, L->buf[which], stage, layout, 1);
+        move(ctx, L, which, stage, layout, 1);
         ck(cudaMemcpyAsync(host, stage, bytes, cudaMemcpyDeviceToHost, ctx->stream), "download");
         ck(cudaStreamSynchronize(ctx->stream), "download");
     });
@@ -1877,7 +2110,7 @@ int sh_level_write_device(sh_ctx *ctx, sh_level *L, int which, int layout, const
     return guarded(ctx, [&] {
         L->version++;
         set_device(ctx);
-        move(ctx, L, L->buf[which], const_cast<double *>(dev), layout, 0);
+        move(ctx, L, which, const_cast<double *>(dev), layout, 0);
     });
 }
 
@@ -1885,7 +2118,7 @@ int sh_level_read_device(sh_ctx *ctx, const sh_level *L, int which, int layout, 
     if (!ctx || !L || !dev || (which != SH_NEW && which != SH_OLD)) return SH_ERR_ARG;
     return guarded(ctx, [&] {
         set_device(ctx);
-        move(ctx, L, L->buf[which], dev, layout, 1);
+        move(ctx, L, which, dev, layout, 1);
     });
 }
 
@@ -1913,6 +2146,7 @@ int sh_level_set_coarse(sh_ctx *ctx, sh_level *fine, sh_level *coarse) {
         fine->coarse = nullptr;
         if (!coarse) return;
         require(coarse != fine, "a level cannot be its own coarse level");
+        require(coarse->esize == fine->esize, "fine and coarse levels differ in precision");
         FillPlan P = build_fill_plan(fine, fine, coarse, true, false);
         const std::vector<CfItem> items = cf_items(P.cf, fine);
         fine->d_cf = upload_items(ctx, items, "coarse-fine plan");
@@ -1931,6 +2165,9 @@ int sh_level_fill_from(sh_ctx *ctx, sh_level *dst, int which_dst, const sh_level
         set_device(ctx);
         require(src != dst, "source and destination must differ");
         if (src) require(src->ncomp == dst->ncomp, "source differs in components");
+        if (src) require(src->esize == dst->esize, "source differs in precision");
+        if (coarse) require(coarse->esize == dst->esize, "coarse level differs in precision");
+        const bool f32 = dst->esize == 4;
         FillPlan P = build_fill_plan(dst, src, coarse, false);
         CopyItem *d_rects = nullptr;
         CfItem *d_cf = nullptr;
@@ -1938,8 +2175,18 @@ int sh_level_fill_from(sh_ctx *ctx, sh_level *dst, int which_dst, const sh_level
             const std::vector<CopyItem> items = copy_items(P.rects, dst, src);
             d_rects = upload_items(ctx, items, "fill plan");
             ProfScope ps(ctx, kProfFill);
-            copy_items_kernel<<<(int)items.size(), kItemThreads, 0, ctx->stream>>>(
-                d_rects, dst->buf[which_dst], src->buf[which_src], dst->ncomp);
+            if (f32) {
+                /* values and their compensations */
+                copy_items_kernel<float><<<(int)items.size(), kItemThreads, 0, ctx->stream>>>(
+                    d_rects, (float *)dst->buf[which_dst], (const float *)src->buf[which_src],
+                    dst->ncomp);
+                copy_items_kernel<float><<<(int)items.size(), kItemThreads, 0, ctx->stream>>>(
+                    d_rects, dst->cmp[which_dst], src->cmp[which_src], dst->ncomp);
+                ctx->launches++;
+            } else {
+                copy_items_kernel<double><<<(int)items.size(), kItemThreads, 0, ctx->stream>>>(
+                    d_rects, dst->buf[which_dst], src->buf[which_src], dst->ncomp);
+            }
             ctx->launches++;
             ck(cudaGetLastError(), "fill copy launch");
         }
@@ -1951,10 +2198,16 @@ int sh_level_fill_from(sh_ctx *ctx, sh_level *dst, int which_dst, const sh_level
             double alpha, beta;
             coarse_time_weights(coarse, time, mode, alpha, beta);
             ProfScope ps(ctx, kProfCf);
-            cf_interp_kernel<<<(int)items.size(), 128, 0, ctx->stream>>>(
-                d_cf, coarse->d_boxes, dst->buf[which_dst], owner_map_dev(coarse),
-                coarse->buf[SH_OLD], coarse->buf[SH_NEW], mode, alpha, beta, dst->ncomp, nullptr,
-                0);
+            if (f32)
+                cf_interp_kernel<float><<<(int)items.size(), 128, 0, ctx->stream>>>(
+                    d_cf, coarse->d_boxes, (float *)dst->buf[which_dst], owner_map_dev(coarse),
+                    (const float *)coarse->buf[SH_OLD], (const float *)coarse->buf[SH_NEW], mode,
+                    alpha, beta, dst->ncomp, nullptr, 0, dst->cmp[which_dst]);
+            else
+                cf_interp_kernel<double><<<(int)items.size(), 128, 0, ctx->stream>>>(
+                    d_cf, coarse->d_boxes, dst->buf[which_dst], owner_map_dev(coarse),
+                    coarse->buf[SH_OLD], coarse->buf[SH_NEW], mode, alpha, beta, dst->ncomp,
+                    nullptr, 0, nullptr);
             ctx->launches++;
             ck(cudaGetLastError(), "coarse fill launch");
         }
@@ -1975,6 +2228,7 @@ int sh_level_advance(sh_ctx *ctx, sh_level *L, int integrator, const double *tab
         require(dt > 0 && dx > 0, "dt and dx must be positive");
         if (!(flags & SH_ADVANCE_NO_SWAP)) {
             std::swap(L->buf[SH_NEW], L->buf[SH_OLD]);
+            std::swap(L->cmp[SH_NEW], L->cmp[SH_OLD]);
             std::swap(L->t[SH_NEW], L->t[SH_OLD]);
             std::swap(L->istep[SH_NEW], L->istep[SH_OLD]);
         }
@@ -1984,8 +2238,13 @@ int sh_level_advance(sh_ctx *ctx, sh_level *L, int integrator, const double *tab
          * sub-steps): the ghost values would be the same */
         if (!fill_current(L, L->buf[SH_OLD], L->t[SH_OLD], ver))
             fill_patch(ctx, L, L->buf[SH_OLD], L->t[SH_OLD]);
-        integrate(ctx, L, integrator, tableau, nstages, dt, dx, params, nparams, gw_params, ngw,
-                  ko_order, ko_strength);
+        if (L->esize == 4) {
+            require(!L->with_gw && ngw == 0, "FP32 levels carry no GW tensor");
+            integrate32(ctx, L, integrator, dt, dx, params, nparams, ko_order);
+        } else {
+            integrate(ctx, L, integrator, tableau, nstages, dt, dx, params, nparams, gw_params,
+                      ngw, ko_order, ko_strength);
+        }
         L->t[SH_NEW] = L->t[SH_OLD] + dt;
         L->istep[SH_NEW] = L->istep[SH_OLD] + 1;
         ck(cudaGetLastError(), "advance");
@@ -1999,6 +2258,7 @@ int sh_level_rhs(sh_ctx *ctx, sh_level *L, int which, double time, int lev, doub
     return guarded(ctx, [&] {
         L->version++;
         set_device(ctx);
+        require_fp64(L, "the Rhs through the project hooks");
         StageArgs a;
         fill_common(a, L, dt, dx, params, nparams, gw_params, ngw, ko_order, ko_strength);
         a.state = L->buf[which];
@@ -2009,7 +2269,7 @@ int sh_level_rhs(sh_ctx *ctx, sh_level *L, int which, double time, int lev, doub
         launch_stage(ctx, L, a, ko_order);
         const size_t bytes = (size_t)L->nvalid * L->ncomp * sizeof(double);
         double *stage = (double *)ctx_scratch(ctx, bytes);
-        move(ctx, L, L->buf[2], stage, 1, 1);
+        move(ctx, L, 2, stage, 1, 1);
         ck(cudaMemcpyAsync(host_rhs, stage, bytes, cudaMemcpyDeviceToHost, ctx->stream),
            "download");
         ck(cudaStreamSynchronize(ctx->stream), "rhs");
@@ -2042,6 +2302,7 @@ int sh_level_add_bubbles(sh_ctx *ctx, sh_level *L, int which, int comp_phi, int 
         ck(cudaMemcpyAsync(d + nx, profile, np * sizeof(double), cudaMemcpyHostToDevice,
                            ctx->stream),
            "bubble upload");
+        require_fp64(L, "bubble injection");
         BubbleList bl{d, d + nx, nb, nbins, inv_dx, Lcut};
         level_bubbles_kernel<<<grid_for(L->nvalid), 256, 0, ctx->stream>>>(
             L->d_boxes, L->d_vbase, (int)L->boxes.size(), L->nvalid, L->ncomp, comp_phi,
@@ -2082,7 +2343,7 @@ int sh_scalar_spectrum(sh_ctx *ctx, const sh_level *L, int fn, int comp, double 
             [&](double *real) {
                 out_pack_kernel<<<grid_for(L->nvalid), 256, 0, ctx->stream>>>(
                     L->d_boxes, L->d_vbase, (int)L->boxes.size(), L->nvalid, L->ncomp, fn, comp,
-                    L->buf[SH_NEW], real, N, L->dlo[0], L->dlo[1], L->dlo[2]);
+                    state64(ctx, L, SH_NEW), real, N, L->dlo[0], L->dlo[1], L->dlo[2]);
             });
         if (!err.empty()) throw ShError(SH_ERR_CUDA, err);
         ck(e, "scalar spectrum");
@@ -2122,7 +2383,7 @@ int sh_projection(sh_ctx *ctx, const sh_level *const *levels, int nlev, int fn, 
             if (l > 0) require(N == 2 * a.lev[l - 1].dimN, "levels must refine by 2");
             a.lev[l].map = owner_map_dev(L);
             a.lev[l].boxes = L->d_boxes;
-            a.lev[l].buf = L->buf[SH_NEW];
+            a.lev[l].buf = state64(ctx, L, SH_NEW);
             a.lev[l].ncomp = L->ncomp;
             a.lev[l].dimN = N;
         }
@@ -2152,8 +2413,8 @@ int sh_level_reduce(sh_ctx *ctx, const sh_level *L, int which, int op, int comp,
         set_device(ctx);
         const int nbox = (int)L->boxes.size();
         double *d = (double *)ctx_scratch(ctx, ((size_t)nbox + 1) * sizeof(double));
-        reduce_boxes_kernel<<<nbox, kReduceThreads, 0, ctx->stream>>>(L->d_boxes, L->buf[which],
-                                                                     L->ncomp, comp, op, d + 1);
+        reduce_boxes_kernel<<<nbox, kReduceThreads, 0, ctx->stream>>>(
+            L->d_boxes, state64(ctx, L, which), L->ncomp, comp, op, d + 1);
         reduce_final_kernel<<<1, kReduceThreads, 0, ctx->stream>>>(d + 1, nbox, op, d);
         ctx->launches += 2;
         ck(cudaGetLastError(), "reduce launch");
@@ -2171,9 +2432,10 @@ int sh_level_check_finite(sh_ctx *ctx, const sh_level *L, int which, long long *
         set_device(ctx);
         const int nbox = (int)L->boxes.size();
         double *d = (double *)ctx_scratch(ctx, ((size_t)nbox + L->ncomp) * sizeof(double));
+        const double *st = state64(ctx, L, which);
         for (int c = 0; c < L->ncomp; ++c) {
             reduce_boxes_kernel<<<nbox, kReduceThreads, 0, ctx->stream>>>(
-                L->d_boxes, L->buf[which], L->ncomp, c, SH_REDUCE_COUNT_NONFINITE, d + L->ncomp);
+                L->d_boxes, st, L->ncomp, c, SH_REDUCE_COUNT_NONFINITE, d + L->ncomp);
             reduce_final_kernel<<<1, kReduceThreads, 0, ctx->stream>>>(
                 d + L->ncomp, nbox, SH_REDUCE_COUNT_NONFINITE, d + c);
             ctx->launches += 2;
@@ -2211,7 +2473,7 @@ int sh_level_string_tags(sh_ctx *ctx, sh_level *L, double time, int lev, double 
         std::memset(&a, 0, sizeof(a));
         a.boxes = L->d_boxes;
         a.tiles = L->d_tiles;
-        a.state = L->buf[SH_NEW];
+        a.state = state64(ctx, L, SH_NEW);
         a.te = nullptr;
         a.ncomp = L->ncomp;
         a.lev = lev;
@@ -2261,7 +2523,7 @@ int sh_average_down(sh_ctx *ctx, const sh_level *F, int which_f, sh_level *C, in
     return guarded(ctx, [&] {
         C->version++;
         set_device(ctx);
-        average_down_impl(ctx, F, F->buf[which_f], C, C->buf[which_c], nullptr);
+        average_down_impl(ctx, F, which_f, C, which_c, false);
     });
 }
 
@@ -2271,7 +2533,7 @@ int sh_average_down_te(sh_ctx *ctx, sh_level *F, sh_level *C) {
         C->version++;
         F->version++;
         set_device(ctx);
-        average_down_impl(ctx, F, F->buf[SH_NEW], C, C->buf[SH_NEW], F->buf[SH_OLD]);
+        average_down_impl(ctx, F, SH_NEW, C, SH_NEW, true);
     });
 }
 
@@ -2297,8 +2559,8 @@ int sh_tag(sh_ctx *ctx, sh_level *L, int use_te, double time, int lev, double dt
         std::memset(&a, 0, sizeof(a));
         a.boxes = L->d_boxes;
         a.tiles = L->d_tiles;
-        a.state = L->buf[SH_NEW];
-        a.te = use_te ? L->buf[SH_OLD] : nullptr;
+        a.state = state64(ctx, L, SH_NEW);
+        a.te = use_te ? te_of(L) : nullptr;
         a.ncomp = L->ncomp;
         a.lev = lev;
         a.time = time;
@@ -2390,8 +2652,8 @@ int sh_tag_blocks(sh_ctx *ctx, sh_level *L, int use_te, double time, int lev, do
         std::memset(&a, 0, sizeof(a));
         a.boxes = L->d_boxes;
         a.tiles = L->d_tiles;
-        a.state = L->buf[SH_NEW];
-        a.te = use_te ? L->buf[SH_OLD] : nullptr;
+        a.state = state64(ctx, L, SH_NEW);
+        a.te = use_te ? te_of(L) : nullptr;
         a.ncomp = L->ncomp;
         a.lev = lev;
         a.time = time;
@@ -2473,7 +2735,7 @@ int sh_gw_spectrum(sh_ctx *ctx, const sh_level *L, const int *comps, int zero_pa
         ProfScope ps(ctx, kProfGw);
         cudaError_t e = gw_spectrum_device(ctx->gw, ctx->stream, L->d_boxes, L->d_vbase,
                                            (int)L->boxes.size(), L->nvalid, L->ncomp,
-                                           L->buf[SH_NEW], c6, N, L->dlo, zero_padding,
+                                           state64(ctx, L, SH_NEW), c6, N, L->dlo, zero_padding,
                                            projection_type, unbinned, (double *)base, bins_dev,
                                            &nb, &ctx->launches, err);
         if (!err.empty()) throw ShError(SH_ERR_CUDA, err);
@@ -2600,6 +2862,7 @@ extern "C" int sh_tag_static(sh_ctx *ctx, sh_level *L, int use_te, double time, 
         std::memset(&a, 0, sizeof(a));
         a.boxes = L->d_boxes;
         a.tiles = L->d_tiles;
+        require_fp64(L, "tagging without allocations");
         a.state = L->buf[SH_NEW];
         a.te = use_te ? L->buf[SH_OLD] : nullptr;
         a.ncomp = L->ncomp;

@@ -1,0 +1,116 @@
+/* RKN4 stage kernels of FP32 levels (the precision form on levels and AMR
+ * hierarchies) for the axion-string projects of this library
+ * (AxionStringsLap1 / AxionStringsLap2):
+ *   Psi' = Pi,
+ *   Pi'  = -2 Pi / eta + lap_N(Psi) - lambda Psi [eta^2 (|Psi|^2 - 1) + c]
+ * with lambda = params[0], c = params[1], written against the equations in
+ * FP32 (the plugin hooks compute in FP64, which runs at 1/64 of the FP32
+ * rate on GB300).
+ *
+ * Same schedule as the FP64 stage kernel (sh_stage.cuh) with the RKN4
+ * tableau of source/integrators/rkn.cpp:130-139 (c = {0, 1/2, 1},
+ * a_21 = 1/8, a_32 = 1/2, a_31 = 0, bbar = {1/6, 1/3, 0},
+ * b = {1/6, 2/3, 1/6}; every stage uses the step's initial momenta,
+ * rkn.cpp:55-117):
+ *   STAGE 0: K0 = accel(y0);  Y1 = y0 + h/2 y0' + h^2/8 K0
+ *   STAGE 1: K1 = accel(Y1);  Y2 = y0 + h y0' + h^2/2 K1
+ *   STAGE 2: K2 = accel(Y2);  y1 = y0 + h y0' + h^2 (K0/6 + K1/3),
+ *                             y1' = y0' + h ((K0 + K2)/6 + 2 K1/3)
+ * The stage buffers hold Y_i and a copy of y0' so that the level's ghost
+ * fill (same-level copies, coarse-fine interpolation at the stage time)
+ * serves them unchanged.  The last stage adds the increments with Kahan
+ * compensation (the value y and its compensation c stand for y - c; the
+ * compensations of the new state are written beside it).
+ *
+ * The arithmetic is the explicitly rounded FP32 of the ensemble kernels
+ * (sh_f32.cuh): Laplacian, potential, acceleration, stage positions and
+ * increments round exactly as there.
+ */
+#ifndef SH_STAGE32_CUH_
+#define SH_STAGE32_CUH_
+
+#include "sh_f32.cuh"
+#include "sh_internal.h"
+
+namespace sh {
+
+struct Stage32Args {
+    const TileDev *tiles;
+    const BoxDev *boxes;
+    const float *state; /* Y_i with filled ghost cells (stage 0: y0) */
+    const float *y0;    /* the step's initial state (positions and momenta) */
+    float *out;         /* stages 0, 1: Y_{i+1} (+ copy of y0'); stage 2: y1 */
+    const float *k0, *k1; /* K buffers, two components each (box layout) */
+    float *kout;
+    const float *c_old;   /* compensations of y0 */
+    float *c_new;         /* compensations of y1 */
+    float h, cm, ck;      /* dt; stage position coefficients of y0' and K */
+    float h2;             /* dt^2 */
+    float inv;            /* 1/dx^2 (7 points) or 1/(12 dx^2) (13 points) */
+    float lam, cst;       /* params[0], params[1] */
+    float friction, eta2; /* -2/eta and eta^2 at the stage time */
+};
+
+template <int ORDER, int STAGE>
+__global__ void __launch_bounds__(kThreads) stage32_axion_kernel(const __grid_constant__ Stage32Args a) {
+    const TileDev t = a.tiles[blockIdx.x];
+    const BoxDev b = a.boxes[t.box];
+    const int tid = threadIdx.x + kTileX * threadIdx.y;
+    const int ty = tid / t.nx;
+    const int i = t.x0 + (tid - ty * t.nx);
+    const int j = t.y0 + ty;
+    if (ty >= kThreads / t.nx || i > b.hi[0] || j > b.hi[1]) return;
+    const int kend = min(t.z0 + t.nz - 1, b.hi[2]);
+    const long long gx = b.gdim[0], gxy = gx * b.gdim[1], gvol = b.gvol;
+    for (int k = t.z0; k <= kend; ++k) {
+        const long long lc =
+            (i - b.glo[0]) + (long long)(j - b.glo[1]) * gx + (long long)(k - b.glo[2]) * gxy;
+        const long long sb = b.off * 4 + lc; /* component 0 of the cell */
+        const long long kb = b.off * 2 + lc; /* K component 0 of the cell */
+        float lap[2];
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            const float *s = a.state + sb + c * gvol;
+            if constexpr (ORDER == 1) {
+                lap[c] = f32::lap7(s[0], s[1], s[-1], s[gx], s[-gx], s[gxy], s[-gxy], a.inv);
+            } else {
+                const float s1 = f32::ring(s[1], s[-1], s[gx], s[-gx], s[gxy], s[-gxy]);
+                const float s2 =
+                    f32::ring(s[2], s[-2], s[2 * gx], s[-2 * gx], s[2 * gxy], s[-2 * gxy]);
+                lap[c] = f32::lap13(s[0], s1, s2, a.inv);
+            }
+        }
+        const float p0 = a.state[sb], p1 = a.state[sb + gvol];
+        const float q0 = a.y0[sb + 2 * gvol], q1 = a.y0[sb + 3 * gvol];
+        const float v = f32::potential(p0, p1, a.lam, a.eta2, a.cst);
+        const float kq[2] = {f32::accel(q0, lap[0], p0, v, a.friction),
+                             f32::accel(q1, lap[1], p1, v, a.friction)};
+        const float q[2] = {q0, q1};
+        if constexpr (STAGE < 2) {
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                a.kout[kb + c * gvol] = kq[c];
+                const float y = a.y0[sb + c * gvol];
+                a.out[sb + c * gvol] = f32::stage_pos(y, q[c], kq[c], a.cm, a.ck);
+                a.out[sb + (2 + c) * gvol] = q[c];
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                const float ka = a.k0[kb + c * gvol], kbv = a.k1[kb + c * gvol];
+                float y = a.y0[sb + c * gvol], cy = a.c_old[sb + c * gvol];
+                float m = q[c], cmo = a.c_old[sb + (2 + c) * gvol];
+                f32::kahan(y, f32::dpos(q[c], ka, kbv, a.h, a.h2), cy);
+                f32::kahan(m, f32::dmom(ka, kbv, kq[c], a.h), cmo);
+                a.out[sb + c * gvol] = y;
+                a.out[sb + (2 + c) * gvol] = m;
+                a.c_new[sb + c * gvol] = cy;
+                a.c_new[sb + (2 + c) * gvol] = cmo;
+            }
+        }
+    }
+}
+
+} // namespace sh
+
+#endif

@@ -1,0 +1,145 @@
+"""FP32 + Kahan levels and AMR hierarchies (sh_level_create_prec,
+csrc/sh_stage32.cuh): the precision form on the drop-in path, with FP32
+values and compensations, FP32 stage arithmetic and everything that decides
+the hierarchy (truncation errors, tags through the project's hooks,
+average-down sums, time) in FP64.
+
+* A periodic FP32 level, in one box or in several (ghost cells from the
+  same-level copies), evolves bit for bit as the FP32 + Kahan ensemble
+  kernels do on the same FP32-representable state: same stage schedule,
+  same explicitly rounded FP32 arithmetic.
+* Tags of an FP32 level (winding through the hooks on the FP64 values v - c)
+  and its reductions equal those of an FP64 level holding the same values.
+* An FP32 hierarchy against the FP64 oracle's hierarchy: the same levels and
+  boxes after every coarse step, fields within 2e-6 relative L2 per level
+  (the FP32 rounding of the stencils), regrid masks compared cell by cell
+  with the mismatches counted.
+* A checkpoint of an FP32 hierarchy restarts to the same evolution.
+* FP64-only operations refuse FP32 levels with SH_ERR_UNSUPPORTED.
+"""
+import numpy as np
+import pytest
+
+import sledgehamr_gb300 as sh
+from sledgehamr_gb300 import _lib, ic
+from tests.amr_common import config, level0
+from tests.conftest import rel_l2
+from tests.oracle_lib import OracleAmr
+
+pytestmark = pytest.mark.gpu
+F32 = sh.PREC_FP32_KAHAN
+
+
+def _state(N, L, seed):
+    """An axion-string state whose values are FP32 numbers (so an upload
+    leaves zero compensations, as an ensemble upload does)."""
+    st = ic.axion_string_ic(N, L, kmax=1.5, seed=seed)
+    st[2:] = 0.2 * ic.axion_string_ic(N, L, kmax=1.0, seed=seed + 100)[:2]
+    return st.astype(np.float32).astype(np.float64)
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_fp32_level_equals_fp32_ensemble(ctx, order):
+    N, dx, dt, t0, steps = 32, 0.25, 0.0625, 0.7, 6
+    params = [0.8, 0.1]
+    st = _state(N, N * dx, 3 + order)
+    fam = sh.FAMILY_AXION_LAP1 if order == 1 else sh.FAMILY_AXION_LAP2
+    E = sh.Ensemble(ctx, fam, F32, [N], [dx], params + [0.0, 0.0])
+    E.write(0, st)
+    E.set_time(t0)
+    E.step(dt, steps)
+    ref = np.asarray(E.read(0)).ravel()
+    E.close()
+    for max_grid in (0, 16):
+        lv = sh.Level.periodic(ctx, f"AxionStringsLap{order}", N, order, max_grid=max_grid,
+                               precision=F32)
+        lv.write(st)
+        lv.set_time(t0)
+        for _ in range(steps):
+            lv.advance(sh.RKN4, dt, dx, params=params)
+        out = lv.read().ravel()
+        assert abs(lv.time()[0] - (t0 + dt * steps)) < 1e-12
+        lv.close()
+        assert np.array_equal(out, ref), (max_grid, rel_l2(out, ref))
+
+
+def test_fp32_level_tags_and_reductions_equal_fp64(ctx):
+    N, L = 32, 8.0
+    st = _state(N, L, 11)
+    a = sh.Level.periodic(ctx, "AxionStringsLap2", N, 2, max_grid=16, precision=F32)
+    b = sh.Level.periodic(ctx, "AxionStringsLap2", N, 2, max_grid=16)
+    for lv in (a, b):
+        lv.write(st)
+        lv.fill_patch()
+    ma, ca, _ = a.tag(1.0, 0, 0.0625, 0.25)
+    mb, cb, _ = b.tag(1.0, 0, 0.0625, 0.25)
+    assert ma.sum() > 0
+    assert np.array_equal(ma, mb) and np.array_equal(ca, cb)
+    for op in (sh.REDUCE_MAX_ABS, sh.REDUCE_SUM, sh.REDUCE_SUM_MODULUS):
+        assert a.reduce(op, 0) == b.reduce(op, 0)
+    assert a.string_tags(1.0, 0, 0.0625, 0.25) == b.string_tags(1.0, 0, 0.0625, 0.25)
+    assert np.array_equal(a.read(), st)
+    a.close()
+    b.close()
+
+
+def test_fp32_hierarchy_against_fp64_oracle(ctx):
+    g = sh.Amr(ctx, config(precision=F32), level0())
+    o = OracleAmr(config(), level0())
+    errors = []
+    for step in range(4):
+        g.step(1)
+        o.step(1)
+        gi, oi = g.info(), o.info()
+        assert gi["finest"] == oi["finest"], step
+        assert gi["cell_updates"] == oi["cell_updates"]
+        for lev in range(gi["finest"] + 1):
+            assert g.level(lev).boxes == o.boxes(lev), (step, lev)
+            e = rel_l2(g.level(lev).read(), o.read(lev)[0])
+            errors.append((step, lev, e))
+            assert e <= 2e-6, (step, lev, e)
+    assert g.info()["finest"] >= 1
+    mism, cells = 0, 0
+    for q in range(g.info()["nregrids"]):
+        rg, ro = g.regrid_record(q), o.regrid_record(q)
+        assert rg["lev"] == ro["lev"] and rg["time"] == ro["time"]
+        mism += int(np.count_nonzero(rg["mask"] != ro["mask"]))
+        cells += rg["mask"].size
+    print("FP32 hierarchy: rel L2 per (step, level)", errors,
+          f"tag mismatches {mism} of {cells} cells")
+    assert mism <= cells // 1000
+    g.close()
+    o.close()
+
+
+def test_fp32_hierarchy_checkpoint_restart(ctx, tmp_path):
+    cfg = config(precision=F32)
+    g = sh.Amr(ctx, cfg, level0(2))
+    for _ in range(3):
+        g.step(1)
+    g.checkpoint(str(tmp_path / "ck"))
+    r = sh.Amr.restart(ctx, cfg, str(tmp_path / "ck"))
+    for _ in range(2):
+        g.step(1)
+        r.step(1)
+    assert g.info() == r.info()
+    for lev in range(g.info()["finest"] + 1):
+        assert g.level(lev).boxes == r.level(lev).boxes
+        # values and compensations are stored as v - c and split again on
+        # restart: identical except where a compensation sat on a rounding tie
+        assert rel_l2(r.level(lev).read(), g.level(lev).read()) <= 1e-8
+    g.close()
+    r.close()
+
+
+def test_fp64_only_operations_refuse_fp32_levels(ctx):
+    lv = sh.Level.periodic(ctx, "AxionStringsLap1", 16, 1, precision=F32)
+    lv.write(_state(16, 4.0, 1))
+    with pytest.raises(sh.ShError) as e:
+        lv.rhs(1.0, 0, 0.0625, 0.25, params=[1.0, 0.0])
+    assert e.value.code == _lib.SH_ERR_UNSUPPORTED
+    with pytest.raises(sh.ShError):
+        lv.advance(sh.LEAPFROG, 0.0625, 0.25, params=[1.0, 0.0])
+    lv.close()
+    with pytest.raises(sh.ShError):
+        sh.Level.periodic(ctx, "FirstOrderPhaseTransition", 16, 2, precision=F32)
