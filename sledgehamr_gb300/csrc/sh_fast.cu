@@ -658,17 +658,19 @@ __global__ void load_kernel(const R *src, const R *comp, double *dst, long long 
     }
 }
 
-/* Pack one GW component of realisation r into a zero-padded (pN)^3 FP64
- * array for the spectrum (compensation included). */
+/* Pack two GW components of realisation r (compensations included) into
+ * the real and imaginary parts of a zero-padded complex (pN)^3 FP64 array
+ * for the spectrum. */
 template <class R>
-__global__ void gw_pack_fast_kernel(const R *src, const R *comp, long long off, int N, int P,
-                                    double *dst, int stride) {
+__global__ void gw_pack_fast_kernel(const R *sa, const R *ca, const R *sb, const R *cb,
+                                    long long off, int N, int P, double2 *dst) {
     const long long n = (long long)N * N * N;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
         const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / ((long long)N * N));
-        dst[stride * (((long long)z * P + y) * P + x)] =
-            (double)src[off + i] - (comp ? (double)comp[off + i] : 0.);
+        dst[((long long)z * P + y) * P + x] =
+            make_double2((double)sa[off + i] - (ca ? (double)ca[off + i] : 0.),
+                         (double)sb[off + i] - (cb ? (double)cb[off + i] : 0.));
     }
 }
 
@@ -1580,15 +1582,17 @@ int sh_ensemble_gw_spectrum(sh_ensemble *E, int r, int zero_padding, int project
         std::string err;
         cudaError_t e = sh::gw_spectrum_packed(
             E->gw, s, P, N, projection_type, unbinned, scratch, bins_dev, &nb, &E->launches, err,
-            [&](int q, double *dst, int stride) {
-                const int c = sel[q];
-                if (E->esize == 8)
+            [&](int p, double2 *dst) {
+                const int a = sel[2 * p], b = sel[2 * p + 1];
+                if (E->esize == 8) {
                     gw_pack_fast_kernel<double><<<fgrid(n), 256, 0, s>>>(
-                        (double *)E->A[c], nullptr, o, N, P, dst, stride);
-                else
+                        (double *)E->A[a], nullptr, (double *)E->A[b], nullptr, o, N, P, dst);
+                } else {
+                    const bool k = !E->C.empty();
                     gw_pack_fast_kernel<float><<<fgrid(n), 256, 0, s>>>(
-                        (float *)E->A[c], E->C.empty() ? nullptr : (float *)E->C[c], o, N, P,
-                        dst, stride);
+                        (float *)E->A[a], k ? (float *)E->C[a] : nullptr, (float *)E->A[b],
+                        k ? (float *)E->C[b] : nullptr, o, N, P, dst);
+                }
             });
         if (!err.empty()) throw FastErr(SH_ERR_CUDA, err);
         fck(e, "gw spectrum");

@@ -76,12 +76,12 @@ std::vector<double> index_to_k_host(int N, int type) {
 
 namespace {
 
-/* Pack component `comp` of a level buffer (valid cells, any box layout
- * covering [0,N)^3) into the first N^3 block of a zero-initialised (pN)^3
- * array whose elements are `stride` doubles apart. */
+/* Pack components ca (real part) and cb (imaginary part) of a level buffer
+ * (valid cells, any box layout covering [0,N)^3) into the first N^3 block
+ * of a zero-initialised complex (pN)^3 array. */
 __global__ void gw_pack_kernel(const BoxDev *boxes, const long long *vbase, int nbox,
-                               long long nvalid, int ncomp, int comp, const double *buf,
-                               double *dst, int stride, int P, int dlo0, int dlo1, int dlo2) {
+                               long long nvalid, int ncomp, int ca, int cb, const double *buf,
+                               double2 *dst, int P, int dlo0, int dlo1, int dlo2) {
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nvalid;
          v += (long long)gridDim.x * blockDim.x) {
         int lo = 0, hi = nbox - 1;
@@ -96,10 +96,11 @@ __global__ void gw_pack_kernel(const BoxDev *boxes, const long long *vbase, int 
         const int i = b.lo[0] + (int)(lv % vx);
         const int j = b.lo[1] + (int)((lv / vx) % vy);
         const int k = b.lo[2] + (int)(lv / ((long long)vx * vy));
-        const long long bi = b.off * ncomp + (long long)comp * b.gvol + (i - b.glo[0]) +
+        const long long bi = b.off * ncomp + (i - b.glo[0]) +
                              (long long)(j - b.glo[1]) * b.gdim[0] +
                              (long long)(k - b.glo[2]) * b.gdim[0] * b.gdim[1];
-        dst[stride * (((long long)(k - dlo2) * P + (j - dlo1)) * P + (i - dlo0))] = buf[bi];
+        dst[((long long)(k - dlo2) * P + (j - dlo1)) * P + (i - dlo0)] =
+            make_double2(buf[bi + (long long)ca * b.gvol], buf[bi + (long long)cb * b.gvol]);
     }
 }
 
@@ -392,7 +393,7 @@ cudaError_t gw_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, int N
                                int projection_type, int unbinned, double *scratch,
                                double *bins_dev, int *nbins, long long *launches,
                                std::string &err,
-                               const std::function<void(int, double *, int)> &pack) {
+                               const std::function<void(int, double2 *)> &pack) {
     cache.prepare(P, unbinned, projection_type);
     const int H = P / 2 + 1;
     const long long nfull = (long long)P * P * P;
@@ -408,8 +409,8 @@ cudaError_t gw_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, int N
     double *vals = (double *)(Z + 3 * nfull);
     /* the pack covers all of P^3 without zero padding */
     if (P != N) cudaMemsetAsync(Z, 0, 3 * nfull * sizeof(double2), stream);
-    for (int q = 0; q < 6; ++q) {
-        pack(q, (double *)(Z + (q / 2) * nfull) + (q & 1), 2);
+    for (int p = 0; p < 3; ++p) {
+        pack(p, Z + p * nfull);
         (*launches)++;
     }
     if (cufftExecZ2Z(plan, (cufftDoubleComplex *)Z, (cufftDoubleComplex *)Z, CUFFT_FORWARD) !=
@@ -474,11 +475,11 @@ cudaError_t gw_spectrum_device(GwCache &cache, cudaStream_t stream, const BoxDev
     const int P = N * zero_padding;
     return gw_spectrum_packed(
         cache, stream, P, N, projection_type, unbinned, scratch, bins_dev, nbins, launches, err,
-        [&](int q, double *dst, int stride) {
+        [&](int p, double2 *dst) {
             int g = (int)std::min<long long>((nvalid + 255) / 256, 152LL * 32);
-            gw_pack_kernel<<<std::max(g, 1), 256, 0, stream>>>(boxes, vbase, nbox, nvalid, ncomp,
-                                                                comps[q], buf, dst, stride, P,
-                                                                dlo[0], dlo[1], dlo[2]);
+            gw_pack_kernel<<<std::max(g, 1), 256, 0, stream>>>(
+                boxes, vbase, nbox, nvalid, ncomp, comps[2 * p], comps[2 * p + 1], buf, dst, P,
+                dlo[0], dlo[1], dlo[2]);
         });
 }
 

@@ -60,16 +60,17 @@ cudaError_t scalar_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, d
                                    double *scratch, double *bins_dev, int *nbins,
                                    long long *launches, std::string &err,
                                    const std::function<void(double *)> &pack);
-/* FFT, TT projection and binning of six P^3 real fields that
- * `pack(q, dst, stride)` writes (enqueued on `stream`) for q = 0..5 in the
- * order du_xx, du_xy, du_xz, du_yy, du_yz, du_zz, element (x, y, z) at
- * dst[stride * ((z P + y) P + x)]; the destination is zeroed first only
- * when the packed N^3 block does not fill it (N < P). */
+/* FFT, TT projection and binning of six P^3 real fields, which
+ * `pack(p, dst)` writes (enqueued on `stream`) in pairs p = 0..2 as the real
+ * and imaginary parts of a complex array, element (x, y, z) at
+ * dst[(z P + y) P + x]: (du_xx, du_xy), (du_xz, du_yy), (du_yz, du_zz); the
+ * destination is zeroed first only when the packed N^3 block does not fill
+ * it (N < P). */
 cudaError_t gw_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, int N,
                                int projection_type, int unbinned, double *scratch,
                                double *bins_dev, int *nbins, long long *launches,
                                std::string &err,
-                               const std::function<void(int, double *, int)> &pack);
+                               const std::function<void(int, double2 *)> &pack);
 cudaError_t gw_spectrum_device(GwCache &cache, cudaStream_t stream, const BoxDev *boxes,
                                const long long *vbase, int nbox, long long nvalid, int ncomp,
                                const double *buf, const int comps[6], int N, const int dlo[3],
