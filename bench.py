@@ -726,8 +726,9 @@ def run_case(name):
     realisation, 3 RKN4 steps (9 stage launches; -tma with the stencil planes
     staged by tensor copies); fopt-fp32k: one 192^3 FOPT + GW realisation, 3
     leapfrog steps; gw384 / gw256: GW spectra of an FP64 FOPT + GW level
-    (binned and unbinned, twice each); amr / amr128: the AMR workload at N0 = 64 (L = 16), 40
-    coarse steps, or N0 = 128 (L = 32), 60 coarse steps; single: the 128^3
+    (binned and unbinned, twice each); amr / amr128 / amr-fp32: the AMR
+    workload at N0 = 64 (L = 16), 40 coarse steps, or N0 = 128 (L = 32), 60
+    coarse steps, or N0 = 64 on FP32 + Kahan levels; single: the 128^3
     FP64 level, 3 RKN4 steps; fp64-peak: prints the measured FP64 FMA issue
     rate (the FP64 roofline's peak)."""
     import sledgehamr_gb300 as sh
@@ -756,10 +757,12 @@ def run_case(name):
         E.write(0, st)
         E.step(0.05, 3)
         E.close()
-    elif name in ("amr", "amr128"):
+    elif name in ("amr", "amr128", "amr-fp32"):
         a = AMR
-        n0 = 64 if name == "amr" else 128
-        cfg = sh.amr_config(a["project"], N0=n0, L=n0 * 0.25, cfl=a["cfl"], t_start=a["t_start"],
+        n0 = 128 if name == "amr128" else 64
+        prec = sh.PREC_FP32_KAHAN if name == "amr-fp32" else sh.PREC_FP64
+        cfg = sh.amr_config(a["project"], precision=prec, N0=n0, L=n0 * 0.25, cfl=a["cfl"],
+                            t_start=a["t_start"],
                             nghost=a["nghost"], max_level=a["max_level"],
                             blocking_factor=a["blocking_factor"],
                             max_grid_size=a["max_grid_size"], n_error_buf=a["n_error_buf"],
@@ -999,6 +1002,7 @@ def run_amr_fp32(sh, ctx, stream, flush, K, pre, sim64, ms64):
     stage_ms, stage_n = ctx.profile_read("rhs")
     fill_ms, _ = ctx.profile_read("fill_patch")
     cf_ms, _ = ctx.profile_read("coarse_fine")
+    other = {c: ctx.profile_read(c)[0] for c in ("average_down", "tagging", "data_move")}
     ctx.profile(False)
     mine, ref = amr_levels(sh, ctx, sim), amr_levels(sh, ctx, sim64)
     err = []
@@ -1013,7 +1017,7 @@ def run_amr_fp32(sh, ctx, stream, flush, K, pre, sim64, ms64):
     return {"value": cus / (ms / 1e3), "unit": METRIC, "ms_per_step": ms / K,
             "speedup_vs_fp64": ms64 / ms, "levels_in_timed_window": sorted({f + 1 for f in finest}),
             "stage_ms_total": stage_ms, "stage_launches": stage_n, "fill_ms_total": fill_ms,
-            "coarse_fine_ms_total": cf_ms, "error_vs_fp64": err,
+            "coarse_fine_ms_total": cf_ms, "other_ms": other, "error_vs_fp64": err,
             "note": "FP32 values with FP32 Kahan compensations on every level, FP32 stage "
                     "arithmetic (csrc/sh_stage32.cuh); truncation errors, tags through the "
                     "project hooks, average-down sums and time in FP64"}
@@ -1032,7 +1036,8 @@ def main():
     ap.add_argument("--serve-max-n", type=int, default=SERVE["max_n"])
     ap.add_argument("--case", default=None,
                     help="run one small profiling case and exit: axion-fp32k, axion-fp64, "
-                         "axion-fp32k-tma, fopt-fp32k, amr, amr128, single, gw384, gw256, "
+                         "axion-fp32k-tma, fopt-fp32k, amr, amr128, amr-fp32, single, gw384, "
+                         "gw256, "
                          "fp64-peak")
     args = ap.parse_args()
     if args.case:

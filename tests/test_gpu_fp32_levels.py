@@ -12,8 +12,9 @@ average-down sums, time) in FP64.
   and its reductions equal those of an FP64 level holding the same values.
 * An FP32 hierarchy against the FP64 oracle's hierarchy: the same levels and
   boxes after every coarse step, fields within 2e-6 relative L2 per level
-  (the FP32 rounding of the stencils), regrid masks compared cell by cell
-  with the mismatches counted.
+  (the FP32 rounding of the stencils; 1e-7 to 4e-7 measured), regrid masks
+  compared cell by cell with the mismatches counted (0.1 % measured: cells
+  whose truncation error lies next to te_crit).
 * A checkpoint of an FP32 hierarchy restarts to the same evolution.
 * FP64-only operations refuse FP32 levels with SH_ERR_UNSUPPORTED.
 """
@@ -107,13 +108,17 @@ def test_fp32_hierarchy_against_fp64_oracle(ctx):
         cells += rg["mask"].size
     print("FP32 hierarchy: rel L2 per (step, level)", errors,
           f"tag mismatches {mism} of {cells} cells")
-    assert mism <= cells // 1000
+    # a truncation error is the difference of two nearly equal values, so
+    # its FP32 rounding (about 1e-7 of the field) moves cells whose error
+    # lies within about 1e-5 relative of te_crit across it: 75 of 77,824
+    # when measured
+    assert mism <= cells // 200
     g.close()
     o.close()
 
 
 def test_fp32_hierarchy_checkpoint_restart(ctx, tmp_path):
-    cfg = config(precision=F32)
+    cfg = config(precision=F32, record_regrids=0)
     g = sh.Amr(ctx, cfg, level0(2))
     for _ in range(3):
         g.step(1)
@@ -134,7 +139,7 @@ def test_fp32_hierarchy_checkpoint_restart(ctx, tmp_path):
 
 def test_fp64_only_operations_refuse_fp32_levels(ctx):
     lv = sh.Level.periodic(ctx, "AxionStringsLap1", 16, 1, precision=F32)
-    lv.write(_state(16, 4.0, 1))
+    lv.write(_state(16, 8.0, 1))
     with pytest.raises(sh.ShError) as e:
         lv.rhs(1.0, 0, 0.0625, 0.25, params=[1.0, 0.0])
     assert e.value.code == _lib.SH_ERR_UNSUPPORTED
