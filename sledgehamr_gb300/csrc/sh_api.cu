@@ -1316,11 +1316,11 @@ bool fill_current(const sh_level *L, const double *buf, double t, long long ver)
 }
 
 template <class T>
-void fill_patch_t(sh_ctx *ctx, sh_level *L, T *buf, double t) {
+void fill_patch_t(sh_ctx *ctx, sh_level *L, T *buf, double t, int nfill) {
     if (L->nghost_items > 0) {
         ProfScope ps(ctx, kProfFill);
         copy_items_kernel<T><<<L->nghost_items, kItemThreads, 0, ctx->stream>>>(L->d_ghost, buf,
-                                                                              buf, L->ncomp);
+                                                                              buf, nfill);
         ctx->launches++;
         ck(cudaGetLastError(), "ghost fill launch");
     }
@@ -1350,7 +1350,7 @@ void fill_patch_t(sh_ctx *ctx, sh_level *L, T *buf, double t) {
         double alpha, beta;
         coarse_time_weights(C, t, mode, alpha, beta);
         cf_combine_kernel<T><<<L->ncf_items, kItemThreads, 0, ctx->stream>>>(
-            L->d_cf, buf, (const T *)L->cf_old, (const T *)L->cf_new, mode, alpha, beta, L->ncomp,
+            L->d_cf, buf, (const T *)L->cf_old, (const T *)L->cf_new, mode, alpha, beta, nfill,
             L->ncf);
         ctx->launches++;
         ck(cudaGetLastError(), "coarse-fine fill launch");
@@ -1360,9 +1360,15 @@ void fill_patch_t(sh_ctx *ctx, sh_level *L, T *buf, double t) {
 /* FP32 levels store floats behind the double pointers of their buffers
  * (and of the coarse-fine value caches): same layout, element size 4. */
 void fill_patch(sh_ctx *ctx, sh_level *L, double *buf, double t) {
-    if (L->esize == 4) fill_patch_t<float>(ctx, L, (float *)buf, t);
-    else fill_patch_t<double>(ctx, L, buf, t);
+    if (L->esize == 4) fill_patch_t<float>(ctx, L, (float *)buf, t, L->ncomp);
+    else fill_patch_t<double>(ctx, L, buf, t, L->ncomp);
     note_fill(L, buf, t);
+}
+
+/* The ghost cells of the first nfill components of an FP32 stage buffer
+ * (its positions); not recorded as a fill of the buffer. */
+void fill_patch_positions(sh_ctx *ctx, sh_level *L, double *buf, double t, int nfill) {
+    fill_patch_t<float>(ctx, L, (float *)buf, t, nfill);
 }
 
 void launch_stage(sh_ctx *ctx, sh_level *L, StageArgs &a, int ko_order) {
@@ -1565,8 +1571,9 @@ int stage32_family(const ProjectOps *ops) {
 /* One RKN4 step of an FP32 level (the old buffer's ghost cells filled):
  * the stage schedule of integrate() with the FP32 axion kernels; the stage
  * buffers' ghost cells are filled at the stage times between launches.
- * Stage 0 writes Y1 into SH_NEW, stage 1 Y2 into the third buffer, the
- * last stage y1 into SH_NEW with its compensations. */
+ * Stage 0 writes Y1 into SH_NEW, stage 1 Y2 into the third buffer (the
+ * positions only, whose ghost cells are filled), the last stage y1 into
+ * SH_NEW with its compensations. */
 void integrate32(sh_ctx *ctx, sh_level *L, int type, double dt, double dx,
                  const double *params, int nparams, int ko_order) {
     require(type == SH_INTEGRATOR_RKN4, "FP32 levels integrate with RKN4 (type 21)");
@@ -1623,7 +1630,10 @@ void integrate32(sh_ctx *ctx, sh_level *L, int type, double dt, double dx,
                 ck(cudaGetLastError(), "FP32 stage kernel launch");
             }
         }
-        fill_patch(ctx, L, dst[st], st < 2 ? t0 + dt * node[st + 1] : t0 + dt);
+        if (st < 2)
+            fill_patch_positions(ctx, L, dst[st], t0 + dt * node[st + 1], 2);
+        else
+            fill_patch(ctx, L, dst[st], t0 + dt);
     }
 }
 

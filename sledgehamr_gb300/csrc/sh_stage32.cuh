@@ -16,11 +16,12 @@
  *   STAGE 1: K1 = accel(Y1);  Y2 = y0 + h y0' + h^2/2 K1
  *   STAGE 2: K2 = accel(Y2);  y1 = y0 + h y0' + h^2 (K0/6 + K1/3),
  *                             y1' = y0' + h ((K0 + K2)/6 + 2 K1/3)
- * The stage buffers hold Y_i and a copy of y0' so that the level's ghost
- * fill (same-level copies, coarse-fine interpolation at the stage time)
- * serves them unchanged.  The last stage adds the increments with Kahan
- * compensation (the value y and its compensation c stand for y - c; the
- * compensations of the new state are written beside it).
+ * The stage buffers hold the positions Y_i only (every stage reads the
+ * momenta y0' of the step's initial state), and only their two position
+ * components get ghost cells at the stage times.  The last stage adds the
+ * increments with Kahan compensation (the value y and its compensation c
+ * stand for y - c; the compensations of the new state are written beside
+ * it).
  *
  * The arithmetic is the explicitly rounded FP32 of the ensemble kernels
  * (sh_f32.cuh): Laplacian, potential, acceleration, stage positions and
@@ -37,9 +38,9 @@ namespace sh {
 struct Stage32Args {
     const TileDev *tiles;
     const BoxDev *boxes;
-    const float *state; /* Y_i with filled ghost cells (stage 0: y0) */
+    const float *state; /* Y_i, positions with filled ghost cells (stage 0: y0) */
     const float *y0;    /* the step's initial state (positions and momenta) */
-    float *out;         /* stages 0, 1: Y_{i+1} (+ copy of y0'); stage 2: y1 */
+    float *out;         /* stages 0, 1: Y_{i+1} (positions); stage 2: y1 */
     const float *k0, *k1; /* K buffers, two components each (box layout) */
     float *kout;
     const float *c_old;   /* compensations of y0 */
@@ -92,7 +93,6 @@ __global__ void __launch_bounds__(kThreads) stage32_axion_kernel(const __grid_co
                 a.kout[kb + c * gvol] = kq[c];
                 const float y = a.y0[sb + c * gvol];
                 a.out[sb + c * gvol] = f32::stage_pos(y, q[c], kq[c], a.cm, a.ck);
-                a.out[sb + (2 + c) * gvol] = q[c];
             }
         } else {
 #pragma unroll
