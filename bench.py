@@ -727,8 +727,8 @@ def run_case(name):
     staged by tensor copies); fopt-fp32k: one 192^3 FOPT + GW realisation, 3
     leapfrog steps; gw384 / gw256: GW spectra of an FP64 FOPT + GW level
     (binned and unbinned, twice each); amr / amr128 / amr-fp32: the AMR
-    workload at N0 = 64 (L = 16), 40 coarse steps, or N0 = 128 (L = 32), 60
-    coarse steps, or N0 = 64 on FP32 + Kahan levels; single: the 128^3
+    workload at N0 = 64 (L = 16) or N0 = 128 (L = 32), 60 coarse steps (three
+    levels at the end), or at N0 = 64 on FP32 + Kahan levels; single: the 128^3
     FP64 level, 3 RKN4 steps; fp64-peak: prints the measured FP64 FMA issue
     rate (the FP64 roofline's peak)."""
     import sledgehamr_gb300 as sh
@@ -770,7 +770,7 @@ def run_case(name):
                             params=a["params"],
                             string_width_threshold=a["string_width_threshold"])
         sim = sh.Amr(ctx, cfg, ic.axion_string_ic(n0, n0 * 0.25, kmax=1.0, seed=0))
-        for q in range(40 if name == "amr" else 60):
+        for q in range(60):
             sim.step(1)
             # valid cells and stage-kernel tiles (grid size) of every level,
             # to relate a profiled launch to the cells it updated
@@ -842,9 +842,11 @@ def timed_steps(step, steps, warmup, stream, flush, clk=None, before=None):
 
 
 # FP64 thread instructions (DFMA + DMUL + DADD) per cell-update of the stage
-# kernels of the 128^3 level (ncu sass instruction counters of the three
-# launches of one RKN4 step, `--case single`, divided by the cells).
-FP64_INSTR_PER_CELL_UPDATE = {"single": 55.25, "amr": None}
+# kernels (ncu SASS instruction counters of the three launches of one RKN4
+# step divided by the cells): the 7-point kernel of the 128^3 level
+# (`--case single`) and the 13-point kernel of the AMR workload (level 0 of
+# `--case amr`; the per-cell count does not depend on the level).
+FP64_INSTR_PER_CELL_UPDATE = {"single": 55.25, "amr": 61.625}
 
 
 def fp64_probe(device):
