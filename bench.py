@@ -915,6 +915,7 @@ def run_amr_leg(sh, ctx, stream, flush, steps, warmup, peak, peak_kind):
     K = max(1, min(steps, job - pre))
     l0 = ctx.kernel_launches
     cu0 = sim.info()["cell_updates"]
+    tm0 = sim.timers()
     ctx.profile(True)
     ms, finest = timed_steps(lambda: sim.step(1), K, 0, stream, flush,
                              before=lambda: sim.info()["finest"])
@@ -928,7 +929,7 @@ def run_amr_leg(sh, ctx, stream, flush, steps, warmup, peak, peak_kind):
     info = sim.info()
     levels = [{"level": l, "boxes": sim.level(l).nbox, "cells": sim.level(l).nvalid}
               for l in range(info["finest"] + 1)]
-    timers = {k: round(v[0], 4) for k, v in sim.timers().items()}
+    timers = window_timers(sim, tm0)
     # the precision form on the same hierarchy: FP32 + Kahan levels, FP64
     # truncation errors and tags, the same pre-roll and timed window
     fp32 = run_amr_fp32(sh, ctx, stream, flush, K, pre, sim, ms)
@@ -970,6 +971,12 @@ def run_amr_leg(sh, ctx, stream, flush, steps, warmup, peak, peak_kind):
     return out
 
 
+def window_timers(sim, before):
+    """Host seconds per time-stepper phase spent since `before` (the
+    timed window), rounded."""
+    return {k: round(v[0] - before.get(k, (0.0, 0))[0], 4) for k, v in sim.timers().items()}
+
+
 def amr_levels(sh, ctx, sim):
     """Boxes, FP64 values (boxes layout, on the device) and string-tag
     counts of every level of a hierarchy."""
@@ -997,6 +1004,7 @@ def run_amr_fp32(sh, ctx, stream, flush, K, pre, sim64, ms64):
     for _ in range(pre):
         sim.step(1)
     cu0 = sim.info()["cell_updates"]
+    tm0 = sim.timers()
     ctx.profile(True)
     ms, finest = timed_steps(lambda: sim.step(1), K, 0, stream, flush,
                              before=lambda: sim.info()["finest"])
@@ -1006,6 +1014,7 @@ def run_amr_fp32(sh, ctx, stream, flush, K, pre, sim64, ms64):
     cf_ms, _ = ctx.profile_read("coarse_fine")
     other = {c: ctx.profile_read(c)[0] for c in ("average_down", "tagging", "data_move")}
     ctx.profile(False)
+    timers = window_timers(sim, tm0)
     mine, ref = amr_levels(sh, ctx, sim), amr_levels(sh, ctx, sim64)
     err = []
     for l, ((b32, d32, t32), (b64, d64, t64)) in enumerate(zip(mine, ref)):
@@ -1019,7 +1028,8 @@ def run_amr_fp32(sh, ctx, stream, flush, K, pre, sim64, ms64):
     return {"value": cus / (ms / 1e3), "unit": METRIC, "ms_per_step": ms / K,
             "speedup_vs_fp64": ms64 / ms, "levels_in_timed_window": sorted({f + 1 for f in finest}),
             "stage_ms_total": stage_ms, "stage_launches": stage_n, "fill_ms_total": fill_ms,
-            "coarse_fine_ms_total": cf_ms, "other_ms": other, "error_vs_fp64": err,
+            "coarse_fine_ms_total": cf_ms, "other_ms": other, "host_timers_s": timers,
+            "error_vs_fp64": err,
             "note": "FP32 values with FP32 Kahan compensations on every level, FP32 stage "
                     "arithmetic (csrc/sh_stage32.cuh); truncation errors, tags through the "
                     "project hooks, average-down sums and time in FP64"}
