@@ -549,7 +549,10 @@ __global__ void cf_interp_kernel(const CfItem *items, const BoxDev *cboxes, T *f
                                 (W[2] - cb.glo[2]) * cxy;
         for (int nn = 0; nn < ncomp; ++nn) {
             const long long base = cbase + nn * cb.gvol;
-            auto put = [&](int fi, int fj, int fk, double v) {
+            /* FP32 levels interpolate in FP32 (no FP32/FP64 conversions,
+             * which GB300 runs at the FP64 rate), FP64 levels in FP64 */
+            using A = T;
+            auto put = [&](int fi, int fj, int fk, A v) {
                 if (store) {
                     store[it.first + (fi - lo[0]) +
                           (long long)it.nx * ((fj - lo[1]) + (long long)it.ny * (fk - lo[2])) +
@@ -558,44 +561,48 @@ __global__ void cf_interp_kernel(const CfItem *items, const BoxDev *cboxes, T *f
                     const long long d = it.dst + (fi - lo[0]) + (long long)(fj - lo[1]) * it.dsy +
                                         (long long)(fk - lo[2]) * it.dsz + nn * it.dgvol;
                     fbuf[d] = (T)v;
-                    /* FP32 levels: the compensation of a cell filled for good */
-                    if (fcmp) fcmp[d] = (float)((double)(T)v - v);
+                    /* FP32 levels: a cell filled for good starts without compensation */
+                    if (fcmp) fcmp[d] = 0.f;
                 }
             };
-            if (mode != 2 && cf_children_fixed(mode == 0 ? c_old : c_new, base, cx, cxy, P, c0,
-                                               c1, put))
-                continue;
-            auto u = [&](int a, int b2, int d) {
+            if constexpr (sizeof(T) == 8) {
+                if (mode != 2 && cf_children_fixed(mode == 0 ? c_old : c_new, base, cx, cxy, P,
+                                                   c0, c1, put))
+                    continue;
+            }
+            const A al = (A)alpha, be = (A)beta;
+            auto u = [&](int a, int b2, int d) -> A {
                 const long long e = base + a + b2 * cx + d * cxy;
-                if (mode == 0) return (double)c_old[e];
-                if (mode == 1) return (double)c_new[e];
-                return alpha * (double)c_old[e] + beta * (double)c_new[e];
+                if (mode == 0) return c_old[e];
+                if (mode == 1) return c_new[e];
+                return al * c_old[e] + be * c_new[e];
             };
-            const double u0 = u(0, 0, 0);
-            const double dxp = u(1, 0, 0), dxm = u(-1, 0, 0);
-            const double dyp = u(0, 1, 0), dym = u(0, -1, 0);
-            const double dzp = u(0, 0, 1), dzm = u(0, 0, -1);
-            const double Dx = (dxp - dxm) * 0.5, Dy = (dyp - dym) * 0.5, Dz = (dzp - dzm) * 0.5;
-            const double Dxx = dxp - 2. * u0 + dxm;
-            const double Dyy = dyp - 2. * u0 + dym;
-            const double Dzz = dzp - 2. * u0 + dzm;
-            const double Dxy = (u(1, 1, 0) - u(1, -1, 0) - u(-1, 1, 0) + u(-1, -1, 0)) * 0.25;
-            const double Dxz = (u(1, 0, 1) - u(1, 0, -1) - u(-1, 0, 1) + u(-1, 0, -1)) * 0.25;
-            const double Dyz = (u(0, 1, 1) - u(0, 1, -1) - u(0, -1, 1) + u(0, -1, -1)) * 0.25;
+            const A half = (A)0.5, quarter = (A)0.25, sixteenth = (A)0.0625, two = (A)2.;
+            const A u0 = u(0, 0, 0);
+            const A dxp = u(1, 0, 0), dxm = u(-1, 0, 0);
+            const A dyp = u(0, 1, 0), dym = u(0, -1, 0);
+            const A dzp = u(0, 0, 1), dzm = u(0, 0, -1);
+            const A Dx = (dxp - dxm) * half, Dy = (dyp - dym) * half, Dz = (dzp - dzm) * half;
+            const A Dxx = dxp - two * u0 + dxm;
+            const A Dyy = dyp - two * u0 + dym;
+            const A Dzz = dzp - two * u0 + dzm;
+            const A Dxy = (u(1, 1, 0) - u(1, -1, 0) - u(-1, 1, 0) + u(-1, -1, 0)) * quarter;
+            const A Dxz = (u(1, 0, 1) - u(1, 0, -1) - u(-1, 0, 1) + u(-1, 0, -1)) * quarter;
+            const A Dyz = (u(0, 1, 1) - u(0, 1, -1) - u(0, -1, 1) + u(0, -1, -1)) * quarter;
             /* every child has xi_d^2 = 1/16: with s_d = +-1,
              * u = S + sum_d s_d E_d + sum_{d<e} s_d s_e F_de,
              * S = u000 + (Dxx + Dyy + Dzz)/32, E_d = D_d/4, F_de = D_de/16 */
-            const double S = u0 + 0.5 * (0.0625 * Dxx + 0.0625 * Dyy + 0.0625 * Dzz);
-            const double Ex = 0.25 * Dx, Ey = 0.25 * Dy, Ez = 0.25 * Dz;
-            const double Fxy = 0.0625 * Dxy, Fxz = 0.0625 * Dxz, Fyz = 0.0625 * Dyz;
+            const A S = u0 + half * (sixteenth * Dxx + sixteenth * Dyy + sixteenth * Dzz);
+            const A Ex = quarter * Dx, Ey = quarter * Dy, Ez = quarter * Dz;
+            const A Fxy = sixteenth * Dxy, Fxz = sixteenth * Dxz, Fyz = sixteenth * Dyz;
             for (int fk = c0[2]; fk <= c1[2]; ++fk) {
                 const bool zp = (fk - 2 * P[2]) != 0;
                 for (int fj = c0[1]; fj <= c1[1]; ++fj) {
                     const bool yp = (fj - 2 * P[1]) != 0;
                     /* the part without x, and the coefficient of s_x */
-                    const double fyz = (yp == zp) ? Fyz : -Fyz;
-                    const double base = S + (yp ? Ey : -Ey) + (zp ? Ez : -Ez) + fyz;
-                    const double slope = Ex + (yp ? Fxy : -Fxy) + (zp ? Fxz : -Fxz);
+                    const A fyz = (yp == zp) ? Fyz : -Fyz;
+                    const A base = S + (yp ? Ey : -Ey) + (zp ? Ez : -Ez) + fyz;
+                    const A slope = Ex + (yp ? Fxy : -Fxy) + (zp ? Fxz : -Fxz);
                     for (int fi = c0[0]; fi <= c1[0]; ++fi)
                         put(fi, fj, fk, (fi - 2 * P[0]) ? base + slope : base - slope);
                 }
@@ -626,18 +633,19 @@ __global__ void cf_combine_kernel(const CfItem *__restrict__ items, T *__restric
         const long long c = it.first + q;
         /* four components in flight: loaded before any is stored */
         for (int c0 = 0; c0 < ncomp; c0 += 4) {
-            double v[4];
+            /* in the storage type: FP32 levels combine in FP32 */
+            T v[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 if (c0 + u >= ncomp) continue;
                 const long long e = c + (c0 + u) * ncf;
-                if (mode == 0) v[u] = (double)__ldg(i_old + e);
-                else if (mode == 1) v[u] = (double)__ldg(i_new + e);
-                else v[u] = alpha * (double)__ldg(i_old + e) + beta * (double)__ldg(i_new + e);
+                if (mode == 0) v[u] = __ldg(i_old + e);
+                else if (mode == 1) v[u] = __ldg(i_new + e);
+                else v[u] = (T)alpha * __ldg(i_old + e) + (T)beta * __ldg(i_new + e);
             }
 #pragma unroll
             for (int u = 0; u < 4; ++u)
-                if (c0 + u < ncomp) fbuf[d + (c0 + u) * it.dgvol] = (T)v[u];
+                if (c0 + u < ncomp) fbuf[d + (c0 + u) * it.dgvol] = v[u];
         }
     }
 }
@@ -853,21 +861,42 @@ __global__ void avgdown_kernel(const AvgRect *rects, int nrects, long long ncell
                              (long long)(j - cb.glo[1]) * cb.gdim[0] +
                              (long long)(k - cb.glo[2]) * cb.gdim[0] * cb.gdim[1];
         if constexpr (sizeof(T) == 4) {
+            /* The sum of the eight children's v - c in FP32 pairs (hi, lo)
+             * with error-free TwoSum steps, about 48 bits, without the
+             * FP32/FP64 conversions that GB300 runs at the FP64 rate; the
+             * average is (hi, lo) / 8 (exact), stored as value hi and
+             * compensation -lo.  The truncation error is formed the same
+             * way and widened to FP64 once. */
+            auto two_sum = [](float a, float b, float &err) {
+                const float s = __fadd_rn(a, b);
+                const float bb = __fsub_rn(s, a);
+                err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+                return s;
+            };
             for (int n = 0; n < ncomp; ++n) {
                 const long long fo = f0 + n * fb.gvol;
-                double s = 0.0;
+                float hi = 0.f, lo = 0.f, e;
                 for (int dk = 0; dk < 2; ++dk)
                     for (int dj = 0; dj < 2; ++dj)
                         for (int di = 0; di < 2; ++di) {
-                            const long long e = fo + di + dj * fx + dk * fxy;
-                            s += (double)fine[e] - (double)fc[e];
+                            const long long q = fo + di + dj * fx + dk * fxy;
+                            hi = two_sum(hi, fine[q], e);
+                            lo = __fadd_rn(lo, e);
+                            hi = two_sum(hi, -fc[q], e);
+                            lo = __fadd_rn(lo, e);
                         }
-                const double avg = 0.125 * s;
+                hi = two_sum(hi, lo, lo);
+                hi = __fmul_rn(hi, 0.125f);
+                lo = __fmul_rn(lo, 0.125f);
                 const long long co = c0 + n * cb.gvol;
-                if (te) te[fo] = fabs(((double)crse[co] - (double)cc[co]) - avg);
-                const float v = (float)avg;
-                crse[co] = v;
-                cc[co] = (float)((double)v - avg);
+                if (te) {
+                    /* (v_c - c_c) - (hi + lo) */
+                    const float d = two_sum(crse[co], -hi, e);
+                    const float r = __fadd_rn(e, __fsub_rn(-cc[co], lo));
+                    te[fo] = fabs((double)d + (double)r);
+                }
+                crse[co] = hi;
+                cc[co] = -lo;
             }
             continue;
         } else
@@ -2000,7 +2029,16 @@ int sh_level_create_prec(sh_ctx *ctx, int project, int with_gw, const int domain
         ck(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device),
            "SM count");
         make_tiles(kTileZ);
-        if ((long long)tiles.size() < 2LL * 7 * nsm) make_tiles(kTileZShallow);
+        if (L->esize == 8) {
+            if ((long long)tiles.size() < 2LL * 7 * nsm) make_tiles(kTileZShallow);
+        } else {
+            /* the FP32 stage kernels (32-40 registers, up to 16 blocks per
+             * SM) wait on memory: shallower tiles until the level gives
+             * four waves of them */
+            for (int depth = kTileZ / 2; depth >= 1 && (long long)tiles.size() < 4LL * 16 * nsm;
+                 depth /= 2)
+                make_tiles(depth);
+        }
         L->total_gvol = base;
         L->nvalid = vb;
         L->ntiles = (int)tiles.size();
