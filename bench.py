@@ -1031,8 +1031,8 @@ def run_amr_fp32(sh, ctx, stream, flush, K, pre, sim64, ms64):
             "coarse_fine_ms_total": cf_ms, "other_ms": other, "host_timers_s": timers,
             "error_vs_fp64": err,
             "note": "FP32 values with FP32 Kahan compensations on every level, FP32 stage "
-                    "arithmetic (csrc/sh_stage32.cuh); truncation errors, tags through the "
-                    "project hooks, average-down sums and time in FP64"}
+                    "arithmetic (csrc/sh_stage32.cuh), FP32 ghost fills and average-down "
+                    "pairs; truncation errors, tags through the project hooks and time in FP64"}
 
 
 def main():

@@ -157,9 +157,10 @@ SH_API int sh_level_create(sh_ctx *ctx, int project, int with_gw, const int doma
  * FP32 values with FP32 Kahan compensations (value v and compensation c
  * stand for v - c), advanced by FP32 stage kernels written against the
  * equations (RKN4 only; the axion-string projects AxionStringsLap1 / Lap2
- * without GW tensor), while time, average-down, truncation errors (kept in
- * FP64), tagging through the project's hooks, reductions, spectra and
- * outputs work on the FP64 values v - c.  Reads and writes convert; the
+ * without GW tensor), FP32 ghost fills and average-down (sums as FP32
+ * TwoSum pairs), while time, truncation errors (kept in FP64), tagging
+ * through the project's hooks, reductions, spectra and outputs work on the
+ * FP64 values v - c.  Reads and writes convert; the
  * Rhs hook (sh_level_rhs), bubble injection and sh_tag_static need FP64
  * levels (SH_ERR_UNSUPPORTED).  No reference counterpart (sledgehamr
  * stores FP64 only). */
@@ -518,8 +519,8 @@ typedef struct sh_amr_config {
     double volume_threshold_weak;
     /* storage of every level: SH_PREC_FP64 (default) or SH_PREC_FP32_KAHAN
      * (sh_level_create_prec; RKN4, AxionStringsLap1 / Lap2): the precision
-     * form on hierarchies, with the truncation errors, tags, average-down
-     * sums and time in FP64 */
+     * form on hierarchies, with the truncation errors, tags and time in
+     * FP64 */
     int precision;
 } sh_amr_config;
 /* New-grid generation from the buffered tags (at blocking-factor

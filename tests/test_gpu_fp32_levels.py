@@ -1,8 +1,8 @@
 """FP32 + Kahan levels and AMR hierarchies (sh_level_create_prec,
 csrc/sh_stage32.cuh): the precision form on the drop-in path, with FP32
-values and compensations, FP32 stage arithmetic and everything that decides
-the hierarchy (truncation errors, tags through the project's hooks,
-average-down sums, time) in FP64.
+values and compensations, FP32 stage arithmetic, FP32 ghost fills,
+average-down sums as FP32 TwoSum pairs, and the truncation errors, tags
+through the project's hooks and time in FP64.
 
 * A periodic FP32 level, in one box or in several (ghost cells from the
   same-level copies), evolves bit for bit as the FP32 + Kahan ensemble
