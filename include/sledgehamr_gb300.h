@@ -156,13 +156,14 @@ SH_API int sh_level_create(sh_ctx *ctx, int project, int with_gw, const int doma
  * FArrayBox data), or SH_PREC_FP32_KAHAN, the precision form on levels:
  * FP32 values with FP32 Kahan compensations (value v and compensation c
  * stand for v - c), advanced by FP32 stage kernels written against the
- * equations (RKN4 only; the axion-string projects AxionStringsLap1 / Lap2
- * without GW tensor), FP32 ghost fills and average-down (sums as FP32
- * TwoSum pairs), while time, truncation errors (kept in FP64), tagging
- * through the project's hooks, reductions, spectra and outputs work on the
- * FP64 values v - c.  Reads and writes convert; the
- * Rhs hook (sh_level_rhs), bubble injection and sh_tag_static need FP64
- * levels (SH_ERR_UNSUPPORTED).  No reference counterpart (sledgehamr
+ * equations (the axion-string projects AxionStringsLap1 / Lap2 with RKN4,
+ * no GW tensor; FirstOrderPhaseTransition with the pure potential and the
+ * leapfrog, with or without GW tensor), FP32 ghost fills and average-down
+ * (sums as FP32 TwoSum pairs), while time, truncation errors (kept in
+ * FP64), tagging through the project's hooks, reductions, spectra and
+ * outputs work on the FP64 values v - c.  Reads, writes and bubble
+ * injection convert; the Rhs hook (sh_level_rhs) and sh_tag_static need
+ * FP64 levels (SH_ERR_UNSUPPORTED).  No reference counterpart (sledgehamr
  * stores FP64 only). */
 SH_API int sh_level_create_prec(sh_ctx *ctx, int project, int with_gw,
                                 const int domain_lo[3], const int domain_hi[3],
@@ -518,9 +519,9 @@ typedef struct sh_amr_config {
     double volume_threshold_strong;
     double volume_threshold_weak;
     /* storage of every level: SH_PREC_FP64 (default) or SH_PREC_FP32_KAHAN
-     * (sh_level_create_prec; RKN4, AxionStringsLap1 / Lap2): the precision
-     * form on hierarchies, with the truncation errors, tags and time in
-     * FP64 */
+     * (sh_level_create_prec: AxionStringsLap1 / Lap2 with RKN4,
+     * FirstOrderPhaseTransition with the leapfrog): the precision form on
+     * hierarchies, with the truncation errors, tags and time in FP64 */
     int precision;
 } sh_amr_config;
 /* New-grid generation from the buffered tags (at blocking-factor
@@ -710,7 +711,8 @@ SH_API int sh_ensemble_gw_spectrum(sh_ensemble *e, int r, int zero_padding, int 
  * not fit lets later ones pass until the oldest has waited 64 iterations),
  * advances all admitted runs by one step in shared launches, and finishes
  * the runs that reached t_end.  A request with max_level >= 1 runs instead
- * as its own FP64 AMR hierarchy (sh_amr: leapfrog with subcycling,
+ * as its own AMR hierarchy (sh_amr: FP32 + Kahan levels on an FP32 server,
+ * FP64 levels on an FP64 one; leapfrog with subcycling,
  * refinement by the truncation errors of Phi and dPhi against te_crit with
  * the TruncationModifier maxima of level 0, params_mod_norm0), admitted
  * while the device has room for 16 times its level-0 state and advanced to

@@ -729,9 +729,12 @@ __global__ void projection_kernel(const __grid_constant__ ProjArgs a, double *da
 }
 
 /* Bubble injection on the valid cells of a level (sh_level_add_bubbles). */
+/* FP32 levels (T = float): the bubbles are added to the FP64 values v - c
+ * and the sums stored as value and compensation again. */
+template <class T>
 __global__ void level_bubbles_kernel(const BoxDev *boxes, const long long *vbase, int nbox,
                                      long long nvalid, int ncomp, int cphi, int cdphi,
-                                     double *buf, BubbleList bl, double dx, double L) {
+                                     T *buf, float *cmp, BubbleList bl, double dx, double L) {
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nvalid;
          v += (long long)gridDim.x * blockDim.x) {
         const int bx = find_box(vbase, nbox, v);
@@ -744,10 +747,19 @@ __global__ void level_bubbles_kernel(const BoxDev *boxes, const long long *vbase
         const long long c = b.off * ncomp + (i - b.glo[0]) +
                             (long long)(j - b.glo[1]) * b.gdim[0] +
                             (long long)(k - b.glo[2]) * b.gdim[0] * b.gdim[1];
-        double phi = buf[c + cphi * b.gvol], dphi = buf[c + cdphi * b.gvol];
+        const long long ep = c + cphi * b.gvol, ed = c + cdphi * b.gvol;
+        double phi = buf[ep], dphi = buf[ed];
+        if constexpr (sizeof(T) == 4) {
+            phi -= cmp[ep];
+            dphi -= cmp[ed];
+        }
         add_bubbles_at(bl, i, j, k, dx, L, phi, dphi);
-        buf[c + cphi * b.gvol] = phi;
-        buf[c + cdphi * b.gvol] = dphi;
+        buf[ep] = (T)phi;
+        buf[ed] = (T)dphi;
+        if constexpr (sizeof(T) == 4) {
+            cmp[ep] = (float)((double)buf[ep] - phi);
+            cmp[ed] = (float)((double)buf[ed] - dphi);
+        }
     }
 }
 
@@ -1394,9 +1406,9 @@ void fill_patch(sh_ctx *ctx, sh_level *L, double *buf, double t) {
     note_fill(L, buf, t);
 }
 
-/* The ghost cells of the first nfill components of an FP32 stage buffer
- * (its positions); not recorded as a fill of the buffer. */
-void fill_patch_positions(sh_ctx *ctx, sh_level *L, double *buf, double t, int nfill) {
+/* The ghost cells of the first nfill components of an FP32 stage buffer,
+ * not recorded as a fill of the buffer. */
+void fill_patch_stage(sh_ctx *ctx, sh_level *L, double *buf, double t, int nfill) {
     fill_patch_t<float>(ctx, L, (float *)buf, t, nfill);
 }
 
@@ -1588,13 +1600,67 @@ void integrate(sh_ctx *ctx, sh_level *L, int type, const double *tableau, int ns
     }
 }
 
-/* 1 (7-point) or 2 (13-point Laplacian) for the projects whose FP32
- * levels have stage kernels (sh_stage32.cuh), else 0. */
+/* The projects whose FP32 levels have stage kernels (sh_stage32.cuh):
+ * 1, 2 the axion strings with the 7- / 13-point Laplacian (RKN4), 3
+ * FirstOrderPhaseTransition (leapfrog); else 0. */
+constexpr int kFam32Fopt = 3;
 int stage32_family(const ProjectOps *ops) {
     if (!ops || !ops->name) return 0;
     if (std::strcmp(ops->name, "AxionStringsLap1") == 0) return 1;
     if (std::strcmp(ops->name, "AxionStringsLap2") == 0) return 2;
+    if (std::strcmp(ops->name, "FirstOrderPhaseTransition") == 0) return kFam32Fopt;
     return 0;
+}
+
+/* One leapfrog step of an FP32 FirstOrderPhaseTransition level (the old
+ * buffer's ghost cells filled): the drift writes the new positions, whose
+ * ghost cells are then filled at t + dt, and the second kick the new
+ * momenta in place beside them. */
+void integrate32_fopt(sh_ctx *ctx, sh_level *L, int type, double dt, double dx,
+                      const double *params, int nparams) {
+    require(type == SH_INTEGRATOR_LEAPFROG,
+            "FP32 FirstOrderPhaseTransition levels integrate with the leapfrog (type 11)");
+    require(params && nparams >= 4 && params[0] == 0.,
+            "FP32 FirstOrderPhaseTransition levels take the pure potential (params[0] = 0, "
+            "params[1..3] = q2, q3, q4)");
+    const int np = L->npairs;
+    ensure_kbuf(ctx, L, (size_t)L->total_gvol * np, 1); /* vh and its compensation, FP32 */
+    Stage32FoptArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.tiles = L->d_tiles;
+    a.boxes = L->d_boxes;
+    a.y0 = (const float *)L->buf[SH_OLD];
+    a.c_old = L->cmp[SH_OLD];
+    a.out = (float *)L->buf[SH_NEW];
+    a.c_new = L->cmp[SH_NEW];
+    a.kv = (float *)L->kbuf;
+    a.kc = a.kv + (size_t)L->total_gvol * np;
+    a.inv12dx2 = (float)(1. / (12. * dx * dx));
+    a.inv12dx = (float)(1. / (12. * dx));
+    a.hdt = (float)(0.5 * dt);
+    a.dt = (float)dt;
+    a.q2 = (float)params[1];
+    a.q3 = (float)params[2];
+    a.q4 = (float)params[3];
+    const double t0 = L->t[SH_OLD];
+    dim3 block(kTileX, kTileY, 1);
+    for (int st = 0; st < 2; ++st) {
+        a.state = (const float *)(st == 0 ? L->buf[SH_OLD] : L->buf[SH_NEW]);
+        if (L->ntiles > 0) {
+            ProfScope ps(ctx, kProfRhs);
+            if (L->with_gw) {
+                if (st == 0) stage32_fopt_kernel<0, true><<<L->ntiles, block, 0, ctx->stream>>>(a);
+                else stage32_fopt_kernel<1, true><<<L->ntiles, block, 0, ctx->stream>>>(a);
+            } else {
+                if (st == 0) stage32_fopt_kernel<0, false><<<L->ntiles, block, 0, ctx->stream>>>(a);
+                else stage32_fopt_kernel<1, false><<<L->ntiles, block, 0, ctx->stream>>>(a);
+            }
+            ctx->launches++;
+            ck(cudaGetLastError(), "FP32 stage kernel launch");
+        }
+        if (st == 0) fill_patch_stage(ctx, L, L->buf[SH_NEW], t0 + dt, L->ncomp);
+        else fill_patch(ctx, L, L->buf[SH_NEW], t0 + dt);
+    }
 }
 
 /* One RKN4 step of an FP32 level (the old buffer's ghost cells filled):
@@ -1660,7 +1726,7 @@ void integrate32(sh_ctx *ctx, sh_level *L, int type, double dt, double dx,
             }
         }
         if (st < 2)
-            fill_patch_positions(ctx, L, dst[st], t0 + dt * node[st + 1], 2);
+            fill_patch_stage(ctx, L, dst[st], t0 + dt * node[st + 1], 2);
         else
             fill_patch(ctx, L, dst[st], t0 + dt);
     }
@@ -1966,10 +2032,12 @@ int sh_level_create_prec(sh_ctx *ctx, int project, int with_gw, const int domain
         L->project = project;
         L->with_gw = with_gw != 0;
         if (precision == SH_PREC_FP32_KAHAN) {
-            require(stage32_family(L->ops) != 0,
-                    "FP32 levels are available for the axion-string projects AxionStringsLap1 "
-                    "and AxionStringsLap2");
-            require(!L->with_gw, "FP32 levels carry no GW tensor");
+            const int fam = stage32_family(L->ops);
+            require(fam != 0,
+                    "FP32 levels are available for AxionStringsLap1, AxionStringsLap2 and "
+                    "FirstOrderPhaseTransition");
+            require(!L->with_gw || fam == kFam32Fopt,
+                    "FP32 axion-string levels carry no GW tensor");
             L->esize = 4;
         }
         L->ncomp = L->ops->nscalars + (L->with_gw ? 12 : 0);
@@ -2287,8 +2355,11 @@ int sh_level_advance(sh_ctx *ctx, sh_level *L, int integrator, const double *tab
         if (!fill_current(L, L->buf[SH_OLD], L->t[SH_OLD], ver))
             fill_patch(ctx, L, L->buf[SH_OLD], L->t[SH_OLD]);
         if (L->esize == 4) {
-            require(!L->with_gw && ngw == 0, "FP32 levels carry no GW tensor");
-            integrate32(ctx, L, integrator, dt, dx, params, nparams, ko_order);
+            require(ko_order == 0, "FP32 levels have no Kreiss-Oliger dissipation");
+            if (stage32_family(L->ops) == kFam32Fopt)
+                integrate32_fopt(ctx, L, integrator, dt, dx, params, nparams);
+            else
+                integrate32(ctx, L, integrator, dt, dx, params, nparams, ko_order);
         } else {
             integrate(ctx, L, integrator, tableau, nstages, dt, dx, params, nparams, gw_params,
                       ngw, ko_order, ko_strength);
@@ -2350,11 +2421,15 @@ int sh_level_add_bubbles(sh_ctx *ctx, sh_level *L, int which, int comp_phi, int 
         ck(cudaMemcpyAsync(d + nx, profile, np * sizeof(double), cudaMemcpyHostToDevice,
                            ctx->stream),
            "bubble upload");
-        require_fp64(L, "bubble injection");
         BubbleList bl{d, d + nx, nb, nbins, inv_dx, Lcut};
-        level_bubbles_kernel<<<grid_for(L->nvalid), 256, 0, ctx->stream>>>(
-            L->d_boxes, L->d_vbase, (int)L->boxes.size(), L->nvalid, L->ncomp, comp_phi,
-            comp_dphi, L->buf[which], bl, dx, N * dx);
+        if (L->esize == 4)
+            level_bubbles_kernel<float><<<grid_for(L->nvalid), 256, 0, ctx->stream>>>(
+                L->d_boxes, L->d_vbase, (int)L->boxes.size(), L->nvalid, L->ncomp, comp_phi,
+                comp_dphi, (float *)L->buf[which], L->cmp[which], bl, dx, N * dx);
+        else
+            level_bubbles_kernel<double><<<grid_for(L->nvalid), 256, 0, ctx->stream>>>(
+                L->d_boxes, L->d_vbase, (int)L->boxes.size(), L->nvalid, L->ncomp, comp_phi,
+                comp_dphi, L->buf[which], nullptr, bl, dx, N * dx);
         ctx->launches++;
         ck(cudaGetLastError(), "bubble launch");
         ck(cudaStreamSynchronize(ctx->stream), "bubbles");

@@ -12,9 +12,10 @@
  * equations of the ensemble path (leapfrog, 4th-order stencils, bubble
  * injection at t = 0, the GW spectrum of GravitationalWaves::
  * ComputeSpectrum).  Requests with refinement levels run as their own
- * FP64 AMR hierarchies (sh_amr with FirstOrderPhaseTransition + GW, the
+ * AMR hierarchies (sh_amr with FirstOrderPhaseTransition + GW, the
  * leapfrog, truncation-error tags with the field maxima of level 0 as the
- * TruncationModifier parameters), each in a context of its own (its own
+ * TruncationModifier parameters; FP32 + Kahan levels when the pool is FP32,
+ * FP64 levels when it is FP64), each in a context of its own (its own
  * CUDA stream) stepped by a host thread of its own, so that their kernels
  * overlap with the pool's and with each other's; they are admitted while
  * the device has room for 16 times their level-0 state and fail (state 3)
@@ -85,6 +86,7 @@ struct sh_server {
     std::mutex mu;
     std::condition_variable cv; /* an AMR job finished */
     sh_ensemble *pool = nullptr;
+    int precision = SH_PREC_FP64; /* of the pool; FP32 pools run FP32 + Kahan hierarchies */
     std::map<long long, Req> reqs;
     std::deque<long long> queue;
     std::vector<long long> running;
@@ -207,6 +209,9 @@ int admit_amr(sh_server *S, Req &q) {
     for (int k = 4; k < 7; ++k) c.params[k] = 0.;
     c.nparams = 7;
     c.params_mod_norm0 = 1;
+    /* the pool's precision form: FP32 (with or without compensation in the
+     * pool) gives FP32 + Kahan levels */
+    c.precision = S->precision == SH_PREC_FP64 ? SH_PREC_FP64 : SH_PREC_FP32_KAHAN;
     sh_ctx *actx = nullptr;
     rc = sh_ctx_create(S->device, &actx);
     if (rc != SH_OK) return rc;
@@ -246,6 +251,7 @@ int sh_server_create(sh_ctx *ctx, int precision, long long capacity_cells, sh_se
     sh_server *S = new (std::nothrow) sh_server();
     if (!S) return SH_ERR_NOMEM;
     S->ctx = ctx;
+    S->precision = precision;
     int rc = sh_ensemble_create_pool(ctx, SH_FAMILY_FOPT_GW, precision, capacity_cells, &S->pool);
     if (rc != SH_OK) {
         delete S;

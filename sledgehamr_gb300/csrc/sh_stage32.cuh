@@ -111,6 +111,100 @@ __global__ void __launch_bounds__(kThreads) stage32_axion_kernel(const __grid_co
     }
 }
 
+/* Kick-drift-kick leapfrog stages of FP32 levels of FirstOrderPhaseTransition
+ * with the pure potential (params[0] = 0), with or without the GW tensor:
+ *   Phi'' = lap Phi + q2 Phi + q3 Phi^2 + q4 Phi^3,
+ *   u_ij'' = lap u_ij + d_i Phi d_j Phi
+ * (4th-order Laplacian and gradient; projects/FirstOrderPhaseTransition/
+ * kernels_rhs.h:20-109), the schedule of source/integrators/leapfrog.cpp:13-57
+ * (both kicks with the acceleration of the positions they see):
+ *   STAGE 0: a = f(x0);  vh = v0 + dt/2 a;  x1 = x0 + dt vh
+ *   STAGE 1: a = f(x1);  v1 = vh + dt/2 a
+ * with Kahan-compensated updates: vh and its compensation go to the K
+ * buffer, x1 and v1 with theirs to the new state.  The arithmetic is that of
+ * the FP32 ensemble kernel of the same equations (sh_fast.cu). */
+struct Stage32FoptArgs {
+    const TileDev *tiles;
+    const BoxDev *boxes;
+    const float *state; /* positions read by the stencils (stage 0: x0, 1: x1) */
+    const float *y0;    /* the step's initial state */
+    const float *c_old; /* its compensations */
+    float *out;         /* the new state */
+    float *c_new;       /* its compensations */
+    float *kv, *kc;     /* vh and its compensation (np components each) */
+    float inv12dx2, inv12dx, hdt, dt, q2, q3, q4;
+};
+
+template <int STAGE, bool GW>
+__global__ void __launch_bounds__(kThreads)
+    stage32_fopt_kernel(const __grid_constant__ Stage32FoptArgs a) {
+    constexpr int NP = GW ? 7 : 1, NC = 2 * NP;
+    const TileDev t = a.tiles[blockIdx.x];
+    const BoxDev b = a.boxes[t.box];
+    const int tid = threadIdx.x + kTileX * threadIdx.y;
+    const int ty = tid / t.nx;
+    const int i = t.x0 + (tid - ty * t.nx);
+    const int j = t.y0 + ty;
+    if (ty >= kThreads / t.nx || i > b.hi[0] || j > b.hi[1]) return;
+    const int kend = min(t.z0 + t.nz - 1, b.hi[2]);
+    const long long gx = b.gdim[0], gxy = gx * b.gdim[1], gvol = b.gvol;
+    /* position q: Phi, u_xx, u_yy, u_zz, u_xy, u_xz, u_yz; momentum: dPhi,
+     * du_xx, ... (the level's component order) */
+    auto pos = [](int q) { return q == 0 ? 0 : 1 + q; };
+    auto mom = [](int q) { return q == 0 ? 1 : NP + q; };
+    for (int k = t.z0; k <= kend; ++k) {
+        const long long lc =
+            (i - b.glo[0]) + (long long)(j - b.glo[1]) * gx + (long long)(k - b.glo[2]) * gxy;
+        const long long sb = b.off * NC + lc;
+        const long long kb = b.off * NP + lc;
+        float acc[NP];
+#pragma unroll
+        for (int q = 0; q < NP; ++q) {
+            const float *s = a.state + sb + pos(q) * gvol;
+            float s1 = s[1] + s[-1];
+            s1 += s[gx] + s[-gx];
+            s1 += s[gxy] + s[-gxy];
+            float s2 = s[2] + s[-2];
+            s2 += s[2 * gx] + s[-2 * gx];
+            s2 += s[2 * gxy] + s[-2 * gxy];
+            acc[q] = (16.f * s1 - s2 - 90.f * s[0]) * a.inv12dx2;
+        }
+        const float *ph = a.state + sb;
+        const float phi = ph[0];
+        acc[0] += phi * (a.q2 + phi * (a.q3 + phi * a.q4));
+        if constexpr (GW) {
+            float g[3];
+            g[0] = (8.f * (ph[1] - ph[-1]) - (ph[2] - ph[-2])) * a.inv12dx;
+            g[1] = (8.f * (ph[gx] - ph[-gx]) - (ph[2 * gx] - ph[-2 * gx])) * a.inv12dx;
+            g[2] = (8.f * (ph[gxy] - ph[-gxy]) - (ph[2 * gxy] - ph[-2 * gxy])) * a.inv12dx;
+            acc[1] += g[0] * g[0];
+            acc[2] += g[1] * g[1];
+            acc[3] += g[2] * g[2];
+            acc[4] += g[0] * g[1];
+            acc[5] += g[0] * g[2];
+            acc[6] += g[1] * g[2];
+        }
+#pragma unroll
+        for (int q = 0; q < NP; ++q) {
+            if constexpr (STAGE == 0) {
+                float v = a.y0[sb + mom(q) * gvol], cv = a.c_old[sb + mom(q) * gvol];
+                f32::kahan(v, a.hdt * acc[q], cv);
+                a.kv[kb + q * gvol] = v;
+                a.kc[kb + q * gvol] = cv;
+                float x = a.y0[sb + pos(q) * gvol], cx = a.c_old[sb + pos(q) * gvol];
+                f32::kahan(x, a.dt * v, cx);
+                a.out[sb + pos(q) * gvol] = x;
+                a.c_new[sb + pos(q) * gvol] = cx;
+            } else {
+                float v = a.kv[kb + q * gvol], cv = a.kc[kb + q * gvol];
+                f32::kahan(v, a.hdt * acc[q], cv);
+                a.out[sb + mom(q) * gvol] = v;
+                a.c_new[sb + mom(q) * gvol] = cv;
+            }
+        }
+    }
+}
+
 } // namespace sh
 
 #endif

@@ -16,6 +16,9 @@ through the project's hooks and time in FP64.
   compared cell by cell with the mismatches counted (0.1 % measured: cells
   whose truncation error lies next to te_crit).
 * A checkpoint of an FP32 hierarchy restarts to the same evolution.
+* FirstOrderPhaseTransition + GW on FP32 levels (leapfrog) against the FP32
+  ensemble kernel and the FP64 oracle; bubbles on FP32 levels; an FP32
+  hierarchy of that project against the FP64 oracle's.
 * FP64-only operations refuse FP32 levels with SH_ERR_UNSUPPORTED.
 """
 import numpy as np
@@ -147,4 +150,93 @@ def test_fp64_only_operations_refuse_fp32_levels(ctx):
         lv.advance(sh.LEAPFROG, 0.0625, 0.25, params=[1.0, 0.0])
     lv.close()
     with pytest.raises(sh.ShError):
-        sh.Level.periodic(ctx, "FirstOrderPhaseTransition", 16, 2, precision=F32)
+        sh.Level.periodic(ctx, "AxionStringsLap1", 16, 1, with_gw=True, precision=F32)
+
+
+def _fopt_state(N, L, seed):
+    """FirstOrderPhaseTransition + GW state (level order) of FP32 numbers."""
+    s = np.zeros((14, N, N, N))
+    kmax = 0.5 * np.pi * N / L
+    s[0] = 0.5 + 0.3 * ic.gaussian_field(N, L, kmax, seed)
+    s[1] = 0.1 * ic.gaussian_field(N, L, kmax, seed + 1)
+    for q in range(12):
+        s[2 + q] = 1e-3 * ic.gaussian_field(N, L, kmax, seed + 2 + q)
+    return s.astype(np.float32).astype(np.float64)
+
+
+def test_fp32_fopt_level_against_ensemble_and_oracle(ctx, oracle):
+    """FirstOrderPhaseTransition + GW on FP32 levels (leapfrog): one box and
+    eight boxes give the same bits, within 1e-6 of the FP32 ensemble kernel
+    of the same equations (the same FP32 arithmetic in a shared-memory ring)
+    and within 5e-6 of the FP64 oracle after 10 steps."""
+    N, dx, dt, steps = 32, 0.25, 0.05, 10
+    q = [-0.2, 0.5, -0.6]
+    st = _fopt_state(N, N * dx, 21)
+    E = sh.Ensemble(ctx, sh.FAMILY_FOPT_GW, F32, [N], [dx], q + [0.0])
+    E.write(0, st)
+    E.set_time(0.0)
+    E.step(dt, steps)
+    ens = np.asarray(E.read(0)).ravel()
+    E.close()
+    outs = []
+    for max_grid in (0, 16):
+        lv = sh.Level.periodic(ctx, "FirstOrderPhaseTransition", N, 2, max_grid=max_grid,
+                               with_gw=True, precision=F32)
+        lv.write(st)
+        lv.set_time(0.0)
+        for _ in range(steps):
+            lv.advance(sh.LEAPFROG, dt, dx, params=[0.0, *q, 0.0, 0.0, 0.0])
+        outs.append(lv.read().ravel())
+        lv.close()
+    assert np.array_equal(outs[0], outs[1])
+    assert rel_l2(outs[0], ens) <= 1e-6, rel_l2(outs[0], ens)
+    ref = oracle.evolve_periodic("FirstOrderPhaseTransition", sh.LEAPFROG, st, t0=0.0, dt=dt,
+                                 dx=dx, nsteps=steps, params=[0.0, *q, 0.0, 0.0, 0.0],
+                                 with_gw=True, nghost=2).ravel()
+    e = rel_l2(outs[0], ref)
+    eu = rel_l2(outs[0].reshape(14, -1)[2:], ref.reshape(14, -1)[2:])
+    print(f"FP32 FOPT level against FP64: fields {e:.2e}, GW tensor {eu:.2e}")
+    assert e <= 5e-6 and eu <= 5e-5
+
+
+def test_fp32_fopt_bubbles_and_hierarchy_against_fp64_oracle(ctx):
+    """Bubbles injected into an FP32 FirstOrderPhaseTransition + GW level
+    agree with the FP64 level's to FP32 rounding; an FP32 hierarchy of that
+    project (leapfrog, truncation-error tags scaled by level-0 maxima) keeps
+    the FP64 oracle's levels and boxes, fields within 1e-5 per level."""
+    from tests.oracle_lib import oracle_add_bubbles
+    N0, L = 16, 8.0
+    nb = 60
+    r = np.arange(nb) / 8.0
+    prof = np.stack([0.5 * (1 - np.tanh((r - 2.0) / 0.7)), np.zeros(nb)])
+    st = np.zeros((14, N0, N0, N0))
+    st[2:8] = 1e-3 * np.stack([ic.gaussian_field(N0, L, 3.0, 50 + q) for q in range(6)])
+    st = st.astype(np.float32).astype(np.float64)
+    centres = np.array([[4.1, 3.9, 4.2]])
+    a = sh.Level.periodic(ctx, "FirstOrderPhaseTransition", N0, 2, with_gw=True, precision=F32)
+    a.write(st)
+    a.add_bubbles(centres, prof, 8.0, 7.0, L / N0)
+    want = oracle_add_bubbles(st, centres.tolist(), prof, 8.0, 7.0, L / N0)
+    assert rel_l2(a.read(), want) <= 1e-7
+    a.close()
+    lb = 0.8
+    num = 3.0 + np.sqrt(9.0 - 8.0 * lb)
+    params = [0.0, -1.0, 3.0 * num / (4.0 * lb), -num * num / (8.0 * lb), 0.0, 0.0, 0.0]
+    te = [1e-2, 1e-2] + [1e300] * 12
+    kw = dict(N0=N0, L=L, cfl=0.2, t_start=0.0, nghost=2, max_level=2, blocking_factor=8,
+              max_grid_size=16, n_error_buf=1, regrid_dt=0.0, te_crit=te, params=params,
+              with_gw=1, integrator=sh.LEAPFROG, params_mod_norm0=1, record_regrids=0,
+              max_local_regrids=0)
+    g = sh.Amr(ctx, sh.amr_config("FirstOrderPhaseTransition", precision=F32, **kw), want)
+    o = OracleAmr(sh.amr_config("FirstOrderPhaseTransition", **kw), want)
+    for step in range(5):
+        g.step(1)
+        o.step(1)
+        assert g.info()["finest"] == o.info()["finest"], step
+        for lev in range(g.info()["finest"] + 1):
+            assert g.level(lev).boxes == o.boxes(lev), (step, lev)
+            e = rel_l2(g.level(lev).read(), o.read(lev)[0])
+            assert e <= 1e-5, (step, lev, e)
+    assert g.info()["finest"] >= 1
+    g.close()
+    o.close()
