@@ -512,9 +512,12 @@ def run_serve_leg(sh, ctx, max_n):
     r64, s64 = trace(sh.PREC_FP64, reqs)
     tot = [abs(a.sum() - b.sum()) / b.sum() for a, b in zip(s32, s64)]
     Ns = [rq["N"] for rq in reqs]
-    # the same requests with 0-2 refinement levels (AMR requests in FP64)
+    # the same requests with 0-2 refinement levels: an FP32 server (FP32 +
+    # Kahan hierarchies for the refined requests) against an FP64 one
     reqs_amr = serve_requests(max_n, amr=True)
-    r_amr, _ = trace(sh.PREC_FP32_KAHAN, reqs_amr)
+    r_amr, sa32 = trace(sh.PREC_FP32_KAHAN, reqs_amr)
+    r_amr64, sa64 = trace(sh.PREC_FP64, reqs_amr)
+    tot_amr = [abs(a.sum() - b.sum()) / b.sum() for a, b in zip(sa32, sa64)]
     levels = [rq["max_level"] for rq in reqs_amr]
     return {
         "workload": f"{len(reqs)} two-bubble requests, Poisson arrivals {SERVE['rate']}/s "
@@ -526,11 +529,17 @@ def run_serve_leg(sh, ctx, max_n):
         "with_refinement": {
             "workload": f"the same requests with {levels.count(0)} / {levels.count(1)} / "
                         f"{levels.count(2)} of them at 0 / 1 / 2 refinement levels (base grid "
-                        f"N / 2^levels, at least {SERVE['min_base']}; AMR requests as FP64 "
-                        f"hierarchies, te_crit {SERVE['te_crit']}, regrid every "
-                        f"{SERVE['regrid_steps']} coarse steps; spectrum of level 0), "
-                        f"single-level requests in the FP32+Kahan pool",
-            **r_amr},
+                        f"N / 2^levels, at least {SERVE['min_base']}; AMR requests as "
+                        f"hierarchies of the server's precision, te_crit {SERVE['te_crit']}, "
+                        f"regrid every {SERVE['regrid_steps']} coarse steps; spectrum of "
+                        f"level 0)",
+            "fp32_kahan": r_amr, "fp64": r_amr64,
+            "gw_total_rel_err_fp32_vs_fp64": {
+                "max": float(max(tot_amr)), "median": float(np.median(tot_amr)),
+                "by_refinement_levels": {
+                    str(m): float(max(t for t, rq in zip(tot_amr, reqs_amr)
+                                      if rq["max_level"] == m))
+                    for m in sorted(set(levels))}}},
         "gw_total_rel_err_fp32_vs_fp64": {"max": float(max(tot)),
                                           "median": float(np.median(tot))},
     }
