@@ -165,8 +165,10 @@ struct sh_level {
     double *buf[3] = {nullptr, nullptr, nullptr};
     int esize = 8; /* 8: FP64 storage; 4: FP32 values with FP32 Kahan compensations */
     /* FP32 levels: compensations of SH_NEW / SH_OLD (the value v and its
-     * compensation c stand for v - c), the truncation errors in FP64 (an
-     * FP64 level keeps them in its SH_OLD buffer, as the reference does),
+     * compensation c stand for v - c), the truncation errors in FP64 for the
+     * tag comparison (an FP64 level keeps them in its SH_OLD buffer, as the
+     * reference does; an FP32 level writes them there too, for the data
+     * flow of the next shadow level, and reads them from here),
      * and an FP64 copy of one buffer for the read-only operations that go
      * through the FP64 hooks and kernels (tagging, reductions, outputs) */
     float *cmp[2] = {nullptr, nullptr};
@@ -849,7 +851,8 @@ __global__ void __launch_bounds__(kReduceThreads)
 template <class T>
 __global__ void avgdown_kernel(const AvgRect *rects, int nrects, long long ncells,
                                const BoxDev *fboxes, const BoxDev *cboxes, int ncomp,
-                               const T *fine, const float *fc, T *crse, float *cc, double *te) {
+                               const T *fine, const float *fc, T *crse, float *cc, double *te,
+                               T *te_old, float *te_old_c) {
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncells;
          c += (long long)gridDim.x * blockDim.x) {
         int lo = 0, hi = nrects - 1;
@@ -905,7 +908,14 @@ __global__ void avgdown_kernel(const AvgRect *rects, int nrects, long long ncell
                     /* (v_c - c_c) - (hi + lo) */
                     const float d = two_sum(crse[co], -hi, e);
                     const float r = __fadd_rn(e, __fsub_rn(-cc[co], lo));
-                    te[fo] = fabs((double)d + (double)r);
+                    const double tev = fabs((double)d + (double)r);
+                    te[fo] = tev;
+                    /* and into the fine level's old buffer, where the
+                     * reference keeps it (the next shadow level averages
+                     * that buffer down) */
+                    const float tv = (float)tev;
+                    te_old[fo] = tv;
+                    te_old_c[fo] = (float)((double)tv - tev);
                 }
                 crse[co] = hi;
                 cc[co] = -lo;
@@ -1835,12 +1845,12 @@ void average_down_impl(sh_ctx *ctx, const sh_level *F, int which_f, sh_level *C,
         avgdown_kernel<float><<<grid_for(F->avg_cells), 256, 0, ctx->stream>>>(
             (const AvgRect *)F->d_avg, F->navg, F->avg_cells, F->d_boxes, C->d_boxes, F->ncomp,
             (const float *)F->buf[which_f], F->cmp[which_f], (float *)C->buf[which_c],
-            C->cmp[which_c], te);
+            C->cmp[which_c], te, (float *)F->buf[SH_OLD], F->cmp[SH_OLD]);
     } else {
         avgdown_kernel<double><<<grid_for(F->avg_cells), 256, 0, ctx->stream>>>(
             (const AvgRect *)F->d_avg, F->navg, F->avg_cells, F->d_boxes, C->d_boxes, F->ncomp,
             F->buf[which_f], nullptr, C->buf[which_c], nullptr,
-            with_te ? F->buf[SH_OLD] : nullptr);
+            with_te ? F->buf[SH_OLD] : nullptr, nullptr, nullptr);
     }
     ctx->launches++;
     ck(cudaGetLastError(), "average-down launch");

@@ -169,13 +169,15 @@ def amr_request(N, d, seed, max_level=1):
     return rq
 
 
-def run_amr_alone(ctx, rq):
+def run_amr_alone(ctx, rq, precision=sh.PREC_FP64):
     """The AMR request's hierarchy built directly: FirstOrderPhaseTransition
     + GW, leapfrog, TruncationModifier maxima from level 0, bubbles on
     level 0 of a zero state, ceil(t_end / dt) coarse steps, spectrum of
-    level 0."""
+    level 0; levels of the given precision (FP32 servers run FP32 + Kahan
+    hierarchies)."""
     q = rq["params"]
-    cfg = sh.amr_config("FirstOrderPhaseTransition", N0=rq["N"], L=rq["N"] * rq["dx"],
+    cfg = sh.amr_config("FirstOrderPhaseTransition", precision=precision, N0=rq["N"],
+                        L=rq["N"] * rq["dx"],
                         cfl=rq["dt"] / rq["dx"], t_start=0.0, nghost=2,
                         max_level=rq["max_level"], blocking_factor=8, max_grid_size=32,
                         n_error_buf=1, regrid_dt=rq["regrid_dt"],
@@ -198,16 +200,18 @@ def submit_all(S, reqs):
                      regrid_dt=rq.get("regrid_dt", 0.0)) for rq in reqs]
 
 
-def test_amr_requests_equal_alone_and_in_the_mix(ctx):
-    """A request with a refinement level runs as its own hierarchy: its
-    spectrum equals the hierarchy's run outside the server bitwise, alone
-    and beside single-level requests in the same server."""
+@pytest.mark.parametrize("prec", [sh.PREC_FP32_KAHAN, sh.PREC_FP64])
+def test_amr_requests_equal_alone_and_in_the_mix(ctx, prec):
+    """A request with a refinement level runs as its own hierarchy, of the
+    server's precision: its spectrum equals the hierarchy's run outside the
+    server bitwise, alone and beside single-level requests in the same
+    server."""
     ra = amr_request(32, 6.0, 11)
-    alone, finest = run_amr_alone(ctx, ra)
+    alone, finest = run_amr_alone(ctx, ra, prec)
     assert finest >= 1  # the walls were refined
     mixes = ([ra], [request(16, 6.0, 1), ra, request(24, 8.0, 2)])
     for reqs in mixes:
-        S = sh.Server(ctx, sh.PREC_FP32_KAHAN, capacity_cells=60000)
+        S = sh.Server(ctx, prec, capacity_cells=60000)
         ids = submit_all(S, reqs)
         it = 0
         while True:
