@@ -13,8 +13,7 @@ through the project's hooks and time in FP64.
 * An FP32 hierarchy against the FP64 oracle's hierarchy: the same levels and
   boxes after every coarse step, fields within 2e-6 relative L2 per level
   (the FP32 rounding of the stencils; 1e-7 to 4e-7 measured), regrid masks
-  compared cell by cell with the mismatches counted (0.1 % measured: cells
-  whose truncation error lies next to te_crit).
+  compared cell by cell with the mismatches counted (none measured).
 * A checkpoint of an FP32 hierarchy restarts to the same evolution.
 * FirstOrderPhaseTransition + GW on FP32 levels (leapfrog) against the FP32
   ensemble kernel and the FP64 oracle; bubbles on FP32 levels; an FP32
@@ -112,10 +111,10 @@ def test_fp32_hierarchy_against_fp64_oracle(ctx):
     print("FP32 hierarchy: rel L2 per (step, level)", errors,
           f"tag mismatches {mism} of {cells} cells")
     # a truncation error is the difference of two nearly equal values, so
-    # its FP32 rounding (about 1e-7 of the field) moves cells whose error
-    # lies within about 1e-5 relative of te_crit across it: 75 of 77,824
-    # when measured
-    assert mism <= cells // 200
+    # its FP32 rounding (about 1e-7 of the field) can move a cell whose
+    # error lies within about 1e-5 relative of te_crit across it (none of
+    # 77,824 when measured)
+    assert mism <= cells // 1000
     g.close()
     o.close()
 
