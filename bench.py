@@ -352,6 +352,10 @@ def run_fopt_leg(sh, ctx, stream, flush, steps, warmup):
     e32 = E.energy()[0]
     spec32_ms, (gw32, gu32) = spectrum_times(lambda ub: E.gw_spectrum(
         0, zero_padding=1, projection_type=2, unbinned=ub))
+    # the same spectra with FP32 transforms and projection (FP64 bin sums)
+    E.set_spectrum_precision(sh.PREC_FP32)
+    spec32f_ms, (gw32f, gu32f) = spectrum_times(lambda ub: E.gw_spectrum(
+        0, zero_padding=1, projection_type=2, unbinned=ub))
     f32 = E.read(0)
     t32 = E.time()
     E.close()
@@ -392,7 +396,8 @@ def run_fopt_leg(sh, ctx, stream, flush, steps, warmup):
                     f"{nsteps} steps to t {f['t_end']}",
         "timed_steps": steps,
         "fp32_kahan": {"value": cu / (ms32 / 1e3), "ms_per_step": ms32 / steps,
-                       "gw_spectrum_ms": spec32_ms},
+                       "gw_spectrum_ms": spec32_ms,
+                       "gw_spectrum_fp32_transforms_ms": spec32f_ms},
         "fp64_plain": {"value": cu / (ms64 / 1e3), "ms_per_step": ms64 / steps,
                        "gw_spectrum_ms": spec64_ms,
                        "note": f"drop-in level, boxes of {f['max_grid']}^3"},
@@ -405,6 +410,8 @@ def run_fopt_leg(sh, ctx, stream, flush, steps, warmup):
             "time_abs": float(abs(t32 - t64)),
             "gw_binned": spec_err(gw32, gw64),
             "gw_unbinned": spec_err(gu32, gu64),
+            "gw_binned_fp32_transforms": spec_err(gw32f, gw64),
+            "gw_unbinned_fp32_transforms": spec_err(gu32f, gu64),
         },
     }
     return out

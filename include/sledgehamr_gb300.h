@@ -700,6 +700,12 @@ SH_API int sh_ensemble_add_bubbles(sh_ensemble *e, int r, int nb, const double *
 SH_API int sh_ensemble_gw_spectrum(sh_ensemble *e, int r, int zero_padding, int projection_type,
                                    int unbinned, double *bins_out, long long *ks_out,
                                    int max_bins, int *nbins);
+/* Precision of the GW spectrum's transforms and TT projection for this
+ * ensemble: SH_PREC_FP64 (default; the FP64 drop-in's arithmetic) or
+ * SH_PREC_FP32 (FP32 transforms and projection of the FP32 state, FP64
+ * bin sums: the precision form's time-to-spectrum; its error against the
+ * FP64 transform is stated by the benchmark).  No reference counterpart. */
+SH_API int sh_ensemble_set_spectrum_precision(sh_ensemble *e, int precision);
 
 /* ------------------------------------------------------------------------ */
 /* Serving: a request loop over one FP32+Kahan (or FP64) pool of

@@ -796,6 +796,12 @@ class Ensemble:
             self.h, r, xyz.size // 3, _ptr(xyz), _ptr(prof), prof.size // 2, float(inv_dx),
             float(Lcut)), "add_bubbles")
 
+    def set_spectrum_precision(self, precision: int):
+        """PREC_FP64 (default) or PREC_FP32 transforms and TT projection for
+        the GW spectra (FP64 bin sums either way)."""
+        self.check(self.ctx.lib.sh_ensemble_set_spectrum_precision(self.h, precision),
+                   "set_spectrum_precision")
+
     def gw_spectrum(self, r: int, zero_padding: int = 1, projection_type: int = 2,
                     unbinned: bool = True):
         P = self.N[r] * zero_padding

@@ -153,6 +153,7 @@ SIGNATURES = {
                                           C.c_double]),
     "sh_level_add_bubbles": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp,
                                        C.c_int, C.c_double, C.c_double, C.c_double]),
+    "sh_ensemble_set_spectrum_precision": (C.c_int, [vp, C.c_int]),
     "sh_ensemble_gw_spectrum": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp,
                                           C.c_int, ip]),
     "sh_amr_config_defaults": (C.c_int, [C.POINTER(ShAmrConfig)]),

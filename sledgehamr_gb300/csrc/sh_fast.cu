@@ -674,6 +674,21 @@ __global__ void gw_pack_fast_kernel(const R *sa, const R *ca, const R *sb, const
     }
 }
 
+/* The same into complex FP32 arrays (FP32 transforms); v - c in the
+ * storage type, rounded to FP32. */
+template <class R>
+__global__ void gw_pack_fast32_kernel(const R *sa, const R *ca, const R *sb, const R *cb,
+                                      long long off, int N, int P, float2 *dst) {
+    const long long n = (long long)N * N * N;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / ((long long)N * N));
+        const R a = ca ? sa[off + i] - ca[off + i] : sa[off + i];
+        const R b = cb ? sb[off + i] - cb[off + i] : sb[off + i];
+        dst[((long long)z * P + y) * P + x] = make_float2((float)a, (float)b);
+    }
+}
+
 /* Bubbles added to Phi (array phi) and dPhi (array dphi) of realisation r;
  * with compensations the sum is formed from the compensated values and the
  * new compensation holds the rounding of the stored result. */
@@ -765,6 +780,7 @@ struct sh_ensemble {
     sh::GwCache gw;
     void *gw_scratch = nullptr;
     size_t gw_scratch_cap = 0;
+    int spectrum_precision = SH_PREC_FP64; /* of the GW transforms and projection */
     std::string err;
     long long launches = 0;
     /* one CUDA graph of a whole step per buffer parity, for step size graph_dt */
@@ -1580,20 +1596,36 @@ int sh_ensemble_gw_spectrum(sh_ensemble *E, int r, int zero_padding, int project
         const long long n = cells_of(E, r), o = E->desc[r].off;
         int nb = 0;
         std::string err;
-        cudaError_t e = sh::gw_spectrum_packed(
-            E->gw, s, P, N, projection_type, unbinned, scratch, bins_dev, &nb, &E->launches, err,
-            [&](int p, double2 *dst) {
-                const int a = sel[2 * p], b = sel[2 * p + 1];
-                if (E->esize == 8) {
-                    gw_pack_fast_kernel<double><<<fgrid(n), 256, 0, s>>>(
-                        (double *)E->A[a], nullptr, (double *)E->A[b], nullptr, o, N, P, dst);
-                } else {
-                    const bool k = !E->C.empty();
-                    gw_pack_fast_kernel<float><<<fgrid(n), 256, 0, s>>>(
-                        (float *)E->A[a], k ? (float *)E->C[a] : nullptr, (float *)E->A[b],
-                        k ? (float *)E->C[b] : nullptr, o, N, P, dst);
-                }
-            });
+        const bool k = !E->C.empty();
+        cudaError_t e;
+        if (E->spectrum_precision == SH_PREC_FP64)
+            e = sh::gw_spectrum_packed(
+                E->gw, s, P, N, projection_type, unbinned, scratch, bins_dev, &nb, &E->launches,
+                err, [&](int p, double2 *dst) {
+                    const int a = sel[2 * p], b = sel[2 * p + 1];
+                    if (E->esize == 8)
+                        gw_pack_fast_kernel<double><<<fgrid(n), 256, 0, s>>>(
+                            (double *)E->A[a], nullptr, (double *)E->A[b], nullptr, o, N, P,
+                            dst);
+                    else
+                        gw_pack_fast_kernel<float><<<fgrid(n), 256, 0, s>>>(
+                            (float *)E->A[a], k ? (float *)E->C[a] : nullptr, (float *)E->A[b],
+                            k ? (float *)E->C[b] : nullptr, o, N, P, dst);
+                });
+        else
+            e = sh::gw_spectrum_packed32(
+                E->gw, s, P, N, projection_type, unbinned, scratch, bins_dev, &nb, &E->launches,
+                err, [&](int p, float2 *dst) {
+                    const int a = sel[2 * p], b = sel[2 * p + 1];
+                    if (E->esize == 8)
+                        gw_pack_fast32_kernel<double><<<fgrid(n), 256, 0, s>>>(
+                            (double *)E->A[a], nullptr, (double *)E->A[b], nullptr, o, N, P,
+                            dst);
+                    else
+                        gw_pack_fast32_kernel<float><<<fgrid(n), 256, 0, s>>>(
+                            (float *)E->A[a], k ? (float *)E->C[a] : nullptr, (float *)E->A[b],
+                            k ? (float *)E->C[b] : nullptr, o, N, P, dst);
+                });
         if (!err.empty()) throw FastErr(SH_ERR_CUDA, err);
         fck(e, "gw spectrum");
         *nbins = nb;
@@ -1603,6 +1635,12 @@ int sh_ensemble_gw_spectrum(sh_ensemble *E, int r, int zero_padding, int project
         fck(cudaStreamSynchronize(s), "gw spectrum");
         if (ks_out) std::copy(E->gw.ks().begin(), E->gw.ks().end(), ks_out);
     });
+}
+
+int sh_ensemble_set_spectrum_precision(sh_ensemble *E, int precision) {
+    if (!E || (precision != SH_PREC_FP64 && precision != SH_PREC_FP32)) return SH_ERR_ARG;
+    E->spectrum_precision = precision;
+    return SH_OK;
 }
 
 int sh_ensemble_add_bubbles(sh_ensemble *E, int r, int nb, const double *xyz,

@@ -124,14 +124,20 @@ __global__ void gw_pack_kernel(const BoxDev *boxes, const long long *vbase, int 
  * about 100 FP64 operations per cell instead of the ~170 of P U P.  W is
  * the projected tensor itself, so |W|^2 carries rounding of the order of
  * eps |U| |W| (not eps |U|^2), as the explicit form does. */
-__device__ __forceinline__ void split_pair(double2 z, double2 m, double2 &u, double2 &v) {
-    u = make_double2(z.x + m.x, z.y - m.y);
-    v = make_double2(z.y + m.y, m.x - z.x);
+template <class C>
+__device__ __forceinline__ void split_pair(C z, C m, C &u, C &v) {
+    u.x = z.x + m.x;
+    u.y = z.y - m.y;
+    v.x = z.y + m.y;
+    v.y = m.x - z.x;
 }
 
-__global__ void gw_project_kernel(const double2 *__restrict__ Z0, const double2 *__restrict__ Z1,
-                                  const double2 *__restrict__ Z2,
-                                  const double *__restrict__ index_to_k, int P, double *out) {
+/* C, R: double2, double for FP64 transforms; float2, float for FP32 ones
+ * (the per-cell value is widened to FP64 for the bin sums). */
+template <class C, class R>
+__global__ void gw_project_kernel(const C *__restrict__ Z0, const C *__restrict__ Z1,
+                                  const C *__restrict__ Z2, const R *__restrict__ index_to_k,
+                                  int P, double *out) {
     const int H = P / 2 + 1;
     const long long n = (long long)H * P * P;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
@@ -147,45 +153,45 @@ __global__ void gw_project_kernel(const double2 *__restrict__ Z0, const double2 
         const long long g =
             ((long long)(c ? P - c : 0) * P + (b ? P - b : 0)) * P + (a ? P - a : 0);
         /* twice the transforms of the slots xx xy xz yy yz zz */
-        double2 s6[6];
+        C s6[6];
         split_pair(Z0[f], Z0[g], s6[0], s6[1]);
         split_pair(Z1[f], Z1[g], s6[2], s6[3]);
         split_pair(Z2[f], Z2[g], s6[4], s6[5]);
-        const double k[3] = {index_to_k[a], index_to_k[b], index_to_k[c]};
-        const double inv = 1. / (k[0] * k[0] + k[1] * k[1] + k[2] * k[2]);
+        const R k[3] = {index_to_k[a], index_to_k[b], index_to_k[c]};
+        const R inv = (R)1 / (k[0] * k[0] + k[1] * k[1] + k[2] * k[2]);
         const int slot[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
-        double2 v[3];
+        C v[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             v[i].x = s6[slot[i][0]].x * k[0] + s6[slot[i][1]].x * k[1] + s6[slot[i][2]].x * k[2];
             v[i].y = s6[slot[i][0]].y * k[0] + s6[slot[i][1]].y * k[1] + s6[slot[i][2]].y * k[2];
         }
-        const double sx = k[0] * v[0].x + k[1] * v[1].x + k[2] * v[2].x;
-        const double sy = k[0] * v[0].y + k[1] * v[1].y + k[2] * v[2].y;
-        const double h = 0.5 * inv * inv;
-        double2 w[3];
+        const R sx = k[0] * v[0].x + k[1] * v[1].x + k[2] * v[2].x;
+        const R sy = k[0] * v[0].y + k[1] * v[1].y + k[2] * v[2].y;
+        const R h = (R)0.5 * inv * inv;
+        C w[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             w[i].x = inv * v[i].x - h * sx * k[i];
             w[i].y = inv * v[i].y - h * sy * k[i];
         }
-        double first = 0., tr_re = 0., tr_im = 0.;
+        R first = 0, tr_re = 0, tr_im = 0;
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int j = i; j < 3; ++j) {
-                const double2 u = s6[slot[i][j]];
-                const double re = u.x - (k[i] * w[j].x + w[i].x * k[j]);
-                const double im = u.y - (k[i] * w[j].y + w[i].y * k[j]);
-                const double wt = i == j ? 1. : 2.;
+                const C u = s6[slot[i][j]];
+                const R re = u.x - (k[i] * w[j].x + w[i].x * k[j]);
+                const R im = u.y - (k[i] * w[j].y + w[i].y * k[j]);
+                const R wt = i == j ? (R)1 : (R)2;
                 first += wt * (re * re + im * im);
                 if (i == j) {
                     tr_re += re;
                     tr_im += im;
                 }
             }
-        const double multpl = (a == 0 || a == P / 2) ? 1. : 2.;
-        out[e] = multpl * (first - 0.5 * (tr_re * tr_re + tr_im * tr_im));
+        const R multpl = (a == 0 || a == P / 2) ? (R)1 : (R)2;
+        out[e] = (double)(multpl * (first - (R)0.5 * (tr_re * tr_re + tr_im * tr_im)));
     }
 }
 
@@ -257,6 +263,7 @@ void GwCache::prepare(int P, int unbinned, int projection_type) {
         cudaFree(bins[lru].d_off);
         cudaFree(bins[lru].d_cells);
         cudaFree(bins[lru].d_itk);
+        cudaFree(bins[lru].d_itk32);
         bins.erase(bins.begin() + lru);
     }
     GwBins g;
@@ -324,18 +331,22 @@ void GwCache::prepare(int P, int unbinned, int projection_type) {
         for (long long e = t * chunk; e < e1; ++e) cells[(size_t)pos[bin_of(e)]++] = (int)e;
     }
     std::vector<double> itk = index_to_k_host(P, projection_type);
+    std::vector<float> itk32(itk.begin(), itk.end());
     if (cudaMalloc(&g.d_off, off.size() * sizeof(long long)) != cudaSuccess ||
         cudaMalloc(&g.d_cells, cells.size() * sizeof(int)) != cudaSuccess ||
-        cudaMalloc(&g.d_itk, itk.size() * sizeof(double)) != cudaSuccess) {
+        cudaMalloc(&g.d_itk, itk.size() * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&g.d_itk32, itk32.size() * sizeof(float)) != cudaSuccess) {
         cudaGetLastError();
         cudaFree(g.d_off);
         cudaFree(g.d_cells);
         cudaFree(g.d_itk);
+        cudaFree(g.d_itk32);
         throw std::bad_alloc();
     }
     cudaMemcpy(g.d_off, off.data(), off.size() * sizeof(long long), cudaMemcpyHostToDevice);
     cudaMemcpy(g.d_cells, cells.data(), cells.size() * sizeof(int), cudaMemcpyHostToDevice);
     cudaMemcpy(g.d_itk, itk.data(), itk.size() * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(g.d_itk32, itk32.data(), itk32.size() * sizeof(float), cudaMemcpyHostToDevice);
     bins.push_back(std::move(g));
     cur = &bins.back();
 }
@@ -366,8 +377,8 @@ bool GwCache::plan(int P, int kind, cufftHandle *out) {
     const cufftResult r =
         kind == kPlanD2Z
             ? cufftMakePlanMany64(p.h, 3, n, nullptr, 1, 0, nullptr, 1, 0, CUFFT_D2Z, 1, &work)
-            : cufftMakePlanMany64(p.h, 3, n, nullptr, 1, dist, nullptr, 1, dist, CUFFT_Z2Z, 3,
-                                  &work);
+            : cufftMakePlanMany64(p.h, 3, n, nullptr, 1, dist, nullptr, 1, dist,
+                                  kind == kPlanZ2Z3 ? CUFFT_Z2Z : CUFFT_C2C, 3, &work);
     if (r != CUFFT_SUCCESS) {
         cufftDestroy(p.h);
         return false;
@@ -382,6 +393,7 @@ void GwCache::release() {
         cudaFree(b.d_off);
         cudaFree(b.d_cells);
         cudaFree(b.d_itk);
+        cudaFree(b.d_itk32);
     }
     bins.clear();
     for (Plan &p : plans) cufftDestroy(p.h);
@@ -419,11 +431,50 @@ cudaError_t gw_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, int N
         return cudaErrorUnknown;
     }
     int g = (int)std::min<long long>((nhalf + 255) / 256, 152LL * 32);
-    gw_project_kernel<<<std::max(g, 1), 256, 0, stream>>>(Z, Z + nfull, Z + 2 * nfull,
-                                                          cache.cur->d_itk, P, vals);
+    gw_project_kernel<double2, double><<<std::max(g, 1), 256, 0, stream>>>(
+        Z, Z + nfull, Z + 2 * nfull, cache.cur->d_itk, P, vals);
     (*launches)++;
     const int nb = (int)cache.ks().size();
     /* 1/P^6, and 1/4 for the pairs' factor 2 (exact) */
+    const double scale = 0.25 / std::pow((double)P, 6);
+    launch_bins(vals, *cache.cur, scale, bins_dev, stream);
+    (*launches)++;
+    *nbins = nb;
+    return cudaGetLastError();
+}
+
+cudaError_t gw_spectrum_packed32(GwCache &cache, cudaStream_t stream, int P, int N,
+                                 int projection_type, int unbinned, double *scratch,
+                                 double *bins_dev, int *nbins, long long *launches,
+                                 std::string &err,
+                                 const std::function<void(int, float2 *)> &pack) {
+    cache.prepare(P, unbinned, projection_type);
+    const int H = P / 2 + 1;
+    const long long nfull = (long long)P * P * P;
+    const long long nhalf = (long long)H * P * P;
+    cufftHandle plan;
+    if (!cache.plan(P, GwCache::kPlanC2C3, &plan)) {
+        err = "cuFFT plan of three P^3 FP32 complex transforms failed";
+        return cudaErrorUnknown;
+    }
+    cufftSetStream(plan, stream);
+    /* scratch: three complex FP32 P^3 arrays (component pairs) | per-cell values */
+    float2 *Z = (float2 *)scratch;
+    double *vals = (double *)(Z + 3 * nfull);
+    if (P != N) cudaMemsetAsync(Z, 0, 3 * nfull * sizeof(float2), stream);
+    for (int p = 0; p < 3; ++p) {
+        pack(p, Z + p * nfull);
+        (*launches)++;
+    }
+    if (cufftExecC2C(plan, (cufftComplex *)Z, (cufftComplex *)Z, CUFFT_FORWARD) != CUFFT_SUCCESS) {
+        err = "cufftExecC2C failed";
+        return cudaErrorUnknown;
+    }
+    int g = (int)std::min<long long>((nhalf + 255) / 256, 152LL * 32);
+    gw_project_kernel<float2, float><<<std::max(g, 1), 256, 0, stream>>>(
+        Z, Z + nfull, Z + 2 * nfull, cache.cur->d_itk32, P, vals);
+    (*launches)++;
+    const int nb = (int)cache.ks().size();
     const double scale = 0.25 / std::pow((double)P, 6);
     launch_bins(vals, *cache.cur, scale, bins_dev, stream);
     (*launches)++;

@@ -20,6 +20,7 @@ struct GwBins {
     long long *d_off = nullptr; /* nbins + 1 */
     int *d_cells = nullptr;     /* cells sorted by bin, ascending within a bin */
     double *d_itk = nullptr;    /* index_to_k[P] */
+    float *d_itk32 = nullptr;   /* the same in FP32 (FP32 transforms) */
     long long used = 0;         /* last use (for eviction) */
 };
 
@@ -31,8 +32,9 @@ struct GwBins {
 struct GwCache {
     static constexpr int kMaxBins = 4, kMaxPlans = 3;
     /* plan kinds: one real-to-complex P^3 transform (scalar spectra), three
-     * in-place complex P^3 transforms (the GW components in pairs) */
-    static constexpr int kPlanD2Z = 0, kPlanZ2Z3 = 1;
+     * in-place complex P^3 transforms (the GW components in pairs), in FP64
+     * or in FP32 */
+    static constexpr int kPlanD2Z = 0, kPlanZ2Z3 = 1, kPlanC2C3 = 2;
     std::vector<GwBins> bins;
     struct Plan {
         int P = 0, kind = 0;
@@ -71,6 +73,14 @@ cudaError_t gw_spectrum_packed(GwCache &cache, cudaStream_t stream, int P, int N
                                double *bins_dev, int *nbins, long long *launches,
                                std::string &err,
                                const std::function<void(int, double2 *)> &pack);
+/* gw_spectrum_packed with FP32 transforms and an FP32 projection (the
+ * precision form's spectra: FP32 state, FP64 bin sums): `pack(p, dst)`
+ * writes the pairs into complex FP32 arrays. */
+cudaError_t gw_spectrum_packed32(GwCache &cache, cudaStream_t stream, int P, int N,
+                                 int projection_type, int unbinned, double *scratch,
+                                 double *bins_dev, int *nbins, long long *launches,
+                                 std::string &err,
+                                 const std::function<void(int, float2 *)> &pack);
 cudaError_t gw_spectrum_device(GwCache &cache, cudaStream_t stream, const BoxDev *boxes,
                                const long long *vbase, int nbox, long long nvalid, int ncomp,
                                const double *buf, const int comps[6], int N, const int dlo[3],

@@ -276,3 +276,26 @@ def test_ensemble_bubbles_vs_golden(ctx):
             ref = oracle_add_bubbles(s32, g["xyz"], g["profile"], float(g["inv_dx"]),
                                      float(g["Lcut"]), dx)
             assert np.max(np.abs(out - ref)) <= 1e-14 * np.abs(ref).max()
+
+
+def test_fp32_spectrum_transforms_against_fp64_transforms(ctx):
+    """GW spectra of an FP32 + Kahan ensemble with FP32 transforms and TT
+    projection (sh_ensemble_set_spectrum_precision) against the FP64 ones of
+    the same state: total power within 1e-5, bins holding more than 1e-6 of
+    the largest within 1e-3 (FP32 rounding of the transforms, relative to
+    the field's norm)."""
+    N = 64
+    st = fopt_state(N, 16.0, 9)
+    with sh.Ensemble(ctx, sh.FAMILY_FOPT_GW, sh.PREC_FP32_KAHAN, [N], [0.25],
+                     [-0.2, 0.5, -0.6, 0]) as E:
+        E.write(0, st)
+        E.step(0.05, 4)
+        for unbinned in (False, True):
+            a, ka = E.gw_spectrum(0, unbinned=unbinned)
+            E.set_spectrum_precision(sh.PREC_FP32)
+            b, kb = E.gw_spectrum(0, unbinned=unbinned)
+            E.set_spectrum_precision(sh.PREC_FP64)
+            assert np.array_equal(ka, kb)
+            assert abs(b.sum() - a.sum()) / a.sum() <= 1e-5
+            sig = a > 1e-6 * a.max()
+            assert np.max(np.abs(b - a)[sig] / a[sig]) <= 1e-3
