@@ -157,8 +157,19 @@ __global__ void gw_project_kernel(const C *__restrict__ Z0, const C *__restrict_
         split_pair(Z0[f], Z0[g], s6[0], s6[1]);
         split_pair(Z1[f], Z1[g], s6[2], s6[3]);
         split_pair(Z2[f], Z2[g], s6[4], s6[5]);
-        const R k[3] = {index_to_k[a], index_to_k[b], index_to_k[c]};
-        const R inv = (R)1 / (k[0] * k[0] + k[1] * k[1] + k[2] * k[2]);
+        R k[3] = {index_to_k[a], index_to_k[b], index_to_k[c]};
+        R inv;
+        if constexpr (sizeof(R) == 4) {
+            /* FP32: the unit vector k / |k| (near the Nyquist planes |k| is
+             * ~1e-16, and 1 / |k|^4 would overflow) */
+            const R rn = rsqrtf(k[0] * k[0] + k[1] * k[1] + k[2] * k[2]);
+            k[0] *= rn;
+            k[1] *= rn;
+            k[2] *= rn;
+            inv = (R)1;
+        } else {
+            inv = (R)1 / (k[0] * k[0] + k[1] * k[1] + k[2] * k[2]);
+        }
         const int slot[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
         C v[3];
 #pragma unroll
