@@ -239,3 +239,27 @@ def test_fp32_fopt_bubbles_and_hierarchy_against_fp64_oracle(ctx):
     assert g.info()["finest"] >= 1
     g.close()
     o.close()
+
+
+def test_fp32_hierarchy_local_regrids_against_fp64_oracle(ctx):
+    """Local regrids on an FP32 hierarchy (blocks added next to coarse/fine
+    boundaries, both time levels of the new boxes interpolated) take the FP64
+    oracle's decisions: the same boxes after every coarse step, fields
+    within 2e-6."""
+    kw = dict(record_regrids=0, regrid_dt=0.125, max_local_regrids=10)
+    g = sh.Amr(ctx, config(precision=F32, **kw), level0(1))
+    o = OracleAmr(config(**kw), level0(1))
+    g.set_trace(True)
+    o.set_trace(True)
+    for step in range(10):
+        g.step(1)
+        o.step(1)
+        assert g.info()["finest"] == o.info()["finest"], step
+        for lev in range(g.info()["finest"] + 1):
+            assert g.level(lev).boxes == o.boxes(lev), (step, lev)
+            e = rel_l2(g.level(lev).read(), o.read(lev)[0])
+            assert e <= 2e-6, (step, lev, e)
+    assert g.trace() == o.trace()
+    assert len(g.level(2).boxes) == 66  # level 2 grew by a block, as in the FP64 test
+    g.close()
+    o.close()
