@@ -52,8 +52,15 @@ struct Stage32Args {
     float friction, eta2; /* -2/eta and eta^2 at the stage time */
 };
 
+/* Each thread walks its z-column keeping the 2 ORDER + 1 values of the two
+ * position components along z in registers (one new plane value per step
+ * instead of 2 ORDER + 1 loads), with restrict-qualified pointers (every
+ * buffer of a stage is distinct) so that the next plane's loads can be
+ * issued ahead of the current plane's stores.  The sums are formed in the
+ * order of the ensemble kernels (x+, x-, y+, y-, z+, z-). */
 template <int ORDER, int STAGE>
 __global__ void __launch_bounds__(kThreads) stage32_axion_kernel(const __grid_constant__ Stage32Args a) {
+    constexpr int R = ORDER; /* stencil reach */
     const TileDev t = a.tiles[blockIdx.x];
     const BoxDev b = a.boxes[t.box];
     const int tid = threadIdx.x + kTileX * threadIdx.y;
@@ -63,26 +70,43 @@ __global__ void __launch_bounds__(kThreads) stage32_axion_kernel(const __grid_co
     if (ty >= kThreads / t.nx || i > b.hi[0] || j > b.hi[1]) return;
     const int kend = min(t.z0 + t.nz - 1, b.hi[2]);
     const long long gx = b.gdim[0], gxy = gx * b.gdim[1], gvol = b.gvol;
+    const float *__restrict__ st = a.state;
+    const float *__restrict__ y0 = a.y0;
+    const float *__restrict__ k0 = a.k0;
+    const float *__restrict__ k1 = a.k1;
+    const float *__restrict__ c_old = a.c_old;
+    float *__restrict__ out = a.out;
+    float *__restrict__ kout = a.kout;
+    float *__restrict__ c_new = a.c_new;
+    const long long col =
+        b.off * 4 + (i - b.glo[0]) + (long long)(j - b.glo[1]) * gx; /* component 0, z = glo */
+    const long long kcol = b.off * 2 + (i - b.glo[0]) + (long long)(j - b.glo[1]) * gx;
+    /* z-window of the two positions: w[c][d] = value at plane k - R + d */
+    float w[2][2 * R + 1];
+#pragma unroll
+    for (int c = 0; c < 2; ++c)
+#pragma unroll
+        for (int d = 0; d < 2 * R; ++d)
+            w[c][d] = st[col + c * gvol + (long long)(t.z0 - R + d - b.glo[2]) * gxy];
     for (int k = t.z0; k <= kend; ++k) {
-        const long long lc =
-            (i - b.glo[0]) + (long long)(j - b.glo[1]) * gx + (long long)(k - b.glo[2]) * gxy;
-        const long long sb = b.off * 4 + lc; /* component 0 of the cell */
-        const long long kb = b.off * 2 + lc; /* K component 0 of the cell */
+        const long long lz = (long long)(k - b.glo[2]) * gxy;
+        const long long sb = col + lz;  /* component 0 of the cell */
+        const long long kb = kcol + lz; /* K component 0 of the cell */
         float lap[2];
 #pragma unroll
         for (int c = 0; c < 2; ++c) {
-            const float *s = a.state + sb + c * gvol;
+            const float *s = st + sb + c * gvol;
+            w[c][2 * R] = s[R * gxy];
             if constexpr (ORDER == 1) {
-                lap[c] = f32::lap7(s[0], s[1], s[-1], s[gx], s[-gx], s[gxy], s[-gxy], a.inv);
+                lap[c] = f32::lap7(w[c][1], s[1], s[-1], s[gx], s[-gx], w[c][2], w[c][0], a.inv);
             } else {
-                const float s1 = f32::ring(s[1], s[-1], s[gx], s[-gx], s[gxy], s[-gxy]);
-                const float s2 =
-                    f32::ring(s[2], s[-2], s[2 * gx], s[-2 * gx], s[2 * gxy], s[-2 * gxy]);
-                lap[c] = f32::lap13(s[0], s1, s2, a.inv);
+                const float s1 = f32::ring(s[1], s[-1], s[gx], s[-gx], w[c][3], w[c][1]);
+                const float s2 = f32::ring(s[2], s[-2], s[2 * gx], s[-2 * gx], w[c][4], w[c][0]);
+                lap[c] = f32::lap13(w[c][2], s1, s2, a.inv);
             }
         }
-        const float p0 = a.state[sb], p1 = a.state[sb + gvol];
-        const float q0 = a.y0[sb + 2 * gvol], q1 = a.y0[sb + 3 * gvol];
+        const float p0 = w[0][R], p1 = w[1][R];
+        const float q0 = y0[sb + 2 * gvol], q1 = y0[sb + 3 * gvol];
         const float v = f32::potential(p0, p1, a.lam, a.eta2, a.cst);
         const float kq[2] = {f32::accel(q0, lap[0], p0, v, a.friction),
                              f32::accel(q1, lap[1], p1, v, a.friction)};
@@ -90,24 +114,28 @@ __global__ void __launch_bounds__(kThreads) stage32_axion_kernel(const __grid_co
         if constexpr (STAGE < 2) {
 #pragma unroll
             for (int c = 0; c < 2; ++c) {
-                a.kout[kb + c * gvol] = kq[c];
-                const float y = a.y0[sb + c * gvol];
-                a.out[sb + c * gvol] = f32::stage_pos(y, q[c], kq[c], a.cm, a.ck);
+                kout[kb + c * gvol] = kq[c];
+                const float y = y0[sb + c * gvol];
+                out[sb + c * gvol] = f32::stage_pos(y, q[c], kq[c], a.cm, a.ck);
             }
         } else {
 #pragma unroll
             for (int c = 0; c < 2; ++c) {
-                const float ka = a.k0[kb + c * gvol], kbv = a.k1[kb + c * gvol];
-                float y = a.y0[sb + c * gvol], cy = a.c_old[sb + c * gvol];
-                float m = q[c], cmo = a.c_old[sb + (2 + c) * gvol];
+                const float ka = k0[kb + c * gvol], kbv = k1[kb + c * gvol];
+                float y = y0[sb + c * gvol], cy = c_old[sb + c * gvol];
+                float m = q[c], cmo = c_old[sb + (2 + c) * gvol];
                 f32::kahan(y, f32::dpos(q[c], ka, kbv, a.h, a.h2), cy);
                 f32::kahan(m, f32::dmom(ka, kbv, kq[c], a.h), cmo);
-                a.out[sb + c * gvol] = y;
-                a.out[sb + (2 + c) * gvol] = m;
-                a.c_new[sb + c * gvol] = cy;
-                a.c_new[sb + (2 + c) * gvol] = cmo;
+                out[sb + c * gvol] = y;
+                out[sb + (2 + c) * gvol] = m;
+                c_new[sb + c * gvol] = cy;
+                c_new[sb + (2 + c) * gvol] = cmo;
             }
         }
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+#pragma unroll
+            for (int d = 0; d < 2 * R; ++d) w[c][d] = w[c][d + 1];
     }
 }
 
