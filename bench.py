@@ -858,7 +858,7 @@ def timed_steps(step, steps, warmup, stream, flush, clk=None, before=None):
 
 
 # FP64 thread instructions (DFMA + DMUL + DADD) per cell-update of the stage
-# kernels (ncu SASS instruction counters of the three launches of one RKN4
+# kernels (ncu executed-instruction counters of the three launches of one RKN4
 # step divided by the cells): the 7-point kernel of the 128^3 level
 # (`--case single`) and the 13-point kernel of the AMR workload (level 0 of
 # `--case amr`; the per-cell count does not depend on the level).
