@@ -155,10 +155,57 @@ struct RegridRecord {
 struct BlockSet {
     const std::vector<uint8_t> &bits;
     int nb;
+    /* optional integral volume of bits, (nb+1)^3 entries: sum[(z m + y) m +
+     * x] = set blocks in [0, x) x [0, y) x [0, z), m = nb + 1 */
+    const std::vector<int> *sum = nullptr;
     bool at(int x, int y, int z) const {
         return bits[((size_t)z * nb + y) * nb + x] != 0;
     }
+    /* set blocks in [x0, x1] x [y0, y1] x [z0, z1] (needs sum) */
+    long long box_sum(int x0, int x1, int y0, int y1, int z0, int z1) const {
+        const size_t m = (size_t)nb + 1;
+        auto S = [&](int x, int y, int z) { return (long long)(*sum)[((size_t)z * m + y) * m + x]; };
+        ++x1;
+        ++y1;
+        ++z1;
+        return S(x1, y1, z1) - S(x0, y1, z1) - S(x1, y0, z1) - S(x1, y1, z0) + S(x0, y0, z1) +
+               S(x0, y1, z0) + S(x1, y0, z0) - S(x0, y0, z0);
+    }
 };
+
+/* The integral volume of an nb^3 block set (prefix sums along x, y, z),
+ * built on `threads` host threads. */
+inline std::vector<int> integral_volume(const std::vector<uint8_t> &bits, int nb, int threads) {
+    const size_t m = (size_t)nb + 1;
+    std::vector<int> s(m * m * m, 0);
+    (void)threads;
+#pragma omp parallel for schedule(static) num_threads(threads)
+    for (int z = 0; z < nb; ++z)
+        for (int y = 0; y < nb; ++y) {
+            const uint8_t *p = &bits[((size_t)z * nb + y) * nb];
+            int *q = &s[((size_t)(z + 1) * m + (y + 1)) * m + 1];
+            int run = 0;
+            for (int x = 0; x < nb; ++x) {
+                run += p[x] != 0;
+                q[x] = run;
+            }
+        }
+#pragma omp parallel for schedule(static) num_threads(threads)
+    for (int z = 1; z <= nb; ++z)
+        for (int y = 2; y <= nb; ++y) {
+            int *q = &s[((size_t)z * m + y) * m];
+            const int *r = q - m;
+            for (size_t x = 1; x < m; ++x) q[x] += r[x];
+        }
+#pragma omp parallel for schedule(static) num_threads(threads)
+    for (int y = 1; y <= nb; ++y)
+        for (int z = 2; z <= nb; ++z) {
+            int *q = &s[((size_t)z * m + y) * m];
+            const int *r = q - m * m;
+            for (size_t x = 1; x < m; ++x) q[x] += r[x];
+        }
+    return s;
+}
 
 /* Cut of a signature h[0..n-1] (both ends non-zero): position p in
  * [1, n-1] splitting [0, p) | [p, n); kind 2 hole, 1 inflection, 0 none. */
@@ -208,7 +255,17 @@ inline void cluster_impl(const BlockSet &t, IBox bx, double eff, std::vector<IBo
     std::vector<long long> sig[3];
     for (int d = 0; d < 3; ++d) sig[d].assign(bx.hi[d] - bx.lo[d] + 1, 0);
     long long ntag = 0;
-    {
+    if (t.sum) {
+        /* from the integral volume: O(side) instead of O(volume) */
+        const int *lo = bx.lo, *hi = bx.hi;
+        for (int x = lo[0]; x <= hi[0]; ++x)
+            sig[0][x - lo[0]] = t.box_sum(x, x, lo[1], hi[1], lo[2], hi[2]);
+        for (int y = lo[1]; y <= hi[1]; ++y)
+            sig[1][y - lo[1]] = t.box_sum(lo[0], hi[0], y, y, lo[2], hi[2]);
+        for (int z = lo[2]; z <= hi[2]; ++z)
+            sig[2][z - lo[2]] = t.box_sum(lo[0], hi[0], lo[1], hi[1], z, z);
+        for (long long v : sig[0]) ntag += v;
+    } else {
         /* row by row without branches: x counts per element, y and z
          * counts per row sum */
         const int nx = bx.hi[0] - bx.lo[0] + 1;
@@ -358,13 +415,21 @@ inline void radix_sort_keyed(std::vector<std::pair<unsigned long long, unsigned>
  * lo[d]) and neighbours in that order merged, until no direction merges
  * anything.  The boxes are disjoint, so that key is unique and any sort
  * gives the same order; with coordinates in [0, 4096) it is packed into one
- * 64-bit integer and radix-sorted.  A direction is skipped while the boxes
+ * 64-bit integer (as many bits per coordinate as the largest needs) and
+ * radix-sorted.  A direction is skipped while the boxes
  * have not changed since it last merged nothing (it would merge nothing
  * again), so the merges, and the result, are those of full passes. */
 inline void simplify(std::vector<IBox> &v) {
     bool small = true;
+    int maxc = 0;
     for (const IBox &x : v)
-        for (int d = 0; d < 3; ++d) small = small && x.lo[d] >= 0 && x.hi[d] < 4096;
+        for (int d = 0; d < 3; ++d) {
+            small = small && x.lo[d] >= 0 && x.hi[d] < 4096;
+            maxc = std::max(maxc, x.hi[d]);
+        }
+    /* bits per packed coordinate: as many as the largest one needs */
+    int cb = 1;
+    while (cb < 12 && (maxc >> cb) != 0) ++cb;
     std::vector<std::pair<unsigned long long, unsigned>> keyed, tmp;
     std::vector<IBox> sorted;
     int clean = 0; /* directions in a row known to merge nothing */
@@ -374,14 +439,14 @@ inline void simplify(std::vector<IBox> &v) {
             keyed.resize(v.size());
             for (size_t q = 0; q < v.size(); ++q) {
                 const IBox &a = v[q];
-                keyed[q].first = ((unsigned long long)a.lo[e] << 48) |
-                                 ((unsigned long long)a.hi[e] << 36) |
-                                 ((unsigned long long)a.lo[f] << 24) |
-                                 ((unsigned long long)a.hi[f] << 12) |
+                keyed[q].first = ((unsigned long long)a.lo[e] << (4 * cb)) |
+                                 ((unsigned long long)a.hi[e] << (3 * cb)) |
+                                 ((unsigned long long)a.lo[f] << (2 * cb)) |
+                                 ((unsigned long long)a.hi[f] << cb) |
                                  (unsigned long long)a.lo[d];
                 keyed[q].second = (unsigned)q;
             }
-            radix_sort_keyed(keyed, tmp, 60);
+            radix_sort_keyed(keyed, tmp, 5 * cb);
             sorted.resize(v.size());
             for (size_t q = 0; q < v.size(); ++q) sorted[q] = v[keyed[q].second];
             v.swap(sorted);
@@ -540,8 +605,15 @@ inline std::vector<IBox> make_boxes(const std::vector<uint8_t> &tagbits,
         order(bb);
         return bb;
     }
+    /* signatures from an integral volume where it fits in 64 MiB */
+    std::vector<int> sum;
+    BlockSet tagsum{tagbits, nb};
+    if ((long long)(nb + 1) * (nb + 1) * (nb + 1) * sizeof(int) <= (64LL << 20)) {
+        sum = integral_volume(tagbits, nb, nthreads);
+        tagsum.sum = &sum;
+    }
     std::vector<IBox> cl;
-    cluster_parallel(tags, IBox{{0, 0, 0}, {nb - 1, nb - 1, nb - 1}}, grid_eff, cl, nthreads);
+    cluster_parallel(tagsum, IBox{{0, 0, 0}, {nb - 1, nb - 1, nb - 1}}, grid_eff, cl, nthreads);
     nested(cl, bb);
     simplify(bb);
     max_size(bb, w);
