@@ -70,8 +70,9 @@ WORDS_PER_CELL_UPDATE = 40
 # bytes read + written of the three launches of one RKN4 step), scaled to a
 # launch of the benchmark by the cells it updates.  AMR: level 1 of the AMR
 # run at N0 = 128 (5.55 GB for 12,729,344 cells); 128^3 level: the three
-# launches of one step of `--case single` (602.3 MB for 2,097,152 cells).
-TRAFFIC_B_PER_CELL_UPDATE = {"amr": 436.0, "single": 287.2}
+# launches of one step of `--case single`, ghost images written by the stage
+# kernel (599.7 MB for 2,097,152 cells).
+TRAFFIC_B_PER_CELL_UPDATE = {"amr": 436.0, "single": 286.0}
 
 SINGLE = dict(N=128, L=32.0, project="AxionStringsLap1", params=[1.0, 0.0], nghost=1,
               eta0=0.1, total_steps=200, seed=0)

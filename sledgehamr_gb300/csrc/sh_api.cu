@@ -164,6 +164,10 @@ struct sh_level {
      * FP64 path is untouched */
     double *buf[3] = {nullptr, nullptr, nullptr};
     int esize = 8; /* 8: FP64 storage; 4: FP32 values with FP32 Kahan compensations */
+    /* one box covering the periodic domain (FP64): the stage kernels without
+     * Kreiss-Oliger dissipation write the periodic images of their outputs
+     * into the ghost cells themselves */
+    bool self_periodic = false;
     /* FP32 levels: compensations of SH_NEW / SH_OLD (the value v and its
      * compensation c stand for v - c), the truncation errors in FP64 for the
      * tag comparison (an FP64 level keeps them in its SH_OLD buffer, as the
@@ -1450,6 +1454,9 @@ void fill_common(StageArgs &a, const sh_level *L, double dt, double dx, const do
     std::memset(&a, 0, sizeof(a));
     a.dt = dt;
     a.dx = dx;
+    a.self_periodic = (L->self_periodic && ko_order == 0) ? 1 : 0;
+    a.ng = L->nghost;
+    for (int d = 0; d < 3; ++d) a.per[d] = L->dhi[d] - L->dlo[d] + 1;
     for (int q = 0; q < nparams; ++q) a.params[q] = params[q];
     for (int q = 0; q < ngw; ++q) a.gw_params[q] = gw_params[q];
     if (ko_order)
@@ -1492,6 +1499,14 @@ Tableau rkn_tableau(int type, const double *flat, int s) {
 
 /* Integrate old -> new with the fused stage kernels.  Buffers: 0 = new,
  * 1 = old, 2 = alt; stage states alternate between new and alt. */
+/* The ghost cells of a stage's output buffer for time t: where the stage
+ * kernel wrote them itself (periodic images, a.self_periodic), only the fill
+ * is recorded; otherwise FillIntermediatePatch. */
+void after_stage(sh_ctx *ctx, sh_level *L, const StageArgs &a, double *buf, double t) {
+    if (a.self_periodic) note_fill(L, buf, t);
+    else fill_patch(ctx, L, buf, t);
+}
+
 void integrate(sh_ctx *ctx, sh_level *L, int type, const double *tableau, int nstages,
                double dt, double dx, const double *params, int nparams, const double *gw_params,
                int ngw, int ko_order, const double *ko_strength) {
@@ -1546,7 +1561,7 @@ void integrate(sh_ctx *ctx, sh_level *L, int type, const double *tableau, int ns
                 if (tb.bbar[S - 1] == 0.) s.epi = kEpiRknFinalNoKqPos;
             }
             launch_stage(ctx, L, s, ko_order);
-            fill_patch(ctx, L, L->buf[next], i < S - 1 ? t0 + dt * tb.nodes[i + 1] : t0 + dt);
+            after_stage(ctx, L, a, L->buf[next], i < S - 1 ? t0 + dt * tb.nodes[i + 1] : t0 + dt);
             cur = next;
         }
         if (cur != SH_NEW) std::swap(L->buf[SH_NEW], L->buf[2]);
@@ -1561,7 +1576,7 @@ void integrate(sh_ctx *ctx, sh_level *L, int type, const double *tableau, int ns
         s.c_out = dt;
         s.out = L->buf[SH_NEW];
         launch_stage(ctx, L, s, ko_order);
-        fill_patch(ctx, L, L->buf[SH_NEW], t0 + dt);
+        after_stage(ctx, L, a, L->buf[SH_NEW], t0 + dt);
         /* k1 = f(u1) + k1; u2 = y0 + dt/4 k1 */
         s.state = L->buf[SH_NEW];
         s.time = t0 + dt;
@@ -1573,7 +1588,7 @@ void integrate(sh_ctx *ctx, sh_level *L, int type, const double *tableau, int ns
         s.c_out = dt / 4.;
         s.out = L->buf[2];
         launch_stage(ctx, L, s, ko_order);
-        fill_patch(ctx, L, L->buf[2], t0 + dt / 2.);
+        after_stage(ctx, L, a, L->buf[2], t0 + dt / 2.);
         /* k1 = f(u2) + k1/4; y1 = y0 + 2dt/3 k1 */
         s.state = L->buf[2];
         s.time = t0 + dt / 2.;
@@ -1582,7 +1597,7 @@ void integrate(sh_ctx *ctx, sh_level *L, int type, const double *tableau, int ns
         s.c_out = dt * 2. / 3.;
         s.out = L->buf[SH_NEW];
         launch_stage(ctx, L, s, ko_order);
-        fill_patch(ctx, L, L->buf[SH_NEW], t0 + dt);
+        after_stage(ctx, L, a, L->buf[SH_NEW], t0 + dt);
     } else if (type == SH_INTEGRATOR_LEAPFROG) {
         ensure_kbuf(ctx, L, (size_t)L->total_gvol * L->npairs, 1);
         StageArgs s = a;
@@ -1592,7 +1607,7 @@ void integrate(sh_ctx *ctx, sh_level *L, int type, const double *tableau, int ns
         s.kout = L->kbuf;
         s.out = L->buf[SH_NEW];
         launch_stage(ctx, L, s, ko_order);
-        fill_patch(ctx, L, L->buf[SH_NEW], t0 + dt);
+        after_stage(ctx, L, a, L->buf[SH_NEW], t0 + dt);
         s.state = L->buf[SH_NEW];
         s.time = t0 + dt;
         s.epi = kEpiLf1;
@@ -1601,7 +1616,7 @@ void integrate(sh_ctx *ctx, sh_level *L, int type, const double *tableau, int ns
         s.kout = nullptr;
         s.out = L->buf[2];
         launch_stage(ctx, L, s, ko_order);
-        fill_patch(ctx, L, L->buf[2], t0 + dt);
+        after_stage(ctx, L, a, L->buf[2], t0 + dt);
         std::swap(L->buf[SH_NEW], L->buf[2]);
     } else if (type >= 0 && type <= 4) {
         throw ShError(SH_ERR_UNSUPPORTED, "AMReX integrators (types 0-4) are not supported");
@@ -2119,6 +2134,13 @@ int sh_level_create_prec(sh_ctx *ctx, int project, int with_gw, const int domain
         }
         L->total_gvol = base;
         L->nvalid = vb;
+        if (L->esize == 8 && nbox == 1) {
+            bool whole = true;
+            for (int d = 0; d < 3; ++d)
+                whole = whole && boxes[0].lo[d] == domain_lo[d] && boxes[0].hi[d] == domain_hi[d] &&
+                        2 * nghost <= domain_hi[d] - domain_lo[d] + 1;
+            L->self_periodic = whole;
+        }
         L->ntiles = (int)tiles.size();
         L->d_boxes = upload_async(ctx, L->hboxes.data(), L->hboxes.size(), "box table");
         L->d_tiles = upload_async(ctx, tiles.data(), tiles.size(), "tile table");

@@ -90,6 +90,14 @@ struct StageArgs {
     int pos[kMaxComp / 2];
     int mom[kMaxComp / 2];
     double time, dt, dx;
+    /* a level of one box covering its periodic domain (extent per[d], ng
+     * ghost cells): the stage kernel also writes every output value into
+     * the ghost cells that are periodic images of its cell, so that no
+     * separate ghost fill is needed (0: ghost cells left to the fill; set
+     * only without Kreiss-Oliger dissipation) */
+    int self_periodic;
+    int ng;
+    int per[3];
     double c_mom;                /* coefficient of y0' in the stage positions */
     double c_k[kMaxStages];      /* coefficients of K_j in the stage positions */
     double c_k2[kMaxStages];     /* coefficients of K_j in the momenta (final) */

@@ -63,7 +63,7 @@ constexpr int stage_min_blocks() {
     return (GW || KO != 0) ? 1 : 7;
 }
 
-template <class H, bool GW, int KO>
+template <class H, bool GW, int KO, bool SP = false>
 __global__ void __launch_bounds__(kTileX *kTileY, (stage_min_blocks<GW, KO>()))
     stage_kernel(const __grid_constant__ StageArgs a) {
     using PR = Pairs<H::kNScalars, GW>;
@@ -85,6 +85,18 @@ __global__ void __launch_bounds__(kTileX *kTileY, (stage_min_blocks<GW, KO>()))
     const amrex::Dim3 glo{b.glo[0], b.glo[1], b.glo[2]};
     const amrex::Dim3 ghi{b.glo[0] + b.gdim[0], b.glo[1] + b.gdim[1], b.glo[2] + b.gdim[2]};
     const amrex::Array4<const double> st(a.state + b.off * NC, gx, gxy, gvol, glo, ghi, NC);
+    /* periodic images of a cell in the ghost cells of a self-periodic box:
+     * along each axis within ng of a face, the element offset of its image
+     * across the domain (0 elsewhere); the cell's images are the non-empty
+     * combinations of the non-zero offsets (x and y fixed per thread, z per
+     * cell).  SP: the instantiation for such boxes (a.self_periodic set). */
+    long long ox = 0, oy = 0;
+    if constexpr (SP) {
+        if (i < b.lo[0] + a.ng) ox = a.per[0];
+        else if (i > b.hi[0] - a.ng) ox = -a.per[0];
+        if (j < b.lo[1] + a.ng) oy = a.per[1] * gx;
+        else if (j > b.hi[1] - a.ng) oy = -a.per[1] * gx;
+    }
 
     for (int k = t.z0; k <= kend; ++k) {
         double r[NC];
@@ -107,6 +119,12 @@ __global__ void __launch_bounds__(kTileX *kTileY, (stage_min_blocks<GW, KO>()))
 
         const long long lc = (i - glo.x) + (j - glo.y) * gx + (k - glo.z) * gxy;
         const long long sbase = b.off * NC + lc; /* state-layout element of comp 0 */
+        long long oz = 0;
+        if constexpr (SP) {
+            if (k < b.lo[2] + a.ng) oz = a.per[2] * gxy;
+            else if (k > b.hi[2] - a.ng) oz = -a.per[2] * gxy;
+        }
+        auto put = [&](long long e, double v) { a.out[e] = v; };
         switch (a.epi) {
         case kEpiPlainRhs: {
 #pragma unroll
@@ -124,8 +142,8 @@ __global__ void __launch_bounds__(kTileX *kTileY, (stage_min_blocks<GW, KO>()))
                 y += a.c_mom * m;
                 for (int s = 0; s < a.nkin; ++s) y += a.c_k[s] * a.kin[s][kb + q * gvol];
                 y += a.c_k[a.nkin] * kq;
-                a.out[sbase + PR::pos(q) * gvol] = y;
-                a.out[sbase + PR::mom(q) * gvol] = m;
+                put(sbase + PR::pos(q) * gvol, y);
+                put(sbase + PR::mom(q) * gvol, m);
             }
             break;
         }
@@ -148,8 +166,8 @@ __global__ void __launch_bounds__(kTileX *kTileY, (stage_min_blocks<GW, KO>()))
                     const double kq = r[PR::mom(q)];
                     if constexpr (decltype(kq_pos)::value) y += a.c_k[a.nkin] * kq;
                     m += a.c_k2[a.nkin] * kq;
-                    a.out[sbase + PR::pos(q) * gvol] = y;
-                    a.out[sbase + PR::mom(q) * gvol] = m;
+                    put(sbase + PR::pos(q) * gvol, y);
+                    put(sbase + PR::mom(q) * gvol, m);
                 }
             };
             if (a.epi == kEpiRknFinal)
@@ -166,7 +184,7 @@ __global__ void __launch_bounds__(kTileX *kTileY, (stage_min_blocks<GW, KO>()))
                 double kn = r[n];
                 if (a.epi == kEpiSspAdd) kn += a.weight * a.kin[0][kb + n * gvol];
                 if (a.kout) a.kout[kb + n * gvol] = kn;
-                a.out[sbase + n * gvol] = 1. * a.y0[sbase + n * gvol] + a.c_out * kn;
+                put(sbase + n * gvol, 1. * a.y0[sbase + n * gvol] + a.c_out * kn);
             }
             break;
         }
@@ -177,7 +195,7 @@ __global__ void __launch_bounds__(kTileX *kTileY, (stage_min_blocks<GW, KO>()))
                 const double vh =
                     1. * a.y0[sbase + PR::mom(q) * gvol] + (a.dt / 2.) * r[PR::mom(q)];
                 a.kout[kb + q * gvol] = vh;
-                a.out[sbase + PR::pos(q) * gvol] = 1. * a.y0[sbase + PR::pos(q) * gvol] + a.dt * vh;
+                put(sbase + PR::pos(q) * gvol, 1. * a.y0[sbase + PR::pos(q) * gvol] + a.dt * vh);
             }
             break;
         }
@@ -185,14 +203,40 @@ __global__ void __launch_bounds__(kTileX *kTileY, (stage_min_blocks<GW, KO>()))
             const long long kb = b.off * NP + lc;
 #pragma unroll
             for (int q = 0; q < NP; ++q) {
-                a.out[sbase + PR::mom(q) * gvol] =
-                    1. * a.kin[0][kb + q * gvol] + (a.dt / 2.) * r[PR::mom(q)];
-                a.out[sbase + PR::pos(q) * gvol] = a.state[sbase + PR::pos(q) * gvol];
+                put(sbase + PR::mom(q) * gvol,
+                    1. * a.kin[0][kb + q * gvol] + (a.dt / 2.) * r[PR::mom(q)]);
+                put(sbase + PR::pos(q) * gvol, a.state[sbase + PR::pos(q) * gvol]);
             }
             break;
         }
         default:
             break;
+        }
+        /* a cell within ng of a face of a self-periodic box: its stored
+         * values (every component, as a fill copies them) read back and
+         * written to its periodic images, out of the epilogue so that no
+         * value stays live across the image stores */
+        if constexpr (SP) {
+            if (((ox | oy | oz) != 0) && a.epi != kEpiPlainRhs) {
+#pragma unroll
+                for (int n = 0; n < NC; ++n) {
+                    const long long e = sbase + n * gvol;
+                    const double v = a.out[e];
+                    if (ox != 0) a.out[e + ox] = v;
+                    if (oy != 0) {
+                        a.out[e + oy] = v;
+                        if (ox != 0) a.out[e + ox + oy] = v;
+                    }
+                    if (oz != 0) {
+                        a.out[e + oz] = v;
+                        if (ox != 0) a.out[e + ox + oz] = v;
+                        if (oy != 0) {
+                            a.out[e + oy + oz] = v;
+                            if (ox != 0) a.out[e + ox + oy + oz] = v;
+                        }
+                    }
+                }
+            }
         }
     }
 }
@@ -277,7 +321,12 @@ cudaError_t launch_stage_impl(const StageLaunch &L, cudaStream_t s) {
             switch (L.ko_order) {
             case 2: stage_kernel<H, true, 2><<<grid, block, 0, s>>>(L.args); break;
             case 3: stage_kernel<H, true, 3><<<grid, block, 0, s>>>(L.args); break;
-            default: stage_kernel<H, true, 0><<<grid, block, 0, s>>>(L.args); break;
+            default:
+                if (L.args.self_periodic)
+                    stage_kernel<H, true, 0, true><<<grid, block, 0, s>>>(L.args);
+                else
+                    stage_kernel<H, true, 0><<<grid, block, 0, s>>>(L.args);
+                break;
             }
         } else {
             return cudaErrorNotSupported;
@@ -286,7 +335,12 @@ cudaError_t launch_stage_impl(const StageLaunch &L, cudaStream_t s) {
         switch (L.ko_order) {
         case 2: stage_kernel<H, false, 2><<<grid, block, 0, s>>>(L.args); break;
         case 3: stage_kernel<H, false, 3><<<grid, block, 0, s>>>(L.args); break;
-        default: stage_kernel<H, false, 0><<<grid, block, 0, s>>>(L.args); break;
+        default:
+            if (L.args.self_periodic)
+                stage_kernel<H, false, 0, true><<<grid, block, 0, s>>>(L.args);
+            else
+                stage_kernel<H, false, 0><<<grid, block, 0, s>>>(L.args);
+            break;
         }
     }
     return cudaGetLastError();
