@@ -28,7 +28,8 @@ value   : device-resident state; each timed step bracketed by CUDA events on
 e2e     : the whole job through the public C ABI with host buffers: the
           level created and the initial state uploaded from pinned host
           memory, every step, the final state read back to pinned host
-          memory (per-step bytes = totals / steps of the job).
+          memory (per-step bytes = totals / steps of the job); the median
+          of three such jobs.
 roofline: the fused stage kernels (Rhs + RKN4 stage update): algorithmic bytes
           of all their launches over their summed duration (CUDA events the
           library records around each launch on its stream), against the
@@ -73,6 +74,8 @@ WORDS_PER_CELL_UPDATE = 40
 # launches of one step of `--case single`, ghost images written by the stage
 # kernel (599.7 MB for 2,097,152 cells).
 TRAFFIC_B_PER_CELL_UPDATE = {"amr": 436.0, "single": 286.0}
+# whole-job end-to-end runs of the 128^3 level (the median is reported)
+E2E_JOBS = 3
 
 SINGLE = dict(N=128, L=32.0, project="AxionStringsLap1", params=[1.0, 0.0], nghost=1,
               eta0=0.1, total_steps=200, seed=0)
@@ -1130,26 +1133,34 @@ def main():
     roof["fp64_roofline"] = fp64_roofline(roof, "single", local)
     roof.pop("_cell_updates", None)
 
-    # e2e: the whole 200-step job through the C ABI with pinned host buffers
+    # e2e: the whole 200-step job through the C ABI with pinned host buffers,
+    # the median of three jobs (a job is about 60 ms, so one job's figure
+    # moves by a few percent with the host's scheduling)
     host_in = torch.from_numpy(np.ascontiguousarray(state)).pin_memory()
     host_out = torch.empty_like(host_in).pin_memory()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    lv2 = sh.Level.periodic(ctx, s["project"], N, s["nghost"])
-    ctx.check(ctx.lib.sh_level_write(ctx.h, lv2.h, sh.SH_NEW, 0, host_in.data_ptr()), "write")
-    lv2.set_time(s["eta0"])
-    for _ in range(s["total_steps"]):
-        lv2.advance(sh.RKN4, dt, dx, params=s["params"])
-    ctx.check(ctx.lib.sh_level_read(ctx.h, lv2.h, sh.SH_NEW, 0, host_out.data_ptr()), "read")
-    torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    lv2.close()
+    e2e_runs = []
+    for _ in range(E2E_JOBS):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        lv2 = sh.Level.periodic(ctx, s["project"], N, s["nghost"])
+        ctx.check(ctx.lib.sh_level_write(ctx.h, lv2.h, sh.SH_NEW, 0, host_in.data_ptr()),
+                  "write")
+        lv2.set_time(s["eta0"])
+        for _ in range(s["total_steps"]):
+            lv2.advance(sh.RKN4, dt, dx, params=s["params"])
+        ctx.check(ctx.lib.sh_level_read(ctx.h, lv2.h, sh.SH_NEW, 0, host_out.data_ptr()),
+                  "read")
+        torch.cuda.synchronize()
+        e2e_runs.append(time.perf_counter() - t0)
+        lv2.close()
+    e2e_s = float(np.median(e2e_runs))
     e2e = {"value": world * N ** 3 * s["total_steps"] / e2e_s, "unit": METRIC,
+           "jobs": E2E_JOBS, "job_s": [round(x, 5) for x in e2e_runs],
            "h2d_bytes_per_step": state.size * 8 / s["total_steps"],
            "d2h_bytes_per_step": state.size * 8 / s["total_steps"],
            "job_steps": s["total_steps"],
            "note": "level created, initial state uploaded from pinned host memory, 200 RKN4 "
-                   "steps, final state read back to pinned host memory"}
+                   "steps, final state read back to pinned host memory; median of the jobs"}
 
     legs = {}
     want = [f for f in args.legs.split(",") if f]
