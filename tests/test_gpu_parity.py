@@ -210,26 +210,30 @@ def test_runs_are_bitwise_deterministic(ctx):
     assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("project,integ,nghost", [
-    ("AxionStringsLap1", sh.RKN4, 1),
-    ("AxionStringsLap2", sh.RKN5, 2),
-    ("AxionStringsLap3", sh.LSSSPRK3, 3),
-    ("AxionStrings", sh.LEAPFROG, 2),
+@pytest.mark.parametrize("project,integ,nghost,N", [
+    ("AxionStringsLap1", sh.RKN4, 1, 16),
+    ("AxionStringsLap2", sh.RKN5, 2, 16),
+    ("AxionStringsLap3", sh.LSSSPRK3, 3, 16),
+    ("AxionStrings", sh.LEAPFROG, 2, 16),
+    ("AxionStringsLap2", sh.RKN4, 2, 20),  # tiles of 20 cells in x, 6 rows
+    ("AxionStringsLap1", sh.RKN4, 1, 40),  # a ragged second tile in x
+    ("AxionStringsLap3", sh.RKN4, 3, 6),   # ghost depth half the extent
 ])
-def test_one_box_ghost_images_equal_the_fill(ctx, project, integ, nghost):
+def test_one_box_ghost_images_equal_the_fill(ctx, project, integ, nghost, N):
     """A level of one box covering the periodic domain has the stage kernels
     write the periodic images of their outputs into its ghost cells instead
     of a separate fill: the result equals the same level chopped into boxes
     (ghosts filled by copies) bit for bit, and the ghost cells after a step
     equal a fresh fill (the Rhs, which reads them as they are, is unchanged
     by an explicit FillPatch)."""
-    st = axion_state()
+    L = N / 4.0
+    st = axion_state(N, L)
     params = [0.8, 0.3] if project.startswith("AxionStringsLap") else [0.8]
     kw = dict(t0=1.0, dt=0.0625, dx=0.25, nsteps=3, params=params, nghost=nghost)
     one = ctx.evolve_periodic(project, integ, st, max_grid=0, **kw)
-    chopped = ctx.evolve_periodic(project, integ, st, max_grid=8, **kw)
+    chopped = ctx.evolve_periodic(project, integ, st, max_grid=N // 2, **kw)
     assert np.array_equal(one, chopped)
-    lv = sh.Level.periodic(ctx, project, 16, nghost)
+    lv = sh.Level.periodic(ctx, project, N, nghost)
     assert lv.nbox == 1
     lv.write(st)
     lv.set_time(1.0)
