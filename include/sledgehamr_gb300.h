@@ -226,7 +226,11 @@ SH_API int sh_level_fill_from(sh_ctx *ctx, sh_level *dst, int which_dst, const s
  * tableau (type 20 only): nodes[s], bbar[s], b[s], then the lower triangle
  * of a including the diagonal, row by row.  params/gw_params: the vectors
  * that SetParamsRhs / SetParamsGravitationalWaveRhs produce (at most 32 and
- * 16 doubles).  ko_order 0 (off), 2 or 3 with ko_strength[ncomp]. */
+ * 16 doubles).  ko_order 0 (off), 2 or 3 with ko_strength[ncomp].
+ * Every stage's output, new included, leaves with its ghost cells filled
+ * (FillIntermediatePatch); on an FP64 level of one box covering its periodic
+ * domain without dissipation the stage kernels write those periodic images
+ * themselves, with the same values. */
 SH_API int sh_level_advance(sh_ctx *ctx, sh_level *level, int integrator, const double *tableau,
                      int nstages, double dt, double dx, const double *params, int nparams,
                      const double *gw_params, int ngw, int ko_order, const double *ko_strength,
