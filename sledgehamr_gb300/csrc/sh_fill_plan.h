@@ -15,11 +15,16 @@
 #define SH_FILL_PLAN_H_
 
 #include <algorithm>
+#include <climits>
 #include <stdexcept>
 #include <string>
 #include <vector>
 
 #include "sledgehamr_gb300.h"
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 namespace sh {
 
@@ -159,22 +164,44 @@ inline FillPlan build_fill_plan(const PlanLevel &D, const PlanLevel *S, const Pl
     struct Blk {
         int kind; /* 0 skip, 1 copy, 2 interpolate */
         int own;
-        int sh[3];
-        int lo[3], hi[3];
     };
     struct Run {
         int kind, own, sh[3], lo[3], hi[3];
     };
     const long long nbox = (long long)D.nbox;
-    std::vector<std::vector<GhostCopyDev>> box_rects(nbox);
-    std::vector<std::vector<CfRect>> box_cf(nbox);
+    /* boxes are independent: host threads share them and append their
+     * rectangles to buffers of their own; where each box's rectangles went
+     * (thread, first, count) puts them back in box order afterwards, so the
+     * plan is deterministic */
+    struct Where {
+        int thread;
+        int nrect, ncf;
+        size_t rect0, cf0;
+    };
+    std::vector<Where> where((size_t)nbox);
+    std::vector<std::vector<GhostCopyDev>> thr_rects;
+    std::vector<std::vector<CfRect>> thr_cf;
     bool uncovered = false;
-    /* boxes are independent: host threads share them, results are
-     * concatenated in box order afterwards (the plan is deterministic) */
 #pragma omp parallel
     {
+#ifdef _OPENMP
+    const int tid = omp_get_thread_num();
+#pragma omp single
+    {
+        thr_rects.resize(omp_get_num_threads());
+        thr_cf.resize(omp_get_num_threads());
+    }
+#else
+    const int tid = 0;
+    thr_rects.resize(1);
+    thr_cf.resize(1);
+#endif
+    std::vector<GhostCopyDev> &my_rects = thr_rects[tid];
+    std::vector<CfRect> &my_cf = thr_cf[tid];
     std::vector<Blk> blk;
     std::vector<Run> runs, merged;
+    std::vector<int> open_prev, open_cur; /* merged rectangle ending at the
+                                             previous row / plane, by start */
     struct Axis {
         int lo, hi, wb, sh;
         bool inside;
@@ -206,31 +233,26 @@ inline FillPlan build_fill_plan(const PlanLevel &D, const PlanLevel *S, const Pl
                 a.inside = a.lo >= D.boxes[b].lo[d] && a.hi <= D.boxes[b].hi[d];
             }
         }
+        /* the blocks, row by row: kind and source box (the periodic shift
+         * of a block is that of its axis columns) */
         for (int z = 0; z < nbk[2]; ++z)
-            for (int y = 0; y < nbk[1]; ++y)
+            for (int y = 0; y < nbk[1]; ++y) {
+                const Axis &ay = ax[1][y], &az = ax[2][z];
+                const bool inside_yz = ay.inside && az.inside;
+                const bool unshifted_yz = ay.sh == 0 && az.sh == 0;
+                const int *own_row =
+                    S ? S->owner + ((size_t)az.wb * G.owner_nb[1] + ay.wb) * G.owner_nb[0]
+                      : nullptr;
+                Blk *row = blk.data() + ((size_t)z * nbk[1] + y) * nbk[0];
                 for (int x = 0; x < nbk[0]; ++x) {
-                    Blk &k = blk[((size_t)z * nbk[1] + y) * nbk[0] + x];
-                    const Axis *axk[3] = {&ax[0][x], &ax[1][y], &ax[2][z]};
-                    int wb[3];
-                    bool inside_valid = true;
-                    for (int d = 0; d < 3; ++d) {
-                        k.lo[d] = axk[d]->lo;
-                        k.hi[d] = axk[d]->hi;
-                        wb[d] = axk[d]->wb;
-                        k.sh[d] = axk[d]->sh;
-                        inside_valid = inside_valid && axk[d]->inside;
-                    }
+                    const Axis &axx = ax[0][x];
+                    Blk &k = row[x];
                     k.kind = 0;
                     k.own = -1;
-                    if (ghosts_only && inside_valid) continue;
-                    const int own = S ? S->owner[((size_t)wb[2] * G.owner_nb[1] + wb[1]) *
-                                                     G.owner_nb[0] +
-                                                 wb[0]]
-                                      : -1;
+                    if (ghosts_only && inside_yz && axx.inside) continue;
+                    const int own = own_row ? own_row[axx.wb] : -1;
                     if (own >= 0) {
-                        if (S == &D && own == (int)b && k.sh[0] == 0 && k.sh[1] == 0 &&
-                            k.sh[2] == 0)
-                            continue;
+                        if (S == &D && own == (int)b && unshifted_yz && axx.sh == 0) continue;
                         k.kind = 1;
                         k.own = own;
                         continue;
@@ -238,56 +260,117 @@ inline FillPlan build_fill_plan(const PlanLevel &D, const PlanLevel *S, const Pl
                     if (!C) continue; /* nothing to fill from: left as is */
                     k.kind = 2; /* parents checked per merged rectangle below */
                 }
+            }
         /* x-runs of equal kind / source */
         runs.clear();
         for (int z = 0; z < nbk[2]; ++z)
             for (int y = 0; y < nbk[1]; ++y) {
+                const Axis &ay = ax[1][y], &az = ax[2][z];
+                const Blk *row = blk.data() + ((size_t)z * nbk[1] + y) * nbk[0];
                 int x = 0;
                 while (x < nbk[0]) {
-                    const Blk &k = blk[((size_t)z * nbk[1] + y) * nbk[0] + x];
+                    const Blk &k = row[x];
                     if (k.kind == 0) {
                         ++x;
                         continue;
                     }
                     int x1 = x;
-                    while (x1 + 1 < nbk[0]) {
-                        const Blk &n = blk[((size_t)z * nbk[1] + y) * nbk[0] + x1 + 1];
-                        if (n.kind != k.kind || n.own != k.own || n.sh[0] != k.sh[0] ||
-                            n.sh[1] != k.sh[1] || n.sh[2] != k.sh[2])
-                            break;
+                    while (x1 + 1 < nbk[0] && row[x1 + 1].kind == k.kind &&
+                           row[x1 + 1].own == k.own && ax[0][x1 + 1].sh == ax[0][x].sh)
                         ++x1;
-                    }
-                    const Blk &e = blk[((size_t)z * nbk[1] + y) * nbk[0] + x1];
-                    Run r{k.kind, k.own, {k.sh[0], k.sh[1], k.sh[2]},
-                          {k.lo[0], k.lo[1], k.lo[2]}, {e.hi[0], k.hi[1], k.hi[2]}};
+                    Run r{k.kind, k.own, {ax[0][x].sh, ay.sh, az.sh},
+                          {ax[0][x].lo, ay.lo, az.lo}, {ax[0][x1].hi, ay.hi, az.hi}};
                     runs.push_back(r);
                     x = x1 + 1;
                 }
             }
-        /* merge along y, then along z (same kind, source and x extent) */
-        for (int d = 1; d <= 2; ++d) {
-            merged.clear();
+        /* merge along y, then along z (same kind and source, the same
+         * extent along the other axes, adjacent along the merged one).  Runs
+         * come in (z, y, x) order; a run can only join the rectangle that
+         * starts at its first block and ends on the row (plane) before it -
+         * two such rectangles would overlap - which open_prev holds by
+         * start block; rectangles keep the order of their first run. */
+        auto same_source = [](const Run &m, const Run &r) {
+            return m.kind == r.kind && m.own == r.own && m.sh[0] == r.sh[0] &&
+                   m.sh[1] == r.sh[1] && m.sh[2] == r.sh[2];
+        };
+        const int nx = nbk[0], nxy = nbk[0] * nbk[1];
+        auto start_x = [&](const Run &r) { return (int)(std::lower_bound(
+                                                            ax[0].begin(), ax[0].end(), r.lo[0],
+                                                            [](const Axis &a, int v) {
+                                                                return a.lo < v;
+                                                            }) -
+                                                        ax[0].begin()); };
+        auto start_y = [&](const Run &r) { return (int)(std::lower_bound(
+                                                            ax[1].begin(), ax[1].end(), r.lo[1],
+                                                            [](const Axis &a, int v) {
+                                                                return a.lo < v;
+                                                            }) -
+                                                        ax[1].begin()); };
+        /* along y: rows of one plane */
+        merged.clear();
+        open_prev.assign(nx, -1);
+        open_cur.assign(nx, -1);
+        {
+            int row_y = INT_MIN, row_z = INT_MIN;
             for (const Run &r : runs) {
-                bool done = false;
-                for (size_t q = merged.size(); q-- > 0;) {
-                    Run &m = merged[q];
-                    /* runs are ordered by z: along y only the same plane */
-                    if (d == 1 && m.lo[2] != r.lo[2]) break;
-                    bool same = m.kind == r.kind && m.own == r.own && m.sh[0] == r.sh[0] &&
-                                m.sh[1] == r.sh[1] && m.sh[2] == r.sh[2] &&
-                                m.hi[d] + 1 == r.lo[d];
-                    for (int e = 0; e < 3 && same; ++e)
-                        if (e != d) same = m.lo[e] == r.lo[e] && m.hi[e] == r.hi[e];
-                    if (same) {
-                        m.hi[d] = r.hi[d];
-                        done = true;
-                        break;
+                if (r.lo[2] != row_z) { /* a new plane: nothing open */
+                    std::fill(open_prev.begin(), open_prev.end(), -1);
+                    std::fill(open_cur.begin(), open_cur.end(), -1);
+                    row_z = r.lo[2];
+                    row_y = r.lo[1];
+                } else if (r.lo[1] != row_y) { /* the next row */
+                    open_prev.swap(open_cur);
+                    std::fill(open_cur.begin(), open_cur.end(), -1);
+                    row_y = r.lo[1];
+                }
+                const int x0 = start_x(r);
+                const int c = open_prev[x0];
+                if (c >= 0) {
+                    Run &m = merged[c];
+                    if (same_source(m, r) && m.hi[1] + 1 == r.lo[1] && m.hi[0] == r.hi[0]) {
+                        m.hi[1] = r.hi[1];
+                        open_cur[x0] = c;
+                        continue;
                     }
                 }
-                if (!done) merged.push_back(r);
+                open_cur[x0] = (int)merged.size();
+                merged.push_back(r);
             }
-            runs.swap(merged);
         }
+        runs.swap(merged);
+        /* along z: rectangles in the order of their first plane */
+        merged.clear();
+        open_prev.assign(nxy, -1);
+        open_cur.assign(nxy, -1);
+        {
+            int plane = INT_MIN;
+            for (const Run &r : runs) {
+                if (r.lo[2] != plane) {
+                    open_prev.swap(open_cur);
+                    std::fill(open_cur.begin(), open_cur.end(), -1);
+                    plane = r.lo[2];
+                }
+                const int key = start_x(r) + nx * start_y(r);
+                const int c = open_prev[key];
+                if (c >= 0) {
+                    Run &m = merged[c];
+                    if (same_source(m, r) && m.hi[2] + 1 == r.lo[2] && m.hi[0] == r.hi[0] &&
+                        m.lo[1] == r.lo[1] && m.hi[1] == r.hi[1]) {
+                        m.hi[2] = r.hi[2];
+                        open_cur[key] = c;
+                        continue;
+                    }
+                }
+                open_cur[key] = (int)merged.size();
+                merged.push_back(r);
+            }
+        }
+        runs.swap(merged);
+        Where &w = where[(size_t)b];
+        w.thread = tid;
+        w.rect0 = my_rects.size();
+        w.cf0 = my_cf.size();
         for (const Run &r : runs) {
             if (r.kind == 1) {
                 if (!want_copies) continue;
@@ -299,7 +382,7 @@ inline FillPlan build_fill_plan(const PlanLevel &D, const PlanLevel *S, const Pl
                     c.hi[d] = r.hi[d];
                     c.shift[d] = r.sh[d];
                 }
-                box_rects[b].push_back(c);
+                my_rects.push_back(c);
             } else {
                 /* the parents of the region must lie on the coarse level
                  * (checked per coarse block) */
@@ -331,9 +414,11 @@ inline FillPlan build_fill_plan(const PlanLevel &D, const PlanLevel *S, const Pl
                     c.lo[d] = r.lo[d];
                     c.hi[d] = r.hi[d];
                 }
-                box_cf[b].push_back(c);
+                my_cf.push_back(c);
             }
         }
+        w.nrect = (int)(my_rects.size() - w.rect0);
+        w.ncf = (int)(my_cf.size() - w.cf0);
     }
     } /* omp parallel */
     if (uncovered)
@@ -342,17 +427,27 @@ inline FillPlan build_fill_plan(const PlanLevel &D, const PlanLevel *S, const Pl
     auto cells = [](const int lo[3], const int hi[3]) {
         return (long long)(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
     };
-    for (long long b = 0; b < nbox; ++b) {
-        for (GhostCopyDev &c : box_rects[b]) {
-            c.first = P.rect_cells;
-            P.rect_cells += cells(c.lo, c.hi);
-            P.rects.push_back(c);
-        }
-        for (CfRect &c : box_cf[b]) {
-            c.first = P.cf_cells;
-            P.cf_cells += cells(c.lo, c.hi);
-            P.cf.push_back(c);
-        }
+    size_t nr = 0, nc = 0;
+    for (const Where &w : where) {
+        nr += w.nrect;
+        nc += w.ncf;
+    }
+    P.rects.resize(nr);
+    P.cf.resize(nc);
+    nr = nc = 0;
+    for (const Where &w : where) {
+        std::copy_n(thr_rects[w.thread].begin() + w.rect0, w.nrect, P.rects.begin() + nr);
+        std::copy_n(thr_cf[w.thread].begin() + w.cf0, w.ncf, P.cf.begin() + nc);
+        nr += w.nrect;
+        nc += w.ncf;
+    }
+    for (GhostCopyDev &c : P.rects) {
+        c.first = P.rect_cells;
+        P.rect_cells += cells(c.lo, c.hi);
+    }
+    for (CfRect &c : P.cf) {
+        c.first = P.cf_cells;
+        P.cf_cells += cells(c.lo, c.hi);
     }
     return P;
 }
