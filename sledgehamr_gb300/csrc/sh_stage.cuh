@@ -124,7 +124,6 @@ __global__ void __launch_bounds__(kTileX *kTileY, (stage_min_blocks<GW, KO>()))
             if (k < b.lo[2] + a.ng) oz = a.per[2] * gxy;
             else if (k > b.hi[2] - a.ng) oz = -a.per[2] * gxy;
         }
-        auto put = [&](long long e, double v) { a.out[e] = v; };
         switch (a.epi) {
         case kEpiPlainRhs: {
 #pragma unroll
@@ -142,8 +141,8 @@ __global__ void __launch_bounds__(kTileX *kTileY, (stage_min_blocks<GW, KO>()))
                 y += a.c_mom * m;
                 for (int s = 0; s < a.nkin; ++s) y += a.c_k[s] * a.kin[s][kb + q * gvol];
                 y += a.c_k[a.nkin] * kq;
-                put(sbase + PR::pos(q) * gvol, y);
-                put(sbase + PR::mom(q) * gvol, m);
+                a.out[sbase + PR::pos(q) * gvol] = y;
+                a.out[sbase + PR::mom(q) * gvol] = m;
             }
             break;
         }
@@ -166,8 +165,8 @@ __global__ void __launch_bounds__(kTileX *kTileY, (stage_min_blocks<GW, KO>()))
                     const double kq = r[PR::mom(q)];
                     if constexpr (decltype(kq_pos)::value) y += a.c_k[a.nkin] * kq;
                     m += a.c_k2[a.nkin] * kq;
-                    put(sbase + PR::pos(q) * gvol, y);
-                    put(sbase + PR::mom(q) * gvol, m);
+                    a.out[sbase + PR::pos(q) * gvol] = y;
+                    a.out[sbase + PR::mom(q) * gvol] = m;
                 }
             };
             if (a.epi == kEpiRknFinal)
@@ -184,7 +183,7 @@ __global__ void __launch_bounds__(kTileX *kTileY, (stage_min_blocks<GW, KO>()))
                 double kn = r[n];
                 if (a.epi == kEpiSspAdd) kn += a.weight * a.kin[0][kb + n * gvol];
                 if (a.kout) a.kout[kb + n * gvol] = kn;
-                put(sbase + n * gvol, 1. * a.y0[sbase + n * gvol] + a.c_out * kn);
+                a.out[sbase + n * gvol] = 1. * a.y0[sbase + n * gvol] + a.c_out * kn;
             }
             break;
         }
@@ -195,7 +194,7 @@ __global__ void __launch_bounds__(kTileX *kTileY, (stage_min_blocks<GW, KO>()))
                 const double vh =
                     1. * a.y0[sbase + PR::mom(q) * gvol] + (a.dt / 2.) * r[PR::mom(q)];
                 a.kout[kb + q * gvol] = vh;
-                put(sbase + PR::pos(q) * gvol, 1. * a.y0[sbase + PR::pos(q) * gvol] + a.dt * vh);
+                a.out[sbase + PR::pos(q) * gvol] = 1. * a.y0[sbase + PR::pos(q) * gvol] + a.dt * vh;
             }
             break;
         }
@@ -203,9 +202,9 @@ __global__ void __launch_bounds__(kTileX *kTileY, (stage_min_blocks<GW, KO>()))
             const long long kb = b.off * NP + lc;
 #pragma unroll
             for (int q = 0; q < NP; ++q) {
-                put(sbase + PR::mom(q) * gvol,
-                    1. * a.kin[0][kb + q * gvol] + (a.dt / 2.) * r[PR::mom(q)]);
-                put(sbase + PR::pos(q) * gvol, a.state[sbase + PR::pos(q) * gvol]);
+                a.out[sbase + PR::mom(q) * gvol] =
+                    1. * a.kin[0][kb + q * gvol] + (a.dt / 2.) * r[PR::mom(q)];
+                a.out[sbase + PR::pos(q) * gvol] = a.state[sbase + PR::pos(q) * gvol];
             }
             break;
         }
