@@ -261,29 +261,39 @@ def test_full_size_translation_invariance(ctx):
     assert np.array_equal(np.roll(a, sh_, axis=(1, 2, 3)), b)
 
 
-def test_beyond_2_31_elements_translation_invariance(ctx):
+@pytest.mark.parametrize("precision,integ", [(sh.PREC_FP64, sh.LEAPFROG),
+                                             (sh.PREC_FP32_KAHAN, sh.RKN4)])
+def test_beyond_2_31_elements_translation_invariance(precision, integ):
     """A level whose buffers hold more than 2^31 elements (832^3 cells, four
     components, 64 boxes of 208^3: the element offsets of the later boxes,
     of their ghost copies and of the canonical-layout moves need 64 bits):
-    a periodic shift of the initial state shifts the result of two
-    leapfrog steps exactly.  The data are made and compared on the device
-    (about 125 GB at the peak), so that no host array of that size exists."""
+    a periodic shift of the initial state shifts the result of two steps
+    exactly, on FP64 and on FP32 + Kahan storage.  The data are made and
+    compared on the device (about 125 GB at the peak), so that no host
+    array of that size exists; a context of its own returns the level
+    memory when the test ends."""
     torch = pytest.importorskip("torch")
     N, mg = 832, 208
+    # the device's memory pool keeps what earlier tests freed until a
+    # context is destroyed: destroying a fresh one returns it
+    sh.Context(0).close()
+    torch.cuda.empty_cache()
     free, _ = torch.cuda.mem_get_info()
     if free < 160e9:
         pytest.skip("needs about 160 GB of free device memory")
+    ctx = sh.Context(0)
     dx, dt = 0.25, 0.0625
     shift = (3, 5, 7)
 
     def run(state):
-        lv = sh.Level.periodic(ctx, "AxionStringsLap1", N, 1, max_grid=mg)
+        lv = sh.Level.periodic(ctx, "AxionStringsLap1", N, 1, max_grid=mg,
+                               precision=precision)
         assert lv.nbox == 64
         torch.cuda.synchronize()
         lv.write_device(state.data_ptr())
         lv.set_time(1.0)
         for _ in range(2):
-            lv.advance(sh.LEAPFROG, dt, dx, [1.0, 0.0])
+            lv.advance(integ, dt, dx, [1.0, 0.0])
         out = torch.empty_like(state)
         lv.read_device(out.data_ptr())
         ctx.synchronize()
@@ -296,8 +306,12 @@ def test_beyond_2_31_elements_translation_invariance(ctx):
     st = torch.roll(st, shift, dims=(1, 2, 3))
     b = run(st)
     del st
-    assert torch.isfinite(a).all()
-    assert torch.equal(torch.roll(a, shift, dims=(1, 2, 3)), b)
+    ctx.close()
+    finite = bool(torch.isfinite(a).all())
+    shifted = bool(torch.equal(torch.roll(a, shift, dims=(1, 2, 3)), b))
+    del a, b
+    torch.cuda.empty_cache()
+    assert finite and shifted
 
 
 def test_full_size_linearity(ctx):
