@@ -295,18 +295,12 @@ inline FillPlan build_fill_plan(const PlanLevel &D, const PlanLevel *S, const Pl
                    m.sh[1] == r.sh[1] && m.sh[2] == r.sh[2];
         };
         const int nx = nbk[0], nxy = nbk[0] * nbk[1];
-        auto start_x = [&](const Run &r) { return (int)(std::lower_bound(
-                                                            ax[0].begin(), ax[0].end(), r.lo[0],
-                                                            [](const Axis &a, int v) {
-                                                                return a.lo < v;
-                                                            }) -
-                                                        ax[0].begin()); };
-        auto start_y = [&](const Run &r) { return (int)(std::lower_bound(
-                                                            ax[1].begin(), ax[1].end(), r.lo[1],
-                                                            [](const Axis &a, int v) {
-                                                                return a.lo < v;
-                                                            }) -
-                                                        ax[1].begin()); };
+        /* the block column of axis d that starts at cell lo */
+        auto start_block = [&](int d, int lo) {
+            return (int)(std::lower_bound(ax[d].begin(), ax[d].end(), lo,
+                                          [](const Axis &a, int v) { return a.lo < v; }) -
+                         ax[d].begin());
+        };
         /* along y: rows of one plane */
         merged.clear();
         open_prev.assign(nx, -1);
@@ -324,7 +318,7 @@ inline FillPlan build_fill_plan(const PlanLevel &D, const PlanLevel *S, const Pl
                     std::fill(open_cur.begin(), open_cur.end(), -1);
                     row_y = r.lo[1];
                 }
-                const int x0 = start_x(r);
+                const int x0 = start_block(0, r.lo[0]);
                 const int c = open_prev[x0];
                 if (c >= 0) {
                     Run &m = merged[c];
@@ -351,7 +345,7 @@ inline FillPlan build_fill_plan(const PlanLevel &D, const PlanLevel *S, const Pl
                     std::fill(open_cur.begin(), open_cur.end(), -1);
                     plane = r.lo[2];
                 }
-                const int key = start_x(r) + nx * start_y(r);
+                const int key = start_block(0, r.lo[0]) + nx * start_block(1, r.lo[1]);
                 const int c = open_prev[key];
                 if (c >= 0) {
                     Run &m = merged[c];
