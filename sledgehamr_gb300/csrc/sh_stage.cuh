@@ -99,6 +99,23 @@ __global__ void __launch_bounds__(kTileX *kTileY, (stage_min_blocks<GW, KO>()))
     }
 
     for (int k = t.z0; k <= kend; ++k) {
+        /* the epilogue's inputs of the next cell (y0 and the earlier K) asked
+         * into L1 while this cell's stencil runs; the stencil's own loads
+         * are left to the cache (prefetching them too measured no better) */
+        if (k < kend) {
+            const long long next = (i - glo.x) + (j - glo.y) * gx + (k + 1 - glo.z) * gxy;
+            if (a.y0) {
+#pragma unroll
+                for (int n = 0; n < NC; ++n)
+                    asm volatile("prefetch.global.L1 [%0];" ::"l"(a.y0 + b.off * NC + next +
+                                                                 n * gvol));
+            }
+            for (int s = 0; s < a.nkin; ++s)
+#pragma unroll
+                for (int q = 0; q < NP; ++q)
+                    asm volatile("prefetch.global.L1 [%0];" ::"l"(a.kin[s] + b.off * NP + next +
+                                                                 q * gvol));
+        }
         double r[NC];
 #pragma unroll
         for (int n = 0; n < NC; ++n) r[n] = 0.;
