@@ -72,8 +72,8 @@ WORDS_PER_CELL_UPDATE = 40
 # launch of the benchmark by the cells it updates.  AMR: level 1 of the AMR
 # run at N0 = 128 (5.55 GB for 12,729,344 cells); 128^3 level: the three
 # launches of one step of `--case single`, ghost images written by the stage
-# kernel (599.7 MB for 2,097,152 cells).
-TRAFFIC_B_PER_CELL_UPDATE = {"amr": 436.0, "single": 286.0}
+# kernel (603.1 MB for 2,097,152 cells).
+TRAFFIC_B_PER_CELL_UPDATE = {"amr": 436.0, "single": 287.6}
 # whole-job end-to-end runs of the 128^3 level (the median is reported)
 E2E_JOBS = 3
 
