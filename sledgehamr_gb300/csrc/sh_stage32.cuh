@@ -92,6 +92,23 @@ __global__ void __launch_bounds__(kThreads) stage32_axion_kernel(const __grid_co
         const long long lz = (long long)(k - b.glo[2]) * gxy;
         const long long sb = col + lz;  /* component 0 of the cell */
         const long long kb = kcol + lz; /* K component 0 of the cell */
+        /* the next cell's y0 (and, in the last stage, K and compensations)
+         * asked into L1 while this cell is computed */
+        if (k < kend) {
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                asm volatile("prefetch.global.L1 [%0];" ::"l"(y0 + sb + gxy + c * gvol));
+            if constexpr (STAGE == 2) {
+#pragma unroll
+                for (int c = 0; c < 2; ++c) {
+                    asm volatile("prefetch.global.L1 [%0];" ::"l"(k0 + kb + gxy + c * gvol));
+                    asm volatile("prefetch.global.L1 [%0];" ::"l"(k1 + kb + gxy + c * gvol));
+                }
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                    asm volatile("prefetch.global.L1 [%0];" ::"l"(c_old + sb + gxy + c * gvol));
+            }
+        }
         float lap[2];
 #pragma unroll
         for (int c = 0; c < 2; ++c) {
