@@ -110,11 +110,21 @@ __global__ void __launch_bounds__(kTileX *kTileY, (stage_min_blocks<GW, KO>()))
                     asm volatile("prefetch.global.L1 [%0];" ::"l"(a.y0 + b.off * NC + next +
                                                                  n * gvol));
             }
-            for (int s = 0; s < a.nkin; ++s)
+            /* the K buffers hold every component in the SSPRK3 stages and
+             * the momenta of the pairs otherwise */
+            if (a.epi == kEpiSsp0 || a.epi == kEpiSspAdd) {
+                for (int s = 0; s < a.nkin; ++s)
 #pragma unroll
-                for (int q = 0; q < NP; ++q)
-                    asm volatile("prefetch.global.L1 [%0];" ::"l"(a.kin[s] + b.off * NP + next +
-                                                                 q * gvol));
+                    for (int n = 0; n < NC; ++n)
+                        asm volatile("prefetch.global.L1 [%0];" ::"l"(
+                            a.kin[s] + b.off * NC + next + n * gvol));
+            } else {
+                for (int s = 0; s < a.nkin; ++s)
+#pragma unroll
+                    for (int q = 0; q < NP; ++q)
+                        asm volatile("prefetch.global.L1 [%0];" ::"l"(
+                            a.kin[s] + b.off * NP + next + q * gvol));
+            }
         }
         double r[NC];
 #pragma unroll
